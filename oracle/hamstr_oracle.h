@@ -1,0 +1,65 @@
+/*
+ * hamstr_oracle.h -- CPU restatement of HAMSTR's steady ADI iteration.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * the smoke check and the CPU-baseline leg of bench.py call it, the product
+ * never does.  It restates, in plain C with the reference's operation order,
+ * the reference's case reader (io.cpp:58-372), preprocessing
+ * (preprocess.cpp:15-241), flow initialisation (initFlow.cpp:12-93),
+ * computeRHS (computeRHS.cpp:17-427), fluxRoe2D (interfaceFlux.cpp:24-169),
+ * jacobianRoe2D/3D in the frozen-eigenvalue mode (jacobianRoe.cpp:9-70,
+ * 92-620), the reconstructions (reconstruction.cpp), ADI with the 4x4 block
+ * tridiagonal solvers (ADI.cpp:15-266, triSolvers.cpp:769-1046) and
+ * computeLinearRHS (computeLinearRHS.cpp:13-371).
+ *
+ * Its results are pinned bit for bit against the reference compiled from its
+ * own sources (oracle/Makefile `ref`) and against the committed golden
+ * fixtures in tests/golden/.
+ *
+ * The handle API mirrors oracle/ref_harness.cpp so one Python wrapper drives
+ * either implementation.
+ */
+#ifndef HAMSTR_ORACLE_H
+#define HAMSTR_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ho_case ho_case;
+
+/* Reads <case_dir>/input.hamstr and <case_dir>/input/domain000/*.dat,
+ * preprocesses and initialises to freestream.  NULL on failure, with a
+ * message in err. */
+ho_case* ho_open(const char* case_dir, char* err, int errlen);
+ho_case* ho_clone(const ho_case* c);
+void     ho_close(ho_case* c);
+
+/* nCell nFace nChain nChainFace nMaxChain order msweep nGhost nNode nColor */
+void ho_sizes(const ho_case* c, int* out);
+/* Mach alpha CFL gamma rinf uinf vinf einf pinf */
+void ho_params(const ho_case* c, double* out);
+void ho_set_freestream(ho_case* c, double uinf, double vinf, double einf);
+void ho_set_run(ho_case* c, int order, int msweep, double cfl);
+
+/* Each returns 0, or -1 when a spectral radius is NaN (the reference exits
+ * the process there, interfaceFlux.cpp:117-124). */
+int  ho_compute_rhs(ho_case* c, int implicit, double* l2, double* linf);
+int  ho_adi(ho_case* c, double* l2, double* linf);
+int  ho_linear_rhs(ho_case* c, double* l2, double* linf);
+int  ho_step(ho_case* c, double* out4);
+int  ho_march(ho_case* c, int n, double* hist);
+/* Runs `iters` steps on each of n independent cases, one host thread per
+ * case (OpenMP); the CPU-baseline throughput leg. */
+int  ho_march_replicas(ho_case** cases, int n, int iters);
+
+/* Named arrays: q r r0 dq sigma ff x vol normVec refMtx (doubles) and
+ * faces chainConn faceStartPerChain c2chain bFaces chainsPerColor (ints). */
+int ho_get(const ho_case* c, const char* name, double* out);
+int ho_set(ho_case* c, const char* name, const double* in);
+int ho_get_int(const ho_case* c, const char* name, int* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

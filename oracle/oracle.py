@@ -1,0 +1,206 @@
+"""ctypes driver for the two CPU oracles (TEST INFRASTRUCTURE ONLY).
+
+* ``kind="port"``      -- oracle/_ref/libhamstr_oracle.so, the C restatement
+  (hamstr_oracle.c); builds everywhere, including the GPU host.
+* ``kind="reference"`` -- oracle/_ref/libhamstr_ref.so, the reference's own
+  sources compiled with ref_harness.cpp; only where the reference sources
+  are present.
+
+Both expose the same handle API, so tests compare them array by array.  Only
+tests/, the smoke check and the CPU-baseline leg of bench.py import this.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+PORT_LIB = os.path.join(REF_DIR, "libhamstr_oracle.so")
+REF_LIB = os.path.join(REF_DIR, "libhamstr_ref.so")
+REFERENCE_SOURCES = os.environ.get("HAMSTR_REFERENCE_DIR", "/root/reference")
+
+SIZE_NAMES = ("nCell", "nFace", "nChain", "nChainFace", "nMaxChain", "order",
+              "msweep", "nGhost", "nNode", "nColor")
+PARAM_NAMES = ("Mach", "alpha", "CFL", "gamma", "rinf", "uinf", "vinf", "einf", "pinf")
+
+
+def build(reference: bool | None = None) -> None:
+    """Compile the port (always) and the reference library (when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if reference is None:
+        reference = os.path.isdir(REFERENCE_SOURCES)
+    if reference:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFDIR=" + REFERENCE_SOURCES], check=True)
+
+
+_LIBS: dict = {}
+
+
+def _lib(kind: str):
+    if kind in _LIBS:
+        return _LIBS[kind]
+    path = PORT_LIB if kind == "port" else REF_LIB
+    if not os.path.exists(path):
+        build(reference=(kind == "reference"))
+    lib = ctypes.CDLL(path)
+    p = "ho_" if kind == "port" else "ref_"
+    vp, dp, ip, i, d = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    fns = {
+        "open": (vp, [ctypes.c_char_p] + ([ctypes.c_char_p, i] if kind == "port" else [])),
+        "close": (None, [vp]),
+        "sizes": (None, [vp, ip]),
+        "params": (None, [vp, dp]),
+        "set_freestream": (None, [vp, d, d, d]),
+        "set_run": (None, [vp, i, i, d]),
+        "compute_rhs": (i if kind == "port" else None, [vp, i, dp, dp]),
+        "adi": (i if kind == "port" else None, [vp, dp, dp]),
+        "linear_rhs": (i if kind == "port" else None, [vp, dp, dp]),
+        "step": (i if kind == "port" else None, [vp, dp]),
+        "march": (i if kind == "port" else None, [vp, i, dp]),
+        "get": (i, [vp, ctypes.c_char_p, dp]),
+        "set": (i, [vp, ctypes.c_char_p, dp]),
+        "get_int": (i, [vp, ctypes.c_char_p, ip]),
+    }
+    for name, (res, args) in fns.items():
+        fn = getattr(lib, p + name)
+        fn.restype, fn.argtypes = res, args
+    if kind == "port":
+        lib.ho_clone.restype, lib.ho_clone.argtypes = vp, [vp]
+        lib.ho_march_replicas.restype = i
+        lib.ho_march_replicas.argtypes = [ctypes.POINTER(vp), i, i]
+    _LIBS[kind] = (lib, p)
+    return _LIBS[kind]
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleCase:
+    """One case directory driven through either CPU oracle."""
+
+    def __init__(self, case_dir: str, kind: str = "port", _handle=None):
+        self.kind = kind
+        self.lib, self.p = _lib(kind)
+        self.case_dir = case_dir
+        if _handle is not None:
+            self.h = _handle
+        elif kind == "port":
+            err = ctypes.create_string_buffer(512)
+            self.h = self._fn("open")(case_dir.encode(), err, 512)
+            if not self.h:
+                raise RuntimeError("oracle open failed: " + err.value.decode())
+        else:
+            self.h = self._fn("open")(os.path.abspath(case_dir).encode())
+            if not self.h:
+                raise RuntimeError("reference open failed for " + case_dir)
+        s = np.zeros(10, dtype=np.int32)
+        self._fn("sizes")(self.h, _ptr(s))
+        self.sizes = dict(zip(SIZE_NAMES, (int(v) for v in s)))
+
+    def _fn(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def close(self):
+        if self.h:
+            self._fn("close")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clone(self) -> "OracleCase":
+        assert self.kind == "port"
+        return OracleCase(self.case_dir, "port", _handle=self.lib.ho_clone(self.h))
+
+    @property
+    def params(self) -> dict:
+        v = np.zeros(9)
+        self._fn("params")(self.h, _ptr(v))
+        return dict(zip(PARAM_NAMES, (float(x) for x in v)))
+
+    def set_freestream(self, uinf, vinf, einf):
+        self._fn("set_freestream")(self.h, uinf, vinf, einf)
+
+    def set_run(self, order, msweep, cfl):
+        self._fn("set_run")(self.h, order, msweep, cfl)
+
+    def _check(self, rc):
+        if rc is not None and rc != 0:
+            raise RuntimeError("oracle returned status %d" % rc)
+
+    def compute_rhs(self, implicit=True):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self._fn("compute_rhs")(self.h, int(implicit), ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def adi(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self._fn("adi")(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def linear_rhs(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self._fn("linear_rhs")(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def step(self):
+        out = np.zeros(4)
+        self._check(self._fn("step")(self.h, _ptr(out)))
+        return out
+
+    def march(self, n):
+        hist = np.zeros((n, 4))
+        self._check(self._fn("march")(self.h, n, _ptr(hist)))
+        return hist
+
+    _DSIZE = {"q": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
+              "sigma": ("nCell", 1), "ff": ("nFace", 32), "x": ("nNode", 2), "vol": ("nCell", 1),
+              "normVec": ("nFace", 2), "refMtx": ("nFace", 4)}
+
+    def get(self, name) -> np.ndarray:
+        key, w = self._DSIZE[name]
+        out = np.zeros(self.sizes[key] * w)
+        rc = self._fn("get")(self.h, name.encode(), _ptr(out))
+        if rc != 0:
+            raise KeyError(name)
+        return out
+
+    def set(self, name, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        key, w = self._DSIZE[name]
+        assert arr.size == self.sizes[key] * w
+        rc = self._fn("set")(self.h, name.encode(), _ptr(arr))
+        if rc != 0:
+            raise KeyError(name)
+
+    _ISIZE = {"faces": ("nFace", 6), "chainConn": ("nChainFace", 1),
+              "faceStartPerChain": ("nChain", 1), "c2chain": ("nCell", 2),
+              "bFaces": ("nFace", 1), "chainsPerColor": ("nColor", 1)}
+
+    def get_int(self, name) -> np.ndarray:
+        key, w = self._ISIZE[name]
+        n = self.sizes[key] * w + (1 if name == "faceStartPerChain" else 0)
+        out = np.zeros(n, dtype=np.int32)
+        rc = self._fn("get_int")(self.h, name.encode(), _ptr(out))
+        if rc < 0:
+            raise KeyError(name)
+        if name == "bFaces":
+            out = out[:rc]
+        return out
+
+
+def march_replicas(cases, iters: int) -> None:
+    """Run ``iters`` steps on each port case, one OpenMP thread per case."""
+    lib, _ = _lib("port")
+    arr = (ctypes.c_void_p * len(cases))(*[c.h for c in cases])
+    rc = lib.ho_march_replicas(arr, len(cases), iters)
+    if rc != 0:
+        raise RuntimeError("oracle replica march failed")
