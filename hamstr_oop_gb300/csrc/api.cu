@@ -1,0 +1,570 @@
+// ##################################################################
+//
+// api.cu -- the device solver handle and its C ABI (include/hamstr_gpu.h)
+//
+// A pseudo-time step (march.cpp:381-386) is the launch sequence
+//   rhs_face(J) rhs_cell(+ADI init) norm  adi_factor
+//   msweep x { adi_solve per wave, dq += r, lin_face, lin_cell, [norm] }
+//   step_end
+// captured once into a CUDA graph and replayed; the last lin_cell also
+// applies q += dq.  Every kernel returns at once when a march's stop flag
+// is up, so a run of captured steps ends exactly at the converged step.
+// ##################################################################
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hamstr_gpu.h"
+#include "device_state.h"
+#include "plan.h"
+
+using namespace hamstr;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& m) { g_last_error = m; }
+
+#define CK(call)                                                                        \
+   do {                                                                                 \
+      cudaError_t e_ = (call);                                                          \
+      if (e_ != cudaSuccess) {                                                          \
+         set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+         return HAMSTR_GPU_ERR_CUDA;                                                    \
+      }                                                                                 \
+   } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t n, std::vector<void*>& owned)
+{
+   *p = nullptr;
+   if (n == 0) n = 1;
+   cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+   if (e != cudaSuccess) {
+      set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      return e == cudaErrorMemoryAllocation ? HAMSTR_GPU_ERR_NOMEM : HAMSTR_GPU_ERR_CUDA;
+   }
+   owned.push_back((void*)*p);
+   return HAMSTR_GPU_OK;
+}
+
+template <typename T>
+int upload(T** p, const std::vector<T>& v, std::vector<void*>& owned)
+{
+   int st = dalloc(p, v.size(), owned);
+   if (st) return st;
+   if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+   return HAMSTR_GPU_OK;
+}
+
+}  // namespace
+
+struct hamstr_gpu {
+   DeviceState d{};
+   Plan plan;
+   int msweep = 1;
+   cudaStream_t stream = nullptr;
+   std::vector<void*> owned;
+   cudaGraphExec_t step_exec = nullptr;
+   cudaGraph_t step_graph = nullptr;
+   int launches_per_step = 0;
+   double tol_host = 0.0;   // staging for the async copy into d.tol
+
+   // one pseudo-time step on `stream` (graph body)
+   int enqueue_step(bool check_tol)
+   {
+      int n = 0;
+      launch_rhs_face(d, true, stream); n++;
+      launch_rhs_cell(d, true, stream); n++;
+      launch_norm_final(d, 0, check_tol, stream); n++;
+      launch_adi_factor(d, stream); n++;
+      for (int s = 0; s < msweep; s++) {
+         for (int w = 0; w < plan.nWave; w++) {
+            launch_adi_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
+            n++;
+         }
+         launch_dq_update(d, stream); n++;
+         launch_lin_face(d, stream); n++;
+         launch_lin_cell(d, s == msweep - 1, stream); n++;
+         if (s == msweep - 1) { launch_norm_final(d, 2, false, stream); n++; }
+      }
+      launch_step_end(d, stream); n++;
+      launches_per_step = n;
+      CK(cudaGetLastError());
+      return HAMSTR_GPU_OK;
+   }
+
+   int capture()
+   {
+      if (step_exec) return HAMSTR_GPU_OK;
+      CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      int st = enqueue_step(true);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (st) return st;
+      if (e != cudaSuccess) {
+         set_error(std::string("graph capture: ") + cudaGetErrorString(e));
+         return HAMSTR_GPU_ERR_CUDA;
+      }
+      step_graph = g;
+      CK(cudaGraphInstantiate(&step_exec, step_graph, 0));
+      return HAMSTR_GPU_OK;
+   }
+
+   int reset_ctl(double tol)
+   {
+      tol_host = tol;
+      CK(cudaMemsetAsync(d.ctl, 0, 2 * sizeof(int), stream));
+      CK(cudaMemcpyAsync(d.tol, &tol_host, sizeof(double), cudaMemcpyHostToDevice, stream));
+      return HAMSTR_GPU_OK;
+   }
+
+   int status_check()
+   {
+      int s = 0;
+      CK(cudaMemcpyAsync(&s, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      if (s & DEV_ERR_NAN_SPEC) {
+         set_error("NaN spectral radius (non-physical state)");
+         CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+         return HAMSTR_GPU_ERR_NAN;
+      }
+      return HAMSTR_GPU_OK;
+   }
+
+   int read_norms(double* out, int n)
+   {
+      CK(cudaMemcpyAsync(out, d.norms, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+      return status_check();
+   }
+};
+
+extern "C" {
+
+const char* hamstr_gpu_strerror(int st)
+{
+   switch (st) {
+      case HAMSTR_GPU_OK: return "ok";
+      case HAMSTR_GPU_ERR_ARG: return "invalid argument";
+      case HAMSTR_GPU_ERR_TOPOLOGY: return "mesh/chain topology not supported";
+      case HAMSTR_GPU_ERR_CUDA: return "CUDA error";
+      case HAMSTR_GPU_ERR_NAN: return "NaN spectral radius";
+      case HAMSTR_GPU_ERR_IO: return "missing or malformed input file";
+      case HAMSTR_GPU_ERR_NOMEM: return "out of memory";
+      default: return "unknown status";
+   }
+}
+
+const char* hamstr_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const int* faces, const double* normVec,
+                      const double* refMtx, int nChain, const int* faceStartPerChain, const int* chainConn,
+                      hamstr_gpu** out)
+{
+   if (!p || !faces || !normVec || !refMtx || !faceStartPerChain || !chainConn || !out) return HAMSTR_GPU_ERR_ARG;
+   *out = nullptr;
+   if (p->msweep < 1 || !(p->CFL > 0.0)) {
+      set_error("msweep must be >= 1 and CFL > 0");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   MeshInput in;
+   in.nCell = nCell;
+   in.nFace = nFace;
+   in.nChain = nChain;
+   in.nChainFace = faceStartPerChain[nChain];
+   in.order = p->order;
+   in.faces = faces;
+   in.faceStartPerChain = faceStartPerChain;
+   in.chainConn = chainConn;
+   hamstr_gpu* g = new hamstr_gpu;
+   std::string msg;
+   try {
+      msg = build_plan(in, g->plan);
+   } catch (const std::bad_alloc&) {
+      delete g;
+      return HAMSTR_GPU_ERR_NOMEM;
+   }
+   if (!msg.empty()) {
+      set_error(msg);
+      delete g;
+      return HAMSTR_GPU_ERR_TOPOLOGY;
+   }
+   const Plan& P = g->plan;
+   DeviceState& d = g->d;
+   d.nCell = nCell;
+   d.nFace = nFace;
+   d.nSlot = P.nSlot;
+   d.nSten = P.nSten;
+   d.nRow = P.nRow;
+   d.nChain = P.nChain;
+   d.order = P.order;
+   d.nGhost = P.nGhost;
+   d.fc.gamma = p->gamma;
+   d.fc.rinf = p->rinf;
+   d.fc.uinf = p->uinf;
+   d.fc.vinf = p->vinf;
+   d.fc.einf = p->einf;
+   d.fc.cfl = p->CFL;
+   d.fs1 = p->rinf * p->uinf;
+   d.fs2 = p->rinf * p->vinf;
+   g->msweep = p->msweep;
+
+   // host-side packing
+   std::vector<int4> sten(P.nSten);
+   for (int i = 0; i < P.nSten; i++) sten[i] = make_int4(P.sten_cell[i], P.sten_kind[i], P.sten_face[i], 0);
+   std::vector<int4> slot(P.nSlot);
+   std::vector<double2> normal(P.nSlot);
+   for (int s = 0; s < P.nSlot; s++) {
+      slot[s] = make_int4(P.slot_n[s], P.slot_left[s], P.slot_right[s], P.slot_swap[s] | (P.slot_owner[s] << 1));
+      normal[s] = make_double2(normVec[2 * (size_t)P.slot_face[s]], normVec[2 * (size_t)P.slot_face[s] + 1]);
+   }
+   std::vector<double4> refl(nFace);
+   for (int f = 0; f < nFace; f++)
+      refl[f] = make_double4(refMtx[4 * (size_t)f], refMtx[4 * (size_t)f + 1], refMtx[4 * (size_t)f + 2],
+                             refMtx[4 * (size_t)f + 3]);
+   std::vector<int> chain_facN(P.nChain, -1);
+   int nper = 0;
+   for (int c = 0; c < P.nChain; c++)
+      if (P.chain_periodic[c]) chain_facN[c] = nper++;
+   std::vector<int> cell_written(P.cell_last_wave_writer);
+
+   int st = HAMSTR_GPU_OK;
+   auto& o = g->owned;
+   const size_t nc = (size_t)nCell;
+#define TRY(x)                          \
+   do {                                 \
+      st = (x);                         \
+      if (st) {                         \
+         hamstr_gpu_destroy(g);         \
+         return st;                     \
+      }                                 \
+   } while (0)
+   TRY(dalloc(&d.q, 4 * nc, o));
+   TRY(dalloc(&d.r, 4 * nc, o));
+   TRY(dalloc(&d.r0, 4 * nc, o));
+   TRY(dalloc(&d.dq, 4 * nc, o));
+   TRY(dalloc(&d.sigma, nc, o));
+   TRY(dalloc(&d.dtfac, nc, o));
+   TRY(dalloc(&d.flux, 4 * (size_t)P.nSlot, o));
+   TRY(dalloc(&d.spec, (size_t)P.nSlot, o));
+   TRY(dalloc(&d.ff, 32 * (size_t)P.nSlot, o));
+   TRY(upload(&d.sten, sten, o));
+   TRY(upload(&d.slot, slot, o));
+   TRY(upload(&d.slot_face, P.slot_face, o));
+   TRY(upload(&d.normal, normal, o));
+   TRY(upload(&d.refl, refl, o));
+   TRY(upload(&d.cell_ptr, P.cell_ptr, o));
+   TRY(upload(&d.cell_ent, P.cell_ent, o));
+   TRY(upload(&d.chain_periodic, P.chain_periodic, o));
+   TRY(upload(&d.chain_nrows, P.chain_nrows, o));
+   TRY(upload(&d.chain_row0, P.chain_row0, o));
+   TRY(upload(&d.wave_chains, P.wave_chains, o));
+   TRY(upload(&d.row_scell, P.row_scell, o));
+   TRY(upload(&d.row_fcell, P.row_fcell, o));
+   TRY(upload(&d.row_ops, P.row_ops, o));
+   TRY(upload(&d.cell_written, cell_written, o));
+   TRY(upload(&d.chain_facN, chain_facN, o));
+   TRY(dalloc(&d.fac, 80 * (size_t)std::max(P.nRow, 1), o));
+   TRY(dalloc(&d.fsc, 4 * (size_t)std::max(P.nRow, 1), o));
+   TRY(dalloc(&d.facN, 16 * (size_t)std::max(nper, 1), o));
+   d.norm_blocks = (nCell + 255) / 256;
+   TRY(dalloc(&d.norm_part, (size_t)d.norm_blocks, o));
+   TRY(dalloc(&d.norms, 4, o));
+   TRY(dalloc(&d.status, 1, o));
+   TRY(dalloc(&d.ctl, 2, o));
+   TRY(dalloc(&d.tol, 1, o));
+   d.hist_cap = 1 << 16;
+   TRY(dalloc(&d.hist, 4 * (size_t)d.hist_cap, o));
+#undef TRY
+   cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+   if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      hamstr_gpu_destroy(g);
+      return HAMSTR_GPU_ERR_CUDA;
+   }
+   e = cudaMemsetAsync(d.status, 0, sizeof(int), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.ctl, 0, 2 * sizeof(int), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.tol, 0, sizeof(double), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.ff, 0, 32 * (size_t)P.nSlot * sizeof(double), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.dq, 0, 4 * nc * sizeof(double), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.r, 0, 4 * nc * sizeof(double), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.r0, 0, 4 * nc * sizeof(double), g->stream);
+   if (e == cudaSuccess) e = cudaMemsetAsync(d.sigma, 0, nc * sizeof(double), g->stream);
+   if (e == cudaSuccess) {
+      // freestream initial state (initFlow.cpp:67-91)
+      std::vector<double> q(4 * nc);
+      for (size_t i = 0; i < nc; i++) {
+         q[4 * i] = p->rinf;
+         q[4 * i + 1] = p->rinf * p->uinf;
+         q[4 * i + 2] = p->rinf * p->vinf;
+         q[4 * i + 3] = p->einf;
+      }
+      e = cudaMemcpy(d.q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
+   }
+   if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+   if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      hamstr_gpu_destroy(g);
+      return HAMSTR_GPU_ERR_CUDA;
+   }
+   *out = g;
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_destroy(hamstr_gpu* g)
+{
+   if (!g) return HAMSTR_GPU_OK;
+   if (g->stream) cudaStreamSynchronize(g->stream);
+   if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
+   if (g->step_graph) cudaGraphDestroy(g->step_graph);
+   for (void* p : g->owned) cudaFree(p);
+   if (g->stream) cudaStreamDestroy(g->stream);
+   delete g;
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_get(hamstr_gpu* g, const char* name, double* out)
+{
+   if (!g || !name || !out) return HAMSTR_GPU_ERR_ARG;
+   const DeviceState& d = g->d;
+   const size_t nc = (size_t)d.nCell;
+   const double* src = nullptr;
+   size_t n = 0;
+   if (!std::strcmp(name, "q")) { src = d.q; n = 4 * nc; }
+   else if (!std::strcmp(name, "r")) { src = d.r; n = 4 * nc; }
+   else if (!std::strcmp(name, "r0")) { src = d.r0; n = 4 * nc; }
+   else if (!std::strcmp(name, "dq")) { src = d.dq; n = 4 * nc; }
+   else if (!std::strcmp(name, "sigma")) { src = d.sigma; n = nc; }
+   else if (!std::strcmp(name, "ff")) {
+      // per-slot Jacobians to face order (sb->ff[iface], computeRHS.cpp:365-370)
+      std::vector<double> slots(32 * (size_t)d.nSlot);
+      CK(cudaMemcpyAsync(slots.data(), d.ff, slots.size() * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+      CK(cudaStreamSynchronize(g->stream));
+      std::memset(out, 0, 32 * (size_t)d.nFace * sizeof(double));
+      for (int s = 0; s < d.nSlot; s++)
+         if (g->plan.slot_owner[s] == s)
+            std::memcpy(out + 32 * (size_t)g->plan.slot_face[s], slots.data() + 32 * (size_t)s, 32 * sizeof(double));
+      return HAMSTR_GPU_OK;
+   } else {
+      set_error(std::string("unknown array ") + name);
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   CK(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+   CK(cudaStreamSynchronize(g->stream));
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_set(hamstr_gpu* g, const char* name, const double* in)
+{
+   if (!g || !name || !in) return HAMSTR_GPU_ERR_ARG;
+   DeviceState& d = g->d;
+   const size_t nc = (size_t)d.nCell;
+   double* dst = nullptr;
+   size_t n = 0;
+   if (!std::strcmp(name, "q")) { dst = d.q; n = 4 * nc; }
+   else if (!std::strcmp(name, "r")) { dst = d.r; n = 4 * nc; }
+   else if (!std::strcmp(name, "r0")) { dst = d.r0; n = 4 * nc; }
+   else if (!std::strcmp(name, "dq")) { dst = d.dq; n = 4 * nc; }
+   else if (!std::strcmp(name, "sigma")) { dst = d.sigma; n = nc; }
+   else if (!std::strcmp(name, "ff")) {
+      std::vector<double> slots(32 * (size_t)d.nSlot);
+      for (int s = 0; s < d.nSlot; s++)
+         std::memcpy(slots.data() + 32 * (size_t)s, in + 32 * (size_t)g->plan.slot_face[s], 32 * sizeof(double));
+      CK(cudaMemcpyAsync(d.ff, slots.data(), slots.size() * sizeof(double), cudaMemcpyHostToDevice, g->stream));
+      CK(cudaStreamSynchronize(g->stream));
+      return HAMSTR_GPU_OK;
+   } else {
+      set_error(std::string("unknown array ") + name);
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   CK(cudaMemcpyAsync(dst, in, n * sizeof(double), cudaMemcpyHostToDevice, g->stream));
+   CK(cudaStreamSynchronize(g->stream));
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_compute_rhs(hamstr_gpu* g, int implicit, double* l2, double* linf)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   launch_rhs_face(g->d, implicit != 0, g->stream);
+   launch_rhs_cell(g->d, false, g->stream);
+   launch_norm_final(g->d, 0, false, g->stream);
+   CK(cudaGetLastError());
+   double n[2];
+   st = g->read_norms(n, 2);
+   if (st) return st;
+   if (l2) *l2 = n[0];
+   if (linf) *linf = n[1];
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   launch_dtfac(g->d, g->stream);
+   launch_lin_face(g->d, g->stream);
+   launch_lin_cell(g->d, false, g->stream);
+   launch_norm_final(g->d, 2, false, g->stream);
+   CK(cudaGetLastError());
+   double n[4];
+   st = g->read_norms(n, 4);
+   if (st) return st;
+   if (l2) *l2 = n[2];
+   if (linf) *linf = n[3];
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   const DeviceState& d = g->d;
+   launch_adi_init(d, g->stream);
+   launch_adi_factor(d, g->stream);
+   for (int s = 0; s < g->msweep; s++) {
+      for (int w = 0; w < g->plan.nWave; w++)
+         launch_adi_solve(d, g->plan.wave_ptr[w], g->plan.wave_ptr[w + 1] - g->plan.wave_ptr[w], g->stream);
+      launch_dq_update(d, g->stream);
+      launch_lin_face(d, g->stream);
+      launch_lin_cell(d, s == g->msweep - 1, g->stream);
+   }
+   launch_norm_final(d, 2, false, g->stream);
+   CK(cudaGetLastError());
+   double n[4];
+   st = g->read_norms(n, 4);
+   if (st) return st;
+   if (l2) *l2 = n[2];
+   if (linf) *linf = n[3];
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_step(hamstr_gpu* g, double* norms4)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   int st = g->capture();
+   if (st) return st;
+   st = g->reset_ctl(0.0);
+   if (st) return st;
+   CK(cudaGraphLaunch(g->step_exec, g->stream));
+   double n[4];
+   st = g->read_norms(n, 4);
+   if (st) return st;
+   if (norms4) std::memcpy(norms4, n, sizeof(n));
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged)
+{
+   if (!g || nsteps < 0) return HAMSTR_GPU_ERR_ARG;
+   int st = g->capture();
+   if (st) return st;
+   DeviceState& d = g->d;
+   if (nsteps > d.hist_cap) {
+      set_error("nsteps beyond the history capacity of one march call (65536)");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   st = g->reset_ctl(tol);
+   if (st) return st;
+   if (hist) {
+      std::vector<double> nanfill(4 * (size_t)std::max(nsteps, 1), std::nan(""));
+      CK(cudaMemcpyAsync(d.hist, nanfill.data(), nanfill.size() * sizeof(double), cudaMemcpyHostToDevice, g->stream));
+      CK(cudaStreamSynchronize(g->stream));
+   }
+   for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(g->step_exec, g->stream));
+   int ctl[2] = {0, 0};
+   CK(cudaMemcpyAsync(ctl, d.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream));
+   st = g->status_check();
+   if (st) return st;
+   const int rows = ctl[0] ? ctl[1] + 1 : ctl[1];
+   if (hist && rows > 0) {
+      CK(cudaMemcpyAsync(hist, d.hist, 4 * (size_t)rows * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+      CK(cudaStreamSynchronize(g->stream));
+   }
+   if (evals) *evals = rows;
+   if (converged) *converged = ctl[0];
+   return HAMSTR_GPU_OK;
+}
+
+void* hamstr_gpu_stream(hamstr_gpu* g) { return g ? (void*)g->stream : nullptr; }
+
+int hamstr_gpu_launches_per_step(hamstr_gpu* g)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   if (!g->launches_per_step) {
+      int st = g->capture();
+      if (st) return st;
+   }
+   return g->launches_per_step;
+}
+
+int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double* ms, int* launches, int* n)
+{
+   // eager launches of one step with events around each kernel class
+   if (!g || reps < 1 || !names || !ms || !launches || !n) return HAMSTR_GPU_ERR_ARG;
+   static const char* kNames[] = {"rhs_face", "rhs_cell", "norm_final", "adi_factor", "adi_solve",
+                                  "dq_update", "lin_face", "lin_cell", "step_end"};
+   const int K = 9;
+   std::vector<double> acc(K, 0.0);
+   std::vector<int> cnt(K, 0);
+   cudaEvent_t a, b;
+   CK(cudaEventCreate(&a));
+   CK(cudaEventCreate(&b));
+   DeviceState& d = g->d;
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   auto timed = [&](int k, auto fn) -> int {
+      CK(cudaEventRecord(a, g->stream));
+      fn();
+      CK(cudaEventRecord(b, g->stream));
+      CK(cudaEventSynchronize(b));
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, a, b));
+      acc[k] += t;
+      cnt[k] += 1;
+      return HAMSTR_GPU_OK;
+   };
+   for (int r = 0; r < reps; r++) {
+      if ((st = timed(0, [&] { launch_rhs_face(d, true, g->stream); }))) return st;
+      if ((st = timed(1, [&] { launch_rhs_cell(d, true, g->stream); }))) return st;
+      if ((st = timed(2, [&] { launch_norm_final(d, 0, false, g->stream); }))) return st;
+      if ((st = timed(3, [&] { launch_adi_factor(d, g->stream); }))) return st;
+      for (int s = 0; s < g->msweep; s++) {
+         for (int w = 0; w < g->plan.nWave; w++)
+            if ((st = timed(4, [&] {
+                    launch_adi_solve(d, g->plan.wave_ptr[w], g->plan.wave_ptr[w + 1] - g->plan.wave_ptr[w], g->stream);
+                 })))
+               return st;
+         if ((st = timed(5, [&] { launch_dq_update(d, g->stream); }))) return st;
+         if ((st = timed(6, [&] { launch_lin_face(d, g->stream); }))) return st;
+         if ((st = timed(7, [&] { launch_lin_cell(d, s == g->msweep - 1, g->stream); }))) return st;
+         if (s == g->msweep - 1)
+            if ((st = timed(2, [&] { launch_norm_final(d, 2, false, g->stream); }))) return st;
+      }
+      if ((st = timed(8, [&] { launch_step_end(d, g->stream); }))) return st;
+   }
+   cudaEventDestroy(a);
+   cudaEventDestroy(b);
+   CK(cudaGetLastError());
+   st = g->status_check();
+   if (st) return st;
+   const int cap = *n;
+   *n = K;
+   for (int k = 0; k < K && k < cap; k++) {
+      names[k] = kNames[k];
+      ms[k] = acc[k] / reps;
+      launches[k] = cnt[k] / reps;
+   }
+   return HAMSTR_GPU_OK;
+}
+
+}  // extern "C"

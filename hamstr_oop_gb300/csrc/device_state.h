@@ -1,0 +1,87 @@
+// ##################################################################
+//
+// device_state.h -- device buffers of one solver handle and the kernel
+// launchers shared between the translation units
+//
+// Layout in HBM (all FP64 values are the reference's doubles):
+//   q, r, r0, dq      [nCell][4]  array-of-structs, 32 B per cell: one
+//                                  sector per cell for the stencil gathers
+//   sigma, dtfac      [nCell]
+//   flux              [nSlot][4]  face flux (computeRHS) or linear flux
+//   spec              [nSlot]     spectral radius times area
+//   ff                [nSlot][32] lmat[4][4] then rmat[4][4] per face slot
+//   stencil           [nSten]     int4 {cell, kind, face, -}
+//   slot              [nSlot]     int4 {n, left, right, swap|owner<<1}
+//   normal            [nSlot]     double2 face normal (dy, -dx)
+//   refl              [nFace]     double4 wall reflection 2x2
+//   factor storage    [nRow][80]  per ADI row: A, LU, C', fill', cN
+// ##################################################################
+#ifndef HAMSTR_GPU_DEVICE_STATE_H
+#define HAMSTR_GPU_DEVICE_STATE_H
+
+#include <cuda_runtime.h>
+
+namespace hamstr {
+
+// status bits raised by kernels into DeviceState::status
+enum {
+   DEV_ERR_NAN_SPEC = 1,     // spectral radius is NaN (interfaceFlux.cpp:117-124)
+};
+
+struct FlowConst {
+   double gamma, rinf, uinf, vinf, einf, cfl;
+};
+
+struct DeviceState {
+   int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
+   FlowConst fc;
+   double fs1, fs2;        // freestream rho*u, rho*v (computeRHS.cpp:247-248)
+
+   double *q, *r, *r0, *dq, *sigma, *dtfac;
+   double *flux, *spec, *ff;
+   int4* sten;
+   int4* slot;
+   int* slot_face;
+   double2* normal;
+   double4* refl;
+   int *cell_ptr, *cell_ent;
+   int *chain_periodic, *chain_nrows, *chain_row0;
+   int *wave_chains;
+   int *row_scell, *row_fcell, *row_ops;
+   int *cell_written;
+   double* fac;            // per-row factor storage
+   double* fsc;            // per-row right-hand side / solution scratch [nRow][4]
+   double* facN;           // per periodic chain: final LU of the last row (16)
+   int* chain_facN;        // periodic chain -> index into facN (or -1)
+   double2* norm_part;     // per-block {sum r_rho^2, max |r_rho|}
+   double* norms;          // [0]=L2 [1]=Linf of the last reduction
+   int* status;            // device error word
+   int* ctl;               // [0] stop flag (march converged), [1] step counter
+   double* hist;           // [hist_cap][4] norms per step (march)
+   int hist_cap;
+   double* tol;            // [0] march stop tolerance on the computeRHS L2 norm (<= 0: off)
+   int norm_blocks;
+};
+
+// true once a march has met its tolerance: every later kernel of the step
+// returns at once, so a captured run of steps stops exactly there
+__device__ __forceinline__ bool halted(const DeviceState& d) { return *(volatile const int*)d.ctl != 0; }
+
+// launchers (rhs.cu)
+void launch_rhs_face(const DeviceState& d, bool jacobian, cudaStream_t st);
+void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st);
+void launch_lin_face(const DeviceState& d, cudaStream_t st);
+void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
+// norms -> d.norms[off], d.norms[off+1] and hist row ctl[1] (when logging);
+// with check_tol, raises the stop flag when L2 <= tol
+void launch_norm_final(const DeviceState& d, int off, bool check_tol, cudaStream_t st);
+void launch_step_end(const DeviceState& d, cudaStream_t st);
+void launch_dtfac(const DeviceState& d, cudaStream_t st);
+void launch_adi_init(const DeviceState& d, cudaStream_t st);
+void launch_dq_update(const DeviceState& d, cudaStream_t st);
+// launchers (adi.cu)
+void launch_adi_factor(const DeviceState& d, cudaStream_t st);
+void launch_adi_solve(const DeviceState& d, int wave_begin, int wave_count, cudaStream_t st);
+
+}  // namespace hamstr
+#endif

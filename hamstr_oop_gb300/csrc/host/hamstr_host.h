@@ -1,0 +1,156 @@
+// ##################################################################
+//
+// hamstr_host.h -- drop-in C++ classes of the reference's driver layer
+//
+// Same class names, public methods and argument meaning as the reference
+// (hamstr.h:16-49, meshBlock.h:15-73, solnBlock.h:13-91, solver.h:14-55).
+// Differences a caller sees:
+//   * errors throw hamstr::Error instead of calling exit(1)
+//     (io.cpp:19-23,138-141; interfaceFlux.cpp:117-124);
+//   * the solution lives on the GPU; SOLVER::syncHost() refreshes the
+//     SOLNBLOCK host arrays (q, r, r0, dq, sigma, ff), and marchInTime()
+//     does so at its end;
+//   * readMeshData / readSolutionInputs also accept a case root directory
+//     (the reference reads ./input... from the working directory).
+// ##################################################################
+#ifndef HAMSTR_HOST_H
+#define HAMSTR_HOST_H
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../../include/hamstr_gpu.h"
+
+namespace hamstr {
+struct Error : std::runtime_error {
+   int status;
+   Error(int st, const std::string& m) : std::runtime_error(m), status(st) {}
+};
+}  // namespace hamstr
+
+struct hamstr_case;
+
+// ------------------------------------------------------------------
+class MESHBLOCK
+{
+   friend class SOLVER;
+   friend struct hamstr_case;
+
+  private:
+   int myid = 0;
+   int nNode = 0, nCell = 0, nFace = 0, nBface = 0, nColor = 0;
+   int nChain = 0, nMaxChain = 0, nChainFace = 0, nStrand = 0;
+   int sol_visc = 0;
+   std::vector<int> conn, faces, chainsPerColor, faceStartPerChain, chainConn;
+   std::vector<int> c2chain, bFaces;
+   std::vector<double> vol, x, normVec, refMtx;   // normVec [nFace][2], refMtx [nFace][2][2]
+   double volmax = 0.0, volmin = 0.0;
+
+  public:
+   MESHBLOCK() {}
+   ~MESHBLOCK() {}
+   // io.cpp:58-372; root "" means the working directory
+   void readMeshData(int myid);
+   void readMeshData(int myid, const std::string& root);
+   // preprocess.cpp:15-241
+   void preprocess(void);
+   void setViscosity(int visc) { sol_visc = visc; }
+};
+
+// ------------------------------------------------------------------
+class SOLNBLOCK
+{
+   friend class SOLVER;
+   friend struct hamstr_case;
+   friend void hamstr_init_flow(SOLNBLOCK& sb, int nCell);
+
+  private:
+   int order = 3, timeacc = 0, nsteps = 0, nwrite = 0, msweep = 1, test = 0, outform = 0;
+   double Mach = 0, alpha = 0, beta = 0, rey = 0, CFL = 0, dt = 0;
+   char timeInteg[64] = {0};
+   char scheme[64] = {0};
+   int visc = 0;
+   int nGhost = 2;
+   double uinf = 0, vinf = 0, winf = 0, einf = 0, pinf = 0, rinf = 0;
+   double gamma = 0, invGamma = 0, gm1 = 0, c2b = 0, rgas = 0, pr = 0, prtr = 0;
+   double LInfNorm = 0, L2Norm = 0;
+   // host copies of the solution (refreshed by SOLVER::syncHost)
+   std::vector<double> q, r, r0, dq, sigma, ff;
+
+  public:
+   SOLNBLOCK() {}
+   ~SOLNBLOCK() {}
+   // io.cpp:13-51
+   void readSolutionInputs(void);
+   void readSolutionInputs(const std::string& root);
+};
+
+// ------------------------------------------------------------------
+class SOLVER
+{
+  private:
+   double dt = 0;
+   const char* stepType = nullptr;
+   MESHBLOCK* mb;
+   SOLNBLOCK* sb;
+   hamstr_gpu* gpu = nullptr;
+   void ensureGpu();
+
+  public:
+   SOLVER(MESHBLOCK* mbin, SOLNBLOCK* sbin);
+   ~SOLVER();
+   void initFlow(void);                  // initFlow.cpp:12-93
+   void marchInTime(void);               // march.cpp:15-59
+   void stepSolution(void);              // march.cpp:66-134 (ADI branch)
+   void computeRHS(char* option);        // computeRHS.cpp:17-427
+   void computeLinearRHS(void);          // computeLinearRHS.cpp:13-371
+   void ADI(void);                       // ADI.cpp:15-266
+   void basicScreenOutput(void);         // io.cpp:412-446
+   void syncHost(void);
+   hamstr_gpu* device(void) { ensureGpu(); return gpu; }
+   double l2Norm() const { return sb->L2Norm; }
+   double lInfNorm() const { return sb->LInfNorm; }
+};
+
+// ------------------------------------------------------------------
+class HAMSTR
+{
+  private:
+   int nGrid, procID;
+   MESHBLOCK* mb;
+   SOLNBLOCK* sb;
+   SOLVER* solv = nullptr;
+   std::string root;
+
+  public:
+   HAMSTR(const int nprocs, const int myid, const std::string& root = "");
+   ~HAMSTR();
+   void readInputs(int myid);            // hamstr.cpp:33-48
+   void preprocessor(void);              // hamstr.cpp:54-66
+   void marchInTime(void);               // hamstr.cpp:72-77
+   void welcome(void);
+   void thanks(void);
+   SOLVER* solver() { return solv; }
+};
+
+// freestream + initial state (initFlow.cpp:12-93) on host arrays
+void hamstr_init_flow(SOLNBLOCK& sb, int nCell);
+
+// the C handle behind hamstr_case_* (api.cu)
+struct hamstr_case {
+   MESHBLOCK mb;
+   SOLNBLOCK sb;
+   // reference order of the flat accessors
+   static void sizes(const hamstr_case& c, int* out);
+   static void params(const hamstr_case& c, double* out);
+   static int get_int(const hamstr_case& c, const std::string& name, int* out, int* count);
+   static int get(const hamstr_case& c, const std::string& name, double* out);
+   static void set_run(hamstr_case& c, int order, int msweep, double cfl);
+   static void set_freestream(hamstr_case& c, double u, double v, double e);
+   static hamstr_gpu_params gpu_params(const hamstr_case& c);
+   static void load(hamstr_case& c, const std::string& dir);
+   static int create_gpu(const hamstr_case& c, hamstr_gpu** out);
+};
+
+#endif

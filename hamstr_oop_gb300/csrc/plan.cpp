@@ -1,0 +1,243 @@
+// ##################################################################
+//
+// plan.cpp -- derive the per-mesh kernel layout from the chain files
+//
+// Follows the reference's per-call logic once, up front:
+//   stencil + ghosts   computeRHS.cpp:57-149, :154-260
+//   face order         computeRHS.cpp:278-408
+//   block assembly     ADI.cpp:62-217
+//   chain order        ADI.cpp:57 (file order; realised as waves of
+//                      cell-disjoint chains that commute)
+// ##################################################################
+#include "plan.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <unordered_map>
+
+namespace hamstr {
+
+namespace {
+
+std::string fmt(const char* f, int a, int b = 0)
+{
+   char buf[256];
+   std::snprintf(buf, sizeof(buf), f, a, b);
+   return buf;
+}
+
+struct BlockOps {
+   int op[kOpsPerBlock];
+   int n = 0;
+   BlockOps() { for (int& o : op) o = -1; }
+   bool add(int v)
+   {
+      if (n >= kOpsPerBlock) return false;
+      op[n++] = v;
+      return true;
+   }
+};
+
+}  // namespace
+
+std::string build_plan(const MeshInput& in, Plan& p)
+{
+   p = Plan();
+   p.nCell = in.nCell;
+   p.nFace = in.nFace;
+   p.nChain = in.nChain;
+   p.order = in.order;
+   if (in.order != 1 && in.order != 3 && in.order != 5)
+      return fmt("unsupported reconstruction order %d", in.order);
+   p.nGhost = (in.order == 5) ? 3 : 2;
+   const int g = p.nGhost;
+   if (in.nCell <= 0 || in.nFace <= 0 || in.nChain <= 0) return "empty mesh";
+   auto left_of = [&](int face) { return in.faces[6 * face + 2]; };
+   auto right_of = [&](int face) { return in.faces[6 * face + 4]; };
+
+   // ---- validation of ids ------------------------------------------
+   for (int i = 0; i < in.nFace; i++) {
+      int l = left_of(i), r = right_of(i);
+      if (l < 0 || l >= in.nCell) return fmt("face %d has invalid left cell %d", i, l);
+      if (r >= in.nCell) return fmt("face %d has invalid right cell %d", i, r);
+      if (r == -5) return fmt("face %d is an inter-domain face (not supported)", i);
+      if (r < -2) return fmt("face %d has unknown boundary tag %d", i, r);
+   }
+   for (int c = 0; c <= in.nChain; c++) {
+      int s = in.faceStartPerChain[c];
+      if (s < 0 || s > in.nChainFace) return fmt("chain offset %d out of range (%d)", c, s);
+      if (c > 0 && s <= in.faceStartPerChain[c - 1]) return fmt("chain %d is empty or reversed", c - 1);
+   }
+   for (int f = 0; f < in.nChainFace; f++)
+      if (in.chainConn[f] < 0 || in.chainConn[f] >= in.nFace)
+         return fmt("chain face entry %d is not a face (%d)", f, in.chainConn[f]);
+
+   // ---- stencils and slots -----------------------------------------
+   std::vector<int> chain_sten0(in.nChain);
+   std::vector<int> ci;
+   std::vector<int> face_last_slot(in.nFace, -1);
+   for (int ich = 0; ich < in.nChain; ich++) {
+      const int f1 = in.faceStartPerChain[ich], f2 = in.faceStartPerChain[ich + 1];
+      const int nf = f2 - f1;
+      const bool closed = in.chainConn[f1] == in.chainConn[f2 - 1];
+      if (closed && (nf < 3 || nf < g + 1)) return fmt("closed chain %d too short (%d faces)", ich, nf);
+      if (!closed && nf < (g == 3 ? 3 : 2)) return fmt("open chain %d too short (%d faces)", ich, nf);
+      ci.assign(nf + 2 * g + 2, 0);
+      int m = g, size;
+      for (int f = f1; f < f2; f++) ci[m++] = left_of(in.chainConn[f]);
+      if (closed) {
+         ci[m++] = left_of(in.chainConn[f1 + 1]);
+         size = m;
+         m = 0;
+         for (int f = f2 - g - 1; f < f2 - 1; f++) ci[m++] = left_of(in.chainConn[f]);
+      } else if (g == 3) {
+         m--; ci[m] = -ci[m];
+         m++; ci[m] = -ci[m - 3];
+         m++; ci[m] = -ci[m - 5];
+         size = m + 1;
+         ci[0] = -ci[5];
+         ci[1] = -ci[4];
+         ci[2] = -ci[3];
+      } else {
+         m--; ci[m] = -ci[m];
+         m++; ci[m] = -ci[m - 3];
+         size = m + 1;
+         ci[0] = -ci[3];
+         ci[1] = -ci[2];
+      }
+      chain_sten0[ich] = (int)p.sten_cell.size();
+      for (int j = 0; j < size; j++) {
+         const int icell = ci[j];
+         const bool ghost = icell < 0 || (icell == 0 && (j == g - 1 || j == size - g));
+         int kind = STEN_CELL, cell = icell, face = -1;
+         if (ghost) {
+            const int iface = (j < g) ? in.chainConn[f1] : in.chainConn[f2 - 1];
+            const int right = right_of(iface);
+            if (right == -2) {
+               kind = STEN_WALL;
+               cell = -icell;
+               face = iface;
+            } else {
+               kind = STEN_FREESTREAM;
+               cell = -1;
+            }
+         }
+         if (kind != STEN_FREESTREAM && (cell < 0 || cell >= in.nCell))
+            return fmt("chain %d stencil slot %d names no cell", ich, j);
+         p.sten_cell.push_back(cell);
+         p.sten_kind.push_back(kind);
+         p.sten_face.push_back(face);
+      }
+      // processed faces (computeRHS.cpp:278-281)
+      const int per = closed ? 1 : 0;
+      for (int f = f1; f < f2 - per; f++) {
+         const int iface = in.chainConn[f];
+         const int s = (int)p.slot_face.size();
+         p.slot_face.push_back(iface);
+         p.slot_left.push_back(left_of(iface));
+         p.slot_right.push_back(right_of(iface));
+         p.slot_n.push_back(chain_sten0[ich] + (g - 1) + (f - f1));
+         p.slot_swap.push_back((f == f2 - 1 && !closed) ? 1 : 0);
+         face_last_slot[iface] = s;
+      }
+   }
+   p.nSten = (int)p.sten_cell.size();
+   p.nSlot = (int)p.slot_face.size();
+   p.slot_owner.resize(p.nSlot);
+   for (int s = 0; s < p.nSlot; s++) p.slot_owner[s] = face_last_slot[p.slot_face[s]];
+
+   // ---- per-cell ordered contributions -----------------------------
+   std::vector<int> cnt(in.nCell + 1, 0);
+   for (int s = 0; s < p.nSlot; s++) {
+      cnt[p.slot_left[s] + 1]++;
+      if (p.slot_right[s] > -1) cnt[p.slot_right[s] + 1]++;
+   }
+   p.cell_ptr.assign(in.nCell + 1, 0);
+   for (int c = 0; c < in.nCell; c++) p.cell_ptr[c + 1] = p.cell_ptr[c] + cnt[c + 1];
+   p.cell_ent.assign(p.cell_ptr[in.nCell], 0);
+   std::vector<int> fill(p.cell_ptr.begin(), p.cell_ptr.end() - 1);
+   for (int s = 0; s < p.nSlot; s++) {
+      p.cell_ent[fill[p.slot_left[s]]++] = 2 * s;
+      if (p.slot_right[s] > -1) p.cell_ent[fill[p.slot_right[s]]++] = 2 * s + 1;
+   }
+
+   // ---- ADI rows (ADI.cpp:62-217) -----------------------------------
+   int slot0 = 0;
+   std::vector<int> lastwave(in.nCell, -1);
+   p.cell_last_wave_writer.assign(in.nCell, 0);
+   for (int ich = 0; ich < in.nChain; ich++) {
+      const int f1 = in.faceStartPerChain[ich], f2 = in.faceStartPerChain[ich + 1];
+      const int per = (in.chainConn[f1] == in.chainConn[f2 - 1]) ? 1 : 0;
+      const int nproc = f2 - per - f1;
+      const int N = per ? nproc : nproc - 1;
+      std::vector<BlockOps> A(nproc + 1), B(nproc + 1), C(nproc + 1);
+      std::vector<int> fcell(nproc + 1, -1);
+      int m = 0;
+      bool ok = true;
+      for (int f = f1; f < f2 - per; f++) {
+         const int s = slot0 + (f - f1);
+         const int own = p.slot_owner[s];
+         const int iface = in.chainConn[f];
+         const int right = right_of(iface);
+         const int L = (own << 3) | (OP_SEL_L << 1), R = (own << 3) | (OP_SEL_R << 1);
+         const int Rr = (own << 3) | (OP_SEL_RREFL << 1);
+         if (per) {
+            const int mm1 = (m == 0) ? nproc - 1 : m - 1;
+            ok &= B[m].add(L);
+            ok &= B[mm1].add(R | 1);
+            ok &= A[m].add(R);
+            ok &= C[mm1].add(L | 1);
+            fcell[m] = left_of(iface);
+         } else {
+            const int mm1 = m - 1;
+            if (right < 0 && f == f2 - 1) m--;
+            ok &= B[m].add(L);
+            if (mm1 > -1 && right > -1) {
+               ok &= A[m].add(R);
+               ok &= B[mm1].add(R | 1);
+               ok &= C[mm1].add(L | 1);
+            } else if (right == -2) {
+               ok &= B[m].add(Rr);
+            }
+            fcell[m] = left_of(iface);
+         }
+         m++;
+      }
+      if (!ok) return fmt("chain %d needs more than %d terms in one block", ich, kOpsPerBlock);
+      p.chain_periodic.push_back(per);
+      p.chain_nrows.push_back(N);
+      p.chain_row0.push_back((int)p.row_scell.size());
+      p.maxRows = std::max(p.maxRows, N);
+      int wave = 0;
+      for (int r = 0; r < N; r++) {
+         const int sc = left_of(in.chainConn[f1 + r]);
+         p.row_scell.push_back(sc);
+         p.row_fcell.push_back(fcell[r]);
+         for (int o = 0; o < kOpsPerBlock; o++) p.row_ops.push_back(A[r].op[o]);
+         for (int o = 0; o < kOpsPerBlock; o++) p.row_ops.push_back(B[r].op[o]);
+         for (int o = 0; o < kOpsPerBlock; o++) p.row_ops.push_back(C[r].op[o]);
+         wave = std::max(wave, lastwave[sc] + 1);
+         if (fcell[r] >= 0) wave = std::max(wave, lastwave[fcell[r]] + 1);
+      }
+      for (int r = 0; r < N; r++) {
+         const int sc = p.row_scell[p.chain_row0.back() + r];
+         lastwave[sc] = std::max(lastwave[sc], wave);
+         p.cell_last_wave_writer[sc] = 1;
+         const int fc = p.row_fcell[p.chain_row0.back() + r];
+         if (fc >= 0) lastwave[fc] = std::max(lastwave[fc], wave);
+      }
+      p.chain_wave.push_back(wave);
+      p.nWave = std::max(p.nWave, wave + 1);
+      slot0 += nproc;
+   }
+   p.nRow = (int)p.row_scell.size();
+   p.wave_ptr.assign(p.nWave + 1, 0);
+   for (int w : p.chain_wave) p.wave_ptr[w + 1]++;
+   for (int w = 0; w < p.nWave; w++) p.wave_ptr[w + 1] += p.wave_ptr[w];
+   p.wave_chains.assign(in.nChain, 0);
+   std::vector<int> wfill(p.wave_ptr.begin(), p.wave_ptr.end() - 1);
+   for (int ich = 0; ich < in.nChain; ich++) p.wave_chains[wfill[p.chain_wave[ich]]++] = ich;
+   return "";
+}
+
+}  // namespace hamstr

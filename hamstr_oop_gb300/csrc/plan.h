@@ -1,0 +1,65 @@
+// ##################################################################
+//
+// plan.h -- host-side layout of one mesh for the GPU kernels
+//
+// The reference rebuilds each chain's stencil, ghost states, block
+// assembly pattern and accumulation order on every call
+// (computeRHS.cpp:53-149, computeLinearRHS.cpp:52-143, ADI.cpp:62-191).
+// All of that depends only on the mesh, so it is derived once here, by the
+// reference's own rules, into flat arrays the kernels index directly.
+// ##################################################################
+#ifndef HAMSTR_GPU_PLAN_H
+#define HAMSTR_GPU_PLAN_H
+
+#include <string>
+#include <vector>
+
+namespace hamstr {
+
+// stencil entry kinds (sten_kind)
+enum { STEN_CELL = 0, STEN_WALL = 1, STEN_FREESTREAM = 2 };
+
+// block assembly operation: (ffslot << 3) | (sel << 1) | neg
+enum { OP_SEL_L = 0, OP_SEL_R = 1, OP_SEL_RREFL = 2 };
+constexpr int kOpsPerBlock = 4;   // A, B and C each take up to 4 ordered terms
+
+struct MeshInput {
+   int nCell = 0, nFace = 0, nChain = 0, nChainFace = 0;
+   int order = 3;
+   const int* faces = nullptr;            // 6*nFace: n1 n2 cL eL cR eR (walls tagged -2)
+   const int* faceStartPerChain = nullptr;// nChain+1
+   const int* chainConn = nullptr;        // nChainFace
+};
+
+struct Plan {
+   int nCell = 0, nFace = 0, nChain = 0, nSlot = 0, nSten = 0, nRow = 0;
+   int order = 3, nGhost = 2, nWave = 0, maxRows = 0;
+
+   // stencil entries, chain after chain (chainSize entries each)
+   std::vector<int> sten_cell;   // cell read (mirrored cell for walls, -1 for freestream)
+   std::vector<int> sten_kind;   // STEN_*
+   std::vector<int> sten_face;   // reflection face for STEN_WALL, else -1
+
+   // processed face slots, in the reference's chain-major face order
+   std::vector<int> slot_face, slot_left, slot_right;
+   std::vector<int> slot_n;      // global stencil index of slot n (left state qr[n+1], right ql[n])
+   std::vector<int> slot_swap;   // 1 for the last face of an open chain (ql[n] | qr[n+1])
+   std::vector<int> slot_owner;  // slot whose Jacobian the reference keeps in ff[face] (last writer)
+
+   // per-cell ordered contributions: entry = slot*2 + (cell is the right cell)
+   std::vector<int> cell_ptr, cell_ent;
+
+   // chains / ADI rows
+   std::vector<int> chain_periodic, chain_nrows, chain_row0, chain_wave;
+   std::vector<int> wave_ptr, wave_chains;        // chains grouped by wave
+   std::vector<int> row_scell;   // cell scaled by CFL/sigma and written back (ADI.cpp:200-244)
+   std::vector<int> row_fcell;   // cell whose residual forms the right-hand side (-1: zero)
+   std::vector<int> row_ops;     // 3*kOpsPerBlock per row: A, B, C terms, -1 terminated
+   std::vector<int> cell_last_wave_writer;         // 1 if some chain writes this cell
+};
+
+// Builds the plan; returns "" on success or a description of the problem.
+std::string build_plan(const MeshInput& in, Plan& out);
+
+}  // namespace hamstr
+#endif

@@ -1,0 +1,227 @@
+// ##################################################################
+//
+// roe.cuh -- Roe flux and its frozen-eigenvalue Jacobian, per face
+//
+// Compiled with -fmad=false: every a*b+c below rounds the product and the
+// sum separately, the arithmetic of the reference on x86-64, and `/` and
+// sqrt are the IEEE correctly rounded operations.  Expressions keep the
+// reference's association order so the results are bit-identical.
+//
+// Flux: fluxRoe2D, interfaceFlux.cpp:24-169.
+// Jacobian: jacobianRoe2D -> jacobianRoe3D with IMODE=1
+// (jacobianRoe.cpp:9-70, 92-337, 488-620).  The reference embeds the 2D
+// state in 5 variables with w=0 and nz=0 and keeps rows/columns {0,1,2,4}.
+// Every term it forms from w, nz or a structurally zero derivative is an
+// exact zero (x*0 or 0*x with finite x) added to a non-zero partial sum,
+// which leaves the sum unchanged, so those terms are dropped here and only
+// the 32 kept entries are formed.  The flux and the Jacobian share the
+// primitive states and Roe averages, which the reference computes twice
+// with identical expressions.  The Jacobian's unit normal is nxd/area
+// (jacobianRoe.cpp:164) while the flux's is nxd*(1/area)
+// (interfaceFlux.cpp:62-65); both are formed.
+// ##################################################################
+#ifndef HAMSTR_GPU_ROE_CUH
+#define HAMSTR_GPU_ROE_CUH
+
+namespace hamstr {
+
+struct RoeOut {
+   double flux[4];
+   double spec;
+};
+
+// lm/rm receive the 4x4 left/right Jacobians (row-major) times the area.
+// Returns false when the spectral radius is NaN.
+template <bool JAC>
+__device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&ql)[4],
+                                         const double (&qr)[4], double gam, RoeOut& o,
+                                         double* __restrict__ lm, double* __restrict__ rm)
+{
+   const double gm1 = gam - 1.0;
+   const double area = sqrt(nxd * nxd + nyd * nyd);
+   const double invArea = 1. / area;
+   const double nx = nxd * invArea;
+   const double ny = nyd * invArea;
+
+   const double rol = ql[0];
+   const double ul = ql[1] / ql[0];
+   const double vl = ql[2] / ql[0];
+   const double pl = gm1 * (ql[3] - 0.5 * rol * (ul * ul + vl * vl));
+   const double hl = (ql[3] + pl) / rol;
+   const double ror = qr[0];
+   const double ur = qr[1] / qr[0];
+   const double vr = qr[2] / qr[0];
+   const double pr = gm1 * (qr[3] - 0.5 * ror * (ur * ur + vr * vr));
+   const double hr = (qr[3] + pr) / ror;
+   const double dp = pr - pl;
+   const double uconr = ur * nx + vr * ny;
+   const double uconl = ul * nx + vl * ny;
+
+   const double fact = sqrt(ror / rol);
+   const double A = 1.0 / (1.0 + fact);
+   const double B = fact / (1.0 + fact);
+   const double robar = rol * fact;
+   const double ubar = ul * A + ur * B;
+   const double vbar = vl * A + vr * B;
+   const double hbar = hl * A + hr * B;
+   double cbar = gm1 * (hbar - 0.5 * (ubar * ubar + vbar * vbar));
+   cbar = sqrt(cbar);
+   const double uconbar = ubar * nx + vbar * ny;
+
+   {
+      const double eig1 = fabs(uconbar);
+      const double eig2 = fabs(uconbar + cbar);
+      const double eig3 = fabs(uconbar - cbar);
+      double spec = eig1 + cbar;
+      if (spec != spec) return false;
+      const double term1 = -eig1 + 0.5 * (eig2 + eig3);
+      const double term2 = 0.5 * (eig2 - eig3);
+      const double del1 = term1 * dp / cbar / cbar + term2 * robar * (uconr - uconl) / cbar;
+      const double del2 = term1 * (uconr - uconl) * robar + term2 * dp / cbar;
+      double fm0 = eig1 * (qr[0] - ql[0]);
+      double fm1 = eig1 * (qr[1] - ql[1]);
+      double fm2 = eig1 * (qr[2] - ql[2]);
+      double fm3 = eig1 * (qr[3] - ql[3]);
+      fm0 = fm0 + del1;
+      fm1 = fm1 + del1 * ubar + del2 * nx;
+      fm2 = fm2 + del1 * vbar + del2 * ny;
+      fm3 = fm3 + del1 * hbar + del2 * uconbar;
+      const double fl0 = rol * uconl, fr0 = ror * uconr;
+      const double fl1 = rol * uconl * ul + nx * pl, fr1 = ror * uconr * ur + nx * pr;
+      const double fl2 = rol * uconl * vl + ny * pl, fr2 = ror * uconr * vr + ny * pr;
+      const double fl3 = (ql[3] + pl) * uconl, fr3 = (qr[3] + pr) * uconr;
+      o.flux[0] = 0.5 * (fl0 + fr0 - fm0);
+      o.flux[1] = 0.5 * (fl1 + fr1 - fm1);
+      o.flux[2] = 0.5 * (fl2 + fr2 - fm2);
+      o.flux[3] = 0.5 * (fl3 + fr3 - fm3);
+      o.flux[0] *= area;
+      o.flux[1] *= area;
+      o.flux[2] *= area;
+      o.flux[3] *= area;
+      spec *= area;
+      o.spec = spec;
+   }
+   if (!JAC) return true;
+
+   // ---------------- Jacobian (jacobianRoe3D, IMODE=1) ----------------
+   const double nxj = nxd / area;
+   const double nyj = nyd / area;
+   const double uconlj = ul * nxj + vl * nyj;
+   const double uconrj = ur * nxj + vr * nyj;
+   const double uconbarj = ubar * nxj + vbar * nyj;
+   const double e1 = fabs(uconbarj);
+   const double e2 = fabs(uconbarj + cbar);
+   const double e3 = fabs(uconbarj - cbar);
+   const double t1 = -e1 + 0.5 * (e2 + e3);
+   const double t2 = 0.5 * (e2 - e3);
+   const double t2rb = t2 * robar;
+
+   // derivative vectors, kept components {rho, rho u, rho v, E}
+   // left (jacobianRoe.cpp:209-250)
+   const double du0l = -ul / rol;
+   const double irl = 1.0 / rol;
+   const double dv0l = -vl / rol;
+   const double dp0l = 0.5 * gm1 * (ul * ul + vl * vl);
+   const double dp1l = -gm1 * ul;
+   const double dp2l = -gm1 * vl;
+   const double dc0l = -uconlj / rol;
+   const double dc1l = nxj / rol;
+   const double dc2l = nyj / rol;
+   // right (jacobianRoe.cpp:257-296)
+   const double du0r = -ur / ror;
+   const double irr = 1.0 / ror;
+   const double dv0r = -vr / ror;
+   const double dp0r = 0.5 * gm1 * (ur * ur + vr * vr);
+   const double dp1r = -gm1 * ur;
+   const double dp2r = -gm1 * vr;
+   const double dc0r = -uconrj / ror;
+   const double dc1r = nxj / ror;
+   const double dc2r = nyj / ror;
+
+   // frozen-eigenvalue linearisation of del1/del2 (jacobianRoe.cpp:323-334)
+   const double mt1 = -t1;
+   double D1l[4], D2l[4], D1r[4], D2r[4];
+   D1l[0] = mt1 * dp0l / cbar / cbar - t2rb * dc0l / cbar;
+   D1l[1] = mt1 * dp1l / cbar / cbar - t2rb * dc1l / cbar;
+   D1l[2] = mt1 * dp2l / cbar / cbar - t2rb * dc2l / cbar;
+   D1l[3] = mt1 * gm1 / cbar / cbar;
+   D2l[0] = mt1 * dc0l * robar - t2 * dp0l / cbar;
+   D2l[1] = mt1 * dc1l * robar - t2 * dp1l / cbar;
+   D2l[2] = mt1 * dc2l * robar - t2 * dp2l / cbar;
+   D2l[3] = -(t2 * gm1 / cbar);
+   D1r[0] = t1 * dp0r / cbar / cbar + t2rb * dc0r / cbar;
+   D1r[1] = t1 * dp1r / cbar / cbar + t2rb * dc1r / cbar;
+   D1r[2] = t1 * dp2r / cbar / cbar + t2rb * dc2r / cbar;
+   D1r[3] = t1 * gm1 / cbar / cbar;
+   D2r[0] = t1 * dc0r * robar + t2 * dp0r / cbar;
+   D2r[1] = t1 * dc1r * robar + t2 * dp1r / cbar;
+   D2r[2] = t1 * dc2r * robar + t2 * dp2r / cbar;
+   D2r[3] = t2 * gm1 / cbar;
+
+   // native flux Jacobians (jacobianRoe.cpp:573-605), kept rows/columns
+   const double el = ql[3] + pl, er = qr[3] + pr;
+   const double rcl = rol * uconlj, rcr = ror * uconrj;
+   double L1[16], R1[16];
+   L1[0] = uconlj + rol * dc0l;
+   L1[1] = rol * dc1l;
+   L1[2] = rol * dc2l;
+   L1[3] = 0.0;
+   L1[4] = uconlj * ul + rol * dc0l * ul + rcl * du0l + nxj * dp0l;
+   L1[5] = rol * dc1l * ul + rcl * irl + nxj * dp1l;
+   L1[6] = rol * dc2l * ul + nxj * dp2l;
+   L1[7] = nxj * gm1;
+   L1[8] = uconlj * vl + rol * dc0l * vl + rcl * dv0l + nyj * dp0l;
+   L1[9] = rol * dc1l * vl + nyj * dp1l;
+   L1[10] = rol * dc2l * vl + rcl * irl + nyj * dp2l;
+   L1[11] = nyj * gm1;
+   L1[12] = dp0l * uconlj + el * dc0l;
+   L1[13] = dp1l * uconlj + el * dc1l;
+   L1[14] = dp2l * uconlj + el * dc2l;
+   L1[15] = (1.0 + gm1) * uconlj;
+   R1[0] = uconrj + ror * dc0r;
+   R1[1] = ror * dc1r;
+   R1[2] = ror * dc2r;
+   R1[3] = 0.0;
+   R1[4] = uconrj * ur + ror * dc0r * ur + rcr * du0r + nxj * dp0r;
+   R1[5] = ror * dc1r * ur + rcr * irr + nxj * dp1r;
+   R1[6] = ror * dc2r * ur + nxj * dp2r;
+   R1[7] = nxj * gm1;
+   R1[8] = uconrj * vr + ror * dc0r * vr + rcr * dv0r + nyj * dp0r;
+   R1[9] = ror * dc1r * vr + nyj * dp1r;
+   R1[10] = ror * dc2r * vr + rcr * irr + nyj * dp2r;
+   R1[11] = nyj * gm1;
+   R1[12] = dp0r * uconrj + er * dc0r;
+   R1[13] = dp1r * uconrj + er * dc1r;
+   R1[14] = dp2r * uconrj + er * dc2r;
+   R1[15] = (1.0 + gm1) * uconrj;
+
+   // dissipation part (jacobianRoe.cpp:500-521) and the final
+   // 0.5*(native - dissipation) times area (jacobianRoe.cpp:611-618, :63-68)
+   const double rowc[4] = {0.0, ubar, vbar, hbar};
+   const double rown[4] = {0.0, nxj, nyj, uconbarj};
+#pragma unroll
+   for (int rI = 0; rI < 4; rI++) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+         double ml, mr;
+         if (rI == 0) {
+            ml = (c == 0) ? (-e1 + D1l[0]) : D1l[c];
+            mr = (c == 0) ? (e1 + D1r[0]) : D1r[c];
+         } else {
+            if (c == rI) {
+               ml = -e1 + D1l[c] * rowc[rI] + D2l[c] * rown[rI];
+               mr = e1 + D1r[c] * rowc[rI] + D2r[c] * rown[rI];
+            } else {
+               ml = D1l[c] * rowc[rI] + D2l[c] * rown[rI];
+               mr = D1r[c] * rowc[rI] + D2r[c] * rown[rI];
+            }
+         }
+         lm[4 * rI + c] = 0.5 * (L1[4 * rI + c] - ml) * area;
+         rm[4 * rI + c] = 0.5 * (R1[4 * rI + c] - mr) * area;
+      }
+   }
+   return true;
+}
+
+}  // namespace hamstr
+#endif

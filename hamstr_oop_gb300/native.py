@@ -1,0 +1,245 @@
+"""ctypes bindings of the C ABI in include/hamstr_gpu.h.
+
+The library is ``hamstr_oop_gb300/lib/libhamstr_gb300.so`` built by
+``hamstr_oop_gb300.build``.  There is no CPU fallback: if the library is
+missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libhamstr_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "hamstr_gpu.h")
+
+SIZE_NAMES = ("nCell", "nFace", "nChain", "nChainFace", "nMaxChain", "order",
+              "msweep", "nGhost", "nNode", "nColor")
+PARAM_NAMES = ("Mach", "alpha", "CFL", "gamma", "rinf", "uinf", "vinf", "einf", "pinf")
+
+_lib = None
+
+
+class HamstrError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("msweep", ctypes.c_int), ("CFL", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("rinf", ctypes.c_double), ("uinf", ctypes.c_double),
+                ("vinf", ctypes.c_double), ("einf", ctypes.c_double)]
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load the native library (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError("libhamstr_gb300.so is not built; run `python -m hamstr_oop_gb300.build`")
+        from . import build
+        build.build()
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i, d, cp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "hamstr_case_open": (i, [cp, pp, cp, i]),
+        "hamstr_case_close": (None, [vp]),
+        "hamstr_case_sizes": (i, [vp, vp]),
+        "hamstr_case_params": (i, [vp, vp]),
+        "hamstr_case_get_int": (i, [vp, cp, vp, ctypes.POINTER(i)]),
+        "hamstr_case_get": (i, [vp, cp, vp]),
+        "hamstr_case_set_run": (i, [vp, i, i, d]),
+        "hamstr_case_set_freestream": (i, [vp, d, d, d]),
+        "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
+        "hamstr_gpu_create_from_case": (i, [vp, pp]),
+        "hamstr_gpu_destroy": (i, [vp]),
+        "hamstr_gpu_strerror": (cp, [i]),
+        "hamstr_gpu_last_error": (cp, []),
+        "hamstr_gpu_get": (i, [vp, cp, vp]),
+        "hamstr_gpu_set": (i, [vp, cp, vp]),
+        "hamstr_gpu_compute_rhs": (i, [vp, i, ctypes.POINTER(d), ctypes.POINTER(d)]),
+        "hamstr_gpu_adi": (i, [vp, ctypes.POINTER(d), ctypes.POINTER(d)]),
+        "hamstr_gpu_linear_rhs": (i, [vp, ctypes.POINTER(d), ctypes.POINTER(d)]),
+        "hamstr_gpu_step": (i, [vp, vp]),
+        "hamstr_gpu_march": (i, [vp, i, d, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "hamstr_gpu_stream": (vp, [vp]),
+        "hamstr_gpu_profile_step": (i, [vp, i, ctypes.POINTER(cp), vp, vp, ctypes.POINTER(i)]),
+        "hamstr_gpu_launches_per_step": (i, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = res, args
+    _lib = L
+    return L
+
+
+def declared_symbols() -> list:
+    """Function names declared in include/hamstr_gpu.h."""
+    import re
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(hamstr_[a-z_0-9]+)\s*\(", txt)))
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(st: int):
+    if st != 0:
+        L = load()
+        msg = L.hamstr_gpu_strerror(st).decode()
+        det = L.hamstr_gpu_last_error()
+        if det:
+            msg += ": " + det.decode()
+        raise HamstrError(st, msg)
+
+
+class Case:
+    """Host-side case: the reference reader + preprocessing + initial state."""
+
+    def __init__(self, case_dir: str):
+        L = load()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(1024)
+        st = L.hamstr_case_open(case_dir.encode(), ctypes.byref(h), err, 1024)
+        if st != 0:
+            raise HamstrError(st, err.value.decode())
+        self.h = h
+        self.case_dir = case_dir
+        s = np.zeros(10, dtype=np.int32)
+        _check(L.hamstr_case_sizes(self.h, _ptr(s)))
+        self.sizes = dict(zip(SIZE_NAMES, (int(v) for v in s)))
+
+    def close(self):
+        if self.h:
+            load().hamstr_case_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> dict:
+        v = np.zeros(9)
+        _check(load().hamstr_case_params(self.h, _ptr(v)))
+        return dict(zip(PARAM_NAMES, (float(x) for x in v)))
+
+    def get_int(self, name: str) -> np.ndarray:
+        L = load()
+        n = ctypes.c_int(0)
+        _check(L.hamstr_case_get_int(self.h, name.encode(), None, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), dtype=np.int32)
+        _check(L.hamstr_case_get_int(self.h, name.encode(), _ptr(out), ctypes.byref(n)))
+        return out[:n.value]
+
+    _DW = {"x": ("nNode", 2), "vol": ("nCell", 1), "normVec": ("nFace", 2), "refMtx": ("nFace", 4),
+           "q": ("nCell", 4)}
+
+    def get(self, name: str) -> np.ndarray:
+        key, w = self._DW[name]
+        out = np.zeros(self.sizes[key] * w)
+        _check(load().hamstr_case_get(self.h, name.encode(), _ptr(out)))
+        return out
+
+    def set_run(self, order: int, msweep: int, cfl: float):
+        _check(load().hamstr_case_set_run(self.h, order, msweep, cfl))
+        self.sizes = dict(self.sizes, order=order, msweep=msweep, nGhost=3 if order == 5 else 2)
+
+    def set_freestream(self, uinf: float, vinf: float, einf: float):
+        _check(load().hamstr_case_set_freestream(self.h, uinf, vinf, einf))
+
+
+class GpuSolver:
+    """Device solver handle (the SOLVER of the drop-in)."""
+
+    def __init__(self, case: Case):
+        L = load()
+        h = ctypes.c_void_p()
+        _check(L.hamstr_gpu_create_from_case(case.h, ctypes.byref(h)))
+        self.h = h
+        self.sizes = dict(case.sizes)
+
+    def close(self):
+        if self.h:
+            load().hamstr_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    _DW = {"q": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
+           "sigma": ("nCell", 1), "ff": ("nFace", 32)}
+
+    def get(self, name: str) -> np.ndarray:
+        key, w = self._DW[name]
+        out = np.zeros(self.sizes[key] * w)
+        _check(load().hamstr_gpu_get(self.h, name.encode(), _ptr(out)))
+        return out
+
+    def set(self, name: str, arr) -> None:
+        key, w = self._DW[name]
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        if a.size != self.sizes[key] * w:
+            raise ValueError("%s needs %d values" % (name, self.sizes[key] * w))
+        _check(load().hamstr_gpu_set(self.h, name.encode(), _ptr(a)))
+
+    def compute_rhs(self, implicit: bool = True):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(load().hamstr_gpu_compute_rhs(self.h, int(implicit), ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def adi(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(load().hamstr_gpu_adi(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def linear_rhs(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(load().hamstr_gpu_linear_rhs(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def step(self) -> np.ndarray:
+        out = np.zeros(4)
+        _check(load().hamstr_gpu_step(self.h, _ptr(out)))
+        return out
+
+    def march(self, nsteps: int, tol: float = 0.0):
+        hist = np.zeros((max(nsteps, 1), 4))
+        ev, conv = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load().hamstr_gpu_march(self.h, nsteps, tol, _ptr(hist), ctypes.byref(ev), ctypes.byref(conv)))
+        return hist[:ev.value], bool(conv.value)
+
+    @property
+    def stream(self) -> int:
+        return int(load().hamstr_gpu_stream(self.h) or 0)
+
+    def launches_per_step(self) -> int:
+        n = load().hamstr_gpu_launches_per_step(self.h)
+        if n < 0:
+            _check(n)
+        return n
+
+    def profile_step(self, reps: int = 3) -> dict:
+        names = (ctypes.c_char_p * 16)()
+        ms = np.zeros(16)
+        cnt = np.zeros(16, dtype=np.int32)
+        n = ctypes.c_int(16)
+        _check(load().hamstr_gpu_profile_step(self.h, reps, names, _ptr(ms), _ptr(cnt), ctypes.byref(n)))
+        return {names[k].decode(): (float(ms[k]), int(cnt[k])) for k in range(n.value)}

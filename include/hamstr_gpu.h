@@ -1,0 +1,126 @@
+/*
+ * hamstr_gpu.h -- C ABI of the GB300 HAMSTR steady ADI iteration.
+ *
+ * The reference (HAMSTR_OOP, 2D Euler, line-implicit) is a C++ program with
+ * no library boundary: its SOLVER class reaches the mesh and solution
+ * through friend access (meshBlock.h:18, solnBlock.h:15) and runs
+ * single-threaded on the host.  This header is the boundary its hot path
+ * moves behind.  Each entry point names the reference interface it
+ * replaces.  The C++ drop-in classes MESHBLOCK / SOLNBLOCK / SOLVER / HAMSTR
+ * (hamstr_oop_gb300/csrc/host/) are thin callers of these functions.
+ *
+ * Conventions
+ *   - Plain pointers and sizes; arrays are the reference's layouts:
+ *       q, r, r0, dq      [nCell][4] doubles (rho, rho u, rho v, E)
+ *       sigma             [nCell]
+ *       faces             [nFace][6] ints  n1 n2 cL eL cR eR (io.cpp:349-355),
+ *                         after the reader's swap and preprocessing's wall
+ *                         tag cR = -2 (io.cpp:360-365, preprocess.cpp:182)
+ *       normVec           [nFace][2]  (dy, -dx)  (preprocess.cpp:86-87)
+ *       refMtx            [nFace][2][2]          (preprocess.cpp:97-101)
+ *       faceStartPerChain [nChain+1], chainConn [nChainFace] (io.cpp:223-264)
+ *       ff                [nFace][2][4][4]  FACEMAT lmat, rmat (codetypes.h:64-68)
+ *   - Every function returns an int status: 0 on success, a negative
+ *     HAMSTR_GPU_ERR_* code otherwise.  Nothing exits the process (the
+ *     reference calls exit(1) on a NaN spectral radius,
+ *     interfaceFlux.cpp:117-124, and on missing files, io.cpp:19-23).
+ *   - A solver handle owns its device memory and one CUDA stream; calls on
+ *     one handle are not re-entrant (the reference is single-threaded).
+ *     Host arrays belong to the caller; every copy is explicit.
+ */
+#ifndef HAMSTR_GPU_H
+#define HAMSTR_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HAMSTR_GPU_OK             0
+#define HAMSTR_GPU_ERR_ARG       -1   /* bad argument or unknown array name */
+#define HAMSTR_GPU_ERR_TOPOLOGY  -2   /* chains/faces the reference cannot process */
+#define HAMSTR_GPU_ERR_CUDA      -3   /* CUDA runtime failure */
+#define HAMSTR_GPU_ERR_NAN       -4   /* NaN spectral radius (interfaceFlux.cpp:117-124) */
+#define HAMSTR_GPU_ERR_IO        -5   /* missing or malformed case file (io.cpp:19-23,138-141) */
+#define HAMSTR_GPU_ERR_NOMEM     -6   /* host or device allocation failed */
+
+typedef struct hamstr_case hamstr_case; /* host mesh + inputs: MESHBLOCK + SOLNBLOCK */
+typedef struct hamstr_gpu hamstr_gpu;   /* device solver: SOLVER */
+
+typedef struct hamstr_gpu_params {
+   int    order;      /* 1, 3 (MUSCL) or 5 (WENO)         solnBlock.h:30 */
+   int    msweep;     /* ADI sweeps per step              solnBlock.h:34 */
+   double CFL;        /*                                  solnBlock.h:41 */
+   double gamma;      /* 1.4                              initFlow.cpp:19 */
+   double rinf, uinf, vinf, einf;   /* freestream         initFlow.cpp:24-57 */
+} hamstr_gpu_params;
+
+/* ---------------- host side (reader, preprocessing, initial state) -------
+ * Replaces MESHBLOCK::readMeshData (io.cpp:58-372), SOLNBLOCK::
+ * readSolutionInputs (io.cpp:13-51), MESHBLOCK::setViscosity(0) +
+ * preprocess (meshBlock.h:52, preprocess.cpp:15-241) and SOLVER::initFlow
+ * (initFlow.cpp:12-93): reads <case_dir>/input.hamstr and
+ * <case_dir>/input/domain000/*.dat. */
+int  hamstr_case_open(const char* case_dir, hamstr_case** out, char* err, int errlen);
+void hamstr_case_close(hamstr_case* c);
+/* out[10]: nCell nFace nChain nChainFace nMaxChain order msweep nGhost nNode nColor */
+int  hamstr_case_sizes(const hamstr_case* c, int* out);
+/* out[9]: Mach alpha CFL gamma rinf uinf vinf einf pinf */
+int  hamstr_case_params(const hamstr_case* c, double* out);
+/* int arrays: faces chainConn faceStartPerChain c2chain bFaces chainsPerColor
+ * double arrays: x vol normVec refMtx q  (q is the freestream initial state) */
+int  hamstr_case_get_int(const hamstr_case* c, const char* name, int* out, int* count);
+int  hamstr_case_get(const hamstr_case* c, const char* name, double* out);
+/* overrides of input.hamstr values (order, msweep, CFL) and the freestream */
+int  hamstr_case_set_run(hamstr_case* c, int order, int msweep, double cfl);
+int  hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double einf);
+
+/* ---------------- device solver ------------------------------------------
+ * hamstr_gpu_create replaces SOLVER::SOLVER (solver.cpp:13-81): it copies
+ * the mesh and chain arrays to the GPU, derives the per-mesh stencil,
+ * accumulation and block-assembly layout once, and sets q to freestream. */
+int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace,
+                      const int* faces, const double* normVec, const double* refMtx,
+                      int nChain, const int* faceStartPerChain, const int* chainConn,
+                      hamstr_gpu** out);
+int hamstr_gpu_create_from_case(const hamstr_case* c, hamstr_gpu** out);
+int hamstr_gpu_destroy(hamstr_gpu* g);
+const char* hamstr_gpu_strerror(int status);
+/* last detailed message (topology problems, CUDA errors) for this thread */
+const char* hamstr_gpu_last_error(void);
+
+/* named device arrays to/from host memory: q r r0 dq sigma (cell arrays) and
+ * ff ([nFace][32], face order as sb->ff; faces outside every chain read 0) */
+int hamstr_gpu_get(hamstr_gpu* g, const char* name, double* out);
+int hamstr_gpu_set(hamstr_gpu* g, const char* name, const double* in);
+
+/* SOLVER::computeRHS (computeRHS.cpp:17-427): r, sigma and, when implicit,
+ * the face Jacobians ff; *l2 = sqrt(sum r_rho^2)/nCell, *linf = max|r_rho|. */
+int hamstr_gpu_compute_rhs(hamstr_gpu* g, int implicit, double* l2, double* linf);
+/* SOLVER::ADI (ADI.cpp:15-266): msweep line sweeps, dq, q += dq; the norms
+ * are those of the final linear residual (computeLinearRHS.cpp:354-368). */
+int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf);
+/* SOLVER::computeLinearRHS (computeLinearRHS.cpp:13-371) on the current
+ * r0, dq, sigma and ff. */
+int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf);
+/* SOLVER::stepSolution, ADI branch (march.cpp:381-386):
+ * norms4 = {computeRHS L2, Linf, final linear L2, Linf}. */
+int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
+/* SOLVER::marchInTime (march.cpp:15-59) with a convergence stop: runs up
+ * to nsteps steps; stops before the ADI of the first step whose computeRHS
+ * L2 norm is <= tol (tol <= 0: never).  hist (may be NULL) receives 4
+ * doubles per computeRHS evaluation; *evals = number of rows written,
+ * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
+int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
+
+/* the CUDA stream (cudaStream_t) the handle launches on */
+void* hamstr_gpu_stream(hamstr_gpu* g);
+/* Per-kernel CUDA-event timing of one step (eager launches on the handle's
+ * stream): ms[i] and launches[i] for i < *n kernel names (names[i]). */
+int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double* ms, int* launches, int* n);
+/* number of kernel launches of one step (for launch accounting) */
+int hamstr_gpu_launches_per_step(hamstr_gpu* g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
