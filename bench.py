@@ -1,0 +1,365 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 HAMSTR steady ADI iteration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c2|c1]
+
+A step is one pseudo-time iteration (computeRHS + ADI with msweep sweeps,
+march.cpp:381-386) over one mesh.  The metric is cell-iterations per second
+(cells x steps / time), whole job.  Workloads (seeded synthetic meshes; the
+reference ships none):
+
+  c2  NACA 0012 O-grid 512 x 128 (65,536 cells), WENO (order 5), CFL 20,
+      msweep 2, Mach 0.5, alpha 1.25 deg -- the plain FP64 GPU drop-in
+      configuration (quadrilaterals; the mixed tri/quad split is not applied)
+  c1  NACA 0012 O-grid 128 x 32 (4,096 cells), MUSCL (order 3), CFL 10
+
+gb300 arm ("value"): state resident in HBM, K captured steps timed with CUDA
+events on the solver's stream, an L2 flush (write of 512 MiB) between timed
+steps.  "e2e": the same steps through the C ABI with host buffers (pinned q
+in, step, q and norms out) timed on the host clock.  Multi-GPU runs are
+independent replicas (one mesh per rank, no collective on the data path).
+
+reference arm: the reference algorithm on the host cores (the CPU oracle:
+the reference library where it was compiled on this machine, else the C
+restatement), one independent copy of the mesh per host thread.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cell-iters/s"
+UNIT = "cell-iter/s"
+WORKLOADS = {
+    "c2": dict(ni=512, nj=128, order=5, CFL=20.0, msweep=2, Mach=0.5, alpha=1.25,
+               name="naca0012_ogrid_512x128_weno5_cfl20_msweep2"),
+    "c1": dict(ni=128, nj=32, order=3, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
+               name="naca0012_ogrid_128x32_muscl3_cfl10_msweep2"),
+}
+L2_FLUSH_BYTES = 512 << 20
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def make_case(wl: dict, rank: int) -> str:
+    from hamstr_oop_gb300 import meshgen
+    base = os.environ.get("HAMSTR_BENCH_DIR", "/tmp/hamstr_bench")
+    d = os.path.join(base, "%s_r%d" % (wl["name"], rank))
+    marker = os.path.join(d, "input.hamstr")
+    if not os.path.exists(marker):
+        meshgen.make_case(d, wl["ni"], wl["nj"], order=wl["order"], CFL=wl["CFL"], msweep=wl["msweep"],
+                          Mach=wl["Mach"], alpha=wl["alpha"], nsteps=1)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.lines = index, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# FP64 issue peak of the GPU, warp instructions per second, measured with an
+# independent-chain DADD loop (profiles/fp64_pipe_gb300.md)
+FP64_WARP_INSTR_PER_S = 15.8e9
+
+
+def ncu_profile_table() -> dict:
+    """kernel -> {dram_bytes, fp64_inst, launches} from profiles/ncu_kernel_table.txt."""
+    p = os.path.join(ROOT, "profiles", "ncu_kernel_table.txt")
+    out = {}
+    if not os.path.exists(p):
+        return out
+    for ln in open(p):
+        ln = ln.strip()
+        if not ln or ln.startswith("#"):
+            continue
+        f = ln.split()
+        if len(f) >= 4:
+            try:
+                out[f[0]] = {"workload": f[1], "dram_bytes": float(f[2]), "fp64_warp_inst": float(f[3])}
+            except ValueError:
+                pass
+    return out
+
+
+def algorithmic_bytes(kernel: str, lay: dict, sizes: dict, order: int) -> float:
+    """Compulsory HBM bytes of one launch (each array touched once)."""
+    nc, ns, nr = sizes["nCell"], lay["nSlot"], lay["nRow"]
+    npr = lay["nPeriodicRows"]
+    sten = {1: 2, 3: 4, 5: 6}[order]
+    if kernel == "rhs_face":
+        # slot record 32 + normal 16 + stencil entries 16*sten/2 (shared by neighbours)
+        # + q once per cell; writes flux 32, spec 8, ff 256
+        return ns * (32 + 16 + 8 * sten + 32 + 8 + 256) + nc * 32
+    if kernel == "lin_face":
+        return ns * (32 + 8 * sten + 256 + 32) + nc * 64
+    if kernel == "adi_factor":
+        # ff once per slot, dtfac, row ops/cells 56 B; writes A, LU, C' (+ a', c_N for periodic rows)
+        return ns * 256 + nc * 8 + nr * 56 + (nr - npr) * 8 * 48 + npr * 8 * 80
+    if kernel == "adi_solve":
+        # per wave launch: rows of that wave read their factors; averaged over waves
+        per_row_open, per_row_per = 8 * 48 + 64 + 64, 8 * 80 + 64 + 64
+        return ((nr - npr) * per_row_open + npr * per_row_per) / max(lay["nWave"], 1)
+    if kernel == "rhs_cell":
+        return ns * 40 + nc * (4 + 16 + 96 + 16)
+    if kernel == "lin_cell":
+        return ns * 32 + nc * (4 + 16 + 8 + 32 + 32 + 32)
+    if kernel == "dq_update":
+        return nc * 96
+    return 0.0
+
+
+def run_gpu(args, wl, rank, local_rank, world):
+    import numpy as np
+    import torch
+    from hamstr_oop_gb300 import native
+
+    torch.cuda.set_device(local_rank)
+    native.load()
+    case_dir = make_case(wl, rank)
+    case = native.Case(case_dir)
+    gpu = native.GpuSolver(case)
+    sizes = case.sizes
+    lay = gpu.layout()
+    nc = sizes["nCell"]
+    hs = torch.cuda.ExternalStream(gpu.stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # warm-up (W >= 3 steps), also builds the CUDA graph
+    gpu.enqueue_steps(max(args.warmup, 1))
+    gpu.sync()
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t0 = time.perf_counter()
+    with torch.cuda.stream(hs):
+        for k in range(args.steps):
+            flush.fill_(float(k))                 # L2 flush, outside the timed events
+            starts[k].record(hs)
+            gpu.enqueue_steps(1)
+            ends[k].record(hs)
+    gpu.sync()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = world * nc * args.steps / (ms * 1e-3)
+
+    # end-to-end through the C ABI with host buffers
+    qhost = torch.empty(4 * nc, dtype=torch.float64, pin_memory=True)
+    qnp = qhost.numpy()
+    qnp[:] = gpu.get("q")
+    e2e_steps = max(1, min(args.steps, 20))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        gpu.set("q", qnp)
+        gpu.step()
+        qnp[:] = gpu.get("q")
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * nc * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 32 * nc, "d2h_bytes_per_step": 32 * nc + 32, "steps": e2e_steps}
+
+    out = None
+    if rank == 0:
+        prof = gpu.profile_step(reps=3)
+        per_step = {k: v[0] for k, v in prof.items()}
+        dom = max(per_step, key=per_step.get)
+        launches = prof[dom][1]
+        avg_ms = per_step[dom] / max(launches, 1)
+        peaks = measured_peaks()
+        alg = algorithmic_bytes(dom, lay, sizes, wl["order"])
+        achieved = alg / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else None
+        table = ncu_profile_table()
+        traffic = table.get(dom, {}).get("dram_bytes")
+        fp64 = None
+        if dom in table and table[dom].get("fp64_warp_inst"):
+            rate = table[dom]["fp64_warp_inst"] / (avg_ms * 1e-3)
+            fp64 = {"achieved_warp_inst_per_s": rate, "peak_warp_inst_per_s": FP64_WARP_INSTR_PER_S,
+                    "frac": rate / FP64_WARP_INSTR_PER_S,
+                    "note": "FP64 issue rate from ncu instruction counts over the live CUDA-event duration"}
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                    "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                    "avg_launch_ms": avg_ms, "peak_source": peaks["source"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                    "fp64": fp64,
+                    "kernel_ms_per_step": {k: round(v, 4) for k, v in per_step.items()}}
+        cpu = cpu_baseline(wl, case_dir, nc) if (world == 1 and not args.no_cpu) else None
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["name"], "cells": nc, "faces": sizes["nFace"], "chains": sizes["nChain"],
+                       "order": wl["order"], "msweep": wl["msweep"], "CFL": wl["CFL"], "mach": wl["Mach"],
+                       "alpha_deg": wl["alpha"], "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "512 MiB flush write between timed steps (untimed)",
+                       "mesh": "quadrilateral O-grid; mixed tri/quad split not applied"},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": gpu.launches_per_step() * args.steps,
+            "wall_s_timed_region": wall,
+        }
+    gpu.close()
+    return out
+
+
+def cpu_baseline(wl, case_dir, nc, steps=None) -> dict:
+    """The oracle on the host cores: one copy of the mesh per thread, a bounded sample."""
+    from oracle import oracle
+    oracle.build(reference=False)
+    threads = os.cpu_count() or 1
+    steps = steps or (2 if nc > 20000 else 20)
+    base = oracle.OracleCase(case_dir, "port")
+    cases = [base] + [base.clone() for _ in range(threads - 1)]
+    oracle.march_replicas(cases, 1)          # warm-up step
+    t0 = time.perf_counter()
+    oracle.march_replicas(cases, steps)
+    dt = time.perf_counter() - t0
+    for c in cases:
+        c.close()
+    return {"value": threads * nc * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d pseudo-time steps on each of %d independent copies of the %s mesh (one per thread)"
+                      % (steps, threads, wl["name"])}
+
+
+def run_reference(args, wl, rank):
+    if rank != 0:
+        return None
+    from oracle import oracle
+    oracle.build(reference=False)
+    case_dir = make_case(wl, 0)
+    threads = os.cpu_count() or 1
+    base = oracle.OracleCase(case_dir, "port")
+    nc = base.sizes["nCell"]
+    cases = [base] + [base.clone() for _ in range(threads - 1)]
+    oracle.march_replicas(cases, max(args.warmup, 1))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.march_replicas(cases, 1)
+    dt = time.perf_counter() - t0
+    for c in cases:
+        c.close()
+    value = threads * nc * args.steps / dt
+    sample = ("each step: one pseudo-time step on each of %d independent copies of the %s mesh "
+              "(one per host thread), C restatement of the reference algorithm (oracle/hamstr_oracle.c, "
+              "bit-identical to the reference on the pinned fixtures)" % (threads, wl["name"]))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": wl["name"], "cells": nc, "order": wl["order"],
+                                            "msweep": wl["msweep"], "CFL": wl["CFL"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    rank, local_rank, world = dist_env()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        out = run_reference(args, wl, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    out = run_gpu(args, wl, rank, local_rank, world)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

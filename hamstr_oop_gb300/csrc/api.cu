@@ -119,9 +119,11 @@ struct hamstr_gpu {
 
    int reset_ctl(double tol)
    {
-      tol_host = tol;
       CK(cudaMemsetAsync(d.ctl, 0, 2 * sizeof(int), stream));
-      CK(cudaMemcpyAsync(d.tol, &tol_host, sizeof(double), cudaMemcpyHostToDevice, stream));
+      if (tol != tol_host) {
+         tol_host = tol;
+         CK(cudaMemcpyAsync(d.tol, &tol_host, sizeof(double), cudaMemcpyHostToDevice, stream));
+      }
       return HAMSTR_GPU_OK;
    }
 
@@ -496,6 +498,38 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
 }
 
 void* hamstr_gpu_stream(hamstr_gpu* g) { return g ? (void*)g->stream : nullptr; }
+
+int hamstr_gpu_enqueue_steps(hamstr_gpu* g, int n)
+{
+   if (!g || n < 0) return HAMSTR_GPU_ERR_ARG;
+   int st = g->capture();
+   if (st) return st;
+   st = g->reset_ctl(0.0);
+   if (st) return st;
+   for (int i = 0; i < n; i++) CK(cudaGraphLaunch(g->step_exec, g->stream));
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_sync(hamstr_gpu* g)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   return g->status_check();
+}
+
+int hamstr_gpu_layout(hamstr_gpu* g, int* out)
+{
+   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
+   const Plan& P = g->plan;
+   int nper = 0, nperrows = 0;
+   for (int c = 0; c < P.nChain; c++)
+      if (P.chain_periodic[c]) {
+         nper++;
+         nperrows += P.chain_nrows[c];
+      }
+   out[0] = P.nSlot; out[1] = P.nSten; out[2] = P.nRow; out[3] = P.nChain;
+   out[4] = P.nWave; out[5] = nper; out[6] = nperrows; out[7] = P.maxRows;
+   return HAMSTR_GPU_OK;
+}
 
 int hamstr_gpu_launches_per_step(hamstr_gpu* g)
 {

@@ -73,6 +73,9 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_step": (i, [vp, vp]),
         "hamstr_gpu_march": (i, [vp, i, d, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "hamstr_gpu_stream": (vp, [vp]),
+        "hamstr_gpu_enqueue_steps": (i, [vp, i]),
+        "hamstr_gpu_sync": (i, [vp]),
+        "hamstr_gpu_layout": (i, [vp, vp]),
         "hamstr_gpu_profile_step": (i, [vp, i, ctypes.POINTER(cp), vp, vp, ctypes.POINTER(i)]),
         "hamstr_gpu_launches_per_step": (i, [vp]),
     }
@@ -225,6 +228,18 @@ class GpuSolver:
         ev, conv = ctypes.c_int(0), ctypes.c_int(0)
         _check(load().hamstr_gpu_march(self.h, nsteps, tol, _ptr(hist), ctypes.byref(ev), ctypes.byref(conv)))
         return hist[:ev.value], bool(conv.value)
+
+    def enqueue_steps(self, n: int) -> None:
+        _check(load().hamstr_gpu_enqueue_steps(self.h, n))
+
+    def sync(self) -> None:
+        _check(load().hamstr_gpu_sync(self.h))
+
+    def layout(self) -> dict:
+        v = np.zeros(8, dtype=np.int32)
+        _check(load().hamstr_gpu_layout(self.h, _ptr(v)))
+        return dict(zip(("nSlot", "nSten", "nRow", "nChain", "nWave", "nPeriodicChains",
+                         "nPeriodicRows", "maxRows"), (int(x) for x in v)))
 
     @property
     def stream(self) -> int:

@@ -112,6 +112,14 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
  * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
 
+/* Enqueues n pseudo-time steps on the handle's stream and returns without
+ * waiting (no tolerance stop, no host copies): for callers that keep the
+ * state on the GPU and synchronise themselves (timing, pipelines). */
+int hamstr_gpu_enqueue_steps(hamstr_gpu* g, int n);
+/* wait for the handle's stream; returns a pending device error, if any */
+int hamstr_gpu_sync(hamstr_gpu* g);
+/* layout[8]: nSlot nSten nRow nChain nWave nPeriodicChains nPeriodicRows maxRows */
+int hamstr_gpu_layout(hamstr_gpu* g, int* layout);
 /* the CUDA stream (cudaStream_t) the handle launches on */
 void* hamstr_gpu_stream(hamstr_gpu* g);
 /* Per-kernel CUDA-event timing of one step (eager launches on the handle's
