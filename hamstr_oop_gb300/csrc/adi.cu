@@ -133,26 +133,38 @@ __device__ __forceinline__ double assemble(const DeviceState& d, const int* __re
    return acc;
 }
 
-__global__ void __launch_bounds__(32) adi_factor_kernel(DeviceState d)
+// blocks A, B, C of every row, scaled by CFL/sigma with B += I
+// (ADI.cpp:197-217); one thread per entry, all rows at once
+__global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
 {
-   if (halted(d)) return;
-   const int ich = blockIdx.x;
-   const int lane = threadIdx.x, h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= 48 * d.nRow || halted(d)) return;
+   const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
+   double v = assemble(d, d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b, e);
+   v *= d.dtfac[d.row_scell[row]];
+   if (b == 1 && (e >> 2) == (e & 3)) v += 1.0;
+   d.blk[t] = v;
+}
+
+// block-Thomas factorisation of one chain by one warp (see file header)
+__device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int lane)
+{
+   const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
+   const double* blk = d.blk + 48 * (size_t)row0;
+   double A = blk[e], B = blk[16 + e], C = blk[32 + e];
    double P = 0.0;   // previous row's solved C' (h=0) or a' (h=1), element (k,j)
    for (int i = 0; i < N; i++) {
-      const int row = row0 + i;
-      const int* ops = d.row_ops + 3 * kOpsPerBlock * row;
-      const double dt = d.dtfac[d.row_scell[row]];
-      double A = assemble(d, ops, e);
-      double B = assemble(d, ops + kOpsPerBlock, e);
-      double C = assemble(d, ops + 2 * kOpsPerBlock, e);
-      A *= dt;
-      B *= dt;
-      C *= dt;
-      if (k == j) B += 1.0;
-      double* rec = d.fac + (size_t)kFac * row;
+      // next row's blocks are loaded while this row is factored
+      double An = 0.0, Bn = 0.0, Cn = 0.0;
+      if (i + 1 < N) {
+         const double* nb = blk + 48 * (size_t)(i + 1);
+         An = nb[e];
+         Bn = nb[16 + e];
+         Cn = nb[32 + e];
+      }
+      double* rec = d.fac + (size_t)kFac * (row0 + i);
       if (h == 0) rec[e] = A;
       // b(i) -= a(i) c'(i-1) and, periodic, a(i) = -a(i) a'(i-1)
       double acc = h ? 0.0 : B;
@@ -186,15 +198,19 @@ __global__ void __launch_bounds__(32) adi_factor_kernel(DeviceState d)
       if (last2 && h == 1) Yp = fromc;
       rec[32 + 16 * h + e] = Yp;
       P = Yp;
+      A = An;
+      B = Bn;
+      C = Cn;
    }
    if (!per) return;
    // last-row elimination (triSolvers.cpp:967-999)
    double cN = __shfl_sync(kFull, P, e);
    double bN = (k == j) ? 1.0 : 0.0;
+   double Y = (N > 1) ? d.fac[(size_t)kFac * row0 + 32 + 16 * h + e] : 0.0;
    for (int i = 0; i < N - 1; i++) {
       double* rec = d.fac + (size_t)kFac * (row0 + i);
+      const double Yn = (i + 2 < N) ? rec[kFac + 32 + 16 * h + e] : 0.0;
       if (h == 0) rec[64 + e] = cN;
-      const double Y = rec[32 + 16 * h + e];
       double acc = h ? bN : 0.0;
 #pragma unroll
       for (int l = 0; l < 4; l++) {
@@ -204,6 +220,7 @@ __global__ void __launch_bounds__(32) adi_factor_kernel(DeviceState d)
       }
       if (h) bN = acc;
       cN = __shfl_sync(kFull, acc, e);
+      Y = Yn;
    }
    double b[16];
 #pragma unroll
@@ -212,13 +229,24 @@ __global__ void __launch_bounds__(32) adi_factor_kernel(DeviceState d)
    if (h == 0) d.facN[16 * d.chain_facN[ich] + e] = lu_get(u, e);
 }
 
+// persistent warps, one per SM sub-partition, each with a job list
+__global__ void __launch_bounds__(128, 1) adi_factor_kernel(DeviceState d, int nwarps)
+{
+   if (halted(d)) return;
+   const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+   if (w >= nwarps) return;
+   const int g = d.sched_warp0[0] + w;
+   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++)
+      factor_chain(d, d.sched_jobs[job], threadIdx.x & 31);
+}
+
 // x_k -= sum_j M[k][j] * v[j] for the lane's component k = lane & 3, then
 // all four components gathered into every lane
-__device__ __forceinline__ void matvec_sub(const double* __restrict__ M, const double (&v)[4], double (&x)[4], int kk)
+__device__ __forceinline__ void matvec_sub(const double (&Mrow)[4], const double (&v)[4], double (&x)[4], int kk)
 {
    double t = sel4(x, kk);
 #pragma unroll
-   for (int jj = 0; jj < 4; jj++) t -= M[4 * kk + jj] * v[jj];
+   for (int jj = 0; jj < 4; jj++) t -= Mrow[jj] * v[jj];
 #pragma unroll
    for (int m = 0; m < 4; m++) x[m] = __shfl_sync(kFull, t, m);
 }
@@ -230,14 +258,34 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4]
    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
-__global__ void __launch_bounds__(32) adi_solve_kernel(DeviceState d, int wave_begin)
+__device__ __forceinline__ void ld16(const double* __restrict__ p, double (&v)[16])
 {
-   if (halted(d)) return;
-   const int ich = d.wave_chains[wave_begin + blockIdx.x];
-   const int lane = threadIdx.x, kk = lane & 3;
+#pragma unroll
+   for (int m = 0; m < 16; m += 2) {
+      const double2 a = *reinterpret_cast<const double2*>(p + m);
+      v[m] = a.x;
+      v[m + 1] = a.y;
+   }
+}
+
+__device__ __forceinline__ LU4 lu_from(const double (&v)[16])
+{
+   LU4 u;
+   u.b11 = v[0];  u.u12 = v[1];  u.u13 = v[2];  u.u14 = v[3];
+   u.b21 = v[4];  u.b22 = v[5];  u.u23 = v[6];  u.u24 = v[7];
+   u.b31 = v[8];  u.b32 = v[9];  u.b33 = v[10]; u.u34 = v[11];
+   u.b41 = v[12]; u.b42 = v[13]; u.b43 = v[14]; u.b44 = v[15];
+   return u;
+}
+
+// right-hand-side replay of one chain's solve with its stored factors
+__device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int lane)
+{
+   const int kk = lane & 3;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    double* fs = d.fsc + 4 * (size_t)row0;
+   const double* fac = d.fac + (size_t)kFac * row0;
    // right-hand side F = r[fcell] (ADI.cpp:116,187)
    for (int r = lane; r < N; r += 32) {
       const int fc = d.row_fcell[row0 + r];
@@ -247,70 +295,104 @@ __global__ void __launch_bounds__(32) adi_solve_kernel(DeviceState d, int wave_b
       *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
    }
    __syncwarp();
-   // forward sweep (triSolvers.cpp:778-822 / 859-933)
+   // forward sweep (triSolvers.cpp:778-822 / 859-933); row i+1 prefetched
    double xp[4] = {0.0, 0.0, 0.0, 0.0};
+   double x[4], arow[4] = {0.0, 0.0, 0.0, 0.0}, lu[16];
+   ld4(fs, x);
+   ld16(fac + 16, lu);
    for (int i = 0; i < N; i++) {
-      const double* rec = d.fac + (size_t)kFac * (row0 + i);
-      double x[4];
-      ld4(fs + 4 * i, x);
-      if (i > 0) matvec_sub(rec, xp, x, kk);
-      const LU4 u = lu_load(rec + 16);
+      double xn[4] = {0.0, 0.0, 0.0, 0.0}, an[4] = {0.0, 0.0, 0.0, 0.0}, lun[16];
+      if (i + 1 < N) {
+         const double* nr = fac + (size_t)kFac * (i + 1);
+         ld4(fs + 4 * (i + 1), xn);
+         ld4(nr + 4 * kk, an);
+         ld16(nr + 16, lun);
+      } else {
+#pragma unroll
+         for (int m = 0; m < 16; m++) lun[m] = 0.0;
+      }
+      if (i > 0) matvec_sub(arow, xp, x, kk);
+      const LU4 u = lu_from(lu);
       lu_solve(u, x[0], x[1], x[2], x[3]);
       if (lane < 4) fs[4 * i + lane] = sel4(x, lane);
 #pragma unroll
-      for (int m = 0; m < 4; m++) xp[m] = x[m];
+      for (int m = 0; m < 4; m++) { xp[m] = x[m]; x[m] = xn[m]; arow[m] = an[m]; }
+#pragma unroll
+      for (int m = 0; m < 16; m++) lu[m] = lun[m];
    }
    __syncwarp();
+   double xn[4];
    if (per) {
       // f(N-1) -= c_{N-1} f(i), then the last-row solve (triSolvers.cpp:991-1029)
       double fN[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) fN[m] = xp[m];
+      double fi[4], crow[4];
+      ld4(fs, fi);
+      ld4(fac + 64 + 4 * kk, crow);
       for (int i = 0; i < N - 1; i++) {
-         const double* rec = d.fac + (size_t)kFac * (row0 + i);
-         double fi[4];
-         ld4(fs + 4 * i, fi);
-         matvec_sub(rec + 64, fi, fN, kk);
+         double fin[4] = {0.0, 0.0, 0.0, 0.0}, cn[4] = {0.0, 0.0, 0.0, 0.0};
+         if (i + 2 < N) {
+            ld4(fs + 4 * (i + 1), fin);
+            ld4(fac + (size_t)kFac * (i + 1) + 64 + 4 * kk, cn);
+         }
+         matvec_sub(crow, fi, fN, kk);
+#pragma unroll
+         for (int m = 0; m < 4; m++) { fi[m] = fin[m]; crow[m] = cn[m]; }
       }
       const LU4 u = lu_load(d.facN + 16 * d.chain_facN[ich]);
       lu_solve(u, fN[0], fN[1], fN[2], fN[3]);
       __syncwarp();
       if (lane < 4) fs[4 * (N - 1) + lane] = sel4(fN, lane);
       // back substitution (triSolvers.cpp:1032-1045)
-      double xn[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) xn[m] = fN[m];
+      double xi[4], cr[4], ar[4];
+      if (N >= 2) {
+         ld4(fs + 4 * (N - 2), xi);
+         ld4(fac + (size_t)kFac * (N - 2) + 32 + 4 * kk, cr);
+         ld4(fac + (size_t)kFac * (N - 2) + 48 + 4 * kk, ar);
+      }
       for (int i = N - 2; i >= 0; i--) {
-         const double* rec = d.fac + (size_t)kFac * (row0 + i);
-         double x[4];
-         ld4(fs + 4 * i, x);
-         double t = sel4(x, kk);
+         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0}, arn[4] = {0.0, 0.0, 0.0, 0.0};
+         if (i > 0) {
+            ld4(fs + 4 * (i - 1), xin);
+            ld4(fac + (size_t)kFac * (i - 1) + 32 + 4 * kk, crn);
+            ld4(fac + (size_t)kFac * (i - 1) + 48 + 4 * kk, arn);
+         }
+         double t = sel4(xi, kk);
          if (i == N - 2) {
 #pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (rec[32 + 4 * kk + jj] * xn[jj]);
+            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj]);
          } else {
 #pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (rec[32 + 4 * kk + jj] * xn[jj] + rec[48 + 4 * kk + jj] * fN[jj]);
+            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj] + ar[jj] * fN[jj]);
          }
 #pragma unroll
-         for (int m = 0; m < 4; m++) x[m] = __shfl_sync(kFull, t, m);
-         if (lane < 4) fs[4 * i + lane] = sel4(x, lane);
+         for (int m = 0; m < 4; m++) xn[m] = __shfl_sync(kFull, t, m);
+         if (lane < 4) fs[4 * i + lane] = sel4(xn, lane);
 #pragma unroll
-         for (int m = 0; m < 4; m++) xn[m] = x[m];
+         for (int m = 0; m < 4; m++) { xi[m] = xin[m]; cr[m] = crn[m]; ar[m] = arn[m]; }
       }
    } else {
       // back substitution (triSolvers.cpp:839-846)
-      double xn[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) xn[m] = xp[m];
+      double xi[4], cr[4];
+      if (N >= 2) {
+         ld4(fs + 4 * (N - 2), xi);
+         ld4(fac + (size_t)kFac * (N - 2) + 32 + 4 * kk, cr);
+      }
       for (int i = N - 2; i >= 0; i--) {
-         const double* rec = d.fac + (size_t)kFac * (row0 + i);
-         double x[4];
-         ld4(fs + 4 * i, x);
-         matvec_sub(rec + 32, xn, x, kk);
-         if (lane < 4) fs[4 * i + lane] = sel4(x, lane);
+         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0};
+         if (i > 0) {
+            ld4(fs + 4 * (i - 1), xin);
+            ld4(fac + (size_t)kFac * (i - 1) + 32 + 4 * kk, crn);
+         }
+         matvec_sub(cr, xn, xi, kk);
+         if (lane < 4) fs[4 * i + lane] = sel4(xi, lane);
 #pragma unroll
-         for (int m = 0; m < 4; m++) xn[m] = x[m];
+         for (int m = 0; m < 4; m++) { xn[m] = xi[m]; xi[m] = xin[m]; cr[m] = crn[m]; }
       }
    }
    __syncwarp();
@@ -324,16 +406,49 @@ __global__ void __launch_bounds__(32) adi_solve_kernel(DeviceState d, int wave_b
    }
 }
 
-}  // namespace
-
-void launch_adi_factor(const DeviceState& d, cudaStream_t st)
+__global__ void __launch_bounds__(128, 1) adi_solve_kernel(DeviceState d, int wave, int nwarps)
 {
-   adi_factor_kernel<<<d.nChain, 32, 0, st>>>(d);
+   if (halted(d)) return;
+   const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+   if (w >= nwarps) return;
+   const int g = d.sched_warp0[1 + wave] + w;
+   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++)
+      solve_chain(d, d.sched_jobs[job], threadIdx.x & 31);
 }
 
-void launch_adi_solve(const DeviceState& d, int wave_begin, int wave_count, cudaStream_t st)
+}  // namespace
+
+// One block of 4 warps per SM: the dynamic shared-memory request below
+// exceeds half an SM's shared memory, so no two blocks share an SM and
+// each warp owns an SM sub-partition's FP64 unit.
+constexpr int kExclusiveSmem = 120 * 1024;
+
+int adi_configure(int max_dynamic_smem)
 {
-   if (wave_count > 0) adi_solve_kernel<<<wave_count, 32, 0, st>>>(d, wave_begin);
+   const int want = max_dynamic_smem >= kExclusiveSmem ? kExclusiveSmem : 0;
+   if (want) {
+      if (cudaFuncSetAttribute(adi_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess)
+         return 0;
+      if (cudaFuncSetAttribute(adi_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess)
+         return 0;
+   }
+   return want;
+}
+
+void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
+{
+   const int n = 48 * d.nRow;
+   adi_assemble_kernel<<<(n + 255) / 256, 256, 0, st>>>(d);
+}
+
+void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
+{
+   adi_factor_kernel<<<(nwarps + 3) / 4, 128, d.exclusive_smem, st>>>(d, nwarps);
+}
+
+void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st)
+{
+   if (nwarps > 0) adi_solve_kernel<<<(nwarps + 3) / 4, 128, d.exclusive_smem, st>>>(d, wave, nwarps);
 }
 
 }  // namespace hamstr

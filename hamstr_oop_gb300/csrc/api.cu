@@ -68,6 +68,7 @@ int upload(T** p, const std::vector<T>& v, std::vector<void*>& owned)
 struct hamstr_gpu {
    DeviceState d{};
    Plan plan;
+   Schedule sched;
    int msweep = 1;
    cudaStream_t stream = nullptr;
    std::vector<void*> owned;
@@ -83,10 +84,11 @@ struct hamstr_gpu {
       launch_rhs_face(d, true, stream); n++;
       launch_rhs_cell(d, true, stream); n++;
       launch_norm_final(d, 0, check_tol, stream); n++;
-      launch_adi_factor(d, stream); n++;
+      launch_adi_assemble(d, stream); n++;
+      launch_adi_factor(d, sched.nwarps[0], stream); n++;
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++) {
-            launch_adi_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
+            launch_adi_solve(d, w, sched.nwarps[1 + w], stream);
             n++;
          }
          launch_dq_update(d, stream); n++;
@@ -272,6 +274,19 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    TRY(upload(&d.row_ops, P.row_ops, o));
    TRY(upload(&d.cell_written, cell_written, o));
    TRY(upload(&d.chain_facN, chain_facN, o));
+   {
+      int dev = 0, nsm = 0, optin = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
+      if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 0;
+      d.exclusive_smem = adi_configure(optin);
+      g->sched = build_schedule(P, 4 * nsm);
+   }
+   TRY(upload(&d.sched_warp0, g->sched.warp0, o));
+   TRY(upload(&d.sched_nwarps, g->sched.nwarps, o));
+   TRY(upload(&d.sched_warp_ptr, g->sched.warp_ptr, o));
+   TRY(upload(&d.sched_jobs, g->sched.jobs, o));
+   TRY(dalloc(&d.blk, 48 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fac, 80 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fsc, 4 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.facN, 16 * (size_t)std::max(nper, 1), o));
@@ -432,10 +447,10 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    if (st) return st;
    const DeviceState& d = g->d;
    launch_adi_init(d, g->stream);
-   launch_adi_factor(d, g->stream);
+   launch_adi_assemble(d, g->stream);
+   launch_adi_factor(d, g->sched.nwarps[0], g->stream);
    for (int s = 0; s < g->msweep; s++) {
-      for (int w = 0; w < g->plan.nWave; w++)
-         launch_adi_solve(d, g->plan.wave_ptr[w], g->plan.wave_ptr[w + 1] - g->plan.wave_ptr[w], g->stream);
+      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, w, g->sched.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
       launch_lin_face(d, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);
@@ -546,8 +561,8 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
    // eager launches of one step with events around each kernel class
    if (!g || reps < 1 || !names || !ms || !launches || !n) return HAMSTR_GPU_ERR_ARG;
    static const char* kNames[] = {"rhs_face", "rhs_cell", "norm_final", "adi_factor", "adi_solve",
-                                  "dq_update", "lin_face", "lin_cell", "step_end"};
-   const int K = 9;
+                                  "dq_update", "lin_face", "lin_cell", "step_end", "adi_assemble"};
+   const int K = 10;
    std::vector<double> acc(K, 0.0);
    std::vector<int> cnt(K, 0);
    cudaEvent_t a, b;
@@ -571,13 +586,11 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
       if ((st = timed(0, [&] { launch_rhs_face(d, true, g->stream); }))) return st;
       if ((st = timed(1, [&] { launch_rhs_cell(d, true, g->stream); }))) return st;
       if ((st = timed(2, [&] { launch_norm_final(d, 0, false, g->stream); }))) return st;
-      if ((st = timed(3, [&] { launch_adi_factor(d, g->stream); }))) return st;
+      if ((st = timed(9, [&] { launch_adi_assemble(d, g->stream); }))) return st;
+      if ((st = timed(3, [&] { launch_adi_factor(d, g->sched.nwarps[0], g->stream); }))) return st;
       for (int s = 0; s < g->msweep; s++) {
          for (int w = 0; w < g->plan.nWave; w++)
-            if ((st = timed(4, [&] {
-                    launch_adi_solve(d, g->plan.wave_ptr[w], g->plan.wave_ptr[w + 1] - g->plan.wave_ptr[w], g->stream);
-                 })))
-               return st;
+            if ((st = timed(4, [&] { launch_adi_solve(d, w, g->sched.nwarps[1 + w], g->stream); }))) return st;
          if ((st = timed(5, [&] { launch_dq_update(d, g->stream); }))) return st;
          if ((st = timed(6, [&] { launch_lin_face(d, g->stream); }))) return st;
          if ((st = timed(7, [&] { launch_lin_cell(d, s == g->msweep - 1, g->stream); }))) return st;

@@ -49,6 +49,8 @@ struct DeviceState {
    int *wave_chains;
    int *row_scell, *row_fcell, *row_ops;
    int *cell_written;
+   double* blk;            // per-row assembled blocks A, B, C (scaled, B + I) [nRow][48]
+   int *sched_warp0, *sched_nwarps, *sched_warp_ptr, *sched_jobs;   // persistent-warp job lists
    double* fac;            // per-row factor storage
    double* fsc;            // per-row right-hand side / solution scratch [nRow][4]
    double* facN;           // per periodic chain: final LU of the last row (16)
@@ -61,6 +63,7 @@ struct DeviceState {
    int hist_cap;
    double* tol;            // [0] march stop tolerance on the computeRHS L2 norm (<= 0: off)
    int norm_blocks;
+   int exclusive_smem;     // dynamic shared memory that keeps ADI blocks one per SM
 };
 
 // true once a march has met its tolerance: every later kernel of the step
@@ -80,8 +83,10 @@ void launch_dtfac(const DeviceState& d, cudaStream_t st);
 void launch_adi_init(const DeviceState& d, cudaStream_t st);
 void launch_dq_update(const DeviceState& d, cudaStream_t st);
 // launchers (adi.cu)
-void launch_adi_factor(const DeviceState& d, cudaStream_t st);
-void launch_adi_solve(const DeviceState& d, int wave_begin, int wave_count, cudaStream_t st);
+void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
+void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
+void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
+int adi_configure(int max_dynamic_smem);
 
 }  // namespace hamstr
 #endif

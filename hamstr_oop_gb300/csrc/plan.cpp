@@ -240,4 +240,39 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
+Schedule build_schedule(const Plan& p, int max_warps)
+{
+   Schedule S;
+   S.warp_ptr.push_back(0);
+   auto assign = [&](const std::vector<int>& chains) {
+      const int W = std::max(1, std::min((int)chains.size(), max_warps));
+      // cost model: rows of FP64 recurrence, periodic rows carry the
+      // fill-in column and the last-row elimination
+      std::vector<std::pair<double, int>> order;
+      for (int c : chains) order.push_back({p.chain_nrows[c] * (p.chain_periodic[c] ? 1.3 : 1.0), c});
+      std::stable_sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+      std::vector<double> load(W, 0.0);
+      std::vector<std::vector<int>> lists(W);
+      for (const auto& oc : order) {
+         const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+         load[w] += oc.first;
+         lists[w].push_back(oc.second);
+      }
+      S.warp0.push_back((int)S.warp_ptr.size() - 1);
+      S.nwarps.push_back(W);
+      for (int w = 0; w < W; w++) {
+         for (int c : lists[w]) S.jobs.push_back(c);
+         S.warp_ptr.push_back((int)S.jobs.size());
+      }
+   };
+   std::vector<int> all(p.nChain);
+   for (int c = 0; c < p.nChain; c++) all[c] = c;
+   assign(all);
+   for (int w = 0; w < p.nWave; w++) {
+      std::vector<int> cs(p.wave_chains.begin() + p.wave_ptr[w], p.wave_chains.begin() + p.wave_ptr[w + 1]);
+      assign(cs);
+   }
+   return S;
+}
+
 }  // namespace hamstr

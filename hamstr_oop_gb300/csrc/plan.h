@@ -61,5 +61,16 @@ struct Plan {
 // Builds the plan; returns "" on success or a description of the problem.
 std::string build_plan(const MeshInput& in, Plan& out);
 
+// Longest-chain-first assignment of chains to persistent warps, one warp
+// per SM sub-partition: schedule 0 is the factorisation (all chains),
+// schedule 1+v the solve of wave v.  Warp w of schedule s owns
+// jobs[warp_ptr[warp0[s] + w] .. warp_ptr[warp0[s] + w + 1]).
+struct Schedule {
+   std::vector<int> warp0, nwarps;   // per schedule
+   std::vector<int> warp_ptr;        // per global warp, +1
+   std::vector<int> jobs;            // chain ids
+};
+Schedule build_schedule(const Plan& p, int max_warps);
+
 }  // namespace hamstr
 #endif
