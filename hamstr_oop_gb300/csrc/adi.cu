@@ -28,83 +28,12 @@
 // ##################################################################
 #include "device_state.h"
 #include "plan.h"
+#include "line_solve.cuh"
 
 namespace hamstr {
 
 namespace {
 
-constexpr int kFac = 80;
-constexpr unsigned kFull = 0xffffffffu;
-
-struct LU4 {
-   double b11, u12, u13, u14, b21, b22, u23, u24, b31, b32, b33, u34, b41, b42, b43, b44;
-};
-
-// unpivoted LU with reciprocal pivots (triSolvers.cpp:796-811)
-__device__ __forceinline__ LU4 lu_factor(const double (&b)[16])
-{
-   LU4 u;
-   u.b11 = 1. / b[0];
-   u.u12 = b[1] * u.b11;
-   u.u13 = b[2] * u.b11;
-   u.u14 = b[3] * u.b11;
-   u.b21 = b[4];
-   u.b22 = 1. / (b[5] - u.b21 * u.u12);
-   u.u23 = (b[6] - u.b21 * u.u13) * u.b22;
-   u.u24 = (b[7] - u.b21 * u.u14) * u.b22;
-   u.b31 = b[8];
-   u.b32 = b[9] - u.b31 * u.u12;
-   u.b33 = 1. / (b[10] - u.b31 * u.u13 - u.b32 * u.u23);
-   u.u34 = (b[11] - u.b31 * u.u14 - u.b32 * u.u24) * u.b33;
-   u.b41 = b[12];
-   u.b42 = b[13] - u.b41 * u.u12;
-   u.b43 = b[14] - u.b41 * u.u13 - u.b42 * u.u23;
-   u.b44 = 1. / (b[15] - u.b41 * u.u14 - u.b42 * u.u24 - u.b43 * u.u34);
-   return u;
-}
-
-// x <- LU^{-1} x (triSolvers.cpp:813-821)
-__device__ __forceinline__ void lu_solve(const LU4& u, double& x0, double& x1, double& x2, double& x3)
-{
-   const double d1 = x0 * u.b11;
-   const double d2 = (x1 - u.b21 * d1) * u.b22;
-   const double d3 = (x2 - u.b31 * d1 - u.b32 * d2) * u.b33;
-   const double d4 = (x3 - u.b41 * d1 - u.b42 * d2 - u.b43 * d3) * u.b44;
-   x3 = d4;
-   x2 = d3 - u.u34 * x3;
-   x1 = d2 - u.u23 * x2 - u.u24 * x3;
-   x0 = d1 - u.u12 * x1 - u.u13 * x2 - u.u14 * x3;
-}
-
-__device__ __forceinline__ double lu_get(const LU4& u, int e)
-{
-   double v = u.b11;
-   v = (e == 1) ? u.u12 : v;  v = (e == 2) ? u.u13 : v;  v = (e == 3) ? u.u14 : v;
-   v = (e == 4) ? u.b21 : v;  v = (e == 5) ? u.b22 : v;  v = (e == 6) ? u.u23 : v;
-   v = (e == 7) ? u.u24 : v;  v = (e == 8) ? u.b31 : v;  v = (e == 9) ? u.b32 : v;
-   v = (e == 10) ? u.b33 : v; v = (e == 11) ? u.u34 : v; v = (e == 12) ? u.b41 : v;
-   v = (e == 13) ? u.b42 : v; v = (e == 14) ? u.b43 : v; v = (e == 15) ? u.b44 : v;
-   return v;
-}
-
-__device__ __forceinline__ LU4 lu_load(const double* __restrict__ p)
-{
-   LU4 u;
-   u.b11 = p[0];  u.u12 = p[1];  u.u13 = p[2];  u.u14 = p[3];
-   u.b21 = p[4];  u.b22 = p[5];  u.u23 = p[6];  u.u24 = p[7];
-   u.b31 = p[8];  u.b32 = p[9];  u.b33 = p[10]; u.u34 = p[11];
-   u.b41 = p[12]; u.b42 = p[13]; u.b43 = p[14]; u.b44 = p[15];
-   return u;
-}
-
-__device__ __forceinline__ double sel4(const double (&x)[4], int k)
-{
-   double v = x[0];
-   v = (k == 1) ? x[1] : v;
-   v = (k == 2) ? x[2] : v;
-   v = (k == 3) ? x[3] : v;
-   return v;
-}
 
 // one block entry (row-major element e) in the reference's term order
 // (ADI.cpp:103-188): 0.0, then += / -= the listed face-matrix entries
@@ -146,87 +75,14 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
    d.blk[t] = v;
 }
 
-// block-Thomas factorisation of one chain by one warp (see file header)
+// block-Thomas factorisation of chain ich (its assembled rows in blk)
 __device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int lane)
 {
-   const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const double* blk = d.blk + 48 * (size_t)row0;
-   double A = blk[e], B = blk[16 + e], C = blk[32 + e];
-   double P = 0.0;   // previous row's solved C' (h=0) or a' (h=1), element (k,j)
-   for (int i = 0; i < N; i++) {
-      // next row's blocks are loaded while this row is factored
-      double An = 0.0, Bn = 0.0, Cn = 0.0;
-      if (i + 1 < N) {
-         const double* nb = blk + 48 * (size_t)(i + 1);
-         An = nb[e];
-         Bn = nb[16 + e];
-         Cn = nb[32 + e];
-      }
-      double* rec = d.fac + (size_t)kFac * (row0 + i);
-      if (h == 0) rec[e] = A;
-      // b(i) -= a(i) c'(i-1) and, periodic, a(i) = -a(i) a'(i-1)
-      double acc = h ? 0.0 : B;
-      if (i > 0) {
-#pragma unroll
-         for (int l = 0; l < 4; l++) {
-            const double a = __shfl_sync(kFull, A, 16 * h + 4 * k + l);
-            const double x = __shfl_sync(kFull, P, 16 * h + 4 * l + j);
-            acc -= a * x;
-         }
-      } else if (h) {
-         acc = A;
-      }
-      double b[16];
-#pragma unroll
-      for (int m = 0; m < 16; m++) b[m] = __shfl_sync(kFull, acc, m);
-      const LU4 u = lu_factor(b);
-      if (h == 0) rec[16 + e] = lu_get(u, e);
-      // c'(i) = B'^{-1} c(i), a'(i) = B'^{-1} a(i); at i == N-2 of a
-      // periodic chain c(i) += a(i) first and a'(i) = c'(i)
-      const bool last2 = per && (i == N - 2);
-      double Y = h ? acc : C;
-      const double fillv = __shfl_sync(kFull, acc, 16 + e);
-      if (last2 && h == 0) Y = C + fillv;
-      double y[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) y[r] = __shfl_sync(kFull, Y, 16 * h + 4 * r + j);
-      lu_solve(u, y[0], y[1], y[2], y[3]);
-      double Yp = sel4(y, k);
-      const double fromc = __shfl_sync(kFull, Yp, e);
-      if (last2 && h == 1) Yp = fromc;
-      rec[32 + 16 * h + e] = Yp;
-      P = Yp;
-      A = An;
-      B = Bn;
-      C = Cn;
-   }
-   if (!per) return;
-   // last-row elimination (triSolvers.cpp:967-999)
-   double cN = __shfl_sync(kFull, P, e);
-   double bN = (k == j) ? 1.0 : 0.0;
-   double Y = (N > 1) ? d.fac[(size_t)kFac * row0 + 32 + 16 * h + e] : 0.0;
-   for (int i = 0; i < N - 1; i++) {
-      double* rec = d.fac + (size_t)kFac * (row0 + i);
-      const double Yn = (i + 2 < N) ? rec[kFac + 32 + 16 * h + e] : 0.0;
-      if (h == 0) rec[64 + e] = cN;
-      double acc = h ? bN : 0.0;
-#pragma unroll
-      for (int l = 0; l < 4; l++) {
-         const double c = __shfl_sync(kFull, cN, 16 * h + 4 * k + l);
-         const double y = __shfl_sync(kFull, Y, 16 * h + 4 * l + j);
-         acc -= c * y;
-      }
-      if (h) bN = acc;
-      cN = __shfl_sync(kFull, acc, e);
-      Y = Yn;
-   }
-   double b[16];
-#pragma unroll
-   for (int m = 0; m < 16; m++) b[m] = __shfl_sync(kFull, bN, 16 + m);
-   const LU4 u = lu_factor(b);
-   if (h == 0) d.facN[16 * d.chain_facN[ich] + e] = lu_get(u, e);
+   factor_line(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
+               per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane);
 }
 
 // persistent warps, one per SM sub-partition, each with a job list
@@ -240,53 +96,13 @@ __global__ void __launch_bounds__(128, 1) adi_factor_kernel(DeviceState d, int n
       factor_chain(d, d.sched_jobs[job], threadIdx.x & 31);
 }
 
-// x_k -= sum_j M[k][j] * v[j] for the lane's component k = lane & 3, then
-// all four components gathered into every lane
-__device__ __forceinline__ void matvec_sub(const double (&Mrow)[4], const double (&v)[4], double (&x)[4], int kk)
-{
-   double t = sel4(x, kk);
-#pragma unroll
-   for (int jj = 0; jj < 4; jj++) t -= Mrow[jj] * v[jj];
-#pragma unroll
-   for (int m = 0; m < 4; m++) x[m] = __shfl_sync(kFull, t, m);
-}
-
-__device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
-{
-   const double2 a = *reinterpret_cast<const double2*>(p);
-   const double2 b = *reinterpret_cast<const double2*>(p + 2);
-   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-}
-
-__device__ __forceinline__ void ld16(const double* __restrict__ p, double (&v)[16])
-{
-#pragma unroll
-   for (int m = 0; m < 16; m += 2) {
-      const double2 a = *reinterpret_cast<const double2*>(p + m);
-      v[m] = a.x;
-      v[m + 1] = a.y;
-   }
-}
-
-__device__ __forceinline__ LU4 lu_from(const double (&v)[16])
-{
-   LU4 u;
-   u.b11 = v[0];  u.u12 = v[1];  u.u13 = v[2];  u.u14 = v[3];
-   u.b21 = v[4];  u.b22 = v[5];  u.u23 = v[6];  u.u24 = v[7];
-   u.b31 = v[8];  u.b32 = v[9];  u.b33 = v[10]; u.u34 = v[11];
-   u.b41 = v[12]; u.b42 = v[13]; u.b43 = v[14]; u.b44 = v[15];
-   return u;
-}
-
-// right-hand-side replay of one chain's solve with its stored factors
+// one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the
+// replay, and the write-back r[scell] = F (ADI.cpp:232-244)
 __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int lane)
 {
-   const int kk = lane & 3;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    double* fs = d.fsc + 4 * (size_t)row0;
-   const double* fac = d.fac + (size_t)kFac * row0;
-   // right-hand side F = r[fcell] (ADI.cpp:116,187)
    for (int r = lane; r < N; r += 32) {
       const int fc = d.row_fcell[row0 + r];
       double v[4] = {0.0, 0.0, 0.0, 0.0};
@@ -295,108 +111,8 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
       *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
    }
    __syncwarp();
-   // forward sweep (triSolvers.cpp:778-822 / 859-933); row i+1 prefetched
-   double xp[4] = {0.0, 0.0, 0.0, 0.0};
-   double x[4], arow[4] = {0.0, 0.0, 0.0, 0.0}, lu[16];
-   ld4(fs, x);
-   ld16(fac + 16, lu);
-   for (int i = 0; i < N; i++) {
-      double xn[4] = {0.0, 0.0, 0.0, 0.0}, an[4] = {0.0, 0.0, 0.0, 0.0}, lun[16];
-      if (i + 1 < N) {
-         const double* nr = fac + (size_t)kFac * (i + 1);
-         ld4(fs + 4 * (i + 1), xn);
-         ld4(nr + 4 * kk, an);
-         ld16(nr + 16, lun);
-      } else {
-#pragma unroll
-         for (int m = 0; m < 16; m++) lun[m] = 0.0;
-      }
-      if (i > 0) matvec_sub(arow, xp, x, kk);
-      const LU4 u = lu_from(lu);
-      lu_solve(u, x[0], x[1], x[2], x[3]);
-      if (lane < 4) fs[4 * i + lane] = sel4(x, lane);
-#pragma unroll
-      for (int m = 0; m < 4; m++) { xp[m] = x[m]; x[m] = xn[m]; arow[m] = an[m]; }
-#pragma unroll
-      for (int m = 0; m < 16; m++) lu[m] = lun[m];
-   }
+   solve_line(d.fac + (size_t)kFacRec * row0, per ? d.facN + 16 * d.chain_facN[ich] : nullptr, N, per, fs, lane);
    __syncwarp();
-   double xn[4];
-   if (per) {
-      // f(N-1) -= c_{N-1} f(i), then the last-row solve (triSolvers.cpp:991-1029)
-      double fN[4];
-#pragma unroll
-      for (int m = 0; m < 4; m++) fN[m] = xp[m];
-      double fi[4], crow[4];
-      ld4(fs, fi);
-      ld4(fac + 64 + 4 * kk, crow);
-      for (int i = 0; i < N - 1; i++) {
-         double fin[4] = {0.0, 0.0, 0.0, 0.0}, cn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i + 2 < N) {
-            ld4(fs + 4 * (i + 1), fin);
-            ld4(fac + (size_t)kFac * (i + 1) + 64 + 4 * kk, cn);
-         }
-         matvec_sub(crow, fi, fN, kk);
-#pragma unroll
-         for (int m = 0; m < 4; m++) { fi[m] = fin[m]; crow[m] = cn[m]; }
-      }
-      const LU4 u = lu_load(d.facN + 16 * d.chain_facN[ich]);
-      lu_solve(u, fN[0], fN[1], fN[2], fN[3]);
-      __syncwarp();
-      if (lane < 4) fs[4 * (N - 1) + lane] = sel4(fN, lane);
-      // back substitution (triSolvers.cpp:1032-1045)
-#pragma unroll
-      for (int m = 0; m < 4; m++) xn[m] = fN[m];
-      double xi[4], cr[4], ar[4];
-      if (N >= 2) {
-         ld4(fs + 4 * (N - 2), xi);
-         ld4(fac + (size_t)kFac * (N - 2) + 32 + 4 * kk, cr);
-         ld4(fac + (size_t)kFac * (N - 2) + 48 + 4 * kk, ar);
-      }
-      for (int i = N - 2; i >= 0; i--) {
-         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0}, arn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i > 0) {
-            ld4(fs + 4 * (i - 1), xin);
-            ld4(fac + (size_t)kFac * (i - 1) + 32 + 4 * kk, crn);
-            ld4(fac + (size_t)kFac * (i - 1) + 48 + 4 * kk, arn);
-         }
-         double t = sel4(xi, kk);
-         if (i == N - 2) {
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj]);
-         } else {
-#pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj] + ar[jj] * fN[jj]);
-         }
-#pragma unroll
-         for (int m = 0; m < 4; m++) xn[m] = __shfl_sync(kFull, t, m);
-         if (lane < 4) fs[4 * i + lane] = sel4(xn, lane);
-#pragma unroll
-         for (int m = 0; m < 4; m++) { xi[m] = xin[m]; cr[m] = crn[m]; ar[m] = arn[m]; }
-      }
-   } else {
-      // back substitution (triSolvers.cpp:839-846)
-#pragma unroll
-      for (int m = 0; m < 4; m++) xn[m] = xp[m];
-      double xi[4], cr[4];
-      if (N >= 2) {
-         ld4(fs + 4 * (N - 2), xi);
-         ld4(fac + (size_t)kFac * (N - 2) + 32 + 4 * kk, cr);
-      }
-      for (int i = N - 2; i >= 0; i--) {
-         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i > 0) {
-            ld4(fs + 4 * (i - 1), xin);
-            ld4(fac + (size_t)kFac * (i - 1) + 32 + 4 * kk, crn);
-         }
-         matvec_sub(cr, xn, xi, kk);
-         if (lane < 4) fs[4 * i + lane] = sel4(xi, lane);
-#pragma unroll
-         for (int m = 0; m < 4; m++) { xn[m] = xi[m]; xi[m] = xin[m]; cr[m] = crn[m]; }
-      }
-   }
-   __syncwarp();
-   // scatter back (ADI.cpp:232-244)
    for (int r = lane; r < N; r += 32) {
       const int sc = d.row_scell[row0 + r];
       double v[4];

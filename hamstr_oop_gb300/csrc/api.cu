@@ -31,6 +31,14 @@ thread_local std::string g_last_error;
 
 void set_error(const std::string& m) { g_last_error = m; }
 
+}  // namespace
+
+namespace hamstr {
+void set_last_error(const std::string& m) { set_error(m); }
+}  // namespace hamstr
+
+namespace {
+
 #define CK(call)                                                                        \
    do {                                                                                 \
       cudaError_t e_ = (call);                                                          \

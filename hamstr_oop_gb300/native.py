@@ -78,6 +78,7 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_layout": (i, [vp, vp]),
         "hamstr_gpu_profile_step": (i, [vp, i, ctypes.POINTER(cp), vp, vp, ctypes.POINTER(i)]),
         "hamstr_gpu_launches_per_step": (i, [vp]),
+        "hamstr_gpu_block_tridag4": (i, [i, i, i, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -92,6 +93,18 @@ def declared_symbols() -> list:
     txt = open(HEADER).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(hamstr_[a-z_0-9]+)\s*\(", txt)))
+
+
+def block_tridag4(A, B, C, F, periodic: bool, stream: int = 0):
+    """Batched block-tridiagonal solve on device memory (torch CUDA tensors).
+
+    A, B, C: (nlines, N, 4, 4) float64; F: (nlines, N, 4) float64, solved in place."""
+    nl, n = int(F.shape[0]), int(F.shape[1])
+    for t in (A, B, C, F):
+        if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float64"):
+            raise ValueError("block_tridag4 needs contiguous float64 CUDA tensors")
+    _check(load().hamstr_gpu_block_tridag4(nl, n, int(periodic), A.data_ptr(), B.data_ptr(), C.data_ptr(),
+                                           F.data_ptr(), stream or None))
 
 
 def _ptr(a: np.ndarray):

@@ -112,6 +112,21 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
  * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
 
+/* TRISOLVER::blockTridag4 (triSolvers.cpp:769-847) and blockTridagPeriodic4
+ * (triSolvers.cpp:850-1046), batched over nlines independent lines of N
+ * block rows, on DEVICE arrays:
+ *   A, B, C  [nlines][N][4][4] row-major blocks (read only; the reference
+ *            overwrites b and c as scratch)
+ *   F        [nlines][N][4] right-hand sides, overwritten with the solution
+ *            as the reference's f is
+ * periodic = 1 selects the cyclic solver (A_0 couples row 0 to row N-1 and
+ * C_{N-1} row N-1 to row 0; needs N >= 2); 0 the open one (A_0, C_{N-1}
+ * unused).  stream is a cudaStream_t or NULL.  Scratch of (80 N + 16)
+ * doubles per line is allocated and freed inside the call, which
+ * synchronises the stream. */
+int hamstr_gpu_block_tridag4(int nlines, int N, int periodic, const double* A, const double* B,
+                             const double* C, double* F, void* stream);
+
 /* Enqueues n pseudo-time steps on the handle's stream and returns without
  * waiting (no tolerance stop, no host copies): for callers that keep the
  * state on the GPU and synchronise themselves (timing, pipelines). */

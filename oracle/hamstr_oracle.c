@@ -955,6 +955,14 @@ static void block_tridag_periodic4(double (*a)[NQ][NQ], double (*b)[NQ][NQ], dou
          for (j = 0; j < NQ; j++) f[i][k] -= (c[i][k][j] * f[i + 1][j] + a[i][k][j] * f[N - 1][j]);
 }
 
+int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic)
+{
+   if (N < 1 || (periodic && N < 2)) return -1;
+   if (periodic) block_tridag_periodic4((double(*)[NQ][NQ])a, (double(*)[NQ][NQ])b, (double(*)[NQ][NQ])c, (double(*)[NQ])f, N);
+   else block_tridag4((double(*)[NQ][NQ])a, (double(*)[NQ][NQ])b, (double(*)[NQ][NQ])c, (double(*)[NQ])f, N);
+   return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* ADI (ADI.cpp:15-266)                                                */
 /* ------------------------------------------------------------------ */

@@ -28,7 +28,7 @@ extern "C" {
 
 typedef struct ho_case ho_case;
 
-/* Reads <case_dir>/input.hamstr and <case_dir>/input/domain000/*.dat,
+/* Reads <case_dir>/input.hamstr and the files under <case_dir>/input/domain000/,
  * preprocesses and initialises to freestream.  NULL on failure, with a
  * message in err. */
 ho_case* ho_open(const char* case_dir, char* err, int errlen);
@@ -52,6 +52,10 @@ int  ho_march(ho_case* c, int n, double* hist);
 /* Runs `iters` steps on each of n independent cases, one host thread per
  * case (OpenMP); the CPU-baseline throughput leg. */
 int  ho_march_replicas(ho_case** cases, int n, int iters);
+
+/* triSolvers.cpp blockTridag4 / blockTridagPeriodic4 on flat [N][4][4]
+ * blocks and [N][4] right-hand sides, in place like the reference. */
+int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic);
 
 /* Named arrays: q r r0 dq sigma ff x vol normVec refMtx (doubles) and
  * faces chainConn faceStartPerChain c2chain bFaces chainsPerColor (ints). */

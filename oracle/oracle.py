@@ -197,6 +197,18 @@ class OracleCase:
         return out
 
 
+def block_tridag4(a, b, c, f, periodic: bool, kind: str = "port"):
+    """In-place 4x4 block-tridiagonal solve of one line (copies are made)."""
+    lib, p = _lib(kind)
+    fn = getattr(lib, p + "block_tridag4")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int]
+    a, b, c, f = (np.array(x, dtype=np.float64, order="C", copy=True) for x in (a, b, c, f))
+    if fn(_ptr(a), _ptr(b), _ptr(c), _ptr(f), int(f.shape[0]), int(periodic)) != 0:
+        raise ValueError("bad block_tridag4 arguments")
+    return f
+
+
 def march_replicas(cases, iters: int) -> None:
     """Run ``iters`` steps on each port case, one OpenMP thread per case."""
     lib, _ = _lib("port")

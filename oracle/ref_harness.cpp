@@ -33,6 +33,7 @@
 #include <limits.h>
 
 #include "hamstr.h"
+#include "triSolvers.h"
 
 // ------------------------------------------------------------------
 // bump arena for the per-call leaks
@@ -264,6 +265,30 @@ int ref_get_int(void* h, const char* name, int* out)
    }
    if (!strcmp(name, "chainsPerColor")) { memcpy(out, m->chainsPerColor, sizeof(int) * m->nColor); return 0; }
    return -1;
+}
+
+// TRISOLVER::blockTridag4 / blockTridagPeriodic4 on flat [N][4][4] blocks
+int ref_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic)
+{
+   if (N < 1 || (periodic && N < 2)) return -1;
+   double*** A = new double**[N];
+   double*** B = new double**[N];
+   double*** C = new double**[N];
+   double** F = new double*[N];
+   for (int i = 0; i < N; i++) {
+      A[i] = new double*[NQ]; B[i] = new double*[NQ]; C[i] = new double*[NQ];
+      F[i] = f + NQ * i;
+      for (int k = 0; k < NQ; k++) {
+         A[i][k] = a + NQ * NQ * i + NQ * k;
+         B[i][k] = b + NQ * NQ * i + NQ * k;
+         C[i][k] = c + NQ * NQ * i + NQ * k;
+      }
+   }
+   if (periodic) TRISOLVER::blockTridagPeriodic4(A, B, C, F, N, NQ);
+   else TRISOLVER::blockTridag4(A, B, C, F, N, NQ);
+   for (int i = 0; i < N; i++) { delete[] A[i]; delete[] B[i]; delete[] C[i]; }
+   delete[] A; delete[] B; delete[] C; delete[] F;
+   return 0;
 }
 
 } // extern "C"
