@@ -9,6 +9,7 @@
 // ##################################################################
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 
 #include "../../include/hamstr_gpu.h"
@@ -92,4 +93,74 @@ extern "C" int hamstr_gpu_block_tridag4(int nlines, int N, int periodic, const d
       return HAMSTR_GPU_ERR_CUDA;
    }
    return HAMSTR_GPU_OK;
+}
+
+// ------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some callers cannot allocate device memory on every call: code that runs
+// in a loop beside work on other streams (cudaFree waits for the whole
+// device, so the allocating entry point above stalls everything), and
+// hosts whose device memory is owned by their own pool allocator with a
+// fixed budget.  This variant runs the same kernel with its scratch in a
+// fixed array that the library image places in device memory when it is
+// loaded: every GPU that loads the library holds these 8 MiB until the
+// process exits, and the call itself allocates nothing.
+// ------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchDoubles = size_t(1) << 20;   // 8 MiB
+static __device__ __align__(256) double g_tridag_scratch[kNoAllocScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_tridag_scratch on the current device, looked up once
+// per device (host code only sees a host-side stand-in for the symbol).
+int noalloc_scratch(double** out)
+{
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess) {
+      set_last_error(std::string("block_tridag4_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+      return HAMSTR_GPU_ERR_CUDA;
+   }
+   if (dev < 0 || dev >= kMaxDevices) {
+      set_last_error("block_tridag4_noalloc: device ordinal beyond 63");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   std::lock_guard<std::mutex> lock(g_scratch_mutex);
+   if (!g_scratch_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_tridag_scratch);
+      if (e != cudaSuccess || !p) {
+         set_last_error(std::string("block_tridag4_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+         return HAMSTR_GPU_ERR_CUDA;
+      }
+      g_scratch_addr[dev] = static_cast<double*>(p);
+   }
+   *out = g_scratch_addr[dev];
+   return HAMSTR_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" int hamstr_gpu_block_tridag4_noalloc(int nlines, int N, int periodic, const double* A, const double* B,
+                                                const double* C, double* F, void* stream)
+{
+   int st = block_tridag_check(nlines, N, periodic, A, B, C, F);
+   if (st || nlines == 0) return st;
+   const size_t need = (size_t)nlines * ((size_t)kFacRec * N + 16);
+   if (need > kNoAllocScratchDoubles) {
+      set_last_error("block_tridag4_noalloc: nlines*(80*N+16) = " + std::to_string(need) +
+                     " doubles exceeds the fixed scratch of " + std::to_string(kNoAllocScratchDoubles));
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   double* scratch = nullptr;
+   st = noalloc_scratch(&scratch);
+   if (st) return st;
+   // every scratch value the kernel reads it has written earlier in the same
+   // launch, so nothing needs clearing between calls
+   return block_tridag_launch(nlines, N, periodic, A, B, C, F, scratch, (cudaStream_t)stream);
 }

@@ -79,6 +79,7 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_profile_step": (i, [vp, i, ctypes.POINTER(cp), vp, vp, ctypes.POINTER(i)]),
         "hamstr_gpu_launches_per_step": (i, [vp]),
         "hamstr_gpu_block_tridag4": (i, [i, i, i, vp, vp, vp, vp, vp]),
+        "hamstr_gpu_block_tridag4_noalloc": (i, [i, i, i, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -105,6 +106,19 @@ def block_tridag4(A, B, C, F, periodic: bool, stream: int = 0):
             raise ValueError("block_tridag4 needs contiguous float64 CUDA tensors")
     _check(load().hamstr_gpu_block_tridag4(nl, n, int(periodic), A.data_ptr(), B.data_ptr(), C.data_ptr(),
                                            F.data_ptr(), stream or None))
+
+
+def block_tridag4_noalloc(A, B, C, F, periodic: bool, stream: int = 0):
+    """block_tridag4 without device allocation (fixed 8 MiB scratch in the
+    library; nlines*(80*N+16) <= 1048576).  Only enqueues on `stream`: the
+    caller synchronises before reading F.  For callers that cannot allocate
+    device memory per call (loops beside other streams, pool-owned memory)."""
+    nl, n = int(F.shape[0]), int(F.shape[1])
+    for t in (A, B, C, F):
+        if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float64"):
+            raise ValueError("block_tridag4_noalloc needs contiguous float64 CUDA tensors")
+    _check(load().hamstr_gpu_block_tridag4_noalloc(nl, n, int(periodic), A.data_ptr(), B.data_ptr(),
+                                                   C.data_ptr(), F.data_ptr(), stream or None))
 
 
 def _ptr(a: np.ndarray):

@@ -127,6 +127,22 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
 int hamstr_gpu_block_tridag4(int nlines, int N, int periodic, const double* A, const double* B,
                              const double* C, double* F, void* stream);
 
+/* The same solve without any device allocation (no counterpart in the
+ * reference, which has no GPU).  For callers that cannot allocate device
+ * memory on every call: loops that run beside work on other streams (the
+ * cudaFree of the entry point above waits for the whole device) and hosts
+ * whose device memory belongs to their own pool allocator.  Scratch is a
+ * fixed 8 MiB array that every GPU loading the library holds until exit;
+ * the call needs nlines*(80*N+16) <= 1048576 doubles and returns
+ * HAMSTR_GPU_ERR_ARG beyond that.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  The call only enqueues
+ * work on `stream` (synchronise it before reading F).  All calls share the
+ * one array: calls whose work overlaps on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller. */
+int hamstr_gpu_block_tridag4_noalloc(int nlines, int N, int periodic, const double* A, const double* B,
+                                     const double* C, double* F, void* stream);
+
 /* Enqueues n pseudo-time steps on the handle's stream and returns without
  * waiting (no tolerance stop, no host copies): for callers that keep the
  * state on the GPU and synchronise themselves (timing, pipelines). */
