@@ -117,17 +117,6 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
    if (h == 0) facN[e] = lu_get(u, e);
 }
 
-// x_k -= sum_j M[k][j] * v[j] for the lane's component k = lane & 3, then
-// all four components gathered into every lane
-__device__ __forceinline__ void matvec_sub(const double (&Mrow)[4], const double (&v)[4], double (&x)[4], int kk)
-{
-   double t = sel4(x, kk);
-#pragma unroll
-   for (int jj = 0; jj < 4; jj++) t -= Mrow[jj] * v[jj];
-#pragma unroll
-   for (int m = 0; m < 4; m++) x[m] = __shfl_sync(kLaneMask, t, m);
-}
-
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
 {
    const double2 a = *reinterpret_cast<const double2*>(p);
@@ -135,130 +124,169 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4]
    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
-__device__ __forceinline__ void ld16(const double* __restrict__ p, double (&v)[16])
-{
-#pragma unroll
-   for (int m = 0; m < 16; m += 2) {
-      const double2 a = *reinterpret_cast<const double2*>(p + m);
-      v[m] = a.x;
-      v[m + 1] = a.y;
-   }
-}
-
-__device__ __forceinline__ LU4 lu_from(const double (&v)[16])
-{
-   LU4 u;
-   u.b11 = v[0];  u.u12 = v[1];  u.u13 = v[2];  u.u14 = v[3];
-   u.b21 = v[4];  u.b22 = v[5];  u.u23 = v[6];  u.u24 = v[7];
-   u.b31 = v[8];  u.b32 = v[9];  u.b33 = v[10]; u.u34 = v[11];
-   u.b41 = v[12]; u.b42 = v[13]; u.b43 = v[14]; u.b44 = v[15];
-   return u;
-}
-
 // Right-hand-side replay of a factored line: fs (N rows of 4, in place)
 // <- solution, with the records of factor_line.  All 32 lanes take part.
+//
+// Lane r = lane & 3 owns component r of the vector being solved; the 16
+// products of a 4x4 matrix-vector step are formed in one instruction by
+// lanes e = 4*pr + pj (e = lane & 15) and handed to their owner lanes with
+// shuffles, so each row costs about 35 FP64 instructions instead of 60.
+// The subtraction order of every component is the reference's.
+__device__ __forceinline__ void lu_solve_dist(const double (&lu)[4], int r, double& xr, double (&xs)[4])
+{
+   // forward: lane r subtracts L[r][l]*d_l for l < r, then d_r = x_r * piv_r
+   // (triSolvers.cpp:813-816); lanes not yet due compute values nobody uses
+   const double piv = sel4(lu, r);
+   double x = xr, d[4];
+#pragma unroll
+   for (int l = 0; l < 4; l++) {
+      const double t = x * piv;
+      d[l] = __shfl_sync(kLaneMask, t, l);
+      if (l < 3) x = x - lu[l] * d[l];
+   }
+   // backward (triSolvers.cpp:818-821): x3 = d3, x2 = d2 - u34 x3,
+   // x1 = (d1 - u23 x2) - u24 x3, x0 = ((d0 - u12 x1) - u13 x2) - u14 x3
+   xs[3] = d[3];
+   const double q3 = lu[3] * xs[3];
+   const double x2l = d[2] - q3;
+   xs[2] = __shfl_sync(kLaneMask, x2l, 2);
+   const double q2 = lu[2] * xs[2];
+   const double t1 = d[1] - q2;
+   const double x1l = t1 - q3;
+   xs[1] = __shfl_sync(kLaneMask, x1l, 1);
+   const double q1 = lu[1] * xs[1];
+   double t0 = d[0] - q1;
+   t0 = t0 - q2;
+   const double x0l = t0 - q3;
+   xs[0] = __shfl_sync(kLaneMask, x0l, 0);
+   xr = sel4(xs, r);
+}
+
 __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const double* __restrict__ facN, int N,
                                            bool per, double* __restrict__ fs, int lane)
 {
-   const int kk = lane & 3;
-   // forward sweep (triSolvers.cpp:778-822 / 859-933); row i+1 prefetched
-   double xp[4] = {0.0, 0.0, 0.0, 0.0};
-   double x[4], arow[4] = {0.0, 0.0, 0.0, 0.0}, lu[16];
-   ld4(fs, x);
-   ld16(fac + 16, lu);
+   const int e = lane & 15, pr = e >> 2, pj = e & 3, hi = lane >> 4;
+   const int r = lane & 3;
+   // ---- forward sweep (triSolvers.cpp:778-822 / 859-933); row i+1 prefetched
+   double xprev[4] = {0.0, 0.0, 0.0, 0.0};
+   double fv = fs[r], av = 0.0, lu[4];
+#pragma unroll
+   for (int c = 0; c < 4; c++) lu[c] = fac[16 + 4 * r + c];
    for (int i = 0; i < N; i++) {
-      double xn[4] = {0.0, 0.0, 0.0, 0.0}, an[4] = {0.0, 0.0, 0.0, 0.0}, lun[16];
+      double fvn = 0.0, avn = 0.0, lun[4] = {0.0, 0.0, 0.0, 0.0};
       if (i + 1 < N) {
          const double* nr = fac + (size_t)kFacRec * (i + 1);
-         ld4(fs + 4 * (i + 1), xn);
-         ld4(nr + 4 * kk, an);
-         ld16(nr + 16, lun);
-      } else {
+         fvn = fs[4 * (i + 1) + r];
+         avn = nr[e];
 #pragma unroll
-         for (int m = 0; m < 16; m++) lun[m] = 0.0;
+         for (int c = 0; c < 4; c++) lun[c] = nr[16 + 4 * r + c];
       }
-      if (i > 0) matvec_sub(arow, xp, x, kk);
-      const LU4 u = lu_from(lu);
-      lu_solve(u, x[0], x[1], x[2], x[3]);
-      if (lane < 4) fs[4 * i + lane] = sel4(x, lane);
+      double x = fv;
+      if (i > 0) {
+         // f(i) -= a(i) f(i-1), the 16 products in one instruction
+         const double p = av * sel4(xprev, pj);
 #pragma unroll
-      for (int m = 0; m < 4; m++) { xp[m] = x[m]; x[m] = xn[m]; arow[m] = an[m]; }
+         for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, p, 4 * r + jj);
+      }
+      double xs[4];
+      lu_solve_dist(lu, r, x, xs);
+      if (lane < 4) fs[4 * i + lane] = x;
 #pragma unroll
-      for (int m = 0; m < 16; m++) lu[m] = lun[m];
+      for (int m = 0; m < 4; m++) { xprev[m] = xs[m]; lu[m] = lun[m]; }
+      fv = fvn;
+      av = avn;
    }
    __syncwarp();
-   double xn[4];
    if (per) {
-      // f(N-1) -= c_{N-1} f(i), then the last-row solve (triSolvers.cpp:991-1029)
-      double fN[4];
-#pragma unroll
-      for (int m = 0; m < 4; m++) fN[m] = xp[m];
-      double fi[4], crow[4];
-      ld4(fs, fi);
-      ld4(fac + 64 + 4 * kk, crow);
-      for (int i = 0; i < N - 1; i++) {
-         double fin[4] = {0.0, 0.0, 0.0, 0.0}, cn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i + 2 < N) {
-            ld4(fs + 4 * (i + 1), fin);
-            ld4(fac + (size_t)kFacRec * (i + 1) + 64 + 4 * kk, cn);
-         }
-         matvec_sub(crow, fi, fN, kk);
-#pragma unroll
-         for (int m = 0; m < 4; m++) { fi[m] = fin[m]; crow[m] = cn[m]; }
+      // f(N-1) -= c_{N-1}^{(i)} f(i), i = 0..N-2 (triSolvers.cpp:991-999);
+      // the products of rows i and i+1 in one instruction (lanes 0-15, 16-31)
+      double fN = sel4(xprev, r);
+      int i = 0;
+      double c = 0.0, f = 0.0;
+      if (hi < N - 1) {
+         c = fac[(size_t)kFacRec * hi + 64 + e];
+         f = fs[4 * hi + pj];
       }
-      const LU4 u = lu_load(facN);
-      lu_solve(u, fN[0], fN[1], fN[2], fN[3]);
+      for (; i < N - 1; i += 2) {
+         const int rn = i + 2 + hi;
+         double cn = 0.0, fn = 0.0;
+         if (rn < N - 1) {
+            cn = fac[(size_t)kFacRec * rn + 64 + e];
+            fn = fs[4 * rn + pj];
+         }
+         const double p = c * f;
+#pragma unroll
+         for (int jj = 0; jj < 4; jj++) fN = fN - __shfl_sync(kLaneMask, p, 4 * r + jj);
+         if (i + 1 < N - 1) {
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) fN = fN - __shfl_sync(kLaneMask, p, 16 + 4 * r + jj);
+         }
+         c = cn;
+         f = fn;
+      }
+      double luN[4], xn[4];
+#pragma unroll
+      for (int cc = 0; cc < 4; cc++) luN[cc] = facN[4 * r + cc];
+      lu_solve_dist(luN, r, fN, xn);
       __syncwarp();
-      if (lane < 4) fs[4 * (N - 1) + lane] = sel4(fN, lane);
-      // back substitution (triSolvers.cpp:1032-1045)
+      if (lane < 4) fs[4 * (N - 1) + lane] = fN;
+      // back substitution (triSolvers.cpp:1032-1045):
+      // f(i) -= (c'(i) f(i+1) + a'(i) f(N-1)), c' products in lanes 0-15 and
+      // a' products in lanes 16-31 of one instruction
+      double fNall[4];
 #pragma unroll
-      for (int m = 0; m < 4; m++) xn[m] = fN[m];
-      double xi[4], cr[4], ar[4];
+      for (int m = 0; m < 4; m++) fNall[m] = xn[m];
+      double xnext[4];
+#pragma unroll
+      for (int m = 0; m < 4; m++) xnext[m] = xn[m];
+      double mv = 0.0, xi = 0.0;
       if (N >= 2) {
-         ld4(fs + 4 * (N - 2), xi);
-         ld4(fac + (size_t)kFacRec * (N - 2) + 32 + 4 * kk, cr);
-         ld4(fac + (size_t)kFacRec * (N - 2) + 48 + 4 * kk, ar);
+         mv = fac[(size_t)kFacRec * (N - 2) + 32 + 16 * hi + e];
+         xi = fs[4 * (N - 2) + r];
       }
-      for (int i = N - 2; i >= 0; i--) {
-         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0}, arn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i > 0) {
-            ld4(fs + 4 * (i - 1), xin);
-            ld4(fac + (size_t)kFacRec * (i - 1) + 32 + 4 * kk, crn);
-            ld4(fac + (size_t)kFacRec * (i - 1) + 48 + 4 * kk, arn);
+      for (int ii = N - 2; ii >= 0; ii--) {
+         double mvn = 0.0, xin = 0.0;
+         if (ii > 0) {
+            mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + 16 * hi + e];
+            xin = fs[4 * (ii - 1) + r];
          }
-         double t = sel4(xi, kk);
-         if (i == N - 2) {
+         const double prod = mv * (hi ? sel4(fNall, pj) : sel4(xnext, pj));
+         const double other = __shfl_sync(kLaneMask, prod, e + 16);
+         const double sterm = (ii == N - 2) ? prod : prod + other;
+         double x = xi;
 #pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj]);
-         } else {
+         for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, sterm, 4 * r + jj);
 #pragma unroll
-            for (int jj = 0; jj < 4; jj++) t -= (cr[jj] * xn[jj] + ar[jj] * fN[jj]);
-         }
-#pragma unroll
-         for (int m = 0; m < 4; m++) xn[m] = __shfl_sync(kLaneMask, t, m);
-         if (lane < 4) fs[4 * i + lane] = sel4(xn, lane);
-#pragma unroll
-         for (int m = 0; m < 4; m++) { xi[m] = xin[m]; cr[m] = crn[m]; ar[m] = arn[m]; }
+         for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, m);
+         if (lane < 4) fs[4 * ii + lane] = x;
+         mv = mvn;
+         xi = xin;
       }
    } else {
-      // back substitution (triSolvers.cpp:839-846)
+      // back substitution (triSolvers.cpp:839-846): f(i) -= c'(i) f(i+1)
+      double xnext[4];
 #pragma unroll
-      for (int m = 0; m < 4; m++) xn[m] = xp[m];
-      double xi[4], cr[4];
+      for (int m = 0; m < 4; m++) xnext[m] = xprev[m];
+      double mv = 0.0, xi = 0.0;
       if (N >= 2) {
-         ld4(fs + 4 * (N - 2), xi);
-         ld4(fac + (size_t)kFacRec * (N - 2) + 32 + 4 * kk, cr);
+         mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
+         xi = fs[4 * (N - 2) + r];
       }
-      for (int i = N - 2; i >= 0; i--) {
-         double xin[4] = {0.0, 0.0, 0.0, 0.0}, crn[4] = {0.0, 0.0, 0.0, 0.0};
-         if (i > 0) {
-            ld4(fs + 4 * (i - 1), xin);
-            ld4(fac + (size_t)kFacRec * (i - 1) + 32 + 4 * kk, crn);
+      for (int ii = N - 2; ii >= 0; ii--) {
+         double mvn = 0.0, xin = 0.0;
+         if (ii > 0) {
+            mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + e];
+            xin = fs[4 * (ii - 1) + r];
          }
-         matvec_sub(cr, xn, xi, kk);
-         if (lane < 4) fs[4 * i + lane] = sel4(xi, lane);
+         const double prod = mv * sel4(xnext, pj);
+         double x = xi;
 #pragma unroll
-         for (int m = 0; m < 4; m++) { xn[m] = xi[m]; xi[m] = xin[m]; cr[m] = crn[m]; }
+         for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, prod, 4 * r + jj);
+#pragma unroll
+         for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, m);
+         if (lane < 4) fs[4 * ii + lane] = x;
+         mv = mvn;
+         xi = xin;
       }
    }
 }
