@@ -32,6 +32,81 @@ namespace hamstr {
 constexpr int kFacRec = 80;
 constexpr unsigned kLaneMask = 0xffffffffu;
 
+// x <- LU^{-1} x for a 4-vector held one component per lane: component l
+// lives in lane base + stride*l, r is this lane's component and lu its LU
+// row (L[r][0..r-1], reciprocal pivot, U[r][r+1..3]).  Same operations and
+// order as triSolvers.cpp:813-821; lanes whose component is not yet due
+// compute values nobody reads.  Returns this lane's solved component and
+// leaves the whole solution in xs on every lane.
+__device__ __forceinline__ double lu_solve_lanes(const double (&lu)[4], int r, double x, int base, int stride,
+                                                 double (&xs)[4])
+{
+   const double piv = sel4(lu, r);
+   double d[4];
+#pragma unroll
+   for (int l = 0; l < 4; l++) {
+      const double t = x * piv;
+      d[l] = __shfl_sync(kLaneMask, t, base + stride * l);
+      if (l < 3) x = x - lu[l] * d[l];
+   }
+   xs[3] = d[3];
+   const double q3 = lu[3] * xs[3];
+   const double x2l = d[2] - q3;
+   xs[2] = __shfl_sync(kLaneMask, x2l, base + 2 * stride);
+   const double q2 = lu[2] * xs[2];
+   const double t1 = d[1] - q2;
+   const double x1l = t1 - q3;
+   xs[1] = __shfl_sync(kLaneMask, x1l, base + stride);
+   const double q1 = lu[1] * xs[1];
+   double t0 = d[0] - q1;
+   t0 = t0 - q2;
+   const double x0l = t0 - q3;
+   xs[0] = __shfl_sync(kLaneMask, x0l, base);
+   return sel4(xs, r);
+}
+
+// LU of a 4x4 block held one element per lane (element e = 4k+j in lane
+// base + e), as a wavefront over the lanes: returns in each lane element e
+// of the LU record (L below the diagonal, reciprocal pivots on it, U above),
+// with the operations and order of triSolvers.cpp:796-811.
+__device__ __forceinline__ double lu_wavefront(double w, int base, int e)
+{
+   const int k = e >> 2, j = e & 3;
+   const double piv0 = 1. / __shfl_sync(kLaneMask, w, base);
+   {
+      const double m = w * piv0;
+      if (k == 0 && j >= 1) w = m;
+   }
+   {
+      const double L = __shfl_sync(kLaneMask, w, base + 4 * k), U = __shfl_sync(kLaneMask, w, base + j);
+      const double t = w - L * U;
+      if (k >= 1 && j >= 1) w = t;
+   }
+   const double piv1 = 1. / __shfl_sync(kLaneMask, w, base + 5);
+   {
+      const double m = w * piv1;
+      if (k == 1 && j >= 2) w = m;
+   }
+   {
+      const double L = __shfl_sync(kLaneMask, w, base + 4 * k + 1), U = __shfl_sync(kLaneMask, w, base + 4 + j);
+      const double t = w - L * U;
+      if (k >= 2 && j >= 2) w = t;
+   }
+   const double piv2 = 1. / __shfl_sync(kLaneMask, w, base + 10);
+   {
+      const double m = w * piv2;
+      if (k == 2 && j == 3) w = m;
+   }
+   {
+      const double L = __shfl_sync(kLaneMask, w, base + 14), U = __shfl_sync(kLaneMask, w, base + 11);
+      const double t = w - L * U;
+      if (k == 3 && j == 3) w = t;
+   }
+   const double piv3 = 1. / __shfl_sync(kLaneMask, w, base + 15);
+   if (k == j) w = (k == 0) ? piv0 : (k == 1) ? piv1 : (k == 2) ? piv2 : piv3;
+   return w;
+}
+
 // Block-Thomas factorisation of one line of N rows by one warp: blocks
 // A_i = Ab + i*stride, B_i = Bb + i*stride, C_i = Cb + i*stride (row-major
 // 4x4); writes the per-row records `fac` (kFacRec doubles per row) and,
@@ -66,22 +141,21 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
       } else if (h) {
          acc = A;
       }
-      double b[16];
+      // LU of B'(i), computed by both halves on their own copy
+      const double w = lu_wavefront(__shfl_sync(kLaneMask, acc, e), 16 * h, e);
+      if (h == 0) rec[16 + e] = w;
+      double lu[4];
 #pragma unroll
-      for (int m = 0; m < 16; m++) b[m] = __shfl_sync(kLaneMask, acc, m);
-      const LU4 u = lu_factor(b);
-      if (h == 0) rec[16 + e] = lu_get(u, e);
-      // c'(i) = B'^{-1} c(i), a'(i) = B'^{-1} a(i); at i == N-2 of a
-      // periodic chain c(i) += a(i) first and a'(i) = c'(i)
+      for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, 16 * h + 4 * k + c);
+      // c'(i) = B'^{-1} c(i), a'(i) = B'^{-1} a(i), one column per lane
+      // group (component k of column j in lane 16h + 4k + j); at i == N-2
+      // of a periodic chain c(i) += a(i) first and a'(i) = c'(i)
       const bool last2 = per && (i == N - 2);
       double Y = h ? acc : C;
       const double fillv = __shfl_sync(kLaneMask, acc, 16 + e);
       if (last2 && h == 0) Y = C + fillv;
-      double y[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) y[r] = __shfl_sync(kLaneMask, Y, 16 * h + 4 * r + j);
-      lu_solve(u, y[0], y[1], y[2], y[3]);
-      double Yp = sel4(y, k);
+      double ys[4];
+      double Yp = lu_solve_lanes(lu, k, Y, 16 * h + j, 4, ys);
       const double fromc = __shfl_sync(kLaneMask, Yp, e);
       if (last2 && h == 1) Yp = fromc;
       rec[32 + 16 * h + e] = Yp;
@@ -110,11 +184,8 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
       cN = __shfl_sync(kLaneMask, acc, e);
       Y = Yn;
    }
-   double b[16];
-#pragma unroll
-   for (int m = 0; m < 16; m++) b[m] = __shfl_sync(kLaneMask, bN, 16 + m);
-   const LU4 u = lu_factor(b);
-   if (h == 0) facN[e] = lu_get(u, e);
+   const double w = lu_wavefront(__shfl_sync(kLaneMask, bN, 16 + e), 16 * h, e);
+   if (h == 0) facN[e] = w;
 }
 
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
@@ -132,36 +203,6 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4]
 // lanes e = 4*pr + pj (e = lane & 15) and handed to their owner lanes with
 // shuffles, so each row costs about 35 FP64 instructions instead of 60.
 // The subtraction order of every component is the reference's.
-__device__ __forceinline__ void lu_solve_dist(const double (&lu)[4], int r, double& xr, double (&xs)[4])
-{
-   // forward: lane r subtracts L[r][l]*d_l for l < r, then d_r = x_r * piv_r
-   // (triSolvers.cpp:813-816); lanes not yet due compute values nobody uses
-   const double piv = sel4(lu, r);
-   double x = xr, d[4];
-#pragma unroll
-   for (int l = 0; l < 4; l++) {
-      const double t = x * piv;
-      d[l] = __shfl_sync(kLaneMask, t, l);
-      if (l < 3) x = x - lu[l] * d[l];
-   }
-   // backward (triSolvers.cpp:818-821): x3 = d3, x2 = d2 - u34 x3,
-   // x1 = (d1 - u23 x2) - u24 x3, x0 = ((d0 - u12 x1) - u13 x2) - u14 x3
-   xs[3] = d[3];
-   const double q3 = lu[3] * xs[3];
-   const double x2l = d[2] - q3;
-   xs[2] = __shfl_sync(kLaneMask, x2l, 2);
-   const double q2 = lu[2] * xs[2];
-   const double t1 = d[1] - q2;
-   const double x1l = t1 - q3;
-   xs[1] = __shfl_sync(kLaneMask, x1l, 1);
-   const double q1 = lu[1] * xs[1];
-   double t0 = d[0] - q1;
-   t0 = t0 - q2;
-   const double x0l = t0 - q3;
-   xs[0] = __shfl_sync(kLaneMask, x0l, 0);
-   xr = sel4(xs, r);
-}
-
 __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const double* __restrict__ facN, int N,
                                            bool per, double* __restrict__ fs, int lane)
 {
@@ -189,7 +230,7 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
          for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, p, 4 * r + jj);
       }
       double xs[4];
-      lu_solve_dist(lu, r, x, xs);
+      x = lu_solve_lanes(lu, r, x, 0, 1, xs);
       if (lane < 4) fs[4 * i + lane] = x;
 #pragma unroll
       for (int m = 0; m < 4; m++) { xprev[m] = xs[m]; lu[m] = lun[m]; }
@@ -227,7 +268,7 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       double luN[4], xn[4];
 #pragma unroll
       for (int cc = 0; cc < 4; cc++) luN[cc] = facN[4 * r + cc];
-      lu_solve_dist(luN, r, fN, xn);
+      fN = lu_solve_lanes(luN, r, fN, 0, 1, xn);
       __syncwarp();
       if (lane < 4) fs[4 * (N - 1) + lane] = fN;
       // back substitution (triSolvers.cpp:1032-1045):
