@@ -259,6 +259,7 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    } while (0)
    TRY(dalloc(&d.q, 4 * nc, o));
    TRY(dalloc(&d.r, 4 * nc, o));
+   TRY(dalloc(&d.qt, 4 * nc, o));
    TRY(dalloc(&d.r0, 4 * nc, o));
    TRY(dalloc(&d.dq, 4 * nc, o));
    TRY(dalloc(&d.sigma, nc, o));
@@ -331,6 +332,7 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
          q[4 * i + 3] = p->einf;
       }
       e = cudaMemcpy(d.q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(d.qt, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
    }
    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
    if (e != cudaSuccess) {
@@ -362,6 +364,7 @@ int hamstr_gpu_get(hamstr_gpu* g, const char* name, double* out)
    const double* src = nullptr;
    size_t n = 0;
    if (!std::strcmp(name, "q")) { src = d.q; n = 4 * nc; }
+   else if (!std::strcmp(name, "qt")) { src = d.qt; n = 4 * nc; }
    else if (!std::strcmp(name, "r")) { src = d.r; n = 4 * nc; }
    else if (!std::strcmp(name, "r0")) { src = d.r0; n = 4 * nc; }
    else if (!std::strcmp(name, "dq")) { src = d.dq; n = 4 * nc; }
@@ -393,6 +396,7 @@ int hamstr_gpu_set(hamstr_gpu* g, const char* name, const double* in)
    double* dst = nullptr;
    size_t n = 0;
    if (!std::strcmp(name, "q")) { dst = d.q; n = 4 * nc; }
+   else if (!std::strcmp(name, "qt")) { dst = d.qt; n = 4 * nc; }
    else if (!std::strcmp(name, "r")) { dst = d.r; n = 4 * nc; }
    else if (!std::strcmp(name, "r0")) { dst = d.r0; n = 4 * nc; }
    else if (!std::strcmp(name, "dq")) { dst = d.dq; n = 4 * nc; }
@@ -517,6 +521,59 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
    }
    if (evals) *evals = rows;
    if (converged) *converged = ctl[0];
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_gpu_update_solution(hamstr_gpu* g, const char* qold, const char* qnew, double coef)
+{
+   if (!g || !qold || !qnew) return HAMSTR_GPU_ERR_ARG;
+   auto pick = [&](const char* n) -> double* {
+      if (!std::strcmp(n, "q")) return g->d.q;
+      if (!std::strcmp(n, "qt")) return g->d.qt;
+      return nullptr;
+   };
+   double* src = pick(qold);
+   double* dst = pick(qnew);
+   if (!src || !dst) {
+      set_error("updateSolution arrays are \"q\" or \"qt\"");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   launch_update(g->d, src, dst, coef, g->stream);
+   CK(cudaGetLastError());
+   return g->status_check();
+}
+
+int hamstr_gpu_step_explicit(hamstr_gpu* g, int scheme, double* norms2)
+{
+   // march.cpp:342-377: "euler" (scheme 0) and the 3-stage "rk3" (scheme 1)
+   if (!g || (scheme != 0 && scheme != 1)) return HAMSTR_GPU_ERR_ARG;
+   int st = g->reset_ctl(0.0);
+   if (st) return st;
+   DeviceState& d = g->d;
+   auto rhs = [&]() {
+      launch_rhs_face(d, false, g->stream);
+      launch_rhs_cell(d, false, g->stream);
+      launch_norm_final(d, 0, false, g->stream);
+   };
+   if (scheme == 0) {
+      rhs();
+      launch_update(d, d.q, d.q, 1.0, g->stream);
+   } else {
+      rhs();
+      launch_update(d, d.q, d.qt, 0.25, g->stream);
+      launch_update(d, d.q, d.q, 8.0 / 15, g->stream);
+      rhs();
+      launch_update(d, d.qt, d.q, 5.0 / 12, g->stream);
+      rhs();
+      launch_update(d, d.qt, d.q, 3.0 / 4.0, g->stream);
+   }
+   CK(cudaGetLastError());
+   double n[2];
+   st = g->read_norms(n, 2);
+   if (st) return st;
+   if (norms2) { norms2[0] = n[0]; norms2[1] = n[1]; }
    return HAMSTR_GPU_OK;
 }
 

@@ -38,6 +38,7 @@ struct DeviceState {
    double fs1, fs2;        // freestream rho*u, rho*v (computeRHS.cpp:247-248)
 
    double *q, *r, *r0, *dq, *sigma, *dtfac;
+   double* qt;             // second state of the RK3 scheme (solnBlock.h:47)
    double *flux, *spec, *ff;
    int4* sten;
    int4* slot;
@@ -80,6 +81,8 @@ void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 void launch_norm_final(const DeviceState& d, int off, bool check_tol, cudaStream_t st);
 void launch_step_end(const DeviceState& d, cudaStream_t st);
 void launch_dtfac(const DeviceState& d, cudaStream_t st);
+// qnew = qold + coef*CFL/sigma * r (march.cpp:411-433)
+void launch_update(const DeviceState& d, const double* qold, double* qnew, double coef, cudaStream_t st);
 void launch_adi_init(const DeviceState& d, cudaStream_t st);
 void launch_dq_update(const DeviceState& d, cudaStream_t st);
 // launchers (adi.cu)

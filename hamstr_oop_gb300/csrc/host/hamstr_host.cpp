@@ -252,6 +252,7 @@ void hamstr_init_flow(SOLNBLOCK& sb, int nCell)
       sb.q[4 * (size_t)i + 2] = sb.rinf * sb.vinf;
       sb.q[4 * (size_t)i + 3] = sb.einf;
    }
+   sb.qt = sb.q;
 }
 
 // ==================================================================
@@ -274,6 +275,7 @@ SOLVER::SOLVER(MESHBLOCK* mbin, SOLNBLOCK* sbin) : mb(mbin), sb(sbin)
    stepType = sb->scheme;
    const size_t nc = (size_t)mb->nCell;
    sb->q.assign(4 * nc, 0.0);
+   sb->qt.assign(4 * nc, 0.0);
    sb->r.assign(4 * nc, 0.0);
    sb->r0.assign(4 * nc, 0.0);
    sb->dq.assign(4 * nc, 0.0);
@@ -330,20 +332,44 @@ void SOLVER::ADI(void)
 
 void SOLVER::stepSolution(void)
 {
-   if (std::strcmp(stepType, "ADI") != 0)
-      throw Error(HAMSTR_GPU_ERR_ARG, std::string("time marching scheme '") + stepType +
-                                          "' is not on the GPU path (ADI only)");
    ensureGpu();
-   double n4[4];
-   check(hamstr_gpu_step(gpu, n4));
-   sb->L2Norm = n4[2];
-   sb->LInfNorm = n4[3];
+   if (std::strcmp(stepType, "ADI") == 0) {
+      double n4[4];
+      check(hamstr_gpu_step(gpu, n4));
+      sb->L2Norm = n4[2];
+      sb->LInfNorm = n4[3];
+      return;
+   }
+   int scheme = -1;
+   if (std::strcmp(stepType, "euler") == 0) scheme = 0;
+   if (std::strcmp(stepType, "rk3") == 0) scheme = 1;
+   if (scheme < 0)
+      throw Error(HAMSTR_GPU_ERR_ARG, std::string("unknown time marching scheme '") + stepType + "'");
+   if (scheme == 0 && sb->visc)
+      throw Error(HAMSTR_GPU_ERR_ARG, "viscous explicit step not implemented (march.cpp:344-349)");
+   double n2[2];
+   check(hamstr_gpu_step_explicit(gpu, scheme, n2));
+   sb->L2Norm = n2[0];
+   sb->LInfNorm = n2[1];
+}
+
+void SOLVER::updateSolution(double* qold, double* qnew, double coef)
+{
+   // the reference passes its q / qt host arrays; the device copies are updated
+   ensureGpu();
+   auto name = [&](const double* p) -> const char* {
+      if (p == sb->q.data()) return "q";
+      if (p == sb->qt.data()) return "qt";
+      throw Error(HAMSTR_GPU_ERR_ARG, "updateSolution takes the solver's q or qt arrays");
+   };
+   check(hamstr_gpu_update_solution(gpu, name(qold), name(qnew), coef));
 }
 
 void SOLVER::syncHost(void)
 {
    ensureGpu();
    check(hamstr_gpu_get(gpu, "q", sb->q.data()));
+   check(hamstr_gpu_get(gpu, "qt", sb->qt.data()));
    check(hamstr_gpu_get(gpu, "r", sb->r.data()));
    check(hamstr_gpu_get(gpu, "r0", sb->r0.data()));
    check(hamstr_gpu_get(gpu, "dq", sb->dq.data()));
@@ -355,8 +381,6 @@ void SOLVER::marchInTime(void)
 {
    // march.cpp:15-59: nsteps steps and the per-step table
    ensureGpu();
-   if (std::strcmp(stepType, "ADI") != 0)
-      throw Error(HAMSTR_GPU_ERR_ARG, "only the ADI scheme is on the GPU path");
    double cpuTime = 0.0;
    for (int n = 0; n < sb->nsteps; n++) {
       const std::clock_t start = std::clock();

@@ -76,7 +76,7 @@ class SOLNBLOCK
    double gamma = 0, invGamma = 0, gm1 = 0, c2b = 0, rgas = 0, pr = 0, prtr = 0;
    double LInfNorm = 0, L2Norm = 0;
    // host copies of the solution (refreshed by SOLVER::syncHost)
-   std::vector<double> q, r, r0, dq, sigma, ff;
+   std::vector<double> q, qt, r, r0, dq, sigma, ff;
 
   public:
    SOLNBLOCK() {}
@@ -102,7 +102,8 @@ class SOLVER
    ~SOLVER();
    void initFlow(void);                  // initFlow.cpp:12-93
    void marchInTime(void);               // march.cpp:15-59
-   void stepSolution(void);              // march.cpp:66-134 (ADI branch)
+   void stepSolution(void);              // march.cpp:66-134 (ADI, euler, rk3)
+   void updateSolution(double* qold, double* qnew, double coef);   // march.cpp:411-433
    void computeRHS(char* option);        // computeRHS.cpp:17-427
    void computeLinearRHS(void);          // computeLinearRHS.cpp:13-371
    void ADI(void);                       // ADI.cpp:15-266

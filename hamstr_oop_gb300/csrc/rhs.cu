@@ -467,6 +467,22 @@ __global__ void step_end_kernel(DeviceState d)
    if (!halted(d)) d.ctl[1] = d.ctl[1] + 1;
 }
 
+// explicit update (updateSolution, march.cpp:411-433):
+// qnew = qold + (coef*CFL/sigma) * r, per cell and component
+__global__ void __launch_bounds__(kThreads) update_kernel(DeviceState d, const double* __restrict__ qold,
+                                                          double* __restrict__ qnew, double coef)
+{
+   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+   if (c >= d.nCell || halted(d)) return;
+   const double dtfac = coef * d.fc.cfl / d.sigma[c];
+   double qo[4], r[4], qn[4];
+   ld4(qold + 4 * (size_t)c, qo);
+   ld4(d.r + 4 * (size_t)c, r);
+#pragma unroll
+   for (int k = 0; k < 4; k++) qn[k] = qo[k] + dtfac * r[k];
+   st4(qnew + 4 * (size_t)c, qn);
+}
+
 __global__ void __launch_bounds__(kThreads) dtfac_kernel(DeviceState d)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -545,6 +561,11 @@ void launch_norm_final(const DeviceState& d, int off, bool check_tol, cudaStream
 }
 
 void launch_step_end(const DeviceState& d, cudaStream_t st) { step_end_kernel<<<1, 1, 0, st>>>(d); }
+
+void launch_update(const DeviceState& d, const double* qold, double* qnew, double coef, cudaStream_t st)
+{
+   update_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d, qold, qnew, coef);
+}
 
 void launch_dtfac(const DeviceState& d, cudaStream_t st)
 {

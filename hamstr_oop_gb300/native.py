@@ -73,6 +73,8 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_step": (i, [vp, vp]),
         "hamstr_gpu_march": (i, [vp, i, d, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "hamstr_gpu_stream": (vp, [vp]),
+        "hamstr_gpu_step_explicit": (i, [vp, i, vp]),
+        "hamstr_gpu_update_solution": (i, [vp, cp, cp, d]),
         "hamstr_gpu_enqueue_steps": (i, [vp, i]),
         "hamstr_gpu_sync": (i, [vp]),
         "hamstr_gpu_layout": (i, [vp, vp]),
@@ -214,8 +216,16 @@ class GpuSolver:
         except Exception:
             pass
 
-    _DW = {"q": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
+    _DW = {"q": ("nCell", 4), "qt": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
            "sigma": ("nCell", 1), "ff": ("nFace", 32)}
+
+    def step_explicit(self, scheme: str) -> np.ndarray:
+        out = np.zeros(2)
+        _check(load().hamstr_gpu_step_explicit(self.h, {"euler": 0, "rk3": 1}[scheme], _ptr(out)))
+        return out
+
+    def update_solution(self, qold: str, qnew: str, coef: float) -> None:
+        _check(load().hamstr_gpu_update_solution(self.h, qold.encode(), qnew.encode(), coef))
 
     def get(self, name: str) -> np.ndarray:
         key, w = self._DW[name]

@@ -88,7 +88,7 @@ const char* hamstr_gpu_strerror(int status);
 /* last detailed message (topology problems, CUDA errors) for this thread */
 const char* hamstr_gpu_last_error(void);
 
-/* named device arrays to/from host memory: q r r0 dq sigma (cell arrays) and
+/* named device arrays to/from host memory: q qt r r0 dq sigma (cell arrays) and
  * ff ([nFace][32], face order as sb->ff; faces outside every chain read 0) */
 int hamstr_gpu_get(hamstr_gpu* g, const char* name, double* out);
 int hamstr_gpu_set(hamstr_gpu* g, const char* name, const double* in);
@@ -111,6 +111,15 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
  * doubles per computeRHS evaluation; *evals = number of rows written,
  * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
+
+/* SOLVER::stepSolution, explicit branches (march.cpp:342-377): scheme 0 is
+ * "euler" (computeRHS("explicit") then q += CFL/sigma r), scheme 1 the
+ * 3-stage "rk3" through the second state qt.  norms2 = the last
+ * computeRHS L2 and Linf. */
+int hamstr_gpu_step_explicit(hamstr_gpu* g, int scheme, double* norms2);
+/* SOLVER::updateSolution(qold, qnew, coef) (march.cpp:411-433) on the device
+ * arrays named "q" or "qt": qnew = qold + coef*CFL/sigma * r. */
+int hamstr_gpu_update_solution(hamstr_gpu* g, const char* qold, const char* qnew, double coef);
 
 /* TRISOLVER::blockTridag4 (triSolvers.cpp:769-847) and blockTridagPeriodic4
  * (triSolvers.cpp:850-1046), batched over nlines independent lines of N

@@ -53,7 +53,7 @@ struct ho_case {
    int nGhost;
    double L2Norm, LInfNorm;
    /* solution arrays (solver.cpp:26-38) */
-   double *q, *r, *r0, *dq, *sigma;
+   double *q, *qt, *r, *r0, *dq, *sigma;
    double* ff;           /* nFace * 32: lmat[4][4] then rmat[4][4] */
    /* per-chain work arrays of length nMaxChain+5 */
    int work;
@@ -258,12 +258,14 @@ static void init_flow(ho_case* c)
       c->q[4 * i + 2] = c->rinf * c->vinf;
       c->q[4 * i + 3] = c->einf;
    }
+   memcpy(c->qt, c->q, sizeof(double) * NQ * c->nCell);
 }
 
 static void alloc_solution(ho_case* c)
 {
    int n = c->nCell > 0 ? c->nCell : 1;
    c->q = (double*)calloc((size_t)NQ * n, sizeof(double));
+   c->qt = (double*)calloc((size_t)NQ * n, sizeof(double));
    c->r = (double*)calloc((size_t)NQ * n, sizeof(double));
    c->r0 = (double*)calloc((size_t)NQ * n, sizeof(double));
    c->dq = (double*)calloc((size_t)NQ * n, sizeof(double));
@@ -1076,6 +1078,46 @@ int ho_step(ho_case* c, double* out4)
    return ho_adi(c, &out4[2], &out4[3]);
 }
 
+/* updateSolution (march.cpp:411-433) */
+static void update_solution(ho_case* c, const double* qold, double* qnew, double coef)
+{
+   int i, j, m = 0;
+   for (i = 0; i < c->nCell; i++)
+      for (j = 0; j < NQ; j++) {
+         double dtfac = coef * c->CFL / c->sigma[i];
+         qnew[m] = qold[m] + dtfac * c->r[m];
+         m++;
+      }
+}
+
+int ho_update_solution(ho_case* c, const char* qold, const char* qnew, double coef)
+{
+   double* s = !strcmp(qold, "q") ? c->q : !strcmp(qold, "qt") ? c->qt : NULL;
+   double* d = !strcmp(qnew, "q") ? c->q : !strcmp(qnew, "qt") ? c->qt : NULL;
+   if (!s || !d) return -1;
+   update_solution(c, s, d, coef);
+   return 0;
+}
+
+/* explicit branches of stepSolution (march.cpp:342-377) */
+int ho_step_explicit(ho_case* c, int scheme, double* out2)
+{
+   int rc;
+   if (scheme == 0) {
+      if ((rc = ho_compute_rhs(c, 0, &out2[0], &out2[1]))) return rc;
+      update_solution(c, c->q, c->q, 1.);
+      return 0;
+   }
+   if ((rc = ho_compute_rhs(c, 0, &out2[0], &out2[1]))) return rc;
+   update_solution(c, c->q, c->qt, 0.25);
+   update_solution(c, c->q, c->q, 8.0 / 15);
+   if ((rc = ho_compute_rhs(c, 0, &out2[0], &out2[1]))) return rc;
+   update_solution(c, c->qt, c->q, 5.0 / 12);
+   if ((rc = ho_compute_rhs(c, 0, &out2[0], &out2[1]))) return rc;
+   update_solution(c, c->qt, c->q, 3.0 / 4.0);
+   return 0;
+}
+
 int ho_march(ho_case* c, int n, double* hist)
 {
    int i, rc;
@@ -1133,6 +1175,7 @@ ho_case* ho_clone(const ho_case* s)
    DUP(c->refMtx, s->refMtx, 4 * nf);
    alloc_solution(c);
    memcpy(c->q, s->q, sizeof(double) * NQ * nc);
+   memcpy(c->qt, s->qt, sizeof(double) * NQ * nc);
    memcpy(c->r, s->r, sizeof(double) * NQ * nc);
    memcpy(c->r0, s->r0, sizeof(double) * NQ * nc);
    memcpy(c->dq, s->dq, sizeof(double) * NQ * nc);
@@ -1147,7 +1190,7 @@ void ho_close(ho_case* c)
    free(c->x); free(c->conn); free(c->chainsPerColor); free(c->faceStart);
    free(c->chainConn); free(c->faces); free(c->bFaces); free(c->c2chain);
    free(c->vol); free(c->normVec); free(c->refMtx);
-   free(c->q); free(c->r); free(c->r0); free(c->dq); free(c->sigma); free(c->ff);
+   free(c->q); free(c->qt); free(c->r); free(c->r0); free(c->dq); free(c->sigma); free(c->ff);
    free(c->cindx); free(c->f); free(c->df); free(c->ql); free(c->qr); free(c->f2);
    free(c->A); free(c->B); free(c->C); free(c->F);
    free(c);
@@ -1179,6 +1222,7 @@ void ho_set_run(ho_case* c, int order, int msweep, double cfl)
 static double* darr(const ho_case* c, const char* name, size_t* n)
 {
    if (!strcmp(name, "q"))     { *n = (size_t)NQ * c->nCell; return c->q; }
+   if (!strcmp(name, "qt"))    { *n = (size_t)NQ * c->nCell; return c->qt; }
    if (!strcmp(name, "r"))     { *n = (size_t)NQ * c->nCell; return c->r; }
    if (!strcmp(name, "r0"))    { *n = (size_t)NQ * c->nCell; return c->r0; }
    if (!strcmp(name, "dq"))    { *n = (size_t)NQ * c->nCell; return c->dq; }

@@ -49,6 +49,11 @@ int  ho_adi(ho_case* c, double* l2, double* linf);
 int  ho_linear_rhs(ho_case* c, double* l2, double* linf);
 int  ho_step(ho_case* c, double* out4);
 int  ho_march(ho_case* c, int n, double* hist);
+/* explicit branches of stepSolution (march.cpp:342-377): scheme 0 "euler",
+ * 1 "rk3"; out2 = last computeRHS L2, Linf */
+int  ho_step_explicit(ho_case* c, int scheme, double* out2);
+/* updateSolution (march.cpp:411-433) on "q" / "qt" */
+int  ho_update_solution(ho_case* c, const char* qold, const char* qnew, double coef);
 /* Runs `iters` steps on each of n independent cases, one host thread per
  * case (OpenMP); the CPU-baseline throughput leg. */
 int  ho_march_replicas(ho_case** cases, int n, int iters);
@@ -57,7 +62,7 @@ int  ho_march_replicas(ho_case** cases, int n, int iters);
  * blocks and [N][4] right-hand sides, in place like the reference. */
 int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic);
 
-/* Named arrays: q r r0 dq sigma ff x vol normVec refMtx (doubles) and
+/* Named arrays: q qt r r0 dq sigma ff x vol normVec refMtx (doubles) and
  * faces chainConn faceStartPerChain c2chain bFaces chainsPerColor (ints). */
 int ho_get(const ho_case* c, const char* name, double* out);
 int ho_set(ho_case* c, const char* name, const double* in);

@@ -161,7 +161,19 @@ class OracleCase:
         self._check(self._fn("march")(self.h, n, _ptr(hist)))
         return hist
 
-    _DSIZE = {"q": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
+    def step_explicit(self, scheme: str):
+        out = np.zeros(2)
+        if self.kind == "port":
+            fn = self.lib.ho_step_explicit
+            fn.restype, fn.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            self._check(fn(self.h, {"euler": 0, "rk3": 1}[scheme], _ptr(out)))
+        else:
+            fn = self.lib.ref_step_scheme
+            fn.restype, fn.argtypes = None, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]
+            fn(self.h, scheme.encode(), _ptr(out))
+        return out
+
+    _DSIZE = {"q": ("nCell", 4), "qt": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
               "sigma": ("nCell", 1), "ff": ("nFace", 32), "x": ("nNode", 2), "vol": ("nCell", 1),
               "normVec": ("nFace", 2), "refMtx": ("nFace", 4)}
 

@@ -198,6 +198,20 @@ void ref_step(void* h, double* out)
    out[2] = c->sb->L2Norm; out[3] = c->sb->LInfNorm;
 }
 
+// one step of the named scheme ("ADI", "euler", "rk3") through the
+// reference's own stepSolution (march.cpp:335-403); out2 = L2, Linf
+void ref_step_scheme(void* h, const char* scheme, double* out2)
+{
+   RefCase* c = (RefCase*)h;
+   char saved[20];
+   memcpy(saved, c->sb->scheme, sizeof(saved));
+   snprintf(c->sb->scheme, sizeof(c->sb->scheme), "%s", scheme);
+   ArenaScope a;
+   c->solv->stepSolution();
+   memcpy(c->sb->scheme, saved, sizeof(saved));
+   out2[0] = c->sb->L2Norm; out2[1] = c->sb->LInfNorm;
+}
+
 // run n steps; hist gets 4 doubles per step as in ref_step
 void ref_march(void* h, int n, double* hist)
 {
@@ -208,6 +222,7 @@ static double* dptr(RefCase* c, const char* name, size_t* n)
 {
    int nc = c->mb->nCell;
    if (!strcmp(name, "q"))     { *n = (size_t)NQ * nc; return c->sb->q; }
+   if (!strcmp(name, "qt"))    { *n = (size_t)NQ * nc; return c->sb->qt; }
    if (!strcmp(name, "r"))     { *n = (size_t)NQ * nc; return c->sb->r; }
    if (!strcmp(name, "r0"))    { *n = (size_t)NQ * nc; return c->sb->r0; }
    if (!strcmp(name, "dq"))    { *n = (size_t)NQ * nc; return c->sb->dq; }

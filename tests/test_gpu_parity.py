@@ -128,3 +128,27 @@ def test_nan_state_reports_error(make_case, oracle_lib, native_lib):
     # the handle stays usable
     gpu.set("q", orc.get("q"))
     gpu.compute_rhs(True)
+
+
+@pytest.mark.parametrize("order", [1, 3, 5])
+@pytest.mark.parametrize("scheme", ["euler", "rk3"])
+def test_explicit_steps_bitexact(make_case, oracle_lib, native_lib, order, scheme):
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 24, 6, order=order, CFL=0.8)
+    for it in range(4):
+        no, ng = orc.step_explicit(scheme), gpu.step_explicit(scheme)
+        _norm_close(ng[0], no[0], "explicit L2 step %d" % it)
+        assert ng[1] == no[1]
+    for name in ("q", "qt", "r", "sigma"):
+        _eq(gpu.get(name), orc.get(name), name)
+
+
+def test_update_solution_bitexact(make_case, oracle_lib, native_lib):
+    import ctypes
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 16, 4, order=3, CFL=0.5)
+    orc.compute_rhs(False)
+    gpu.compute_rhs(False)
+    fn = orc.lib.ho_update_solution
+    fn.restype, fn.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_double]
+    assert fn(orc.h, b"q", b"qt", 0.25) == 0
+    gpu.update_solution("q", "qt", 0.25)
+    _eq(gpu.get("qt"), orc.get("qt"), "qt")

@@ -36,3 +36,14 @@ def test_block_tridag_bitexact(oracle_lib, periodic):
         x1 = oracle_lib.block_tridag4(a, b, c, f, periodic, "port")
         x2 = oracle_lib.block_tridag4(a, b, c, f, periodic, "reference")
         assert np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("order", [1, 3, 5])
+def test_explicit_schemes_bitexact(make_case, oracle_lib, order):
+    case = make_case(20, 6, order=order, CFL=0.8)
+    ref = oracle_lib.OracleCase(case, "reference")
+    port = oracle_lib.OracleCase(case, "port")
+    for scheme in ("euler", "rk3", "rk3", "euler"):
+        assert np.array_equal(ref.step_explicit(scheme), port.step_explicit(scheme))
+    for name in ("q", "qt", "r", "sigma"):
+        assert np.array_equal(ref.get(name), port.get(name)), name
