@@ -84,10 +84,62 @@ struct hamstr_gpu {
    cudaGraph_t step_graph = nullptr;
    int launches_per_step = 0;
    double tol_host = 0.0;   // staging for the async copy into d.tol
+   int mixed = 0;           // 0: FP64 drop-in, 1: FP32 operator defect correction
+
+   // one pseudo-time step of the mixed-precision form
+   int enqueue_mixed_step(bool check_tol)
+   {
+      int n = 0;
+      launch_mx_rhs_face(d, stream); n++;
+      launch_rhs_cell(d, true, stream); n++;
+      launch_norm_final(d, 0, check_tol, stream); n++;
+      launch_mx_init(d, stream); n++;
+      for (int s = 0; s < msweep; s++) {
+         launch_mx_assemble(d, stream); n++;
+         for (int w = 0; w < plan.nWave; w++) {
+            launch_mx_lines(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
+            n++;
+         }
+         launch_mx_dq_update(d, stream); n++;
+         launch_mx_lin_face(d, stream); n++;
+         launch_mx_lin_cell(d, s == msweep - 1, stream); n++;
+         if (s == msweep - 1) { launch_norm_final(d, 2, false, stream); n++; }
+      }
+      launch_step_end(d, stream); n++;
+      launches_per_step = n;
+      CK(cudaGetLastError());
+      return HAMSTR_GPU_OK;
+   }
+
+   // allocate the FP32 buffers of the mixed form on first use
+   int ensure_mixed_buffers()
+   {
+      if (d.ff32) return HAMSTR_GPU_OK;
+      const size_t nc = (size_t)d.nCell;
+      int st;
+      if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
+      if ((st = dalloc(&d.blk32, 48 * (size_t)std::max(d.nRow, 1), owned))) return st;
+      if ((st = dalloc(&d.fsc32, 4 * (size_t)std::max(d.nRow, 1), owned))) return st;
+      if ((st = dalloc(&d.r32, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
+      // chains of each wave ordered longest first, so a warp's threads
+      // (one chain each) run for similar lengths
+      std::vector<int> lc(plan.wave_chains);
+      for (int w = 0; w < plan.nWave; w++)
+         std::stable_sort(lc.begin() + plan.wave_ptr[w], lc.begin() + plan.wave_ptr[w + 1],
+                          [&](int a, int b) { return plan.chain_nrows[a] > plan.chain_nrows[b]; });
+      if ((st = upload(&d.line_chains, lc, owned))) return st;
+      CK(cudaMemsetAsync(d.ff32, 0, 32 * (size_t)d.nSlot * sizeof(float), stream));
+      CK(cudaMemsetAsync(d.dq32, 0, 4 * nc * sizeof(float), stream));
+      return HAMSTR_GPU_OK;
+   }
 
    // one pseudo-time step on `stream` (graph body)
    int enqueue_step(bool check_tol)
    {
+      if (mixed) return enqueue_mixed_step(check_tol);
       int n = 0;
       launch_rhs_face(d, true, stream); n++;
       launch_rhs_cell(d, true, stream); n++;
@@ -680,3 +732,21 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
 }
 
 }  // extern "C"
+
+extern "C" int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed)
+{
+   if (!g || (mixed != 0 && mixed != 1)) return HAMSTR_GPU_ERR_ARG;
+   if (mixed) {
+      int st = g->ensure_mixed_buffers();
+      if (st) return st;
+   }
+   if (g->mixed != mixed) {
+      g->mixed = mixed;
+      if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
+      if (g->step_graph) cudaGraphDestroy(g->step_graph);
+      g->step_exec = nullptr;
+      g->step_graph = nullptr;
+      g->launches_per_step = 0;
+   }
+   return HAMSTR_GPU_OK;
+}

@@ -65,6 +65,14 @@ struct DeviceState {
    double* tol;            // [0] march stop tolerance on the computeRHS L2 norm (<= 0: off)
    int norm_blocks;
    int exclusive_smem;     // dynamic shared memory that keeps ADI blocks one per SM
+
+   // mixed-precision defect correction (FP64 residual, FP32 operator)
+   float* ff32;            // [nSlot][32] FP32 face Jacobians
+   float* blk32;           // [nRow][48] FP32 blocks, factored in place each sweep
+   float* fsc32;           // [nRow][4]
+   float *r32, *r032, *dq32;   // [nCell][4]
+   float* g32;             // [nSlot][4] linear face fluxes
+   int* line_chains;       // chains of each wave, longest first (thread per chain)
 };
 
 // true once a march has met its tolerance: every later kernel of the step
@@ -86,6 +94,14 @@ void launch_update(const DeviceState& d, const double* qold, double* qnew, doubl
 void launch_adi_init(const DeviceState& d, cudaStream_t st);
 void launch_dq_update(const DeviceState& d, cudaStream_t st);
 // launchers (adi.cu)
+// launchers (mixed.cu): FP64 residual + FP32 Jacobian/ADI defect correction
+void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st);
+void launch_mx_init(const DeviceState& d, cudaStream_t st);
+void launch_mx_assemble(const DeviceState& d, cudaStream_t st);
+void launch_mx_lines(const DeviceState& d, int first, int count, cudaStream_t st);
+void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
+void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
+void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);

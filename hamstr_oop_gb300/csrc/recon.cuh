@@ -1,0 +1,294 @@
+// ##################################################################
+//
+// recon.cuh -- chain stencil gather and reconstructions along a chain
+//
+// Shared by the FP64 path (rhs.cu, T = double: the reference's arithmetic
+// and order, bit-identical) and the mixed-precision path (mixed.cu, the
+// linearised reconstruction with T = float).  Every literal goes through
+// T(...), so the double instantiation is exactly the reference's
+// expression while the float one stays in single precision.
+// ##################################################################
+#ifndef HAMSTR_GPU_RECON_CUH
+#define HAMSTR_GPU_RECON_CUH
+
+#include "device_state.h"
+#include "plan.h"
+
+namespace hamstr {
+
+constexpr double kTh = 0.3333333333333333e+00;   // THIRD (utils.h:52)
+constexpr double kEps = 1e-10;                  // computeRHS.cpp:271
+
+__device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
+{
+   const double2 a = *reinterpret_cast<const double2*>(p);
+   const double2 b = *reinterpret_cast<const double2*>(p + 2);
+   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+__device__ __forceinline__ void ld4(const float* __restrict__ p, float (&v)[4])
+{
+   const float4 a = *reinterpret_cast<const float4*>(p);
+   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+
+__device__ __forceinline__ void st4(double* __restrict__ p, const double (&v)[4])
+{
+   *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+   *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+
+__device__ __forceinline__ void st4(float* __restrict__ p, const float (&v)[4])
+{
+   *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// stencil entry value (computeRHS.cpp:154-260), and with dqv also the dq
+// entry (computeLinearRHS.cpp:148-276); q is read in FP64 and rounded to T
+template <typename T, bool DQ>
+__device__ __forceinline__ void load_sten(const DeviceState& d, const T* __restrict__ dqv, int idx, T (&f)[4],
+                                          T (&df)[4])
+{
+   const int4 e = d.sten[idx];
+   if (e.y == STEN_CELL) {
+      double s[4];
+      ld4(d.q + 4 * e.x, s);
+#pragma unroll
+      for (int k = 0; k < 4; k++) f[k] = T(s[k]);
+      if (DQ) ld4(dqv + 4 * e.x, df);
+   } else if (e.y == STEN_WALL) {
+      const double4 R = d.refl[e.z];
+      const T rx = T(R.x), ry = T(R.y), rz = T(R.z), rw = T(R.w);
+      double s[4];
+      ld4(d.q + 4 * e.x, s);
+      const T s0 = T(s[0]), s1 = T(s[1]), s2 = T(s[2]), s3 = T(s[3]);
+      f[0] = s0;
+      f[1] = (s1 * rx + s2 * ry);
+      f[2] = (s1 * rz + s2 * rw);
+      f[3] = s3;
+      if (DQ) {
+         T t[4];
+         ld4(dqv + 4 * e.x, t);
+         df[0] = t[0];
+         df[1] = (t[1] * rx + t[2] * ry);
+         df[2] = (t[1] * rz + t[2] * rw);
+         df[3] = t[3];
+      }
+   } else {
+      f[0] = T(d.fc.rinf);
+      f[1] = T(d.fs1);
+      f[2] = T(d.fs2);
+      f[3] = T(d.fc.einf);
+      if (DQ) { df[0] = T(0); df[1] = T(0); df[2] = T(0); df[3] = T(0); }
+   }
+}
+
+// MUSCL face states for one component from f[n-1..n+2]
+// (reconstruction.cpp:170-183): left state of slot n, right of slot n+1
+__device__ __forceinline__ void muscl2(double fm1, double f0, double fp1, double fp2, double& ql_n, double& qr_n1)
+{
+   const double qt = 0.25;
+   const double thm = 1.0 - kTh, thp = 1.0 + kTh;
+   const double f2m = f0 - fm1, f20 = fp1 - f0, f2p = fp2 - fp1;
+   {
+      const double a1 = 3.0 * (f20 * f2m + kEps);
+      const double a2 = 2.0 * (f20 - f2m) * (f20 - f2m) + a1;
+      const double f3qt = qt * (a1 / a2);
+      ql_n = f0 + f3qt * (thm * f2m + thp * f20);
+   }
+   {
+      const double a1 = 3.0 * (f2p * f20 + kEps);
+      const double a2 = 2.0 * (f2p - f20) * (f2p - f20) + a1;
+      const double f3qt = qt * (a1 / a2);
+      qr_n1 = fp1 - f3qt * (thp * f20 + thm * f2p);
+   }
+}
+
+// MUSCL_DERIV for one component (reconstruction.cpp:328-349)
+template <typename T>
+__device__ __forceinline__ void muscl_deriv2(T fm1, T f0, T fp1, T fp2, T dm1, T d0, T dp1, T dp2, T& ql_n, T& qr_n1)
+{
+   const T qt = T(0.25);
+   const T thm = T(1.0 - kTh), thp = T(1.0 + kTh), eps = T(kEps);
+   const T f2m = f0 - fm1, f20 = fp1 - f0, f2p = fp2 - fp1;
+   {
+      // slot n: f2i = f20, f2i1 = f2m
+      const T df2i = dp1 - d0, df2i1 = d0 - dm1;
+      const T a1 = T(3.0) * (f20 * f2m + eps);
+      const T da1 = T(3.0) * (df2i * f2m + f20 * df2i1);
+      const T a2 = T(2.0) * (f20 - f2m) * (f20 - f2m) + a1;
+      const T da2 = T(2.0 * 2.0) * (f20 - f2m) * (df2i - df2i1) + da1;
+      const T f3i = a1 / a2;
+      const T df3i = da1 / a2 - a1 * da2 / (a2 * a2);
+      const T f3qt = qt * f3i, df3qt = qt * df3i;
+      ql_n = d0 + df3qt * (thm * f2m + thp * f20) + f3qt * (thm * df2i1 + thp * df2i);
+   }
+   {
+      // slot n+1: f2i = f2p, f2i1 = f20
+      const T df2i = dp2 - dp1, df2i1 = dp1 - d0;
+      const T a1 = T(3.0) * (f2p * f20 + eps);
+      const T da1 = T(3.0) * (df2i * f20 + f2p * df2i1);
+      const T a2 = T(2.0) * (f2p - f20) * (f2p - f20) + a1;
+      const T da2 = T(2.0 * 2.0) * (f2p - f20) * (df2i - df2i1) + da1;
+      const T f3i = a1 / a2;
+      const T df3i = da1 / a2 - a1 * da2 / (a2 * a2);
+      const T f3qt = qt * f3i, df3qt = qt * df3i;
+      qr_n1 = dp1 - df3qt * (thp * f20 + thm * f2p) - f3qt * (thp * df2i1 + thm * df2i);
+   }
+}
+
+// WENO5 (reconstruction.cpp:193-239); pow(x, 1) is x
+__device__ __forceinline__ double weno5(double a, double b, double c, double d, double e)
+{
+   const double epsw = 1e-15;
+   const double b1 = 13. / 12., b2 = 1. / 6.;
+   const double djm1 = a - 2. * b + c;
+   const double ejm1 = a - 4. * b + 3. * c;
+   const double dj = b - 2. * c + d;
+   const double ej = b - d;
+   const double djp1 = c - 2. * d + e;
+   const double ejp1 = 3. * c - 4. * d + e;
+   const double dis0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1 + epsw;
+   const double dis1 = b1 * dj * dj + 0.25 * ej * ej + epsw;
+   const double dis2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1 + epsw;
+   const double q30 = 2. * a - 7. * b + 11. * c;
+   const double q31 = -b + 5. * c + 2. * d;
+   const double q32 = 2. * c + 5. * d - e;
+   const double d01 = dis0 / dis1;
+   const double d02 = dis0 / dis2;
+   const double a1ba0 = 6. * d01;
+   const double a2ba0 = 3. * d02;
+   const double w0 = 1.0 / (1.0 + a1ba0 + a2ba0);
+   const double w1 = a1ba0 * w0;
+   const double w2 = 1. - w0 - w1;
+   return b2 * (w0 * q30 + w1 * q31 + w2 * q32);
+}
+
+// WENO_5 linearisation (reconstruction.cpp:358-462); the linear residual
+// passes eps = 1e-10 (computeLinearRHS.cpp:286,292)
+template <typename T>
+__device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, T c_d, T d_d, T e_d)
+{
+   const T epsw = T(1e-10);
+   const T b1 = T(13. / 12.), b2 = T(1. / 6.);
+   const T djm1 = a - T(2.) * b + c;
+   const T ejm1 = a - T(4.) * b + T(3.) * c;
+   const T dj = b - T(2.) * c + d;
+   const T ej = b - d;
+   const T djp1 = c - T(2.) * d + e;
+   const T ejp1 = T(3.) * c - T(4.) * d + e;
+   const T dis0 = b1 * djm1 * djm1 + T(0.25) * ejm1 * ejm1 + epsw;
+   const T dis1 = b1 * dj * dj + T(0.25) * ej * ej + epsw;
+   const T dis2 = b1 * djp1 * djp1 + T(0.25) * ejp1 * ejp1 + epsw;
+   const T q30 = T(2.) * a - T(7.) * b + T(11.) * c;
+   const T q31 = -b + T(5.) * c + T(2.) * d;
+   const T q32 = T(2.) * c + T(5.) * d - e;
+   const T d01 = dis0 / dis1;
+   const T d02 = dis0 / dis2;
+   const T a1ba0 = T(6.) * d01;
+   const T a2ba0 = T(3.) * d02;
+   const T w0 = T(1.0) / (T(1.0) + a1ba0 + a2ba0);
+   const T w1 = a1ba0 * w0;
+   const T w2 = T(1.) - w0 - w1;
+   const T djm1_d = a_d - T(2.) * b_d + c_d;
+   const T ejm1_d = a_d - T(4.) * b_d + T(3.) * c_d;
+   const T dj_d = b_d - T(2.) * c_d + d_d;
+   const T ej_d = b_d - d_d;
+   const T djp1_d = c_d - T(2.) * d_d + e_d;
+   const T ejp1_d = T(3.) * c_d - T(4.) * d_d + e_d;
+   const T q30_d = T(2.) * a_d - T(7.) * b_d + T(11.) * c_d;
+   const T q31_d = -b_d + T(5.) * c_d + T(2.) * d_d;
+   const T q32_d = T(2.) * c_d + T(5.) * d_d - e_d;
+   const T term1 = b2 * w0 * q30_d;
+   const T term2 = b2 * w1 * q31_d;
+   const T term3 = b2 * w2 * q32_d;
+   const T dbeta0 = b1 * T(2) * djm1 * djm1_d + T(0.25) * T(2) * ejm1 * ejm1_d;
+   const T dbeta1 = b1 * T(2) * dj * dj_d + T(0.25) * T(2) * ej * ej_d;
+   const T dbeta2 = b1 * T(2) * djp1 * djp1_d + T(0.25) * T(2) * ejp1 * ejp1_d;
+   const T beta0 = dis0, beta1 = dis1, beta2 = dis2;
+   const T dw0_down = beta1 * beta2 + T(6) * beta0 * beta2 + T(3) * beta0 * beta1;
+   const T dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
+   const T dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
+                                       + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
+   const T dw0 = (dw0_up_1 - dw0_up_2) / (dw0_down * dw0_down);
+   const T dw1_up_1 = T(6) * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
+   const T dw1_up_2 = T(6) * dw0_up_2 / beta1 * beta0;
+   const T dw1 = (dw1_up_1 - dw1_up_2) / (dw0_down * dw0_down);
+   const T dw2_up_1 = T(3) * (dbeta0 * beta1 + beta0 * dbeta1) * dw0_down;
+   const T dw2_up_2 = T(3) * dw0_up_2 / beta2 * beta0;
+   const T dw2 = (dw2_up_1 - dw2_up_2) / (dw0_down * dw0_down);
+   return term1 + term2 + term3 + b2 * dw0 * q30 + b2 * dw1 * q31 + b2 * dw2 * q32;
+}
+
+// reconstructed states at the two sides of a face slot, FP64
+// (computeRHS.cpp:266-304)
+template <int ORDER>
+__device__ __forceinline__ void face_states(const DeviceState& d, int n, bool swap, double (&L)[4], double (&R)[4])
+{
+   double qln[4], qrn1[4], dummy[4];
+   if (ORDER == 1) {
+      load_sten<double, false>(d, nullptr, n, qln, dummy);
+      load_sten<double, false>(d, nullptr, n + 1, qrn1, dummy);
+   } else if (ORDER == 3) {
+      double fm1[4], f0[4], fp1[4], fp2[4];
+      load_sten<double, false>(d, nullptr, n - 1, fm1, dummy);
+      load_sten<double, false>(d, nullptr, n, f0, dummy);
+      load_sten<double, false>(d, nullptr, n + 1, fp1, dummy);
+      load_sten<double, false>(d, nullptr, n + 2, fp2, dummy);
+#pragma unroll
+      for (int k = 0; k < 4; k++) muscl2(fm1[k], f0[k], fp1[k], fp2[k], qln[k], qrn1[k]);
+   } else {
+      double f[6][4];
+#pragma unroll
+      for (int j = 0; j < 6; j++) load_sten<double, false>(d, nullptr, n - 2 + j, f[j], dummy);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+         qln[k] = weno5(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k]);
+         qrn1[k] = weno5(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k]);
+      }
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      L[k] = swap ? qln[k] : qrn1[k];
+      R[k] = swap ? qrn1[k] : qln[k];
+   }
+}
+
+// linearised states (computeLinearRHS.cpp:281-315) in T, dq from dqv
+template <int ORDER, typename T>
+__device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __restrict__ dqv, int n, bool swap,
+                                             T (&L)[4], T (&R)[4])
+{
+   T qln[4], qrn1[4];
+   if (ORDER == 1) {
+      T f[4];
+      load_sten<T, true>(d, dqv, n, f, qln);
+      load_sten<T, true>(d, dqv, n + 1, f, qrn1);
+   } else if (ORDER == 3) {
+      T f[4][4], df[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) load_sten<T, true>(d, dqv, n - 1 + j, f[j], df[j]);
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+         muscl_deriv2<T>(f[0][k], f[1][k], f[2][k], f[3][k], df[0][k], df[1][k], df[2][k], df[3][k], qln[k], qrn1[k]);
+   } else {
+      T f[6][4], df[6][4];
+#pragma unroll
+      for (int j = 0; j < 6; j++) load_sten<T, true>(d, dqv, n - 2 + j, f[j], df[j]);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+         qln[k] = weno5_deriv<T>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k], df[0][k], df[1][k], df[2][k],
+                                 df[3][k], df[4][k]);
+         qrn1[k] = weno5_deriv<T>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], df[5][k], df[4][k], df[3][k],
+                                  df[2][k], df[1][k]);
+      }
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      L[k] = swap ? qln[k] : qrn1[k];
+      R[k] = swap ? qrn1[k] : qln[k];
+   }
+}
+
+}  // namespace hamstr
+#endif

@@ -24,6 +24,7 @@
 // ##################################################################
 #include "device_state.h"
 #include "plan.h"
+#include "recon.cuh"
 #include "roe.cuh"
 
 namespace hamstr {
@@ -31,261 +32,6 @@ namespace hamstr {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr double kTh = 0.3333333333333333e+00;   // THIRD (utils.h:52)
-constexpr double kThm = 1.0 - kTh;
-constexpr double kThp = 1.0 + kTh;
-constexpr double kEps = 1e-10;                  // computeRHS.cpp:271
-
-__device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
-{
-   const double2 a = *reinterpret_cast<const double2*>(p);
-   const double2 b = *reinterpret_cast<const double2*>(p + 2);
-   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-}
-
-__device__ __forceinline__ void st4(double* __restrict__ p, const double (&v)[4])
-{
-   *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
-   *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
-}
-
-// stencil entry value (computeRHS.cpp:154-260); with DQ also the dq
-// entry (computeLinearRHS.cpp:148-276)
-template <bool DQ>
-__device__ __forceinline__ void load_sten(const DeviceState& d, int idx, double (&f)[4], double (&df)[4])
-{
-   const int4 e = d.sten[idx];
-   if (e.y == STEN_CELL) {
-      ld4(d.q + 4 * e.x, f);
-      if (DQ) ld4(d.dq + 4 * e.x, df);
-   } else if (e.y == STEN_WALL) {
-      const double4 R = d.refl[e.z];
-      double s[4];
-      ld4(d.q + 4 * e.x, s);
-      f[0] = s[0];
-      f[1] = (s[1] * R.x + s[2] * R.y);
-      f[2] = (s[1] * R.z + s[2] * R.w);
-      f[3] = s[3];
-      if (DQ) {
-         ld4(d.dq + 4 * e.x, s);
-         df[0] = s[0];
-         df[1] = (s[1] * R.x + s[2] * R.y);
-         df[2] = (s[1] * R.z + s[2] * R.w);
-         df[3] = s[3];
-      }
-   } else {
-      f[0] = d.fc.rinf;
-      f[1] = d.fs1;
-      f[2] = d.fs2;
-      f[3] = d.fc.einf;
-      if (DQ) { df[0] = 0.0; df[1] = 0.0; df[2] = 0.0; df[3] = 0.0; }
-   }
-}
-
-// MUSCL face states for one component from f[n-1..n+2]
-// (reconstruction.cpp:170-183): left of slot n and right of slot n+1.
-__device__ __forceinline__ void muscl2(double fm1, double f0, double fp1, double fp2, double& ql_n, double& qr_n1)
-{
-   const double qt = 0.25;
-   const double f2m = f0 - fm1, f20 = fp1 - f0, f2p = fp2 - fp1;
-   {
-      const double a1 = 3.0 * (f20 * f2m + kEps);
-      const double a2 = 2.0 * (f20 - f2m) * (f20 - f2m) + a1;
-      const double f3qt = qt * (a1 / a2);
-      ql_n = f0 + f3qt * (kThm * f2m + kThp * f20);
-   }
-   {
-      const double a1 = 3.0 * (f2p * f20 + kEps);
-      const double a2 = 2.0 * (f2p - f20) * (f2p - f20) + a1;
-      const double f3qt = qt * (a1 / a2);
-      qr_n1 = fp1 - f3qt * (kThp * f20 + kThm * f2p);
-   }
-}
-
-// MUSCL_DERIV for one component (reconstruction.cpp:328-349)
-__device__ __forceinline__ void muscl_deriv2(double fm1, double f0, double fp1, double fp2,
-                                             double dm1, double d0, double dp1, double dp2,
-                                             double& ql_n, double& qr_n1)
-{
-   const double qt = 0.25;
-   const double f2m = f0 - fm1, f20 = fp1 - f0, f2p = fp2 - fp1;
-   {
-      // slot n: f2i = f20, f2i1 = f2m
-      const double df2i = dp1 - d0, df2i1 = d0 - dm1;
-      const double a1 = 3.0 * (f20 * f2m + kEps);
-      const double da1 = 3.0 * (df2i * f2m + f20 * df2i1);
-      const double a2 = 2.0 * (f20 - f2m) * (f20 - f2m) + a1;
-      const double da2 = 2.0 * 2.0 * (f20 - f2m) * (df2i - df2i1) + da1;
-      const double f3i = a1 / a2;
-      const double df3i = da1 / a2 - a1 * da2 / (a2 * a2);
-      const double f3qt = qt * f3i, df3qt = qt * df3i;
-      ql_n = d0 + df3qt * (kThm * f2m + kThp * f20) + f3qt * (kThm * df2i1 + kThp * df2i);
-   }
-   {
-      // slot n+1: f2i = f2p, f2i1 = f20
-      const double df2i = dp2 - dp1, df2i1 = dp1 - d0;
-      const double a1 = 3.0 * (f2p * f20 + kEps);
-      const double da1 = 3.0 * (df2i * f20 + f2p * df2i1);
-      const double a2 = 2.0 * (f2p - f20) * (f2p - f20) + a1;
-      const double da2 = 2.0 * 2.0 * (f2p - f20) * (df2i - df2i1) + da1;
-      const double f3i = a1 / a2;
-      const double df3i = da1 / a2 - a1 * da2 / (a2 * a2);
-      const double f3qt = qt * f3i, df3qt = qt * df3i;
-      qr_n1 = dp1 - df3qt * (kThp * f20 + kThm * f2p) - f3qt * (kThp * df2i1 + kThm * df2i);
-   }
-}
-
-// WENO5 (reconstruction.cpp:193-239); pow(x, 1) is x
-__device__ __forceinline__ double weno5(double a, double b, double c, double d, double e)
-{
-   const double epsw = 1e-15;
-   const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double djm1 = a - 2. * b + c;
-   const double ejm1 = a - 4. * b + 3. * c;
-   const double dj = b - 2. * c + d;
-   const double ej = b - d;
-   const double djp1 = c - 2. * d + e;
-   const double ejp1 = 3. * c - 4. * d + e;
-   const double dis0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1 + epsw;
-   const double dis1 = b1 * dj * dj + 0.25 * ej * ej + epsw;
-   const double dis2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1 + epsw;
-   const double q30 = 2. * a - 7. * b + 11. * c;
-   const double q31 = -b + 5. * c + 2. * d;
-   const double q32 = 2. * c + 5. * d - e;
-   const double d01 = dis0 / dis1;
-   const double d02 = dis0 / dis2;
-   const double a1ba0 = 6. * d01;
-   const double a2ba0 = 3. * d02;
-   const double w0 = 1.0 / (1.0 + a1ba0 + a2ba0);
-   const double w1 = a1ba0 * w0;
-   const double w2 = 1. - w0 - w1;
-   return b2 * (w0 * q30 + w1 * q31 + w2 * q32);
-}
-
-// WENO_5 linearisation (reconstruction.cpp:358-462); the linear residual
-// passes eps = 1e-10 (computeLinearRHS.cpp:286,292)
-__device__ __forceinline__ double weno5_deriv(double a, double b, double c, double d, double e,
-                                              double a_d, double b_d, double c_d, double d_d, double e_d)
-{
-   const double epsw = 1e-10;
-   const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double djm1 = a - 2. * b + c;
-   const double ejm1 = a - 4. * b + 3. * c;
-   const double dj = b - 2. * c + d;
-   const double ej = b - d;
-   const double djp1 = c - 2. * d + e;
-   const double ejp1 = 3. * c - 4. * d + e;
-   const double dis0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1 + epsw;
-   const double dis1 = b1 * dj * dj + 0.25 * ej * ej + epsw;
-   const double dis2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1 + epsw;
-   const double q30 = 2. * a - 7. * b + 11. * c;
-   const double q31 = -b + 5. * c + 2. * d;
-   const double q32 = 2. * c + 5. * d - e;
-   const double d01 = dis0 / dis1;
-   const double d02 = dis0 / dis2;
-   const double a1ba0 = 6. * d01;
-   const double a2ba0 = 3. * d02;
-   const double w0 = 1.0 / (1.0 + a1ba0 + a2ba0);
-   const double w1 = a1ba0 * w0;
-   const double w2 = 1. - w0 - w1;
-   const double djm1_d = a_d - 2. * b_d + c_d;
-   const double ejm1_d = a_d - 4. * b_d + 3. * c_d;
-   const double dj_d = b_d - 2. * c_d + d_d;
-   const double ej_d = b_d - d_d;
-   const double djp1_d = c_d - 2. * d_d + e_d;
-   const double ejp1_d = 3. * c_d - 4. * d_d + e_d;
-   const double q30_d = 2. * a_d - 7. * b_d + 11. * c_d;
-   const double q31_d = -b_d + 5. * c_d + 2. * d_d;
-   const double q32_d = 2. * c_d + 5. * d_d - e_d;
-   const double term1 = b2 * w0 * q30_d;
-   const double term2 = b2 * w1 * q31_d;
-   const double term3 = b2 * w2 * q32_d;
-   const double dbeta0 = b1 * 2 * djm1 * djm1_d + 0.25 * 2 * ejm1 * ejm1_d;
-   const double dbeta1 = b1 * 2 * dj * dj_d + 0.25 * 2 * ej * ej_d;
-   const double dbeta2 = b1 * 2 * djp1 * djp1_d + 0.25 * 2 * ejp1 * ejp1_d;
-   const double beta0 = dis0, beta1 = dis1, beta2 = dis2;
-   const double dw0_down = beta1 * beta2 + 6 * beta0 * beta2 + 3 * beta0 * beta1;
-   const double dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
-   const double dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + 6 * (dbeta0 * beta2 + beta0 * dbeta2)
-                                            + 3 * (dbeta0 * beta1 + beta0 * dbeta1));
-   const double dw0 = (dw0_up_1 - dw0_up_2) / (dw0_down * dw0_down);
-   const double dw1_up_1 = 6 * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
-   const double dw1_up_2 = 6 * dw0_up_2 / beta1 * beta0;
-   const double dw1 = (dw1_up_1 - dw1_up_2) / (dw0_down * dw0_down);
-   const double dw2_up_1 = 3 * (dbeta0 * beta1 + beta0 * dbeta1) * dw0_down;
-   const double dw2_up_2 = 3 * dw0_up_2 / beta2 * beta0;
-   const double dw2 = (dw2_up_1 - dw2_up_2) / (dw0_down * dw0_down);
-   return term1 + term2 + term3 + b2 * dw0 * q30 + b2 * dw1 * q31 + b2 * dw2 * q32;
-}
-
-// reconstructed states at the two sides of a face slot (computeRHS.cpp:266-304)
-template <int ORDER>
-__device__ __forceinline__ void face_states(const DeviceState& d, int n, bool swap, double (&L)[4], double (&R)[4])
-{
-   double qln[4], qrn1[4], dummy[4];
-   if (ORDER == 1) {
-      load_sten<false>(d, n, qln, dummy);
-      load_sten<false>(d, n + 1, qrn1, dummy);
-   } else if (ORDER == 3) {
-      double fm1[4], f0[4], fp1[4], fp2[4];
-      load_sten<false>(d, n - 1, fm1, dummy);
-      load_sten<false>(d, n, f0, dummy);
-      load_sten<false>(d, n + 1, fp1, dummy);
-      load_sten<false>(d, n + 2, fp2, dummy);
-#pragma unroll
-      for (int k = 0; k < 4; k++) muscl2(fm1[k], f0[k], fp1[k], fp2[k], qln[k], qrn1[k]);
-   } else {
-      double f[6][4];
-#pragma unroll
-      for (int j = 0; j < 6; j++) load_sten<false>(d, n - 2 + j, f[j], dummy);
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-         qln[k] = weno5(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k]);
-         qrn1[k] = weno5(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k]);
-      }
-   }
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      L[k] = swap ? qln[k] : qrn1[k];
-      R[k] = swap ? qrn1[k] : qln[k];
-   }
-}
-
-// linearised states (computeLinearRHS.cpp:281-315)
-template <int ORDER>
-__device__ __forceinline__ void face_dstates(const DeviceState& d, int n, bool swap, double (&L)[4], double (&R)[4])
-{
-   double qln[4], qrn1[4];
-   if (ORDER == 1) {
-      double f[4];
-      load_sten<true>(d, n, f, qln);
-      load_sten<true>(d, n + 1, f, qrn1);
-   } else if (ORDER == 3) {
-      double f[4][4], df[4][4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) load_sten<true>(d, n - 1 + j, f[j], df[j]);
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-         muscl_deriv2(f[0][k], f[1][k], f[2][k], f[3][k], df[0][k], df[1][k], df[2][k], df[3][k], qln[k], qrn1[k]);
-   } else {
-      double f[6][4], df[6][4];
-#pragma unroll
-      for (int j = 0; j < 6; j++) load_sten<true>(d, n - 2 + j, f[j], df[j]);
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-         qln[k] = weno5_deriv(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k],
-                              df[0][k], df[1][k], df[2][k], df[3][k], df[4][k]);
-         qrn1[k] = weno5_deriv(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k],
-                               df[5][k], df[4][k], df[3][k], df[2][k], df[1][k]);
-      }
-   }
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      L[k] = swap ? qln[k] : qrn1[k];
-      R[k] = swap ? qrn1[k] : qln[k];
-   }
-}
-
 template <int ORDER, bool JAC>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
@@ -316,7 +62,7 @@ __global__ void __launch_bounds__(kThreads) lin_face_kernel(DeviceState d)
    if (s >= d.nSlot || halted(d)) return;
    const int4 sl = d.slot[s];
    double dL[4], dR[4];
-   face_dstates<ORDER>(d, sl.x, (sl.w & 1) != 0, dL, dR);
+   face_dstates<ORDER, double>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
    const double* m = d.ff + 32 * (size_t)(sl.w >> 1);
    double g[4];
 #pragma unroll

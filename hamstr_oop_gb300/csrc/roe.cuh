@@ -223,5 +223,102 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    return true;
 }
 
+// The same frozen-eigenvalue Jacobian evaluated entirely in T (used with
+// T = float by the mixed-precision defect correction, where the Jacobian is
+// only the approximate operator; the FP64 path uses roe_face<true>).
+template <typename T>
+__device__ __forceinline__ void roe_jacobian_only(T nxd, T nyd, const T (&ql)[4], const T (&qr)[4], T gam,
+                                                  T* __restrict__ lm, T* __restrict__ rm)
+{
+   const T gm1 = gam - T(1);
+   const T area = sqrt(nxd * nxd + nyd * nyd);
+   const T rol = ql[0], ul = ql[1] / ql[0], vl = ql[2] / ql[0];
+   const T pl = gm1 * (ql[3] - T(0.5) * rol * (ul * ul + vl * vl));
+   const T hl = (ql[3] + pl) / rol;
+   const T ror = qr[0], ur = qr[1] / qr[0], vr = qr[2] / qr[0];
+   const T pr = gm1 * (qr[3] - T(0.5) * ror * (ur * ur + vr * vr));
+   const T hr = (qr[3] + pr) / ror;
+   const T fact = sqrt(ror / rol);
+   const T A = T(1) / (T(1) + fact), B = fact / (T(1) + fact);
+   const T robar = rol * fact;
+   const T ubar = ul * A + ur * B, vbar = vl * A + vr * B, hbar = hl * A + hr * B;
+   const T cbar = sqrt(gm1 * (hbar - T(0.5) * (ubar * ubar + vbar * vbar)));
+   const T nxj = nxd / area, nyj = nyd / area;
+   const T uconlj = ul * nxj + vl * nyj, uconrj = ur * nxj + vr * nyj;
+   const T uconbarj = ubar * nxj + vbar * nyj;
+   const T e1 = fabs(uconbarj), e2 = fabs(uconbarj + cbar), e3 = fabs(uconbarj - cbar);
+   const T t1 = -e1 + T(0.5) * (e2 + e3), t2 = T(0.5) * (e2 - e3), t2rb = t2 * robar;
+   const T irl = T(1) / rol, irr = T(1) / ror;
+   const T du0l = -ul / rol, dv0l = -vl / rol, du0r = -ur / ror, dv0r = -vr / ror;
+   const T dp0l = T(0.5) * gm1 * (ul * ul + vl * vl), dp1l = -gm1 * ul, dp2l = -gm1 * vl;
+   const T dp0r = T(0.5) * gm1 * (ur * ur + vr * vr), dp1r = -gm1 * ur, dp2r = -gm1 * vr;
+   const T dc0l = -uconlj / rol, dc1l = nxj / rol, dc2l = nyj / rol;
+   const T dc0r = -uconrj / ror, dc1r = nxj / ror, dc2r = nyj / ror;
+   const T mt1 = -t1;
+   T D1l[4], D2l[4], D1r[4], D2r[4];
+   D1l[0] = mt1 * dp0l / cbar / cbar - t2rb * dc0l / cbar;
+   D1l[1] = mt1 * dp1l / cbar / cbar - t2rb * dc1l / cbar;
+   D1l[2] = mt1 * dp2l / cbar / cbar - t2rb * dc2l / cbar;
+   D1l[3] = mt1 * gm1 / cbar / cbar;
+   D2l[0] = mt1 * dc0l * robar - t2 * dp0l / cbar;
+   D2l[1] = mt1 * dc1l * robar - t2 * dp1l / cbar;
+   D2l[2] = mt1 * dc2l * robar - t2 * dp2l / cbar;
+   D2l[3] = -(t2 * gm1 / cbar);
+   D1r[0] = t1 * dp0r / cbar / cbar + t2rb * dc0r / cbar;
+   D1r[1] = t1 * dp1r / cbar / cbar + t2rb * dc1r / cbar;
+   D1r[2] = t1 * dp2r / cbar / cbar + t2rb * dc2r / cbar;
+   D1r[3] = t1 * gm1 / cbar / cbar;
+   D2r[0] = t1 * dc0r * robar + t2 * dp0r / cbar;
+   D2r[1] = t1 * dc1r * robar + t2 * dp1r / cbar;
+   D2r[2] = t1 * dc2r * robar + t2 * dp2r / cbar;
+   D2r[3] = t2 * gm1 / cbar;
+   const T el = ql[3] + pl, er = qr[3] + pr;
+   const T rcl = rol * uconlj, rcr = ror * uconrj;
+   T L1[16], R1[16];
+   L1[0] = uconlj + rol * dc0l;  L1[1] = rol * dc1l;  L1[2] = rol * dc2l;  L1[3] = T(0);
+   L1[4] = uconlj * ul + rol * dc0l * ul + rcl * du0l + nxj * dp0l;
+   L1[5] = rol * dc1l * ul + rcl * irl + nxj * dp1l;
+   L1[6] = rol * dc2l * ul + nxj * dp2l;
+   L1[7] = nxj * gm1;
+   L1[8] = uconlj * vl + rol * dc0l * vl + rcl * dv0l + nyj * dp0l;
+   L1[9] = rol * dc1l * vl + nyj * dp1l;
+   L1[10] = rol * dc2l * vl + rcl * irl + nyj * dp2l;
+   L1[11] = nyj * gm1;
+   L1[12] = dp0l * uconlj + el * dc0l;  L1[13] = dp1l * uconlj + el * dc1l;
+   L1[14] = dp2l * uconlj + el * dc2l;  L1[15] = (T(1) + gm1) * uconlj;
+   R1[0] = uconrj + ror * dc0r;  R1[1] = ror * dc1r;  R1[2] = ror * dc2r;  R1[3] = T(0);
+   R1[4] = uconrj * ur + ror * dc0r * ur + rcr * du0r + nxj * dp0r;
+   R1[5] = ror * dc1r * ur + rcr * irr + nxj * dp1r;
+   R1[6] = ror * dc2r * ur + nxj * dp2r;
+   R1[7] = nxj * gm1;
+   R1[8] = uconrj * vr + ror * dc0r * vr + rcr * dv0r + nyj * dp0r;
+   R1[9] = ror * dc1r * vr + nyj * dp1r;
+   R1[10] = ror * dc2r * vr + rcr * irr + nyj * dp2r;
+   R1[11] = nyj * gm1;
+   R1[12] = dp0r * uconrj + er * dc0r;  R1[13] = dp1r * uconrj + er * dc1r;
+   R1[14] = dp2r * uconrj + er * dc2r;  R1[15] = (T(1) + gm1) * uconrj;
+   const T rowc[4] = {T(0), ubar, vbar, hbar};
+   const T rown[4] = {T(0), nxj, nyj, uconbarj};
+#pragma unroll
+   for (int rI = 0; rI < 4; rI++) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+         T ml, mr;
+         if (rI == 0) {
+            ml = (c == 0) ? (-e1 + D1l[0]) : D1l[c];
+            mr = (c == 0) ? (e1 + D1r[0]) : D1r[c];
+         } else if (c == rI) {
+            ml = -e1 + D1l[c] * rowc[rI] + D2l[c] * rown[rI];
+            mr = e1 + D1r[c] * rowc[rI] + D2r[c] * rown[rI];
+         } else {
+            ml = D1l[c] * rowc[rI] + D2l[c] * rown[rI];
+            mr = D1r[c] * rowc[rI] + D2r[c] * rown[rI];
+         }
+         lm[4 * rI + c] = T(0.5) * (L1[4 * rI + c] - ml) * area;
+         rm[4 * rI + c] = T(0.5) * (R1[4 * rI + c] - mr) * area;
+      }
+   }
+}
+
 }  // namespace hamstr
 #endif

@@ -74,6 +74,7 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_march": (i, [vp, i, d, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "hamstr_gpu_stream": (vp, [vp]),
         "hamstr_gpu_step_explicit": (i, [vp, i, vp]),
+        "hamstr_gpu_set_precision": (i, [vp, i]),
         "hamstr_gpu_update_solution": (i, [vp, cp, cp, d]),
         "hamstr_gpu_enqueue_steps": (i, [vp, i]),
         "hamstr_gpu_sync": (i, [vp]),
@@ -218,6 +219,11 @@ class GpuSolver:
 
     _DW = {"q": ("nCell", 4), "qt": ("nCell", 4), "r": ("nCell", 4), "r0": ("nCell", 4), "dq": ("nCell", 4),
            "sigma": ("nCell", 1), "ff": ("nFace", 32)}
+
+    def set_precision(self, mixed: bool) -> None:
+        """False: plain FP64 (bit-identical); True: FP64 residual with an FP32
+        Jacobian/ADI operator (defect correction)."""
+        _check(load().hamstr_gpu_set_precision(self.h, int(bool(mixed))))
 
     def step_explicit(self, scheme: str) -> np.ndarray:
         out = np.zeros(2)

@@ -112,6 +112,17 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
  * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
 
+/* Arithmetic of the implicit step taken by hamstr_gpu_step / _march /
+ * _enqueue_steps (no counterpart in the reference, which is FP64 only):
+ *   0 (default)  plain FP64, bit-identical to the reference;
+ *   1            defect correction: the residual (reconstruction, Roe flux,
+ *                computeRHS sums) stays FP64 and identical to the
+ *                reference, while the Roe Jacobians, the ADI line solves and
+ *                the linearised residual of the sweeps run in FP32.  The
+ *                converged state is the FP64 residual's zero; the iteration
+ *                history differs from the reference's. */
+int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
+
 /* SOLVER::stepSolution, explicit branches (march.cpp:342-377): scheme 0 is
  * "euler" (computeRHS("explicit") then q += CFL/sigma r), scheme 1 the
  * 3-stage "rk3" through the second state qt.  norms2 = the last
