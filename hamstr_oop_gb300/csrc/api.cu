@@ -94,10 +94,11 @@ struct hamstr_gpu {
       launch_rhs_cell(d, true, stream); n++;
       launch_norm_final(d, 0, check_tol, stream); n++;
       launch_mx_init(d, stream); n++;
+      launch_mx_assemble(d, stream); n++;
+      launch_mx_factor(d, stream); n++;
       for (int s = 0; s < msweep; s++) {
-         launch_mx_assemble(d, stream); n++;
          for (int w = 0; w < plan.nWave; w++) {
-            launch_mx_lines(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
+            launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
             n++;
          }
          launch_mx_dq_update(d, stream); n++;
@@ -120,6 +121,15 @@ struct hamstr_gpu {
       if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
       if ((st = dalloc(&d.blk32, 48 * (size_t)std::max(d.nRow, 1), owned))) return st;
       if ((st = dalloc(&d.fsc32, 4 * (size_t)std::max(d.nRow, 1), owned))) return st;
+      if ((st = dalloc(&d.fac32, 80 * (size_t)std::max(d.nRow, 1), owned))) return st;
+      int nper = 0;
+      for (int c = 0; c < plan.nChain; c++) nper += plan.chain_periodic[c] ? 1 : 0;
+      if ((st = dalloc(&d.facN32, 16 * (size_t)std::max(nper, 1), owned))) return st;
+      std::vector<int> all(plan.nChain);
+      for (int c = 0; c < plan.nChain; c++) all[c] = c;
+      std::stable_sort(all.begin(), all.end(),
+                       [&](int a, int b) { return plan.chain_nrows[a] > plan.chain_nrows[b]; });
+      if ((st = upload(&d.fac_chains32, all, owned))) return st;
       if ((st = dalloc(&d.r32, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;

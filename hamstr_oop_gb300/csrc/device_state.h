@@ -70,6 +70,9 @@ struct DeviceState {
    float* ff32;            // [nSlot][32] FP32 face Jacobians
    float* blk32;           // [nRow][48] FP32 blocks, factored in place each sweep
    float* fsc32;           // [nRow][4]
+   float* fac32;           // [nRow][80] FP32 factor records
+   float* facN32;          // [periodic chains][16]
+   int* fac_chains32;      // all chains, longest first (thread per chain)
    float *r32, *r032, *dq32;   // [nCell][4]
    float* g32;             // [nSlot][4] linear face fluxes
    int* line_chains;       // chains of each wave, longest first (thread per chain)
@@ -98,7 +101,8 @@ void launch_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_init(const DeviceState& d, cudaStream_t st);
 void launch_mx_assemble(const DeviceState& d, cudaStream_t st);
-void launch_mx_lines(const DeviceState& d, int first, int count, cudaStream_t st);
+void launch_mx_factor(const DeviceState& d, cudaStream_t st);
+void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st);
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);

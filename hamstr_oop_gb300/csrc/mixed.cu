@@ -12,8 +12,8 @@
 //
 // GB300 issues FP32 about 70x faster than FP64 (64-cycle dependent FP64
 // latency against 4 for FP32), so the line solves here are one thread per
-// chain running the reference's block Thomas elimination in registers,
-// with chains of similar length sharing a warp.
+// chain running the block Thomas elimination in registers, with chains of
+// similar length sharing a warp.
 // ##################################################################
 #include "device_state.h"
 #include "plan.h"
@@ -96,256 +96,265 @@ __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
    d.blk32[t] = acc;
 }
 
-// ---------------- scalar block-tridiagonal solvers in T ----------------
-template <typename T>
-struct LUs {
-   T b11, u12, u13, u14, b21, b22, u23, u24, b31, b32, b33, u34, b41, b42, b43, b44;
+// ---------------- FP32 line solves, one thread per chain ----------------
+// The same split as the FP64 path: the block factorisation runs once per
+// step (mx_factor), each sweep replays the right-hand side (mx_solve).  One
+// thread carries a whole chain in registers (FP32 latency is 4 cycles, so
+// the recurrence is short), rows are prefetched one ahead, and products use
+// FMA since this operator is approximate by design.  Record layout per row
+// (80 floats): A, LU of B', C', fill-in a', c_{N-1} at elimination step i.
+constexpr int kRec = 80;
+
+struct LUf {
+   float p0, u01, u02, u03, l10, p1, u12, u13, l20, l21, p2, u23, l30, l31, l32, p3;
 };
 
-template <typename T>
-__device__ __forceinline__ LUs<T> lus_factor(const T (&b)[16])
+__device__ __forceinline__ LUf luf_factor(const float (&b)[16])
 {
-   LUs<T> u;
-   u.b11 = T(1) / b[0];
-   u.u12 = b[1] * u.b11; u.u13 = b[2] * u.b11; u.u14 = b[3] * u.b11;
-   u.b21 = b[4];
-   u.b22 = T(1) / (b[5] - u.b21 * u.u12);
-   u.u23 = (b[6] - u.b21 * u.u13) * u.b22;
-   u.u24 = (b[7] - u.b21 * u.u14) * u.b22;
-   u.b31 = b[8];
-   u.b32 = b[9] - u.b31 * u.u12;
-   u.b33 = T(1) / (b[10] - u.b31 * u.u13 - u.b32 * u.u23);
-   u.u34 = (b[11] - u.b31 * u.u14 - u.b32 * u.u24) * u.b33;
-   u.b41 = b[12];
-   u.b42 = b[13] - u.b41 * u.u12;
-   u.b43 = b[14] - u.b41 * u.u13 - u.b42 * u.u23;
-   u.b44 = T(1) / (b[15] - u.b41 * u.u14 - u.b42 * u.u24 - u.b43 * u.u34);
+   LUf u;
+   u.p0 = 1.f / b[0];
+   u.u01 = b[1] * u.p0; u.u02 = b[2] * u.p0; u.u03 = b[3] * u.p0;
+   u.l10 = b[4];
+   u.p1 = 1.f / __fmaf_rn(-u.l10, u.u01, b[5]);
+   u.u12 = __fmaf_rn(-u.l10, u.u02, b[6]) * u.p1;
+   u.u13 = __fmaf_rn(-u.l10, u.u03, b[7]) * u.p1;
+   u.l20 = b[8];
+   u.l21 = __fmaf_rn(-u.l20, u.u01, b[9]);
+   u.p2 = 1.f / __fmaf_rn(-u.l21, u.u12, __fmaf_rn(-u.l20, u.u02, b[10]));
+   u.u23 = __fmaf_rn(-u.l21, u.u13, __fmaf_rn(-u.l20, u.u03, b[11])) * u.p2;
+   u.l30 = b[12];
+   u.l31 = __fmaf_rn(-u.l30, u.u01, b[13]);
+   u.l32 = __fmaf_rn(-u.l31, u.u12, __fmaf_rn(-u.l30, u.u02, b[14]));
+   u.p3 = 1.f / __fmaf_rn(-u.l32, u.u23, __fmaf_rn(-u.l31, u.u13, __fmaf_rn(-u.l30, u.u03, b[15])));
    return u;
 }
 
-template <typename T>
-__device__ __forceinline__ void lus_solve(const LUs<T>& u, T& x0, T& x1, T& x2, T& x3)
+__device__ __forceinline__ void luf_solve(const LUf& u, float& x0, float& x1, float& x2, float& x3)
 {
-   const T d1 = x0 * u.b11;
-   const T d2 = (x1 - u.b21 * d1) * u.b22;
-   const T d3 = (x2 - u.b31 * d1 - u.b32 * d2) * u.b33;
-   const T d4 = (x3 - u.b41 * d1 - u.b42 * d2 - u.b43 * d3) * u.b44;
-   x3 = d4;
-   x2 = d3 - u.u34 * x3;
-   x1 = d2 - u.u23 * x2 - u.u24 * x3;
-   x0 = d1 - u.u12 * x1 - u.u13 * x2 - u.u14 * x3;
+   const float d0 = x0 * u.p0;
+   const float d1 = __fmaf_rn(-u.l10, d0, x1) * u.p1;
+   const float d2 = __fmaf_rn(-u.l21, d1, __fmaf_rn(-u.l20, d0, x2)) * u.p2;
+   const float d3 = __fmaf_rn(-u.l32, d2, __fmaf_rn(-u.l31, d1, __fmaf_rn(-u.l30, d0, x3))) * u.p3;
+   x3 = d3;
+   x2 = __fmaf_rn(-u.u23, x3, d2);
+   x1 = __fmaf_rn(-u.u13, x3, __fmaf_rn(-u.u12, x2, d1));
+   x0 = __fmaf_rn(-u.u03, x3, __fmaf_rn(-u.u02, x2, __fmaf_rn(-u.u01, x1, d0)));
 }
 
-template <typename T>
-__device__ __forceinline__ void lus_cols(const LUs<T>& u, T (&m)[16])
+__device__ __forceinline__ void luf_store(float* p, const LUf& u)
 {
+   const float v[16] = {u.p0, u.u01, u.u02, u.u03, u.l10, u.p1, u.u12, u.u13,
+                        u.l20, u.l21, u.p2, u.u23, u.l30, u.l31, u.l32, u.p3};
 #pragma unroll
-   for (int j = 0; j < 4; j++) lus_solve(u, m[j], m[4 + j], m[8 + j], m[12 + j]);
+   for (int m = 0; m < 16; m += 4) *reinterpret_cast<float4*>(p + m) = make_float4(v[m], v[m + 1], v[m + 2], v[m + 3]);
 }
 
-template <typename T>
-__device__ __forceinline__ void ld16(const T* p, T (&v)[16])
+__device__ __forceinline__ LUf luf_load(const float* p)
 {
+   float v[16];
 #pragma unroll
-   for (int m = 0; m < 16; m++) v[m] = p[m];
-}
-
-template <typename T>
-__device__ __forceinline__ void st16(T* p, const T (&v)[16])
-{
-#pragma unroll
-   for (int m = 0; m < 16; m++) p[m] = v[m];
-}
-
-// blockTridag4 (triSolvers.cpp:769-847), rows of 48 (A, B, C) in place
-template <typename T>
-__device__ void tridag_open(T* __restrict__ blk, T* __restrict__ f, int N)
-{
-   T cp[16], fp[4];
-   for (int i = 0; i < N; i++) {
-      T* row = blk + 48 * (size_t)i;
-      T a[16], b[16], c[16], x[4];
-      ld16(row, a);
-      ld16(row + 16, b);
-      ld16(row + 32, c);
-#pragma unroll
-      for (int k = 0; k < 4; k++) x[k] = f[4 * i + k];
-      if (i != 0) {
-#pragma unroll
-         for (int k = 0; k < 4; k++)
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-#pragma unroll
-               for (int l = 0; l < 4; l++) b[4 * k + j] -= a[4 * k + l] * cp[4 * l + j];
-#pragma unroll
-         for (int k = 0; k < 4; k++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) x[k] -= a[4 * k + j] * fp[j];
-      }
-      const LUs<T> u = lus_factor(b);
-      lus_solve(u, x[0], x[1], x[2], x[3]);
-      if (i != N - 1) lus_cols(u, c);
-      st16(row + 32, c);
-#pragma unroll
-      for (int k = 0; k < 4; k++) { f[4 * i + k] = x[k]; fp[k] = x[k]; }
-#pragma unroll
-      for (int m = 0; m < 16; m++) cp[m] = c[m];
+   for (int m = 0; m < 16; m += 4) {
+      const float4 a = *reinterpret_cast<const float4*>(p + m);
+      v[m] = a.x; v[m + 1] = a.y; v[m + 2] = a.z; v[m + 3] = a.w;
    }
-   T xn[4];
+   LUf u;
+   u.p0 = v[0]; u.u01 = v[1]; u.u02 = v[2]; u.u03 = v[3]; u.l10 = v[4]; u.p1 = v[5]; u.u12 = v[6]; u.u13 = v[7];
+   u.l20 = v[8]; u.l21 = v[9]; u.p2 = v[10]; u.u23 = v[11]; u.l30 = v[12]; u.l31 = v[13]; u.l32 = v[14]; u.p3 = v[15];
+   return u;
+}
+
+__device__ __forceinline__ void ld16f(const float* p, float (&v)[16])
+{
 #pragma unroll
-   for (int k = 0; k < 4; k++) xn[k] = f[4 * (N - 1) + k];
-   for (int i = N - 2; i >= 0; i--) {
-      T c[16], x[4];
-      ld16(blk + 48 * (size_t)i + 32, c);
-#pragma unroll
-      for (int k = 0; k < 4; k++) x[k] = f[4 * i + k];
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-#pragma unroll
-         for (int j = 0; j < 4; j++) x[k] -= c[4 * k + j] * xn[j];
-#pragma unroll
-      for (int k = 0; k < 4; k++) { f[4 * i + k] = x[k]; xn[k] = x[k]; }
+   for (int m = 0; m < 16; m += 4) {
+      const float4 a = *reinterpret_cast<const float4*>(p + m);
+      v[m] = a.x; v[m + 1] = a.y; v[m + 2] = a.z; v[m + 3] = a.w;
    }
 }
 
-// blockTridagPeriodic4 (triSolvers.cpp:850-1046), rows of 48 in place;
-// a(i) is overwritten by the fill-in column as in the reference
-template <typename T>
-__device__ void tridag_periodic(T* __restrict__ blk, T* __restrict__ f, int N)
+__device__ __forceinline__ void st16f(float* p, const float (&v)[16])
 {
-   T cp[16], ap[16], fp[4];
-   for (int i = 0; i < N; i++) {
-      T* row = blk + 48 * (size_t)i;
-      T a[16], b[16], c[16], x[4];
-      ld16(row, a);
-      ld16(row + 16, b);
-      ld16(row + 32, c);
 #pragma unroll
-      for (int k = 0; k < 4; k++) x[k] = f[4 * i + k];
-      if (i != 0) {
+   for (int m = 0; m < 16; m += 4) *reinterpret_cast<float4*>(p + m) = make_float4(v[m], v[m + 1], v[m + 2], v[m + 3]);
+}
+
+// M <- LU^{-1} M, column by column
+__device__ __forceinline__ void luf_cols(const LUf& u, float (&m)[16])
+{
 #pragma unroll
-         for (int k = 0; k < 4; k++)
+   for (int j = 0; j < 4; j++) luf_solve(u, m[j], m[4 + j], m[8 + j], m[12 + j]);
+}
+
+// out = acc - M * X (4x4), acc = nullptr for 0
+__device__ __forceinline__ void mm_sub(const float (&M)[16], const float (&X)[16], float (&acc)[16])
+{
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+   for (int k = 0; k < 4; k++)
 #pragma unroll
-               for (int l = 0; l < 4; l++) b[4 * k + j] -= a[4 * k + l] * cp[4 * l + j];
+      for (int j = 0; j < 4; j++) {
+         float a = acc[4 * k + j];
 #pragma unroll
-         for (int k = 0; k < 4; k++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) x[k] -= a[4 * k + j] * fp[j];
-         T t[16];
-#pragma unroll
-         for (int k = 0; k < 4; k++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-               T acc = T(0);
-#pragma unroll
-               for (int l = 0; l < 4; l++) acc -= a[4 * k + l] * ap[4 * l + j];
-               t[4 * k + j] = acc;
-            }
-#pragma unroll
-         for (int m = 0; m < 16; m++) a[m] = t[m];
+         for (int l = 0; l < 4; l++) a = __fmaf_rn(-M[4 * k + l], X[4 * l + j], a);
+         acc[4 * k + j] = a;
       }
-      const LUs<T> u = lus_factor(b);
-      lus_solve(u, x[0], x[1], x[2], x[3]);
-      if (i != N - 2) {
-         lus_cols(u, c);
-         lus_cols(u, a);
+}
+
+__global__ void __launch_bounds__(64) mx_factor_kernel(DeviceState d, int count)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= count || halted(d)) return;
+   const int ich = d.fac_chains32[t];
+   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
+   const bool per = d.chain_periodic[ich] != 0;
+   const float* blk = d.blk32 + 48 * (size_t)row0;
+   float* fac = d.fac32 + (size_t)kRec * row0;
+   float A[16], B[16], C[16], cp[16], ap[16];
+   ld16f(blk, A);
+   ld16f(blk + 16, B);
+   ld16f(blk + 32, C);
+   for (int i = 0; i < N; i++) {
+      float An[16], Bn[16], Cn[16];
+      if (i + 1 < N) {
+         ld16f(blk + 48 * (size_t)(i + 1), An);
+         ld16f(blk + 48 * (size_t)(i + 1) + 16, Bn);
+         ld16f(blk + 48 * (size_t)(i + 1) + 32, Cn);
+      }
+      float* rec = fac + (size_t)kRec * i;
+      st16f(rec, A);
+      float fill[16];
+      if (i > 0) {
+         mm_sub(A, cp, B);
+#pragma unroll
+         for (int m = 0; m < 16; m++) fill[m] = 0.f;
+         if (per) mm_sub(A, ap, fill);
       } else {
 #pragma unroll
-         for (int m = 0; m < 16; m++) c[m] += a[m];
-         lus_cols(u, c);
-#pragma unroll
-         for (int m = 0; m < 16; m++) a[m] = c[m];
+         for (int m = 0; m < 16; m++) fill[m] = A[m];
       }
-      st16(row, a);
-      st16(row + 32, c);
+      const LUf u = luf_factor(B);
+      luf_store(rec + 16, u);
+      if (per && i == N - 2) {
 #pragma unroll
-      for (int k = 0; k < 4; k++) { f[4 * i + k] = x[k]; fp[k] = x[k]; }
+         for (int m = 0; m < 16; m++) C[m] += fill[m];
+         luf_cols(u, C);
 #pragma unroll
-      for (int m = 0; m < 16; m++) { cp[m] = c[m]; ap[m] = a[m]; }
+         for (int m = 0; m < 16; m++) fill[m] = C[m];
+      } else {
+         luf_cols(u, C);
+         if (per) luf_cols(u, fill);
+      }
+      st16f(rec + 32, C);
+      if (per) st16f(rec + 48, fill);
+#pragma unroll
+      for (int m = 0; m < 16; m++) { cp[m] = C[m]; ap[m] = fill[m]; }
+      if (i + 1 < N) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) { A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
+      }
    }
-   // last-row elimination and solve (triSolvers.cpp:967-1029)
-   T bN[16], cN[16], fN[4];
+   if (!per) return;
+   // last-row elimination (triSolvers.cpp:967-999)
+   float cN[16], bN[16];
 #pragma unroll
-   for (int m = 0; m < 16; m++) bN[m] = ((m >> 2) == (m & 3)) ? T(1) : T(0);
-   ld16(blk + 48 * (size_t)(N - 1) + 32, cN);
-#pragma unroll
-   for (int k = 0; k < 4; k++) fN[k] = f[4 * (N - 1) + k];
+   for (int m = 0; m < 16; m++) { cN[m] = cp[m]; bN[m] = ((m >> 2) == (m & 3)) ? 1.f : 0.f; }
    for (int i = 0; i < N - 1; i++) {
-      T ci[16], ai[16], t[16];
-      ld16(blk + 48 * (size_t)i + 32, ci);
-      ld16(blk + 48 * (size_t)i, ai);
+      float* rec = fac + (size_t)kRec * i;
+      float ci[16], ai[16], tt[16];
+      ld16f(rec + 32, ci);
+      ld16f(rec + 48, ai);
+      st16f(rec + 64, cN);
 #pragma unroll
-      for (int k = 0; k < 4; k++)
+      for (int m = 0; m < 16; m++) tt[m] = 0.f;
+      mm_sub(cN, ci, tt);
+      mm_sub(cN, ai, bN);
 #pragma unroll
-         for (int j = 0; j < 4; j++) {
-            T acc = T(0);
-#pragma unroll
-            for (int l = 0; l < 4; l++) {
-               acc -= cN[4 * k + l] * ci[4 * l + j];
-               bN[4 * k + j] -= cN[4 * k + l] * ai[4 * l + j];
-            }
-            t[4 * k + j] = acc;
-         }
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-#pragma unroll
-         for (int j = 0; j < 4; j++) fN[k] -= cN[4 * k + j] * f[4 * i + j];
-#pragma unroll
-      for (int m = 0; m < 16; m++) cN[m] = t[m];
+      for (int m = 0; m < 16; m++) cN[m] = tt[m];
    }
-   const LUs<T> u = lus_factor(bN);
-   lus_solve(u, fN[0], fN[1], fN[2], fN[3]);
-#pragma unroll
-   for (int k = 0; k < 4; k++) f[4 * (N - 1) + k] = fN[k];
-   if (N < 2) return;
-   {
-      T c[16], x[4];
-      ld16(blk + 48 * (size_t)(N - 2) + 32, c);
-#pragma unroll
-      for (int k = 0; k < 4; k++) x[k] = f[4 * (N - 2) + k];
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-#pragma unroll
-         for (int j = 0; j < 4; j++) x[k] -= (c[4 * k + j] * fN[j]);
-#pragma unroll
-      for (int k = 0; k < 4; k++) f[4 * (N - 2) + k] = x[k];
-   }
-   T xn[4];
-#pragma unroll
-   for (int k = 0; k < 4; k++) xn[k] = f[4 * (N - 2) + k];
-   for (int i = N - 3; i >= 0; i--) {
-      T c[16], a[16], x[4];
-      ld16(blk + 48 * (size_t)i + 32, c);
-      ld16(blk + 48 * (size_t)i, a);
-#pragma unroll
-      for (int k = 0; k < 4; k++) x[k] = f[4 * i + k];
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-#pragma unroll
-         for (int j = 0; j < 4; j++) x[k] -= (c[4 * k + j] * xn[j] + a[4 * k + j] * fN[j]);
-#pragma unroll
-      for (int k = 0; k < 4; k++) { f[4 * i + k] = x[k]; xn[k] = x[k]; }
-   }
+   luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
 
-// one FP32 line solve per thread: F = r[fcell], solve, r[scell] = F
-__global__ void __launch_bounds__(64) mx_lines_kernel(DeviceState d, int first, int count)
+__global__ void __launch_bounds__(64) mx_solve_kernel(DeviceState d, int first, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
    const int ich = d.line_chains[first + t];
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
+   const bool per = d.chain_periodic[ich] != 0;
+   const float* fac = d.fac32 + (size_t)kRec * row0;
    float* fs = d.fsc32 + 4 * (size_t)row0;
-   for (int r = 0; r < N; r++) {
-      const int fc = d.row_fcell[row0 + r];
-      float v[4] = {0.f, 0.f, 0.f, 0.f};
-      if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, v);
-      st4(fs + 4 * r, v);
+   // forward: f(i) = LU^{-1}(F(i) - A(i) f(i-1)), F(i) = r[fcell]
+   float xp[4] = {0.f, 0.f, 0.f, 0.f};
+   int fc = d.row_fcell[row0];
+   for (int i = 0; i < N; i++) {
+      const float* rec = fac + (size_t)kRec * i;
+      const int fcn = (i + 1 < N) ? d.row_fcell[row0 + i + 1] : -1;
+      float x[4] = {0.f, 0.f, 0.f, 0.f};
+      if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, x);
+      if (i > 0) {
+         float a[16];
+         ld16f(rec, a);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-a[4 * k + j], xp[j], x[k]);
+      }
+      const LUf u = luf_load(rec + 16);
+      luf_solve(u, x[0], x[1], x[2], x[3]);
+      st4(fs + 4 * i, x);
+#pragma unroll
+      for (int k = 0; k < 4; k++) xp[k] = x[k];
+      fc = fcn;
    }
-   if (d.chain_periodic[ich]) tridag_periodic<float>(d.blk32 + 48 * (size_t)row0, fs, N);
-   else tridag_open<float>(d.blk32 + 48 * (size_t)row0, fs, N);
+   float xn[4];
+   if (per) {
+      float fN[4] = {xp[0], xp[1], xp[2], xp[3]};
+      for (int i = 0; i < N - 1; i++) {
+         float c[16], f[4];
+         ld16f(fac + (size_t)kRec * i + 64, c);
+         ld4(fs + 4 * i, f);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) fN[k] = __fmaf_rn(-c[4 * k + j], f[j], fN[k]);
+      }
+      const LUf u = luf_load(d.facN32 + 16 * d.chain_facN[ich]);
+      luf_solve(u, fN[0], fN[1], fN[2], fN[3]);
+      st4(fs + 4 * (N - 1), fN);
+#pragma unroll
+      for (int k = 0; k < 4; k++) xn[k] = fN[k];
+      for (int i = N - 2; i >= 0; i--) {
+         const float* rec = fac + (size_t)kRec * i;
+         float c[16], a[16], x[4];
+         ld16f(rec + 32, c);
+         ld16f(rec + 48, a);
+         ld4(fs + 4 * i, x);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+               const float s = (i == N - 2) ? c[4 * k + j] * xn[j] : __fmaf_rn(a[4 * k + j], fN[j], c[4 * k + j] * xn[j]);
+               x[k] -= s;
+            }
+         st4(fs + 4 * i, x);
+#pragma unroll
+         for (int k = 0; k < 4; k++) xn[k] = x[k];
+      }
+   } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) xn[k] = xp[k];
+      for (int i = N - 2; i >= 0; i--) {
+         float c[16], x[4];
+         ld16f(fac + (size_t)kRec * i + 32, c);
+         ld4(fs + 4 * i, x);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-c[4 * k + j], xn[j], x[k]);
+         st4(fs + 4 * i, x);
+#pragma unroll
+         for (int k = 0; k < 4; k++) xn[k] = x[k];
+      }
+   }
    for (int r = 0; r < N; r++) {
       float v[4];
       ld4(fs + 4 * r, v);
@@ -458,9 +467,14 @@ void launch_mx_assemble(const DeviceState& d, cudaStream_t st)
    mx_assemble_kernel<<<blocks_for(48 * d.nRow), kThreads, 0, st>>>(d);
 }
 
-void launch_mx_lines(const DeviceState& d, int first, int count, cudaStream_t st)
+void launch_mx_factor(const DeviceState& d, cudaStream_t st)
 {
-   if (count > 0) mx_lines_kernel<<<(count + 63) / 64, 64, 0, st>>>(d, first, count);
+   mx_factor_kernel<<<(d.nChain + 63) / 64, 64, 0, st>>>(d, d.nChain);
+}
+
+void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st)
+{
+   if (count > 0) mx_solve_kernel<<<(count + 63) / 64, 64, 0, st>>>(d, first, count);
 }
 
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)
