@@ -29,7 +29,7 @@ def test_first_residual_is_the_fp64_residual(make_case, native_lib, order):
     assert hm[0] == hp[0] and hm[1] == hp[1]
     # one mixed step moves q close to the FP64 step (FP32 operator)
     qm, qp = gm.get("q"), gp.get("q")
-    assert np.max(np.abs(qm - qp)) < 1e-5 * np.max(np.abs(qp))
+    assert np.max(np.abs(qm - qp)) < 1e-4 * np.max(np.abs(qp))
 
 
 @pytest.mark.parametrize("order,cfl", [(1, 10.0), (3, 10.0)])
