@@ -86,27 +86,44 @@ struct hamstr_gpu {
    double tol_host = 0.0;   // staging for the async copy into d.tol
    int mixed = 0;           // 0: FP64 drop-in, 1: FP32 operator defect correction
 
+   // optional per-launch timing (hamstr_gpu_profile_step)
+   std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>>* prof = nullptr;
+   template <class F>
+   void L(const char* name, int& n, F&& launch)
+   {
+      cudaEvent_t a = nullptr, b = nullptr;
+      if (prof) {
+         cudaEventCreate(&a);
+         cudaEventCreate(&b);
+         cudaEventRecord(a, stream);
+      }
+      launch();
+      n++;
+      if (prof) {
+         cudaEventRecord(b, stream);
+         prof->push_back({name, {a, b}});
+      }
+   }
+
    // one pseudo-time step of the mixed-precision form
    int enqueue_mixed_step(bool check_tol)
    {
       int n = 0;
-      launch_mx_rhs_face(d, stream); n++;
-      launch_rhs_cell(d, true, stream); n++;
-      launch_norm_final(d, 0, check_tol, stream); n++;
-      launch_mx_init(d, stream); n++;
-      launch_mx_assemble(d, stream); n++;
-      launch_mx_factor(d, stream); n++;
+      L("mx_rhs_face", n, [&] { launch_mx_rhs_face(d, stream); });
+      L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
+      L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
+      L("mx_init", n, [&] { launch_mx_init(d, stream); });
+      L("mx_assemble", n, [&] { launch_mx_assemble(d, stream); });
+      L("mx_factor", n, [&] { launch_mx_factor(d, stream); });
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++) {
-            launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream);
-            n++;
-         }
-         launch_mx_dq_update(d, stream); n++;
-         launch_mx_lin_face(d, stream); n++;
-         launch_mx_lin_cell(d, s == msweep - 1, stream); n++;
-         if (s == msweep - 1) { launch_norm_final(d, 2, false, stream); n++; }
+         for (int w = 0; w < plan.nWave; w++)
+            L("mx_solve", n, [&] { launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream); });
+         L("mx_dq_update", n, [&] { launch_mx_dq_update(d, stream); });
+         L("mx_lin_face", n, [&] { launch_mx_lin_face(d, stream); });
+         L("mx_lin_cell", n, [&] { launch_mx_lin_cell(d, s == msweep - 1, stream); });
+         if (s == msweep - 1) L("norm_final", n, [&] { launch_norm_final(d, 2, false, stream); });
       }
-      launch_step_end(d, stream); n++;
+      L("step_end", n, [&] { launch_step_end(d, stream); });
       launches_per_step = n;
       CK(cudaGetLastError());
       return HAMSTR_GPU_OK;
@@ -151,22 +168,19 @@ struct hamstr_gpu {
    {
       if (mixed) return enqueue_mixed_step(check_tol);
       int n = 0;
-      launch_rhs_face(d, true, stream); n++;
-      launch_rhs_cell(d, true, stream); n++;
-      launch_norm_final(d, 0, check_tol, stream); n++;
-      launch_adi_assemble(d, stream); n++;
-      launch_adi_factor(d, sched.nwarps[0], stream); n++;
+      L("rhs_face", n, [&] { launch_rhs_face(d, true, stream); });
+      L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
+      L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
+      L("adi_assemble", n, [&] { launch_adi_assemble(d, stream); });
+      L("adi_factor", n, [&] { launch_adi_factor(d, sched.nwarps[0], stream); });
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++) {
-            launch_adi_solve(d, w, sched.nwarps[1 + w], stream);
-            n++;
-         }
-         launch_dq_update(d, stream); n++;
-         launch_lin_face(d, stream); n++;
-         launch_lin_cell(d, s == msweep - 1, stream); n++;
-         if (s == msweep - 1) { launch_norm_final(d, 2, false, stream); n++; }
+         for (int w = 0; w < plan.nWave; w++) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
+         L("dq_update", n, [&] { launch_dq_update(d, stream); });
+         L("lin_face", n, [&] { launch_lin_face(d, stream); });
+         L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
+         if (s == msweep - 1) L("norm_final", n, [&] { launch_norm_final(d, 2, false, stream); });
       }
-      launch_step_end(d, stream); n++;
+      L("step_end", n, [&] { launch_step_end(d, stream); });
       launches_per_step = n;
       CK(cudaGetLastError());
       return HAMSTR_GPU_OK;
@@ -685,56 +699,43 @@ int hamstr_gpu_launches_per_step(hamstr_gpu* g)
 
 int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double* ms, int* launches, int* n)
 {
-   // eager launches of one step with events around each kernel class
+   // eager launches of the current mode's step with events around each kernel
    if (!g || reps < 1 || !names || !ms || !launches || !n) return HAMSTR_GPU_ERR_ARG;
-   static const char* kNames[] = {"rhs_face", "rhs_cell", "norm_final", "adi_factor", "adi_solve",
-                                  "dq_update", "lin_face", "lin_cell", "step_end", "adi_assemble"};
-   const int K = 10;
-   std::vector<double> acc(K, 0.0);
-   std::vector<int> cnt(K, 0);
-   cudaEvent_t a, b;
-   CK(cudaEventCreate(&a));
-   CK(cudaEventCreate(&b));
-   DeviceState& d = g->d;
    int st = g->reset_ctl(0.0);
    if (st) return st;
-   auto timed = [&](int k, auto fn) -> int {
-      CK(cudaEventRecord(a, g->stream));
-      fn();
-      CK(cudaEventRecord(b, g->stream));
-      CK(cudaEventSynchronize(b));
-      float t = 0.f;
-      CK(cudaEventElapsedTime(&t, a, b));
-      acc[k] += t;
-      cnt[k] += 1;
-      return HAMSTR_GPU_OK;
-   };
+   std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>> rec;
+   std::vector<const char*> order;
+   std::vector<double> acc;
+   std::vector<int> cnt;
    for (int r = 0; r < reps; r++) {
-      if ((st = timed(0, [&] { launch_rhs_face(d, true, g->stream); }))) return st;
-      if ((st = timed(1, [&] { launch_rhs_cell(d, true, g->stream); }))) return st;
-      if ((st = timed(2, [&] { launch_norm_final(d, 0, false, g->stream); }))) return st;
-      if ((st = timed(9, [&] { launch_adi_assemble(d, g->stream); }))) return st;
-      if ((st = timed(3, [&] { launch_adi_factor(d, g->sched.nwarps[0], g->stream); }))) return st;
-      for (int s = 0; s < g->msweep; s++) {
-         for (int w = 0; w < g->plan.nWave; w++)
-            if ((st = timed(4, [&] { launch_adi_solve(d, w, g->sched.nwarps[1 + w], g->stream); }))) return st;
-         if ((st = timed(5, [&] { launch_dq_update(d, g->stream); }))) return st;
-         if ((st = timed(6, [&] { launch_lin_face(d, g->stream); }))) return st;
-         if ((st = timed(7, [&] { launch_lin_cell(d, s == g->msweep - 1, g->stream); }))) return st;
-         if (s == g->msweep - 1)
-            if ((st = timed(2, [&] { launch_norm_final(d, 2, false, g->stream); }))) return st;
+      rec.clear();
+      g->prof = &rec;
+      st = g->enqueue_step(false);
+      g->prof = nullptr;
+      if (st) return st;
+      CK(cudaStreamSynchronize(g->stream));
+      for (auto& e : rec) {
+         float t = 0.f;
+         cudaEventElapsedTime(&t, e.second.first, e.second.second);
+         cudaEventDestroy(e.second.first);
+         cudaEventDestroy(e.second.second);
+         size_t k = 0;
+         while (k < order.size() && std::strcmp(order[k], e.first) != 0) k++;
+         if (k == order.size()) {
+            order.push_back(e.first);
+            acc.push_back(0.0);
+            cnt.push_back(0);
+         }
+         acc[k] += t;
+         cnt[k] += 1;
       }
-      if ((st = timed(8, [&] { launch_step_end(d, g->stream); }))) return st;
    }
-   cudaEventDestroy(a);
-   cudaEventDestroy(b);
-   CK(cudaGetLastError());
    st = g->status_check();
    if (st) return st;
    const int cap = *n;
-   *n = K;
-   for (int k = 0; k < K && k < cap; k++) {
-      names[k] = kNames[k];
+   *n = (int)order.size();
+   for (int k = 0; k < (int)order.size() && k < cap; k++) {
+      names[k] = order[k];
       ms[k] = acc[k] / reps;
       launches[k] = cnt[k] / reps;
    }
