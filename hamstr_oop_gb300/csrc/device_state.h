@@ -68,7 +68,7 @@ struct DeviceState {
 
    // mixed-precision defect correction (FP64 residual, FP32 operator)
    float* ff32;            // [nSlot][32] FP32 face Jacobians
-   float* blk32;           // [nRow][48] FP32 blocks, factored in place each sweep
+   float* blk32;           // [nRow][48] FP32 assembled blocks A, B, C (B + I)
    float* fsc32;           // [nRow][4]
    float* fac32;           // [nRow][80] FP32 factor records
    float* facN32;          // [periodic chains][16]
