@@ -41,16 +41,23 @@ if ROOT not in sys.path:
 
 METRIC = "cell-iters/s"
 UNIT = "cell-iter/s"
+# Each workload: mesh (split = probability that a quad is split into two
+# triangles, seeded), reconstruction order, CFL, sweeps, freestream, the
+# chain end rule, and a CFL ramp (steps, CFL) run before the measured steps:
+# WENO at CFL 20 on the half-split mesh diverges from an impulsive start.
 WORKLOADS = {
-    "c2": dict(ni=512, nj=128, order=5, CFL=20.0, msweep=2, Mach=0.5, alpha=1.25,
-               name="naca0012_ogrid_512x128_weno5_cfl20_msweep2"),
-    "c1": dict(ni=128, nj=32, order=3, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
-               name="naca0012_ogrid_128x32_muscl3_cfl10_msweep2"),
+    "c2": dict(ni=512, nj=128, split=0.5, seed=0, end_rule=1, order=5, CFL=20.0, msweep=2, Mach=0.5, alpha=1.25,
+               ramp=((50, 2.0), (50, 5.0), (100, 10.0)),
+               name="naca0012_ogrid_512x128_split50_weno5_cfl20_msweep2"),
+    "c2quad": dict(ni=512, nj=128, split=0.0, seed=0, end_rule=0, order=5, CFL=20.0, msweep=2, Mach=0.5,
+                   alpha=1.25, ramp=(), name="naca0012_ogrid_512x128_weno5_cfl20_msweep2"),
+    "c1": dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=3, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
+               ramp=(), name="naca0012_ogrid_128x32_muscl3_cfl10_msweep2"),
 }
 # converged-solve measurement: a case that reaches 1e-10 (the MUSCL and WENO
 # cases plateau near 1e-9 on these meshes, as the survey's probes found)
-CONVERGE = dict(ni=128, nj=32, order=1, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25, tol=1e-10, cap=6000,
-                name="naca0012_ogrid_128x32_order1_cfl10_msweep2")
+CONVERGE = dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
+                tol=1e-10, cap=6000, name="naca0012_ogrid_128x32_order1_cfl10_msweep2")
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -66,8 +73,44 @@ def make_case(wl: dict, rank: int) -> str:
     marker = os.path.join(d, "input.hamstr")
     if not os.path.exists(marker):
         meshgen.make_case(d, wl["ni"], wl["nj"], order=wl["order"], CFL=wl["CFL"], msweep=wl["msweep"],
-                          Mach=wl["Mach"], alpha=wl["alpha"], nsteps=1)
+                          Mach=wl["Mach"], alpha=wl["alpha"], nsteps=1, split=wl["split"], seed=wl["seed"])
     return d
+
+
+def mesh_note(wl: dict) -> str:
+    if wl["split"] > 0:
+        return ("NACA 0012 O-grid, each quad split into two triangles with probability %g (seed %d); "
+                "chains from meshgen.extract_chains; extended chain end rule" % (wl["split"], wl["seed"]))
+    return "NACA 0012 quadrilateral O-grid; reference chain end rule"
+
+
+def open_case(wl: dict, case_dir: str):
+    from hamstr_oop_gb300 import native
+    case = native.Case(case_dir)
+    case.set_option("chain_end_rule", wl["end_rule"])
+    return case
+
+
+def open_oracle(wl: dict, case_dir: str):
+    from oracle import oracle
+    o = oracle.OracleCase(case_dir, "port")
+    o.set_option("chain_end_rule", wl["end_rule"])
+    return o
+
+
+def time_oracle_steps(cases: list, q0: list, steps: int) -> float:
+    """Seconds for `steps` pseudo-time steps on every case (one host thread
+    each), each step taken from the state q0 so that WENO at the workload's
+    CFL stays finite without a ramp; the resets are not timed."""
+    from oracle import oracle
+    total = 0.0
+    for _ in range(steps):
+        for c, q in zip(cases, q0):
+            c.set("q", q)
+        t0 = time.perf_counter()
+        oracle.march_replicas(cases, 1)
+        total += time.perf_counter() - t0
+    return total
 
 
 class ClockSampler:
@@ -189,9 +232,14 @@ def run_gpu(args, wl, rank, local_rank, world):
     torch.cuda.set_device(local_rank)
     native.load()
     case_dir = make_case(wl, rank)
-    case = native.Case(case_dir)
+    case = open_case(wl, case_dir)
     gpu = native.GpuSolver(case)
     sizes = case.sizes
+    for n, cfl in wl["ramp"]:
+        gpu.set_cfl(cfl)
+        gpu.enqueue_steps(n)
+    gpu.set_cfl(wl["CFL"])
+    gpu.sync()
     lay = gpu.layout()
     nc = sizes["nCell"]
     hs = torch.cuda.ExternalStream(gpu.stream)
@@ -304,7 +352,7 @@ def run_gpu(args, wl, rank, local_rank, world):
                        "order": wl["order"], "msweep": wl["msweep"], "CFL": wl["CFL"], "mach": wl["Mach"],
                        "alpha_deg": wl["alpha"], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "512 MiB flush write between timed steps (untimed)",
-                       "mesh": "quadrilateral O-grid; mixed tri/quad split not applied"},
+                       "mesh": mesh_note(wl), "cfl_ramp_before_timing": [list(r) for r in wl["ramp"]]},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "mixed_precision": mixed, "converged": conv,
             "gpu_launches": gpu.launches_per_step() * args.steps,
@@ -344,17 +392,16 @@ def cpu_baseline(wl, case_dir, nc, steps=None) -> dict:
     oracle.build(reference=False)
     threads = os.cpu_count() or 1
     steps = steps or (2 if nc > 20000 else 20)
-    base = oracle.OracleCase(case_dir, "port")
+    base = open_oracle(wl, case_dir)
     cases = [base] + [base.clone() for _ in range(threads - 1)]
-    oracle.march_replicas(cases, 1)          # warm-up step
-    t0 = time.perf_counter()
-    oracle.march_replicas(cases, steps)
-    dt = time.perf_counter() - t0
+    q0 = [c.get("q") for c in cases]
+    time_oracle_steps(cases, q0, 1)          # warm-up step
+    dt = time_oracle_steps(cases, q0, steps)
     for c in cases:
         c.close()
     return {"value": threads * nc * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d pseudo-time steps on each of %d independent copies of the %s mesh (one per thread)"
-                      % (steps, threads, wl["name"])}
+            "sample": "%d pseudo-time steps (each from the freestream state) on each of %d independent copies "
+                      "of the %s mesh (one per thread)" % (steps, threads, wl["name"])}
 
 
 def run_reference(args, wl, rank):
@@ -364,25 +411,23 @@ def run_reference(args, wl, rank):
     oracle.build(reference=False)
     case_dir = make_case(wl, 0)
     threads = os.cpu_count() or 1
-    base = oracle.OracleCase(case_dir, "port")
+    base = open_oracle(wl, case_dir)
     nc = base.sizes["nCell"]
     cases = [base] + [base.clone() for _ in range(threads - 1)]
-    oracle.march_replicas(cases, max(args.warmup, 1))
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle.march_replicas(cases, 1)
-    dt = time.perf_counter() - t0
+    q0 = [c.get("q") for c in cases]
+    time_oracle_steps(cases, q0, max(args.warmup, 1))
+    dt = time_oracle_steps(cases, q0, args.steps)
     for c in cases:
         c.close()
     value = threads * nc * args.steps / dt
-    sample = ("each step: one pseudo-time step on each of %d independent copies of the %s mesh "
+    sample = ("each step: one pseudo-time step (from the freestream state) on each of %d independent copies of the %s mesh "
               "(one per host thread), C restatement of the reference algorithm (oracle/hamstr_oracle.c, "
               "bit-identical to the reference on the pinned fixtures)" % (threads, wl["name"]))
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": wl["name"], "cells": nc, "order": wl["order"],
-                                            "msweep": wl["msweep"], "CFL": wl["CFL"]},
+                                            "msweep": wl["msweep"], "CFL": wl["CFL"], "mesh": mesh_note(wl)},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -267,6 +267,7 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    in.nChain = nChain;
    in.nChainFace = faceStartPerChain[nChain];
    in.order = p->order;
+   in.end_rule = p->chain_end_rule;
    in.faces = faces;
    in.faceStartPerChain = faceStartPerChain;
    in.chainConn = chainConn;
@@ -743,6 +744,20 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
 }
 
 }  // extern "C"
+
+extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
+{
+   if (!g || !(cfl > 0.0) || !(cfl < 1e300)) return HAMSTR_GPU_ERR_ARG;
+   if (g->d.fc.cfl != cfl) {
+      g->d.fc.cfl = cfl;   // kernels take the state by value: recapture the step
+      if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
+      if (g->step_graph) cudaGraphDestroy(g->step_graph);
+      g->step_exec = nullptr;
+      g->step_graph = nullptr;
+      g->launches_per_step = 0;
+   }
+   return HAMSTR_GPU_OK;
+}
 
 extern "C" int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed)
 {

@@ -200,6 +200,13 @@ void MESHBLOCK::preprocess(void)
 // ==================================================================
 void SOLNBLOCK::readSolutionInputs(void) { readSolutionInputs(""); }
 
+void SOLNBLOCK::setChainEndRule(int rule)
+{
+   if (rule != HAMSTR_END_RULE_REFERENCE && rule != HAMSTR_END_RULE_EXTENDED)
+      throw hamstr::Error(HAMSTR_GPU_ERR_ARG, "unknown chain end rule");
+   chainEndRule = rule;
+}
+
 void SOLNBLOCK::readSolutionInputs(const std::string& root)
 {
    const std::string p = (root.empty() ? std::string("") : root + "/") + "input.hamstr";
@@ -306,6 +313,7 @@ void SOLVER::ensureGpu()
    p.uinf = sb->uinf;
    p.vinf = sb->vinf;
    p.einf = sb->einf;
+   p.chain_end_rule = sb->chainEndRule;
    check(hamstr_gpu_create(&p, mb->nCell, mb->nFace, mb->faces.data(), mb->normVec.data(), mb->refMtx.data(),
                            mb->nChain, mb->faceStartPerChain.data(), mb->chainConn.data(), &gpu));
    check(hamstr_gpu_set(gpu, "q", sb->q.data()));
@@ -554,6 +562,16 @@ void hamstr_case::set_freestream(hamstr_case& c, double u, double v, double e)
    }
 }
 
+int hamstr_case::set_option(hamstr_case& c, const std::string& name, int value)
+{
+   if (name == "chain_end_rule") {
+      if (value != HAMSTR_END_RULE_REFERENCE && value != HAMSTR_END_RULE_EXTENDED) return HAMSTR_GPU_ERR_ARG;
+      c.sb.chainEndRule = value;
+      return HAMSTR_GPU_OK;
+   }
+   return HAMSTR_GPU_ERR_ARG;
+}
+
 void hamstr_case::load(hamstr_case& c, const std::string& dir)
 {
    c.mb.readMeshData(0, dir);
@@ -584,6 +602,7 @@ hamstr_gpu_params hamstr_case::gpu_params(const hamstr_case& c)
    p.uinf = c.sb.uinf;
    p.vinf = c.sb.vinf;
    p.einf = c.sb.einf;
+   p.chain_end_rule = c.sb.chainEndRule;
    return p;
 }
 
@@ -650,6 +669,12 @@ int hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double 
    if (!c) return HAMSTR_GPU_ERR_ARG;
    hamstr_case::set_freestream(*c, uinf, vinf, einf);
    return HAMSTR_GPU_OK;
+}
+
+int hamstr_case_set_option(hamstr_case* c, const char* name, int value)
+{
+   if (!c || !name) return HAMSTR_GPU_ERR_ARG;
+   return hamstr_case::set_option(*c, name, value);
 }
 
 int hamstr_gpu_create_from_case(const hamstr_case* c, hamstr_gpu** out)

@@ -72,6 +72,7 @@ class SOLNBLOCK
    char scheme[64] = {0};
    int visc = 0;
    int nGhost = 2;
+   int chainEndRule = 0;   // project option: HAMSTR_END_RULE_* (not in the reference)
    double uinf = 0, vinf = 0, winf = 0, einf = 0, pinf = 0, rinf = 0;
    double gamma = 0, invGamma = 0, gm1 = 0, c2b = 0, rgas = 0, pr = 0, prtr = 0;
    double LInfNorm = 0, L2Norm = 0;
@@ -84,6 +85,9 @@ class SOLNBLOCK
    // io.cpp:13-51
    void readSolutionInputs(void);
    void readSolutionInputs(const std::string& root);
+   // project addition: HAMSTR_END_RULE_* for meshes whose open chains end
+   // at interior faces (mixed tri/quad meshes); throws on other values
+   void setChainEndRule(int rule);
 };
 
 // ------------------------------------------------------------------
@@ -149,6 +153,7 @@ struct hamstr_case {
    static int get(const hamstr_case& c, const std::string& name, double* out);
    static void set_run(hamstr_case& c, int order, int msweep, double cfl);
    static void set_freestream(hamstr_case& c, double u, double v, double e);
+   static int set_option(hamstr_case& c, const std::string& name, int value);
    static hamstr_gpu_params gpu_params(const hamstr_case& c);
    static void load(hamstr_case& c, const std::string& dir);
    static int create_gpu(const hamstr_case& c, hamstr_gpu** out);

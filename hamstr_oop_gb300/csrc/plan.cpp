@@ -73,6 +73,15 @@ std::string build_plan(const MeshInput& in, Plan& p)
          return fmt("chain face entry %d is not a face (%d)", f, in.chainConn[f]);
 
    // ---- stencils and slots -----------------------------------------
+   // Under END_RULE_EXTENDED an open chain's ghosts are set by position:
+   // the k-th ghost beyond an end face holds the neighbour across an
+   // interior face, the wall mirror of the k-th cell from that end (the
+   // last one on shorter chains), or the freestream.  The reference's rule
+   // reads ghost ids that the chain itself never wrote when an open chain
+   // has fewer than nGhost (order 5) or 2 cells, so such chains are
+   // rejected there.
+   const bool ext = in.end_rule == END_RULE_EXTENDED;
+   if (in.end_rule != END_RULE_REFERENCE && !ext) return fmt("unknown chain end rule %d", in.end_rule);
    std::vector<int> chain_sten0(in.nChain);
    std::vector<int> ci;
    std::vector<int> face_last_slot(in.nFace, -1);
@@ -81,7 +90,10 @@ std::string build_plan(const MeshInput& in, Plan& p)
       const int nf = f2 - f1;
       const bool closed = in.chainConn[f1] == in.chainConn[f2 - 1];
       if (closed && (nf < 3 || nf < g + 1)) return fmt("closed chain %d too short (%d faces)", ich, nf);
-      if (!closed && nf < (g == 3 ? 3 : 2)) return fmt("open chain %d too short (%d faces)", ich, nf);
+      if (!closed && nf < 2) return fmt("open chain %d too short (%d faces)", ich, nf);
+      if (!closed && !ext && nf - 1 < (g == 3 ? 3 : 2))
+         return fmt("open chain %d has %d cells: the reference's ghost rule needs more "
+                    "(use the extended chain end rule)", ich, nf - 1);
       ci.assign(nf + 2 * g + 2, 0);
       int m = g, size;
       for (int f = f1; f < f2; f++) ci[m++] = left_of(in.chainConn[f]);
@@ -106,7 +118,33 @@ std::string build_plan(const MeshInput& in, Plan& p)
          ci[1] = -ci[2];
       }
       chain_sten0[ich] = (int)p.sten_cell.size();
-      for (int j = 0; j < size; j++) {
+      if (ext && !closed) {
+         const int n = size - 2 * g;
+         auto ghost = [&](int iface, int mc) {
+            const int right = right_of(iface);
+            if (right >= 0) {
+               p.sten_cell.push_back(right);
+               p.sten_kind.push_back(STEN_CELL);
+               p.sten_face.push_back(-1);
+            } else if (right == -2) {
+               p.sten_cell.push_back(mc);
+               p.sten_kind.push_back(STEN_WALL);
+               p.sten_face.push_back(iface);
+            } else {
+               p.sten_cell.push_back(-1);
+               p.sten_kind.push_back(STEN_FREESTREAM);
+               p.sten_face.push_back(-1);
+            }
+         };
+         for (int k = g; k >= 1; k--) ghost(in.chainConn[f1], ci[g + std::min(k - 1, n - 1)]);
+         for (int j = g; j < g + n; j++) {
+            p.sten_cell.push_back(ci[j]);
+            p.sten_kind.push_back(STEN_CELL);
+            p.sten_face.push_back(-1);
+         }
+         for (int k = 1; k <= g; k++) ghost(in.chainConn[f2 - 1], ci[g + n - 1 - std::min(k - 1, n - 1)]);
+      }
+      for (int j = 0; j < size && !(ext && !closed); j++) {
          const int icell = ci[j];
          const bool ghost = icell < 0 || (icell == 0 && (j == g - 1 || j == size - g));
          int kind = STEN_CELL, cell = icell, face = -1;
@@ -162,6 +200,28 @@ std::string build_plan(const MeshInput& in, Plan& p)
    }
 
    // ---- ADI rows (ADI.cpp:62-217) -----------------------------------
+   // extended rule: chain-end faces whose right cell lies on another chain
+   // (CSR over that cell, ascending face ids) and each cell's first chain
+   std::vector<int> xptr(in.nCell + 1, 0), xent, first_chain(in.nCell, -1);
+   if (ext) {
+      std::vector<char> isend(in.nFace, 0);
+      for (int ich = 0; ich < in.nChain; ich++) {
+         const int a = in.chainConn[in.faceStartPerChain[ich]];
+         const int b = in.chainConn[in.faceStartPerChain[ich + 1] - 1];
+         if (a == b) continue;
+         isend[a] = isend[b] = 1;
+      }
+      for (int f = 0; f < in.nFace; f++)
+         if (isend[f] && right_of(f) >= 0) xptr[right_of(f) + 1]++;
+      for (int c = 0; c < in.nCell; c++) xptr[c + 1] += xptr[c];
+      xent.assign(xptr[in.nCell], 0);
+      std::vector<int> xf(xptr.begin(), xptr.end() - 1);
+      for (int f = 0; f < in.nFace; f++)
+         if (isend[f] && right_of(f) >= 0) xent[xf[right_of(f)]++] = f;
+      for (int ich = in.nChain - 1; ich >= 0; ich--)
+         for (int f = in.faceStartPerChain[ich]; f < in.faceStartPerChain[ich + 1] - 1; f++)
+            first_chain[left_of(in.chainConn[f])] = ich;
+   }
    int slot0 = 0;
    std::vector<int> lastwave(in.nCell, -1);
    p.cell_last_wave_writer.assign(in.nCell, 0);
@@ -190,9 +250,12 @@ std::string build_plan(const MeshInput& in, Plan& p)
             fcell[m] = left_of(iface);
          } else {
             const int mm1 = m - 1;
-            if (right < 0 && f == f2 - 1) m--;
+            // extended rule: an interior last face couples explicitly, like
+            // the far field (the reference indexes a row past the chain)
+            const bool ext_last = ext && f == f2 - 1;
+            if ((right < 0 || ext_last) && f == f2 - 1) m--;
             ok &= B[m].add(L);
-            if (mm1 > -1 && right > -1) {
+            if (mm1 > -1 && right > -1 && !ext_last) {
                ok &= A[m].add(R);
                ok &= B[mm1].add(R | 1);
                ok &= C[mm1].add(L | 1);
@@ -202,6 +265,16 @@ std::string build_plan(const MeshInput& in, Plan& p)
             fcell[m] = left_of(iface);
          }
          m++;
+      }
+      if (ext) {
+         // a cell's first chain also carries the diagonal term of each
+         // chain-end face leading into it from another chain
+         for (int r = 0; r < N; r++) {
+            const int sc = left_of(in.chainConn[f1 + r]);
+            if (first_chain[sc] != ich) continue;
+            for (int e = xptr[sc]; e < xptr[sc + 1]; e++)
+               ok &= B[r].add((p.slot_owner[face_last_slot[xent[e]]] << 3) | (OP_SEL_R << 1) | 1);
+         }
       }
       if (!ok) return fmt("chain %d needs more than %d terms in one block", ich, kOpsPerBlock);
       p.chain_periodic.push_back(per);

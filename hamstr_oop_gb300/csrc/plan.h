@@ -23,9 +23,16 @@ enum { STEN_CELL = 0, STEN_WALL = 1, STEN_FREESTREAM = 2 };
 enum { OP_SEL_L = 0, OP_SEL_R = 1, OP_SEL_RREFL = 2 };
 constexpr int kOpsPerBlock = 4;   // A, B and C each take up to 4 ordered terms
 
+// how open chains take ghost states at their end faces
+enum {
+   END_RULE_REFERENCE = 0,   // computeRHS.cpp:86-149, 154-260 and ADI.cpp:126-190 exactly
+   END_RULE_EXTENDED = 1,    // open chains may end at interior faces (mixed meshes)
+};
+
 struct MeshInput {
    int nCell = 0, nFace = 0, nChain = 0, nChainFace = 0;
    int order = 3;
+   int end_rule = END_RULE_REFERENCE;
    const int* faces = nullptr;            // 6*nFace: n1 n2 cL eL cR eR (walls tagged -2)
    const int* faceStartPerChain = nullptr;// nChain+1
    const int* chainConn = nullptr;        // nChainFace

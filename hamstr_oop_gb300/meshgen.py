@@ -79,29 +79,8 @@ def _stretch_ratio(ds1: float, n: int, total: float) -> float:
     return 0.5 * (lo + hi)
 
 
-def naca0012_ogrid(ni: int, nj: int, ds1: float = 2e-3, rfar: float = 20.0,
-                   loop_start: int | None = None) -> Mesh:
-    """Structured NACA 0012 O-grid with ``ni`` wrap-around x ``nj`` wall-normal quads.
-
-    Surface points use cosine clustering in x (dense at the leading and
-    trailing edges).  Grid lines are straight rays from the surface point to
-    the far-field circle at the same polar angle about (0.5, 0); the aerofoil
-    is star-shaped about that point so the rays never cross.  Wall-normal
-    spacing starts at ``ds1`` chords and grows geometrically to the far field.
-
-    Cells are numbered ``j * ni + i``.  Colour 0 holds the ``nj`` closed loops
-    (one per wall-normal layer), colour 1 the ``ni`` open wall-to-far-field
-    lines.  Each loop starts at index ``loop_start`` (default ``ni // 2``, the
-    leading edge) so that cell 0 is never the first or last cell of a loop;
-    the reference's ghost test treats cell id 0 specially at those stencil
-    positions (computeRHS.cpp:158,170), and starting loops at 0 would make the
-    wall loop read a freestream ghost.  ``loop_start=0`` reproduces that case
-    on purpose for parity tests.
-    """
-    if ni < 4 or nj < 2:
-        raise ValueError("ogrid needs ni >= 4 and nj >= 2")
-    if loop_start is None:
-        loop_start = ni // 2
+def _ogrid_nodes(ni: int, nj: int, ds1: float, rfar: float) -> np.ndarray:
+    """Node coordinates of the NACA 0012 O-grid, node (i, j) at row ``j * ni + i``."""
     theta = 2.0 * math.pi * np.arange(ni) / ni
     sx = 0.5 * (1.0 + np.cos(theta))
     sy = naca0012_half_thickness(sx) * np.where(theta <= math.pi, 1.0, -1.0)
@@ -117,48 +96,521 @@ def naca0012_ogrid(ni: int, nj: int, ds1: float = 2e-3, rfar: float = 20.0,
     for j in range(nj + 1):
         nodes[j * ni:(j + 1) * ni, 0] = sx + s[j] * (fx - sx)
         nodes[j * ni:(j + 1) * ni, 1] = sy + s[j] * (fy - sy)
+    return nodes
 
-    def nid(i, j):
-        return j * ni + (i % ni)
 
-    def cid(i, j):
-        return j * ni + (i % ni)
+# sides of a grid cell: W (radial edge at i), E (radial edge at i+1),
+# S (wall-side edge at j), N (far-side edge at j+1)
+W, E, S, N = 0, 1, 2, 3
+# local edge numbers written to qedges.dat (unused by the solver): quad
+# bottom 0, right 1, top 2, left 3; the diagonal of a split cell 4
+_EDGE_NO = {W: 3, E: 1, S: 0, N: 2}
 
-    conn = np.empty((ni * nj, 4), dtype=np.int64)
-    for j in range(nj):
-        for i in range(ni):
-            conn[cid(i, j)] = (nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1))
-    centroid = nodes[conn].mean(axis=1)
 
-    faces = []
+def naca0012_ogrid(ni: int, nj: int, ds1: float = 2e-3, rfar: float = 20.0,
+                   loop_start: int | None = None, split: float = 0.0,
+                   seed: int = 0) -> Mesh:
+    """NACA 0012 O-grid with ``ni`` wrap-around x ``nj`` wall-normal cells.
 
-    def add_face(a, b, left, right, el, er):
+    Surface points use cosine clustering in x (dense at the leading and
+    trailing edges).  Grid lines are straight rays from the surface point to
+    the far-field circle at the same polar angle about (0.5, 0); the aerofoil
+    is star-shaped about that point so the rays never cross.  Wall-normal
+    spacing starts at ``ds1`` chords and grows geometrically to the far field.
+
+    ``split`` > 0 turns each quad, by a seeded coin flip with that
+    probability, into two triangles along a diagonal chosen by a second flip
+    (``numpy.random.default_rng(seed)``), giving a mixed tri/quad mesh; the
+    line chains are then extracted by :func:`extract_chains`.
+
+    Cells are numbered row by row (``j`` then ``i``; a split cell gets two
+    ids, lower triangle first).  Colour 0 holds the chains along the
+    wrap-around rows, colour 1 those along the wall-normal columns.  Closed
+    row loops start at index ``loop_start`` (default ``ni // 2``, the leading
+    edge) so that cell 0 is never the first or last cell of a loop; the
+    reference's ghost test treats cell id 0 specially at those stencil
+    positions (computeRHS.cpp:158,170), and starting loops at 0 makes the
+    wall loop read a freestream ghost.  ``loop_start=0`` reproduces that case
+    on purpose for parity tests.  On split meshes cell 0 is moved, if needed,
+    to a cell where that test is harmless.
+    """
+    if ni < 4 or nj < 2:
+        raise ValueError("ogrid needs ni >= 4 and nj >= 2")
+    if not 0.0 <= split <= 1.0:
+        raise ValueError("split probability must lie in [0, 1]")
+    if loop_start is None:
+        loop_start = ni // 2
+    nodes = _ogrid_nodes(ni, nj, ds1, rfar)
+    rng = np.random.default_rng(seed)
+    if split > 0.0:
+        is_split = rng.random((nj, ni)) < split
+        diag_up = rng.random((nj, ni)) < 0.5     # True: SW-NE diagonal
+    else:
+        is_split = np.zeros((nj, ni), dtype=bool)
+        diag_up = np.zeros((nj, ni), dtype=bool)
+    grid = _SplitGrid(ni, nj, is_split, diag_up)
+    chains, colors = extract_chains(grid, loop_start)
+    return _assemble(grid, nodes, chains, colors)
+
+
+class _SplitGrid:
+    """Cells, sides and edges of an O-grid whose cells may be split in two."""
+
+    def __init__(self, ni, nj, is_split, diag_up):
+        self.ni, self.nj = ni, nj
+        self.is_split, self.diag_up = is_split, diag_up
+        self.cells = []                       # (i, j, part) part: -1 quad, 0 lower, 1 upper triangle
+        self.ids = np.full((nj, ni, 2), -1, dtype=np.int64)
+        for j in range(nj):
+            for i in range(ni):
+                if is_split[j, i]:
+                    for part in (0, 1):
+                        self.ids[j, i, part] = len(self.cells)
+                        self.cells.append((i, j, part))
+                else:
+                    self.ids[j, i, 0] = self.ids[j, i, 1] = len(self.cells)
+                    self.cells.append((i, j, -1))
+
+    def nid(self, i, j):
+        return j * self.ni + (i % self.ni)
+
+    def owner(self, i, j, side):
+        """Cell id holding ``side`` of grid cell (i, j); -1 outside the grid."""
+        if j < 0 or j >= self.nj:
+            return -1
+        i %= self.ni
+        if not self.is_split[j, i]:
+            return int(self.ids[j, i, 0])
+        if side == S:
+            return int(self.ids[j, i, 0])
+        if side == N:
+            return int(self.ids[j, i, 1])
+        # SW-NE diagonal: lower triangle (SW, SE, NE) holds E, upper holds W
+        lower_has_e = bool(self.diag_up[j, i])
+        return int(self.ids[j, i, 0 if (side == E) == lower_has_e else 1])
+
+    def side_edge(self, i, j, side):
+        """Edge key of a side: ('R', i, j) radial, ('C', i, j) circumferential."""
+        i %= self.ni
+        if side == W:
+            return ("R", i, j)
+        if side == E:
+            return ("R", (i + 1) % self.ni, j)
+        if side == S:
+            return ("C", i, j)
+        return ("C", i, j + 1)
+
+    def edge_nodes(self, key):
+        kind, i, j = key
+        if kind == "R":
+            return self.nid(i, j), self.nid(i, j + 1)
+        if kind == "C":
+            return self.nid(i, j), self.nid(i + 1, j)
+        if self.diag_up[j, i]:
+            return self.nid(i, j), self.nid(i + 1, j + 1)
+        return self.nid(i + 1, j), self.nid(i, j + 1)
+
+    def edge_cells(self, key):
+        """The (up to two) cells on an edge; -1 for the outside of a boundary edge."""
+        kind, i, j = key
+        if kind == "R":
+            return self.owner(i, j, W), self.owner(i - 1, j, E)
+        if kind == "C":
+            return self.owner(i, j, S), self.owner(i, j - 1, N)
+        return int(self.ids[j, i, 0]), int(self.ids[j, i, 1])
+
+    def cell_nodes(self, c):
+        i, j, part = self.cells[c]
+        sw, se, ne, nw = self.nid(i, j), self.nid(i + 1, j), self.nid(i + 1, j + 1), self.nid(i, j + 1)
+        if part < 0:
+            return (sw, se, ne, nw)
+        if self.diag_up[j, i]:
+            return (sw, se, ne) if part == 0 else (sw, ne, nw)
+        return (sw, se, nw) if part == 0 else (se, ne, nw)
+
+
+def _split_modes(grid: _SplitGrid) -> dict:
+    """How the two triangles of each split cell join the line chains.
+
+    A triangle has three sides and each chain through it uses two, so one
+    side of every triangle is left to a neighbouring chain, which ends
+    there.  Per split cell (i, j) the mode says which pairs of sides each
+    triangle joins (X_lo / X_hi: the radial side of the lower / upper
+    triangle, D the diagonal):
+
+    ``I``   lower {X_lo, D}, upper {D, X_hi}: the row chain passes through
+            both triangles; S and N are left to the column chains.
+    ``MD``  lower {S, X_lo}, upper {X_hi, D}: covers S, W and E, leaves N.
+    ``MU``  upper {N, X_hi}, lower {X_lo, D}: covers N, W and E, leaves S.
+    ``JM``  lower {S, X_lo}, upper {D, N}: covers S, N and X_lo, leaves X_hi
+            (only for a column split from wall to far field).
+
+    Every face must lie in exactly one chain, so no face may be left by the
+    cells on both of its sides, and wall and far-field faces must be
+    covered.  Quads cover all four sides.  In each column a maximal run of
+    split cells rows a..b therefore takes: ``I`` at a then ``MD`` above it
+    when the run touches neither boundary; ``MD`` throughout from the wall;
+    ``MU`` throughout up to the far field; and ``MD``, one ``JM`` near
+    ``nj // 2``, ``MU`` above it for a fully split column.  Only ``JM``
+    leaves a radial side, so neighbouring fully split columns put their
+    ``JM`` cells on different rows.
+    """
+    ni, nj = grid.ni, grid.nj
+    mode, full = {}, []
+    for i in range(ni):
+        j = 0
+        while j < nj:
+            if not grid.is_split[j, i]:
+                j += 1
+                continue
+            a = j
+            while j < nj and grid.is_split[j, i]:
+                j += 1
+            b = j - 1
+            if a > 0 and b < nj - 1:
+                mode[(i, a)] = "I"
+                for jj in range(a + 1, b + 1):
+                    mode[(i, jj)] = "MD"
+            elif b < nj - 1:
+                for jj in range(a, b + 1):
+                    mode[(i, jj)] = "MD"
+            elif a > 0:
+                for jj in range(a, b + 1):
+                    mode[(i, jj)] = "MU"
+            else:
+                full.append(i)
+    # fully split columns: the JM rows of neighbouring columns must differ
+    jm = {}
+    cands = sorted(range(nj), key=lambda r: (abs(r - nj // 2), r))
+    for i in full:
+        taken = {jm.get((i - 1) % ni), jm.get((i + 1) % ni)}
+        m = next((r for r in cands if r not in taken), None)
+        if m is None:
+            raise ValueError("cannot place the column crossing of fully split column %d" % i)
+        jm[i] = m
+        for jj in range(nj):
+            mode[(i, jj)] = "MD" if jj < m else ("JM" if jj == m else "MU")
+    return mode
+
+
+def _visits(grid: _SplitGrid, mode: dict) -> list:
+    """Each cell's passages: (cell, edge, edge, 'i' row / 'j' column)."""
+    out = []
+    for j in range(grid.nj):
+        for i in range(grid.ni):
+            def e(side):
+                return grid.side_edge(i, j, side)
+            if not grid.is_split[j, i]:
+                q = int(grid.ids[j, i, 0])
+                out.append((q, e(W), e(E), "i"))
+                out.append((q, e(S), e(N), "j"))
+                continue
+            lo, hi = int(grid.ids[j, i, 0]), int(grid.ids[j, i, 1])
+            dg = ("D", i, j)
+            xlo, xhi = (E, W) if grid.diag_up[j, i] else (W, E)
+            md = mode[(i, j)]
+            if md == "I":
+                tw, te = grid.owner(i, j, W), grid.owner(i, j, E)
+                out.append((tw, e(W), dg, "i"))
+                out.append((te, dg, e(E), "i"))
+            elif md == "MD":
+                out.append((lo, e(S), e(xlo), "i"))
+                out.append((hi, e(xhi), dg, "i"))
+            elif md == "MU":
+                out.append((hi, e(N), e(xhi), "i"))
+                out.append((lo, e(xlo), dg, "i"))
+            else:
+                out.append((lo, e(S), e(xlo), "i"))
+                out.append((hi, dg, e(N), "j"))
+    return out
+
+
+def extract_chains(grid: _SplitGrid, loop_start: int):
+    """Line chains of a (possibly split) O-grid in the reference's chain model.
+
+    The reference computes fluxes only on chain faces (computeRHS.cpp:281-408)
+    and solves one block-tridiagonal system per chain (ADI.cpp:57-245), so
+    every face must lie in exactly one chain and every cell in at least one.
+    Quads lie on one row and one column chain; each triangle lies on one
+    chain (see :func:`_split_modes`).  Passages that share a face link into
+    a chain; a face used by one passage only is a chain end, whose other
+    side is a wall, the far field or a cell of another chain.
+
+    Returns ``(chains, colors)``: chains as dicts with ``cells``
+    (c_0..c_{n-1}), ``edges`` (open: e_0..e_n with e_k between c_{k-1} and
+    c_k; closed: e_0..e_{n-1}, e_0 between c_{n-1} and c_0), ``closed`` and
+    ``kind``; chains per colour (rows, then columns).
+    """
+    ni, nj = grid.ni, grid.nj
+    mode = _split_modes(grid)
+    visits = _visits(grid, mode)
+    ev = {}
+    for v, (_, a, b, _) in enumerate(visits):
+        ev.setdefault(a, []).append(v)
+        ev.setdefault(b, []).append(v)
+    edges = [("R", i, j) for j in range(nj) for i in range(ni)]
+    edges += [("C", i, j) for j in range(nj + 1) for i in range(ni)]
+    edges += [("D", i, j) for j in range(nj) for i in range(ni) if grid.is_split[j, i]]
+    for k in edges:
+        n = len(ev.get(k, ()))
+        if n == 0:
+            raise ValueError("edge %r lies on no chain (neighbouring fully split columns)" % (k,))
+        if n > 2:
+            raise AssertionError("edge %r on %d passages" % (k, n))
+
+    used = [False] * len(visits)
+
+    def walk(v0, via):
+        seq, cur = [], v0
+        while True:
+            c, a, b, _ = visits[cur]
+            out = b if via == a else a
+            nxt = [w for w in ev[out] if w != cur]
+            seq.append(out)
+            if not nxt:
+                return seq, [], False
+            if nxt[0] == v0:
+                return seq, [], True
+            cur = nxt[0]
+            via = out
+            seq.append(cur)
+
+    chains = []
+    for v0 in range(len(visits)):
+        if used[v0]:
+            continue
+        c0, a0, b0, _ = visits[v0]
+        fwd, _, cyc = walk(v0, a0)
+        if cyc:
+            # fwd = out_0, v_1, out_1, ..., v_{n-1}, out_{n-1} (back into v0)
+            vs = [v0] + fwd[1::2]
+            es = [fwd[-1]] + fwd[0::2][:-1]
+            ch = {"visits": vs, "edges": es, "closed": True}
+        else:
+            bwd, _, _ = walk(v0, b0)
+            # bwd: edge, visit, edge, visit, ..., end edge (leaving v0 through a0)
+            back_vs = bwd[1::2][::-1]
+            back_es = bwd[0::2][::-1]
+            vs = back_vs + [v0] + fwd[1::2]
+            es = back_es + fwd[0::2]
+            ch = {"visits": vs, "edges": es, "closed": False}
+        for v in ch["visits"]:
+            if used[v]:
+                raise AssertionError("passage %d on two chains" % v)
+            used[v] = True
+        ch["cells"] = [visits[v][0] for v in ch["visits"]]
+        ch["kind"] = "i" if any(visits[v][3] == "i" for v in ch["visits"]) else "j"
+        chains.append(ch)
+
+    def gpos(c):
+        i, j, part = grid.cells[c]
+        return i, j, part
+
+    def prio(edge):
+        if edge[0] == "C" and edge[2] == 0:
+            return 0                      # wall first (the reference's line convention)
+        if edge[0] == "C" and edge[2] == nj:
+            return 2                      # far field last
+        return 1
+
+    def ascending(cells, kind):
+        for a, b in zip(cells, cells[1:]):
+            (ia, ja, _), (ib, jb, _) = gpos(a), gpos(b)
+            if kind == "i" and ia != ib:
+                return (ib - ia) % ni == 1
+            if kind == "j" and ja != jb:
+                return jb > ja
+        return True
+
+    for ch in chains:
+        cells, es = ch["cells"], ch["edges"]
+        if ch["closed"]:
+            j = gpos(cells[0])[1]
+            start = grid.owner(loop_start, j, W)
+            first = grid.side_edge(loop_start, j, W)
+            if not ascending(cells, "i"):
+                # reversed, e_k (between c_{k-1} and c_k) becomes e_0, e_{n-1}, ..., e_1
+                cells = cells[::-1]
+                es = [es[0]] + es[1:][::-1]
+            k = cells.index(start)
+            cells = cells[k:] + cells[:k]
+            es = es[k:] + es[:k]
+            if es[0] != first:
+                raise AssertionError("loop of row %d does not start at its seam" % j)
+        else:
+            rev = prio(es[0]) > prio(es[-1]) or (
+                prio(es[0]) == prio(es[-1]) and not ascending(cells, ch["kind"]))
+            if rev:
+                cells, es = cells[::-1], es[::-1]
+        ch["cells"], ch["edges"] = cells, es
+
+    def key(ch):
+        i, j, part = gpos(ch["cells"][0])
+        if ch["kind"] == "i":
+            return (0, j, (i - loop_start) % ni, part)
+        return (1, i, j, part)
+
+    chains.sort(key=key)
+    colors = [sum(1 for c in chains if c["kind"] == "i"), sum(1 for c in chains if c["kind"] == "j")]
+    return chains, colors
+
+
+def _assemble(grid: _SplitGrid, nodes: np.ndarray, chains: list, colors: list) -> Mesh:
+    """Number faces in chain order, orient them to their chains, renumber cell 0."""
+    ncell = len(grid.cells)
+    conn = np.empty((ncell, 4), dtype=np.int64)
+    centroid = np.empty((ncell, 2))
+    for c in range(ncell):
+        cn = grid.cell_nodes(c)
+        conn[c] = cn if len(cn) == 4 else (cn[0], cn[1], cn[2], cn[2])
+        centroid[c] = nodes[list(cn)].mean(axis=0)
+
+    def edge_no(cell, edge):
+        if cell < 0:
+            return -1
+        if edge[0] == "D":
+            return 4
+        i, j, _ = grid.cells[cell]
+        for side in (W, E, S, N):
+            if grid.side_edge(i, j, side) == edge:
+                return _EDGE_NO[side]
+        raise AssertionError("edge %r is not a side of cell %d" % (edge, cell))
+
+    face_id, faces, out_chains = {}, [], []
+
+    def add(edge, left):
+        ca, cb = grid.edge_cells(edge)
+        right = cb if ca == left else ca
+        if left not in (ca, cb):
+            raise AssertionError("cell %d is not on edge %r" % (left, edge))
+        a, b = grid.edge_nodes(edge)
         (x1, y1), (x2, y2) = nodes[a], nodes[b]
         nx, ny = (y2 - y1), -(x2 - x1)
         mx, my = 0.5 * (x1 + x2), 0.5 * (y1 + y2)
         cx, cy = centroid[left]
         if nx * (mx - cx) + ny * (my - cy) < 0.0:
             a, b = b, a
-        faces.append((a, b, left, right, el, er))
-        return len(faces) - 1
+        if edge in face_id:
+            raise AssertionError("edge %r on two chains" % (edge,))
+        face_id[edge] = len(faces)
+        faces.append((a, b, left, right, edge_no(left, edge), edge_no(right, edge)))
+        return face_id[edge]
 
-    chains = []
-    # colour 0: closed loops; local edges 0 bottom, 1 right, 2 top, 3 left
-    for j in range(nj):
-        ch = []
-        for k in range(ni):
-            i = (loop_start + k) % ni
-            ch.append(add_face(nid(i, j), nid(i, j + 1), cid(i, j), cid(i - 1, j), 3, 1))
-        chains.append(ch + [ch[0]])
-    # colour 1: open wall-normal lines
-    for i in range(ni):
-        ch = [add_face(nid(i, 0), nid(i + 1, 0), cid(i, 0), -1, 0, -1)]
-        for j in range(1, nj):
-            ch.append(add_face(nid(i, j), nid(i + 1, j), cid(i, j), cid(i, j - 1), 0, 2))
-        ch.append(add_face(nid(i, nj), nid(i + 1, nj), cid(i, nj - 1), -1, 2, -1))
-        chains.append(ch)
-    return Mesh(nodes=nodes, conn=conn, faces=np.asarray(faces, dtype=np.int64),
-                chains=chains, colors=[nj, ni], ni=ni, nj=nj)
+    for ch in chains:
+        cells, es = ch["cells"], ch["edges"]
+        if ch["closed"]:
+            ids = [add(es[k], cells[k]) for k in range(len(cells))]
+            out_chains.append(ids + [ids[0]])
+        else:
+            n = len(cells)
+            ids = [add(es[k], cells[k]) for k in range(n)]
+            ids.append(add(es[n], cells[n - 1]))
+            out_chains.append(ids)
+    faces = np.asarray(faces, dtype=np.int64)
+    if bool(grid.is_split.any()):
+        _move_cell_zero(conn, faces, chains)
+    return Mesh(nodes=nodes, conn=conn, faces=faces, chains=out_chains, colors=colors,
+                ni=grid.ni, nj=grid.nj)
+
+
+def _move_cell_zero(conn: np.ndarray, faces: np.ndarray, chains: list) -> None:
+    """Give id 0 to a cell where the reference's id-0 ghost test is harmless.
+
+    computeRHS.cpp:158,170 mistake cell 0 for a ghost (or a ghost for cell
+    0) when it is mirrored into, or wrapped into, a ghost slot other than
+    the two it special-cases.  Those are the 2nd and 3rd cells from either
+    end of an open chain and the three cells either side of a closed
+    chain's seam.
+    """
+    bad = set()
+    for ch in chains:
+        cells = ch["cells"]
+        n = len(cells)
+        if ch["closed"]:
+            idx = [0, 1, 2, n - 3, n - 2, n - 1]
+        else:
+            idx = [1, 2, n - 2, n - 3]
+        bad.update(cells[k] for k in idx if 0 <= k < n)
+    if 0 not in bad:
+        return
+    k = next(c for c in range(conn.shape[0]) if c not in bad)
+    conn[[0, k]] = conn[[k, 0]]
+    for col in (2, 3):
+        v = faces[:, col]
+        z, kk = v == 0, v == k
+        v[z], v[kk] = k, 0
+
+
+def validate(mesh: Mesh) -> dict:
+    """Check a mesh against the chain model the solver relies on; returns stats.
+
+    Raises ``ValueError`` unless: every face lies in exactly one chain; each
+    chain is a path (or loop) of distinct cells with face k between cells
+    k-1 (right) and k (left) and its end faces' left cell the end cell; every
+    cell lies on a chain and chains of one colour share no cell; each face
+    normal points out of its left cell; every cell has positive area.
+    """
+    faces, nodes = mesh.faces, mesh.nodes
+    nf, nc = mesh.n_face, mesh.n_cell
+    seen = np.zeros(nf, dtype=np.int64)
+    on_chain = np.zeros(nc, dtype=np.int64)
+    left, right = faces[:, 2], faces[:, 3]
+    lengths = []
+    ch_id = 0
+    for col, ncol in enumerate(mesh.colors):
+        in_colour = np.zeros(nc, dtype=bool)
+        for _ in range(ncol):
+            ch = list(mesh.chains[ch_id])
+            closed = ch[0] == ch[-1]
+            body = ch[:-1] if closed else ch
+            for f in body:
+                seen[f] += 1
+            if closed:
+                cells = [int(left[f]) for f in body]
+                for k, f in enumerate(body):
+                    if right[f] != cells[k - 1]:
+                        raise ValueError("chain %d face %d: right cell is not the previous cell" % (ch_id, k))
+            else:
+                cells = [int(left[f]) for f in body[:-1]]
+                if int(left[body[-1]]) != cells[-1]:
+                    raise ValueError("chain %d: last face's left cell is not the end cell" % ch_id)
+                for k in range(1, len(body) - 1):
+                    if right[body[k]] != cells[k - 1]:
+                        raise ValueError("chain %d face %d: right cell is not the previous cell" % (ch_id, k))
+            if len(set(cells)) != len(cells):
+                raise ValueError("chain %d visits a cell twice" % ch_id)
+            if in_colour[cells].any():
+                raise ValueError("chain %d shares a cell with another chain of colour %d" % (ch_id, col))
+            in_colour[cells] = True
+            on_chain[cells] += 1
+            lengths.append(len(cells))
+            ch_id += 1
+    if ch_id != len(mesh.chains):
+        raise ValueError("colour counts do not add up to the chain count")
+    if (seen != 1).any():
+        raise ValueError("%d faces are not on exactly one chain" % int((seen != 1).sum()))
+    if (on_chain == 0).any():
+        raise ValueError("%d cells lie on no chain" % int((on_chain == 0).sum()))
+    cen = nodes[mesh.conn].mean(axis=1)
+    tri = mesh.conn[:, 2] == mesh.conn[:, 3]
+    cen[tri] = nodes[mesh.conn[tri, :3]].mean(axis=1)
+    p1, p2 = nodes[faces[:, 0]], nodes[faces[:, 1]]
+    nrm = np.stack([p2[:, 1] - p1[:, 1], -(p2[:, 0] - p1[:, 0])], axis=1)
+    mid = 0.5 * (p1 + p2)
+    if ((nrm * (mid - cen[left])).sum(axis=1) <= 0).any():
+        raise ValueError("a face normal points into its left cell")
+    dv = 0.5 * (p1[:, 0] * p2[:, 1] - p2[:, 0] * p1[:, 1])
+    vol = np.zeros(nc)
+    np.add.at(vol, left, dv)
+    inner = right >= 0
+    np.add.at(vol, right[inner], -dv[inner])
+    if (vol <= 0).any():
+        raise ValueError("%d cells have non-positive area" % int((vol <= 0).sum()))
+    lengths = np.asarray(lengths)
+    return {"cells": nc, "faces": nf, "chains": len(mesh.chains), "triangles": int(tri.sum()),
+            "min_chain": int(lengths.min()), "mean_chain": float(lengths.mean()),
+            "max_chain": int(lengths.max()), "quads_on_two": int((on_chain[~tri] == 2).sum()),
+            "tris_on_one": int((on_chain[tri] == 1).sum())}
 
 
 def default_inputs(**over) -> dict:
@@ -213,5 +665,7 @@ def write_case(case_dir: str, mesh: Mesh, inputs: dict | None = None,
 def make_case(case_dir: str, ni: int, nj: int, **inputs) -> str:
     """Generate an O-grid case directory in one call (keyword args are inputs)."""
     loop_start = inputs.pop("loop_start", None)
-    mesh = naca0012_ogrid(ni, nj, loop_start=loop_start)
+    split = inputs.pop("split", 0.0)
+    seed = inputs.pop("seed", 0)
+    mesh = naca0012_ogrid(ni, nj, loop_start=loop_start, split=split, seed=seed)
     return write_case(case_dir, mesh, inputs)

@@ -31,7 +31,10 @@ class HamstrError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("order", ctypes.c_int), ("msweep", ctypes.c_int), ("CFL", ctypes.c_double),
                 ("gamma", ctypes.c_double), ("rinf", ctypes.c_double), ("uinf", ctypes.c_double),
-                ("vinf", ctypes.c_double), ("einf", ctypes.c_double)]
+                ("vinf", ctypes.c_double), ("einf", ctypes.c_double), ("chain_end_rule", ctypes.c_int)]
+
+END_RULE_REFERENCE = 0
+END_RULE_EXTENDED = 1
 
 
 def lib_path() -> str:
@@ -60,6 +63,8 @@ def load(build_if_missing: bool = False):
         "hamstr_case_get": (i, [vp, cp, vp]),
         "hamstr_case_set_run": (i, [vp, i, i, d]),
         "hamstr_case_set_freestream": (i, [vp, d, d, d]),
+        "hamstr_case_set_option": (i, [vp, ctypes.c_char_p, i]),
+        "hamstr_gpu_set_cfl": (i, [vp, d]),
         "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
         "hamstr_gpu_create_from_case": (i, [vp, pp]),
         "hamstr_gpu_destroy": (i, [vp]),
@@ -195,6 +200,10 @@ class Case:
     def set_freestream(self, uinf: float, vinf: float, einf: float):
         _check(load().hamstr_case_set_freestream(self.h, uinf, vinf, einf))
 
+    def set_option(self, name: str, value: int) -> None:
+        """Project options (``chain_end_rule``: END_RULE_REFERENCE / END_RULE_EXTENDED)."""
+        _check(load().hamstr_case_set_option(self.h, name.encode(), int(value)))
+
 
 class GpuSolver:
     """Device solver handle (the SOLVER of the drop-in)."""
@@ -224,6 +233,10 @@ class GpuSolver:
         """False: plain FP64 (bit-identical); True: FP64 residual with an FP32
         Jacobian/ADI operator (defect correction)."""
         _check(load().hamstr_gpu_set_precision(self.h, int(bool(mixed))))
+
+    def set_cfl(self, cfl: float) -> None:
+        """CFL of later steps (a project addition for CFL ramping)."""
+        _check(load().hamstr_gpu_set_cfl(self.h, float(cfl)))
 
     def step_explicit(self, scheme: str) -> np.ndarray:
         out = np.zeros(2)

@@ -52,7 +52,20 @@ typedef struct hamstr_gpu_params {
    double CFL;        /*                                  solnBlock.h:41 */
    double gamma;      /* 1.4                              initFlow.cpp:19 */
    double rinf, uinf, vinf, einf;   /* freestream         initFlow.cpp:24-57 */
+   /* project option, no reference counterpart: how open chains take ghost
+      states at their end faces.  HAMSTR_END_RULE_REFERENCE (0) is
+      computeRHS.cpp:86-149, 154-260 and ADI.cpp:126-190 exactly;
+      HAMSTR_END_RULE_EXTENDED (1) lets open chains end at interior faces
+      (mixed tri/quad meshes): ghosts beyond such a face hold the true
+      neighbour's state, its coupling to that neighbour is lagged in ADI
+      while both diagonal terms stay implicit, and wall ghosts mirror by
+      position.  On meshes whose open chains all end at walls or the far
+      field and have at least 3 cells, both rules give the same results. */
+   int    chain_end_rule;
 } hamstr_gpu_params;
+
+#define HAMSTR_END_RULE_REFERENCE 0
+#define HAMSTR_END_RULE_EXTENDED  1
 
 /* ---------------- host side (reader, preprocessing, initial state) -------
  * Replaces MESHBLOCK::readMeshData (io.cpp:58-372), SOLNBLOCK::
@@ -73,6 +86,9 @@ int  hamstr_case_get(const hamstr_case* c, const char* name, double* out);
 /* overrides of input.hamstr values (order, msweep, CFL) and the freestream */
 int  hamstr_case_set_run(hamstr_case* c, int order, int msweep, double cfl);
 int  hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double einf);
+/* Project options (no reference counterpart): "chain_end_rule" =
+ * HAMSTR_END_RULE_*.  Used by hamstr_gpu_create_from_case. */
+int  hamstr_case_set_option(hamstr_case* c, const char* name, int value);
 
 /* ---------------- device solver ------------------------------------------
  * hamstr_gpu_create replaces SOLVER::SOLVER (solver.cpp:13-81): it copies
@@ -122,6 +138,11 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
  *                converged state is the FP64 residual's zero; the iteration
  *                history differs from the reference's. */
 int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
+
+/* Changes the pseudo-time CFL number of later steps (no counterpart in the
+ * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
+ * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */
+int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl);
 
 /* SOLVER::stepSolution, explicit branches (march.cpp:342-377): scheme 0 is
  * "euler" (computeRHS("explicit") then q += CFL/sigma r), scheme 1 the

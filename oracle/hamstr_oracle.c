@@ -51,6 +51,9 @@ struct ho_case {
    /* flow (initFlow.cpp) */
    double gamma, gm1, rinf, pinf, uinf, vinf, einf;
    int nGhost;
+   /* project option, not in the reference: how open chains take ghost
+      states at their end faces (HO_END_RULE_*) */
+   int end_rule;
    double L2Norm, LInfNorm;
    /* solution arrays (solver.cpp:26-38) */
    double *q, *qt, *r, *r0, *dq, *sigma;
@@ -320,14 +323,70 @@ static int chain_stencil(ho_case* c, int ich)
    return size;
 }
 
+/* One ghost state of the extended end rule: the true neighbour across an
+   interior end face, the wall mirror of end cell `mc`, or the freestream. */
+static void ghost_ext(ho_case* c, int j, int iface, int mc, const double* dqv)
+{
+   int right = c->faces[6 * iface + 4], k;
+   if (right >= 0) {
+      for (k = 0; k < NQ; k++) {
+         c->f[j][k] = c->q[NQ * right + k];
+         if (dqv) c->df[j][k] = dqv[NQ * right + k];
+      }
+   } else if (right == BC_WALL) {
+      const double* R = c->refMtx + 4 * iface;
+      const double* s = c->q + NQ * mc;
+      c->f[j][0] = s[0];
+      c->f[j][1] = (s[1] * R[0] + s[2] * R[1]);
+      c->f[j][2] = (s[1] * R[2] + s[2] * R[3]);
+      c->f[j][3] = s[3];
+      if (dqv) {
+         const double* d = dqv + NQ * mc;
+         c->df[j][0] = d[0];
+         c->df[j][1] = (d[1] * R[0] + d[2] * R[1]);
+         c->df[j][2] = (d[1] * R[2] + d[2] * R[3]);
+         c->df[j][3] = d[3];
+      }
+   } else {
+      c->f[j][0] = c->rinf;
+      c->f[j][1] = c->rinf * c->uinf;
+      c->f[j][2] = c->rinf * c->vinf;
+      c->f[j][3] = c->einf;
+      if (dqv) c->df[j][0] = c->df[j][1] = c->df[j][2] = c->df[j][3] = 0.0;
+   }
+}
+
 /* Fills the work arrays f (and df when dqv != NULL) from q (and dq) with
    wall-mirror and freestream ghosts (computeRHS.cpp:154-260,
    computeLinearRHS.cpp:148-276).  Cell id 0 is a ghost only at stencil
-   positions nGhost-1 and size-nGhost, as in the reference. */
+   positions nGhost-1 and size-nGhost, as in the reference.
+
+   Under HO_END_RULE_EXTENDED (a project rule for meshes whose open chains
+   may end at interior faces) the ghosts of an open chain are set by
+   position instead: the k-th ghost beyond an end face (k = 1..nGhost)
+   holds the true neighbour's state when the face is interior, the wall
+   mirror of the chain's k-th cell from that end (the last one for chains
+   shorter than k) at a wall, and the freestream at the far field. */
 static int chain_gather(ho_case* c, int ich, int size, const double* dqv)
 {
    int f1 = c->faceStart[ich], f2 = c->faceStart[ich + 1];
    int g = c->nGhost, j, k;
+   if (c->end_rule == HO_END_RULE_EXTENDED && c->chainConn[f1] != c->chainConn[f2 - 1]) {
+      int n = size - 2 * g;     /* cells on the chain */
+      for (j = g; j < g + n; j++) {
+         int icell = c->cindx[j];
+         for (k = 0; k < NQ; k++) {
+            c->f[j][k] = c->q[NQ * icell + k];
+            if (dqv) c->df[j][k] = dqv[NQ * icell + k];
+         }
+      }
+      for (k = 1; k <= g; k++) {
+         int mk = (k - 1 < n - 1) ? k - 1 : n - 1;
+         ghost_ext(c, g - k, c->chainConn[f1], c->cindx[g + mk], dqv);
+         ghost_ext(c, g + n - 1 + k, c->chainConn[f2 - 1], c->cindx[g + n - 1 - mk], dqv);
+      }
+      return 0;
+   }
    for (j = 0; j < size; j++) {
       int icell = c->cindx[j];
       if (icell >= 0) {
@@ -969,9 +1028,50 @@ int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int peri
 /* ADI (ADI.cpp:15-266)                                                */
 /* ------------------------------------------------------------------ */
 
+/* Extended rule: the end faces of open chains that lead into a cell of
+   another chain.  Returned as a CSR over cells (the face's right cell),
+   ascending face ids; NULL pointers when there are none. */
+static void foreign_faces(const ho_case* c, int** ptr, int** ent)
+{
+   int i, n = 0;
+   int* cnt = (int*)calloc((size_t)c->nCell + 1, sizeof(int));
+   for (i = 0; i < c->nChain; i++) {
+      int f1 = c->faceStart[i], f2 = c->faceStart[i + 1];
+      int a = c->chainConn[f1], b = c->chainConn[f2 - 1];
+      if (a == b) continue;
+      if (c->faces[6 * a + 4] >= 0) { cnt[c->faces[6 * a + 4] + 1]++; n++; }
+      if (c->faces[6 * b + 4] >= 0) { cnt[c->faces[6 * b + 4] + 1]++; n++; }
+   }
+   for (i = 0; i < c->nCell; i++) cnt[i + 1] += cnt[i];
+   *ptr = cnt;
+   *ent = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+   {
+      int* fill = (int*)malloc(sizeof(int) * (size_t)(c->nCell + 1));
+      int f;
+      memcpy(fill, cnt, sizeof(int) * (size_t)(c->nCell + 1));
+      /* ascending face ids: scan faces, keep chain-end faces */
+      char* isend = (char*)calloc((size_t)c->nFace + 1, 1);
+      for (i = 0; i < c->nChain; i++) {
+         int f1 = c->faceStart[i], f2 = c->faceStart[i + 1];
+         int a = c->chainConn[f1], b = c->chainConn[f2 - 1];
+         if (a == b) continue;
+         isend[a] = 1;
+         isend[b] = 1;
+      }
+      for (f = 0; f < c->nFace; f++) {
+         int r = c->faces[6 * f + 4];
+         if (isend[f] && r >= 0) (*ent)[fill[r]++] = f;
+      }
+      free(isend);
+      free(fill);
+   }
+}
+
 int ho_adi(ho_case* c, double* l2, double* linf)
 {
    int i, j, k, m, f, isweep, rc;
+   int *xptr = NULL, *xent = NULL;
+   if (c->end_rule == HO_END_RULE_EXTENDED) foreign_faces(c, &xptr, &xent);
    for (i = 0; i < c->nCell; i++) {
       double dtfac = c->CFL / c->sigma[i];
       for (m = 0; m < NQ; m++) {
@@ -1018,11 +1118,15 @@ int ho_adi(ho_case* c, double* l2, double* linf)
                      R[j][2] = rf[2] * r01 + rf[3] * r02;
                   }
                }
-               if (right < 0 && f == f2 - 1) m--;
+               /* extended rule: an interior last face couples explicitly,
+                  like the far field (the reference indexes a row past the
+                  chain there, ADI.cpp:166-181) */
+               int ext_last = (c->end_rule == HO_END_RULE_EXTENDED && f == f2 - 1);
+               if ((right < 0 || ext_last) && f == f2 - 1) m--;
                for (j = 0; j < NQ; j++) {
                   for (k = 0; k < NQ; k++) {
                      c->B[m][j][k] += L[j][k];
-                     if (mm1 > -1 && right > -1) {
+                     if (mm1 > -1 && right > -1 && !ext_last) {
                         c->A[m][j][k] += R[j][k];
                         c->B[mm1][j][k] -= R[j][k];
                         c->C[mm1][j][k] -= L[j][k];
@@ -1036,6 +1140,24 @@ int ho_adi(ho_case* c, double* l2, double* linf)
             m++;
          }
          size = size - (per == 0);
+         /* extended rule: a cell's first chain also carries the diagonal
+            term of every chain-end face that leads into it from another
+            chain (its right-cell Jacobian), so each face's diagonal terms
+            stay implicit; only the coupling across the end is lagged */
+         if (xptr) {
+            m = 0;
+            for (f = f1; f < f2 - 1; f++) {
+               int left = c->faces[6 * c->chainConn[f] + 2], e;
+               if (c->c2chain[2 * left] == i) {
+                  for (e = xptr[left]; e < xptr[left + 1]; e++) {
+                     const double* R = c->ff + 32 * xent[e] + 16;
+                     for (j = 0; j < NQ; j++)
+                        for (k = 0; k < NQ; k++) c->B[m][j][k] -= R[4 * j + k];
+                  }
+               }
+               m++;
+            }
+         }
          m = 0;
          for (f = f1; f < f2 - 1; f++) {
             int left = c->faces[6 * c->chainConn[f] + 2];
@@ -1060,8 +1182,10 @@ int ho_adi(ho_case* c, double* l2, double* linf)
       }
       for (i = 0; i < NQ * c->nCell; i++) c->dq[i] += c->r[i];
       rc = ho_linear_rhs(c, l2, linf);
-      if (rc) return rc;
+      if (rc) { free(xptr); free(xent); return rc; }
    }
+   free(xptr);
+   free(xent);
    for (i = 0; i < NQ * c->nCell; i++) c->q[i] += c->dq[i];
    *l2 = c->L2Norm; *linf = c->LInfNorm;
    return 0;
@@ -1212,6 +1336,16 @@ void ho_params(const ho_case* c, double* out)
 void ho_set_freestream(ho_case* c, double uinf, double vinf, double einf)
 {
    c->uinf = uinf; c->vinf = vinf; c->einf = einf;
+}
+
+int ho_set_option(ho_case* c, const char* name, int value)
+{
+   if (strcmp(name, "chain_end_rule") == 0) {
+      if (value != HO_END_RULE_REFERENCE && value != HO_END_RULE_EXTENDED) return -1;
+      c->end_rule = value;
+      return 0;
+   }
+   return -1;
 }
 
 void ho_set_run(ho_case* c, int order, int msweep, double cfl)

@@ -42,6 +42,18 @@ void ho_params(const ho_case* c, double* out);
 void ho_set_freestream(ho_case* c, double uinf, double vinf, double einf);
 void ho_set_run(ho_case* c, int order, int msweep, double cfl);
 
+/* Project options (absent from the reference):
+ *   "chain_end_rule"  HO_END_RULE_REFERENCE (0, default): ghosts exactly as
+ *                     computeRHS.cpp:86-149, 154-260; HO_END_RULE_EXTENDED
+ *                     (1): open chains may end at interior faces (mixed
+ *                     tri/quad meshes) -- ghosts beyond such a face hold the
+ *                     true neighbour's state and the face couples to it
+ *                     explicitly in ADI; wall ghosts mirror by position.
+ * Returns 0, or -1 for an unknown name or value. */
+#define HO_END_RULE_REFERENCE 0
+#define HO_END_RULE_EXTENDED 1
+int  ho_set_option(ho_case* c, const char* name, int value);
+
 /* Each returns 0, or -1 when a spectral radius is NaN (the reference exits
  * the process there, interfaceFlux.cpp:117-124). */
 int  ho_compute_rhs(ho_case* c, int implicit, double* l2, double* linf);

@@ -132,6 +132,18 @@ class OracleCase:
     def set_run(self, order, msweep, cfl):
         self._fn("set_run")(self.h, order, msweep, cfl)
 
+    def set_option(self, name: str, value: int) -> None:
+        """Project options of the restatement (``chain_end_rule``); the
+        reference build has none and accepts only the reference values."""
+        if self.kind != "port":
+            if value != 0:
+                raise ValueError("the reference has no option %s=%d" % (name, value))
+            return
+        fn = self.lib.ho_set_option
+        fn.restype, fn.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+        if fn(self.h, name.encode(), int(value)) != 0:
+            raise ValueError("bad oracle option %s=%r" % (name, value))
+
     def _check(self, rc):
         if rc is not None and rc != 0:
             raise RuntimeError("oracle returned status %d" % rc)

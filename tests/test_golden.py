@@ -20,13 +20,14 @@ def _load(name):
 
 
 def test_fixtures_present():
-    assert len(CASES) >= 4
+    assert len(CASES) >= 6
 
 
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_reproduces_golden(oracle_lib, name):
     g = _load(name)
     orc = oracle_lib.OracleCase(os.path.join(HERE, name), "port")
+    orc.set_option("chain_end_rule", int(g.get("end_rule", 0)))
     orc.set_freestream(*g["freestream"])
     orc.set("q", g["q0"])
     hist = orc.march(g["hist"].shape[0])
@@ -42,6 +43,7 @@ def test_gpu_reproduces_golden(native_lib, name):
     g = _load(name)
     case = native.Case(os.path.join(HERE, name))
     case.set_freestream(*g["freestream"])
+    case.set_option("chain_end_rule", int(g.get("end_rule", 0)))
     gpu = native.GpuSolver(case)
     gpu.set("q", g["q0"])
     for i, want in enumerate(g["hist"]):
