@@ -115,13 +115,14 @@ def test_mixed_precision_on_split_mesh(make_case, oracle_lib, native_lib):
     """FP32 operator on a half-split mesh reaches the FP64 oracle's steady state.
 
     On this coarse mesh the state at L2 = 1e-10 is still ~6e-4 from the
-    steady state (slow modes), so both runs go to 1e-14 before comparing."""
+    steady state (slow modes; 1e-14 still ~1e-8), so both run 8000 steps,
+    to below 1e-15, before comparing."""
     orc, gpu = _pair(make_case, oracle_lib, HALF, 1, order=1, CFL=10.0, msweep=2)
     gpu.set_precision(True)
-    hist, conv = gpu.march(8000, 1e-14)
-    assert conv, hist[-1, 0]
+    hist, _ = gpu.march(8000, 0.0)
+    assert hist[-1, 0] <= 1e-15, hist[-1, 0]
     ho = orc.march(8000)
-    assert ho[-1, 0] <= 1e-14
+    assert ho[-1, 0] <= 1e-15
     qo, qg = orc.get("q"), gpu.get("q")
     assert np.max(np.abs(qg - qo)) / np.max(np.abs(qo)) < 1e-8
 
