@@ -240,6 +240,16 @@ def run_gpu(args, wl, rank, local_rank, world):
         gpu.enqueue_steps(n)
     gpu.set_cfl(wl["CFL"])
     gpu.sync()
+    if args.profile_steps:
+        # a plain run of the workload for ncu: ramp, then N captured steps
+        gpu.set_precision(args.profile_precision == "mixed")
+        gpu.enqueue_steps(args.profile_steps)
+        gpu.sync()
+        if rank == 0:
+            print(json.dumps({"profile_steps": args.profile_steps, "precision": args.profile_precision,
+                              "workload": wl["name"], "ramp_steps": sum(n for n, _ in wl["ramp"]),
+                              "launches_per_step": gpu.launches_per_step()}), flush=True)
+        return None
     lay = gpu.layout()
     nc = sizes["nCell"]
     hs = torch.cuda.ExternalStream(gpu.stream)
@@ -441,6 +451,9 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-converge", action="store_true", help="skip the converged-solve leg")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only ramp and run this many steps (a plain run for ncu), no timing")
+    ap.add_argument("--profile-precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
     wl = WORKLOADS[args.workload]
