@@ -379,8 +379,9 @@ def converged_solves() -> dict:
     c = CONVERGE
     case_dir = make_case(c, 0)
     out = {"workload": c["name"], "tol": c["tol"], "cap": c["cap"]}
+    qs = {}
     for label, mixed in (("fp64", False), ("mixed", True)):
-        g = native.GpuSolver(native.Case(case_dir))
+        g = native.GpuSolver(open_case(c, case_dir))
         g.set_precision(mixed)
         g.march(3, 0.0)                       # graph capture and warm-up
         g.set("q", native.Case(case_dir).get("q"))
@@ -388,11 +389,21 @@ def converged_solves() -> dict:
         t0 = time.perf_counter()
         hist, ok = g.march(c["cap"], c["tol"])
         dt = time.perf_counter() - t0
+        f = g.forces()
+        qs[label] = g.get("q")
         out[label] = {"converged": ok, "steps": int(hist.shape[0]), "seconds": dt,
-                      "solves_per_s": (1.0 / dt) if ok else None, "final_l2": float(hist[-1, 0])}
+                      "solves_per_s": (1.0 / dt) if ok else None, "final_l2": float(hist[-1, 0]),
+                      "CL": f["CL"], "CD": f["CD"], "CM": f["CM"]}
         g.close()
     if out["fp64"]["converged"] and out["mixed"]["converged"]:
         out["mixed_speedup_vs_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+        import numpy as np
+        q64, qmx = qs["fp64"].reshape(-1, 4), qs["mixed"].reshape(-1, 4)
+        out["mixed_vs_fp64_at_tol"] = {
+            "max_rel_density": float(np.max(np.abs(qmx[:, 0] - q64[:, 0]) / np.abs(q64[:, 0]))),
+            "max_abs_over_max_q": float(np.max(np.abs(qmx - q64)) / np.max(np.abs(q64))),
+            "dCL": abs(out["mixed"]["CL"] - out["fp64"]["CL"]), "dCD": abs(out["mixed"]["CD"] - out["fp64"]["CD"]),
+            "note": "both states stopped at the same L2 tolerance; each is that far from the steady state"}
     return out
 
 

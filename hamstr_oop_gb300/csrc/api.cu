@@ -86,6 +86,13 @@ struct hamstr_gpu {
    double tol_host = 0.0;   // staging for the async copy into d.tol
    int mixed = 0;           // 0: FP64 drop-in, 1: FP32 operator defect correction
 
+   // wall faces (right cell tagged -2), ascending face id: the force integral
+   std::vector<int> wall_face, wall_n1, wall_n2;
+   std::vector<double> wall_normal;     // [nWall][2]
+   int* wall_cell = nullptr;            // device: adjacent cell per wall face
+   double4* wall_geo = nullptr;         // device: nx, ny, midpoint x, y (after set_geometry)
+   double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums
+
    // optional per-launch timing (hamstr_gpu_profile_step)
    std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>>* prof = nullptr;
    template <class F>
@@ -322,6 +329,16 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    for (int c = 0; c < P.nChain; c++)
       if (P.chain_periodic[c]) chain_facN[c] = nper++;
    std::vector<int> cell_written(P.cell_last_wave_writer);
+   std::vector<int> wall_cell;
+   for (int f = 0; f < nFace; f++) {
+      if (faces[6 * (size_t)f + 4] != -2) continue;
+      g->wall_face.push_back(f);
+      g->wall_n1.push_back(faces[6 * (size_t)f]);
+      g->wall_n2.push_back(faces[6 * (size_t)f + 1]);
+      g->wall_normal.push_back(normVec[2 * (size_t)f]);
+      g->wall_normal.push_back(normVec[2 * (size_t)f + 1]);
+      wall_cell.push_back(faces[6 * (size_t)f + 2]);
+   }
 
    int st = HAMSTR_GPU_OK;
    auto& o = g->owned;
@@ -384,6 +401,8 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    TRY(dalloc(&d.tol, 1, o));
    d.hist_cap = 1 << 16;
    TRY(dalloc(&d.hist, 4 * (size_t)d.hist_cap, o));
+   TRY(upload(&g->wall_cell, wall_cell, o));
+   TRY(dalloc(&g->wall_scr, 3 * wall_cell.size() + 3, o));
 #undef TRY
    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
    if (e != cudaSuccess) {
@@ -744,6 +763,59 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
 }
 
 }  // extern "C"
+
+extern "C" int hamstr_gpu_set_geometry(hamstr_gpu* g, int nNode, const double* xy)
+{
+   if (!g || !xy || nNode <= 0) return HAMSTR_GPU_ERR_ARG;
+   const size_t nw = g->wall_face.size();
+   std::vector<double4> geo(nw);
+   for (size_t k = 0; k < nw; k++) {
+      const int a = g->wall_n1[k], b = g->wall_n2[k];
+      if (a < 0 || a >= nNode || b < 0 || b >= nNode) {
+         set_error("wall face node id outside the node array");
+         return HAMSTR_GPU_ERR_ARG;
+      }
+      geo[k] = make_double4(g->wall_normal[2 * k], g->wall_normal[2 * k + 1], 0.5 * (xy[2 * (size_t)a] + xy[2 * (size_t)b]),
+                            0.5 * (xy[2 * (size_t)a + 1] + xy[2 * (size_t)b + 1]));
+   }
+   if (!g->wall_geo) {
+      int st = dalloc(&g->wall_geo, nw, g->owned);
+      if (st) return st;
+   }
+   if (nw) CK(cudaMemcpyAsync(g->wall_geo, geo.data(), nw * sizeof(double4), cudaMemcpyHostToDevice, g->stream));
+   CK(cudaStreamSynchronize(g->stream));
+   return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_forces(hamstr_gpu* g, double* out)
+{
+   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
+   if (!g->wall_geo) {
+      set_error("hamstr_gpu_forces needs hamstr_gpu_set_geometry first");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   const DeviceState& d = g->d;
+   const int nw = (int)g->wall_face.size();
+   double* sums = g->wall_scr + 3 * (size_t)nw;
+   launch_forces(d.q, g->wall_cell, g->wall_geo, nw, d.fc.gamma - 1.0, g->wall_scr, sums, g->stream);
+   CK(cudaGetLastError());
+   double s[3];
+   CK(cudaMemcpyAsync(s, sums, sizeof(s), cudaMemcpyDeviceToHost, g->stream));
+   CK(cudaStreamSynchronize(g->stream));
+   // coefficients on a unit chord from the freestream (same expressions as
+   // the oracle's ho_forces)
+   const double V2 = d.fc.uinf * d.fc.uinf + d.fc.vinf * d.fc.vinf;
+   const double qinf = 0.5 * d.fc.rinf * V2;
+   const double V = std::sqrt(V2);
+   const double ca = d.fc.uinf / V, sa = d.fc.vinf / V;
+   out[0] = s[0];
+   out[1] = s[1];
+   out[2] = s[2];
+   out[3] = (s[1] * ca - s[0] * sa) / qinf;
+   out[4] = (s[0] * ca + s[1] * sa) / qinf;
+   out[5] = s[2] / qinf;
+   return HAMSTR_GPU_OK;
+}
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
 {

@@ -110,6 +110,9 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
 int adi_configure(int max_dynamic_smem);
+// launcher (forces.cu): out = {Fx, Fy, M} over n wall faces, scr = 3n doubles
+void launch_forces(const double* q, const int* wall_cell, const double4* geo, int n, double gm1, double* scr,
+                   double* out, cudaStream_t st);
 
 }  // namespace hamstr
 #endif

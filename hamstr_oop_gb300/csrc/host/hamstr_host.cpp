@@ -316,6 +316,7 @@ void SOLVER::ensureGpu()
    p.chain_end_rule = sb->chainEndRule;
    check(hamstr_gpu_create(&p, mb->nCell, mb->nFace, mb->faces.data(), mb->normVec.data(), mb->refMtx.data(),
                            mb->nChain, mb->faceStartPerChain.data(), mb->chainConn.data(), &gpu));
+   check(hamstr_gpu_set_geometry(gpu, mb->nNode, mb->x.data()));
    check(hamstr_gpu_set(gpu, "q", sb->q.data()));
 }
 
@@ -587,6 +588,8 @@ int hamstr_case::create_gpu(const hamstr_case& c, hamstr_gpu** out)
    int st = hamstr_gpu_create(&p, c.mb.nCell, c.mb.nFace, c.mb.faces.data(), c.mb.normVec.data(),
                               c.mb.refMtx.data(), c.mb.nChain, c.mb.faceStartPerChain.data(),
                               c.mb.chainConn.data(), out);
+   if (st != HAMSTR_GPU_OK) return st;
+   st = hamstr_gpu_set_geometry(*out, c.mb.nNode, c.mb.x.data());
    if (st != HAMSTR_GPU_OK) return st;
    return hamstr_gpu_set(*out, "q", c.sb.q.data());
 }

@@ -65,6 +65,8 @@ def load(build_if_missing: bool = False):
         "hamstr_case_set_freestream": (i, [vp, d, d, d]),
         "hamstr_case_set_option": (i, [vp, ctypes.c_char_p, i]),
         "hamstr_gpu_set_cfl": (i, [vp, d]),
+        "hamstr_gpu_set_geometry": (i, [vp, i, vp]),
+        "hamstr_gpu_forces": (i, [vp, vp]),
         "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
         "hamstr_gpu_create_from_case": (i, [vp, pp]),
         "hamstr_gpu_destroy": (i, [vp]),
@@ -233,6 +235,12 @@ class GpuSolver:
         """False: plain FP64 (bit-identical); True: FP64 residual with an FP32
         Jacobian/ADI operator (defect correction)."""
         _check(load().hamstr_gpu_set_precision(self.h, int(bool(mixed))))
+
+    def forces(self) -> dict:
+        """Wall pressure force of the current state: Fx, Fy, M (about x=0.25), CL, CD, CM."""
+        out = np.zeros(6)
+        _check(load().hamstr_gpu_forces(self.h, _ptr(out)))
+        return dict(zip(("Fx", "Fy", "M", "CL", "CD", "CM"), (float(v) for v in out)))
 
     def set_cfl(self, cfl: float) -> None:
         """CFL of later steps (a project addition for CFL ramping)."""

@@ -139,6 +139,18 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
  *                history differs from the reference's. */
 int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
 
+/* Wall forces (no counterpart in the reference, which computes none).
+ * hamstr_gpu_set_geometry hands over the node coordinates (x y per node,
+ * coord.dat order; io.cpp:144-156) for the faces' midpoints;
+ * hamstr_gpu_create_from_case does it itself.  hamstr_gpu_forces then
+ * integrates the wall pressure of the current state: for each wall face
+ * (right cell -2, ascending face id) p * (dy, -dx) with p from the adjacent
+ * cell, summed in face order, and the moment about (0.25, 0).
+ * out6 = {Fx, Fy, M, CL, CD, CM} with coefficients on a unit chord and the
+ * freestream dynamic pressure and flow direction. */
+int hamstr_gpu_set_geometry(hamstr_gpu* g, int nNode, const double* xy);
+int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
+
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
  * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */

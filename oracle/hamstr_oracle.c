@@ -1267,6 +1267,46 @@ int ho_march_replicas(ho_case** cases, int n, int iters)
 /* handle                                                              */
 /* ------------------------------------------------------------------ */
 
+/* ------------------------------------------------------------------ */
+/* wall forces (project addition; the reference has none)              */
+/* ------------------------------------------------------------------ */
+
+/* Pressure force on the wall faces (bFaces, preprocess.cpp:180-184, in
+   ascending face order) from the adjacent cell's pressure, its moment
+   about (0.25, 0), and the coefficients on a unit chord:
+   out = {Fx, Fy, M, CL, CD, CM}. */
+int ho_forces(const ho_case* c, double* out)
+{
+   double Fx = 0.0, Fy = 0.0, M = 0.0;
+   double V2, qinf, V, ca, sa;
+   int k;
+   for (k = 0; k < c->nBface; k++) {
+      int f = c->bFaces[k];
+      const int* fr = c->faces + 6 * f;
+      const double* s = c->q + NQ * fr[2];
+      double p = c->gm1 * (s[3] - 0.5 * (s[1] * s[1] + s[2] * s[2]) / s[0]);
+      double fx = p * c->normVec[2 * f];
+      double fy = p * c->normVec[2 * f + 1];
+      double xm = 0.5 * (c->x[2 * fr[0]] + c->x[2 * fr[1]]);
+      double ym = 0.5 * (c->x[2 * fr[0] + 1] + c->x[2 * fr[1] + 1]);
+      Fx = Fx + fx;
+      Fy = Fy + fy;
+      M = M + ((xm - 0.25) * fy - ym * fx);
+   }
+   V2 = c->uinf * c->uinf + c->vinf * c->vinf;
+   qinf = 0.5 * c->rinf * V2;
+   V = sqrt(V2);
+   ca = c->uinf / V;
+   sa = c->vinf / V;
+   out[0] = Fx;
+   out[1] = Fy;
+   out[2] = M;
+   out[3] = (Fy * ca - Fx * sa) / qinf;
+   out[4] = (Fx * ca + Fy * sa) / qinf;
+   out[5] = M / qinf;
+   return 0;
+}
+
 ho_case* ho_open(const char* dir, char* err, int errlen)
 {
    ho_case* c = (ho_case*)calloc(1, sizeof(ho_case));

@@ -70,6 +70,11 @@ int  ho_update_solution(ho_case* c, const char* qold, const char* qnew, double c
  * case (OpenMP); the CPU-baseline throughput leg. */
 int  ho_march_replicas(ho_case** cases, int n, int iters);
 
+/* Wall pressure force (project addition, no reference counterpart): the
+ * wall faces' p * normal, p from the adjacent cell, summed in ascending face
+ * order; out = {Fx, Fy, M about (0.25, 0), CL, CD, CM} on a unit chord. */
+int ho_forces(const ho_case* c, double* out6);
+
 /* triSolvers.cpp blockTridag4 / blockTridagPeriodic4 on flat [N][4][4]
  * blocks and [N][4] right-hand sides, in place like the reference. */
 int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic);

@@ -144,6 +144,16 @@ class OracleCase:
         if fn(self.h, name.encode(), int(value)) != 0:
             raise ValueError("bad oracle option %s=%r" % (name, value))
 
+    def forces(self) -> dict:
+        """Wall pressure force (project addition, restated by ho_forces)."""
+        if self.kind != "port":
+            raise ValueError("the reference computes no forces")
+        fn = self.lib.ho_forces
+        fn.restype, fn.argtypes = ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]
+        out = np.zeros(6)
+        self._check(fn(self.h, _ptr(out)))
+        return dict(zip(("Fx", "Fy", "M", "CL", "CD", "CM"), (float(v) for v in out)))
+
     def _check(self, rc):
         if rc is not None and rc != 0:
             raise RuntimeError("oracle returned status %d" % rc)
