@@ -51,8 +51,11 @@ WORKLOADS = {
                name="naca0012_ogrid_512x128_split50_weno5_cfl20_msweep2"),
     "c2quad": dict(ni=512, nj=128, split=0.0, seed=0, end_rule=0, order=5, CFL=20.0, msweep=2, Mach=0.5,
                    alpha=1.25, ramp=(), name="naca0012_ogrid_512x128_weno5_cfl20_msweep2"),
-    "c1": dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=3, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
-               ramp=(), name="naca0012_ogrid_128x32_muscl3_cfl10_msweep2"),
+    "c1": dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=3, limiter=1, CFL=10.0, msweep=2, Mach=0.5,
+               alpha=1.25, ramp=(), name="naca0012_ogrid_128x32_muscl_minmod_cfl10_msweep2"),
+    "c3": dict(ni=1024, nj=256, split=0.3, seed=0, end_rule=1, order=3, limiter=2, CFL=10.0, msweep=2, Mach=0.8,
+               alpha=1.25, ramp=((50, 2.0), (50, 5.0)),
+               name="naca0012_ogrid_1024x256_split30_muscl_vanalbada_m08_cfl10_msweep2"),
 }
 # converged-solve measurement: a case that reaches 1e-10 (the MUSCL and WENO
 # cases plateau near 1e-9 on these meshes, as the survey's probes found)
@@ -77,6 +80,9 @@ def make_case(wl: dict, rank: int) -> str:
     return d
 
 
+LIMITER_NAMES = {0: "reference kappa-limiter", 1: "minmod", 2: "van Albada"}
+
+
 def mesh_note(wl: dict) -> str:
     if wl["split"] > 0:
         return ("NACA 0012 O-grid, each quad split into two triangles with probability %g (seed %d); "
@@ -88,6 +94,7 @@ def open_case(wl: dict, case_dir: str):
     from hamstr_oop_gb300 import native
     case = native.Case(case_dir)
     case.set_option("chain_end_rule", wl["end_rule"])
+    case.set_option("limiter", wl.get("limiter", 0))
     return case
 
 
@@ -95,6 +102,7 @@ def open_oracle(wl: dict, case_dir: str):
     from oracle import oracle
     o = oracle.OracleCase(case_dir, "port")
     o.set_option("chain_end_rule", wl["end_rule"])
+    o.set_option("limiter", wl.get("limiter", 0))
     return o
 
 
@@ -362,7 +370,8 @@ def run_gpu(args, wl, rank, local_rank, world):
                        "order": wl["order"], "msweep": wl["msweep"], "CFL": wl["CFL"], "mach": wl["Mach"],
                        "alpha_deg": wl["alpha"], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "512 MiB flush write between timed steps (untimed)",
-                       "mesh": mesh_note(wl), "cfl_ramp_before_timing": [list(r) for r in wl["ramp"]]},
+                       "mesh": mesh_note(wl), "cfl_ramp_before_timing": [list(r) for r in wl["ramp"]],
+                       "limiter": LIMITER_NAMES[wl.get("limiter", 0)] if wl["order"] == 3 else None},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "mixed_precision": mixed, "converged": conv,
             "gpu_launches": gpu.launches_per_step() * args.steps,

@@ -268,6 +268,10 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
       set_error("msweep must be >= 1 and CFL > 0");
       return HAMSTR_GPU_ERR_ARG;
    }
+   if (p->limiter < HAMSTR_LIMITER_REFERENCE || p->limiter > HAMSTR_LIMITER_VANALBADA) {
+      set_error("unknown limiter");
+      return HAMSTR_GPU_ERR_ARG;
+   }
    MeshInput in;
    in.nCell = nCell;
    in.nFace = nFace;
@@ -300,6 +304,7 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    d.nRow = P.nRow;
    d.nChain = P.nChain;
    d.order = P.order;
+   d.recon = (P.order == 3 && p->limiter != HAMSTR_LIMITER_REFERENCE) ? 30 + p->limiter : P.order;
    d.nGhost = P.nGhost;
    d.fc.gamma = p->gamma;
    d.fc.rinf = p->rinf;

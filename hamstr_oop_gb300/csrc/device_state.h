@@ -34,6 +34,7 @@ struct FlowConst {
 
 struct DeviceState {
    int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
+   int recon;              // reconstruction code: order, or 31/32 for MUSCL with a project limiter (recon.cuh)
    FlowConst fc;
    double fs1, fs2;        // freestream rho*u, rho*v (computeRHS.cpp:247-248)
 

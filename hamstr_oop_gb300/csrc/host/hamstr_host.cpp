@@ -207,6 +207,13 @@ void SOLNBLOCK::setChainEndRule(int rule)
    chainEndRule = rule;
 }
 
+void SOLNBLOCK::setLimiter(int lim)
+{
+   if (lim < HAMSTR_LIMITER_REFERENCE || lim > HAMSTR_LIMITER_VANALBADA)
+      throw hamstr::Error(HAMSTR_GPU_ERR_ARG, "unknown limiter");
+   limiter = lim;
+}
+
 void SOLNBLOCK::readSolutionInputs(const std::string& root)
 {
    const std::string p = (root.empty() ? std::string("") : root + "/") + "input.hamstr";
@@ -314,6 +321,7 @@ void SOLVER::ensureGpu()
    p.vinf = sb->vinf;
    p.einf = sb->einf;
    p.chain_end_rule = sb->chainEndRule;
+   p.limiter = sb->limiter;
    check(hamstr_gpu_create(&p, mb->nCell, mb->nFace, mb->faces.data(), mb->normVec.data(), mb->refMtx.data(),
                            mb->nChain, mb->faceStartPerChain.data(), mb->chainConn.data(), &gpu));
    check(hamstr_gpu_set_geometry(gpu, mb->nNode, mb->x.data()));
@@ -570,6 +578,11 @@ int hamstr_case::set_option(hamstr_case& c, const std::string& name, int value)
       c.sb.chainEndRule = value;
       return HAMSTR_GPU_OK;
    }
+   if (name == "limiter") {
+      if (value < HAMSTR_LIMITER_REFERENCE || value > HAMSTR_LIMITER_VANALBADA) return HAMSTR_GPU_ERR_ARG;
+      c.sb.limiter = value;
+      return HAMSTR_GPU_OK;
+   }
    return HAMSTR_GPU_ERR_ARG;
 }
 
@@ -606,6 +619,7 @@ hamstr_gpu_params hamstr_case::gpu_params(const hamstr_case& c)
    p.vinf = c.sb.vinf;
    p.einf = c.sb.einf;
    p.chain_end_rule = c.sb.chainEndRule;
+   p.limiter = c.sb.limiter;
    return p;
 }
 

@@ -73,6 +73,7 @@ class SOLNBLOCK
    int visc = 0;
    int nGhost = 2;
    int chainEndRule = 0;   // project option: HAMSTR_END_RULE_* (not in the reference)
+   int limiter = 0;        // project option: HAMSTR_LIMITER_* (not in the reference)
    double uinf = 0, vinf = 0, winf = 0, einf = 0, pinf = 0, rinf = 0;
    double gamma = 0, invGamma = 0, gm1 = 0, c2b = 0, rgas = 0, pr = 0, prtr = 0;
    double LInfNorm = 0, L2Norm = 0;
@@ -88,6 +89,8 @@ class SOLNBLOCK
    // project addition: HAMSTR_END_RULE_* for meshes whose open chains end
    // at interior faces (mixed tri/quad meshes); throws on other values
    void setChainEndRule(int rule);
+   // project addition: HAMSTR_LIMITER_* for order 3; throws on other values
+   void setLimiter(int lim);
 };
 
 // ------------------------------------------------------------------

@@ -455,9 +455,13 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
 {
    const int b = blocks_for(d.nSlot);
-   if (d.order == 1) mx_rhs_face_kernel<1><<<b, kThreads, 0, st>>>(d);
-   else if (d.order == 3) mx_rhs_face_kernel<3><<<b, kThreads, 0, st>>>(d);
-   else mx_rhs_face_kernel<5><<<b, kThreads, 0, st>>>(d);
+   switch (d.recon) {
+      case 1: mx_rhs_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
+      case 3: mx_rhs_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
+      case 5: mx_rhs_face_kernel<5><<<b, kThreads, 0, st>>>(d); break;
+      case 31: mx_rhs_face_kernel<31><<<b, kThreads, 0, st>>>(d); break;
+      default: mx_rhs_face_kernel<32><<<b, kThreads, 0, st>>>(d); break;
+   }
 }
 
 void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d); }
@@ -485,9 +489,13 @@ void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st)
 {
    const int b = blocks_for(d.nSlot);
-   if (d.order == 1) mx_lin_face_kernel<1><<<b, kThreads, 0, st>>>(d);
-   else if (d.order == 3) mx_lin_face_kernel<3><<<b, kThreads, 0, st>>>(d);
-   else mx_lin_face_kernel<5><<<b, kThreads, 0, st>>>(d);
+   switch (d.recon) {
+      case 1: mx_lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
+      case 3: mx_lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
+      case 5: mx_lin_face_kernel<5><<<b, kThreads, 0, st>>>(d); break;
+      case 31: mx_lin_face_kernel<31><<<b, kThreads, 0, st>>>(d); break;
+      default: mx_lin_face_kernel<32><<<b, kThreads, 0, st>>>(d); break;
+   }
 }
 
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st)

@@ -19,6 +19,23 @@ namespace hamstr {
 constexpr double kTh = 0.3333333333333333e+00;   // THIRD (utils.h:52)
 constexpr double kEps = 1e-10;                  // computeRHS.cpp:271
 
+// Reconstruction codes (template argument ORDER): 1, 3 (MUSCL with the
+// reference's limiter, reconstruction.cpp:16-70), 5 (WENO), and MUSCL with
+// one of the project's limiters (no reference counterpart):
+//   31  minmod-limited differences of the kappa scheme (Anderson, Thomas and
+//       van Leer, AIAA J. 24(9), 1986): a~ = minmod(a, b*beta),
+//       b~ = minmod(b, a*beta), beta = (3 - kappa)/(1 - kappa) = 4;
+//       ql = f + qt (thm a~ + thp b~), qr = f - qt (thp a~ + thm b~)
+//   32  van Albada's differentiable limiter in the same paper's form:
+//       s = (2ab + eps)/(a^2 + b^2 + eps), sk = kappa s;
+//       ql = f + qt s ((1 - sk) a + (1 + sk) b),
+//       qr = f - qt s ((1 + sk) a + (1 - sk) b)
+// with a = f_i - f_{i-1}, b = f_{i+1} - f_i, kappa = 1/3, qt = 1/4.  The
+// linearised forms (for the sweeps' residual) are the exact derivatives,
+// minmod with its selection frozen.
+enum { RECON_MUSCL_MINMOD = 31, RECON_MUSCL_VANALBADA = 32 };
+__host__ __device__ constexpr bool is_muscl(int r) { return r == 3 || r == RECON_MUSCL_MINMOD || r == RECON_MUSCL_VANALBADA; }
+
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
 {
    const double2 a = *reinterpret_cast<const double2*>(p);
@@ -102,6 +119,82 @@ __device__ __forceinline__ void muscl2(double fm1, double f0, double fp1, double
       const double f3qt = qt * (a1 / a2);
       qr_n1 = fp1 - f3qt * (thp * f20 + thm * f2p);
    }
+}
+
+// minmod(x, y) as a selection: 0 -> 0, 1 -> x, 2 -> y
+__device__ __forceinline__ int minmod_sel(double x, double y)
+{
+   if (x > 0.0) return (y <= 0.0) ? 0 : ((x <= y) ? 1 : 2);
+   if (x < 0.0) return (y >= 0.0) ? 0 : ((x >= y) ? 1 : 2);
+   return 0;
+}
+template <typename T>
+__device__ __forceinline__ T pick(int sel, T x, T y) { return sel == 0 ? T(0) : (sel == 1 ? x : y); }
+
+// project limiters (RECON_MUSCL_MINMOD / _VANALBADA), one cell: ql, qr at
+// its two faces from a = f - fm, b = fp - f
+template <int R>
+__device__ __forceinline__ void muscl_lim_cell(double f, double a, double b, double& ql, double& qr)
+{
+   const double qt = 0.25;
+   const double thm = 1.0 - kTh, thp = 1.0 + kTh;
+   if (R == RECON_MUSCL_MINMOD) {
+      const double at = pick<double>(minmod_sel(a, 4.0 * b), a, 4.0 * b);
+      const double bt = pick<double>(minmod_sel(b, 4.0 * a), b, 4.0 * a);
+      ql = f + qt * (thm * at + thp * bt);
+      qr = f - qt * (thp * at + thm * bt);
+   } else {
+      const double s = (2.0 * a * b + kEps) / (a * a + b * b + kEps);
+      const double sk = kTh * s;
+      ql = f + (qt * s) * ((1.0 - sk) * a + (1.0 + sk) * b);
+      qr = f - (qt * s) * ((1.0 + sk) * a + (1.0 - sk) * b);
+   }
+}
+
+template <int R>
+__device__ __forceinline__ void muscl2_lim(double fm1, double f0, double fp1, double fp2, double& ql_n, double& qr_n1)
+{
+   double dummy;
+   muscl_lim_cell<R>(f0, f0 - fm1, fp1 - f0, ql_n, dummy);
+   muscl_lim_cell<R>(fp1, fp1 - f0, fp2 - fp1, dummy, qr_n1);
+}
+
+// linearisation of muscl_lim_cell: dql, dqr from the state differences
+// (a, b) and their perturbations (da, db)
+template <int R, typename T>
+__device__ __forceinline__ void muscl_lim_dcell(T df, T a, T b, T da, T db, T& dql, T& dqr)
+{
+   const T qt = T(0.25);
+   const T thm = T(1.0 - kTh), thp = T(1.0 + kTh);
+   if (R == RECON_MUSCL_MINMOD) {
+      const int sa = minmod_sel(double(a), 4.0 * double(b));
+      const int sb = minmod_sel(double(b), 4.0 * double(a));
+      const T dat = pick<T>(sa, da, T(4.0) * db);
+      const T dbt = pick<T>(sb, db, T(4.0) * da);
+      dql = df + qt * (thm * dat + thp * dbt);
+      dqr = df - qt * (thp * dat + thm * dbt);
+   } else {
+      const T eps = T(kEps), kt = T(kTh);
+      const T den = a * a + b * b + eps;
+      const T s = (T(2.0) * a * b + eps) / den;
+      const T ds = (T(2.0) * (da * b + a * db) - s * (T(2.0) * (a * da + b * db))) / den;
+      const T sk = kt * s, dsk = kt * ds;
+      const T A = (T(1.0) - sk) * a + (T(1.0) + sk) * b;
+      const T dA = (T(1.0) - sk) * da + (T(1.0) + sk) * db + dsk * (b - a);
+      const T B = (T(1.0) + sk) * a + (T(1.0) - sk) * b;
+      const T dB = (T(1.0) + sk) * da + (T(1.0) - sk) * db + dsk * (a - b);
+      dql = df + qt * (ds * A + s * dA);
+      dqr = df - qt * (ds * B + s * dB);
+   }
+}
+
+template <int R, typename T>
+__device__ __forceinline__ void muscl_deriv2_lim(T fm1, T f0, T fp1, T fp2, T dm1, T d0, T dp1, T dp2, T& ql_n,
+                                                 T& qr_n1)
+{
+   T dummy;
+   muscl_lim_dcell<R, T>(d0, f0 - fm1, fp1 - f0, d0 - dm1, dp1 - d0, ql_n, dummy);
+   muscl_lim_dcell<R, T>(dp1, fp1 - f0, fp2 - fp1, dp1 - d0, dp2 - dp1, dummy, qr_n1);
 }
 
 // MUSCL_DERIV for one component (reconstruction.cpp:328-349)
@@ -229,14 +322,17 @@ __device__ __forceinline__ void face_states(const DeviceState& d, int n, bool sw
    if (ORDER == 1) {
       load_sten<double, false>(d, nullptr, n, qln, dummy);
       load_sten<double, false>(d, nullptr, n + 1, qrn1, dummy);
-   } else if (ORDER == 3) {
+   } else if (is_muscl(ORDER)) {
       double fm1[4], f0[4], fp1[4], fp2[4];
       load_sten<double, false>(d, nullptr, n - 1, fm1, dummy);
       load_sten<double, false>(d, nullptr, n, f0, dummy);
       load_sten<double, false>(d, nullptr, n + 1, fp1, dummy);
       load_sten<double, false>(d, nullptr, n + 2, fp2, dummy);
 #pragma unroll
-      for (int k = 0; k < 4; k++) muscl2(fm1[k], f0[k], fp1[k], fp2[k], qln[k], qrn1[k]);
+      for (int k = 0; k < 4; k++) {
+         if (ORDER == 3) muscl2(fm1[k], f0[k], fp1[k], fp2[k], qln[k], qrn1[k]);
+         else muscl2_lim<ORDER>(fm1[k], f0[k], fp1[k], fp2[k], qln[k], qrn1[k]);
+      }
    } else {
       double f[6][4];
 #pragma unroll
@@ -264,13 +360,19 @@ __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __re
       T f[4];
       load_sten<T, true>(d, dqv, n, f, qln);
       load_sten<T, true>(d, dqv, n + 1, f, qrn1);
-   } else if (ORDER == 3) {
+   } else if (is_muscl(ORDER)) {
       T f[4][4], df[4][4];
 #pragma unroll
       for (int j = 0; j < 4; j++) load_sten<T, true>(d, dqv, n - 1 + j, f[j], df[j]);
 #pragma unroll
-      for (int k = 0; k < 4; k++)
-         muscl_deriv2<T>(f[0][k], f[1][k], f[2][k], f[3][k], df[0][k], df[1][k], df[2][k], df[3][k], qln[k], qrn1[k]);
+      for (int k = 0; k < 4; k++) {
+         if (ORDER == 3)
+            muscl_deriv2<T>(f[0][k], f[1][k], f[2][k], f[3][k], df[0][k], df[1][k], df[2][k], df[3][k], qln[k],
+                            qrn1[k]);
+         else
+            muscl_deriv2_lim<ORDER, T>(f[0][k], f[1][k], f[2][k], f[3][k], df[0][k], df[1][k], df[2][k], df[3][k],
+                                       qln[k], qrn1[k]);
+      }
    } else {
       T f[6][4], df[6][4];
 #pragma unroll

@@ -271,13 +271,17 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 void launch_rhs_face(const DeviceState& d, bool jac, cudaStream_t st)
 {
    const int b = blocks_for(d.nSlot);
-   switch (d.order * 2 + (jac ? 1 : 0)) {
+   switch (d.recon * 2 + (jac ? 1 : 0)) {
       case 2: rhs_face_kernel<1, false><<<b, kThreads, 0, st>>>(d); break;
       case 3: rhs_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
       case 6: rhs_face_kernel<3, false><<<b, kThreads, 0, st>>>(d); break;
       case 7: rhs_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;
       case 10: rhs_face_kernel<5, false><<<b, kThreads, 0, st>>>(d); break;
-      default: rhs_face_kernel<5, true><<<b, kThreads, 0, st>>>(d); break;
+      case 11: rhs_face_kernel<5, true><<<b, kThreads, 0, st>>>(d); break;
+      case 62: rhs_face_kernel<31, false><<<b, kThreads, 0, st>>>(d); break;
+      case 63: rhs_face_kernel<31, true><<<b, kThreads, 0, st>>>(d); break;
+      case 64: rhs_face_kernel<32, false><<<b, kThreads, 0, st>>>(d); break;
+      default: rhs_face_kernel<32, true><<<b, kThreads, 0, st>>>(d); break;
    }
 }
 
@@ -290,9 +294,13 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
 void launch_lin_face(const DeviceState& d, cudaStream_t st)
 {
    const int b = blocks_for(d.nSlot);
-   if (d.order == 1) lin_face_kernel<1><<<b, kThreads, 0, st>>>(d);
-   else if (d.order == 3) lin_face_kernel<3><<<b, kThreads, 0, st>>>(d);
-   else lin_face_kernel<5><<<b, kThreads, 0, st>>>(d);
+   switch (d.recon) {
+      case 1: lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
+      case 3: lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
+      case 5: lin_face_kernel<5><<<b, kThreads, 0, st>>>(d); break;
+      case 31: lin_face_kernel<31><<<b, kThreads, 0, st>>>(d); break;
+      default: lin_face_kernel<32><<<b, kThreads, 0, st>>>(d); break;
+   }
 }
 
 void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st)

@@ -31,10 +31,14 @@ class HamstrError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("order", ctypes.c_int), ("msweep", ctypes.c_int), ("CFL", ctypes.c_double),
                 ("gamma", ctypes.c_double), ("rinf", ctypes.c_double), ("uinf", ctypes.c_double),
-                ("vinf", ctypes.c_double), ("einf", ctypes.c_double), ("chain_end_rule", ctypes.c_int)]
+                ("vinf", ctypes.c_double), ("einf", ctypes.c_double), ("chain_end_rule", ctypes.c_int),
+                ("limiter", ctypes.c_int)]
 
 END_RULE_REFERENCE = 0
 END_RULE_EXTENDED = 1
+LIMITER_REFERENCE = 0
+LIMITER_MINMOD = 1
+LIMITER_VANALBADA = 2
 
 
 def lib_path() -> str:
@@ -203,7 +207,7 @@ class Case:
         _check(load().hamstr_case_set_freestream(self.h, uinf, vinf, einf))
 
     def set_option(self, name: str, value: int) -> None:
-        """Project options (``chain_end_rule``: END_RULE_REFERENCE / END_RULE_EXTENDED)."""
+        """Project options: ``chain_end_rule`` (END_RULE_*), ``limiter`` (LIMITER_*)."""
         _check(load().hamstr_case_set_option(self.h, name.encode(), int(value)))
 
 

@@ -62,7 +62,17 @@ typedef struct hamstr_gpu_params {
       position.  On meshes whose open chains all end at walls or the far
       field and have at least 3 cells, both rules give the same results. */
    int    chain_end_rule;
+   /* project option, no reference counterpart: the MUSCL limiter of order 3.
+      HAMSTR_LIMITER_REFERENCE (0) is reconstruction.cpp:16-70; MINMOD (1)
+      and VANALBADA (2) are the kappa = 1/3 scheme with minmod-limited
+      differences or van Albada's limiter (Anderson, Thomas & van Leer, AIAA
+      J. 24(9), 1986).  Orders 1 and 5 ignore it. */
+   int    limiter;
 } hamstr_gpu_params;
+
+#define HAMSTR_LIMITER_REFERENCE 0
+#define HAMSTR_LIMITER_MINMOD    1
+#define HAMSTR_LIMITER_VANALBADA 2
 
 #define HAMSTR_END_RULE_REFERENCE 0
 #define HAMSTR_END_RULE_EXTENDED  1
@@ -87,7 +97,8 @@ int  hamstr_case_get(const hamstr_case* c, const char* name, double* out);
 int  hamstr_case_set_run(hamstr_case* c, int order, int msweep, double cfl);
 int  hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double einf);
 /* Project options (no reference counterpart): "chain_end_rule" =
- * HAMSTR_END_RULE_*.  Used by hamstr_gpu_create_from_case. */
+ * HAMSTR_END_RULE_*, "limiter" = HAMSTR_LIMITER_*.  Used by
+ * hamstr_gpu_create_from_case. */
 int  hamstr_case_set_option(hamstr_case* c, const char* name, int value);
 
 /* ---------------- device solver ------------------------------------------

@@ -54,6 +54,8 @@ struct ho_case {
    /* project option, not in the reference: how open chains take ghost
       states at their end faces (HO_END_RULE_*) */
    int end_rule;
+   /* project option: MUSCL limiter of order 3 (HO_LIMITER_*) */
+   int limiter;
    double L2Norm, LInfNorm;
    /* solution arrays (solver.cpp:26-38) */
    double *q, *qt, *r, *r0, *dq, *sigma;
@@ -432,6 +434,78 @@ static int chain_gather(ho_case* c, int ich, int size, const double* dqv)
 /* ------------------------------------------------------------------ */
 
 /* MUSCL, reconstruction.cpp:16-70, over slots is..ie-1 */
+/* minmod(x, y) as a selection: 0 -> 0, 1 -> x, 2 -> y */
+static int minmod_sel(double x, double y)
+{
+   if (x > 0.0) return (y <= 0.0) ? 0 : ((x <= y) ? 1 : 2);
+   if (x < 0.0) return (y >= 0.0) ? 0 : ((x >= y) ? 1 : 2);
+   return 0;
+}
+
+static double pick(int sel, double x, double y) { return sel == 0 ? 0.0 : (sel == 1 ? x : y); }
+
+/* Project limiters for the kappa = 1/3 MUSCL scheme (no reference
+   counterpart), after Anderson, Thomas and van Leer, AIAA J. 24(9), 1986:
+   minmod-limited differences a~ = minmod(a, 4b), b~ = minmod(b, 4a), or
+   van Albada's s = (2ab + eps)/(a^2 + b^2 + eps) with sk = kappa s.
+   a = f_i - f_{i-1}, b = f_{i+1} - f_i. */
+static void muscl_lim(ho_case* c, int is, int ie, double qt)
+{
+   const double th = 0.3333333333333333e+00, eps = 1e-10;
+   double thm = 1.0 - th, thp = 1.0 + th;
+   int i, n;
+   for (n = 0; n < NQ; n++) {
+      for (i = 0; i < ie; i++) c->f2[i][n] = c->f[i + 1][n] - c->f[i][n];
+      for (i = is; i < ie; i++) {
+         double a = c->f2[i - 1][n], b = c->f2[i][n], f = c->f[i][n];
+         if (c->limiter == HO_LIMITER_MINMOD) {
+            double at = pick(minmod_sel(a, 4.0 * b), a, 4.0 * b);
+            double bt = pick(minmod_sel(b, 4.0 * a), b, 4.0 * a);
+            c->ql[i][n] = f + qt * (thm * at + thp * bt);
+            c->qr[i][n] = f - qt * (thp * at + thm * bt);
+         } else {
+            double s = (2.0 * a * b + eps) / (a * a + b * b + eps);
+            double sk = th * s;
+            c->ql[i][n] = f + (qt * s) * ((1.0 - sk) * a + (1.0 + sk) * b);
+            c->qr[i][n] = f - (qt * s) * ((1.0 + sk) * a + (1.0 - sk) * b);
+         }
+      }
+   }
+}
+
+/* linearisation of muscl_lim (minmod with its selection frozen) */
+static void muscl_lim_deriv(ho_case* c, int is, int ie, double qt)
+{
+   const double th = 0.3333333333333333e+00, eps = 1e-10;
+   double thm = 1.0 - th, thp = 1.0 + th;
+   int i, n;
+   for (n = 0; n < NQ; n++) {
+      for (i = 0; i < ie; i++) c->f2[i][n] = c->f[i + 1][n] - c->f[i][n];
+      for (i = is; i < ie; i++) {
+         double a = c->f2[i - 1][n], b = c->f2[i][n];
+         double df = c->df[i][n];
+         double da = c->df[i][n] - c->df[i - 1][n], db = c->df[i + 1][n] - c->df[i][n];
+         if (c->limiter == HO_LIMITER_MINMOD) {
+            double dat = pick(minmod_sel(a, 4.0 * b), da, 4.0 * db);
+            double dbt = pick(minmod_sel(b, 4.0 * a), db, 4.0 * da);
+            c->ql[i][n] = df + qt * (thm * dat + thp * dbt);
+            c->qr[i][n] = df - qt * (thp * dat + thm * dbt);
+         } else {
+            double den = a * a + b * b + eps;
+            double s = (2.0 * a * b + eps) / den;
+            double ds = (2.0 * (da * b + a * db) - s * (2.0 * (a * da + b * db))) / den;
+            double sk = th * s, dsk = th * ds;
+            double A = (1.0 - sk) * a + (1.0 + sk) * b;
+            double dA = (1.0 - sk) * da + (1.0 + sk) * db + dsk * (b - a);
+            double B = (1.0 + sk) * a + (1.0 - sk) * b;
+            double dB = (1.0 + sk) * da + (1.0 - sk) * db + dsk * (a - b);
+            c->ql[i][n] = df + qt * (ds * A + s * dA);
+            c->qr[i][n] = df - qt * (ds * B + s * dB);
+         }
+      }
+   }
+}
+
 static void muscl(ho_case* c, int is, int ie, double qt)
 {
    const double th = 0.3333333333333333e+00, eps = 1e-10;
@@ -440,6 +514,10 @@ static void muscl(ho_case* c, int is, int ie, double qt)
    if (qt == 0.0) {
       for (n = 0; n < NQ; n++)
          for (i = is; i <= ie; i++) c->ql[i][n] = c->qr[i][n] = c->f[i][n];
+      return;
+   }
+   if (c->limiter != HO_LIMITER_REFERENCE) {
+      muscl_lim(c, is, ie, qt);
       return;
    }
    for (n = 0; n < NQ; n++) {
@@ -465,6 +543,10 @@ static void muscl_deriv(ho_case* c, int is, int ie, double qt)
    if (qt == 0.0) {
       for (n = 0; n < NQ; n++)
          for (i = is; i <= ie; i++) c->ql[i][n] = c->qr[i][n] = c->df[i][n];
+      return;
+   }
+   if (c->limiter != HO_LIMITER_REFERENCE) {
+      muscl_lim_deriv(c, is, ie, qt);
       return;
    }
    for (n = 0; n < NQ; n++) {
@@ -1380,6 +1462,11 @@ void ho_set_freestream(ho_case* c, double uinf, double vinf, double einf)
 
 int ho_set_option(ho_case* c, const char* name, int value)
 {
+   if (strcmp(name, "limiter") == 0) {
+      if (value < HO_LIMITER_REFERENCE || value > HO_LIMITER_VANALBADA) return -1;
+      c->limiter = value;
+      return 0;
+   }
    if (strcmp(name, "chain_end_rule") == 0) {
       if (value != HO_END_RULE_REFERENCE && value != HO_END_RULE_EXTENDED) return -1;
       c->end_rule = value;

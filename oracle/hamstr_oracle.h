@@ -52,6 +52,14 @@ void ho_set_run(ho_case* c, int order, int msweep, double cfl);
  * Returns 0, or -1 for an unknown name or value. */
 #define HO_END_RULE_REFERENCE 0
 #define HO_END_RULE_EXTENDED 1
+/*   "limiter"         MUSCL limiter of order 3: HO_LIMITER_REFERENCE (0,
+ *                     default, reconstruction.cpp:16-70), HO_LIMITER_MINMOD
+ *                     (1) or HO_LIMITER_VANALBADA (2): the kappa = 1/3 scheme
+ *                     with minmod-limited differences or van Albada's
+ *                     limiter (Anderson, Thomas & van Leer, AIAA J. 1986). */
+#define HO_LIMITER_REFERENCE 0
+#define HO_LIMITER_MINMOD 1
+#define HO_LIMITER_VANALBADA 2
 int  ho_set_option(ho_case* c, const char* name, int value);
 
 /* Each returns 0, or -1 when a spectral radius is NaN (the reference exits
