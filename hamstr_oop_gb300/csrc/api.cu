@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/hamstr_gpu.h"
+#include "api_internal.h"
 #include "device_state.h"
 #include "plan.h"
 
@@ -90,8 +91,13 @@ struct hamstr_gpu {
    std::vector<int> wall_face, wall_n1, wall_n2;
    std::vector<double> wall_normal;     // [nWall][2]
    int* wall_cell = nullptr;            // device: adjacent cell per wall face
+   int* wall0 = nullptr;                // device: [nInst+1] first wall face of each instance
    double4* wall_geo = nullptr;         // device: nx, ny, midpoint x, y (after set_geometry)
-   double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums
+   double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums per instance
+
+   // instances (a plain handle has one)
+   std::vector<int> inst_cell0;         // [nInst+1]
+   std::vector<double> inst_free;       // [nInst][4]: rinf uinf vinf einf
 
    // optional per-launch timing (hamstr_gpu_profile_step)
    std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>>* prof = nullptr;
@@ -262,6 +268,16 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
                       const double* refMtx, int nChain, const int* faceStartPerChain, const int* chainConn,
                       hamstr_gpu** out)
 {
+   return hamstr::create_gpu(p, nCell, nFace, faces, normVec, refMtx, nChain, faceStartPerChain, chainConn, nullptr,
+                             out);
+}
+
+}  // extern "C"
+
+int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const int* faces, const double* normVec,
+                       const double* refMtx, int nChain, const int* faceStartPerChain, const int* chainConn,
+                       const InstanceInfo* inst, hamstr_gpu** out)
+{
    if (!p || !faces || !normVec || !refMtx || !faceStartPerChain || !chainConn || !out) return HAMSTR_GPU_ERR_ARG;
    *out = nullptr;
    if (p->msweep < 1 || !(p->CFL > 0.0)) {
@@ -312,13 +328,53 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    d.fc.vinf = p->vinf;
    d.fc.einf = p->einf;
    d.fc.cfl = p->CFL;
-   d.fs1 = p->rinf * p->uinf;
-   d.fs2 = p->rinf * p->vinf;
    g->msweep = p->msweep;
 
+   // instances: cell and chain ranges, freestream per instance
+   InstanceInfo one;
+   if (!inst) {
+      one.cell0 = {0, nCell};
+      one.chain0 = {0, nChain};
+      one.freestream = {p->rinf, p->uinf, p->vinf, p->einf};
+      inst = &one;
+   }
+   const int ni = inst->n;
+   if (ni < 1 || (int)inst->cell0.size() != ni + 1 || (int)inst->chain0.size() != ni + 1 ||
+       (int)inst->freestream.size() != 4 * ni || inst->cell0[0] != 0 || inst->cell0[ni] != nCell ||
+       inst->chain0[0] != 0 || inst->chain0[ni] != nChain) {
+      set_error("inconsistent instance ranges");
+      delete g;
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   d.nInst = ni;
+   g->inst_cell0 = inst->cell0;
+   g->inst_free = inst->freestream;
+   std::vector<double4> fstab(ni);
+   for (int k = 0; k < ni; k++) {
+      const double* f = &inst->freestream[4 * (size_t)k];
+      // computeRHS.cpp:247-250: rinf, rinf*uinf, rinf*vinf, einf
+      fstab[k] = make_double4(f[0], f[0] * f[1], f[0] * f[2], f[3]);
+   }
+   std::vector<int> chain_inst(nChain);
+   for (int k = 0; k < ni; k++)
+      for (int c = inst->chain0[k]; c < inst->chain0[k + 1]; c++) chain_inst[c] = k;
+   std::vector<int2> cell_blocks;
+   std::vector<int> inst_block0(1, 0), inst_ncell(ni);
+   for (int k = 0; k < ni; k++) {
+      for (int c = inst->cell0[k]; c < inst->cell0[k + 1]; c += kNormBlock)
+         cell_blocks.push_back(make_int2(c, std::min(c + kNormBlock, inst->cell0[k + 1])));
+      inst_block0.push_back((int)cell_blocks.size());
+      inst_ncell[k] = inst->cell0[k + 1] - inst->cell0[k];
+   }
+
    // host-side packing
+   // stencil entries carry their chain's instance (the freestream to use)
    std::vector<int4> sten(P.nSten);
-   for (int i = 0; i < P.nSten; i++) sten[i] = make_int4(P.sten_cell[i], P.sten_kind[i], P.sten_face[i], 0);
+   for (int c = 0; c < P.nChain; c++) {
+      const int e1 = (c + 1 < P.nChain) ? P.chain_sten0[c + 1] : P.nSten;
+      for (int i = P.chain_sten0[c]; i < e1; i++)
+         sten[i] = make_int4(P.sten_cell[i], P.sten_kind[i], P.sten_face[i], chain_inst[c]);
+   }
    std::vector<int4> slot(P.nSlot);
    std::vector<double2> normal(P.nSlot);
    for (int s = 0; s < P.nSlot; s++) {
@@ -334,9 +390,13 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    for (int c = 0; c < P.nChain; c++)
       if (P.chain_periodic[c]) chain_facN[c] = nper++;
    std::vector<int> cell_written(P.cell_last_wave_writer);
-   std::vector<int> wall_cell;
+   std::vector<int> wall_cell, wall0(ni + 1, 0);
    for (int f = 0; f < nFace; f++) {
       if (faces[6 * (size_t)f + 4] != -2) continue;
+      // instance of the adjacent cell (faces come instance after instance)
+      const int lc = faces[6 * (size_t)f + 2];
+      int k = (int)(std::upper_bound(inst->cell0.begin(), inst->cell0.end(), lc) - inst->cell0.begin()) - 1;
+      wall0[k + 1]++;
       g->wall_face.push_back(f);
       g->wall_n1.push_back(faces[6 * (size_t)f]);
       g->wall_n2.push_back(faces[6 * (size_t)f + 1]);
@@ -398,16 +458,22 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    TRY(dalloc(&d.fac, 80 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fsc, 4 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.facN, 16 * (size_t)std::max(nper, 1), o));
-   d.norm_blocks = (nCell + 255) / 256;
+   d.norm_blocks = (int)cell_blocks.size();
    TRY(dalloc(&d.norm_part, (size_t)d.norm_blocks, o));
-   TRY(dalloc(&d.norms, 4, o));
+   TRY(upload(&d.cell_blocks, cell_blocks, o));
+   TRY(upload(&d.inst_block0, inst_block0, o));
+   TRY(upload(&d.inst_ncell, inst_ncell, o));
+   TRY(upload(&d.fstab, fstab, o));
+   TRY(dalloc(&d.norms, 4 * (size_t)ni, o));
    TRY(dalloc(&d.status, 1, o));
    TRY(dalloc(&d.ctl, 2, o));
    TRY(dalloc(&d.tol, 1, o));
-   d.hist_cap = 1 << 16;
-   TRY(dalloc(&d.hist, 4 * (size_t)d.hist_cap, o));
+   d.hist_cap = std::min(1 << 16, std::max(1024, (1 << 22) / ni));
+   TRY(dalloc(&d.hist, 4 * (size_t)d.hist_cap * ni, o));
+   for (int k = 0; k < ni; k++) wall0[k + 1] += wall0[k];
    TRY(upload(&g->wall_cell, wall_cell, o));
-   TRY(dalloc(&g->wall_scr, 3 * wall_cell.size() + 3, o));
+   TRY(upload(&g->wall0, wall0, o));
+   TRY(dalloc(&g->wall_scr, 3 * wall_cell.size() + 3 * (size_t)ni, o));
 #undef TRY
    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
    if (e != cudaSuccess) {
@@ -424,13 +490,16 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    if (e == cudaSuccess) e = cudaMemsetAsync(d.r0, 0, 4 * nc * sizeof(double), g->stream);
    if (e == cudaSuccess) e = cudaMemsetAsync(d.sigma, 0, nc * sizeof(double), g->stream);
    if (e == cudaSuccess) {
-      // freestream initial state (initFlow.cpp:67-91)
+      // freestream initial state (initFlow.cpp:67-91), per instance
       std::vector<double> q(4 * nc);
-      for (size_t i = 0; i < nc; i++) {
-         q[4 * i] = p->rinf;
-         q[4 * i + 1] = p->rinf * p->uinf;
-         q[4 * i + 2] = p->rinf * p->vinf;
-         q[4 * i + 3] = p->einf;
+      for (int k = 0; k < ni; k++) {
+         const double* f = &inst->freestream[4 * (size_t)k];
+         for (size_t i = (size_t)inst->cell0[k]; i < (size_t)inst->cell0[k + 1]; i++) {
+            q[4 * i] = f[0];
+            q[4 * i + 1] = f[0] * f[1];
+            q[4 * i + 2] = f[0] * f[2];
+            q[4 * i + 3] = f[3];
+         }
       }
       e = cudaMemcpy(d.q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
       if (e == cudaSuccess) e = cudaMemcpy(d.qt, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -444,6 +513,8 @@ int hamstr_gpu_create(const hamstr_gpu_params* p, int nCell, int nFace, const in
    *out = g;
    return HAMSTR_GPU_OK;
 }
+
+extern "C" {
 
 int hamstr_gpu_destroy(hamstr_gpu* g)
 {
@@ -600,13 +671,14 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
    if (st) return st;
    DeviceState& d = g->d;
    if (nsteps > d.hist_cap) {
-      set_error("nsteps beyond the history capacity of one march call (65536)");
+      set_error("nsteps beyond the history capacity of one march call (" + std::to_string(d.hist_cap) + ")");
       return HAMSTR_GPU_ERR_ARG;
    }
    st = g->reset_ctl(tol);
    if (st) return st;
+   const size_t row = 4 * (size_t)d.nInst;
    if (hist) {
-      std::vector<double> nanfill(4 * (size_t)std::max(nsteps, 1), std::nan(""));
+      std::vector<double> nanfill(row * (size_t)std::max(nsteps, 1), std::nan(""));
       CK(cudaMemcpyAsync(d.hist, nanfill.data(), nanfill.size() * sizeof(double), cudaMemcpyHostToDevice, g->stream));
       CK(cudaStreamSynchronize(g->stream));
    }
@@ -617,7 +689,7 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
    if (st) return st;
    const int rows = ctl[0] ? ctl[1] + 1 : ctl[1];
    if (hist && rows > 0) {
-      CK(cudaMemcpyAsync(hist, d.hist, 4 * (size_t)rows * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+      CK(cudaMemcpyAsync(hist, d.hist, row * (size_t)rows * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
       CK(cudaStreamSynchronize(g->stream));
    }
    if (evals) *evals = rows;
@@ -792,34 +864,70 @@ extern "C" int hamstr_gpu_set_geometry(hamstr_gpu* g, int nNode, const double* x
    return HAMSTR_GPU_OK;
 }
 
-extern "C" int hamstr_gpu_forces(hamstr_gpu* g, double* out)
+// forces of every instance: out[6k..6k+5] = {Fx, Fy, M, CL, CD, CM}
+static int forces_all(hamstr_gpu* g, double* out)
 {
-   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
    if (!g->wall_geo) {
-      set_error("hamstr_gpu_forces needs hamstr_gpu_set_geometry first");
+      set_error("forces need hamstr_gpu_set_geometry first");
       return HAMSTR_GPU_ERR_ARG;
    }
    const DeviceState& d = g->d;
-   const int nw = (int)g->wall_face.size();
-   double* sums = g->wall_scr + 3 * (size_t)nw;
-   launch_forces(d.q, g->wall_cell, g->wall_geo, nw, d.fc.gamma - 1.0, g->wall_scr, sums, g->stream);
+   const int ni = d.nInst;
+   const size_t nw = g->wall_face.size();
+   double* sums = g->wall_scr + 3 * nw;
+   launch_forces(d.q, g->wall_cell, g->wall_geo, g->wall0, ni, d.fc.gamma - 1.0, g->wall_scr, sums, g->stream);
    CK(cudaGetLastError());
-   double s[3];
-   CK(cudaMemcpyAsync(s, sums, sizeof(s), cudaMemcpyDeviceToHost, g->stream));
+   std::vector<double> s(3 * (size_t)ni);
+   CK(cudaMemcpyAsync(s.data(), sums, s.size() * sizeof(double), cudaMemcpyDeviceToHost, g->stream));
    CK(cudaStreamSynchronize(g->stream));
-   // coefficients on a unit chord from the freestream (same expressions as
-   // the oracle's ho_forces)
-   const double V2 = d.fc.uinf * d.fc.uinf + d.fc.vinf * d.fc.vinf;
-   const double qinf = 0.5 * d.fc.rinf * V2;
-   const double V = std::sqrt(V2);
-   const double ca = d.fc.uinf / V, sa = d.fc.vinf / V;
-   out[0] = s[0];
-   out[1] = s[1];
-   out[2] = s[2];
-   out[3] = (s[1] * ca - s[0] * sa) / qinf;
-   out[4] = (s[0] * ca + s[1] * sa) / qinf;
-   out[5] = s[2] / qinf;
+   for (int k = 0; k < ni; k++) {
+      // coefficients on a unit chord from the instance's freestream (the
+      // oracle's ho_forces expressions)
+      const double rinf = g->inst_free[4 * k], uinf = g->inst_free[4 * k + 1], vinf = g->inst_free[4 * k + 2];
+      const double V2 = uinf * uinf + vinf * vinf;
+      const double qinf = 0.5 * rinf * V2;
+      const double V = std::sqrt(V2);
+      const double ca = uinf / V, sa = vinf / V;
+      const double Fx = s[3 * k], Fy = s[3 * k + 1], M = s[3 * k + 2];
+      double* o = out + 6 * (size_t)k;
+      o[0] = Fx;
+      o[1] = Fy;
+      o[2] = M;
+      o[3] = (Fy * ca - Fx * sa) / qinf;
+      o[4] = (Fx * ca + Fy * sa) / qinf;
+      o[5] = M / qinf;
+   }
    return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_forces(hamstr_gpu* g, double* out)
+{
+   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
+   std::vector<double> all(6 * (size_t)g->d.nInst);
+   const int st = forces_all(g, all.data());
+   if (st) return st;
+   std::memcpy(out, all.data(), 6 * sizeof(double));
+   return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_batch_forces(hamstr_gpu* g, double* out)
+{
+   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
+   return forces_all(g, out);
+}
+
+extern "C" int hamstr_gpu_instances(hamstr_gpu* g, int* n, int* cell0)
+{
+   if (!g || !n) return HAMSTR_GPU_ERR_ARG;
+   *n = g->d.nInst;
+   if (cell0) std::memcpy(cell0, g->inst_cell0.data(), g->inst_cell0.size() * sizeof(int));
+   return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_instance_norms(hamstr_gpu* g, double* out)
+{
+   if (!g || !out) return HAMSTR_GPU_ERR_ARG;
+   return g->read_norms(out, 4 * g->d.nInst);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

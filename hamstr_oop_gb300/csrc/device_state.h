@@ -36,7 +36,15 @@ struct DeviceState {
    int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
    int recon;              // reconstruction code: order, or 31/32 for MUSCL with a project limiter (recon.cuh)
    FlowConst fc;
-   double fs1, fs2;        // freestream rho*u, rho*v (computeRHS.cpp:247-248)
+
+   // instances: the batched form holds several meshes / flow conditions in
+   // one handle (a disjoint union; every launch covers all of them); a
+   // plain handle has one.  Norms, histories and forces are per instance.
+   int nInst;
+   double4* fstab;         // [nInst] freestream ghost state rho, rho u, rho v, E (computeRHS.cpp:239-256)
+   int2* cell_blocks;      // [norm_blocks] cells of each norm block; a block never spans two instances
+   int* inst_block0;       // [nInst+1] first norm block of each instance
+   int* inst_ncell;        // [nInst] cells per instance (the L2 norm's divisor)
 
    double *q, *r, *r0, *dq, *sigma, *dtfac;
    double* qt;             // second state of the RK3 scheme (solnBlock.h:47)
@@ -58,10 +66,10 @@ struct DeviceState {
    double* facN;           // per periodic chain: final LU of the last row (16)
    int* chain_facN;        // periodic chain -> index into facN (or -1)
    double2* norm_part;     // per-block {sum r_rho^2, max |r_rho|}
-   double* norms;          // [0]=L2 [1]=Linf of the last reduction
+   double* norms;          // [nInst][4]: computeRHS L2, Linf, linear L2, Linf of the last reductions
    int* status;            // device error word
    int* ctl;               // [0] stop flag (march converged), [1] step counter
-   double* hist;           // [hist_cap][4] norms per step (march)
+   double* hist;           // [hist_cap][nInst][4] norms per step (march)
    int hist_cap;
    double* tol;            // [0] march stop tolerance on the computeRHS L2 norm (<= 0: off)
    int norm_blocks;
@@ -82,6 +90,18 @@ struct DeviceState {
 // true once a march has met its tolerance: every later kernel of the step
 // returns at once, so a captured run of steps stops exactly there
 __device__ __forceinline__ bool halted(const DeviceState& d) { return *(volatile const int*)d.ctl != 0; }
+
+// block size of every kernel that reduces norms over cells
+constexpr int kNormBlock = 256;
+
+// this thread's cell in a norm-block launch (kNormBlock threads per block,
+// one block per d.cell_blocks entry), or -1 past the block's cells
+__device__ __forceinline__ int norm_cell(const DeviceState& d)
+{
+   const int2 cb = d.cell_blocks[blockIdx.x];
+   const int c = cb.x + (int)threadIdx.x;
+   return c < cb.y ? c : -1;
+}
 
 // launchers (rhs.cu)
 void launch_rhs_face(const DeviceState& d, bool jacobian, cudaStream_t st);
@@ -111,9 +131,10 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
 int adi_configure(int max_dynamic_smem);
-// launcher (forces.cu): out = {Fx, Fy, M} over n wall faces, scr = 3n doubles
-void launch_forces(const double* q, const int* wall_cell, const double4* geo, int n, double gm1, double* scr,
-                   double* out, cudaStream_t st);
+// launcher (forces.cu): per instance k, out[3k..3k+2] = {Fx, Fy, M} over
+// its wall faces wall0[k]..wall0[k+1]-1; scr = 3 doubles per wall face
+void launch_forces(const double* q, const int* wall_cell, const double4* geo, const int* wall0, int ninst,
+                   double gm1, double* scr, double* out, cudaStream_t st);
 
 }  // namespace hamstr
 #endif

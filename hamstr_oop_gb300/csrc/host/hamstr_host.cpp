@@ -8,6 +8,8 @@
 // ##################################################################
 #include "hamstr_host.h"
 
+#include "../api_internal.h"
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -603,8 +605,67 @@ int hamstr_case::create_gpu(const hamstr_case& c, hamstr_gpu** out)
                               c.mb.chainConn.data(), out);
    if (st != HAMSTR_GPU_OK) return st;
    st = hamstr_gpu_set_geometry(*out, c.mb.nNode, c.mb.x.data());
+   if (st == HAMSTR_GPU_OK) st = hamstr_gpu_set(*out, "q", c.sb.q.data());
+   if (st != HAMSTR_GPU_OK) {
+      hamstr_gpu_destroy(*out);
+      *out = nullptr;
+   }
+   return st;
+}
+
+int hamstr_case::create_batch(const hamstr_case* const* cs, int n, hamstr_gpu** out)
+{
+   const hamstr_gpu_params p0 = gpu_params(*cs[0]);
+   for (int k = 1; k < n; k++) {
+      const hamstr_gpu_params p = gpu_params(*cs[k]);
+      if (p.order != p0.order || p.msweep != p0.msweep || p.CFL != p0.CFL || p.gamma != p0.gamma ||
+          p.limiter != p0.limiter || p.chain_end_rule != p0.chain_end_rule) {
+         hamstr::set_last_error("batched cases must share order, msweep, CFL, gamma, limiter and chain end rule");
+         return HAMSTR_GPU_ERR_ARG;
+      }
+   }
+   // disjoint union: ids of case k shifted past those of cases 0..k-1
+   std::vector<int> faces, fsp, cc;
+   std::vector<double> normVec, refMtx, x, q;
+   hamstr::InstanceInfo info;
+   info.n = n;
+   info.cell0.push_back(0);
+   info.chain0.push_back(0);
+   int co = 0, fo = 0, no = 0, cfo = 0, cho = 0;
+   for (int k = 0; k < n; k++) {
+      const MESHBLOCK& mb = cs[k]->mb;
+      const SOLNBLOCK& sb = cs[k]->sb;
+      for (int f = 0; f < mb.nFace; f++) {
+         const int* r = &mb.faces[6 * (size_t)f];
+         faces.insert(faces.end(), {r[0] + no, r[1] + no, r[2] + co, r[3], r[4] >= 0 ? r[4] + co : r[4], r[5]});
+      }
+      normVec.insert(normVec.end(), mb.normVec.begin(), mb.normVec.end());
+      refMtx.insert(refMtx.end(), mb.refMtx.begin(), mb.refMtx.end());
+      x.insert(x.end(), mb.x.begin(), mb.x.end());
+      for (int c = 0; c < mb.nChain; c++) fsp.push_back(mb.faceStartPerChain[c] + cfo);
+      const int ncf = mb.faceStartPerChain[mb.nChain];
+      for (int i = 0; i < ncf; i++) cc.push_back(mb.chainConn[i] + fo);
+      q.insert(q.end(), sb.q.begin(), sb.q.end());
+      info.freestream.insert(info.freestream.end(), {sb.rinf, sb.uinf, sb.vinf, sb.einf});
+      co += mb.nCell;
+      fo += mb.nFace;
+      no += mb.nNode;
+      cfo += ncf;
+      cho += mb.nChain;
+      info.cell0.push_back(co);
+      info.chain0.push_back(cho);
+   }
+   fsp.push_back(cfo);
+   int st = hamstr::create_gpu(&p0, co, fo, faces.data(), normVec.data(), refMtx.data(), cho, fsp.data(), cc.data(),
+                               &info, out);
    if (st != HAMSTR_GPU_OK) return st;
-   return hamstr_gpu_set(*out, "q", c.sb.q.data());
+   st = hamstr_gpu_set_geometry(*out, no, x.data());
+   if (st == HAMSTR_GPU_OK) st = hamstr_gpu_set(*out, "q", q.data());
+   if (st != HAMSTR_GPU_OK) {
+      hamstr_gpu_destroy(*out);
+      *out = nullptr;
+   }
+   return st;
 }
 
 hamstr_gpu_params hamstr_case::gpu_params(const hamstr_case& c)
@@ -692,6 +753,19 @@ int hamstr_case_set_option(hamstr_case* c, const char* name, int value)
 {
    if (!c || !name) return HAMSTR_GPU_ERR_ARG;
    return hamstr_case::set_option(*c, name, value);
+}
+
+int hamstr_gpu_create_batch(const hamstr_case* const* cases, int n, hamstr_gpu** out)
+{
+   if (!cases || n < 1 || !out) return HAMSTR_GPU_ERR_ARG;
+   for (int k = 0; k < n; k++)
+      if (!cases[k]) return HAMSTR_GPU_ERR_ARG;
+   *out = nullptr;
+   try {
+      return hamstr_case::create_batch(cases, n, out);
+   } catch (const std::bad_alloc&) {
+      return HAMSTR_GPU_ERR_NOMEM;
+   }
 }
 
 int hamstr_gpu_create_from_case(const hamstr_case* c, hamstr_gpu** out)

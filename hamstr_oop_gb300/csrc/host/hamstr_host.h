@@ -160,6 +160,7 @@ struct hamstr_case {
    static hamstr_gpu_params gpu_params(const hamstr_case& c);
    static void load(hamstr_case& c, const std::string& dir);
    static int create_gpu(const hamstr_case& c, hamstr_gpu** out);
+   static int create_batch(const hamstr_case* const* cs, int n, hamstr_gpu** out);
 };
 
 #endif

@@ -25,6 +25,7 @@ namespace hamstr {
 namespace {
 
 constexpr int kThreads = 256;
+static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
 
 // ---------------- residual + FP32 Jacobian ----------------
 template <int ORDER>
@@ -398,9 +399,9 @@ template <bool UPDATE_Q>
 __global__ void __launch_bounds__(kThreads) mx_lin_cell_kernel(DeviceState d)
 {
    if (halted(d)) return;
-   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+   const int c = norm_cell(d);
    double sq = 0.0, am = 0.0;
-   if (c < d.nCell) {
+   if (c >= 0) {
       float r[4], r0[4], dq[4];
       ld4(d.r032 + 4 * (size_t)c, r0);
       ld4(d.dq32 + 4 * (size_t)c, dq);

@@ -82,7 +82,8 @@ std::string build_plan(const MeshInput& in, Plan& p)
    // rejected there.
    const bool ext = in.end_rule == END_RULE_EXTENDED;
    if (in.end_rule != END_RULE_REFERENCE && !ext) return fmt("unknown chain end rule %d", in.end_rule);
-   std::vector<int> chain_sten0(in.nChain);
+   std::vector<int>& chain_sten0 = p.chain_sten0;
+   chain_sten0.assign(in.nChain, 0);
    std::vector<int> ci;
    std::vector<int> face_last_slot(in.nFace, -1);
    for (int ich = 0; ich < in.nChain; ich++) {

@@ -46,6 +46,7 @@ struct Plan {
    std::vector<int> sten_cell;   // cell read (mirrored cell for walls, -1 for freestream)
    std::vector<int> sten_kind;   // STEN_*
    std::vector<int> sten_face;   // reflection face for STEN_WALL, else -1
+   std::vector<int> chain_sten0; // first stencil entry of each chain
 
    // processed face slots, in the reference's chain-major face order
    std::vector<int> slot_face, slot_left, slot_right;

@@ -92,10 +92,11 @@ __device__ __forceinline__ void load_sten(const DeviceState& d, const T* __restr
          df[3] = t[3];
       }
    } else {
-      f[0] = T(d.fc.rinf);
-      f[1] = T(d.fs1);
-      f[2] = T(d.fs2);
-      f[3] = T(d.fc.einf);
+      const double4 fsv = d.fstab[e.w];   // the entry's instance
+      f[0] = T(fsv.x);
+      f[1] = T(fsv.y);
+      f[2] = T(fsv.z);
+      f[3] = T(fsv.w);
       if (DQ) { df[0] = T(0); df[1] = T(0); df[2] = T(0); df[3] = T(0); }
    }
 }

@@ -32,6 +32,7 @@ namespace hamstr {
 namespace {
 
 constexpr int kThreads = 256;
+static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
 template <int ORDER, bool JAC>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
@@ -101,9 +102,9 @@ template <bool ADI_INIT>
 __global__ void __launch_bounds__(kThreads) rhs_cell_kernel(DeviceState d)
 {
    if (halted(d)) return;
-   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+   const int c = norm_cell(d);
    double sq = 0.0, am = 0.0;
-   if (c < d.nCell) {
+   if (c >= 0) {
       double r[4] = {0.0, 0.0, 0.0, 0.0};
       double sg = 0.0;
       const int e1 = d.cell_ptr[c + 1];
@@ -144,9 +145,9 @@ template <bool UPDATE_Q>
 __global__ void __launch_bounds__(kThreads) lin_cell_kernel(DeviceState d)
 {
    if (halted(d)) return;
-   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+   const int c = norm_cell(d);
    double sq = 0.0, am = 0.0;
-   if (c < d.nCell) {
+   if (c >= 0) {
       double r[4], r0[4], dq[4];
       ld4(d.r0 + 4 * (size_t)c, r0);
       ld4(d.dq + 4 * (size_t)c, dq);
@@ -183,29 +184,38 @@ __global__ void __launch_bounds__(kThreads) lin_cell_kernel(DeviceState d)
 __global__ void norm_final_kernel(DeviceState d, int off, int check_tol)
 {
    if (halted(d)) return;
-   // one warp: fixed-shape reduction of the block partials
-   double a = 0.0, b = 0.0;
-   for (int i = threadIdx.x; i < d.norm_blocks; i += 32) {
-      const double2 p = d.norm_part[i];
-      a += p.x;
-      b = fmax(b, p.y);
-   }
-#pragma unroll
-   for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
-   }
-   if (threadIdx.x == 0) {
-      const double l2 = sqrt(a) / d.nCell;
-      d.norms[off] = l2;
-      d.norms[off + 1] = b;
-      const int it = d.ctl[1];
-      if (it < d.hist_cap) {
-         d.hist[4 * it + off] = l2;
-         d.hist[4 * it + off + 1] = b;
+   // one warp per instance: fixed-shape reduction of its block partials
+   __shared__ int s_open;
+   if (threadIdx.x == 0) s_open = 0;
+   __syncthreads();
+   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+   const int it = d.ctl[1];
+   for (int k = w; k < d.nInst; k += nw) {
+      double a = 0.0, b = 0.0;
+      for (int i = d.inst_block0[k] + l; i < d.inst_block0[k + 1]; i += 32) {
+         const double2 p = d.norm_part[i];
+         a += p.x;
+         b = fmax(b, p.y);
       }
-      if (check_tol && *d.tol > 0.0 && l2 <= *d.tol) d.ctl[0] = 1;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+         a += __shfl_xor_sync(0xffffffffu, a, o);
+         b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+      }
+      if (l == 0) {
+         const double l2 = sqrt(a) / d.inst_ncell[k];
+         d.norms[4 * k + off] = l2;
+         d.norms[4 * k + off + 1] = b;
+         if (it < d.hist_cap) {
+            d.hist[4 * ((size_t)it * d.nInst + k) + off] = l2;
+            d.hist[4 * ((size_t)it * d.nInst + k) + off + 1] = b;
+         }
+         if (!(l2 <= *d.tol)) atomicOr(&s_open, 1);
+      }
    }
+   __syncthreads();
+   // the march stops once every instance's computeRHS L2 is <= tol
+   if (threadIdx.x == 0 && check_tol && *d.tol > 0.0 && s_open == 0) d.ctl[0] = 1;
 }
 
 __global__ void step_end_kernel(DeviceState d)
@@ -311,7 +321,7 @@ void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st)
 
 void launch_norm_final(const DeviceState& d, int off, bool check_tol, cudaStream_t st)
 {
-   norm_final_kernel<<<1, 32, 0, st>>>(d, off, check_tol ? 1 : 0);
+   norm_final_kernel<<<1, 32 * (d.nInst < 32 ? d.nInst : 32), 0, st>>>(d, off, check_tol ? 1 : 0);
 }
 
 void launch_step_end(const DeviceState& d, cudaStream_t st) { step_end_kernel<<<1, 1, 0, st>>>(d); }

@@ -73,6 +73,10 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_forces": (i, [vp, vp]),
         "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
         "hamstr_gpu_create_from_case": (i, [vp, pp]),
+        "hamstr_gpu_create_batch": (i, [vp, i, pp]),
+        "hamstr_gpu_instances": (i, [vp, ctypes.POINTER(i), vp]),
+        "hamstr_gpu_instance_norms": (i, [vp, vp]),
+        "hamstr_gpu_batch_forces": (i, [vp, vp]),
         "hamstr_gpu_destroy": (i, [vp]),
         "hamstr_gpu_strerror": (cp, [i]),
         "hamstr_gpu_last_error": (cp, []),
@@ -214,12 +218,47 @@ class Case:
 class GpuSolver:
     """Device solver handle (the SOLVER of the drop-in)."""
 
-    def __init__(self, case: Case):
-        L = load()
+    def __init__(self, case: Case = None, *, _handle=None, _sizes=None):
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _check(load().hamstr_gpu_create_from_case(case.h, ctypes.byref(h)))
+            self.h = h
+            self.sizes = dict(case.sizes)
+        else:
+            self.h, self.sizes = _handle, _sizes
+        n = ctypes.c_int(0)
+        _check(load().hamstr_gpu_instances(self.h, ctypes.byref(n), None))
+        self.n_instances = n.value
+
+    @classmethod
+    def batch(cls, cases: list) -> "GpuSolver":
+        """The batched form: all cases in one handle (hamstr_gpu_create_batch)."""
+        arr = (ctypes.c_void_p * len(cases))(*[c.h for c in cases])
         h = ctypes.c_void_p()
-        _check(L.hamstr_gpu_create_from_case(case.h, ctypes.byref(h)))
-        self.h = h
-        self.sizes = dict(case.sizes)
+        _check(load().hamstr_gpu_create_batch(arr, len(cases), ctypes.byref(h)))
+        sizes = dict(cases[0].sizes)
+        for k in ("nCell", "nFace", "nChain", "nChainFace", "nNode"):
+            sizes[k] = sum(c.sizes[k] for c in cases)
+        return cls(_handle=h, _sizes=sizes)
+
+    def instance_cells(self) -> np.ndarray:
+        """Cell offsets of the instances (n+1 entries)."""
+        n = ctypes.c_int(0)
+        out = np.zeros(self.n_instances + 1, dtype=np.int32)
+        _check(load().hamstr_gpu_instances(self.h, ctypes.byref(n), _ptr(out)))
+        return out
+
+    def instance_norms(self) -> np.ndarray:
+        """[n][4] last computeRHS L2, Linf and linear L2, Linf of every instance."""
+        out = np.zeros((self.n_instances, 4))
+        _check(load().hamstr_gpu_instance_norms(self.h, _ptr(out)))
+        return out
+
+    def batch_forces(self) -> np.ndarray:
+        """[n][6] Fx, Fy, M, CL, CD, CM of every instance."""
+        out = np.zeros((self.n_instances, 6))
+        _check(load().hamstr_gpu_batch_forces(self.h, _ptr(out)))
+        return out
 
     def close(self):
         if self.h:
@@ -292,10 +331,12 @@ class GpuSolver:
         return out
 
     def march(self, nsteps: int, tol: float = 0.0):
-        hist = np.zeros((max(nsteps, 1), 4))
+        """(hist, converged): hist is [rows][4], or [rows][n][4] on a batched handle."""
+        hist = np.zeros((max(nsteps, 1), self.n_instances, 4))
         ev, conv = ctypes.c_int(0), ctypes.c_int(0)
         _check(load().hamstr_gpu_march(self.h, nsteps, tol, _ptr(hist), ctypes.byref(ev), ctypes.byref(conv)))
-        return hist[:ev.value], bool(conv.value)
+        hist = hist[:ev.value]
+        return (hist[:, 0, :] if self.n_instances == 1 else hist), bool(conv.value)
 
     def enqueue_steps(self, n: int) -> None:
         _check(load().hamstr_gpu_enqueue_steps(self.h, n))

@@ -134,8 +134,10 @@ int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf);
 int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
 /* SOLVER::marchInTime (march.cpp:15-59) with a convergence stop: runs up
  * to nsteps steps; stops before the ADI of the first step whose computeRHS
- * L2 norm is <= tol (tol <= 0: never).  hist (may be NULL) receives 4
- * doubles per computeRHS evaluation; *evals = number of rows written,
+ * L2 norm is <= tol (tol <= 0: never) -- on a batched handle, the first
+ * step at which every instance's is.  hist (may be NULL) receives 4
+ * doubles per computeRHS evaluation and instance ({L2, Linf, linear L2,
+ * Linf}, instances in order); *evals = number of rows written,
  * *converged = 1 when the stop fired.  Norms stay on the GPU until the end. */
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged);
 
@@ -150,6 +152,24 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
  *                history differs from the reference's. */
 int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
 
+/* Batched form (no counterpart in the reference): several cases -- meshes
+ * of any sizes and their flow conditions -- in one handle.  They are held
+ * as a disjoint union (cells, faces and chains of case k follow those of
+ * case k-1), so every kernel launch and every captured step covers all of
+ * them.  The cases must share order, msweep, CFL, gamma, limiter and chain
+ * end rule; each keeps its own freestream (ghost states and initial
+ * state), norms and forces.  Each instance's arithmetic is that of a
+ * plain handle on its case, except the reference's cell-id-0 ghost test
+ * (computeRHS.cpp:158,170), which the union keeps for the first case only.
+ * hamstr_gpu_get/set and the norms of hamstr_gpu_step etc. address the
+ * union (instance 0's norms); hamstr_gpu_instances gives the cell offsets
+ * (n+1 ints, may be NULL), hamstr_gpu_instance_norms the last norms of each
+ * instance ([n][4]), hamstr_gpu_batch_forces the forces of each ([n][6]). */
+int hamstr_gpu_create_batch(const hamstr_case* const* cases, int n, hamstr_gpu** out);
+int hamstr_gpu_instances(hamstr_gpu* g, int* n, int* cell0);
+int hamstr_gpu_instance_norms(hamstr_gpu* g, double* norms);
+int hamstr_gpu_batch_forces(hamstr_gpu* g, double* out);
+
 /* Wall forces (no counterpart in the reference, which computes none).
  * hamstr_gpu_set_geometry hands over the node coordinates (x y per node,
  * coord.dat order; io.cpp:144-156) for the faces' midpoints;
@@ -158,7 +178,7 @@ int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
  * (right cell -2, ascending face id) p * (dy, -dx) with p from the adjacent
  * cell, summed in face order, and the moment about (0.25, 0).
  * out6 = {Fx, Fy, M, CL, CD, CM} with coefficients on a unit chord and the
- * freestream dynamic pressure and flow direction. */
+ * freestream dynamic pressure and flow direction (instance 0 of a batch). */
 int hamstr_gpu_set_geometry(hamstr_gpu* g, int nNode, const double* xy);
 int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
 
