@@ -57,6 +57,17 @@ WORKLOADS = {
                alpha=1.25, ramp=((50, 2.0), (50, 5.0)),
                name="naca0012_ogrid_1024x256_split30_muscl_vanalbada_m08_cfl10_msweep2"),
 }
+# The batched form: `n` flow conditions (Mach, alpha drawn uniformly from a
+# seed) on O-grids of four sizes assigned round-robin, all in one handle.
+BATCH = {
+    "c4": dict(meshes=((128, 32), (256, 64), (384, 96), (512, 128)), n=256, mach=(0.3, 0.85), alpha=(-2.0, 4.0),
+               seed=0, order=1, CFL=10.0, msweep=2, precision="mixed",
+               name="naca0012_batch256_meshes128x32-512x128_order1_cfl10_msweep2_fp32adi",
+               # converged-solve leg: a subset small enough to finish in seconds
+               converge=dict(n=16, meshes=((128, 32),), tol=1e-10, cap=6000)),
+}
+WORKLOADS.update({k: dict(v, batch=True) for k, v in BATCH.items()})
+
 # converged-solve measurement: a case that reaches 1e-10 (the MUSCL and WENO
 # cases plateau near 1e-9 on these meshes, as the survey's probes found)
 CONVERGE = dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
@@ -104,6 +115,180 @@ def open_oracle(wl: dict, case_dir: str):
     o.set_option("chain_end_rule", wl["end_rule"])
     o.set_option("limiter", wl.get("limiter", 0))
     return o
+
+
+def batch_conditions(b: dict, n: int = None, meshes=None):
+    """[(mesh index, Mach, alpha)] of the batch, seeded."""
+    import numpy as np
+    n = n or b["n"]
+    meshes = meshes or b["meshes"]
+    rng = np.random.default_rng(b["seed"])
+    mach = rng.uniform(b["mach"][0], b["mach"][1], n)
+    alpha = rng.uniform(b["alpha"][0], b["alpha"][1], n)
+    return [(k % len(meshes), float(mach[k]), float(alpha[k])) for k in range(n)]
+
+
+def batch_mesh_dirs(b: dict, meshes) -> list:
+    from hamstr_oop_gb300 import meshgen
+    base = os.environ.get("HAMSTR_BENCH_DIR", "/tmp/hamstr_bench")
+    out = []
+    for ni, nj in meshes:
+        d = os.path.join(base, "batch_%dx%d_o%d" % (ni, nj, b["order"]))
+        if not os.path.exists(os.path.join(d, "input.hamstr")):
+            meshgen.make_case(d, ni, nj, order=b["order"], CFL=b["CFL"], msweep=b["msweep"], nsteps=1)
+        out.append(d)
+    return out
+
+
+def batch_cases(b: dict, n: int = None, meshes=None) -> list:
+    """Host cases of the batch: one read per mesh, cloned per condition."""
+    from hamstr_oop_gb300 import native
+    meshes = meshes or b["meshes"]
+    base = [native.Case(d) for d in batch_mesh_dirs(b, meshes)]
+    out = []
+    for m, mach, alpha in batch_conditions(b, n, meshes):
+        c = base[m].clone()
+        c.set_flow(mach, alpha)
+        out.append(c)
+    return out
+
+
+def run_batch(args, wl, rank, local_rank, world):
+    """The batched form: every condition in one handle, one graph per step."""
+    import numpy as np
+    import torch
+    from hamstr_oop_gb300 import native
+    torch.cuda.set_device(local_rank)
+    native.load()
+    t_setup = time.perf_counter()
+    cases = batch_cases(wl)
+    g = native.GpuSolver.batch(cases)
+    t_setup = time.perf_counter() - t_setup
+    nc = g.sizes["nCell"]
+    g.set_precision(wl["precision"] == "mixed")
+    hs = torch.cuda.ExternalStream(g.stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    g.enqueue_steps(max(args.warmup, 3))
+    g.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with torch.cuda.stream(hs):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            starts[k].record(hs)
+            g.enqueue_steps(1)
+            ends[k].record(hs)
+    g.sync()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nc * args.steps / (ms * 1e-3)
+    prof = g.profile_step(reps=2) if rank == 0 else {}
+    # the same batch with the FP64 operator, for comparison
+    g.set_precision(False)
+    g.enqueue_steps(2)
+    g.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(hs):
+        e0.record(hs)
+        g.enqueue_steps(max(args.steps // 2, 1))
+        e1.record(hs)
+    g.sync()
+    fp64_ms = e0.elapsed_time(e1) / max(args.steps // 2, 1)
+    # end to end: q of all conditions in from pinned host memory, one step,
+    # q and the per-condition norms out
+    g.set_precision(wl["precision"] == "mixed")
+    qhost = torch.empty(4 * nc, dtype=torch.float64, pin_memory=True)
+    qnp = qhost.numpy()
+    qnp[:] = g.get("q")
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.set("q", qnp)
+        g.step()
+        qnp[:] = g.get("q")
+        g.instance_norms()
+    e2e_s = time.perf_counter() - t0
+    out = None
+    if rank == 0:
+        conv = batch_converged(wl) if not args.no_converge else None
+        ninst = g.n_instances
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64 residual, f32 Jacobian/ADI" if wl["precision"] == "mixed" else "f64",
+               "data": "synthetic",
+               "config": {"workload": wl["name"], "conditions": ninst, "cells": nc, "meshes": [list(m) for m in wl["meshes"]],
+                          "mach": list(wl["mach"]), "alpha_deg": list(wl["alpha"]), "order": wl["order"],
+                          "CFL": wl["CFL"], "msweep": wl["msweep"], "parallelism": "one batched handle",
+                          "l2": "512 MiB flush write between timed steps (untimed)", "setup_s": t_setup},
+               "e2e": {"value": world * nc * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 32 * nc,
+                       "d2h_bytes_per_step": 32 * nc + 32 * ninst, "steps": e2e_steps},
+               "fp64_operator_ms_per_step": fp64_ms,
+               "kernel_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()},
+               "converged": conv, "clocks": clocks,
+               "gpu_launches": g.launches_per_step() * args.steps}
+    g.close()
+    return out
+
+
+def batch_converged(wl: dict) -> dict:
+    """Time to L2 <= tol for a subset of the batch's conditions: the batched
+    form (one handle, its precision) against the plain FP64 drop-in solving
+    the same conditions one after another."""
+    import numpy as np
+    import torch
+    from hamstr_oop_gb300 import native
+    cv = wl["converge"]
+    cases = batch_cases(wl, cv["n"], cv["meshes"])
+    out = {"conditions": cv["n"], "meshes": [list(m) for m in cv["meshes"]], "tol": cv["tol"], "cap": cv["cap"]}
+    g = native.GpuSolver.batch(cases)
+    g.set_precision(wl["precision"] == "mixed")
+    g.march(2, 0.0)
+    g.set("q", np.concatenate([c.get("q") for c in cases]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist, ok = g.march(cv["cap"], cv["tol"])
+    dt = time.perf_counter() - t0
+    first = [int(np.argmax(hist[:, k, 0] <= cv["tol"])) if (hist[:, k, 0] <= cv["tol"]).any() else None
+             for k in range(cv["n"])]
+    qb = g.get("q").reshape(-1, 4)
+    cell0 = g.instance_cells()
+    fb = g.batch_forces()
+    g.close()
+    out["batched"] = {"all_converged": ok, "steps": int(hist.shape[0]), "seconds": dt,
+                      "solves_per_s": cv["n"] / dt if ok else None,
+                      "steps_per_condition": first}
+    # plain FP64 drop-in, one condition at a time
+    t_plain, steps_plain, worst = 0.0, [], 0.0
+    dcl = 0.0
+    for k, c in enumerate(cases):
+        s = native.GpuSolver(c)
+        s.march(2, 0.0)
+        s.set("q", c.get("q"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h, okk = s.march(cv["cap"], cv["tol"])
+        t_plain += time.perf_counter() - t0
+        steps_plain.append(int(h.shape[0]) if okk else None)
+        q64 = s.get("q").reshape(-1, 4)
+        worst = max(worst, float(np.max(np.abs(qb[cell0[k]:cell0[k + 1]] - q64)) / np.max(np.abs(q64))))
+        dcl = max(dcl, abs(fb[k, 3] - s.forces()["CL"]))
+        s.close()
+    out["plain_fp64_sequential"] = {"seconds": t_plain, "solves_per_s": cv["n"] / t_plain,
+                                    "steps_per_condition": steps_plain}
+    out["speedup_batched_vs_plain"] = t_plain / dt
+    out["batched_vs_plain_at_tol"] = {"max_abs_over_max_q": worst, "max_dCL": dcl,
+                                      "note": "both stopped at the same L2 tolerance"}
+    return out
 
 
 def time_oracle_steps(cases: list, q0: list, steps: int) -> float:
@@ -434,9 +619,45 @@ def cpu_baseline(wl, case_dir, nc, steps=None) -> dict:
                       "of the %s mesh (one per thread)" % (steps, threads, wl["name"])}
 
 
+def run_reference_batch(args, wl):
+    """The reference algorithm (C restatement) on the host cores for the
+    batch's conditions: one condition per thread, a bounded sample."""
+    from oracle import oracle
+    oracle.build(reference=False)
+    threads = os.cpu_count() or 1
+    hosts = batch_cases(wl, threads)
+    dirs = batch_mesh_dirs(wl, wl["meshes"])
+    conds = batch_conditions(wl, threads)
+    cases = []
+    for (m, _, _), h in zip(conds, hosts):
+        o = oracle.OracleCase(dirs[m], "port")
+        p = h.params
+        o.set_freestream(p["uinf"], p["vinf"], p["einf"])
+        o.set("q", h.get("q"))
+        cases.append(o)
+    nc = sum(o.sizes["nCell"] for o in cases)
+    q0 = [c.get("q") for c in cases]
+    time_oracle_steps(cases, q0, max(args.warmup, 1))
+    dt = time_oracle_steps(cases, q0, args.steps)
+    for c in cases:
+        c.close()
+    value = nc * args.steps / dt
+    sample = ("each step: one pseudo-time step (from the freestream state) of %d of the batch's conditions, one per "
+              "host thread (meshes round-robin as in the batch), C restatement of the reference algorithm" % threads)
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": wl["name"], "cells_sampled": nc, "order": wl["order"],
+                                            "msweep": wl["msweep"], "CFL": wl["CFL"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, wl, rank):
     if rank != 0:
         return None
+    if wl.get("batch"):
+        return run_reference_batch(args, wl)
     from oracle import oracle
     oracle.build(reference=False)
     case_dir = make_case(wl, 0)
@@ -485,7 +706,7 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    out = run_gpu(args, wl, rank, local_rank, world)
+    out = (run_batch if wl.get("batch") else run_gpu)(args, wl, rank, local_rank, world)
     if out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -247,7 +247,6 @@ void SOLNBLOCK::readSolutionInputs(const std::string& root)
 // ==================================================================
 void hamstr_init_flow(SOLNBLOCK& sb, int nCell)
 {
-   const double deg2rad = 3.1415926535897932e+00 / 180.0;   // utils.h:55-57
    sb.gamma = 1.4;
    sb.gm1 = sb.gamma - 1.;
    sb.invGamma = 1. / sb.gamma;
@@ -258,6 +257,12 @@ void hamstr_init_flow(SOLNBLOCK& sb, int nCell)
    sb.rey = sb.rey / sb.Mach;
    sb.nGhost = (sb.order == 5) ? 3 : 2;
    if (sb.test != 0) throw Error(HAMSTR_GPU_ERR_ARG, "HAMSTR: test condition not implemented");
+   hamstr_freestream(sb, nCell);
+}
+
+void hamstr_freestream(SOLNBLOCK& sb, int nCell)
+{
+   const double deg2rad = 3.1415926535897932e+00 / 180.0;   // utils.h:55-57
    sb.uinf = sb.Mach * std::cos(sb.alpha * deg2rad);
    sb.vinf = sb.Mach * std::sin(sb.alpha * deg2rad);
    sb.einf = sb.pinf / (sb.gm1) + 0.5 * sb.rinf * (sb.uinf * sb.uinf + sb.vinf * sb.vinf);
@@ -573,6 +578,13 @@ void hamstr_case::set_freestream(hamstr_case& c, double u, double v, double e)
    }
 }
 
+void hamstr_case::set_flow(hamstr_case& c, double mach, double alpha)
+{
+   c.sb.Mach = mach;
+   c.sb.alpha = alpha;
+   hamstr_freestream(c.sb, c.mb.nCell);
+}
+
 int hamstr_case::set_option(hamstr_case& c, const std::string& name, int value)
 {
    if (name == "chain_end_rule") {
@@ -746,6 +758,25 @@ int hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double 
 {
    if (!c) return HAMSTR_GPU_ERR_ARG;
    hamstr_case::set_freestream(*c, uinf, vinf, einf);
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_case_clone(const hamstr_case* c, hamstr_case** out)
+{
+   if (!c || !out) return HAMSTR_GPU_ERR_ARG;
+   try {
+      *out = new hamstr_case(*c);
+   } catch (const std::bad_alloc&) {
+      *out = nullptr;
+      return HAMSTR_GPU_ERR_NOMEM;
+   }
+   return HAMSTR_GPU_OK;
+}
+
+int hamstr_case_set_flow(hamstr_case* c, double mach, double alpha_deg)
+{
+   if (!c || !(mach > 0.0) || !(alpha_deg == alpha_deg)) return HAMSTR_GPU_ERR_ARG;
+   hamstr_case::set_flow(*c, mach, alpha_deg);
    return HAMSTR_GPU_OK;
 }
 

@@ -64,6 +64,7 @@ class SOLNBLOCK
    friend class SOLVER;
    friend struct hamstr_case;
    friend void hamstr_init_flow(SOLNBLOCK& sb, int nCell);
+   friend void hamstr_freestream(SOLNBLOCK& sb, int nCell);
 
   private:
    int order = 3, timeacc = 0, nsteps = 0, nwrite = 0, msweep = 1, test = 0, outform = 0;
@@ -144,6 +145,8 @@ class HAMSTR
 
 // freestream + initial state (initFlow.cpp:12-93) on host arrays
 void hamstr_init_flow(SOLNBLOCK& sb, int nCell);
+// the freestream part of initFlow.cpp:24-91 from sb.Mach and sb.alpha
+void hamstr_freestream(SOLNBLOCK& sb, int nCell);
 
 // the C handle behind hamstr_case_* (api.cu)
 struct hamstr_case {
@@ -157,6 +160,7 @@ struct hamstr_case {
    static void set_run(hamstr_case& c, int order, int msweep, double cfl);
    static void set_freestream(hamstr_case& c, double u, double v, double e);
    static int set_option(hamstr_case& c, const std::string& name, int value);
+   static void set_flow(hamstr_case& c, double mach, double alpha);
    static hamstr_gpu_params gpu_params(const hamstr_case& c);
    static void load(hamstr_case& c, const std::string& dir);
    static int create_gpu(const hamstr_case& c, hamstr_gpu** out);

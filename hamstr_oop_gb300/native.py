@@ -68,6 +68,8 @@ def load(build_if_missing: bool = False):
         "hamstr_case_set_run": (i, [vp, i, i, d]),
         "hamstr_case_set_freestream": (i, [vp, d, d, d]),
         "hamstr_case_set_option": (i, [vp, ctypes.c_char_p, i]),
+        "hamstr_case_clone": (i, [vp, pp]),
+        "hamstr_case_set_flow": (i, [vp, d, d]),
         "hamstr_gpu_set_cfl": (i, [vp, d]),
         "hamstr_gpu_set_geometry": (i, [vp, i, vp]),
         "hamstr_gpu_forces": (i, [vp, vp]),
@@ -213,6 +215,17 @@ class Case:
     def set_option(self, name: str, value: int) -> None:
         """Project options: ``chain_end_rule`` (END_RULE_*), ``limiter`` (LIMITER_*)."""
         _check(load().hamstr_case_set_option(self.h, name.encode(), int(value)))
+
+    def clone(self) -> "Case":
+        h = ctypes.c_void_p()
+        _check(load().hamstr_case_clone(self.h, ctypes.byref(h)))
+        c = Case.__new__(Case)
+        c.h, c.case_dir, c.sizes = h, self.case_dir, dict(self.sizes)
+        return c
+
+    def set_flow(self, mach: float, alpha_deg: float) -> None:
+        """New flow condition: freestream and initial state from Mach and alpha."""
+        _check(load().hamstr_case_set_flow(self.h, float(mach), float(alpha_deg)))
 
 
 class GpuSolver:

@@ -96,6 +96,12 @@ int  hamstr_case_get(const hamstr_case* c, const char* name, double* out);
 /* overrides of input.hamstr values (order, msweep, CFL) and the freestream */
 int  hamstr_case_set_run(hamstr_case* c, int order, int msweep, double cfl);
 int  hamstr_case_set_freestream(hamstr_case* c, double uinf, double vinf, double einf);
+/* A copy of a case (no reference counterpart), e.g. for the members of a
+ * batch that share a mesh; and a new flow condition for a case: Mach and
+ * angle of attack in degrees, the freestream and initial state recomputed
+ * as initFlow.cpp:24-91 does. */
+int  hamstr_case_clone(const hamstr_case* c, hamstr_case** out);
+int  hamstr_case_set_flow(hamstr_case* c, double mach, double alpha_deg);
 /* Project options (no reference counterpart): "chain_end_rule" =
  * HAMSTR_END_RULE_*, "limiter" = HAMSTR_LIMITER_*.  Used by
  * hamstr_gpu_create_from_case. */
