@@ -81,7 +81,8 @@ def test_batch_mixed_precision_converges(make_case, native_lib):
     b = native.GpuSolver.batch([h for _, h in cs])
     b.set_precision(True)
     hist, conv = b.march(6000, 1e-10)
-    assert conv and np.all(np.isfinite(hist))
+    # the last row is the converged computeRHS: no ADI, so no linear norms
+    assert conv and np.all(np.isfinite(hist[:, :, :2])) and np.all(np.isfinite(hist[:-1]))
 
 
 def test_batch_rejects_mismatched_runs(make_case, native_lib):
