@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= 48 * d.nRow || halted(d)) return;
    const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
+   if (frozen_cell(d, d.row_scell[row])) return;
    double v = assemble(d, d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b, e);
    v *= d.dtfac[d.row_scell[row]];
    if (b == 1 && (e >> 2) == (e & 3)) v += 1.0;
@@ -92,8 +93,10 @@ __global__ void __launch_bounds__(128, 1) adi_factor_kernel(DeviceState d, int n
    const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[0] + w;
-   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++)
-      factor_chain(d, d.sched_jobs[job], threadIdx.x & 31);
+   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
+      const int ich = d.sched_jobs[job];
+      if (!frozen_chain(d, ich)) factor_chain(d, ich, threadIdx.x & 31);
+   }
 }
 
 // one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the
@@ -128,8 +131,10 @@ __global__ void __launch_bounds__(128, 1) adi_solve_kernel(DeviceState d, int wa
    const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[1 + wave] + w;
-   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++)
-      solve_chain(d, d.sched_jobs[job], threadIdx.x & 31);
+   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
+      const int ich = d.sched_jobs[job];
+      if (!frozen_chain(d, ich)) solve_chain(d, ich, threadIdx.x & 31);
+   }
 }
 
 }  // namespace

@@ -219,6 +219,7 @@ struct hamstr_gpu {
    int reset_ctl(double tol)
    {
       CK(cudaMemsetAsync(d.ctl, 0, 2 * sizeof(int), stream));
+      CK(cudaMemsetAsync(d.inst_done, 0, (size_t)d.nInst * sizeof(int), stream));
       if (tol != tol_host) {
          tol_host = tol;
          CK(cudaMemcpyAsync(d.tol, &tol_host, sizeof(double), cudaMemcpyHostToDevice, stream));
@@ -464,6 +465,18 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
    TRY(upload(&d.inst_block0, inst_block0, o));
    TRY(upload(&d.inst_ncell, inst_ncell, o));
    TRY(upload(&d.fstab, fstab, o));
+   {
+      std::vector<int> slot_inst(P.nSlot), cell_inst(nCell), block_inst(cell_blocks.size());
+      for (int k = 0; k < ni; k++)
+         for (int c = inst->cell0[k]; c < inst->cell0[k + 1]; c++) cell_inst[c] = k;
+      for (int s = 0; s < P.nSlot; s++) slot_inst[s] = cell_inst[P.slot_left[s]];
+      for (size_t b = 0; b < cell_blocks.size(); b++) block_inst[b] = cell_inst[cell_blocks[b].x];
+      TRY(upload(&d.slot_inst, slot_inst, o));
+      TRY(upload(&d.cell_inst, cell_inst, o));
+      TRY(upload(&d.chain_inst, chain_inst, o));
+      TRY(upload(&d.block_inst, block_inst, o));
+      TRY(dalloc(&d.inst_done, (size_t)ni, o));
+   }
    TRY(dalloc(&d.norms, 4 * (size_t)ni, o));
    TRY(dalloc(&d.status, 1, o));
    TRY(dalloc(&d.ctl, 2, o));

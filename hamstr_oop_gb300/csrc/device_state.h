@@ -45,6 +45,8 @@ struct DeviceState {
    int2* cell_blocks;      // [norm_blocks] cells of each norm block; a block never spans two instances
    int* inst_block0;       // [nInst+1] first norm block of each instance
    int* inst_ncell;        // [nInst] cells per instance (the L2 norm's divisor)
+   int* inst_done;         // [nInst] 1 once an instance has met the march tolerance (frozen)
+   int *slot_inst, *cell_inst, *chain_inst, *block_inst;   // instance of each slot, cell, chain, norm block
 
    double *q, *r, *r0, *dq, *sigma, *dtfac;
    double* qt;             // second state of the RK3 scheme (solnBlock.h:47)
@@ -91,6 +93,24 @@ struct DeviceState {
 // returns at once, so a captured run of steps stops exactly there
 __device__ __forceinline__ bool halted(const DeviceState& d) { return *(volatile const int*)d.ctl != 0; }
 
+// A march over a batch freezes each instance at the step whose computeRHS
+// L2 norm first meets the tolerance -- the state a plain handle's march
+// stops in -- and skips its work from then on.  A plain handle (one
+// instance) never reads these arrays.
+__device__ __forceinline__ bool frozen_inst(const DeviceState& d, int k) { return d.nInst > 1 && d.inst_done[k] != 0; }
+__device__ __forceinline__ bool frozen_slot(const DeviceState& d, int s)
+{
+   return d.nInst > 1 && d.inst_done[d.slot_inst[s]] != 0;
+}
+__device__ __forceinline__ bool frozen_cell(const DeviceState& d, int c)
+{
+   return d.nInst > 1 && d.inst_done[d.cell_inst[c]] != 0;
+}
+__device__ __forceinline__ bool frozen_chain(const DeviceState& d, int ch)
+{
+   return d.nInst > 1 && d.inst_done[d.chain_inst[ch]] != 0;
+}
+
 // block size of every kernel that reduces norms over cells
 constexpr int kNormBlock = 256;
 
@@ -100,6 +120,7 @@ __device__ __forceinline__ int norm_cell(const DeviceState& d)
 {
    const int2 cb = d.cell_blocks[blockIdx.x];
    const int c = cb.x + (int)threadIdx.x;
+   if (d.nInst > 1 && d.inst_done[d.block_inst[blockIdx.x]] != 0) return -1;
    return c < cb.y ? c : -1;
 }
 

@@ -32,7 +32,7 @@ template <int ORDER>
 __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= d.nSlot || halted(d)) return;
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
 __global__ void __launch_bounds__(kThreads) mx_init_kernel(DeviceState d)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= d.nCell || halted(d)) return;
+   if (c >= d.nCell || halted(d) || frozen_cell(d, c)) return;
    double r[4];
    ld4(d.r + 4 * (size_t)c, r);
    const float rf[4] = {float(r[0]), float(r[1]), float(r[2]), float(r[3])};
@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= 48 * d.nRow || halted(d)) return;
    const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
+   if (frozen_cell(d, d.row_scell[row])) return;
    const int* ops = d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b;
    float acc = 0.f;
 #pragma unroll
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(64) mx_factor_kernel(DeviceState d, int count)
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
    const int ich = d.fac_chains32[t];
+   if (frozen_chain(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const float* blk = d.blk32 + 48 * (size_t)row0;
@@ -279,6 +281,7 @@ __global__ void __launch_bounds__(64) mx_solve_kernel(DeviceState d, int first, 
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
    const int ich = d.line_chains[first + t];
+   if (frozen_chain(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const float* fac = d.fac32 + (size_t)kRec * row0;
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(64) mx_solve_kernel(DeviceState d, int first, 
 __global__ void __launch_bounds__(kThreads) mx_dq_update_kernel(DeviceState d)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= d.nCell || halted(d)) return;
+   if (c >= d.nCell || halted(d) || frozen_cell(d, c)) return;
    float r[4], dq[4];
    ld4(d.r32 + 4 * (size_t)c, r);
    ld4(d.dq32 + 4 * (size_t)c, dq);
@@ -379,7 +382,7 @@ template <int ORDER>
 __global__ void __launch_bounds__(kThreads) mx_lin_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= d.nSlot || halted(d)) return;
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    float dL[4], dR[4];
    face_dstates<ORDER, float>(d, d.dq32, sl.x, (sl.w & 1) != 0, dL, dR);

@@ -37,7 +37,7 @@ template <int ORDER, bool JAC>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= d.nSlot || halted(d)) return;
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
@@ -60,7 +60,7 @@ template <int ORDER>
 __global__ void __launch_bounds__(kThreads) lin_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= d.nSlot || halted(d)) return;
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    double dL[4], dR[4];
    face_dstates<ORDER, double>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
@@ -191,6 +191,7 @@ __global__ void norm_final_kernel(DeviceState d, int off, int check_tol)
    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
    const int it = d.ctl[1];
    for (int k = w; k < d.nInst; k += nw) {
+      if (frozen_inst(d, k)) continue;   // its norms stay those of its last step
       double a = 0.0, b = 0.0;
       for (int i = d.inst_block0[k] + l; i < d.inst_block0[k + 1]; i += 32) {
          const double2 p = d.norm_part[i];
@@ -210,11 +211,15 @@ __global__ void norm_final_kernel(DeviceState d, int off, int check_tol)
             d.hist[4 * ((size_t)it * d.nInst + k) + off] = l2;
             d.hist[4 * ((size_t)it * d.nInst + k) + off + 1] = b;
          }
-         if (!(l2 <= *d.tol)) atomicOr(&s_open, 1);
+         if (check_tol && *d.tol > 0.0 && l2 <= *d.tol) {
+            if (d.nInst > 1) d.inst_done[k] = 1;   // frozen from this step's ADI on
+         } else {
+            atomicOr(&s_open, 1);
+         }
       }
    }
    __syncthreads();
-   // the march stops once every instance's computeRHS L2 is <= tol
+   // the march stops once every instance's computeRHS L2 has met tol
    if (threadIdx.x == 0 && check_tol && *d.tol > 0.0 && s_open == 0) d.ctl[0] = 1;
 }
 
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) update_kernel(DeviceState d, const d
                                                           double* __restrict__ qnew, double coef)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= d.nCell || halted(d)) return;
+   if (c >= d.nCell || halted(d) || frozen_cell(d, c)) return;
    const double dtfac = coef * d.fc.cfl / d.sigma[c];
    double qo[4], r[4], qn[4];
    ld4(qold + 4 * (size_t)c, qo);
@@ -249,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) dtfac_kernel(DeviceState d)
 __global__ void __launch_bounds__(kThreads) adi_init_kernel(DeviceState d)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= d.nCell || halted(d)) return;
+   if (c >= d.nCell || halted(d) || frozen_cell(d, c)) return;
    const double dt = d.fc.cfl / d.sigma[c];
    d.dtfac[c] = dt;
    double r[4];
@@ -265,7 +270,7 @@ __global__ void __launch_bounds__(kThreads) adi_init_kernel(DeviceState d)
 __global__ void __launch_bounds__(kThreads) dq_update_kernel(DeviceState d)
 {
    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= d.nCell || halted(d)) return;
+   if (c >= d.nCell || halted(d) || frozen_cell(d, c)) return;
    double r[4], dq[4];
    ld4(d.r + 4 * (size_t)c, r);
    ld4(d.dq + 4 * (size_t)c, dq);

@@ -60,19 +60,29 @@ def test_batch_matches_the_oracle(make_case, oracle_lib, native_lib):
         assert np.array_equal(qb[cell0[k]:cell0[k + 1]], o.get("q").reshape(-1, 4)), k
 
 
-def test_batch_march_stops_when_all_converge(make_case, native_lib):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_batch_march_freezes_each_instance_where_a_plain_march_stops(make_case, native_lib, mixed):
+    """Each instance stops at its own tolerance step: its final state equals
+    a plain handle's march on its case bit for bit; the march ends when the
+    last instance converges, and a frozen instance's history rows stay NaN."""
     from hamstr_oop_gb300 import native
     cs = _cases(make_case, CASES, order=1, CFL=10.0, msweep=2)
     b = native.GpuSolver.batch([h for _, h in cs])
+    b.set_precision(mixed)
     hist, conv = b.march(6000, 1e-10)
     assert conv
     first = [int(np.argmax(hist[:, k, 0] <= 1e-10)) for k in range(3)]
     assert hist.shape[0] == max(first) + 1
-    assert np.all(hist[-1, :, 0] <= 1e-10)
+    cell0 = b.instance_cells()
+    qb = b.get("q").reshape(-1, 4)
     for k, (_, h) in enumerate(cs):
+        assert np.all(np.isnan(hist[first[k] + 1:, k, 0]))
         s = native.GpuSolver(h)
+        s.set_precision(mixed)
         hs, cs_ = s.march(6000, 1e-10)
         assert cs_ and hs.shape[0] == first[k] + 1, (k, hs.shape, first[k])
+        np.testing.assert_array_equal(hist[:first[k] + 1, k, :2], hs[:, :2])
+        assert np.array_equal(qb[cell0[k]:cell0[k + 1]], s.get("q").reshape(-1, 4)), k
 
 
 def test_batch_mixed_precision_converges(make_case, native_lib):
@@ -81,8 +91,11 @@ def test_batch_mixed_precision_converges(make_case, native_lib):
     b = native.GpuSolver.batch([h for _, h in cs])
     b.set_precision(True)
     hist, conv = b.march(6000, 1e-10)
-    # the last row is the converged computeRHS: no ADI, so no linear norms
-    assert conv and np.all(np.isfinite(hist[:, :, :2])) and np.all(np.isfinite(hist[:-1]))
+    assert conv
+    for k in range(3):
+        # rows up to the instance's stop are finite; frozen rows stay NaN
+        kk = int(np.argmax(hist[:, k, 0] <= 1e-10))
+        assert np.all(np.isfinite(hist[:kk + 1, k, :2])) and np.all(np.isfinite(hist[:kk, k]))
 
 
 def test_batch_rejects_mismatched_runs(make_case, native_lib):
