@@ -87,10 +87,10 @@ __device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int 
 }
 
 // persistent warps, one per SM sub-partition, each with a job list
-__global__ void __launch_bounds__(128, 1) adi_factor_kernel(DeviceState d, int nwarps)
+__global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
 {
    if (halted(d)) return;
-   const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[0] + w;
    for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
@@ -125,10 +125,10 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
    }
 }
 
-__global__ void __launch_bounds__(128, 1) adi_solve_kernel(DeviceState d, int wave, int nwarps)
+__global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wave, int nwarps)
 {
    if (halted(d)) return;
-   const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[1 + wave] + w;
    for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(128, 1) adi_solve_kernel(DeviceState d, int wa
 
 }  // namespace
 
-// One block of 4 warps per SM: the dynamic shared-memory request below
-// exceeds half an SM's shared memory, so no two blocks share an SM and
-// each warp owns an SM sub-partition's FP64 unit.
+// One block per SM: the dynamic shared-memory request below exceeds half
+// an SM's shared memory, so no two blocks share an SM.  With 4 warps per
+// block each warp owns an SM sub-partition's FP64 unit; the autotuner may
+// pick 8 (two per sub-partition) where chains are many and short.
 constexpr int kExclusiveSmem = 120 * 1024;
 
 int adi_configure(int max_dynamic_smem)
@@ -164,12 +165,14 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
 
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
 {
-   adi_factor_kernel<<<(nwarps + 3) / 4, 128, d.exclusive_smem, st>>>(d, nwarps);
+   const int wpb = d.adi_wpb;
+   adi_factor_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
 }
 
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st)
 {
-   if (nwarps > 0) adi_solve_kernel<<<(nwarps + 3) / 4, 128, d.exclusive_smem, st>>>(d, wave, nwarps);
+   const int wpb = d.adi_wpb;
+   if (nwarps > 0) adi_solve_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, wave, nwarps);
 }
 
 }  // namespace hamstr

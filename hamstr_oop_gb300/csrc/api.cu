@@ -95,6 +95,8 @@ struct hamstr_gpu {
    double4* wall_geo = nullptr;         // device: nx, ny, midpoint x, y (after set_geometry)
    double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums per instance
 
+   int nsm = 1;                         // SMs of the device (persistent-warp schedules)
+
    // instances (a plain handle has one)
    std::vector<int> inst_cell0;         // [nInst+1]
    std::vector<double> inst_free;       // [nInst][4]: rinf uinf vinf einf
@@ -126,7 +128,6 @@ struct hamstr_gpu {
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
       L("mx_init", n, [&] { launch_mx_init(d, stream); });
-      L("mx_assemble", n, [&] { launch_mx_assemble(d, stream); });
       L("mx_factor", n, [&] { launch_mx_factor(d, stream); });
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++)
@@ -149,7 +150,6 @@ struct hamstr_gpu {
       const size_t nc = (size_t)d.nCell;
       int st;
       if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
-      if ((st = dalloc(&d.blk32, 48 * (size_t)std::max(d.nRow, 1), owned))) return st;
       if ((st = dalloc(&d.fsc32, 4 * (size_t)std::max(d.nRow, 1), owned))) return st;
       if ((st = dalloc(&d.fac32, 80 * (size_t)std::max(d.nRow, 1), owned))) return st;
       int nper = 0;
@@ -196,6 +196,34 @@ struct hamstr_gpu {
       L("step_end", n, [&] { launch_step_end(d, stream); });
       launches_per_step = n;
       CK(cudaGetLastError());
+      return HAMSTR_GPU_OK;
+   }
+
+   // drop the captured step (launch shapes or constants changed)
+   void invalidate()
+   {
+      if (step_exec) cudaGraphExecDestroy(step_exec);
+      if (step_graph) cudaGraphDestroy(step_graph);
+      step_exec = nullptr;
+      step_graph = nullptr;
+      launches_per_step = 0;
+   }
+
+   // launch shapes; a new warps-per-SM count rebuilds the line schedules
+   int apply_shape(int face_block, int adi_wpb, int mx_block)
+   {
+      if (adi_wpb != d.adi_wpb) {
+         sched = build_schedule(plan, adi_wpb * nsm);
+         int st;
+         if ((st = upload(&d.sched_warp0, sched.warp0, owned))) return st;
+         if ((st = upload(&d.sched_nwarps, sched.nwarps, owned))) return st;
+         if ((st = upload(&d.sched_warp_ptr, sched.warp_ptr, owned))) return st;
+         if ((st = upload(&d.sched_jobs, sched.jobs, owned))) return st;
+      }
+      d.face_block = face_block;
+      d.adi_wpb = adi_wpb;
+      d.mx_block = mx_block;
+      invalidate();
       return HAMSTR_GPU_OK;
    }
 
@@ -449,7 +477,11 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
       if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 0;
       d.exclusive_smem = adi_configure(optin);
-      g->sched = build_schedule(P, 4 * nsm);
+      d.face_block = 256;
+      d.adi_wpb = 4;
+      d.mx_block = 64;
+      g->nsm = nsm;
+      g->sched = build_schedule(P, d.adi_wpb * nsm);
    }
    TRY(upload(&d.sched_warp0, g->sched.warp0, o));
    TRY(upload(&d.sched_nwarps, g->sched.nwarps, o));
@@ -943,16 +975,78 @@ extern "C" int hamstr_gpu_instance_norms(hamstr_gpu* g, double* out)
    return g->read_norms(out, 4 * g->d.nInst);
 }
 
+extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len)
+{
+   if (!g || reps < 1) return HAMSTR_GPU_ERR_ARG;
+   DeviceState& d = g->d;
+   // candidates for the current precision: face-kernel block size, and the
+   // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
+   // kernels; FP32: threads per block of the thread-per-chain kernels)
+   struct Cand { int fb, wpb, mb; float ms; };
+   std::vector<Cand> cands;
+   for (int fb : {128, 256}) {
+      if (g->mixed) {
+         for (int mb : {32, 64, 128, 256}) cands.push_back({fb, d.adi_wpb, mb, 0.f});
+      } else {
+         for (int w : {4, 8}) cands.push_back({fb, w, d.mx_block, 0.f});
+      }
+   }
+   // the tuning steps advance the state: keep q and put it back afterwards
+   double* qsave = nullptr;
+   const size_t qbytes = 4 * (size_t)d.nCell * sizeof(double);
+   CK(cudaMallocAsync((void**)&qsave, qbytes, g->stream));
+   CK(cudaMemcpyAsync(qsave, d.q, qbytes, cudaMemcpyDeviceToDevice, g->stream));
+   cudaEvent_t e0, e1;
+   CK(cudaEventCreate(&e0));
+   CK(cudaEventCreate(&e1));
+   int st = HAMSTR_GPU_OK;
+   for (Cand& c : cands) {
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb))) break;
+      if ((st = g->capture())) break;
+      if ((st = g->reset_ctl(0.0))) break;
+      CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
+      CK(cudaEventRecord(e0, g->stream));
+      for (int i = 0; i < reps; i++) CK(cudaGraphLaunch(g->step_exec, g->stream));
+      CK(cudaEventRecord(e1, g->stream));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaEventElapsedTime(&c.ms, e0, e1));
+      c.ms /= reps;
+      if ((st = g->status_check())) break;
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   CK(cudaMemcpyAsync(d.q, qsave, qbytes, cudaMemcpyDeviceToDevice, g->stream));
+   CK(cudaFreeAsync(qsave, g->stream));
+   CK(cudaStreamSynchronize(g->stream));
+   if (st) return st;
+   const Cand* best = &cands[0];
+   for (const Cand& c : cands)
+      if (c.ms < best->ms) best = &c;
+   st = g->apply_shape(best->fb, best->wpb, best->mb);
+   if (st) return st;
+   if (report && report_len > 0) {
+      std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
+      for (size_t i = 0; i < cands.size(); i++) {
+         char buf[160];
+         std::snprintf(buf, sizeof(buf), "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"ms\": %.4f}",
+                       i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].ms);
+         r += buf;
+      }
+      char buf[160];
+      std::snprintf(buf, sizeof(buf), "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d}}",
+                    best->fb, best->wpb, best->mb);
+      r += buf;
+      std::snprintf(report, (size_t)report_len, "%s", r.c_str());
+   }
+   return HAMSTR_GPU_OK;
+}
+
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
 {
    if (!g || !(cfl > 0.0) || !(cfl < 1e300)) return HAMSTR_GPU_ERR_ARG;
    if (g->d.fc.cfl != cfl) {
       g->d.fc.cfl = cfl;   // kernels take the state by value: recapture the step
-      if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
-      if (g->step_graph) cudaGraphDestroy(g->step_graph);
-      g->step_exec = nullptr;
-      g->step_graph = nullptr;
-      g->launches_per_step = 0;
+      g->invalidate();
    }
    return HAMSTR_GPU_OK;
 }
@@ -966,11 +1060,7 @@ extern "C" int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed)
    }
    if (g->mixed != mixed) {
       g->mixed = mixed;
-      if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
-      if (g->step_graph) cudaGraphDestroy(g->step_graph);
-      g->step_exec = nullptr;
-      g->step_graph = nullptr;
-      g->launches_per_step = 0;
+      g->invalidate();
    }
    return HAMSTR_GPU_OK;
 }

@@ -67,37 +67,6 @@ __global__ void __launch_bounds__(kThreads) mx_init_kernel(DeviceState d)
    st4(d.dq32 + 4 * (size_t)c, z);
 }
 
-// FP32 blocks in the reference's term order (ADI.cpp:62-217)
-__global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= 48 * d.nRow || halted(d)) return;
-   const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
-   if (frozen_cell(d, d.row_scell[row])) return;
-   const int* ops = d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b;
-   float acc = 0.f;
-#pragma unroll
-   for (int o = 0; o < kOpsPerBlock; o++) {
-      const int op = ops[o];
-      if (op < 0) break;
-      const int slot = op >> 3, sel = (op >> 1) & 3, col = e & 3;
-      const float* m = d.ff32 + 32 * (size_t)slot;
-      float v;
-      if (sel == OP_SEL_RREFL && (col == 1 || col == 2)) {
-         const double4 rf = d.refl[d.slot_face[slot]];
-         const float r01 = m[16 + (e & ~3) + 1], r02 = m[16 + (e & ~3) + 2];
-         v = (col == 1) ? (float(rf.x) * r01 + float(rf.y) * r02) : (float(rf.z) * r01 + float(rf.w) * r02);
-      } else {
-         v = m[(sel == OP_SEL_L ? 0 : 16) + e];
-      }
-      if (op & 1) acc -= v;
-      else acc += v;
-   }
-   acc *= float(d.dtfac[d.row_scell[row]]);
-   if (b == 1 && (e >> 2) == (e & 3)) acc += 1.f;
-   d.blk32[t] = acc;
-}
-
 // ---------------- FP32 line solves, one thread per chain ----------------
 // The same split as the FP64 path: the block factorisation runs once per
 // step (mx_factor), each sweep replays the right-hand side (mx_solve).  One
@@ -201,7 +170,60 @@ __device__ __forceinline__ void mm_sub(const float (&M)[16], const float (&X)[16
       }
 }
 
-__global__ void __launch_bounds__(64) mx_factor_kernel(DeviceState d, int count)
+// One FP32 block from its term list, in the reference's term order
+// (ADI.cpp:62-217): +/- L or R of a face slot, or R with its velocity
+// columns reflected at a wall (ADI.cpp:151-163)
+__device__ __forceinline__ void mx_block(const DeviceState& d, const int* __restrict__ ops, float (&M)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) M[m] = 0.f;
+#pragma unroll
+   for (int o = 0; o < kOpsPerBlock; o++) {
+      const int op = ops[o];
+      if (op < 0) break;
+      const int slot = op >> 3, sel = (op >> 1) & 3;
+      float v[16];
+      ld16f(d.ff32 + 32 * (size_t)slot + (sel == OP_SEL_L ? 0 : 16), v);
+      if (sel == OP_SEL_RREFL) {
+         const double4 rf = d.refl[d.slot_face[slot]];
+#pragma unroll
+         for (int k = 0; k < 4; k++) {
+            const float r01 = v[4 * k + 1], r02 = v[4 * k + 2];
+            v[4 * k + 1] = float(rf.x) * r01 + float(rf.y) * r02;
+            v[4 * k + 2] = float(rf.z) * r01 + float(rf.w) * r02;
+         }
+      }
+      if (op & 1) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) M[m] -= v[m];
+      } else {
+#pragma unroll
+         for (int m = 0; m < 16; m++) M[m] += v[m];
+      }
+   }
+}
+
+// the three blocks of one ADI row, scaled by CFL/sigma, B + I (ADI.cpp:197-217)
+__device__ __forceinline__ void mx_row(const DeviceState& d, int row, float (&A)[16], float (&B)[16], float (&C)[16])
+{
+   const int* ops = d.row_ops + 3 * kOpsPerBlock * (size_t)row;
+   mx_block(d, ops, A);
+   mx_block(d, ops + kOpsPerBlock, B);
+   mx_block(d, ops + 2 * kOpsPerBlock, C);
+   const float s = float(d.dtfac[d.row_scell[row]]);
+#pragma unroll
+   for (int m = 0; m < 16; m++) {
+      A[m] *= s;
+      B[m] *= s;
+      C[m] *= s;
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) B[5 * k] += 1.f;
+}
+
+// assembly fused with the factorisation: each thread builds its chain's
+// blocks straight from the FP32 face Jacobians
+__global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
@@ -209,19 +231,12 @@ __global__ void __launch_bounds__(64) mx_factor_kernel(DeviceState d, int count)
    if (frozen_chain(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
-   const float* blk = d.blk32 + 48 * (size_t)row0;
    float* fac = d.fac32 + (size_t)kRec * row0;
    float A[16], B[16], C[16], cp[16], ap[16];
-   ld16f(blk, A);
-   ld16f(blk + 16, B);
-   ld16f(blk + 32, C);
+   mx_row(d, row0, A, B, C);
    for (int i = 0; i < N; i++) {
       float An[16], Bn[16], Cn[16];
-      if (i + 1 < N) {
-         ld16f(blk + 48 * (size_t)(i + 1), An);
-         ld16f(blk + 48 * (size_t)(i + 1) + 16, Bn);
-         ld16f(blk + 48 * (size_t)(i + 1) + 32, Cn);
-      }
+      if (i + 1 < N) mx_row(d, row0 + i + 1, An, Bn, Cn);
       float* rec = fac + (size_t)kRec * i;
       st16f(rec, A);
       float fill[16];
@@ -276,7 +291,7 @@ __global__ void __launch_bounds__(64) mx_factor_kernel(DeviceState d, int count)
    luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
 
-__global__ void __launch_bounds__(64) mx_solve_kernel(DeviceState d, int first, int count)
+__global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
@@ -458,7 +473,8 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
 {
-   const int b = blocks_for(d.nSlot);
+   const int kThreads = d.face_block;
+   const int b = (d.nSlot + kThreads - 1) / kThreads;
    switch (d.recon) {
       case 1: mx_rhs_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
       case 3: mx_rhs_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
@@ -470,19 +486,16 @@ void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
 
 void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d); }
 
-void launch_mx_assemble(const DeviceState& d, cudaStream_t st)
-{
-   mx_assemble_kernel<<<blocks_for(48 * d.nRow), kThreads, 0, st>>>(d);
-}
-
 void launch_mx_factor(const DeviceState& d, cudaStream_t st)
 {
-   mx_factor_kernel<<<(d.nChain + 63) / 64, 64, 0, st>>>(d, d.nChain);
+   const int tb = d.mx_block;
+   mx_factor_kernel<<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
 }
 
 void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st)
 {
-   if (count > 0) mx_solve_kernel<<<(count + 63) / 64, 64, 0, st>>>(d, first, count);
+   const int tb = d.mx_block;
+   if (count > 0) mx_solve_kernel<<<(count + tb - 1) / tb, tb, 0, st>>>(d, first, count);
 }
 
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)
@@ -492,7 +505,8 @@ void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)
 
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st)
 {
-   const int b = blocks_for(d.nSlot);
+   const int kThreads = d.face_block;
+   const int b = (d.nSlot + kThreads - 1) / kThreads;
    switch (d.recon) {
       case 1: mx_lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
       case 3: mx_lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;

@@ -285,7 +285,8 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 void launch_rhs_face(const DeviceState& d, bool jac, cudaStream_t st)
 {
-   const int b = blocks_for(d.nSlot);
+   const int kThreads = d.face_block;
+   const int b = (d.nSlot + kThreads - 1) / kThreads;
    switch (d.recon * 2 + (jac ? 1 : 0)) {
       case 2: rhs_face_kernel<1, false><<<b, kThreads, 0, st>>>(d); break;
       case 3: rhs_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
@@ -308,7 +309,8 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
 
 void launch_lin_face(const DeviceState& d, cudaStream_t st)
 {
-   const int b = blocks_for(d.nSlot);
+   const int kThreads = d.face_block;
+   const int b = (d.nSlot + kThreads - 1) / kThreads;
    switch (d.recon) {
       case 1: lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
       case 3: lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;

@@ -71,6 +71,7 @@ def load(build_if_missing: bool = False):
         "hamstr_case_clone": (i, [vp, pp]),
         "hamstr_case_set_flow": (i, [vp, d, d]),
         "hamstr_gpu_set_cfl": (i, [vp, d]),
+        "hamstr_gpu_autotune": (i, [vp, i, ctypes.c_char_p, i]),
         "hamstr_gpu_set_geometry": (i, [vp, i, vp]),
         "hamstr_gpu_forces": (i, [vp, vp]),
         "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
@@ -297,6 +298,13 @@ class GpuSolver:
         out = np.zeros(6)
         _check(load().hamstr_gpu_forces(self.h, _ptr(out)))
         return dict(zip(("Fx", "Fy", "M", "CL", "CD", "CM"), (float(v) for v in out)))
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Pick the fastest launch shapes for the current precision (hamstr_gpu_autotune)."""
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 4096))
+        return json.loads(buf.value.decode())
 
     def set_cfl(self, cfl: float) -> None:
         """CFL of later steps (a project addition for CFL ramping)."""

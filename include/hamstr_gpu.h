@@ -188,6 +188,15 @@ int hamstr_gpu_batch_forces(hamstr_gpu* g, double* out);
 int hamstr_gpu_set_geometry(hamstr_gpu* g, int nNode, const double* xy);
 int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
 
+/* Autotuner (no reference counterpart): times `reps` steps of the current
+ * precision for each candidate launch shape -- face kernels 128 or 256
+ * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
+ * or two per sub-partition, schedules rebuilt longest-chain-first); FP32
+ * line kernels 32..256 threads per block -- and keeps the fastest.  The
+ * state is restored afterwards; results do not depend on the shape.
+ * report (may be NULL) receives a JSON summary of the timings. */
+int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
+
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
  * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */
