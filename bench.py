@@ -166,6 +166,7 @@ def run_batch(args, wl, rank, local_rank, world):
     t_setup = time.perf_counter() - t_setup
     nc = g.sizes["nCell"]
     g.set_precision(wl["precision"] == "mixed")
+    tune = g.autotune(reps=2)
     hs = torch.cuda.ExternalStream(g.stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     g.enqueue_steps(max(args.warmup, 3))
@@ -234,7 +235,7 @@ def run_batch(args, wl, rank, local_rank, world):
                        "d2h_bytes_per_step": 32 * nc + 32 * ninst, "steps": e2e_steps},
                "fp64_operator_ms_per_step": fp64_ms,
                "kernel_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()},
-               "converged": conv, "clocks": clocks,
+               "converged": conv, "clocks": clocks, "autotune": tune,
                "gpu_launches": g.launches_per_step() * args.steps}
     g.close()
     return out
@@ -252,6 +253,7 @@ def batch_converged(wl: dict) -> dict:
     out = {"conditions": cv["n"], "meshes": [list(m) for m in cv["meshes"]], "tol": cv["tol"], "cap": cv["cap"]}
     g = native.GpuSolver.batch(cases)
     g.set_precision(wl["precision"] == "mixed")
+    g.autotune(reps=2)
     g.march(2, 0.0)
     g.set("q", np.concatenate([c.get("q") for c in cases]))
     torch.cuda.synchronize()
@@ -448,7 +450,8 @@ def run_gpu(args, wl, rank, local_rank, world):
     hs = torch.cuda.ExternalStream(gpu.stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    # warm-up (W >= 3 steps), also builds the CUDA graph
+    # launch shapes from the autotuner, then warm-up (W >= 3 steps)
+    tune64 = gpu.autotune(reps=2)
     gpu.enqueue_steps(max(args.warmup, 1))
     gpu.sync()
 
@@ -480,6 +483,7 @@ def run_gpu(args, wl, rank, local_rank, world):
 
     # the mixed-precision form (FP64 residual, FP32 operator) on the same case
     gpu.set_precision(True)
+    tunemx = gpu.autotune(reps=2)
     gpu.enqueue_steps(max(args.warmup, 1))
     gpu.sync()
     mstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -546,7 +550,8 @@ def run_gpu(args, wl, rank, local_rank, world):
                  "ms_per_step": mixed_ms / args.steps,
                  "note": "FP64 residual (bit-identical to the reference), FP32 Jacobians, ADI and linear "
                          "residual; converges to the FP64 steady state (tests/test_gpu_mixed.py)",
-                 "kernel_ms_per_step": {k: round(v[0], 4) for k, v in mixed_prof.items()}}
+                 "kernel_ms_per_step": {k: round(v[0], 4) for k, v in mixed_prof.items()},
+                 "autotune_best": tunemx.get("best")}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -558,7 +563,7 @@ def run_gpu(args, wl, rank, local_rank, world):
                        "mesh": mesh_note(wl), "cfl_ramp_before_timing": [list(r) for r in wl["ramp"]],
                        "limiter": LIMITER_NAMES[wl.get("limiter", 0)] if wl["order"] == 3 else None},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-            "mixed_precision": mixed, "converged": conv,
+            "mixed_precision": mixed, "converged": conv, "autotune_best": tune64.get("best"),
             "gpu_launches": gpu.launches_per_step() * args.steps,
             "wall_s_timed_region": wall,
         }

@@ -128,6 +128,7 @@ struct hamstr_gpu {
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
       L("mx_init", n, [&] { launch_mx_init(d, stream); });
+      if (!d.mx_fused) L("mx_assemble", n, [&] { launch_mx_assemble(d, stream); });
       L("mx_factor", n, [&] { launch_mx_factor(d, stream); });
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++)
@@ -150,6 +151,7 @@ struct hamstr_gpu {
       const size_t nc = (size_t)d.nCell;
       int st;
       if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
+      if (!d.mx_fused && (st = ensure_blk32())) return st;
       if ((st = dalloc(&d.fsc32, 4 * (size_t)std::max(d.nRow, 1), owned))) return st;
       if ((st = dalloc(&d.fac32, 80 * (size_t)std::max(d.nRow, 1), owned))) return st;
       int nper = 0;
@@ -199,6 +201,12 @@ struct hamstr_gpu {
       return HAMSTR_GPU_OK;
    }
 
+   int ensure_blk32()
+   {
+      if (d.blk32) return HAMSTR_GPU_OK;
+      return dalloc(&d.blk32, 48 * (size_t)std::max(d.nRow, 1), owned);
+   }
+
    // drop the captured step (launch shapes or constants changed)
    void invalidate()
    {
@@ -210,8 +218,13 @@ struct hamstr_gpu {
    }
 
    // launch shapes; a new warps-per-SM count rebuilds the line schedules
-   int apply_shape(int face_block, int adi_wpb, int mx_block)
+   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused)
    {
+      if (!mx_fused && d.ff32) {
+         const int st = ensure_blk32();
+         if (st) return st;
+      }
+      d.mx_fused = mx_fused;
       if (adi_wpb != d.adi_wpb) {
          sched = build_schedule(plan, adi_wpb * nsm);
          int st;
@@ -480,6 +493,8 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_block = 256;
       d.adi_wpb = 4;
       d.mx_block = 64;
+      // FP32 assembly inside the factorisation pays off on long chains
+      d.mx_fused = (P.nChain > 0 && P.nRow >= 16 * P.nChain) ? 1 : 0;
       g->nsm = nsm;
       g->sched = build_schedule(P, d.adi_wpb * nsm);
    }
@@ -982,13 +997,14 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb; float ms; };
+   struct Cand { int fb, wpb, mb, fused; float ms; };
    std::vector<Cand> cands;
    for (int fb : {128, 256}) {
       if (g->mixed) {
-         for (int mb : {32, 64, 128, 256}) cands.push_back({fb, d.adi_wpb, mb, 0.f});
+         for (int fused : {0, 1})
+            for (int mb : {32, 64, 128}) cands.push_back({fb, d.adi_wpb, mb, fused, 0.f});
       } else {
-         for (int w : {4, 8}) cands.push_back({fb, w, d.mx_block, 0.f});
+         for (int w : {4, 8}) cands.push_back({fb, w, d.mx_block, d.mx_fused, 0.f});
       }
    }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1001,7 +1017,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1022,19 +1038,22 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb);
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
       for (size_t i = 0; i < cands.size(); i++) {
          char buf[160];
-         std::snprintf(buf, sizeof(buf), "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"ms\": %.4f}",
-                       i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].ms);
+         std::snprintf(buf, sizeof(buf),
+                       "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
+                       "\"ms\": %.4f}",
+                       i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].ms);
          r += buf;
       }
       char buf[160];
-      std::snprintf(buf, sizeof(buf), "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d}}",
-                    best->fb, best->wpb, best->mb);
+      std::snprintf(buf, sizeof(buf),
+                    "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }

@@ -81,9 +81,11 @@ struct DeviceState {
    int face_block;         // threads per block of the face kernels (<= 256)
    int adi_wpb;            // warps per block (= per SM) of the persistent FP64 line kernels (4 or 8)
    int mx_block;           // threads per block of the FP32 thread-per-chain line kernels
+   int mx_fused;           // 1: FP32 blocks assembled inside the factorisation; 0: mx_assemble first
 
    // mixed-precision defect correction (FP64 residual, FP32 operator)
    float* ff32;            // [nSlot][32] FP32 face Jacobians
+   float* blk32;           // [nRow][48] FP32 assembled blocks A, B, C (B + I), unfused assembly only
    float* fsc32;           // [nRow][4]
    float* fac32;           // [nRow][80] FP32 factor records
    float* facN32;          // [periodic chains][16]
@@ -146,6 +148,7 @@ void launch_dq_update(const DeviceState& d, cudaStream_t st);
 // launchers (mixed.cu): FP64 residual + FP32 Jacobian/ADI defect correction
 void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_init(const DeviceState& d, cudaStream_t st);
+void launch_mx_assemble(const DeviceState& d, cudaStream_t st);   // no-op when d.mx_fused
 void launch_mx_factor(const DeviceState& d, cudaStream_t st);
 void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st);
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);

@@ -67,6 +67,39 @@ __global__ void __launch_bounds__(kThreads) mx_init_kernel(DeviceState d)
    st4(d.dq32 + 4 * (size_t)c, z);
 }
 
+// FP32 blocks in the reference's term order (ADI.cpp:62-217), one thread
+// per block entry (coalesced); the unfused alternative to mx_row below,
+// faster where chains are short (the autotuner picks)
+__global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= 48 * d.nRow || halted(d)) return;
+   const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
+   if (frozen_cell(d, d.row_scell[row])) return;
+   const int* ops = d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b;
+   float acc = 0.f;
+#pragma unroll
+   for (int o = 0; o < kOpsPerBlock; o++) {
+      const int op = ops[o];
+      if (op < 0) break;
+      const int slot = op >> 3, sel = (op >> 1) & 3, col = e & 3;
+      const float* m = d.ff32 + 32 * (size_t)slot;
+      float v;
+      if (sel == OP_SEL_RREFL && (col == 1 || col == 2)) {
+         const double4 rf = d.refl[d.slot_face[slot]];
+         const float r01 = m[16 + (e & ~3) + 1], r02 = m[16 + (e & ~3) + 2];
+         v = (col == 1) ? (float(rf.x) * r01 + float(rf.y) * r02) : (float(rf.z) * r01 + float(rf.w) * r02);
+      } else {
+         v = m[(sel == OP_SEL_L ? 0 : 16) + e];
+      }
+      if (op & 1) acc -= v;
+      else acc += v;
+   }
+   acc *= float(d.dtfac[d.row_scell[row]]);
+   if (b == 1 && (e >> 2) == (e & 3)) acc += 1.f;
+   d.blk32[t] = acc;
+}
+
 // ---------------- FP32 line solves, one thread per chain ----------------
 // The same split as the FP64 path: the block factorisation runs once per
 // step (mx_factor), each sweep replays the right-hand side (mx_solve).  One
@@ -221,8 +254,23 @@ __device__ __forceinline__ void mx_row(const DeviceState& d, int row, float (&A)
    for (int k = 0; k < 4; k++) B[5 * k] += 1.f;
 }
 
-// assembly fused with the factorisation: each thread builds its chain's
-// blocks straight from the FP32 face Jacobians
+// FUSED: each thread builds its chain's blocks straight from the FP32 face
+// Jacobians (no block array round trip; best for long chains); otherwise
+// it reads the blocks mx_assemble_kernel wrote
+template <bool FUSED>
+__device__ __forceinline__ void mx_rows(const DeviceState& d, int row, float (&A)[16], float (&B)[16], float (&C)[16])
+{
+   if (FUSED) {
+      mx_row(d, row, A, B, C);
+   } else {
+      const float* blk = d.blk32 + 48 * (size_t)row;
+      ld16f(blk, A);
+      ld16f(blk + 16, B);
+      ld16f(blk + 32, C);
+   }
+}
+
+template <bool FUSED>
 __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -233,10 +281,10 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    const bool per = d.chain_periodic[ich] != 0;
    float* fac = d.fac32 + (size_t)kRec * row0;
    float A[16], B[16], C[16], cp[16], ap[16];
-   mx_row(d, row0, A, B, C);
+   mx_rows<FUSED>(d, row0, A, B, C);
    for (int i = 0; i < N; i++) {
       float An[16], Bn[16], Cn[16];
-      if (i + 1 < N) mx_row(d, row0 + i + 1, An, Bn, Cn);
+      if (i + 1 < N) mx_rows<FUSED>(d, row0 + i + 1, An, Bn, Cn);
       float* rec = fac + (size_t)kRec * i;
       st16f(rec, A);
       float fill[16];
@@ -484,12 +532,18 @@ void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
    }
 }
 
+void launch_mx_assemble(const DeviceState& d, cudaStream_t st)
+{
+   if (!d.mx_fused) mx_assemble_kernel<<<blocks_for(48 * d.nRow), kThreads, 0, st>>>(d);
+}
+
 void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d); }
 
 void launch_mx_factor(const DeviceState& d, cudaStream_t st)
 {
    const int tb = d.mx_block;
-   mx_factor_kernel<<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
+   if (d.mx_fused) mx_factor_kernel<true><<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
+   else mx_factor_kernel<false><<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
 }
 
 void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st)

@@ -43,7 +43,7 @@ def test_autotune_mixed_restores_state_and_results(make_case, native_lib):
     a.set_precision(True)
     b.set_precision(True)
     rep = b.autotune(reps=2)
-    assert rep["precision"] == "mixed" and len(rep["candidates"]) == 8
+    assert rep["precision"] == "mixed" and len(rep["candidates"]) == 12
     assert np.array_equal(a.get("q"), b.get("q"))        # state put back
     a.march(6, 0.0)
     b.march(6, 0.0)
