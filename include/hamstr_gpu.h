@@ -199,6 +199,15 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * report (may be NULL) receives a JSON summary of the timings. */
 int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
 
+/* ---------------- learned warm start (no reference counterpart) --------
+ * C[M][N] (+ split * M * N when splits > 1) = A[M][K] * B[N][K]^T with A, B
+ * BF16 (K contiguous, 16-byte aligned device arrays) and FP32 accumulation
+ * on the tcgen05 tensor cores; M % 128 == 0, K % 64 == 0, N in {16, 64,
+ * 128} or a multiple of 256.  K is cut into `splits` ranges whose partial
+ * products go to consecutive M*N slabs.  *err (device int) becomes 1 if a
+ * wait timed out.  stream: a cudaStream_t or NULL. */
+int hamstr_mlp_gemm(const void* A, const void* B, int M, int N, int K, int splits, float* C, int* err, void* stream);
+
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
  * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */
