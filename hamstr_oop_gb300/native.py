@@ -71,6 +71,17 @@ def load(build_if_missing: bool = False):
         "hamstr_case_clone": (i, [vp, pp]),
         "hamstr_case_set_flow": (i, [vp, d, d]),
         "hamstr_gpu_set_cfl": (i, [vp, d]),
+        "hamstr_mlp_gemm": (i, [vp, vp, i, i, i, i, vp, vp, vp]),
+        "hamstr_mlp_nparams": (i, []),
+        "hamstr_mlp_create": (i, [i, ctypes.c_ulonglong, pp]),
+        "hamstr_mlp_destroy": (i, [vp]),
+        "hamstr_mlp_set_params": (i, [vp, vp]),
+        "hamstr_mlp_get_params": (i, [vp, vp]),
+        "hamstr_mlp_get_grads": (i, [vp, vp]),
+        "hamstr_mlp_forward": (i, [vp, vp, i, vp]),
+        "hamstr_mlp_grad": (i, [vp, vp, vp, i, ctypes.POINTER(d)]),
+        "hamstr_mlp_train_step": (i, [vp, vp, vp, ctypes.c_longlong, i, ctypes.c_ulonglong, ctypes.c_ulonglong,
+                                      ctypes.c_float, ctypes.POINTER(d)]),
         "hamstr_gpu_autotune": (i, [vp, i, ctypes.c_char_p, i]),
         "hamstr_gpu_set_geometry": (i, [vp, i, vp]),
         "hamstr_gpu_forces": (i, [vp, vp]),
@@ -388,3 +399,58 @@ class GpuSolver:
         n = ctypes.c_int(16)
         _check(load().hamstr_gpu_profile_step(self.h, reps, names, _ptr(ms), _ptr(cnt), ctypes.byref(n)))
         return {names[k].decode(): (float(ms[k]), int(cnt[k])) for k in range(n.value)}
+
+
+class Mlp:
+    """The warm-start network on the tensor cores (hamstr_mlp_*).  Device
+    arrays are torch CUDA tensors (float32, contiguous): features [n][5],
+    targets / outputs [n][4]."""
+
+    def __init__(self, batch_capacity: int = 65536, seed: int = 1):
+        h = ctypes.c_void_p()
+        _check(load().hamstr_mlp_create(int(batch_capacity), int(seed), ctypes.byref(h)))
+        self.h = h
+        self.nparams = int(load().hamstr_mlp_nparams())
+
+    def close(self):
+        if self.h:
+            load().hamstr_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.nparams, dtype=np.float32)
+        _check(load().hamstr_mlp_get_params(self.h, _ptr(out)))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(load().hamstr_mlp_set_params(self.h, _ptr(p)))
+
+    def get_grads(self) -> np.ndarray:
+        out = np.zeros(self.nparams, dtype=np.float32)
+        _check(load().hamstr_mlp_get_grads(self.h, _ptr(out)))
+        return out
+
+    def forward(self, feat):
+        import torch
+        y = torch.empty((feat.shape[0], 4), dtype=torch.float32, device=feat.device)
+        _check(load().hamstr_mlp_forward(self.h, feat.data_ptr(), int(feat.shape[0]), y.data_ptr()))
+        return y
+
+    def grad(self, feat, targ) -> float:
+        loss = ctypes.c_double(0.0)
+        _check(load().hamstr_mlp_grad(self.h, feat.data_ptr(), targ.data_ptr(), int(feat.shape[0]),
+                                      ctypes.byref(loss)))
+        return loss.value
+
+    def train_step(self, feat, targ, batch: int, seed: int, step: int, lr: float) -> float:
+        loss = ctypes.c_double(0.0)
+        _check(load().hamstr_mlp_train_step(self.h, feat.data_ptr(), targ.data_ptr(), int(feat.shape[0]), int(batch),
+                                            int(seed), int(step), float(lr), ctypes.byref(loss)))
+        return loss.value

@@ -208,6 +208,31 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  * wait timed out.  stream: a cudaStream_t or NULL. */
 int hamstr_mlp_gemm(const void* A, const void* B, int M, int N, int K, int splits, float* C, int* err, void* stream);
 
+/* The warm-start network (no reference counterpart): 5 -> 256 -> 256 ->
+ * 256 -> 4, GELU, BF16 weights and activations with FP32 accumulation,
+ * forward and backward on the tensor cores (hamstr_mlp_gemm), Adam on FP32
+ * master weights.  Parameters travel as FP32 in the order W1[256][5] b1
+ * W2[256][256] b2 W3[256][256] b3 W4[4][256] b4 (hamstr_mlp_nparams()).
+ * Device arrays: features [n][5], targets and outputs [n][4], FP32.
+ *   _create: batch capacity (rows per pass), seed of the initial weights;
+ *   _forward: outputs for n rows (any n, in chunks of the capacity);
+ *   _grad: loss (mean squared error over n <= capacity rows and the 4
+ *     outputs) and its gradient, kept for _get_grads;
+ *   _train_step: one Adam step (lr; betas 0.9, 0.999) on a minibatch of
+ *     `batch` rows (a multiple of 128) drawn from n_all rows by a seeded
+ *     hash of (seed, step); step counts from 0. */
+typedef struct hamstr_mlp hamstr_mlp;
+int hamstr_mlp_nparams(void);
+int hamstr_mlp_create(int batch_capacity, unsigned long long seed, hamstr_mlp** out);
+int hamstr_mlp_destroy(hamstr_mlp* h);
+int hamstr_mlp_set_params(hamstr_mlp* h, const float* params);
+int hamstr_mlp_get_params(hamstr_mlp* h, float* params);
+int hamstr_mlp_get_grads(hamstr_mlp* h, float* grads);
+int hamstr_mlp_forward(hamstr_mlp* h, const float* features, int n, float* outputs);
+int hamstr_mlp_grad(hamstr_mlp* h, const float* features, const float* targets, int n, double* loss);
+int hamstr_mlp_train_step(hamstr_mlp* h, const float* features, const float* targets, long long n_all, int batch,
+                          unsigned long long seed, unsigned long long step, float lr, double* loss);
+
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
  * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */

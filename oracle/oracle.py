@@ -243,6 +243,30 @@ def block_tridag4(a, b, c, f, periodic: bool, kind: str = "port"):
     return f
 
 
+def mlp_nparams() -> int:
+    lib, _ = _lib("port")
+    lib.mo_nparams.restype = ctypes.c_int
+    return int(lib.mo_nparams())
+
+
+def mlp_loss_grad(params, feat, targ, bf16: bool = True, grad: bool = True):
+    """Loss, gradient (or None) and outputs of the warm-start network
+    restated in FP64 (oracle/mlp_oracle.c); bf16 rounds what the GPU holds
+    in BF16."""
+    lib, _ = _lib("port")
+    fn = lib.mo_loss_grad
+    fn.restype = ctypes.c_double
+    fn.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    f = np.ascontiguousarray(feat, dtype=np.float64)
+    t = np.ascontiguousarray(targ, dtype=np.float64)
+    n = f.shape[0]
+    g = np.zeros(p.shape[0]) if grad else None
+    y = np.zeros((n, 4))
+    loss = fn(_ptr(p), _ptr(f), _ptr(t), n, int(bf16), _ptr(g) if grad else None, _ptr(y))
+    return loss, g, y
+
+
 def march_replicas(cases, iters: int) -> None:
     """Run ``iters`` steps on each port case, one OpenMP thread per case."""
     lib, _ = _lib("port")

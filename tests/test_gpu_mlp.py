@@ -41,3 +41,43 @@ def test_gemm_matches_fp32_product(native_lib, M, N, K, splits):
     scale = ref.abs().max().item()
     err = (C - ref).abs().max().item()
     assert err <= 1e-5 * scale * max(1.0, K / 256), (err, scale)
+
+
+def _data(n, seed):
+    import torch
+    rng = np.random.default_rng(seed)
+    f = rng.uniform(-1.0, 1.0, (n, 5)).astype(np.float32)
+    # a smooth target of the inputs
+    t = np.stack([np.sin(f[:, 0] + f[:, 2]), f[:, 1] * f[:, 3], np.cos(f[:, 4]) - 0.5, f[:, 0] * 0.3 + f[:, 2] ** 2],
+                 axis=1).astype(np.float32)
+    return f, t, torch.from_numpy(f).cuda(), torch.from_numpy(t).cuda()
+
+
+def test_forward_and_gradient_match_the_oracle(native_lib, oracle_lib):
+    from hamstr_oop_gb300 import native
+    net = native.Mlp(batch_capacity=512, seed=7)
+    p = net.get_params().astype(np.float64)
+    f, t, fd, td = _data(384, 3)
+    y_gpu = net.forward(fd).cpu().numpy()
+    loss_o, g_o, y_o = oracle_lib.mlp_loss_grad(p, f, t, bf16=True)
+    assert np.max(np.abs(y_gpu - y_o)) <= 1e-2 * np.max(np.abs(y_o)) + 1e-3
+    loss_g = net.grad(fd, td)
+    assert abs(loss_g - loss_o) <= 2e-3 * loss_o, (loss_g, loss_o)
+    g_g = net.get_grads().astype(np.float64)
+    bounds = np.cumsum([0, 1280, 256, 65536, 256, 65536, 256, 1024, 4])
+    names = ["W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"]
+    for name, a, b in zip(names, bounds[:-1], bounds[1:]):
+        rel = np.linalg.norm(g_g[a:b] - g_o[a:b]) / max(np.linalg.norm(g_o[a:b]), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+
+
+def test_training_reduces_the_loss(native_lib):
+    from hamstr_oop_gb300 import native
+    net = native.Mlp(batch_capacity=4096, seed=11)
+    f, t, fd, td = _data(20000, 5)
+    first = None
+    for step in range(300):
+        loss = net.train_step(fd, td, batch=2048, seed=99, step=step, lr=2e-3)
+        if first is None:
+            first = loss
+    assert loss < 0.1 * first, (first, loss)
