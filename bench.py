@@ -68,6 +68,13 @@ BATCH = {
 }
 WORKLOADS.update({k: dict(v, batch=True) for k, v in BATCH.items()})
 
+# The learned warm start: train on solver-generated converged states, then
+# solve held-out conditions from the network's guess and from freestream.
+WORKLOADS["c5"] = dict(warm=True, ni=256, nj=64, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2,
+                       Mach=0.5, alpha=1.25, ramp=(), train=2048, test=256, tol=1e-10, cap=8000, epochs=30,
+                       batch=16384, lr=2e-3,
+                       name="naca0012_256x64_order1_cfl10_warmstart_mlp5-256x3-4_train2048_test256")
+
 # converged-solve measurement: a case that reaches 1e-10 (the MUSCL and WENO
 # cases plateau near 1e-9 on these meshes, as the survey's probes found)
 CONVERGE = dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
@@ -115,6 +122,77 @@ def open_oracle(wl: dict, case_dir: str):
     o.set_option("chain_end_rule", wl["end_rule"])
     o.set_option("limiter", wl.get("limiter", 0))
     return o
+
+
+def gemm_peak(size: int = 8192, reps: int = 5) -> dict:
+    """The tcgen05 GEMM alone on a large square BF16 problem: the tensor
+    roofline of the warm-start kernels."""
+    import torch
+    from hamstr_oop_gb300 import native
+    L = native.load()
+    A = torch.randn((size, size), device="cuda").to(torch.bfloat16)
+    B = torch.randn((size, size), device="cuda").to(torch.bfloat16)
+    C = torch.empty((size, size), dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(2):
+        native._check(L.hamstr_mlp_gemm(A.data_ptr(), B.data_ptr(), size, size, size, 1, C.data_ptr(),
+                                        err.data_ptr(), st))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        native._check(L.hamstr_mlp_gemm(A.data_ptr(), B.data_ptr(), size, size, size, 1, C.data_ptr(),
+                                        err.data_ptr(), st))
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ok = int(err.item()) == 0
+    rel = float((C[:256, :256] - (A[:256].float() @ B[:256].float().T)).abs().max() /
+                (A[:256].float() @ B[:256].float().T).abs().max())
+    peaks = measured_peaks()
+    tf = 2.0 * size ** 3 / (ms * 1e-3) / 1e12
+    return {"M": size, "N": size, "K": size, "ms": ms, "tflops": tf, "ok": ok, "max_rel_err_vs_fp32": rel,
+            "peak_tflops": peaks.get("bf16_tflops"), "frac": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None}
+
+
+def run_warmstart(args, wl, rank, local_rank, world):
+    """C5: data generation with the batched solver, training on the tensor
+    cores, and the held-out comparison (warm vs freestream start)."""
+    import numpy as np
+    import torch
+    from hamstr_oop_gb300 import native, warmstart
+    torch.cuda.set_device(local_rank)
+    native.load()
+    ntrain = args.c5_train or wl["train"]
+    ntest = args.c5_test or wl["test"]
+    case_dir = make_case(wl, 0)
+    case = open_case(wl, case_dir)
+    t0 = time.perf_counter()
+    train_conds = warmstart.conditions(ntrain, seed=0)
+    data = warmstart.solve_batch(case, train_conds, wl["tol"], wl["cap"])
+    t_data = time.perf_counter() - t0
+    model, trep = warmstart.train(case, data["q"], train_conds, epochs=wl["epochs"], batch=wl["batch"], lr=wl["lr"])
+    test_conds = warmstart.conditions(ntest, seed=1)
+    ev = warmstart.evaluate(case, model, test_conds, wl["tol"], wl["cap"])
+    peak = gemm_peak()
+    peaks = measured_peaks()
+    trep.pop("loss_curve", None)
+    return {"metric": "converged solves/s (L2 <= 1e-10), held-out conditions, warm start",
+            "value": ev["solves_per_s_warm"], "unit": "solves/s", "n_gpus": 1, "steps": None, "warmup": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 residual, f32 Jacobian/ADI; network bf16 with f32 accumulation", "data": "synthetic",
+            "config": {"workload": wl["name"], "mesh": [wl["ni"], wl["nj"]], "train_conditions": ntrain,
+                       "test_conditions": ntest, "order": wl["order"], "CFL": wl["CFL"], "msweep": wl["msweep"],
+                       "tol": wl["tol"], "cap": wl["cap"]},
+            "freestream_start": {"solves_per_s": ev["solves_per_s_freestream"], "steps_mean": ev["steps_freestream_mean"],
+                                 "seconds": ev["seconds_freestream"]},
+            "warm_start": ev, "training": trep,
+            "data_generation": {"conditions": ntrain, "seconds": t_data, "all_converged": data["all_converged"],
+                                "steps_mean": float(np.mean(data["steps"]))},
+            "roofline": {"kernel": "tcgen05 bf16 GEMM (mlp_gemm.cu)", "bound": "tensor",
+                         "achieved": peak["tflops"], "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                         "frac": peak["frac"], "traffic": None, "gemm": peak,
+                         "training_gemm_tflops": trep["gemm_tflops"]}}
 
 
 def batch_conditions(b: dict, n: int = None, meshes=None):
@@ -364,8 +442,9 @@ def measured_peaks() -> dict:
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d.get("bf16_tflops", 1900.0)),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 # FP64 issue peak of the GPU, warp instructions per second, measured with an
@@ -700,6 +779,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only ramp and run this many steps (a plain run for ncu), no timing")
     ap.add_argument("--profile-precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
+    ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
     wl = WORKLOADS[args.workload]
@@ -711,7 +792,10 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    out = (run_batch if wl.get("batch") else run_gpu)(args, wl, rank, local_rank, world)
+    if wl.get("warm"):
+        out = run_warmstart(args, wl, rank, local_rank, world) if rank == 0 else None
+    else:
+        out = (run_batch if wl.get("batch") else run_gpu)(args, wl, rank, local_rank, world)
     if out is not None:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -1,0 +1,210 @@
+"""Learned warm start: a network maps the flow condition and a cell's geometry
+to the converged conserved state, so the solver starts close to its answer.
+
+The network (5 -> 256 -> 256 -> 256 -> 4, GELU, BF16 weights, FP32
+accumulation) is trained on the GPU by the project's own tensor-core kernels
+(``native.Mlp``: tcgen05 GEMMs with fused epilogues, Adam), on converged
+solutions the batched solver generates itself.  The solver then always
+iterates to the same residual tolerance from the network's guess, and falls
+back to the freestream start for any condition whose initial residual is
+worse than the freestream one.
+
+Inputs (normalised, fixed transforms): Mach, alpha (degrees), cell centre
+x, y and distance to the wall.  Outputs: (q - q_freestream) / scale per
+conserved component, scale = the training set's standard deviation.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+GAMMA = 1.4
+
+
+def freestream(mach: float, alpha_deg: float) -> np.ndarray:
+    """rho, rho u, rho v, E of the reference's initial state (initFlow.cpp:24-91)."""
+    a = alpha_deg * np.pi / 180.0
+    u, v = mach * np.cos(a), mach * np.sin(a)
+    pinf = 1.0 / GAMMA
+    return np.array([1.0, u, v, pinf / (GAMMA - 1.0) + 0.5 * (u * u + v * v)])
+
+
+def cell_geometry(case) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Cell centres (the mean of the cell's face midpoints) and the distance
+    from each to the nearest wall face, from a native.Case."""
+    x = case.get("x").reshape(-1, 2)
+    f = case.get_int("faces").reshape(-1, 6)
+    n1, n2, cl, cr = f[:, 0], f[:, 1], f[:, 2], f[:, 4]
+    mid = 0.5 * (x[n1] + x[n2])
+    nc = case.sizes["nCell"]
+    acc = np.zeros((nc, 2))
+    cnt = np.zeros(nc)
+    np.add.at(acc, cl, mid)
+    np.add.at(cnt, cl, 1.0)
+    inner = cr >= 0
+    np.add.at(acc, cr[inner], mid[inner])
+    np.add.at(cnt, cr[inner], 1.0)
+    cen = acc / cnt[:, None]
+    wall = cr == -2
+    a, b = x[n1[wall]], x[n2[wall]]
+    ab = b - a
+    L2 = np.maximum((ab * ab).sum(axis=1), 1e-300)
+    d = np.full(nc, np.inf)
+    for s in range(0, nc, 4096):
+        p = cen[s:s + 4096, None, :]
+        t = np.clip(((p - a[None]) * ab[None]).sum(axis=2) / L2[None], 0.0, 1.0)
+        proj = a[None] + t[..., None] * ab[None]
+        d[s:s + 4096] = np.sqrt(((p - proj) ** 2).sum(axis=2)).min(axis=1)
+    return cen[:, 0], cen[:, 1], d
+
+
+def features(mach: float, alpha: float, geo) -> np.ndarray:
+    """[nCell][5] float32 network inputs for one condition."""
+    xc, yc, d = geo
+    n = xc.shape[0]
+    out = np.empty((n, 5), dtype=np.float32)
+    out[:, 0] = (mach - 0.575) / 0.16
+    out[:, 1] = (alpha - 1.0) / 1.75
+    out[:, 2] = np.arcsinh(2.0 * (xc - 0.5)) / 4.0
+    out[:, 3] = np.arcsinh(2.0 * yc) / 4.0
+    out[:, 4] = np.log10(d + 1e-4) / 2.0 + 1.0
+    return out
+
+
+def conditions(n: int, seed: int, mach=(0.3, 0.85), alpha=(-2.0, 4.0)) -> list:
+    rng = np.random.default_rng(seed)
+    return list(zip(rng.uniform(mach[0], mach[1], n).tolist(), rng.uniform(alpha[0], alpha[1], n).tolist()))
+
+
+def solve_batch(case, conds: list, tol: float, cap: int, q0: list | None = None, mixed: bool = True,
+                batch: int = 256) -> dict:
+    """March every condition to L2 <= tol in batched handles; per-condition
+    steps (rows of computeRHS until its stop, cap if never), final states,
+    and wall time."""
+    import torch
+    from . import native
+    steps, qs, secs, conv = [], [], 0.0, True
+    for s in range(0, len(conds), batch):
+        chunk = conds[s:s + batch]
+        cs = []
+        for m, a in chunk:
+            c = case.clone()
+            c.set_flow(m, a)
+            cs.append(c)
+        g = native.GpuSolver.batch(cs)
+        g.set_precision(mixed)
+        g.march(2, 0.0)                                   # graph capture, warm-up
+        qin = [c.get("q") for c in cs] if q0 is None else [np.ravel(q) for q in q0[s:s + batch]]
+        g.set("q", np.concatenate(qin))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist, ok = g.march(cap, tol)
+        secs += time.perf_counter() - t0
+        conv = conv and ok
+        cell0 = g.instance_cells()
+        q = g.get("q").reshape(-1, 4)
+        for k in range(len(chunk)):
+            hit = np.flatnonzero(hist[:, k, 0] <= tol)
+            steps.append(int(hit[0]) + 1 if hit.size else cap)
+            qs.append(q[cell0[k]:cell0[k + 1]].copy())
+        g.close()
+    return {"steps": steps, "q": qs, "seconds": secs, "all_converged": conv}
+
+
+def initial_residuals(case, conds: list, q0: list, batch: int = 256) -> np.ndarray:
+    """computeRHS L2 of each condition at the given states (one batched evaluation)."""
+    from . import native
+    out = []
+    for s in range(0, len(conds), batch):
+        cs = []
+        for m, a in conds[s:s + batch]:
+            c = case.clone()
+            c.set_flow(m, a)
+            cs.append(c)
+        g = native.GpuSolver.batch(cs)
+        g.set("q", np.concatenate([np.ravel(q) for q in q0[s:s + batch]]))
+        g.compute_rhs(True)
+        out.extend(g.instance_norms()[:, 0].tolist())
+        g.close()
+    return np.asarray(out)
+
+
+@dataclasses.dataclass
+class WarmStartModel:
+    net: object          # native.Mlp
+    scale: np.ndarray    # [4] output scale
+    geo: tuple           # cell geometry of the mesh it was trained on
+
+    def predict(self, conds: list) -> list:
+        """Warm-start states [nCell][4] for each (Mach, alpha)."""
+        import torch
+        out = []
+        for m, a in conds:
+            f = torch.from_numpy(features(m, a, self.geo)).cuda()
+            y = self.net.forward(f).double().cpu().numpy()
+            out.append(freestream(m, a)[None, :] + y * self.scale[None, :])
+        return out
+
+
+def train(case, q_train: list, conds: list, epochs: int = 30, batch: int = 16384, lr: float = 2e-3,
+          seed: int = 1) -> tuple[WarmStartModel, dict]:
+    """Fit the network to converged states; returns the model and a report
+    (loss curve, throughput, tensor-core FLOP rate of the training steps)."""
+    import torch
+    from . import native
+    geo = cell_geometry(case)
+    nc = geo[0].shape[0]
+    feat = np.concatenate([features(m, a, geo) for m, a in conds])
+    delta = np.concatenate([q - freestream(m, a)[None, :] for q, (m, a) in zip(q_train, conds)])
+    scale = delta.std(axis=0) + 1e-12
+    targ = (delta / scale[None, :]).astype(np.float32)
+    fd, td = torch.from_numpy(feat).cuda(), torch.from_numpy(targ).cuda()
+    net = native.Mlp(batch_capacity=batch, seed=seed)
+    n = feat.shape[0]
+    steps = max(1, epochs * n // batch)
+    losses = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        # cosine learning-rate decay to 5% of lr
+        lr_k = lr * (0.05 + 0.95 * 0.5 * (1.0 + np.cos(np.pi * k / steps)))
+        loss = net.train_step(fd, td, batch=batch, seed=seed + 1000, step=k, lr=lr_k)
+        if k % max(1, steps // 50) == 0 or k == steps - 1:
+            losses.append((k, loss))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    # GEMM flops per sample: forward 2*(64*256 + 2*256*256 + 256*16), backward twice that
+    flops = 3.0 * 2.0 * (64 * 256 + 2 * 256 * 256 + 256 * 16)
+    report = {"samples": n, "cells_per_condition": nc, "conditions": len(conds), "batch": batch, "steps": steps,
+              "epochs": epochs, "seconds": dt, "samples_per_s": steps * batch / dt,
+              "gemm_tflops": steps * batch * flops / dt / 1e12, "loss_first": losses[0][1],
+              "loss_last": losses[-1][1], "loss_curve": losses}
+    return WarmStartModel(net=net, scale=scale, geo=geo), report
+
+
+def evaluate(case, model: WarmStartModel, conds: list, tol: float, cap: int, mixed: bool = True) -> dict:
+    """Held-out conditions from the freestream and from the network's guess
+    (falling back to the freestream where its initial residual is worse)."""
+    fs = [np.tile(freestream(m, a), (case.sizes["nCell"], 1)) for m, a in conds]
+    ws = model.predict(conds)
+    r_fs = initial_residuals(case, conds, fs)
+    r_ws = initial_residuals(case, conds, ws)
+    use = [w if rw <= rf else f for w, f, rw, rf in zip(ws, fs, r_ws, r_fs)]
+    fallbacks = int(np.sum(r_ws > r_fs))
+    a = solve_batch(case, conds, tol, cap, q0=fs, mixed=mixed)
+    b = solve_batch(case, conds, tol, cap, q0=use, mixed=mixed)
+    # accuracy of the guess against the converged state
+    err = [np.max(np.abs(w - q)) / np.max(np.abs(q)) for w, q in zip(ws, a["q"])]
+    diff = [np.max(np.abs(p - q)) / np.max(np.abs(q)) for p, q in zip(a["q"], b["q"])]
+    sa, sb = np.asarray(a["steps"]), np.asarray(b["steps"])
+    return {"conditions": len(conds), "tol": tol, "cap": cap, "fallbacks": fallbacks,
+            "initial_l2_freestream_median": float(np.median(r_fs)), "initial_l2_warm_median": float(np.median(r_ws)),
+            "guess_max_rel_error_median": float(np.median(err)),
+            "steps_freestream_mean": float(sa.mean()), "steps_warm_mean": float(sb.mean()),
+            "steps_ratio": float(sa.mean() / max(sb.mean(), 1.0)),
+            "seconds_freestream": a["seconds"], "seconds_warm": b["seconds"],
+            "solves_per_s_freestream": len(conds) / a["seconds"], "solves_per_s_warm": len(conds) / b["seconds"],
+            "all_converged": bool(a["all_converged"] and b["all_converged"]),
+            "converged_state_difference_max": float(np.max(diff))}

@@ -1,0 +1,37 @@
+"""The learned warm start end to end on a small case: converged training
+states from the batched solver, a few epochs on the tensor cores, and the
+held-out conditions solved from the network's guess and from freestream.
+The network must cut the iterations to the tolerance; the converged states
+must not depend on the start."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_warm_start_cuts_iterations(make_case, native_lib):
+    from hamstr_oop_gb300 import native, warmstart
+    case = native.Case(make_case(64, 16, order=1, CFL=10.0, msweep=2))
+    train = warmstart.conditions(48, seed=0)
+    data = warmstart.solve_batch(case, train, 1e-10, 6000)
+    assert data["all_converged"]
+    model, rep = warmstart.train(case, data["q"], train, epochs=200, batch=4096, lr=2e-3)
+    assert rep["loss_last"] < 0.05 * rep["loss_first"], rep
+    test = warmstart.conditions(12, seed=1)
+    ev = warmstart.evaluate(case, model, test, 1e-10, 6000)
+    assert ev["all_converged"]
+    assert ev["initial_l2_warm_median"] < ev["initial_l2_freestream_median"]
+    assert ev["steps_warm_mean"] < ev["steps_freestream_mean"], ev
+    # both starts reach the same steady state (to the tolerance's reach)
+    assert ev["converged_state_difference_max"] < 1e-3, ev
+
+
+def test_features_and_geometry(make_case, native_lib):
+    from hamstr_oop_gb300 import native, warmstart
+    case = native.Case(make_case(32, 8))
+    xc, yc, d = warmstart.cell_geometry(case)
+    assert xc.shape == (256,) and np.all(d > 0)
+    # the first ring of cells sits next to the wall, the last near the far field
+    assert d[:32].max() < 0.05 and d[-32:].min() > 5.0
+    f = warmstart.features(0.5, 1.25, (xc, yc, d))
+    assert f.shape == (256, 5) and np.all(np.isfinite(f))
