@@ -85,7 +85,7 @@ def solve_batch(case, conds: list, tol: float, cap: int, q0: list | None = None,
     and wall time."""
     import torch
     from . import native
-    steps, qs, secs, conv = [], [], 0.0, True
+    steps, qs, hists, secs, conv = [], [], [], 0.0, True
     for s in range(0, len(conds), batch):
         chunk = conds[s:s + batch]
         cs = []
@@ -109,8 +109,9 @@ def solve_batch(case, conds: list, tol: float, cap: int, q0: list | None = None,
             hit = np.flatnonzero(hist[:, k, 0] <= tol)
             steps.append(int(hit[0]) + 1 if hit.size else cap)
             qs.append(q[cell0[k]:cell0[k + 1]].copy())
+            hists.append(hist[:steps[-1], k, 0].copy())
         g.close()
-    return {"steps": steps, "q": qs, "seconds": secs, "all_converged": conv}
+    return {"steps": steps, "q": qs, "hist": hists, "seconds": secs, "all_converged": conv}
 
 
 def initial_residuals(case, conds: list, q0: list, batch: int = 256) -> np.ndarray:
@@ -184,26 +185,40 @@ def train(case, q_train: list, conds: list, epochs: int = 30, batch: int = 16384
     return WarmStartModel(net=net, scale=scale, geo=geo), report
 
 
-def evaluate(case, model: WarmStartModel, conds: list, tol: float, cap: int, mixed: bool = True) -> dict:
-    """Held-out conditions from the freestream and from the network's guess
-    (falling back to the freestream where its initial residual is worse)."""
+def evaluate(case, model: WarmStartModel, conds: list, tol: float, cap: int, mixed: bool = True,
+             probe: int = 20) -> dict:
+    """Held-out conditions solved from the freestream and from the network's
+    guess.  Two guards choose, per condition, which start the solver keeps:
+      "initial": the network's guess unless its initial computeRHS L2 is
+                 larger than the freestream's (no extra work);
+      "probe":   `probe` steps from both starts, then the one with the lower
+                 L2 continues; both probes count against the chosen path.
+    Steps are computeRHS evaluations to L2 <= tol (cap if never)."""
     fs = [np.tile(freestream(m, a), (case.sizes["nCell"], 1)) for m, a in conds]
     ws = model.predict(conds)
     r_fs = initial_residuals(case, conds, fs)
     r_ws = initial_residuals(case, conds, ws)
-    use = [w if rw <= rf else f for w, f, rw, rf in zip(ws, fs, r_ws, r_fs)]
-    fallbacks = int(np.sum(r_ws > r_fs))
     a = solve_batch(case, conds, tol, cap, q0=fs, mixed=mixed)
-    b = solve_batch(case, conds, tol, cap, q0=use, mixed=mixed)
-    # accuracy of the guess against the converged state
+    b = solve_batch(case, conds, tol, cap, q0=ws, mixed=mixed)
+    sa, sb = np.asarray(a["steps"]), np.asarray(b["steps"])
+    init_pick = r_ws <= r_fs
+    s_init = np.where(init_pick, sb, sa)
+
+    def at(h, k):
+        return h[min(k, h.shape[0] - 1)]
+    probe_pick = np.array([at(hb, probe) <= at(ha, probe) for ha, hb in zip(a["hist"], b["hist"])])
+    s_probe = np.where(probe_pick, sb, sa) + np.minimum(np.where(probe_pick, sa, sb), probe)
     err = [np.max(np.abs(w - q)) / np.max(np.abs(q)) for w, q in zip(ws, a["q"])]
     diff = [np.max(np.abs(p - q)) / np.max(np.abs(q)) for p, q in zip(a["q"], b["q"])]
-    sa, sb = np.asarray(a["steps"]), np.asarray(b["steps"])
-    return {"conditions": len(conds), "tol": tol, "cap": cap, "fallbacks": fallbacks,
+    return {"conditions": len(conds), "tol": tol, "cap": cap,
             "initial_l2_freestream_median": float(np.median(r_fs)), "initial_l2_warm_median": float(np.median(r_ws)),
             "guess_max_rel_error_median": float(np.median(err)),
             "steps_freestream_mean": float(sa.mean()), "steps_warm_mean": float(sb.mean()),
-            "steps_ratio": float(sa.mean() / max(sb.mean(), 1.0)),
+            "steps_guard_initial_mean": float(s_init.mean()), "fallbacks_initial": int(np.sum(~init_pick)),
+            "steps_guard_probe_mean": float(s_probe.mean()), "fallbacks_probe": int(np.sum(~probe_pick)),
+            "probe_steps": probe,
+            "steps_ratio_warm": float(sa.mean() / max(sb.mean(), 1.0)),
+            "steps_ratio_guard_probe": float(sa.mean() / max(s_probe.mean(), 1.0)),
             "seconds_freestream": a["seconds"], "seconds_warm": b["seconds"],
             "solves_per_s_freestream": len(conds) / a["seconds"], "solves_per_s_warm": len(conds) / b["seconds"],
             "all_converged": bool(a["all_converged"] and b["all_converged"]),

@@ -20,8 +20,10 @@ def test_warm_start_cuts_iterations(make_case, native_lib):
     test = warmstart.conditions(12, seed=1)
     ev = warmstart.evaluate(case, model, test, 1e-10, 6000)
     assert ev["all_converged"]
-    assert ev["initial_l2_warm_median"] < ev["initial_l2_freestream_median"]
+    assert ev["guess_max_rel_error_median"] < 0.05, ev
     assert ev["steps_warm_mean"] < ev["steps_freestream_mean"], ev
+    # the probe guard keeps the network's start where it helps
+    assert ev["steps_guard_probe_mean"] < ev["steps_freestream_mean"], ev
     # both starts reach the same steady state (to the tolerance's reach)
     assert ev["converged_state_difference_max"] < 1e-3, ev
 
