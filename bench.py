@@ -779,10 +779,17 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only ramp and run this many steps (a plain run for ncu), no timing")
     ap.add_argument("--profile-precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--gemm-only", type=int, default=0, metavar="SIZE",
+                    help="only time the tcgen05 BF16 GEMM on SIZE^3 (a plain run for ncu)")
     ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
     ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
+    if args.gemm_only:
+        import torch
+        torch.cuda.set_device(local_rank)
+        print(json.dumps(gemm_peak(args.gemm_only)), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         out = run_reference(args, wl, rank)
