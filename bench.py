@@ -453,7 +453,7 @@ FP64_WARP_INSTR_PER_S = 15.8e9
 
 
 def ncu_profile_table() -> dict:
-    """kernel -> {workload, dram_bytes, fp64_pipe_pct} from profiles/ncu_kernel_table.txt."""
+    """(kernel, workload) -> {dram_bytes, fp64_pipe_pct} from profiles/ncu_kernel_table.txt."""
     p = os.path.join(ROOT, "profiles", "ncu_kernel_table.txt")
     out = {}
     if not os.path.exists(p):
@@ -465,7 +465,7 @@ def ncu_profile_table() -> dict:
         f = ln.split()
         if len(f) >= 4:
             try:
-                out[f[0]] = {"workload": f[1], "dram_bytes": float(f[2]), "fp64_pipe_pct": float(f[3])}
+                out[(f[0], f[1])] = {"workload": f[1], "dram_bytes": float(f[2]), "fp64_pipe_pct": float(f[3])}
             except ValueError:
                 pass
     return out
@@ -609,13 +609,14 @@ def run_gpu(args, wl, rank, local_rank, world):
         alg = algorithmic_bytes(dom, lay, sizes, wl["order"])
         achieved = alg / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else None
         table = ncu_profile_table()
-        row = table.get(dom, {})
+        row = table.get((dom, wl["name"]), {})
         traffic = row.get("dram_bytes") if row.get("workload") == wl["name"] else None
         fp64 = None
         if row.get("workload") == wl["name"]:
             fp64 = {"pipe_active_pct": row["fp64_pipe_pct"], "peak_warp_inst_per_s": FP64_WARP_INSTR_PER_S,
-                    "source": "ncu sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active, "
-                              "profiles/%s_naca512x128_weno5.md" % dom,
+                    "source": "ncu sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active, " +
+                              ("profiles/fp64_kernels_naca512x128_split50_weno5.md" if wl["split"] > 0
+                               else "profiles/%s_naca512x128_weno5.md" % dom),
                     "note": "the path is FP64-issue bound on GB300; HBM fraction is reported as the contract asks"}
         roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
