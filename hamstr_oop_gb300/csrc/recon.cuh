@@ -13,6 +13,7 @@
 
 #include "device_state.h"
 #include "plan.h"
+#include "softdiv.cuh"
 
 namespace hamstr {
 
@@ -248,11 +249,11 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
    const double q30 = 2. * a - 7. * b + 11. * c;
    const double q31 = -b + 5. * c + 2. * d;
    const double q32 = 2. * c + 5. * d - e;
-   const double d01 = dis0 / dis1;
-   const double d02 = dis0 / dis2;
+   const double d01 = Dv<double>(dis1).div(dis0);
+   const double d02 = Dv<double>(dis2).div(dis0);
    const double a1ba0 = 6. * d01;
    const double a2ba0 = 3. * d02;
-   const double w0 = 1.0 / (1.0 + a1ba0 + a2ba0);
+   const double w0 = Dv<double>(1.0 + a1ba0 + a2ba0).div(1.0);
    const double w1 = a1ba0 * w0;
    const double w2 = 1. - w0 - w1;
    return b2 * (w0 * q30 + w1 * q31 + w2 * q32);
@@ -277,11 +278,12 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
    const T q30 = T(2.) * a - T(7.) * b + T(11.) * c;
    const T q31 = -b + T(5.) * c + T(2.) * d;
    const T q32 = T(2.) * c + T(5.) * d - e;
-   const T d01 = dis0 / dis1;
-   const T d02 = dis0 / dis2;
+   const Dv<T> r1(dis1), r2(dis2);
+   const T d01 = r1.div(dis0);
+   const T d02 = r2.div(dis0);
    const T a1ba0 = T(6.) * d01;
    const T a2ba0 = T(3.) * d02;
-   const T w0 = T(1.0) / (T(1.0) + a1ba0 + a2ba0);
+   const T w0 = Dv<T>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
    const T w1 = a1ba0 * w0;
    const T w2 = T(1.) - w0 - w1;
    const T djm1_d = a_d - T(2.) * b_d + c_d;
@@ -304,13 +306,14 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
    const T dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
    const T dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
                                        + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
-   const T dw0 = (dw0_up_1 - dw0_up_2) / (dw0_down * dw0_down);
+   const Dv<T> rd(dw0_down * dw0_down);
+   const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
    const T dw1_up_1 = T(6) * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
-   const T dw1_up_2 = T(6) * dw0_up_2 / beta1 * beta0;
-   const T dw1 = (dw1_up_1 - dw1_up_2) / (dw0_down * dw0_down);
+   const T dw1_up_2 = r1.div(T(6) * dw0_up_2) * beta0;
+   const T dw1 = rd.div(dw1_up_1 - dw1_up_2);
    const T dw2_up_1 = T(3) * (dbeta0 * beta1 + beta0 * dbeta1) * dw0_down;
-   const T dw2_up_2 = T(3) * dw0_up_2 / beta2 * beta0;
-   const T dw2 = (dw2_up_1 - dw2_up_2) / (dw0_down * dw0_down);
+   const T dw2_up_2 = r2.div(T(3) * dw0_up_2) * beta0;
+   const T dw2 = rd.div(dw2_up_1 - dw2_up_2);
    return term1 + term2 + term3 + b2 * dw0 * q30 + b2 * dw1 * q31 + b2 * dw2 * q32;
 }
 

@@ -3,9 +3,11 @@
 // roe.cuh -- Roe flux and its frozen-eigenvalue Jacobian, per face
 //
 // Compiled with -fmad=false: every a*b+c below rounds the product and the
-// sum separately, the arithmetic of the reference on x86-64, and `/` and
-// sqrt are the IEEE correctly rounded operations.  Expressions keep the
-// reference's association order so the results are bit-identical.
+// sum separately, the arithmetic of the reference on x86-64, and divisions
+// and sqrt are the IEEE correctly rounded operations (the FP64 divisions
+// of roe_face run on the integer pipes, softdiv.cuh, with the same
+// results).  Expressions keep the reference's association order so the
+// results are bit-identical.
 //
 // Flux: fluxRoe2D, interfaceFlux.cpp:24-169.
 // Jacobian: jacobianRoe2D -> jacobianRoe3D with IMODE=1
@@ -23,6 +25,8 @@
 #ifndef HAMSTR_GPU_ROE_CUH
 #define HAMSTR_GPU_ROE_CUH
 
+#include "softdiv.cuh"
+
 namespace hamstr {
 
 struct RoeOut {
@@ -39,33 +43,38 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
 {
    const double gm1 = gam - 1.0;
    const double area = sqrt(nxd * nxd + nyd * nyd);
-   const double invArea = 1. / area;
+   const Dv<double> by_area(area);
+   const double invArea = by_area.div(1.);
    const double nx = nxd * invArea;
    const double ny = nyd * invArea;
 
    const double rol = ql[0];
-   const double ul = ql[1] / ql[0];
-   const double vl = ql[2] / ql[0];
+   const Dv<double> by_rol(rol);
+   const double ul = by_rol.div(ql[1]);
+   const double vl = by_rol.div(ql[2]);
    const double pl = gm1 * (ql[3] - 0.5 * rol * (ul * ul + vl * vl));
-   const double hl = (ql[3] + pl) / rol;
+   const double hl = by_rol.div(ql[3] + pl);
    const double ror = qr[0];
-   const double ur = qr[1] / qr[0];
-   const double vr = qr[2] / qr[0];
+   const Dv<double> by_ror(ror);
+   const double ur = by_ror.div(qr[1]);
+   const double vr = by_ror.div(qr[2]);
    const double pr = gm1 * (qr[3] - 0.5 * ror * (ur * ur + vr * vr));
-   const double hr = (qr[3] + pr) / ror;
+   const double hr = by_ror.div(qr[3] + pr);
    const double dp = pr - pl;
    const double uconr = ur * nx + vr * ny;
    const double uconl = ul * nx + vl * ny;
 
-   const double fact = sqrt(ror / rol);
-   const double A = 1.0 / (1.0 + fact);
-   const double B = fact / (1.0 + fact);
+   const double fact = sqrt(by_rol.div(ror));
+   const Dv<double> by_1f(1.0 + fact);
+   const double A = by_1f.div(1.0);
+   const double B = by_1f.div(fact);
    const double robar = rol * fact;
    const double ubar = ul * A + ur * B;
    const double vbar = vl * A + vr * B;
    const double hbar = hl * A + hr * B;
    double cbar = gm1 * (hbar - 0.5 * (ubar * ubar + vbar * vbar));
    cbar = sqrt(cbar);
+   const Dv<double> by_c(cbar);
    const double uconbar = ubar * nx + vbar * ny;
 
    {
@@ -76,8 +85,8 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
       if (spec != spec) return false;
       const double term1 = -eig1 + 0.5 * (eig2 + eig3);
       const double term2 = 0.5 * (eig2 - eig3);
-      const double del1 = term1 * dp / cbar / cbar + term2 * robar * (uconr - uconl) / cbar;
-      const double del2 = term1 * (uconr - uconl) * robar + term2 * dp / cbar;
+      const double del1 = by_c.div(by_c.div(term1 * dp)) + by_c.div(term2 * robar * (uconr - uconl));
+      const double del2 = term1 * (uconr - uconl) * robar + by_c.div(term2 * dp);
       double fm0 = eig1 * (qr[0] - ql[0]);
       double fm1 = eig1 * (qr[1] - ql[1]);
       double fm2 = eig1 * (qr[2] - ql[2]);
@@ -104,8 +113,8 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    if (!JAC) return true;
 
    // ---------------- Jacobian (jacobianRoe3D, IMODE=1) ----------------
-   const double nxj = nxd / area;
-   const double nyj = nyd / area;
+   const double nxj = by_area.div(nxd);
+   const double nyj = by_area.div(nyd);
    const double uconlj = ul * nxj + vl * nyj;
    const double uconrj = ur * nxj + vr * nyj;
    const double uconbarj = ubar * nxj + vbar * nyj;
@@ -118,45 +127,45 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
 
    // derivative vectors, kept components {rho, rho u, rho v, E}
    // left (jacobianRoe.cpp:209-250)
-   const double du0l = -ul / rol;
-   const double irl = 1.0 / rol;
-   const double dv0l = -vl / rol;
+   const double du0l = by_rol.div(-ul);
+   const double irl = by_rol.div(1.0);
+   const double dv0l = by_rol.div(-vl);
    const double dp0l = 0.5 * gm1 * (ul * ul + vl * vl);
    const double dp1l = -gm1 * ul;
    const double dp2l = -gm1 * vl;
-   const double dc0l = -uconlj / rol;
-   const double dc1l = nxj / rol;
-   const double dc2l = nyj / rol;
+   const double dc0l = by_rol.div(-uconlj);
+   const double dc1l = by_rol.div(nxj);
+   const double dc2l = by_rol.div(nyj);
    // right (jacobianRoe.cpp:257-296)
-   const double du0r = -ur / ror;
-   const double irr = 1.0 / ror;
-   const double dv0r = -vr / ror;
+   const double du0r = by_ror.div(-ur);
+   const double irr = by_ror.div(1.0);
+   const double dv0r = by_ror.div(-vr);
    const double dp0r = 0.5 * gm1 * (ur * ur + vr * vr);
    const double dp1r = -gm1 * ur;
    const double dp2r = -gm1 * vr;
-   const double dc0r = -uconrj / ror;
-   const double dc1r = nxj / ror;
-   const double dc2r = nyj / ror;
+   const double dc0r = by_ror.div(-uconrj);
+   const double dc1r = by_ror.div(nxj);
+   const double dc2r = by_ror.div(nyj);
 
    // frozen-eigenvalue linearisation of del1/del2 (jacobianRoe.cpp:323-334)
    const double mt1 = -t1;
    double D1l[4], D2l[4], D1r[4], D2r[4];
-   D1l[0] = mt1 * dp0l / cbar / cbar - t2rb * dc0l / cbar;
-   D1l[1] = mt1 * dp1l / cbar / cbar - t2rb * dc1l / cbar;
-   D1l[2] = mt1 * dp2l / cbar / cbar - t2rb * dc2l / cbar;
-   D1l[3] = mt1 * gm1 / cbar / cbar;
-   D2l[0] = mt1 * dc0l * robar - t2 * dp0l / cbar;
-   D2l[1] = mt1 * dc1l * robar - t2 * dp1l / cbar;
-   D2l[2] = mt1 * dc2l * robar - t2 * dp2l / cbar;
-   D2l[3] = -(t2 * gm1 / cbar);
-   D1r[0] = t1 * dp0r / cbar / cbar + t2rb * dc0r / cbar;
-   D1r[1] = t1 * dp1r / cbar / cbar + t2rb * dc1r / cbar;
-   D1r[2] = t1 * dp2r / cbar / cbar + t2rb * dc2r / cbar;
-   D1r[3] = t1 * gm1 / cbar / cbar;
-   D2r[0] = t1 * dc0r * robar + t2 * dp0r / cbar;
-   D2r[1] = t1 * dc1r * robar + t2 * dp1r / cbar;
-   D2r[2] = t1 * dc2r * robar + t2 * dp2r / cbar;
-   D2r[3] = t2 * gm1 / cbar;
+   D1l[0] = by_c.div(by_c.div(mt1 * dp0l)) - by_c.div(t2rb * dc0l);
+   D1l[1] = by_c.div(by_c.div(mt1 * dp1l)) - by_c.div(t2rb * dc1l);
+   D1l[2] = by_c.div(by_c.div(mt1 * dp2l)) - by_c.div(t2rb * dc2l);
+   D1l[3] = by_c.div(by_c.div(mt1 * gm1));
+   D2l[0] = mt1 * dc0l * robar - by_c.div(t2 * dp0l);
+   D2l[1] = mt1 * dc1l * robar - by_c.div(t2 * dp1l);
+   D2l[2] = mt1 * dc2l * robar - by_c.div(t2 * dp2l);
+   D2l[3] = -by_c.div(t2 * gm1);
+   D1r[0] = by_c.div(by_c.div(t1 * dp0r)) + by_c.div(t2rb * dc0r);
+   D1r[1] = by_c.div(by_c.div(t1 * dp1r)) + by_c.div(t2rb * dc1r);
+   D1r[2] = by_c.div(by_c.div(t1 * dp2r)) + by_c.div(t2rb * dc2r);
+   D1r[3] = by_c.div(by_c.div(t1 * gm1));
+   D2r[0] = t1 * dc0r * robar + by_c.div(t2 * dp0r);
+   D2r[1] = t1 * dc1r * robar + by_c.div(t2 * dp1r);
+   D2r[2] = t1 * dc2r * robar + by_c.div(t2 * dp2r);
+   D2r[3] = by_c.div(t2 * gm1);
 
    // native flux Jacobians (jacobianRoe.cpp:573-605), kept rows/columns
    const double el = ql[3] + pl, er = qr[3] + pr;

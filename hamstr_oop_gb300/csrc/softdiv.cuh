@@ -1,0 +1,187 @@
+// ##################################################################
+//
+// softdiv.cuh -- correctly rounded FP64 division on the integer pipes
+//
+// GB300 issues one FP64 warp instruction per ~70-80 cycles per SM
+// sub-partition, and an IEEE division takes several of them; the
+// integer units sit idle in the FP64-bound kernels.  These functions
+// divide binary64 numbers with integer arithmetic only (plus one FP32
+// division for a seed), giving the round-to-nearest-even quotient, i.e.
+// exactly what the `/` operator gives, for normal operands.  Anything
+// else (zero, subnormal, infinite or NaN divisor; infinite or NaN
+// dividend; subnormal quotient) falls back to `/`.
+//
+// Method (Moller & Granlund, "Improved division by invariant integers",
+// IEEE Trans. Computers 60(2), 2011): the divisor's 53-bit significand,
+// shifted to a 64-bit word d, gets the reciprocal v = floor((2^128-1)/d)
+// - 2^64 (their Algorithm 2); a 128-by-64-bit division with that
+// reciprocal (their Algorithm 4) then yields the exact integer quotient
+// and remainder of the dividend's significand scaled by 2^54 or 2^55,
+// from which the rounded significand follows.  One reciprocal serves
+// every division by the same divisor.
+// ##################################################################
+#ifndef HAMSTR_GPU_SOFTDIV_CUH
+#define HAMSTR_GPU_SOFTDIV_CUH
+
+#include <cstdint>
+#include <cstring>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
+namespace hamstr {
+namespace sd {
+
+__host__ __device__ __forceinline__ uint64_t mulhi(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+   return __umul64hi(a, b);
+#else
+   return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint64_t bits(double x)
+{
+#ifdef __CUDA_ARCH__
+   return (uint64_t)__double_as_longlong(x);
+#else
+   uint64_t u;
+   std::memcpy(&u, &x, 8);
+   return u;
+#endif
+}
+
+__host__ __device__ __forceinline__ double from_bits(uint64_t u)
+{
+#ifdef __CUDA_ARCH__
+   return __longlong_as_double((long long)u);
+#else
+   double x;
+   std::memcpy(&x, &u, 8);
+   return x;
+#endif
+}
+
+// v = floor((2^128 - 1) / d) - 2^64 for 2^63 <= d < 2^64 (Algorithm 2 of
+// Moller & Granlund; v0 = floor((2^19 - 3*2^8) / d9) from a correctly
+// rounded FP32 division: the true quotient is never within 1/d9 > 2^-13
+// below an integer, so the floor of the rounded quotient is exact)
+__host__ __device__ __forceinline__ uint64_t reciprocal_word(uint64_t d)
+{
+   const uint64_t d0 = d & 1;
+   const uint64_t d9 = d >> 55;
+   const uint64_t d40 = (d >> 24) + 1;
+   const uint64_t d63 = (d >> 1) + d0;
+#ifdef __CUDA_ARCH__
+   const uint64_t v0 = (uint64_t)__float2uint_rz(__fdiv_rn(523520.0f, (float)(uint32_t)d9));
+#else
+   const uint64_t v0 = (uint64_t)(523520u / (uint32_t)d9);
+#endif
+   const uint64_t v1 = (v0 << 11) - ((v0 * v0 * d40) >> 40) - 1;
+   const uint64_t v2 = (v1 << 13) + ((v1 * ((1ull << 60) - v1 * d40)) >> 47);
+   const uint64_t e = ((v2 >> 1) & (0 - d0)) - v2 * d63;
+   const uint64_t v3 = (mulhi(v2, e) >> 1) + (v2 << 31);
+   // v4 = v3 - floor((v3 + 2^64 + 1) d / 2^64)
+   const uint64_t lo = v3 * d, hi = mulhi(v3, d);
+   const uint64_t lo2 = lo + d;
+   const uint64_t hi2 = hi + d + (lo2 < lo ? 1 : 0);
+   return v3 - hi2;
+}
+
+// exact floor((u1 * 2^64 + u0) / d) and remainder, u1 < d, v = reciprocal_word(d)
+// (Algorithm 4 of Moller & Granlund)
+__host__ __device__ __forceinline__ uint64_t div_2by1(uint64_t u1, uint64_t u0, uint64_t d, uint64_t v, uint64_t& r)
+{
+   uint64_t q0 = v * u1;
+   uint64_t q1 = mulhi(v, u1);
+   const uint64_t t = q0 + u0;
+   q1 = q1 + u1 + (t < q0 ? 1 : 0);
+   q0 = t;
+   q1 = q1 + 1;
+   r = u0 - q1 * d;
+   if (r > q0) {
+      q1 = q1 - 1;
+      r = r + d;
+   }
+   if (r >= d) {
+      q1 = q1 + 1;
+      r = r - d;
+   }
+   return q1;
+}
+
+// a divisor prepared once for several divisions
+struct Divisor {
+   double b;
+   uint64_t d, v;    // significand << 11, its reciprocal word
+   int eb;           // biased exponent
+   uint64_t sign;
+   bool ok;          // normal and finite: the integer path applies
+};
+
+__host__ __device__ __forceinline__ Divisor divisor(double b)
+{
+   Divisor D;
+   const uint64_t B = bits(b);
+   D.b = b;
+   D.eb = (int)((B >> 52) & 0x7FF);
+   D.sign = B & 0x8000000000000000ull;
+   D.ok = D.eb != 0 && D.eb != 0x7FF;
+   D.d = ((B & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) << 11;
+   D.v = D.ok ? reciprocal_word(D.d) : 0;
+   return D;
+}
+
+// a / D.b rounded to nearest even, equal to the `/` operator
+__host__ __device__ __forceinline__ double div(double a, const Divisor& D)
+{
+   const uint64_t A = bits(a);
+   const int ea = (int)((A >> 52) & 0x7FF);
+   if (!D.ok || ea == 0x7FF) return a / D.b;
+   const uint64_t sign = (A & 0x8000000000000000ull) ^ D.sign;
+   if ((A & 0x7FFFFFFFFFFFFFFFull) == 0) return from_bits(sign);   // +-0 / normal
+   if (ea == 0) return a / D.b;                                     // subnormal dividend
+   const uint64_t ma = (A & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+   const uint64_t mb = D.d >> 11;
+   // quotient significand in [1, 2): scale by 2^54 (ma >= mb) or 2^55
+   const int s = ma < mb ? 1 : 0;
+   const int e = ea - D.eb + 1023 - s;
+   if (e <= 0) return a / D.b;                                      // subnormal or zero quotient
+   uint64_t r;
+   // floor(ma * 2^(54+s) / mb) = floor(ma * 2^(65+s) / d), numerator (ma << (1+s)) * 2^64
+   const uint64_t q = div_2by1(ma << (1 + s), 0, D.d, D.v, r);    // in [2^54, 2^55)
+   uint64_t m = q >> 2;
+   const uint64_t g = (q >> 1) & 1, low = (q & 1) | (r != 0 ? 1 : 0);
+   if (g && (low || (m & 1))) m = m + 1;                            // round to nearest even
+   // m in [2^52, 2^53]; 2^53 carries into the exponent (and to infinity past 2046)
+   const uint64_t out = ((uint64_t)e << 52) + m - 0x10000000000000ull;
+   if (e >= 0x7FF || (out >> 52) >= 0x7FF) return from_bits(sign | 0x7FF0000000000000ull);
+   return from_bits(sign | out);
+}
+
+__host__ __device__ __forceinline__ double div(double a, double b) { return div(a, divisor(b)); }
+
+}  // namespace sd
+
+// Division by one divisor, possibly several times: in FP64 the correctly
+// rounded integer-pipe division above (identical results to `/`, off the
+// FP64 pipe the FP64 kernels are bound by); in FP32 the operator.
+template <typename T>
+struct Dv {
+   T b;
+   __device__ __forceinline__ explicit Dv(T b_) : b(b_) {}
+   __device__ __forceinline__ T div(T a) const { return a / b; }
+};
+template <>
+struct Dv<double> {
+   sd::Divisor D;
+   __device__ __forceinline__ explicit Dv(double b) : D(sd::divisor(b)) {}
+   __device__ __forceinline__ double div(double a) const { return sd::div(a, D); }
+};
+
+}  // namespace hamstr
+#endif

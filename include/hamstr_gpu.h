@@ -233,6 +233,11 @@ int hamstr_mlp_grad(hamstr_mlp* h, const float* features, const float* targets, 
 int hamstr_mlp_train_step(hamstr_mlp* h, const float* features, const float* targets, long long n_all, int batch,
                           unsigned long long seed, unsigned long long step, float lr, double* loss);
 
+/* Self-test hook: soft[i] = the integer-pipe division the FP64 kernels use
+ * (hamstr_oop_gb300/csrc/softdiv.cuh), hard[i] = the hardware a[i]/b[i],
+ * on device arrays of n doubles.  Tests compare them bit for bit. */
+int hamstr_check_softdiv(const double* a, const double* b, double* soft, double* hard, int n, void* stream);
+
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up
  * from an impulsive start.  HAMSTR_GPU_ERR_ARG unless cfl > 0. */

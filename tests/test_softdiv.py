@@ -1,0 +1,98 @@
+"""Integer-pipe FP64 division (csrc/softdiv.cuh) against IEEE division.
+
+The FP64 kernels divide on the integer units (Moller & Granlund's division
+by a precomputed reciprocal) to relieve the FP64 pipe; every quotient must
+equal the `/` operator's bit for bit.  The CPU test compiles the same
+header with the host compiler (whose division is IEEE) and checks 60 M
+quotients; the GPU test checks the device build against the device's own
+division."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "hamstr_oop_gb300", "csrc")
+
+PROGRAM = r"""
+#include "softdiv.cuh"
+#include <cstdio>
+#include <random>
+using namespace hamstr::sd;
+int main() {
+   std::mt19937_64 rng(1);
+   long bad = 0, n = 0;
+   for (long i = 0; i < 4000000; i++) {
+      uint64_t d = rng() | 0x8000000000000000ull;
+      if (i < 1000) d = 0x8000000000000000ull + i;
+      if (i >= 1000 && i < 2000) d = 0xFFFFFFFFFFFFFFFFull - (i - 1000);
+      unsigned __int128 q = (~(unsigned __int128)0) / d;
+      if ((q >> 64) != 1 || (uint64_t)q != reciprocal_word(d)) bad++;
+   }
+   auto rnd = [&](int emin, int emax) {
+      uint64_t m = rng() & 0xFFFFFFFFFFFFFull;
+      int e = emin + (int)(rng() % (uint64_t)(emax - emin + 1));
+      uint64_t s = rng() & 0x8000000000000000ull, k = rng() % 16;
+      if (k == 0) m = 0;
+      if (k == 1) m = 0xFFFFFFFFFFFFFull;
+      if (k == 2) m = rng() & 0xFFull;
+      if (k == 3) m = 0xFFFFFFFFFFFFFull - (rng() & 0xFF);
+      return from_bits(s | ((uint64_t)e << 52) | m);
+   };
+   for (long i = 0; i < 20000000; i++) {
+      double a, b;
+      if (i % 3 == 0) { a = rnd(1000, 1046); b = rnd(1000, 1046); }
+      else if (i % 3 == 1) { a = rnd(1, 2046); b = rnd(1, 2046); }
+      else { a = rnd(1020, 1026); b = a * (1.0 + 1e-15 * (double)(int)(rng() % 2001 - 1000)); }
+      if (i % 97 == 0) a = 0.0;
+      if (i % 101 == 0) b = rnd(0, 0);
+      double w = a / b, g = div(a, b);
+      n++;
+      if (bits(w) != bits(g) && !(w != w && g != g)) bad++;
+   }
+   printf("%ld %ld\n", bad, n);
+   return bad != 0;
+}
+"""
+
+
+def test_softdiv_matches_ieee_division_on_the_host(tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text(PROGRAM)
+    exe = tmp_path / "t"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    bad, n = (int(x) for x in out.stdout.split())
+    assert out.returncode == 0 and bad == 0 and n == 20000000
+
+
+@pytest.mark.gpu
+def test_softdiv_matches_the_device_division(native_lib):
+    import ctypes
+    import torch
+    rng = np.random.default_rng(3)
+    n = 4_000_000
+    m = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    e = rng.integers(1, 2047, n, dtype=np.uint64)
+    s = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    a = (s | (e << np.uint64(52)) | m).view(np.float64)
+    m2 = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    e2 = rng.integers(960, 1090, n, dtype=np.uint64)
+    b = ((e2 << np.uint64(52)) | m2).view(np.float64)
+    a[::7] = b[::7] * (1.0 + 1e-16 * rng.integers(-50, 50, a[::7].shape))   # near-unit quotients
+    a[::11] = 0.0
+    A, B = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    soft, hard = torch.empty_like(A), torch.empty_like(A)
+    fn = native_lib.hamstr_check_softdiv
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_void_p]
+    assert fn(A.data_ptr(), B.data_ptr(), soft.data_ptr(), hard.data_ptr(), n, None) == 0
+    torch.cuda.synchronize()
+    sb = soft.cpu().numpy().view(np.uint64)
+    hb = hard.cpu().numpy().view(np.uint64)
+    nan = np.isnan(hard.cpu().numpy()) & np.isnan(soft.cpu().numpy())
+    assert np.sum((sb != hb) & ~nan) == 0
+    # and the host's IEEE division agrees too
+    assert np.array_equal(hb, (a / b).view(np.uint64)) or np.sum(hb != (a / b).view(np.uint64)) == 0
