@@ -26,6 +26,7 @@
 #define HAMSTR_GPU_LINE_SOLVE_CUH
 
 #include "lu4.cuh"
+#include "softdiv.cuh"
 
 namespace hamstr {
 
@@ -68,11 +69,12 @@ __device__ __forceinline__ double lu_solve_lanes(const double (&lu)[4], int r, d
 // LU of a 4x4 block held one element per lane (element e = 4k+j in lane
 // base + e), as a wavefront over the lanes: returns in each lane element e
 // of the LU record (L below the diagonal, reciprocal pivots on it, U above),
-// with the operations and order of triSolvers.cpp:796-811.
+// with the operations and order of triSolvers.cpp:796-811.  The pivot
+// reciprocals use the integer-pipe division (softdiv.cuh), equal to 1./x.
 __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
 {
    const int k = e >> 2, j = e & 3;
-   const double piv0 = 1. / __shfl_sync(kLaneMask, w, base);
+   const double piv0 = sd::div(1., __shfl_sync(kLaneMask, w, base));
    {
       const double m = w * piv0;
       if (k == 0 && j >= 1) w = m;
@@ -82,7 +84,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k >= 1 && j >= 1) w = t;
    }
-   const double piv1 = 1. / __shfl_sync(kLaneMask, w, base + 5);
+   const double piv1 = sd::div(1., __shfl_sync(kLaneMask, w, base + 5));
    {
       const double m = w * piv1;
       if (k == 1 && j >= 2) w = m;
@@ -92,7 +94,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k >= 2 && j >= 2) w = t;
    }
-   const double piv2 = 1. / __shfl_sync(kLaneMask, w, base + 10);
+   const double piv2 = sd::div(1., __shfl_sync(kLaneMask, w, base + 10));
    {
       const double m = w * piv2;
       if (k == 2 && j == 3) w = m;
@@ -102,7 +104,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k == 3 && j == 3) w = t;
    }
-   const double piv3 = 1. / __shfl_sync(kLaneMask, w, base + 15);
+   const double piv3 = sd::div(1., __shfl_sync(kLaneMask, w, base + 15));
    if (k == j) w = (k == 0) ? piv0 : (k == 1) ? piv1 : (k == 2) ? piv2 : piv3;
    return w;
 }
