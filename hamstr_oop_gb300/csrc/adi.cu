@@ -77,16 +77,18 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
 }
 
 // block-Thomas factorisation of chain ich (its assembled rows in blk)
+template <bool SD>
 __device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int lane)
 {
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const double* blk = d.blk + 48 * (size_t)row0;
-   factor_line(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
+   factor_line<SD>(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
                per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane);
 }
 
 // persistent warps, one per SM sub-partition, each with a job list
+template <bool SD>
 __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
 {
    if (halted(d)) return;
@@ -95,7 +97,7 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    const int g = d.sched_warp0[0] + w;
    for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
       const int ich = d.sched_jobs[job];
-      if (!frozen_chain(d, ich)) factor_chain(d, ich, threadIdx.x & 31);
+      if (!frozen_chain(d, ich)) factor_chain<SD>(d, ich, threadIdx.x & 31);
    }
 }
 
@@ -149,7 +151,10 @@ int adi_configure(int max_dynamic_smem)
 {
    const int want = max_dynamic_smem >= kExclusiveSmem ? kExclusiveSmem : 0;
    if (want) {
-      if (cudaFuncSetAttribute(adi_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess)
+      if (cudaFuncSetAttribute(adi_factor_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(adi_factor_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+              cudaSuccess)
          return 0;
       if (cudaFuncSetAttribute(adi_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, want) != cudaSuccess)
          return 0;
@@ -166,7 +171,8 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
 {
    const int wpb = d.adi_wpb;
-   adi_factor_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
+   if (d.piv_soft) adi_factor_kernel<true><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
+   else adi_factor_kernel<false><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
 }
 
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st)

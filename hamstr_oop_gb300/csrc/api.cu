@@ -218,8 +218,10 @@ struct hamstr_gpu {
    }
 
    // launch shapes; a new warps-per-SM count rebuilds the line schedules
-   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused)
+   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft)
    {
+      d.face_soft = face_soft;
+      d.piv_soft = piv_soft;
       if (!mx_fused && d.ff32) {
          const int st = ensure_blk32();
          if (st) return st;
@@ -493,8 +495,11 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_block = 256;
       d.adi_wpb = 4;
       d.mx_block = 64;
-      // FP32 assembly inside the factorisation pays off on long chains
+      // FP32 assembly inside the factorisation pays off on long chains, as
+      // do the hardware pivot divisions (their latency is shorter per row)
       d.mx_fused = (P.nChain > 0 && P.nRow >= 16 * P.nChain) ? 1 : 0;
+      d.face_soft = 1;
+      d.piv_soft = d.mx_fused ? 0 : 1;
       g->nsm = nsm;
       g->sched = build_schedule(P, d.adi_wpb * nsm);
    }
@@ -997,16 +1002,18 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft; float ms; };
    std::vector<Cand> cands;
-   for (int fb : {128, 256}) {
-      if (g->mixed) {
-         for (int fused : {0, 1})
-            for (int mb : {32, 64, 128}) cands.push_back({fb, d.adi_wpb, mb, fused, 0.f});
-      } else {
-         for (int w : {4, 8}) cands.push_back({fb, w, d.mx_block, d.mx_fused, 0.f});
+   for (int fb : {128, 256})
+      for (int fsoft : {0, 1}) {
+         if (g->mixed) {
+            for (int fused : {0, 1})
+               for (int mb : {32, 64, 128}) cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, 0.f});
+         } else {
+            for (int w : {4, 8})
+               for (int psoft : {0, 1}) cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, 0.f});
+         }
       }
-   }
    // the tuning steps advance the state: keep q and put it back afterwards
    double* qsave = nullptr;
    const size_t qbytes = 4 * (size_t)d.nCell * sizeof(double);
@@ -1017,7 +1024,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1038,7 +1045,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused);
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1046,14 +1053,16 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          char buf[160];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                       "\"ms\": %.4f}",
-                       i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].ms);
+                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"ms\": %.4f}",
+                       i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
+                       cands[i].psoft, cands[i].ms);
          r += buf;
       }
       char buf[160];
       std::snprintf(buf, sizeof(buf),
-                    "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused);
+                    "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }

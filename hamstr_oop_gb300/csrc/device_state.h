@@ -82,6 +82,8 @@ struct DeviceState {
    int adi_wpb;            // warps per block (= per SM) of the persistent FP64 line kernels (4 or 8)
    int mx_block;           // threads per block of the FP32 thread-per-chain line kernels
    int mx_fused;           // 1: FP32 blocks assembled inside the factorisation; 0: mx_assemble first
+   int face_soft;          // 1: FP64 divisions of the face kernels on the integer pipes (softdiv.cuh)
+   int piv_soft;           // 1: the same for the LU pivots of the FP64 line factorisation
 
    // mixed-precision defect correction (FP64 residual, FP32 operator)
    float* ff32;            // [nSlot][32] FP32 face Jacobians

@@ -69,12 +69,14 @@ __device__ __forceinline__ double lu_solve_lanes(const double (&lu)[4], int r, d
 // LU of a 4x4 block held one element per lane (element e = 4k+j in lane
 // base + e), as a wavefront over the lanes: returns in each lane element e
 // of the LU record (L below the diagonal, reciprocal pivots on it, U above),
-// with the operations and order of triSolvers.cpp:796-811.  The pivot
-// reciprocals use the integer-pipe division (softdiv.cuh), equal to 1./x.
+// with the operations and order of triSolvers.cpp:796-811.  With SD the
+// pivot reciprocals use the integer-pipe division (softdiv.cuh), equal to
+// 1./x: shorter latency, off the FP64 pipe.
+template <bool SD>
 __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
 {
    const int k = e >> 2, j = e & 3;
-   const double piv0 = sd::div(1., __shfl_sync(kLaneMask, w, base));
+   const double piv0 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base)) : 1. / __shfl_sync(kLaneMask, w, base);
    {
       const double m = w * piv0;
       if (k == 0 && j >= 1) w = m;
@@ -84,7 +86,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k >= 1 && j >= 1) w = t;
    }
-   const double piv1 = sd::div(1., __shfl_sync(kLaneMask, w, base + 5));
+   const double piv1 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 5)) : 1. / __shfl_sync(kLaneMask, w, base + 5);
    {
       const double m = w * piv1;
       if (k == 1 && j >= 2) w = m;
@@ -94,7 +96,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k >= 2 && j >= 2) w = t;
    }
-   const double piv2 = sd::div(1., __shfl_sync(kLaneMask, w, base + 10));
+   const double piv2 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 10)) : 1. / __shfl_sync(kLaneMask, w, base + 10);
    {
       const double m = w * piv2;
       if (k == 2 && j == 3) w = m;
@@ -104,7 +106,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
       const double t = w - L * U;
       if (k == 3 && j == 3) w = t;
    }
-   const double piv3 = sd::div(1., __shfl_sync(kLaneMask, w, base + 15));
+   const double piv3 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 15)) : 1. / __shfl_sync(kLaneMask, w, base + 15);
    if (k == j) w = (k == 0) ? piv0 : (k == 1) ? piv1 : (k == 2) ? piv2 : piv3;
    return w;
 }
@@ -113,6 +115,7 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
 // A_i = Ab + i*stride, B_i = Bb + i*stride, C_i = Cb + i*stride (row-major
 // 4x4); writes the per-row records `fac` (kFacRec doubles per row) and,
 // periodic, the LU of the final last-row block into facN.
+template <bool SD = true>
 __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const double* __restrict__ Bb,
                                             const double* __restrict__ Cb, size_t stride, int N, bool per,
                                             double* __restrict__ fac, double* __restrict__ facN, int lane)
@@ -144,7 +147,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
          acc = A;
       }
       // LU of B'(i), computed by both halves on their own copy
-      const double w = lu_wavefront(__shfl_sync(kLaneMask, acc, e), 16 * h, e);
+      const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, acc, e), 16 * h, e);
       if (h == 0) rec[16 + e] = w;
       double lu[4];
 #pragma unroll
@@ -186,7 +189,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
       cN = __shfl_sync(kLaneMask, acc, e);
       Y = Yn;
    }
-   const double w = lu_wavefront(__shfl_sync(kLaneMask, bN, 16 + e), 16 * h, e);
+   const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, bN, 16 + e), 16 * h, e);
    if (h == 0) facN[e] = w;
 }
 

@@ -28,7 +28,7 @@ constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
 
 // ---------------- residual + FP32 Jacobian ----------------
-template <int ORDER>
+template <int ORDER, bool SD>
 __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,9 +36,9 @@ __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
-   face_states<ORDER>(d, sl.x, (sl.w & 1) != 0, L, R);
+   face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
    RoeOut o;
-   if (!roe_face<false>(nv.x, nv.y, L, R, d.fc.gamma, o, nullptr, nullptr)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
+   if (!roe_face<false, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, nullptr, nullptr)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
    st4(d.flux + 4 * (size_t)s, o.flux);
    d.spec[s] = o.spec;
    const float Lf[4] = {float(L[0]), float(L[1]), float(L[2]), float(L[3])};
@@ -519,17 +519,26 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 }  // namespace
 
+namespace {
+template <bool SD>
+void mx_rhs_face_go(const DeviceState& d, int b, int t, cudaStream_t st)
+{
+   switch (d.recon) {
+      case 1: mx_rhs_face_kernel<1, SD><<<b, t, 0, st>>>(d); break;
+      case 3: mx_rhs_face_kernel<3, SD><<<b, t, 0, st>>>(d); break;
+      case 5: mx_rhs_face_kernel<5, SD><<<b, t, 0, st>>>(d); break;
+      case 31: mx_rhs_face_kernel<31, SD><<<b, t, 0, st>>>(d); break;
+      default: mx_rhs_face_kernel<32, SD><<<b, t, 0, st>>>(d); break;
+   }
+}
+}  // namespace
+
 void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
 {
-   const int kThreads = d.face_block;
-   const int b = (d.nSlot + kThreads - 1) / kThreads;
-   switch (d.recon) {
-      case 1: mx_rhs_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
-      case 3: mx_rhs_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
-      case 5: mx_rhs_face_kernel<5><<<b, kThreads, 0, st>>>(d); break;
-      case 31: mx_rhs_face_kernel<31><<<b, kThreads, 0, st>>>(d); break;
-      default: mx_rhs_face_kernel<32><<<b, kThreads, 0, st>>>(d); break;
-   }
+   const int t = d.face_block;
+   const int b = (d.nSlot + t - 1) / t;
+   if (d.face_soft) mx_rhs_face_go<true>(d, b, t, st);
+   else mx_rhs_face_go<false>(d, b, t, st);
 }
 
 void launch_mx_assemble(const DeviceState& d, cudaStream_t st)

@@ -233,6 +233,7 @@ __device__ __forceinline__ void muscl_deriv2(T fm1, T f0, T fp1, T fp2, T dm1, T
 }
 
 // WENO5 (reconstruction.cpp:193-239); pow(x, 1) is x
+template <bool SD>
 __device__ __forceinline__ double weno5(double a, double b, double c, double d, double e)
 {
    const double epsw = 1e-15;
@@ -249,11 +250,11 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
    const double q30 = 2. * a - 7. * b + 11. * c;
    const double q31 = -b + 5. * c + 2. * d;
    const double q32 = 2. * c + 5. * d - e;
-   const double d01 = Dv<double>(dis1).div(dis0);
-   const double d02 = Dv<double>(dis2).div(dis0);
+   const double d01 = Dv<double, SD>(dis1).div(dis0);
+   const double d02 = Dv<double, SD>(dis2).div(dis0);
    const double a1ba0 = 6. * d01;
    const double a2ba0 = 3. * d02;
-   const double w0 = Dv<double>(1.0 + a1ba0 + a2ba0).div(1.0);
+   const double w0 = Dv<double, SD>(1.0 + a1ba0 + a2ba0).div(1.0);
    const double w1 = a1ba0 * w0;
    const double w2 = 1. - w0 - w1;
    return b2 * (w0 * q30 + w1 * q31 + w2 * q32);
@@ -261,7 +262,7 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
 
 // WENO_5 linearisation (reconstruction.cpp:358-462); the linear residual
 // passes eps = 1e-10 (computeLinearRHS.cpp:286,292)
-template <typename T>
+template <typename T, bool SD>
 __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, T c_d, T d_d, T e_d)
 {
    const T epsw = T(1e-10);
@@ -278,12 +279,12 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
    const T q30 = T(2.) * a - T(7.) * b + T(11.) * c;
    const T q31 = -b + T(5.) * c + T(2.) * d;
    const T q32 = T(2.) * c + T(5.) * d - e;
-   const Dv<T> r1(dis1), r2(dis2);
+   const Dv<T, SD> r1(dis1), r2(dis2);
    const T d01 = r1.div(dis0);
    const T d02 = r2.div(dis0);
    const T a1ba0 = T(6.) * d01;
    const T a2ba0 = T(3.) * d02;
-   const T w0 = Dv<T>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
+   const T w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
    const T w1 = a1ba0 * w0;
    const T w2 = T(1.) - w0 - w1;
    const T djm1_d = a_d - T(2.) * b_d + c_d;
@@ -306,7 +307,7 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
    const T dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
    const T dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
                                        + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
-   const Dv<T> rd(dw0_down * dw0_down);
+   const Dv<T, SD> rd(dw0_down * dw0_down);
    const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
    const T dw1_up_1 = T(6) * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
    const T dw1_up_2 = r1.div(T(6) * dw0_up_2) * beta0;
@@ -319,7 +320,7 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
 
 // reconstructed states at the two sides of a face slot, FP64
 // (computeRHS.cpp:266-304)
-template <int ORDER>
+template <int ORDER, bool SD = true>
 __device__ __forceinline__ void face_states(const DeviceState& d, int n, bool swap, double (&L)[4], double (&R)[4])
 {
    double qln[4], qrn1[4], dummy[4];
@@ -343,8 +344,8 @@ __device__ __forceinline__ void face_states(const DeviceState& d, int n, bool sw
       for (int j = 0; j < 6; j++) load_sten<double, false>(d, nullptr, n - 2 + j, f[j], dummy);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-         qln[k] = weno5(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k]);
-         qrn1[k] = weno5(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k]);
+         qln[k] = weno5<SD>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k]);
+         qrn1[k] = weno5<SD>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k]);
       }
    }
 #pragma unroll
@@ -355,7 +356,7 @@ __device__ __forceinline__ void face_states(const DeviceState& d, int n, bool sw
 }
 
 // linearised states (computeLinearRHS.cpp:281-315) in T, dq from dqv
-template <int ORDER, typename T>
+template <int ORDER, typename T, bool SD = true>
 __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __restrict__ dqv, int n, bool swap,
                                              T (&L)[4], T (&R)[4])
 {
@@ -383,9 +384,9 @@ __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __re
       for (int j = 0; j < 6; j++) load_sten<T, true>(d, dqv, n - 2 + j, f[j], df[j]);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-         qln[k] = weno5_deriv<T>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k], df[0][k], df[1][k], df[2][k],
+         qln[k] = weno5_deriv<T, SD>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k], df[0][k], df[1][k], df[2][k],
                                  df[3][k], df[4][k]);
-         qrn1[k] = weno5_deriv<T>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], df[5][k], df[4][k], df[3][k],
+         qrn1[k] = weno5_deriv<T, SD>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], df[5][k], df[4][k], df[3][k],
                                   df[2][k], df[1][k]);
       }
    }

@@ -33,7 +33,7 @@ namespace {
 
 constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
-template <int ORDER, bool JAC>
+template <int ORDER, bool JAC, bool SD>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -41,10 +41,10 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
-   face_states<ORDER>(d, sl.x, (sl.w & 1) != 0, L, R);
+   face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
    RoeOut o;
    double lm[16], rm[16];
-   if (!roe_face<JAC>(nv.x, nv.y, L, R, d.fc.gamma, o, lm, rm)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
+   if (!roe_face<JAC, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, lm, rm)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
    st4(d.flux + 4 * (size_t)s, o.flux);
    d.spec[s] = o.spec;
    if (JAC) {
@@ -56,14 +56,14 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    }
 }
 
-template <int ORDER>
+template <int ORDER, bool SD>
 __global__ void __launch_bounds__(kThreads) lin_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    double dL[4], dR[4];
-   face_dstates<ORDER, double>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
+   face_dstates<ORDER, double, SD>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
    const double* m = d.ff + 32 * (size_t)(sl.w >> 1);
    double g[4];
 #pragma unroll
@@ -283,22 +283,31 @@ inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
 
 }  // namespace
 
+namespace {
+template <bool SD>
+void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
+{
+   switch (d.recon * 2 + (jac ? 1 : 0)) {
+      case 2: rhs_face_kernel<1, false, SD><<<b, t, 0, st>>>(d); break;
+      case 3: rhs_face_kernel<1, true, SD><<<b, t, 0, st>>>(d); break;
+      case 6: rhs_face_kernel<3, false, SD><<<b, t, 0, st>>>(d); break;
+      case 7: rhs_face_kernel<3, true, SD><<<b, t, 0, st>>>(d); break;
+      case 10: rhs_face_kernel<5, false, SD><<<b, t, 0, st>>>(d); break;
+      case 11: rhs_face_kernel<5, true, SD><<<b, t, 0, st>>>(d); break;
+      case 62: rhs_face_kernel<31, false, SD><<<b, t, 0, st>>>(d); break;
+      case 63: rhs_face_kernel<31, true, SD><<<b, t, 0, st>>>(d); break;
+      case 64: rhs_face_kernel<32, false, SD><<<b, t, 0, st>>>(d); break;
+      default: rhs_face_kernel<32, true, SD><<<b, t, 0, st>>>(d); break;
+   }
+}
+}  // namespace
+
 void launch_rhs_face(const DeviceState& d, bool jac, cudaStream_t st)
 {
-   const int kThreads = d.face_block;
-   const int b = (d.nSlot + kThreads - 1) / kThreads;
-   switch (d.recon * 2 + (jac ? 1 : 0)) {
-      case 2: rhs_face_kernel<1, false><<<b, kThreads, 0, st>>>(d); break;
-      case 3: rhs_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
-      case 6: rhs_face_kernel<3, false><<<b, kThreads, 0, st>>>(d); break;
-      case 7: rhs_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;
-      case 10: rhs_face_kernel<5, false><<<b, kThreads, 0, st>>>(d); break;
-      case 11: rhs_face_kernel<5, true><<<b, kThreads, 0, st>>>(d); break;
-      case 62: rhs_face_kernel<31, false><<<b, kThreads, 0, st>>>(d); break;
-      case 63: rhs_face_kernel<31, true><<<b, kThreads, 0, st>>>(d); break;
-      case 64: rhs_face_kernel<32, false><<<b, kThreads, 0, st>>>(d); break;
-      default: rhs_face_kernel<32, true><<<b, kThreads, 0, st>>>(d); break;
-   }
+   const int t = d.face_block;
+   const int b = (d.nSlot + t - 1) / t;
+   if (d.face_soft) rhs_face_go<true>(d, jac, b, t, st);
+   else rhs_face_go<false>(d, jac, b, t, st);
 }
 
 void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
@@ -311,12 +320,16 @@ void launch_lin_face(const DeviceState& d, cudaStream_t st)
 {
    const int kThreads = d.face_block;
    const int b = (d.nSlot + kThreads - 1) / kThreads;
+   // only the WENO linearisation divides in FP64 here
    switch (d.recon) {
-      case 1: lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
-      case 3: lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;
-      case 5: lin_face_kernel<5><<<b, kThreads, 0, st>>>(d); break;
-      case 31: lin_face_kernel<31><<<b, kThreads, 0, st>>>(d); break;
-      default: lin_face_kernel<32><<<b, kThreads, 0, st>>>(d); break;
+      case 1: lin_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
+      case 3: lin_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;
+      case 5:
+         if (d.face_soft) lin_face_kernel<5, true><<<b, kThreads, 0, st>>>(d);
+         else lin_face_kernel<5, false><<<b, kThreads, 0, st>>>(d);
+         break;
+      case 31: lin_face_kernel<31, true><<<b, kThreads, 0, st>>>(d); break;
+      default: lin_face_kernel<32, true><<<b, kThreads, 0, st>>>(d); break;
    }
 }
 

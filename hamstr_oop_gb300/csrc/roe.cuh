@@ -36,26 +36,26 @@ struct RoeOut {
 
 // lm/rm receive the 4x4 left/right Jacobians (row-major) times the area.
 // Returns false when the spectral radius is NaN.
-template <bool JAC>
+template <bool JAC, bool SD = true>
 __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&ql)[4],
                                          const double (&qr)[4], double gam, RoeOut& o,
                                          double* __restrict__ lm, double* __restrict__ rm)
 {
    const double gm1 = gam - 1.0;
    const double area = sqrt(nxd * nxd + nyd * nyd);
-   const Dv<double> by_area(area);
+   const Dv<double, SD> by_area(area);
    const double invArea = by_area.div(1.);
    const double nx = nxd * invArea;
    const double ny = nyd * invArea;
 
    const double rol = ql[0];
-   const Dv<double> by_rol(rol);
+   const Dv<double, SD> by_rol(rol);
    const double ul = by_rol.div(ql[1]);
    const double vl = by_rol.div(ql[2]);
    const double pl = gm1 * (ql[3] - 0.5 * rol * (ul * ul + vl * vl));
    const double hl = by_rol.div(ql[3] + pl);
    const double ror = qr[0];
-   const Dv<double> by_ror(ror);
+   const Dv<double, SD> by_ror(ror);
    const double ur = by_ror.div(qr[1]);
    const double vr = by_ror.div(qr[2]);
    const double pr = gm1 * (qr[3] - 0.5 * ror * (ur * ur + vr * vr));
@@ -65,7 +65,7 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double uconl = ul * nx + vl * ny;
 
    const double fact = sqrt(by_rol.div(ror));
-   const Dv<double> by_1f(1.0 + fact);
+   const Dv<double, SD> by_1f(1.0 + fact);
    const double A = by_1f.div(1.0);
    const double B = by_1f.div(fact);
    const double robar = rol * fact;
@@ -74,7 +74,7 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double hbar = hl * A + hr * B;
    double cbar = gm1 * (hbar - 0.5 * (ubar * ubar + vbar * vbar));
    cbar = sqrt(cbar);
-   const Dv<double> by_c(cbar);
+   const Dv<double, SD> by_c(cbar);
    const double uconbar = ubar * nx + vbar * ny;
 
    {

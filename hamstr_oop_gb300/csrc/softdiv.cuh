@@ -167,17 +167,19 @@ __host__ __device__ __forceinline__ double div(double a, double b) { return div(
 
 }  // namespace sd
 
-// Division by one divisor, possibly several times: in FP64 the correctly
-// rounded integer-pipe division above (identical results to `/`, off the
-// FP64 pipe the FP64 kernels are bound by); in FP32 the operator.
-template <typename T>
+// Division by one divisor, possibly several times: in FP64 with SOFT the
+// correctly rounded integer-pipe division above (identical results to `/`,
+// off the FP64 pipe the FP64 kernels are bound by); otherwise the
+// operator.  Which is faster depends on the kernel and the mesh (the
+// autotuner picks).
+template <typename T, bool SOFT = true>
 struct Dv {
    T b;
    __device__ __forceinline__ explicit Dv(T b_) : b(b_) {}
    __device__ __forceinline__ T div(T a) const { return a / b; }
 };
 template <>
-struct Dv<double> {
+struct Dv<double, true> {
    sd::Divisor D;
    __device__ __forceinline__ explicit Dv(double b) : D(sd::divisor(b)) {}
    __device__ __forceinline__ double div(double a) const { return sd::div(a, D); }

@@ -193,8 +193,9 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
  * or two per sub-partition, schedules rebuilt longest-chain-first); FP32
  * line kernels 32..128 threads per block, with the blocks assembled by a
- * separate coalesced kernel or inside the factorisation -- and keeps the
- * fastest.  The
+ * separate coalesced kernel or inside the factorisation; FP64 divisions of
+ * the face kernels and of the LU pivots on the FP64 pipe or on the integer
+ * pipes (bit-identical) -- and keeps the fastest.  The
  * state is restored afterwards; results do not depend on the shape.
  * report (may be NULL) receives a JSON summary of the timings. */
 int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);

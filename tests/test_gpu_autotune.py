@@ -10,7 +10,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     case = make_case(32, 8, order=3, CFL=10.0, msweep=2)
     g = native.GpuSolver(native.Case(case))
     rep = g.autotune(reps=2)
-    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 4
+    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 16
     assert all(c["ms"] > 0 for c in rep["candidates"])
     o = oracle_lib.OracleCase(case, "port")
     for it in range(5):
@@ -43,7 +43,7 @@ def test_autotune_mixed_restores_state_and_results(make_case, native_lib):
     a.set_precision(True)
     b.set_precision(True)
     rep = b.autotune(reps=2)
-    assert rep["precision"] == "mixed" and len(rep["candidates"]) == 12
+    assert rep["precision"] == "mixed" and len(rep["candidates"]) == 24
     assert np.array_equal(a.get("q"), b.get("q"))        # state put back
     a.march(6, 0.0)
     b.march(6, 0.0)
