@@ -71,7 +71,7 @@ WORKLOADS.update({k: dict(v, batch=True) for k, v in BATCH.items()})
 # The learned warm start: train on solver-generated converged states, then
 # solve held-out conditions from the network's guess and from freestream.
 WORKLOADS["c5"] = dict(warm=True, ni=256, nj=64, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2,
-                       Mach=0.5, alpha=1.25, ramp=(), train=2048, test=256, tol=1e-10, cap=8000, epochs=30,
+                       Mach=0.5, alpha=1.25, ramp=(), train=2048, test=256, tol=1e-10, cap=15000, epochs=30,
                        batch=16384, lr=2e-3,
                        name="naca0012_256x64_order1_cfl10_warmstart_mlp5-256x3-4_train2048_test256")
 
