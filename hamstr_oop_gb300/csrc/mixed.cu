@@ -339,6 +339,11 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
 
+// One sweep's solve of one chain per thread.  The recurrence only carries
+// the 4-vector x in registers; everything a row needs (its factor record,
+// its right-hand side, the cell it writes) is loaded one row ahead, so the
+// loads overlap the previous row's arithmetic.  Solutions go straight to
+// r32 (each cell is written once per chain; chains of a wave share no cell).
 __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -349,28 +354,48 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    const bool per = d.chain_periodic[ich] != 0;
    const float* fac = d.fac32 + (size_t)kRec * row0;
    float* fs = d.fsc32 + 4 * (size_t)row0;
+   const int* fcell = d.row_fcell + row0;
+   const int* scell = d.row_scell + row0;
    // forward: f(i) = LU^{-1}(F(i) - A(i) f(i-1)), F(i) = r[fcell]
    float xp[4] = {0.f, 0.f, 0.f, 0.f};
-   int fc = d.row_fcell[row0];
+   float a[16], xr[4] = {0.f, 0.f, 0.f, 0.f};
+   LUf u;
+   {
+      const int fc = fcell[0];
+      if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, xr);
+      u = luf_load(fac + 16);
+#pragma unroll
+      for (int m = 0; m < 16; m++) a[m] = 0.f;
+   }
    for (int i = 0; i < N; i++) {
-      const float* rec = fac + (size_t)kRec * i;
-      const int fcn = (i + 1 < N) ? d.row_fcell[row0 + i + 1] : -1;
-      float x[4] = {0.f, 0.f, 0.f, 0.f};
-      if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, x);
+      // next row's record and right-hand side, in flight during this row
+      float an[16], xrn[4] = {0.f, 0.f, 0.f, 0.f};
+      LUf un;
+      if (i + 1 < N) {
+         const float* rn = fac + (size_t)kRec * (i + 1);
+         const int fcn = fcell[i + 1];
+         if (fcn >= 0) ld4(d.r32 + 4 * (size_t)fcn, xrn);
+         ld16f(rn, an);
+         un = luf_load(rn + 16);
+      }
+      float x[4] = {xr[0], xr[1], xr[2], xr[3]};
       if (i > 0) {
-         float a[16];
-         ld16f(rec, a);
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
             for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-a[4 * k + j], xp[j], x[k]);
       }
-      const LUf u = luf_load(rec + 16);
       luf_solve(u, x[0], x[1], x[2], x[3]);
       st4(fs + 4 * i, x);
 #pragma unroll
       for (int k = 0; k < 4; k++) xp[k] = x[k];
-      fc = fcn;
+      if (i + 1 < N) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) a[m] = an[m];
+#pragma unroll
+         for (int k = 0; k < 4; k++) xr[k] = xrn[k];
+         u = un;
+      }
    }
    float xn[4];
    if (per) {
@@ -384,48 +409,63 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
 #pragma unroll
             for (int j = 0; j < 4; j++) fN[k] = __fmaf_rn(-c[4 * k + j], f[j], fN[k]);
       }
-      const LUf u = luf_load(d.facN32 + 16 * d.chain_facN[ich]);
-      luf_solve(u, fN[0], fN[1], fN[2], fN[3]);
-      st4(fs + 4 * (N - 1), fN);
+      const LUf uN = luf_load(d.facN32 + 16 * d.chain_facN[ich]);
+      luf_solve(uN, fN[0], fN[1], fN[2], fN[3]);
+      st4(d.r32 + 4 * (size_t)scell[N - 1], fN);
 #pragma unroll
       for (int k = 0; k < 4; k++) xn[k] = fN[k];
       for (int i = N - 2; i >= 0; i--) {
          const float* rec = fac + (size_t)kRec * i;
-         float c[16], a[16], x[4];
+         float c[16], aa[16], x[4];
          ld16f(rec + 32, c);
-         ld16f(rec + 48, a);
+         ld16f(rec + 48, aa);
          ld4(fs + 4 * i, x);
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-               const float s = (i == N - 2) ? c[4 * k + j] * xn[j] : __fmaf_rn(a[4 * k + j], fN[j], c[4 * k + j] * xn[j]);
-               x[k] -= s;
+               const float sv = (i == N - 2) ? c[4 * k + j] * xn[j] : __fmaf_rn(aa[4 * k + j], fN[j], c[4 * k + j] * xn[j]);
+               x[k] -= sv;
             }
-         st4(fs + 4 * i, x);
+         st4(d.r32 + 4 * (size_t)scell[i], x);
 #pragma unroll
          for (int k = 0; k < 4; k++) xn[k] = x[k];
       }
    } else {
 #pragma unroll
       for (int k = 0; k < 4; k++) xn[k] = xp[k];
+      st4(d.r32 + 4 * (size_t)scell[N - 1], xn);
+      // back substitution, row i-1's factor and f prefetched
+      float c[16], x[4];
+      int sc = 0;
+      if (N >= 2) {
+         ld16f(fac + (size_t)kRec * (N - 2) + 32, c);
+         ld4(fs + 4 * (N - 2), x);
+         sc = scell[N - 2];
+      }
       for (int i = N - 2; i >= 0; i--) {
-         float c[16], x[4];
-         ld16f(fac + (size_t)kRec * i + 32, c);
-         ld4(fs + 4 * i, x);
+         float cn[16], xnx[4];
+         int scn = 0;
+         if (i >= 1) {
+            ld16f(fac + (size_t)kRec * (i - 1) + 32, cn);
+            ld4(fs + 4 * (i - 1), xnx);
+            scn = scell[i - 1];
+         }
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
             for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-c[4 * k + j], xn[j], x[k]);
-         st4(fs + 4 * i, x);
+         st4(d.r32 + 4 * (size_t)sc, x);
 #pragma unroll
          for (int k = 0; k < 4; k++) xn[k] = x[k];
+         if (i >= 1) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) c[m] = cn[m];
+#pragma unroll
+            for (int k = 0; k < 4; k++) x[k] = xnx[k];
+            sc = scn;
+         }
       }
-   }
-   for (int r = 0; r < N; r++) {
-      float v[4];
-      ld4(fs + 4 * r, v);
-      st4(d.r32 + 4 * (size_t)d.row_scell[row0 + r], v);
    }
 }
 
