@@ -16,7 +16,8 @@
 // work is packed into lanes: lane = 16*h + 4*k + j holds element (k,j) of
 // a 4x4 block; in periodic chains half h=0 carries the C' recurrence and
 // half h=1 the fill-in column a' (triSolvers.cpp:877-891), which follow
-// the same instruction sequence.
+// the same instruction sequence.  Open chains need one half only, so the
+// schedule may pair them: two open chains per warp, one per half.
 //
 // Per-row factor record (80 doubles):
 //   [ 0..15] A_i scaled      (f update in the forward sweep)
@@ -87,6 +88,21 @@ __device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int 
                per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane);
 }
 
+// rows of chain ich for this half-warp's work: 0 once its instance is frozen
+__device__ __forceinline__ int live_rows(const DeviceState& d, int ich)
+{
+   return frozen_chain(d, ich) ? 0 : d.chain_nrows[ich];
+}
+
+// two open chains, one per half-warp (line_solve.cuh factor_line_pair)
+template <bool SD>
+__device__ __forceinline__ void factor_pair(const DeviceState& d, int ia, int ib, int lane)
+{
+   const int ich = (lane >> 4) ? ib : ia;
+   const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
+   factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
+}
+
 // persistent warps, one per SM sub-partition, each with a job list
 template <bool SD>
 __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
@@ -95,9 +111,15 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[0] + w;
-   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
+   const int end = d.sched_warp_ptr[g + 1];
+   for (int job = d.sched_warp_ptr[g]; job < end; job++) {
       const int ich = d.sched_jobs[job];
-      if (!frozen_chain(d, ich)) factor_chain<SD>(d, ich, threadIdx.x & 31);
+      if (ich & kPairJob) {
+         factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], threadIdx.x & 31);
+         job++;
+      } else if (!frozen_chain(d, ich)) {
+         factor_chain<SD>(d, ich, threadIdx.x & 31);
+      }
    }
 }
 
@@ -127,15 +149,46 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
    }
 }
 
+// the same for two open chains, one per half-warp
+__device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib, int lane)
+{
+   const int ich = (lane >> 4) ? ib : ia, l16 = lane & 15;
+   const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
+   double* fs = d.fsc + 4 * (size_t)row0;
+   for (int r = l16; r < N; r += 16) {
+      const int fc = d.row_fcell[row0 + r];
+      double v[4] = {0.0, 0.0, 0.0, 0.0};
+      if (fc >= 0) ld4(d.r + 4 * (size_t)fc, v);
+      *reinterpret_cast<double2*>(fs + 4 * r) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
+   }
+   __syncwarp();
+   solve_line_pair(d.fac + (size_t)kFacRec * row0, N, fs, lane);
+   __syncwarp();
+   for (int r = l16; r < N; r += 16) {
+      const int sc = d.row_scell[row0 + r];
+      double v[4];
+      ld4(fs + 4 * r, v);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc + 2) = make_double2(v[2], v[3]);
+   }
+}
+
 __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wave, int nwarps)
 {
    if (halted(d)) return;
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[1 + wave] + w;
-   for (int job = d.sched_warp_ptr[g]; job < d.sched_warp_ptr[g + 1]; job++) {
+   const int end = d.sched_warp_ptr[g + 1];
+   for (int job = d.sched_warp_ptr[g]; job < end; job++) {
       const int ich = d.sched_jobs[job];
-      if (!frozen_chain(d, ich)) solve_chain(d, ich, threadIdx.x & 31);
+      if (ich & kPairJob) {
+         solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], threadIdx.x & 31);
+         job++;
+      } else if (!frozen_chain(d, ich)) {
+         solve_chain(d, ich, threadIdx.x & 31);
+      }
    }
 }
 

@@ -96,6 +96,7 @@ struct hamstr_gpu {
    double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums per instance
 
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
+   int adi_pair = 1;                    // open chains two per warp in the FP64 line kernels
 
    // instances (a plain handle has one)
    std::vector<int> inst_cell0;         // [nInst+1]
@@ -218,7 +219,7 @@ struct hamstr_gpu {
    }
 
    // launch shapes; a new warps-per-SM count rebuilds the line schedules
-   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft)
+   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair)
    {
       d.face_soft = face_soft;
       d.piv_soft = piv_soft;
@@ -227,8 +228,9 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb) {
-         sched = build_schedule(plan, adi_wpb * nsm);
+      if (adi_wpb != d.adi_wpb || pair != adi_pair) {
+         adi_pair = pair;
+         sched = build_schedule(plan, adi_wpb * nsm, pair != 0);
          int st;
          if ((st = upload(&d.sched_warp0, sched.warp0, owned))) return st;
          if ((st = upload(&d.sched_nwarps, sched.nwarps, owned))) return st;
@@ -501,7 +503,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_soft = 1;
       d.piv_soft = d.mx_fused ? 0 : 1;
       g->nsm = nsm;
-      g->sched = build_schedule(P, d.adi_wpb * nsm);
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0);
    }
    TRY(upload(&d.sched_warp0, g->sched.warp0, o));
    TRY(upload(&d.sched_nwarps, g->sched.nwarps, o));
@@ -1002,16 +1004,18 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair; float ms; };
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
          if (g->mixed) {
             for (int fused : {0, 1})
-               for (int mb : {32, 64, 128}) cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, 0.f});
+               for (int mb : {32, 64, 128})
+                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, 0.f});
          } else {
             for (int w : {4, 8})
-               for (int psoft : {0, 1}) cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, 0.f});
+               for (int psoft : {0, 1})
+                  for (int pair : {0, 1}) cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1024,7 +1028,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1045,28 +1049,51 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft);
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
       for (size_t i = 0; i < cands.size(); i++) {
-         char buf[160];
+         char buf[200];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"ms\": %.4f}",
+                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].ms);
+                       cands[i].psoft, cands[i].pair, cands[i].ms);
          r += buf;
       }
-      char buf[160];
+      char buf[200];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft);
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }
    return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
+{
+   if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
+   const DeviceState& d = g->d;
+   const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb, d.mx_block, d.mx_fused, d.face_soft, d.piv_soft, g->adi_pair};
+   std::memcpy(shape, v, sizeof(v));
+   return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
+{
+   if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
+   const int* s = shape;
+   const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
+                   (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
+                   (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1);
+   if (!ok) {
+      set_error("set_shape: a value outside its allowed set");
+      return HAMSTR_GPU_ERR_ARG;
+   }
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

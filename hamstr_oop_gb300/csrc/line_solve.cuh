@@ -193,6 +193,130 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
    if (h == 0) facN[e] = w;
 }
 
+// Two open lines per warp, one per half (h = lane >> 4): the same
+// operations as factor_line's half 0 on an open line, so each line's
+// records are bit-identical to a factor_line call.  Lines of different
+// length run to the longer one's count with the shorter half idle (its
+// loads and stores skipped).  Short open lines -- the rule on split meshes
+// -- leave half of factor_line's warp with nothing to do.
+template <bool SD = true>
+__device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
+                                                 double* __restrict__ fac, int lane)
+{
+   const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3, hb = 16 * h;
+   const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
+   double A = 0.0, B = 0.0, C = 0.0;
+   if (N > 0) {
+      A = Ab[e];
+      B = Ab[16 + e];
+      C = Ab[32 + e];
+   }
+   double P = 0.0;
+   for (int i = 0; i < Nmax; i++) {
+      double An = 0.0, Bn = 0.0, Cn = 0.0;
+      if (i + 1 < N) {
+         const size_t o = stride * (size_t)(i + 1);
+         An = Ab[o + e];
+         Bn = Ab[o + 16 + e];
+         Cn = Ab[o + 32 + e];
+      }
+      const bool live = i < N;
+      double* rec = fac + (size_t)kFacRec * i;
+      if (live) rec[e] = A;
+      double acc = B;
+      if (i > 0) {
+#pragma unroll
+         for (int l = 0; l < 4; l++) {
+            const double a = __shfl_sync(kLaneMask, A, hb + 4 * k + l);
+            const double x = __shfl_sync(kLaneMask, P, hb + 4 * l + j);
+            acc -= a * x;
+         }
+      }
+      const double w = lu_wavefront<SD>(acc, hb, e);
+      if (live) rec[16 + e] = w;
+      double lu[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, hb + 4 * k + c);
+      double ys[4];
+      const double Yp = lu_solve_lanes(lu, k, C, hb + j, 4, ys);
+      if (live) rec[32 + e] = Yp;
+      P = Yp;
+      A = An;
+      B = Bn;
+      C = Cn;
+   }
+}
+
+// Right-hand-side replay of two factored open lines, one per half-warp:
+// the operations of solve_line's open branch on lanes 0-15, per half.
+__device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs, int lane)
+{
+   const int e = lane & 15, pj = e & 3, r = lane & 3, hb = lane & 16;
+   const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
+   double xprev[4] = {0.0, 0.0, 0.0, 0.0};
+   double fv = 0.0, av = 0.0, lu[4] = {0.0, 0.0, 0.0, 0.0};
+   if (N > 0) {
+      fv = fs[r];
+#pragma unroll
+      for (int c = 0; c < 4; c++) lu[c] = fac[16 + 4 * r + c];
+   }
+   for (int i = 0; i < Nmax; i++) {
+      double fvn = 0.0, avn = 0.0, lun[4] = {0.0, 0.0, 0.0, 0.0};
+      if (i + 1 < N) {
+         const double* nr = fac + (size_t)kFacRec * (i + 1);
+         fvn = fs[4 * (i + 1) + r];
+         avn = nr[e];
+#pragma unroll
+         for (int c = 0; c < 4; c++) lun[c] = nr[16 + 4 * r + c];
+      }
+      double x = fv;
+      if (i > 0) {
+         const double p = av * sel4(xprev, pj);
+#pragma unroll
+         for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, p, hb + 4 * r + jj);
+      }
+      double xs[4];
+      x = lu_solve_lanes(lu, r, x, hb, 1, xs);
+      const bool live = i < N;   // the shorter line keeps its last row's solution
+      if (e < 4 && live) fs[4 * i + e] = x;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+         if (live) xprev[m] = xs[m];
+         lu[m] = lun[m];
+      }
+      fv = fvn;
+      av = avn;
+   }
+   __syncwarp();
+   // back substitution f(i) -= c'(i) f(i+1), i = N-2..0; the halves run
+   // t = 0..Nmax-2 with i = N-2-t
+   double xnext[4];
+#pragma unroll
+   for (int m = 0; m < 4; m++) xnext[m] = xprev[m];
+   double mv = 0.0, xi = 0.0;
+   if (N >= 2) {
+      mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
+      xi = fs[4 * (N - 2) + r];
+   }
+   for (int t = 0; t <= Nmax - 2; t++) {
+      const int ii = N - 2 - t;
+      double mvn = 0.0, xin = 0.0;
+      if (ii > 0) {
+         mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + e];
+         xin = fs[4 * (ii - 1) + r];
+      }
+      const double prod = mv * sel4(xnext, pj);
+      double x = xi;
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, prod, hb + 4 * r + jj);
+#pragma unroll
+      for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, hb + m);
+      if (e < 4 && ii >= 0) fs[4 * ii + e] = x;
+      mv = mvn;
+      xi = xin;
+   }
+}
+
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
 {
    const double2 a = *reinterpret_cast<const double2*>(p);

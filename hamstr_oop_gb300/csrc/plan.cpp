@@ -314,23 +314,45 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps)
+Schedule build_schedule(const Plan& p, int max_warps, bool pair_open)
 {
    Schedule S;
    S.warp_ptr.push_back(0);
    auto assign = [&](const std::vector<int>& chains) {
-      const int W = std::max(1, std::min((int)chains.size(), max_warps));
-      // cost model: rows of FP64 recurrence, periodic rows carry the
-      // fill-in column and the last-row elimination
-      std::vector<std::pair<double, int>> order;
-      for (int c : chains) order.push_back({p.chain_nrows[c] * (p.chain_periodic[c] ? 1.3 : 1.0), c});
-      std::stable_sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+      // jobs: a periodic chain alone, open chains alone or in pairs of
+      // neighbours in length order (a pair costs its longer chain: both
+      // halves issue the same instructions).  Cost model: rows of FP64
+      // recurrence, periodic rows carrying the fill-in column and the
+      // last-row elimination.
+      std::vector<int> sorted(chains);
+      std::stable_sort(sorted.begin(), sorted.end(),
+                       [&](int a, int b) { return p.chain_nrows[a] > p.chain_nrows[b]; });
+      struct Job { double cost; int a, b; };
+      std::vector<Job> order;
+      int pending = -1;
+      for (int c : sorted) {
+         if (p.chain_periodic[c]) order.push_back({1.3 * p.chain_nrows[c], c, -1});
+         else if (!pair_open) order.push_back({(double)p.chain_nrows[c], c, -1});
+         else if (pending < 0) pending = c;
+         else {
+            order.push_back({(double)p.chain_nrows[pending], pending, c});
+            pending = -1;
+         }
+      }
+      if (pending >= 0) order.push_back({(double)p.chain_nrows[pending], pending, -1});
+      std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
+      const int W = std::max(1, std::min((int)order.size(), max_warps));
       std::vector<double> load(W, 0.0);
       std::vector<std::vector<int>> lists(W);
-      for (const auto& oc : order) {
+      for (const Job& j : order) {
          const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-         load[w] += oc.first;
-         lists[w].push_back(oc.second);
+         load[w] += j.cost;
+         if (j.b >= 0) {
+            lists[w].push_back(j.a | kPairJob);
+            lists[w].push_back(j.b);
+         } else {
+            lists[w].push_back(j.a);
+         }
       }
       S.warp0.push_back((int)S.warp_ptr.size() - 1);
       S.nwarps.push_back(W);

@@ -69,16 +69,20 @@ struct Plan {
 // Builds the plan; returns "" on success or a description of the problem.
 std::string build_plan(const MeshInput& in, Plan& out);
 
-// Longest-chain-first assignment of chains to persistent warps, one warp
+// Longest-job-first assignment of chains to persistent warps, one warp
 // per SM sub-partition: schedule 0 is the factorisation (all chains),
 // schedule 1+v the solve of wave v.  Warp w of schedule s owns
-// jobs[warp_ptr[warp0[s] + w] .. warp_ptr[warp0[s] + w + 1]).
+// jobs[warp_ptr[warp0[s] + w] .. warp_ptr[warp0[s] + w + 1]).  With
+// pair_open, open chains of similar length go in pairs, one per half-warp:
+// an entry with kPairJob set is such a chain, and the next entry its
+// partner.
+constexpr int kPairJob = 1 << 30;
 struct Schedule {
    std::vector<int> warp0, nwarps;   // per schedule
    std::vector<int> warp_ptr;        // per global warp, +1
-   std::vector<int> jobs;            // chain ids
+   std::vector<int> jobs;            // chain ids (| kPairJob: paired with the next)
 };
-Schedule build_schedule(const Plan& p, int max_warps);
+Schedule build_schedule(const Plan& p, int max_warps, bool pair_open);
 
 }  // namespace hamstr
 #endif

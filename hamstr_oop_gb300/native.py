@@ -83,6 +83,8 @@ def load(build_if_missing: bool = False):
         "hamstr_mlp_train_step": (i, [vp, vp, vp, ctypes.c_longlong, i, ctypes.c_ulonglong, ctypes.c_ulonglong,
                                       ctypes.c_float, ctypes.POINTER(d)]),
         "hamstr_gpu_autotune": (i, [vp, i, ctypes.c_char_p, i]),
+        "hamstr_gpu_get_shape": (i, [vp, vp]),
+        "hamstr_gpu_set_shape": (i, [vp, vp]),
         "hamstr_gpu_set_geometry": (i, [vp, i, vp]),
         "hamstr_gpu_forces": (i, [vp, vp]),
         "hamstr_gpu_create": (i, [ctypes.POINTER(Params), i, i, vp, vp, vp, i, vp, vp, pp]),
@@ -313,9 +315,28 @@ class GpuSolver:
     def autotune(self, reps: int = 3) -> dict:
         """Pick the fastest launch shapes for the current precision (hamstr_gpu_autotune)."""
         import json
-        buf = ctypes.create_string_buffer(4096)
-        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 4096))
+        buf = ctypes.create_string_buffer(16384)
+        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 16384))
         return json.loads(buf.value.decode())
+
+    SHAPE_KEYS = ("face_block", "adi_warps_per_sm", "mx_block", "mx_fused", "face_softdiv", "pivot_softdiv",
+                  "adi_pair")
+
+    def shape(self) -> dict:
+        """The launch shape in use (hamstr_gpu_get_shape), keyed as the autotuner's report."""
+        v = (ctypes.c_int * len(self.SHAPE_KEYS))()
+        _check(load().hamstr_gpu_get_shape(self.h, v))
+        return dict(zip(self.SHAPE_KEYS, list(v)))
+
+    def set_shape(self, **kw) -> None:
+        """Change some launch-shape values (hamstr_gpu_set_shape); results do not depend on them."""
+        cur = self.shape()
+        for k, val in kw.items():
+            if k not in cur:
+                raise KeyError(k)
+            cur[k] = int(val)
+        v = (ctypes.c_int * len(self.SHAPE_KEYS))(*[cur[k] for k in self.SHAPE_KEYS])
+        _check(load().hamstr_gpu_set_shape(self.h, v))
 
     def set_cfl(self, cfl: float) -> None:
         """CFL of later steps (a project addition for CFL ramping)."""

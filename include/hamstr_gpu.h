@@ -191,14 +191,29 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
 /* Autotuner (no reference counterpart): times `reps` steps of the current
  * precision for each candidate launch shape -- face kernels 128 or 256
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
- * or two per sub-partition, schedules rebuilt longest-chain-first); FP32
- * line kernels 32..128 threads per block, with the blocks assembled by a
- * separate coalesced kernel or inside the factorisation; FP64 divisions of
- * the face kernels and of the LU pivots on the FP64 pipe or on the integer
- * pipes (bit-identical) -- and keeps the fastest.  The
- * state is restored afterwards; results do not depend on the shape.
- * report (may be NULL) receives a JSON summary of the timings. */
+ * or two per sub-partition, schedules rebuilt longest-job-first), with open
+ * chains one per warp or two per warp (one per half); FP32 line kernels
+ * 32..128 threads per block, with the blocks assembled by a separate
+ * coalesced kernel or inside the factorisation; FP64 divisions of the face
+ * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
+ * (bit-identical) -- and keeps the fastest.  The state is restored
+ * afterwards; results do not depend on the shape.  report (may be NULL)
+ * receives a JSON summary of the timings (about 200 bytes per candidate). */
 int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
+
+/* The launch shape itself (no reference counterpart), HAMSTR_SHAPE_N ints:
+ *   [0] face kernels' threads per block: 128 or 256
+ *   [1] FP64 line kernels' persistent warps per SM: 4 or 8
+ *   [2] FP32 line kernels' threads per block: 32, 64 or 128
+ *   [3] FP32 blocks assembled inside the factorisation: 0 or 1
+ *   [4] face kernels' divisions on the integer pipes: 0 or 1
+ *   [5] FP64 LU pivot reciprocals on the integer pipes: 0 or 1
+ *   [6] open chains two per warp in the FP64 line kernels: 0 or 1
+ * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
+ * not depend on the shape. */
+#define HAMSTR_SHAPE_N 7
+int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
+int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 
 /* ---------------- learned warm start (no reference counterpart) --------
  * C[M][N] (+ split * M * N when splits > 1) = A[M][K] * B[N][K]^T with A, B

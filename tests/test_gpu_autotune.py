@@ -10,7 +10,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     case = make_case(32, 8, order=3, CFL=10.0, msweep=2)
     g = native.GpuSolver(native.Case(case))
     rep = g.autotune(reps=2)
-    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 16
+    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 32
     assert all(c["ms"] > 0 for c in rep["candidates"])
     o = oracle_lib.OracleCase(case, "port")
     for it in range(5):
@@ -19,20 +19,40 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     assert np.array_equal(g.get("q"), o.get("q"))
 
 
-@pytest.mark.parametrize("shape", [(256, 8, 64), (128, 4, 32)])
-def test_every_fp64_shape_is_exact(make_case, oracle_lib, native_lib, shape):
-    """Force each candidate by tuning on a handle, then compare to the oracle."""
+FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_pair=pr)
+               for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for pr in (0, 1)]
+
+
+@pytest.mark.parametrize("order", [3, 5])
+def test_every_fp64_shape_is_exact(make_case, oracle_lib, native_lib, order):
+    """Each FP64 launch shape, set explicitly, on a split mesh (open chains
+    of many lengths, periodic chains) against the oracle."""
     from hamstr_oop_gb300 import native
-    case = make_case(24, 8, split=0.5, seed=3, order=5, CFL=5.0, msweep=2)
+    case = make_case(24, 8, split=0.5, seed=3, order=order, CFL=5.0, msweep=2)
     c = native.Case(case)
     c.set_option("chain_end_rule", 1)
-    g = native.GpuSolver(c)
-    g.autotune(reps=1)
     o = oracle_lib.OracleCase(case, "port")
     o.set_option("chain_end_rule", 1)
     o.march(4)
-    g.march(4, 0.0)
-    assert np.array_equal(g.get("q"), o.get("q"))
+    want = o.get("q")
+    g = native.GpuSolver(c)
+    q0 = g.get("q")
+    for shp in FP64_SHAPES:
+        g.set("q", q0)
+        g.set_shape(**shp)
+        assert {k: g.shape()[k] for k in shp} == shp
+        g.march(4, 0.0)
+        assert np.array_equal(g.get("q"), want), shp
+
+
+def test_set_shape_rejects_bad_values(make_case, native_lib):
+    from hamstr_oop_gb300 import native
+    g = native.GpuSolver(native.Case(make_case(16, 4, order=1, CFL=5.0)))
+    before = g.shape()
+    for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_pair=2)):
+        with pytest.raises(native.HamstrError):
+            g.set_shape(**bad)
+    assert g.shape() == before
 
 
 def test_autotune_mixed_restores_state_and_results(make_case, native_lib):
@@ -48,6 +68,15 @@ def test_autotune_mixed_restores_state_and_results(make_case, native_lib):
     a.march(6, 0.0)
     b.march(6, 0.0)
     assert np.array_equal(a.get("q"), b.get("q"))        # shape-independent arithmetic
+    q0 = a.get("q")
+    for fused in (0, 1):
+        for mb in (32, 64, 128):
+            b.set("q", q0)
+            b.set_shape(mx_fused=fused, mx_block=mb, face_block=128 if mb == 64 else 256)
+            a.set("q", q0)
+            a.march(3, 0.0)
+            b.march(3, 0.0)
+            assert np.array_equal(a.get("q"), b.get("q")), (fused, mb)
 
 
 def test_autotune_on_a_batch(make_case, native_lib):
