@@ -784,6 +784,7 @@ def main():
                     help="only time the tcgen05 BF16 GEMM on SIZE^3 (a plain run for ncu)")
     ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
     ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
+    ap.add_argument("--msweep", type=int, default=0, help="ADI sweeps per step (default: the workload's, 2)")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
     if args.gemm_only:
@@ -791,7 +792,10 @@ def main():
         torch.cuda.set_device(local_rank)
         print(json.dumps(gemm_peak(args.gemm_only)), flush=True)
         return
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.msweep:
+        wl["name"] = wl["name"].replace("msweep%d" % wl["msweep"], "msweep%d" % args.msweep)
+        wl["msweep"] = args.msweep
     if args.impl == "reference":
         out = run_reference(args, wl, rank)
         if out is not None:

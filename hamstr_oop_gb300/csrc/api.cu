@@ -97,6 +97,11 @@ struct hamstr_gpu {
 
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
    int adi_pair = 1;                    // open chains two per warp in the FP64 line kernels
+   // order 5, FP64: the WENO linearisation's f-only values kept from the
+   // implicit computeRHS for the sweeps (d.wlin points here when on)
+   double* wlin_buf = nullptr;
+   int weno_keep = 1;
+   bool wlin_valid = false;             // kept values match the current q (standalone entry points)
 
    // instances (a plain handle has one)
    std::vector<int> inst_cell0;         // [nInst+1]
@@ -192,7 +197,7 @@ struct hamstr_gpu {
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
-         L("lin_face", n, [&] { launch_lin_face(d, stream); });
+         L("lin_face", n, [&] { launch_lin_face(d, true, stream); });
          L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
          if (s == msweep - 1) L("norm_final", n, [&] { launch_norm_final(d, 2, false, stream); });
       }
@@ -219,8 +224,24 @@ struct hamstr_gpu {
    }
 
    // launch shapes; a new warps-per-SM count rebuilds the line schedules
-   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair)
+   int ensure_wlin()
    {
+      if (wlin_buf) return HAMSTR_GPU_OK;
+      return dalloc(&wlin_buf, 2 * 4 * 16 * (size_t)std::max(d.nSlot, 1), owned);
+   }
+
+   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair,
+                   int wkeep)
+   {
+      if (wkeep && d.recon == 5) {
+         const int st = ensure_wlin();
+         if (st) return st;
+         d.wlin = wlin_buf;
+      } else {
+         d.wlin = nullptr;
+      }
+      weno_keep = wkeep;
+      wlin_valid = false;
       d.face_soft = face_soft;
       d.piv_soft = piv_soft;
       if (!mx_fused && d.ff32) {
@@ -472,6 +493,10 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
    TRY(dalloc(&d.flux, 4 * (size_t)P.nSlot, o));
    TRY(dalloc(&d.spec, (size_t)P.nSlot, o));
    TRY(dalloc(&d.ff, 32 * (size_t)P.nSlot, o));
+   if (d.recon == 5) {
+      TRY(g->ensure_wlin());
+      d.wlin = g->wlin_buf;
+   }
    TRY(upload(&d.sten, sten, o));
    TRY(upload(&d.slot, slot, o));
    TRY(upload(&d.slot_face, P.slot_face, o));
@@ -630,6 +655,7 @@ int hamstr_gpu_get(hamstr_gpu* g, const char* name, double* out)
 int hamstr_gpu_set(hamstr_gpu* g, const char* name, const double* in)
 {
    if (!g || !name || !in) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    DeviceState& d = g->d;
    const size_t nc = (size_t)d.nCell;
    double* dst = nullptr;
@@ -662,6 +688,7 @@ int hamstr_gpu_compute_rhs(hamstr_gpu* g, int implicit, double* l2, double* linf
    int st = g->reset_ctl(0.0);
    if (st) return st;
    launch_rhs_face(g->d, implicit != 0, g->stream);
+   if (implicit) g->wlin_valid = g->d.wlin != nullptr;
    launch_rhs_cell(g->d, false, g->stream);
    launch_norm_final(g->d, 0, false, g->stream);
    CK(cudaGetLastError());
@@ -679,7 +706,7 @@ int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf)
    int st = g->reset_ctl(0.0);
    if (st) return st;
    launch_dtfac(g->d, g->stream);
-   launch_lin_face(g->d, g->stream);
+   launch_lin_face(g->d, g->wlin_valid, g->stream);
    launch_lin_cell(g->d, false, g->stream);
    launch_norm_final(g->d, 2, false, g->stream);
    CK(cudaGetLastError());
@@ -703,9 +730,10 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    for (int s = 0; s < g->msweep; s++) {
       for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, w, g->sched.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
-      launch_lin_face(d, g->stream);
+      launch_lin_face(d, g->wlin_valid, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);
    }
+   g->wlin_valid = false;   // q += dq
    launch_norm_final(d, 2, false, g->stream);
    CK(cudaGetLastError());
    double n[4];
@@ -719,6 +747,7 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
 int hamstr_gpu_step(hamstr_gpu* g, double* norms4)
 {
    if (!g) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    int st = g->capture();
    if (st) return st;
    st = g->reset_ctl(0.0);
@@ -734,6 +763,7 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4)
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged)
 {
    if (!g || nsteps < 0) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    int st = g->capture();
    if (st) return st;
    DeviceState& d = g->d;
@@ -767,6 +797,7 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
 int hamstr_gpu_update_solution(hamstr_gpu* g, const char* qold, const char* qnew, double coef)
 {
    if (!g || !qold || !qnew) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    auto pick = [&](const char* n) -> double* {
       if (!std::strcmp(n, "q")) return g->d.q;
       if (!std::strcmp(n, "qt")) return g->d.qt;
@@ -789,6 +820,7 @@ int hamstr_gpu_step_explicit(hamstr_gpu* g, int scheme, double* norms2)
 {
    // march.cpp:342-377: "euler" (scheme 0) and the 3-stage "rk3" (scheme 1)
    if (!g || (scheme != 0 && scheme != 1)) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    int st = g->reset_ctl(0.0);
    if (st) return st;
    DeviceState& d = g->d;
@@ -822,6 +854,7 @@ void* hamstr_gpu_stream(hamstr_gpu* g) { return g ? (void*)g->stream : nullptr; 
 int hamstr_gpu_enqueue_steps(hamstr_gpu* g, int n)
 {
    if (!g || n < 0) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    int st = g->capture();
    if (st) return st;
    st = g->reset_ctl(0.0);
@@ -865,6 +898,7 @@ int hamstr_gpu_profile_step(hamstr_gpu* g, int reps, const char** names, double*
 {
    // eager launches of the current mode's step with events around each kernel
    if (!g || reps < 1 || !names || !ms || !launches || !n) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    int st = g->reset_ctl(0.0);
    if (st) return st;
    std::vector<std::pair<const char*, std::pair<cudaEvent_t, cudaEvent_t>>> rec;
@@ -1005,6 +1039,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
    struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair; float ms; };
+   const int wk = g->weno_keep;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
@@ -1028,7 +1063,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1049,7 +1084,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair);
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, wk);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1077,7 +1112,8 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
 {
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
-   const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb, d.mx_block, d.mx_fused, d.face_soft, d.piv_soft, g->adi_pair};
+   const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb, d.mx_block, d.mx_fused,
+                                  d.face_soft,  d.piv_soft, g->adi_pair, g->weno_keep};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1088,12 +1124,13 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const int* s = shape;
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
-                   (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1);
+                   (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1) &&
+                   (s[7] == 0 || s[7] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
@@ -1109,6 +1146,7 @@ extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
 extern "C" int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed)
 {
    if (!g || (mixed != 0 && mixed != 1)) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q may change: the kept WENO values no longer apply
    if (mixed) {
       int st = g->ensure_mixed_buffers();
       if (st) return st;

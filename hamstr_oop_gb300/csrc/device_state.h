@@ -51,6 +51,10 @@ struct DeviceState {
    double *q, *r, *r0, *dq, *sigma, *dtfac;
    double* qt;             // second state of the RK3 scheme (solnBlock.h:47)
    double *flux, *spec, *ff;
+   // order 5, FP64: f-only values of the WENO linearisation, written by the
+   // implicit computeRHS face kernel and read by the sweeps' linear face
+   // kernels of the same step ([2*4*16][nSlot]); null when not kept
+   double* wlin;
    int4* sten;
    int4* slot;
    int* slot_face;
@@ -135,7 +139,8 @@ __device__ __forceinline__ int norm_cell(const DeviceState& d)
 // launchers (rhs.cu)
 void launch_rhs_face(const DeviceState& d, bool jacobian, cudaStream_t st);
 void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st);
-void launch_lin_face(const DeviceState& d, cudaStream_t st);
+// kept: this step's implicit rhs_face wrote d.wlin from the current q
+void launch_lin_face(const DeviceState& d, bool kept, cudaStream_t st);
 void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 // norms -> d.norms[off], d.norms[off+1] and hist row ctl[1] (when logging);
 // with check_tol, raises the stop flag when L2 <= tol

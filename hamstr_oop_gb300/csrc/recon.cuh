@@ -102,6 +102,31 @@ __device__ __forceinline__ void load_sten(const DeviceState& d, const T* __restr
    }
 }
 
+// the increment part of load_sten alone (dq of a cell, its wall mirror, or
+// zero at a far-field ghost)
+template <typename T>
+__device__ __forceinline__ void load_dsten(const DeviceState& d, const T* __restrict__ dqv, int idx, T (&df)[4])
+{
+   const int4 e = d.sten[idx];
+   if (e.y == STEN_CELL) {
+      ld4(dqv + 4 * e.x, df);
+   } else if (e.y == STEN_WALL) {
+      const double4 R = d.refl[e.z];
+      const T rx = T(R.x), ry = T(R.y), rz = T(R.z), rw = T(R.w);
+      T t[4];
+      ld4(dqv + 4 * e.x, t);
+      df[0] = t[0];
+      df[1] = (t[1] * rx + t[2] * ry);
+      df[2] = (t[1] * rz + t[2] * rw);
+      df[3] = t[3];
+   } else {
+      df[0] = T(0);
+      df[1] = T(0);
+      df[2] = T(0);
+      df[3] = T(0);
+   }
+}
+
 // MUSCL face states for one component from f[n-1..n+2]
 // (reconstruction.cpp:170-183): left state of slot n, right of slot n+1
 __device__ __forceinline__ void muscl2(double fm1, double f0, double fp1, double fp2, double& ql_n, double& qr_n1)
@@ -261,32 +286,91 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
 }
 
 // WENO_5 linearisation (reconstruction.cpp:358-462); the linear residual
-// passes eps = 1e-10 (computeLinearRHS.cpp:286,292)
-template <typename T, bool SD>
-__device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, T c_d, T d_d, T e_d)
+// passes eps = 1e-10 (computeLinearRHS.cpp:286,292).  Split in two: the
+// values formed from the states alone (Weno5Lin, weno5_lin_pre), which stay
+// fixed while q does -- through every sweep of a pseudo-time step -- and
+// the part that takes the increments (weno5_lin_apply).  weno5_deriv is the
+// two in sequence, the same operations in the same order.
+template <typename T>
+struct Weno5Lin {
+   T djm1, ejm1, dj, ej, djp1, ejp1, beta0, beta1, beta2, q30, q31, q32, w0, w1, w2, dwd;
+};
+constexpr int kWeno5LinVals = 16;
+
+template <typename T>
+__device__ __forceinline__ void weno5_lin_put(const Weno5Lin<T>& p, T* __restrict__ out, size_t stride)
 {
-   const T epsw = T(1e-10);
-   const T b1 = T(13. / 12.), b2 = T(1. / 6.);
-   const T djm1 = a - T(2.) * b + c;
-   const T ejm1 = a - T(4.) * b + T(3.) * c;
-   const T dj = b - T(2.) * c + d;
-   const T ej = b - d;
-   const T djp1 = c - T(2.) * d + e;
-   const T ejp1 = T(3.) * c - T(4.) * d + e;
-   const T dis0 = b1 * djm1 * djm1 + T(0.25) * ejm1 * ejm1 + epsw;
-   const T dis1 = b1 * dj * dj + T(0.25) * ej * ej + epsw;
-   const T dis2 = b1 * djp1 * djp1 + T(0.25) * ejp1 * ejp1 + epsw;
-   const T q30 = T(2.) * a - T(7.) * b + T(11.) * c;
-   const T q31 = -b + T(5.) * c + T(2.) * d;
-   const T q32 = T(2.) * c + T(5.) * d - e;
-   const Dv<T, SD> r1(dis1), r2(dis2);
-   const T d01 = r1.div(dis0);
-   const T d02 = r2.div(dis0);
+   const T v[kWeno5LinVals] = {p.djm1, p.ejm1, p.dj, p.ej, p.djp1, p.ejp1, p.beta0, p.beta1,
+                               p.beta2, p.q30, p.q31, p.q32, p.w0, p.w1, p.w2, p.dwd};
+#pragma unroll
+   for (int i = 0; i < kWeno5LinVals; i++) out[stride * i] = v[i];
+}
+
+template <typename T>
+__device__ __forceinline__ Weno5Lin<T> weno5_lin_get(const T* __restrict__ in, size_t stride)
+{
+   Weno5Lin<T> p;
+   p.djm1 = in[0];
+   p.ejm1 = in[stride];
+   p.dj = in[2 * stride];
+   p.ej = in[3 * stride];
+   p.djp1 = in[4 * stride];
+   p.ejp1 = in[5 * stride];
+   p.beta0 = in[6 * stride];
+   p.beta1 = in[7 * stride];
+   p.beta2 = in[8 * stride];
+   p.q30 = in[9 * stride];
+   p.q31 = in[10 * stride];
+   p.q32 = in[11 * stride];
+   p.w0 = in[12 * stride];
+   p.w1 = in[13 * stride];
+   p.w2 = in[14 * stride];
+   p.dwd = in[15 * stride];
+   return p;
+}
+
+// the weights from the smoothness sums (eps added) and the sums' common
+// denominator, shared by weno5_lin_pre and weno5_with_lin
+template <typename T, bool SD>
+__device__ __forceinline__ void weno5_lin_weights(Weno5Lin<T>& p)
+{
+   const Dv<T, SD> r1(p.beta1), r2(p.beta2);
+   const T d01 = r1.div(p.beta0);
+   const T d02 = r2.div(p.beta0);
    const T a1ba0 = T(6.) * d01;
    const T a2ba0 = T(3.) * d02;
-   const T w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
-   const T w1 = a1ba0 * w0;
-   const T w2 = T(1.) - w0 - w1;
+   p.w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
+   p.w1 = a1ba0 * p.w0;
+   p.w2 = T(1.) - p.w0 - p.w1;
+   p.dwd = p.beta1 * p.beta2 + T(6) * p.beta0 * p.beta2 + T(3) * p.beta0 * p.beta1;
+}
+
+template <typename T, bool SD>
+__device__ __forceinline__ Weno5Lin<T> weno5_lin_pre(T a, T b, T c, T d, T e)
+{
+   const T epsw = T(1e-10);
+   const T b1 = T(13. / 12.);
+   Weno5Lin<T> p;
+   p.djm1 = a - T(2.) * b + c;
+   p.ejm1 = a - T(4.) * b + T(3.) * c;
+   p.dj = b - T(2.) * c + d;
+   p.ej = b - d;
+   p.djp1 = c - T(2.) * d + e;
+   p.ejp1 = T(3.) * c - T(4.) * d + e;
+   p.beta0 = b1 * p.djm1 * p.djm1 + T(0.25) * p.ejm1 * p.ejm1 + epsw;
+   p.beta1 = b1 * p.dj * p.dj + T(0.25) * p.ej * p.ej + epsw;
+   p.beta2 = b1 * p.djp1 * p.djp1 + T(0.25) * p.ejp1 * p.ejp1 + epsw;
+   p.q30 = T(2.) * a - T(7.) * b + T(11.) * c;
+   p.q31 = -b + T(5.) * c + T(2.) * d;
+   p.q32 = T(2.) * c + T(5.) * d - e;
+   weno5_lin_weights<T, SD>(p);
+   return p;
+}
+
+template <typename T, bool SD>
+__device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d, T c_d, T d_d, T e_d)
+{
+   const T b1 = T(13. / 12.), b2 = T(1. / 6.);
    const T djm1_d = a_d - T(2.) * b_d + c_d;
    const T ejm1_d = a_d - T(4.) * b_d + T(3.) * c_d;
    const T dj_d = b_d - T(2.) * c_d + d_d;
@@ -296,26 +380,67 @@ __device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, 
    const T q30_d = T(2.) * a_d - T(7.) * b_d + T(11.) * c_d;
    const T q31_d = -b_d + T(5.) * c_d + T(2.) * d_d;
    const T q32_d = T(2.) * c_d + T(5.) * d_d - e_d;
-   const T term1 = b2 * w0 * q30_d;
-   const T term2 = b2 * w1 * q31_d;
-   const T term3 = b2 * w2 * q32_d;
-   const T dbeta0 = b1 * T(2) * djm1 * djm1_d + T(0.25) * T(2) * ejm1 * ejm1_d;
-   const T dbeta1 = b1 * T(2) * dj * dj_d + T(0.25) * T(2) * ej * ej_d;
-   const T dbeta2 = b1 * T(2) * djp1 * djp1_d + T(0.25) * T(2) * ejp1 * ejp1_d;
-   const T beta0 = dis0, beta1 = dis1, beta2 = dis2;
-   const T dw0_down = beta1 * beta2 + T(6) * beta0 * beta2 + T(3) * beta0 * beta1;
+   const T term1 = b2 * p.w0 * q30_d;
+   const T term2 = b2 * p.w1 * q31_d;
+   const T term3 = b2 * p.w2 * q32_d;
+   const T dbeta0 = b1 * T(2) * p.djm1 * djm1_d + T(0.25) * T(2) * p.ejm1 * ejm1_d;
+   const T dbeta1 = b1 * T(2) * p.dj * dj_d + T(0.25) * T(2) * p.ej * ej_d;
+   const T dbeta2 = b1 * T(2) * p.djp1 * djp1_d + T(0.25) * T(2) * p.ejp1 * ejp1_d;
+   const T beta0 = p.beta0, beta1 = p.beta1, beta2 = p.beta2;
+   const T dw0_down = p.dwd;
    const T dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
    const T dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
                                        + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
    const Dv<T, SD> rd(dw0_down * dw0_down);
    const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
    const T dw1_up_1 = T(6) * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
-   const T dw1_up_2 = r1.div(T(6) * dw0_up_2) * beta0;
+   const T dw1_up_2 = Dv<T, SD>(beta1).div(T(6) * dw0_up_2) * beta0;
    const T dw1 = rd.div(dw1_up_1 - dw1_up_2);
    const T dw2_up_1 = T(3) * (dbeta0 * beta1 + beta0 * dbeta1) * dw0_down;
-   const T dw2_up_2 = r2.div(T(3) * dw0_up_2) * beta0;
+   const T dw2_up_2 = Dv<T, SD>(beta2).div(T(3) * dw0_up_2) * beta0;
    const T dw2 = rd.div(dw2_up_1 - dw2_up_2);
-   return term1 + term2 + term3 + b2 * dw0 * q30 + b2 * dw1 * q31 + b2 * dw2 * q32;
+   return term1 + term2 + term3 + b2 * dw0 * p.q30 + b2 * dw1 * p.q31 + b2 * dw2 * p.q32;
+}
+
+template <typename T, bool SD>
+__device__ __forceinline__ T weno5_deriv(T a, T b, T c, T d, T e, T a_d, T b_d, T c_d, T d_d, T e_d)
+{
+   return weno5_lin_apply<T, SD>(weno5_lin_pre<T, SD>(a, b, c, d, e), a_d, b_d, c_d, d_d, e_d);
+}
+
+// weno5 and, from the same differences, the f-only values of its
+// linearisation: the smoothness sums differ only in the eps added last
+// (1e-15 here, 1e-10 there), so the sum before it is shared
+template <bool SD>
+__device__ __forceinline__ double weno5_with_lin(double a, double b, double c, double d, double e,
+                                                 Weno5Lin<double>& p)
+{
+   const double b1 = 13. / 12., b2 = 1. / 6.;
+   p.djm1 = a - 2. * b + c;
+   p.ejm1 = a - 4. * b + 3. * c;
+   p.dj = b - 2. * c + d;
+   p.ej = b - d;
+   p.djp1 = c - 2. * d + e;
+   p.ejp1 = 3. * c - 4. * d + e;
+   const double s0 = b1 * p.djm1 * p.djm1 + 0.25 * p.ejm1 * p.ejm1;
+   const double s1 = b1 * p.dj * p.dj + 0.25 * p.ej * p.ej;
+   const double s2 = b1 * p.djp1 * p.djp1 + 0.25 * p.ejp1 * p.ejp1;
+   const double dis0 = s0 + 1e-15, dis1 = s1 + 1e-15, dis2 = s2 + 1e-15;
+   p.q30 = 2. * a - 7. * b + 11. * c;
+   p.q31 = -b + 5. * c + 2. * d;
+   p.q32 = 2. * c + 5. * d - e;
+   const double d01 = Dv<double, SD>(dis1).div(dis0);
+   const double d02 = Dv<double, SD>(dis2).div(dis0);
+   const double a1ba0 = 6. * d01;
+   const double a2ba0 = 3. * d02;
+   const double w0 = Dv<double, SD>(1.0 + a1ba0 + a2ba0).div(1.0);
+   const double w1 = a1ba0 * w0;
+   const double w2 = 1. - w0 - w1;
+   p.beta0 = s0 + 1e-10;
+   p.beta1 = s1 + 1e-10;
+   p.beta2 = s2 + 1e-10;
+   weno5_lin_weights<double, SD>(p);
+   return b2 * (w0 * p.q30 + w1 * p.q31 + w2 * p.q32);
 }
 
 // reconstructed states at the two sides of a face slot, FP64
@@ -389,6 +514,57 @@ __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __re
          qrn1[k] = weno5_deriv<T, SD>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], df[5][k], df[4][k], df[3][k],
                                   df[2][k], df[1][k]);
       }
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      L[k] = swap ? qln[k] : qrn1[k];
+      R[k] = swap ? qrn1[k] : qln[k];
+   }
+}
+
+// Order-5 face states of slot s that also keep the f-only values of both
+// sides' linearisations for the sweeps of this pseudo-time step, at
+// d.wlin[(16*(4*side + k) + v) * nSlot + s]: side 0 the state left-biased
+// at stencil n, side 1 the one right-biased at n+1 (before the swap)
+template <bool SD>
+__device__ __forceinline__ void face_states_w5(const DeviceState& d, int n, bool swap, int s, double (&L)[4],
+                                               double (&R)[4])
+{
+   double f[6][4], dummy[4], qln[4], qrn1[4];
+#pragma unroll
+   for (int j = 0; j < 6; j++) load_sten<double, false>(d, nullptr, n - 2 + j, f[j], dummy);
+   const size_t ns = (size_t)d.nSlot;
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      Weno5Lin<double> p;
+      qln[k] = weno5_with_lin<SD>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k], p);
+      weno5_lin_put(p, d.wlin + (size_t)(kWeno5LinVals * k) * ns + s, ns);
+      qrn1[k] = weno5_with_lin<SD>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], p);
+      weno5_lin_put(p, d.wlin + (size_t)(kWeno5LinVals * (4 + k)) * ns + s, ns);
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      L[k] = swap ? qln[k] : qrn1[k];
+      R[k] = swap ? qrn1[k] : qln[k];
+   }
+}
+
+// face_dstates at order 5 from the kept f-only values (face_states_w5 of
+// the same q): only the increments are gathered
+template <bool SD>
+__device__ __forceinline__ void face_dstates_w5(const DeviceState& d, const double* __restrict__ dqv, int n, bool swap,
+                                                int s, double (&L)[4], double (&R)[4])
+{
+   double df[6][4], qln[4], qrn1[4];
+#pragma unroll
+   for (int j = 0; j < 6; j++) load_dsten<double>(d, dqv, n - 2 + j, df[j]);
+   const size_t ns = (size_t)d.nSlot;
+#pragma unroll
+   for (int k = 0; k < 4; k++) {
+      const Weno5Lin<double> pl = weno5_lin_get(d.wlin + (size_t)(kWeno5LinVals * k) * ns + s, ns);
+      qln[k] = weno5_lin_apply<double, SD>(pl, df[0][k], df[1][k], df[2][k], df[3][k], df[4][k]);
+      const Weno5Lin<double> pr = weno5_lin_get(d.wlin + (size_t)(kWeno5LinVals * (4 + k)) * ns + s, ns);
+      qrn1[k] = weno5_lin_apply<double, SD>(pr, df[5][k], df[4][k], df[3][k], df[2][k], df[1][k]);
    }
 #pragma unroll
    for (int k = 0; k < 4; k++) {

@@ -33,7 +33,8 @@ namespace {
 
 constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
-template <int ORDER, bool JAC, bool SD>
+// WL: order 5 only, keep the f-only values of the WENO linearisation
+template <int ORDER, bool JAC, bool SD, bool WL = false>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -41,7 +42,8 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
-   face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
+   if (WL) face_states_w5<SD>(d, sl.x, (sl.w & 1) != 0, s, L, R);
+   else face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
    RoeOut o;
    double lm[16], rm[16];
    if (!roe_face<JAC, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, lm, rm)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
@@ -56,14 +58,16 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    }
 }
 
-template <int ORDER, bool SD>
+// WL: order 5 only, the f-only WENO values kept by this step's rhs_face
+template <int ORDER, bool SD, bool WL = false>
 __global__ void __launch_bounds__(kThreads) lin_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    double dL[4], dR[4];
-   face_dstates<ORDER, double, SD>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
+   if (WL) face_dstates_w5<SD>(d, d.dq, sl.x, (sl.w & 1) != 0, s, dL, dR);
+   else face_dstates<ORDER, double, SD>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
    const double* m = d.ff + 32 * (size_t)(sl.w >> 1);
    double g[4];
 #pragma unroll
@@ -293,7 +297,10 @@ void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
       case 6: rhs_face_kernel<3, false, SD><<<b, t, 0, st>>>(d); break;
       case 7: rhs_face_kernel<3, true, SD><<<b, t, 0, st>>>(d); break;
       case 10: rhs_face_kernel<5, false, SD><<<b, t, 0, st>>>(d); break;
-      case 11: rhs_face_kernel<5, true, SD><<<b, t, 0, st>>>(d); break;
+      case 11:
+         if (d.wlin) rhs_face_kernel<5, true, SD, true><<<b, t, 0, st>>>(d);
+         else rhs_face_kernel<5, true, SD><<<b, t, 0, st>>>(d);
+         break;
       case 62: rhs_face_kernel<31, false, SD><<<b, t, 0, st>>>(d); break;
       case 63: rhs_face_kernel<31, true, SD><<<b, t, 0, st>>>(d); break;
       case 64: rhs_face_kernel<32, false, SD><<<b, t, 0, st>>>(d); break;
@@ -316,7 +323,7 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
    else rhs_cell_kernel<false><<<d.norm_blocks, kThreads, 0, st>>>(d);
 }
 
-void launch_lin_face(const DeviceState& d, cudaStream_t st)
+void launch_lin_face(const DeviceState& d, bool kept, cudaStream_t st)
 {
    const int kThreads = d.face_block;
    const int b = (d.nSlot + kThreads - 1) / kThreads;
@@ -325,8 +332,13 @@ void launch_lin_face(const DeviceState& d, cudaStream_t st)
       case 1: lin_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
       case 3: lin_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;
       case 5:
-         if (d.face_soft) lin_face_kernel<5, true><<<b, kThreads, 0, st>>>(d);
-         else lin_face_kernel<5, false><<<b, kThreads, 0, st>>>(d);
+         if (kept && d.wlin) {
+            if (d.face_soft) lin_face_kernel<5, true, true><<<b, kThreads, 0, st>>>(d);
+            else lin_face_kernel<5, false, true><<<b, kThreads, 0, st>>>(d);
+         } else {
+            if (d.face_soft) lin_face_kernel<5, true><<<b, kThreads, 0, st>>>(d);
+            else lin_face_kernel<5, false><<<b, kThreads, 0, st>>>(d);
+         }
          break;
       case 31: lin_face_kernel<31, true><<<b, kThreads, 0, st>>>(d); break;
       default: lin_face_kernel<32, true><<<b, kThreads, 0, st>>>(d); break;

@@ -209,9 +209,13 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *   [4] face kernels' divisions on the integer pipes: 0 or 1
  *   [5] FP64 LU pivot reciprocals on the integer pipes: 0 or 1
  *   [6] open chains two per warp in the FP64 line kernels: 0 or 1
+ *   [7] order 5, FP64: the WENO linearisation's state-only values formed
+ *       once per step by the implicit computeRHS and kept for the sweeps
+ *       (1 KiB per face slot of device memory): 0 or 1 (default 1; not
+ *       tuned by hamstr_gpu_autotune)
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
  * not depend on the shape. */
-#define HAMSTR_SHAPE_N 7
+#define HAMSTR_SHAPE_N 8
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

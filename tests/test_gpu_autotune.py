@@ -37,7 +37,8 @@ def test_every_fp64_shape_is_exact(make_case, oracle_lib, native_lib, order):
     want = o.get("q")
     g = native.GpuSolver(c)
     q0 = g.get("q")
-    for shp in FP64_SHAPES:
+    shapes = FP64_SHAPES + ([dict(s, weno_keep=0) for s in FP64_SHAPES[::3]] if order == 5 else [])
+    for shp in shapes:
         g.set("q", q0)
         g.set_shape(**shp)
         assert {k: g.shape()[k] for k in shp} == shp

@@ -69,8 +69,9 @@ def test_adi_bitexact(make_case, oracle_lib, native_lib, order, msweep):
     assert go[1] == lo[1]
 
 
-def test_linear_rhs_standalone(make_case, oracle_lib, native_lib):
-    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 20, 6, order=3)
+@pytest.mark.parametrize("order", [3, 5])
+def test_linear_rhs_standalone(make_case, oracle_lib, native_lib, order):
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 20, 6, order=order)
     orc.compute_rhs(True)
     gpu.compute_rhs(True)
     rng = np.random.default_rng(3)
@@ -82,6 +83,35 @@ def test_linear_rhs_standalone(make_case, oracle_lib, native_lib):
     lo, go = orc.linear_rhs(), gpu.linear_rhs()
     _eq(gpu.get("r"), orc.get("r"), "r")
     _norm_close(go[0], lo[0], "L2")
+
+
+@pytest.mark.parametrize("keep", [0, 1])
+def test_weno_linear_rhs_kept_and_invalidated(make_case, oracle_lib, native_lib, keep):
+    """Order 5 keeps the WENO linearisation's state-only values from the
+    implicit computeRHS: computeLinearRHS right after it uses them, and after
+    q changes it must not."""
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 24, 8, order=5, msweep=2)
+    gpu.set_shape(weno_keep=keep)
+    assert gpu.shape()["weno_keep"] == keep
+    rng = np.random.default_rng(5)
+    q = orc.get("q").reshape(-1, 4)
+    q = q * (1.0 + 0.03 * rng.standard_normal(q.shape))
+    for h in (orc, gpu):
+        h.set("q", q)
+        h.compute_rhs(True)
+        h.adi()                      # dq != 0, q updated
+        h.compute_rhs(True)          # kept values formed from the new q
+    lo, go = orc.linear_rhs(), gpu.linear_rhs()
+    _eq(gpu.get("r"), orc.get("r"), "r (kept values)")
+    _norm_close(go[0], lo[0], "L2")
+    q2 = orc.get("q").reshape(-1, 4) * (1.0 + 0.01 * rng.standard_normal(q.shape))
+    for h in (orc, gpu):
+        h.set("q", q2)               # the kept values no longer apply
+    lo, go = orc.linear_rhs(), gpu.linear_rhs()
+    _eq(gpu.get("r"), orc.get("r"), "r (after q changed)")
+    lo, go = orc.adi(), gpu.adi()
+    for name in ("dq", "q", "r"):
+        _eq(gpu.get(name), orc.get(name), name)
 
 
 @pytest.mark.parametrize("order", [1, 3, 5])
