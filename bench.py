@@ -498,6 +498,15 @@ def algorithmic_bytes(kernel: str, lay: dict, sizes: dict, order: int) -> float:
     return 0.0
 
 
+def parse_shape(text: str) -> dict:
+    """'key=value,...' into hamstr_gpu_set_shape keywords."""
+    out = {}
+    for item in text.split(","):
+        k, v = item.split("=")
+        out[k.strip()] = int(v)
+    return out
+
+
 def run_gpu(args, wl, rank, local_rank, world):
     import numpy as np
     import torch
@@ -517,6 +526,8 @@ def run_gpu(args, wl, rank, local_rank, world):
     if args.profile_steps:
         # a plain run of the workload for ncu: ramp, then N captured steps
         gpu.set_precision(args.profile_precision == "mixed")
+        if args.shape:
+            gpu.set_shape(**parse_shape(args.shape))
         gpu.enqueue_steps(args.profile_steps)
         gpu.sync()
         if rank == 0:
@@ -785,6 +796,8 @@ def main():
     ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
     ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
     ap.add_argument("--msweep", type=int, default=0, help="ADI sweeps per step (default: the workload's, 2)")
+    ap.add_argument("--shape", default="", help="with --profile-steps: launch shape, e.g. "
+                    "face_block=128,adi_warps_per_sm=8 (hamstr_gpu_set_shape keys)")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
     if args.gemm_only:

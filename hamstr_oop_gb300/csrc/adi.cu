@@ -192,6 +192,30 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wa
    }
 }
 
+// open chains one per thread, longest first (factor_line_thread)
+template <bool SD>
+__global__ void __launch_bounds__(128) adi_tfactor_kernel(DeviceState d, int first, int count)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= count || halted(d)) return;
+   const int ich = d.sched_thread_jobs[first + t];
+   if (frozen_chain(d, ich)) return;
+   const int row0 = d.chain_row0[ich];
+   factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[ich], d.fac + (size_t)kFacRec * row0);
+}
+
+// one sweep's solve of open chains one per thread (solve_line_thread)
+__global__ void __launch_bounds__(128) adi_tsolve_kernel(DeviceState d, int first, int count)
+{
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= count || halted(d)) return;
+   const int ich = d.sched_thread_jobs[first + t];
+   if (frozen_chain(d, ich)) return;
+   const int row0 = d.chain_row0[ich];
+   solve_line_thread(d.fac + (size_t)kFacRec * row0, d.chain_nrows[ich], d.r, d.row_fcell + row0,
+                     d.row_scell + row0, d.fsc + 4 * (size_t)row0);
+}
+
 }  // namespace
 
 // One block per SM: the dynamic shared-memory request below exceeds half
@@ -224,6 +248,7 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
 {
    const int wpb = d.adi_wpb;
+   if (nwarps <= 0) return;
    if (d.piv_soft) adi_factor_kernel<true><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
    else adi_factor_kernel<false><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
 }
@@ -232,6 +257,19 @@ void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t s
 {
    const int wpb = d.adi_wpb;
    if (nwarps > 0) adi_solve_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, wave, nwarps);
+}
+
+void launch_adi_tfactor(const DeviceState& d, int first, int nthreads, cudaStream_t st)
+{
+   if (nthreads <= 0) return;
+   const int b = (nthreads + 127) / 128;
+   if (d.piv_soft) adi_tfactor_kernel<true><<<b, 128, 0, st>>>(d, first, nthreads);
+   else adi_tfactor_kernel<false><<<b, 128, 0, st>>>(d, first, nthreads);
+}
+
+void launch_adi_tsolve(const DeviceState& d, int first, int nthreads, cudaStream_t st)
+{
+   if (nthreads > 0) adi_tsolve_kernel<<<(nthreads + 127) / 128, 128, 0, st>>>(d, first, nthreads);
 }
 
 }  // namespace hamstr

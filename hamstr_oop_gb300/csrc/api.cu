@@ -72,6 +72,19 @@ int upload(T** p, const std::vector<T>& v, std::vector<void*>& owned)
    return HAMSTR_GPU_OK;
 }
 
+// upload in place of an array this handle owns (freed first)
+template <typename T>
+int reupload(T** p, const std::vector<T>& v, std::vector<void*>& owned)
+{
+   for (size_t i = 0; i < owned.size(); i++)
+      if (owned[i] == (void*)*p) {
+         cudaFree(*p);
+         owned.erase(owned.begin() + (long)i);
+         break;
+      }
+   return upload(p, v, owned);
+}
+
 }  // namespace
 
 struct hamstr_gpu {
@@ -97,6 +110,7 @@ struct hamstr_gpu {
 
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
    int adi_pair = 1;                    // open chains two per warp in the FP64 line kernels
+   int adi_thread = 0;                  // open chains one per thread in the FP64 line kernels
    // order 5, FP64: the WENO linearisation's f-only values kept from the
    // implicit computeRHS for the sweeps (d.wlin points here when on)
    double* wlin_buf = nullptr;
@@ -130,6 +144,7 @@ struct hamstr_gpu {
    int enqueue_mixed_step(bool check_tol)
    {
       int n = 0;
+      if (d.recon == 5) L("recon5", n, [&] { launch_recon5(d, false, stream); });
       L("mx_rhs_face", n, [&] { launch_mx_rhs_face(d, stream); });
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
@@ -189,13 +204,14 @@ struct hamstr_gpu {
    {
       if (mixed) return enqueue_mixed_step(check_tol);
       int n = 0;
+      if (d.recon == 5) L("recon5", n, [&] { launch_recon5(d, true, stream); });
       L("rhs_face", n, [&] { launch_rhs_face(d, true, stream); });
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
       L("adi_assemble", n, [&] { launch_adi_assemble(d, stream); });
-      L("adi_factor", n, [&] { launch_adi_factor(d, sched.nwarps[0], stream); });
+      adi_factor_launches(n);
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
+         for (int w = 0; w < plan.nWave; w++) adi_solve_launches(w, n);
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
          L("lin_face", n, [&] { launch_lin_face(d, true, stream); });
          L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
@@ -230,8 +246,32 @@ struct hamstr_gpu {
       return dalloc(&wlin_buf, 2 * 4 * 16 * (size_t)std::max(d.nSlot, 1), owned);
    }
 
+   int upload_schedule()
+   {
+      int st;
+      if ((st = reupload(&d.sched_warp0, sched.warp0, owned))) return st;
+      if ((st = reupload(&d.sched_nwarps, sched.nwarps, owned))) return st;
+      if ((st = reupload(&d.sched_warp_ptr, sched.warp_ptr, owned))) return st;
+      if ((st = reupload(&d.sched_jobs, sched.jobs, owned))) return st;
+      return reupload(&d.sched_thread_jobs, sched.thread_jobs, owned);
+   }
+
+   // the FP64 line kernels of one schedule (0: factorisation, 1 + w: the
+   // solve of wave w)
+   void adi_factor_launches(int& n)
+   {
+      if (sched.nthreads[0] > 0) L("adi_tfactor", n, [&] { launch_adi_tfactor(d, sched.thread0[0], sched.nthreads[0], stream); });
+      if (sched.nwarps[0] > 0) L("adi_factor", n, [&] { launch_adi_factor(d, sched.nwarps[0], stream); });
+   }
+   void adi_solve_launches(int w, int& n)
+   {
+      if (sched.nthreads[1 + w] > 0)
+         L("adi_tsolve", n, [&] { launch_adi_tsolve(d, sched.thread0[1 + w], sched.nthreads[1 + w], stream); });
+      if (sched.nwarps[1 + w] > 0) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
+   }
+
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair,
-                   int wkeep)
+                   int wkeep, int thread)
    {
       if (wkeep && d.recon == 5) {
          const int st = ensure_wlin();
@@ -249,14 +289,12 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb || pair != adi_pair) {
+      if (adi_wpb != d.adi_wpb || pair != adi_pair || thread != adi_thread) {
          adi_pair = pair;
-         sched = build_schedule(plan, adi_wpb * nsm, pair != 0);
-         int st;
-         if ((st = upload(&d.sched_warp0, sched.warp0, owned))) return st;
-         if ((st = upload(&d.sched_nwarps, sched.nwarps, owned))) return st;
-         if ((st = upload(&d.sched_warp_ptr, sched.warp_ptr, owned))) return st;
-         if ((st = upload(&d.sched_jobs, sched.jobs, owned))) return st;
+         adi_thread = thread;
+         sched = build_schedule(plan, adi_wpb * nsm, pair != 0, thread != 0);
+         const int st = upload_schedule();
+         if (st) return st;
       }
       d.face_block = face_block;
       d.adi_wpb = adi_wpb;
@@ -494,6 +532,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
    TRY(dalloc(&d.spec, (size_t)P.nSlot, o));
    TRY(dalloc(&d.ff, 32 * (size_t)P.nSlot, o));
    if (d.recon == 5) {
+      TRY(dalloc(&d.qface, 8 * (size_t)P.nSlot, o));
       TRY(g->ensure_wlin());
       d.wlin = g->wlin_buf;
    }
@@ -528,12 +567,12 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_soft = 1;
       d.piv_soft = d.mx_fused ? 0 : 1;
       g->nsm = nsm;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0);
+      // open chains one per thread where chains are short (the autotuner
+      // checks both)
+      g->adi_thread = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 1 : 0;
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_thread != 0);
    }
-   TRY(upload(&d.sched_warp0, g->sched.warp0, o));
-   TRY(upload(&d.sched_nwarps, g->sched.nwarps, o));
-   TRY(upload(&d.sched_warp_ptr, g->sched.warp_ptr, o));
-   TRY(upload(&d.sched_jobs, g->sched.jobs, o));
+   TRY(g->upload_schedule());
    TRY(dalloc(&d.blk, 48 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fac, 80 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fsc, 4 * (size_t)std::max(P.nRow, 1), o));
@@ -687,6 +726,7 @@ int hamstr_gpu_compute_rhs(hamstr_gpu* g, int implicit, double* l2, double* linf
    if (!g) return HAMSTR_GPU_ERR_ARG;
    int st = g->reset_ctl(0.0);
    if (st) return st;
+   launch_recon5(g->d, implicit != 0, g->stream);
    launch_rhs_face(g->d, implicit != 0, g->stream);
    if (implicit) g->wlin_valid = g->d.wlin != nullptr;
    launch_rhs_cell(g->d, false, g->stream);
@@ -726,9 +766,14 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    const DeviceState& d = g->d;
    launch_adi_init(d, g->stream);
    launch_adi_assemble(d, g->stream);
-   launch_adi_factor(d, g->sched.nwarps[0], g->stream);
+   const Schedule& S = g->sched;
+   launch_adi_tfactor(d, S.thread0[0], S.nthreads[0], g->stream);
+   launch_adi_factor(d, S.nwarps[0], g->stream);
    for (int s = 0; s < g->msweep; s++) {
-      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, w, g->sched.nwarps[1 + w], g->stream);
+      for (int w = 0; w < g->plan.nWave; w++) {
+         launch_adi_tsolve(d, S.thread0[1 + w], S.nthreads[1 + w], g->stream);
+         launch_adi_solve(d, w, S.nwarps[1 + w], g->stream);
+      }
       launch_dq_update(d, g->stream);
       launch_lin_face(d, g->wlin_valid, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);
@@ -825,6 +870,7 @@ int hamstr_gpu_step_explicit(hamstr_gpu* g, int scheme, double* norms2)
    if (st) return st;
    DeviceState& d = g->d;
    auto rhs = [&]() {
+      launch_recon5(d, false, g->stream);
       launch_rhs_face(d, false, g->stream);
       launch_rhs_cell(d, false, g->stream);
       launch_norm_final(d, 0, false, g->stream);
@@ -1038,7 +1084,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair, thread; float ms; };
    const int wk = g->weno_keep;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
@@ -1046,11 +1092,13 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          if (g->mixed) {
             for (int fused : {0, 1})
                for (int mb : {32, 64, 128})
-                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, 0.f});
+                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, g->adi_thread, 0.f});
          } else {
             for (int w : {4, 8})
                for (int psoft : {0, 1})
-                  for (int pair : {0, 1}) cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, 0.f});
+                  for (int pair : {0, 1})
+                     for (int th : {0, 1})
+                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, th, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1063,7 +1111,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk, c.thread))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1084,24 +1132,26 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, wk);
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, wk,
+                       best->thread);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
       for (size_t i = 0; i < cands.size(); i++) {
-         char buf[200];
+         char buf[256];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"ms\": %.4f}",
+                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_thread\": %d, "
+                       "\"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].pair, cands[i].ms);
+                       cands[i].psoft, cands[i].pair, cands[i].thread, cands[i].ms);
          r += buf;
       }
-      char buf[200];
+      char buf[256];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair);
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_thread\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, best->thread);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }
@@ -1112,8 +1162,8 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
 {
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
-   const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb, d.mx_block, d.mx_fused,
-                                  d.face_soft,  d.piv_soft, g->adi_pair, g->weno_keep};
+   const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
+                                  d.piv_soft,   g->adi_pair, g->weno_keep, g->adi_thread};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1125,12 +1175,12 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1) &&
-                   (s[7] == 0 || s[7] == 1);
+                   (s[7] == 0 || s[7] == 1) && (s[8] == 0 || s[8] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

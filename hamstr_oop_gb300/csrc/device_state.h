@@ -55,6 +55,9 @@ struct DeviceState {
    // implicit computeRHS face kernel and read by the sweeps' linear face
    // kernels of the same step ([2*4*16][nSlot]); null when not kept
    double* wlin;
+   // order 5: the two reconstructed states of every slot, [2*4][nSlot]
+   // (recon5 kernel, read by the face kernels); null otherwise
+   double* qface;
    int4* sten;
    int4* slot;
    int* slot_face;
@@ -67,6 +70,7 @@ struct DeviceState {
    int *cell_written;
    double* blk;            // per-row assembled blocks A, B, C (scaled, B + I) [nRow][48]
    int *sched_warp0, *sched_nwarps, *sched_warp_ptr, *sched_jobs;   // persistent-warp job lists
+   int* sched_thread_jobs;   // open chains solved one per thread (Schedule::thread_jobs)
    double* fac;            // per-row factor storage
    double* fsc;            // per-row right-hand side / solution scratch [nRow][4]
    double* facN;           // per periodic chain: final LU of the last row (16)
@@ -137,6 +141,10 @@ __device__ __forceinline__ int norm_cell(const DeviceState& d)
 }
 
 // launchers (rhs.cu)
+// order 5: the reconstructed face states (and, keep_lin with d.wlin, the
+// WENO linearisation's f-only values) ahead of rhs_face / mx_rhs_face; a
+// no-op at other orders
+void launch_recon5(const DeviceState& d, bool keep_lin, cudaStream_t st);
 void launch_rhs_face(const DeviceState& d, bool jacobian, cudaStream_t st);
 void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st);
 // kept: this step's implicit rhs_face wrote d.wlin from the current q
@@ -162,8 +170,12 @@ void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
+// nwarps persistent warps over the warp jobs, then nthreads open chains
+// one per thread from sched_thread_jobs[first..]; either may be 0
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
+void launch_adi_tfactor(const DeviceState& d, int first, int nthreads, cudaStream_t st);
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
+void launch_adi_tsolve(const DeviceState& d, int first, int nthreads, cudaStream_t st);
 int adi_configure(int max_dynamic_smem);
 // launcher (forces.cu): per instance k, out[3k..3k+2] = {Fx, Fy, M} over
 // its wall faces wall0[k]..wall0[k+1]-1; scr = 3 doubles per wall face

@@ -317,6 +317,194 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
    }
 }
 
+// ---- one open line per thread -------------------------------------------
+// The same operations as factor_line / solve_line on an open line, written
+// out for one thread: a warp then carries 32 lines and every FP64
+// instruction does 32 lanes of useful work (the warp forms keep 16 or 4).
+// Records are those of factor_line, so either form can solve what the
+// other factored.  Short open lines -- most of a split mesh -- gain most.
+
+// lu_wavefront on a block held by one thread: element e = 4k + j in w[e]
+template <bool SD>
+__device__ __forceinline__ void lu4_thread(double (&w)[16])
+{
+   const double piv0 = SD ? sd::div(1., w[0]) : 1. / w[0];
+#pragma unroll
+   for (int j = 1; j < 4; j++) w[j] = w[j] * piv0;
+#pragma unroll
+   for (int k = 1; k < 4; k++)
+#pragma unroll
+      for (int j = 1; j < 4; j++) w[4 * k + j] = w[4 * k + j] - w[4 * k] * w[j];
+   const double piv1 = SD ? sd::div(1., w[5]) : 1. / w[5];
+#pragma unroll
+   for (int j = 2; j < 4; j++) w[4 + j] = w[4 + j] * piv1;
+#pragma unroll
+   for (int k = 2; k < 4; k++)
+#pragma unroll
+      for (int j = 2; j < 4; j++) w[4 * k + j] = w[4 * k + j] - w[4 * k + 1] * w[4 + j];
+   const double piv2 = SD ? sd::div(1., w[10]) : 1. / w[10];
+   w[11] = w[11] * piv2;
+   w[15] = w[15] - w[14] * w[11];
+   const double piv3 = SD ? sd::div(1., w[15]) : 1. / w[15];
+   w[0] = piv0;
+   w[5] = piv1;
+   w[10] = piv2;
+   w[15] = piv3;
+}
+
+// lu_solve_lanes for a vector held by one thread (lu: the 16-entry record)
+__device__ __forceinline__ void lu_solve_thread(const double (&lu)[16], double (&x)[4])
+{
+   const double d0 = x[0] * lu[0];
+   double x1 = x[1] - lu[4] * d0;
+   double x2 = x[2] - lu[8] * d0;
+   double x3 = x[3] - lu[12] * d0;
+   const double d1 = x1 * lu[5];
+   x2 = x2 - lu[9] * d1;
+   x3 = x3 - lu[13] * d1;
+   const double d2 = x2 * lu[10];
+   x3 = x3 - lu[14] * d2;
+   const double s3 = x3 * lu[15];
+   const double s2 = d2 - lu[11] * s3;
+   const double s1 = (d1 - lu[6] * s2) - lu[7] * s3;
+   const double s0 = ((d0 - lu[1] * s1) - lu[2] * s2) - lu[3] * s3;
+   x[0] = s0;
+   x[1] = s1;
+   x[2] = s2;
+   x[3] = s3;
+}
+
+__device__ __forceinline__ void ld16(const double* __restrict__ p, double (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m += 2) {
+      const double2 t = *reinterpret_cast<const double2*>(p + m);
+      v[m] = t.x;
+      v[m + 1] = t.y;
+   }
+}
+
+__device__ __forceinline__ void st16(double* __restrict__ p, const double (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m += 2) *reinterpret_cast<double2*>(p + m) = make_double2(v[m], v[m + 1]);
+}
+
+// factor_line on an open line by one thread: blocks of row i at
+// blk + i*stride (A, B, C consecutive, 16 each), records into fac
+template <bool SD>
+__device__ __forceinline__ void factor_line_thread(const double* __restrict__ blk, size_t stride, int N,
+                                                   double* __restrict__ fac)
+{
+   double P[16];   // previous row's C'
+   for (int i = 0; i < N; i++) {
+      const double* b = blk + stride * (size_t)i;
+      double* rec = fac + (size_t)kFacRec * i;
+      double A[16], w[16], C[16];
+      ld16(b, A);
+      ld16(b + 16, w);
+      ld16(b + 32, C);
+      st16(rec, A);
+      if (i > 0) {
+         // b(i) -= a(i) c'(i-1), each entry's four products subtracted in order
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+               double acc = w[4 * k + j];
+#pragma unroll
+               for (int l = 0; l < 4; l++) acc -= A[4 * k + l] * P[4 * l + j];
+               w[4 * k + j] = acc;
+            }
+      }
+      lu4_thread<SD>(w);
+      st16(rec + 16, w);
+      // c'(i) = B'^{-1} c(i), column by column
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+         double x[4] = {C[j], C[4 + j], C[8 + j], C[12 + j]};
+         lu_solve_thread(w, x);
+#pragma unroll
+         for (int k = 0; k < 4; k++) P[4 * k + j] = x[k];
+      }
+      st16(rec + 32, P);
+   }
+}
+
+// solve_line on an open line by one thread, the right-hand side read from
+// r[fcell[i]] (zero where fcell < 0) and the solution written to
+// r[scell[i]]; fs holds the forward sweep's rows.  The next row's record
+// and right-hand side are loaded while this row is solved.
+__device__ __forceinline__ void solve_line_thread(const double* __restrict__ fac, int N, double* __restrict__ r,
+                                                  const int* __restrict__ fcell, const int* __restrict__ scell,
+                                                  double* __restrict__ fs)
+{
+   double xp[4] = {0.0, 0.0, 0.0, 0.0};
+   double a[16], lu[16], xr[4] = {0.0, 0.0, 0.0, 0.0};
+   {
+      const int fc = fcell[0];
+      if (fc >= 0) {
+         const double2 u = *reinterpret_cast<const double2*>(r + 4 * (size_t)fc);
+         const double2 v = *reinterpret_cast<const double2*>(r + 4 * (size_t)fc + 2);
+         xr[0] = u.x; xr[1] = u.y; xr[2] = v.x; xr[3] = v.y;
+      }
+      ld16(fac + 16, lu);
+#pragma unroll
+      for (int m = 0; m < 16; m++) a[m] = 0.0;
+   }
+   for (int i = 0; i < N; i++) {
+      double an[16], lun[16], xrn[4] = {0.0, 0.0, 0.0, 0.0};
+      if (i + 1 < N) {
+         const double* rn = fac + (size_t)kFacRec * (i + 1);
+         const int fcn = fcell[i + 1];
+         if (fcn >= 0) {
+            const double2 u = *reinterpret_cast<const double2*>(r + 4 * (size_t)fcn);
+            const double2 v = *reinterpret_cast<const double2*>(r + 4 * (size_t)fcn + 2);
+            xrn[0] = u.x; xrn[1] = u.y; xrn[2] = v.x; xrn[3] = v.y;
+         }
+         ld16(rn, an);
+         ld16(rn + 16, lun);
+      }
+      double x[4] = {xr[0], xr[1], xr[2], xr[3]};
+      if (i > 0) {
+         // f(i) -= a(i) f(i-1), each component's products subtracted in order
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[k] = x[k] - a[4 * k + j] * xp[j];
+      }
+      lu_solve_thread(lu, x);
+      *reinterpret_cast<double2*>(fs + 4 * i) = make_double2(x[0], x[1]);
+      *reinterpret_cast<double2*>(fs + 4 * i + 2) = make_double2(x[2], x[3]);
+#pragma unroll
+      for (int k = 0; k < 4; k++) { xp[k] = x[k]; xr[k] = xrn[k]; }
+#pragma unroll
+      for (int m = 0; m < 16; m++) { a[m] = an[m]; lu[m] = lun[m]; }
+   }
+   // back substitution f(i) -= c'(i) f(i+1), i = N-2..0
+   {
+      double* o = r + 4 * (size_t)scell[N - 1];
+      *reinterpret_cast<double2*>(o) = make_double2(xp[0], xp[1]);
+      *reinterpret_cast<double2*>(o + 2) = make_double2(xp[2], xp[3]);
+   }
+   for (int i = N - 2; i >= 0; i--) {
+      double c[16], x[4];
+      ld16(fac + (size_t)kFacRec * i + 32, c);
+      const double2 u = *reinterpret_cast<const double2*>(fs + 4 * i);
+      const double2 v = *reinterpret_cast<const double2*>(fs + 4 * i + 2);
+      x[0] = u.x; x[1] = u.y; x[2] = v.x; x[3] = v.y;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+#pragma unroll
+         for (int j = 0; j < 4; j++) x[k] = x[k] - c[4 * k + j] * xp[j];
+      double* o = r + 4 * (size_t)scell[i];
+      *reinterpret_cast<double2*>(o) = make_double2(x[0], x[1]);
+      *reinterpret_cast<double2*>(o + 2) = make_double2(x[2], x[3]);
+#pragma unroll
+      for (int k = 0; k < 4; k++) xp[k] = x[k];
+   }
+}
+
 __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4])
 {
    const double2 a = *reinterpret_cast<const double2*>(p);

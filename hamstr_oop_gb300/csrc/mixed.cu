@@ -28,7 +28,8 @@ constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
 
 // ---------------- residual + FP32 Jacobian ----------------
-template <int ORDER, bool SD>
+// PRE: the order-5 face states come from recon5_kernel
+template <int ORDER, bool SD, bool PRE = false>
 __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,7 +37,8 @@ __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
-   face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
+   if (ORDER == 5 && PRE) face_states_pre(d, s, (sl.w & 1) != 0, L, R);
+   else face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
    RoeOut o;
    if (!roe_face<false, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, nullptr, nullptr)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
    st4(d.flux + 4 * (size_t)s, o.flux);
@@ -566,7 +568,10 @@ void mx_rhs_face_go(const DeviceState& d, int b, int t, cudaStream_t st)
    switch (d.recon) {
       case 1: mx_rhs_face_kernel<1, SD><<<b, t, 0, st>>>(d); break;
       case 3: mx_rhs_face_kernel<3, SD><<<b, t, 0, st>>>(d); break;
-      case 5: mx_rhs_face_kernel<5, SD><<<b, t, 0, st>>>(d); break;
+      case 5:
+         if (d.qface) mx_rhs_face_kernel<5, SD, true><<<b, t, 0, st>>>(d);
+         else mx_rhs_face_kernel<5, SD><<<b, t, 0, st>>>(d);
+         break;
       case 31: mx_rhs_face_kernel<31, SD><<<b, t, 0, st>>>(d); break;
       default: mx_rhs_face_kernel<32, SD><<<b, t, 0, st>>>(d); break;
    }

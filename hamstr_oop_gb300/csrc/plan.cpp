@@ -314,7 +314,7 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps, bool pair_open)
+Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, bool thread_open)
 {
    Schedule S;
    S.warp_ptr.push_back(0);
@@ -330,8 +330,10 @@ Schedule build_schedule(const Plan& p, int max_warps, bool pair_open)
       struct Job { double cost; int a, b; };
       std::vector<Job> order;
       int pending = -1;
+      S.thread0.push_back((int)S.thread_jobs.size());
       for (int c : sorted) {
-         if (p.chain_periodic[c]) order.push_back({1.3 * p.chain_nrows[c], c, -1});
+         if (thread_open && !p.chain_periodic[c]) S.thread_jobs.push_back(c);
+         else if (p.chain_periodic[c]) order.push_back({1.3 * p.chain_nrows[c], c, -1});
          else if (!pair_open) order.push_back({(double)p.chain_nrows[c], c, -1});
          else if (pending < 0) pending = c;
          else {
@@ -341,7 +343,8 @@ Schedule build_schedule(const Plan& p, int max_warps, bool pair_open)
       }
       if (pending >= 0) order.push_back({(double)p.chain_nrows[pending], pending, -1});
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
-      const int W = std::max(1, std::min((int)order.size(), max_warps));
+      S.nthreads.push_back((int)S.thread_jobs.size() - S.thread0.back());
+      const int W = std::min((int)order.size(), max_warps);
       std::vector<double> load(W, 0.0);
       std::vector<std::vector<int>> lists(W);
       for (const Job& j : order) {

@@ -127,6 +127,22 @@ __device__ __forceinline__ void load_dsten(const DeviceState& d, const T* __rest
    }
 }
 
+// component k of stencil entry idx, as load_sten<double, false> forms it
+__device__ __forceinline__ double sten_comp(const DeviceState& d, int idx, int k)
+{
+   const int4 e = d.sten[idx];
+   if (e.y == STEN_CELL) return d.q[4 * (size_t)e.x + k];
+   if (e.y == STEN_WALL) {
+      const double* s = d.q + 4 * (size_t)e.x;
+      if (k == 0 || k == 3) return s[k];
+      const double4 R = d.refl[e.z];
+      const double s1 = s[1], s2 = s[2];
+      return k == 1 ? (s1 * R.x + s2 * R.y) : (s1 * R.z + s2 * R.w);
+   }
+   const double4 f = d.fstab[e.w];
+   return k == 0 ? f.x : k == 1 ? f.y : k == 2 ? f.z : f.w;
+}
+
 // MUSCL face states for one component from f[n-1..n+2]
 // (reconstruction.cpp:170-183): left state of slot n, right of slot n+1
 __device__ __forceinline__ void muscl2(double fm1, double f0, double fp1, double fp2, double& ql_n, double& qr_n1)
@@ -522,35 +538,50 @@ __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __re
    }
 }
 
-// Order-5 face states of slot s that also keep the f-only values of both
-// sides' linearisations for the sweeps of this pseudo-time step, at
-// d.wlin[(16*(4*side + k) + v) * nSlot + s]: side 0 the state left-biased
-// at stencil n, side 1 the one right-biased at n+1 (before the swap)
-template <bool SD>
-__device__ __forceinline__ void face_states_w5(const DeviceState& d, int n, bool swap, int s, double (&L)[4],
-                                               double (&R)[4])
+// One order-5 face state: component k of side `side` (0: left-biased at
+// stencil n, 1: right-biased at n+1) of slot s, into d.qface[(4*side + k) *
+// nSlot + s]; with WL also the f-only values of its linearisation into
+// d.wlin (layout of face_states_w5).  The face kernels then read the
+// states: computeRHS.cpp:266-304 with its 8 reconstructions per face spread
+// over 8 threads.
+template <bool SD, bool WL>
+__device__ __forceinline__ void recon5_one(const DeviceState& d, int s, int side, int k)
 {
-   double f[6][4], dummy[4], qln[4], qrn1[4];
+   const int n = d.slot[s].x;
+   double f[6];
 #pragma unroll
-   for (int j = 0; j < 6; j++) load_sten<double, false>(d, nullptr, n - 2 + j, f[j], dummy);
+   for (int j = 0; j < 6; j++) f[j] = sten_comp(d, n - 2 + j, k);
+   const double a = side ? f[5] : f[0], b = side ? f[4] : f[1], c = side ? f[3] : f[2];
+   const double e4 = side ? f[2] : f[3], e5 = side ? f[1] : f[4];
+   const size_t ns = (size_t)d.nSlot;
+   const int sk = 4 * side + k;
+   double v;
+   if (WL) {
+      Weno5Lin<double> p;
+      v = weno5_with_lin<SD>(a, b, c, e4, e5, p);
+      weno5_lin_put(p, d.wlin + (size_t)(kWeno5LinVals * sk) * ns + s, ns);
+   } else {
+      v = weno5<SD>(a, b, c, e4, e5);
+   }
+   d.qface[(size_t)sk * ns + s] = v;
+}
+
+// the face states recon5_one left for slot s, swapped as face_states does
+__device__ __forceinline__ void face_states_pre(const DeviceState& d, int s, bool swap, double (&L)[4],
+                                                double (&R)[4])
+{
    const size_t ns = (size_t)d.nSlot;
 #pragma unroll
    for (int k = 0; k < 4; k++) {
-      Weno5Lin<double> p;
-      qln[k] = weno5_with_lin<SD>(f[0][k], f[1][k], f[2][k], f[3][k], f[4][k], p);
-      weno5_lin_put(p, d.wlin + (size_t)(kWeno5LinVals * k) * ns + s, ns);
-      qrn1[k] = weno5_with_lin<SD>(f[5][k], f[4][k], f[3][k], f[2][k], f[1][k], p);
-      weno5_lin_put(p, d.wlin + (size_t)(kWeno5LinVals * (4 + k)) * ns + s, ns);
-   }
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      L[k] = swap ? qln[k] : qrn1[k];
-      R[k] = swap ? qrn1[k] : qln[k];
+      const double qln = d.qface[(size_t)k * ns + s], qrn1 = d.qface[(size_t)(4 + k) * ns + s];
+      L[k] = swap ? qln : qrn1;
+      R[k] = swap ? qrn1 : qln;
    }
 }
 
-// face_dstates at order 5 from the kept f-only values (face_states_w5 of
-// the same q): only the increments are gathered
+// face_dstates at order 5 from the kept f-only values (recon5_one with WL
+// on the same q, at d.wlin[(16*(4*side + k) + v) * nSlot + s]): only the
+// increments are gathered
 template <bool SD>
 __device__ __forceinline__ void face_dstates_w5(const DeviceState& d, const double* __restrict__ dqv, int n, bool swap,
                                                 int s, double (&L)[4], double (&R)[4])

@@ -33,8 +33,19 @@ namespace {
 
 constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
-// WL: order 5 only, keep the f-only values of the WENO linearisation
-template <int ORDER, bool JAC, bool SD, bool WL = false>
+// eight order-5 reconstructions per slot, one thread each (recon5_one)
+template <bool SD, bool WL>
+__global__ void __launch_bounds__(kThreads) recon5_kernel(DeviceState d)
+{
+   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = (int)(t >> 3);
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
+   const int sk = (int)(t & 7);
+   recon5_one<SD, WL>(d, s, sk >> 2, sk & 3);
+}
+
+// PRE: the face states come from recon5_kernel (order 5)
+template <int ORDER, bool JAC, bool SD, bool PRE = false>
 __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,7 +53,7 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    const int4 sl = d.slot[s];
    const double2 nv = d.normal[s];
    double L[4], R[4];
-   if (WL) face_states_w5<SD>(d, sl.x, (sl.w & 1) != 0, s, L, R);
+   if (PRE) face_states_pre(d, s, (sl.w & 1) != 0, L, R);
    else face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
    RoeOut o;
    double lm[16], rm[16];
@@ -296,9 +307,12 @@ void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
       case 3: rhs_face_kernel<1, true, SD><<<b, t, 0, st>>>(d); break;
       case 6: rhs_face_kernel<3, false, SD><<<b, t, 0, st>>>(d); break;
       case 7: rhs_face_kernel<3, true, SD><<<b, t, 0, st>>>(d); break;
-      case 10: rhs_face_kernel<5, false, SD><<<b, t, 0, st>>>(d); break;
+      case 10:
+         if (d.qface) rhs_face_kernel<5, false, SD, true><<<b, t, 0, st>>>(d);
+         else rhs_face_kernel<5, false, SD><<<b, t, 0, st>>>(d);
+         break;
       case 11:
-         if (d.wlin) rhs_face_kernel<5, true, SD, true><<<b, t, 0, st>>>(d);
+         if (d.qface) rhs_face_kernel<5, true, SD, true><<<b, t, 0, st>>>(d);
          else rhs_face_kernel<5, true, SD><<<b, t, 0, st>>>(d);
          break;
       case 62: rhs_face_kernel<31, false, SD><<<b, t, 0, st>>>(d); break;
@@ -308,6 +322,21 @@ void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
    }
 }
 }  // namespace
+
+void launch_recon5(const DeviceState& d, bool keep_lin, cudaStream_t st)
+{
+   if (d.recon != 5 || !d.qface) return;
+   const size_t n = 8 * (size_t)d.nSlot;
+   const int b = (int)((n + kThreads - 1) / kThreads);
+   const bool wl = keep_lin && d.wlin;
+   if (d.face_soft) {
+      if (wl) recon5_kernel<true, true><<<b, kThreads, 0, st>>>(d);
+      else recon5_kernel<true, false><<<b, kThreads, 0, st>>>(d);
+   } else {
+      if (wl) recon5_kernel<false, true><<<b, kThreads, 0, st>>>(d);
+      else recon5_kernel<false, false><<<b, kThreads, 0, st>>>(d);
+   }
+}
 
 void launch_rhs_face(const DeviceState& d, bool jac, cudaStream_t st)
 {

@@ -315,12 +315,12 @@ class GpuSolver:
     def autotune(self, reps: int = 3) -> dict:
         """Pick the fastest launch shapes for the current precision (hamstr_gpu_autotune)."""
         import json
-        buf = ctypes.create_string_buffer(16384)
-        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 16384))
+        buf = ctypes.create_string_buffer(32768)
+        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 32768))
         return json.loads(buf.value.decode())
 
     SHAPE_KEYS = ("face_block", "adi_warps_per_sm", "mx_block", "mx_fused", "face_softdiv", "pivot_softdiv",
-                  "adi_pair", "weno_keep")
+                  "adi_pair", "weno_keep", "adi_thread")
 
     def shape(self) -> dict:
         """The launch shape in use (hamstr_gpu_get_shape), keyed as the autotuner's report."""

@@ -192,9 +192,9 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * precision for each candidate launch shape -- face kernels 128 or 256
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
  * or two per sub-partition, schedules rebuilt longest-job-first), with open
- * chains one per warp or two per warp (one per half); FP32 line kernels
- * 32..128 threads per block, with the blocks assembled by a separate
- * coalesced kernel or inside the factorisation; FP64 divisions of the face
+ * chains one per warp, two per warp (one per half) or one per thread; FP32
+ * line kernels 32..128 threads per block, with the blocks assembled by a
+ * separate coalesced kernel or inside the factorisation; FP64 divisions of the face
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
  * (bit-identical) -- and keeps the fastest.  The state is restored
  * afterwards; results do not depend on the shape.  report (may be NULL)
@@ -213,9 +213,11 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       once per step by the implicit computeRHS and kept for the sweeps
  *       (1 KiB per face slot of device memory): 0 or 1 (default 1; not
  *       tuned by hamstr_gpu_autotune)
+ *   [8] open chains one per thread in the FP64 line kernels (the warps
+ *       keep the periodic chains): 0 or 1
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
  * not depend on the shape. */
-#define HAMSTR_SHAPE_N 8
+#define HAMSTR_SHAPE_N 9
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

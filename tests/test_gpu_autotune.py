@@ -10,7 +10,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     case = make_case(32, 8, order=3, CFL=10.0, msweep=2)
     g = native.GpuSolver(native.Case(case))
     rep = g.autotune(reps=2)
-    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 32
+    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 64
     assert all(c["ms"] > 0 for c in rep["candidates"])
     o = oracle_lib.OracleCase(case, "port")
     for it in range(5):
@@ -19,16 +19,18 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     assert np.array_equal(g.get("q"), o.get("q"))
 
 
-FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_pair=pr)
-               for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for pr in (0, 1)]
+FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_pair=pr, adi_thread=th)
+               for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for pr in (0, 1)
+               for th in (0, 1)]
 
 
-@pytest.mark.parametrize("order", [3, 5])
-def test_every_fp64_shape_is_exact(make_case, oracle_lib, native_lib, order):
-    """Each FP64 launch shape, set explicitly, on a split mesh (open chains
-    of many lengths, periodic chains) against the oracle."""
+@pytest.mark.parametrize("order,split", [(3, 0.5), (5, 0.5), (5, 0.0)])
+def test_every_fp64_shape_is_exact(make_case, oracle_lib, native_lib, order, split):
+    """Each FP64 launch shape, set explicitly, against the oracle: on a split
+    mesh (open chains of many lengths) and on the plain O-grid (periodic
+    loops beside open lines)."""
     from hamstr_oop_gb300 import native
-    case = make_case(24, 8, split=0.5, seed=3, order=order, CFL=5.0, msweep=2)
+    case = make_case(24, 8, split=split, seed=3, order=order, CFL=5.0, msweep=2)
     c = native.Case(case)
     c.set_option("chain_end_rule", 1)
     o = oracle_lib.OracleCase(case, "port")
