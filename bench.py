@@ -498,6 +498,26 @@ def algorithmic_bytes(kernel: str, lay: dict, sizes: dict, order: int) -> float:
     return 0.0
 
 
+def tune_summary(rep: dict) -> dict:
+    """The autotuner's choice, its step time, and the best time with each
+    value of each launch-shape key (what each choice is worth)."""
+    cands = rep["candidates"]
+    out = {"best": rep["best"], "candidates": len(cands), "ms_best": min(c["ms"] for c in cands), "ms_by_value": {}}
+    for k in rep["best"]:
+        vals = sorted({c[k] for c in cands})
+        if len(vals) > 1:
+            out["ms_by_value"][k] = {str(v): round(min(c["ms"] for c in cands if c[k] == v), 4) for v in vals}
+    return out
+
+
+def tune_or_set(gpu, shape: str) -> dict:
+    """Autotune, or set the given launch shape (no tuning)."""
+    if shape:
+        gpu.set_shape(**parse_shape(shape))
+        return {"best": gpu.shape(), "set_by": "--shape"}
+    return tune_summary(gpu.autotune(reps=2))
+
+
 def parse_shape(text: str) -> dict:
     """'key=value,...' into hamstr_gpu_set_shape keywords."""
     out = {}
@@ -540,8 +560,8 @@ def run_gpu(args, wl, rank, local_rank, world):
     hs = torch.cuda.ExternalStream(gpu.stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
-    # launch shapes from the autotuner, then warm-up (W >= 3 steps)
-    tune64 = gpu.autotune(reps=2)
+    # launch shapes from the autotuner (or --shape), then warm-up (W >= 3 steps)
+    tune64 = tune_or_set(gpu, args.shape)
     gpu.enqueue_steps(max(args.warmup, 1))
     gpu.sync()
 
@@ -573,7 +593,7 @@ def run_gpu(args, wl, rank, local_rank, world):
 
     # the mixed-precision form (FP64 residual, FP32 operator) on the same case
     gpu.set_precision(True)
-    tunemx = gpu.autotune(reps=2)
+    tunemx = tune_or_set(gpu, args.shape)
     gpu.enqueue_steps(max(args.warmup, 1))
     gpu.sync()
     mstarts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -642,7 +662,7 @@ def run_gpu(args, wl, rank, local_rank, world):
                  "note": "FP64 residual (bit-identical to the reference), FP32 Jacobians, ADI and linear "
                          "residual; converges to the FP64 steady state (tests/test_gpu_mixed.py)",
                  "kernel_ms_per_step": {k: round(v[0], 4) for k, v in mixed_prof.items()},
-                 "autotune_best": tunemx.get("best")}
+                 "autotune": tunemx}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -654,7 +674,7 @@ def run_gpu(args, wl, rank, local_rank, world):
                        "mesh": mesh_note(wl), "cfl_ramp_before_timing": [list(r) for r in wl["ramp"]],
                        "limiter": LIMITER_NAMES[wl.get("limiter", 0)] if wl["order"] == 3 else None},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-            "mixed_precision": mixed, "converged": conv, "autotune_best": tune64.get("best"),
+            "mixed_precision": mixed, "converged": conv, "autotune": tune64,
             "gpu_launches": gpu.launches_per_step() * args.steps,
             "wall_s_timed_region": wall,
         }
@@ -796,7 +816,7 @@ def main():
     ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
     ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
     ap.add_argument("--msweep", type=int, default=0, help="ADI sweeps per step (default: the workload's, 2)")
-    ap.add_argument("--shape", default="", help="with --profile-steps: launch shape, e.g. "
+    ap.add_argument("--shape", default="", help="launch shape instead of the autotuner's, e.g. "
                     "face_block=128,adi_warps_per_sm=8 (hamstr_gpu_set_shape keys)")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()

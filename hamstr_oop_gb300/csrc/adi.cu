@@ -17,7 +17,9 @@
 // a 4x4 block; in periodic chains half h=0 carries the C' recurrence and
 // half h=1 the fill-in column a' (triSolvers.cpp:877-891), which follow
 // the same instruction sequence.  Open chains need one half only, so the
-// schedule may pair them: two open chains per warp, one per half.
+// schedule may pair them: two open chains per warp, one per half.  Short
+// open chains may also go 32 to a warp, one per lane (a bundle), which
+// spends far fewer warp instructions per row on them.
 //
 // Per-row factor record (80 doubles):
 //   [ 0..15] A_i scaled      (f update in the forward sweep)
@@ -111,14 +113,25 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[0] + w;
-   const int end = d.sched_warp_ptr[g + 1];
+   const int end = d.sched_warp_ptr[g + 1], lane = threadIdx.x & 31;
    for (int job = d.sched_warp_ptr[g]; job < end; job++) {
       const int ich = d.sched_jobs[job];
-      if (ich & kPairJob) {
-         factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], threadIdx.x & 31);
+      if (ich & kBundleJob) {
+         const int n = ich & 63;
+         if (lane < n) {
+            const int c = d.sched_jobs[job + 1 + lane];
+            if (!frozen_chain(d, c)) {
+               const int row0 = d.chain_row0[c];
+               factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c], d.fac + (size_t)kFacRec * row0);
+            }
+         }
+         __syncwarp();
+         job += n;
+      } else if (ich & kPairJob) {
+         factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
          job++;
       } else if (!frozen_chain(d, ich)) {
-         factor_chain<SD>(d, ich, threadIdx.x & 31);
+         factor_chain<SD>(d, ich, lane);
       }
    }
 }
@@ -180,40 +193,28 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wa
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
    const int g = d.sched_warp0[1 + wave] + w;
-   const int end = d.sched_warp_ptr[g + 1];
+   const int end = d.sched_warp_ptr[g + 1], lane = threadIdx.x & 31;
    for (int job = d.sched_warp_ptr[g]; job < end; job++) {
       const int ich = d.sched_jobs[job];
-      if (ich & kPairJob) {
-         solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], threadIdx.x & 31);
+      if (ich & kBundleJob) {
+         const int n = ich & 63;
+         if (lane < n) {
+            const int c = d.sched_jobs[job + 1 + lane];
+            if (!frozen_chain(d, c)) {
+               const int row0 = d.chain_row0[c];
+               solve_line_thread(d.fac + (size_t)kFacRec * row0, d.chain_nrows[c], d.r, d.row_fcell + row0,
+                                 d.row_scell + row0, d.fsc + 4 * (size_t)row0);
+            }
+         }
+         __syncwarp();
+         job += n;
+      } else if (ich & kPairJob) {
+         solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
          job++;
       } else if (!frozen_chain(d, ich)) {
-         solve_chain(d, ich, threadIdx.x & 31);
+         solve_chain(d, ich, lane);
       }
    }
-}
-
-// open chains one per thread, longest first (factor_line_thread)
-template <bool SD>
-__global__ void __launch_bounds__(128) adi_tfactor_kernel(DeviceState d, int first, int count)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= count || halted(d)) return;
-   const int ich = d.sched_thread_jobs[first + t];
-   if (frozen_chain(d, ich)) return;
-   const int row0 = d.chain_row0[ich];
-   factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[ich], d.fac + (size_t)kFacRec * row0);
-}
-
-// one sweep's solve of open chains one per thread (solve_line_thread)
-__global__ void __launch_bounds__(128) adi_tsolve_kernel(DeviceState d, int first, int count)
-{
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= count || halted(d)) return;
-   const int ich = d.sched_thread_jobs[first + t];
-   if (frozen_chain(d, ich)) return;
-   const int row0 = d.chain_row0[ich];
-   solve_line_thread(d.fac + (size_t)kFacRec * row0, d.chain_nrows[ich], d.r, d.row_fcell + row0,
-                     d.row_scell + row0, d.fsc + 4 * (size_t)row0);
 }
 
 }  // namespace
@@ -257,19 +258,6 @@ void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t s
 {
    const int wpb = d.adi_wpb;
    if (nwarps > 0) adi_solve_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, wave, nwarps);
-}
-
-void launch_adi_tfactor(const DeviceState& d, int first, int nthreads, cudaStream_t st)
-{
-   if (nthreads <= 0) return;
-   const int b = (nthreads + 127) / 128;
-   if (d.piv_soft) adi_tfactor_kernel<true><<<b, 128, 0, st>>>(d, first, nthreads);
-   else adi_tfactor_kernel<false><<<b, 128, 0, st>>>(d, first, nthreads);
-}
-
-void launch_adi_tsolve(const DeviceState& d, int first, int nthreads, cudaStream_t st)
-{
-   if (nthreads > 0) adi_tsolve_kernel<<<(nthreads + 127) / 128, 128, 0, st>>>(d, first, nthreads);
 }
 
 }  // namespace hamstr

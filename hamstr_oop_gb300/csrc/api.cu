@@ -110,7 +110,7 @@ struct hamstr_gpu {
 
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
    int adi_pair = 1;                    // open chains two per warp in the FP64 line kernels
-   int adi_thread = 0;                  // open chains one per thread in the FP64 line kernels
+   int adi_bundle = 0;                  // open chains of up to this many rows one per lane (0: none)
    // order 5, FP64: the WENO linearisation's f-only values kept from the
    // implicit computeRHS for the sweeps (d.wlin points here when on)
    double* wlin_buf = nullptr;
@@ -252,26 +252,22 @@ struct hamstr_gpu {
       if ((st = reupload(&d.sched_warp0, sched.warp0, owned))) return st;
       if ((st = reupload(&d.sched_nwarps, sched.nwarps, owned))) return st;
       if ((st = reupload(&d.sched_warp_ptr, sched.warp_ptr, owned))) return st;
-      if ((st = reupload(&d.sched_jobs, sched.jobs, owned))) return st;
-      return reupload(&d.sched_thread_jobs, sched.thread_jobs, owned);
+      return reupload(&d.sched_jobs, sched.jobs, owned);
    }
 
    // the FP64 line kernels of one schedule (0: factorisation, 1 + w: the
    // solve of wave w)
    void adi_factor_launches(int& n)
    {
-      if (sched.nthreads[0] > 0) L("adi_tfactor", n, [&] { launch_adi_tfactor(d, sched.thread0[0], sched.nthreads[0], stream); });
       if (sched.nwarps[0] > 0) L("adi_factor", n, [&] { launch_adi_factor(d, sched.nwarps[0], stream); });
    }
    void adi_solve_launches(int w, int& n)
    {
-      if (sched.nthreads[1 + w] > 0)
-         L("adi_tsolve", n, [&] { launch_adi_tsolve(d, sched.thread0[1 + w], sched.nthreads[1 + w], stream); });
       if (sched.nwarps[1 + w] > 0) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair,
-                   int wkeep, int thread)
+                   int wkeep, int bundle)
    {
       if (wkeep && d.recon == 5) {
          const int st = ensure_wlin();
@@ -289,10 +285,10 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb || pair != adi_pair || thread != adi_thread) {
+      if (adi_wpb != d.adi_wpb || pair != adi_pair || bundle != adi_bundle) {
          adi_pair = pair;
-         adi_thread = thread;
-         sched = build_schedule(plan, adi_wpb * nsm, pair != 0, thread != 0);
+         adi_bundle = bundle;
+         sched = build_schedule(plan, adi_wpb * nsm, pair != 0, bundle);
          const int st = upload_schedule();
          if (st) return st;
       }
@@ -567,10 +563,10 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_soft = 1;
       d.piv_soft = d.mx_fused ? 0 : 1;
       g->nsm = nsm;
-      // open chains one per thread where chains are short (the autotuner
-      // checks both)
-      g->adi_thread = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 1 : 0;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_thread != 0);
+      // the shortest open chains one per lane where chains are short (the
+      // autotuner checks the alternatives)
+      g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 2 : 0;
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_bundle);
    }
    TRY(g->upload_schedule());
    TRY(dalloc(&d.blk, 48 * (size_t)std::max(P.nRow, 1), o));
@@ -767,13 +763,9 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    launch_adi_init(d, g->stream);
    launch_adi_assemble(d, g->stream);
    const Schedule& S = g->sched;
-   launch_adi_tfactor(d, S.thread0[0], S.nthreads[0], g->stream);
    launch_adi_factor(d, S.nwarps[0], g->stream);
    for (int s = 0; s < g->msweep; s++) {
-      for (int w = 0; w < g->plan.nWave; w++) {
-         launch_adi_tsolve(d, S.thread0[1 + w], S.nthreads[1 + w], g->stream);
-         launch_adi_solve(d, w, S.nwarps[1 + w], g->stream);
-      }
+      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, w, S.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
       launch_lin_face(d, g->wlin_valid, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);
@@ -1084,7 +1076,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair, thread; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair, bundle; float ms; };
    const int wk = g->weno_keep;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
@@ -1092,13 +1084,13 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          if (g->mixed) {
             for (int fused : {0, 1})
                for (int mb : {32, 64, 128})
-                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, g->adi_thread, 0.f});
+                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, g->adi_bundle, 0.f});
          } else {
             for (int w : {4, 8})
                for (int psoft : {0, 1})
                   for (int pair : {0, 1})
-                     for (int th : {0, 1})
-                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, th, 0.f});
+                     for (int bu : {0, 2, 4})
+                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, bu, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1111,7 +1103,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk, c.thread))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk, c.bundle))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1133,7 +1125,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, wk,
-                       best->thread);
+                       best->bundle);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1141,17 +1133,17 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          char buf[256];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_thread\": %d, "
+                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_bundle_rows\": %d, "
                        "\"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].pair, cands[i].thread, cands[i].ms);
+                       cands[i].psoft, cands[i].pair, cands[i].bundle, cands[i].ms);
          r += buf;
       }
       char buf[256];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_thread\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, best->thread);
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_bundle_rows\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, best->bundle);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }
@@ -1163,7 +1155,7 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
-                                  d.piv_soft,   g->adi_pair, g->weno_keep, g->adi_thread};
+                                  d.piv_soft,   g->adi_pair, g->weno_keep, g->adi_bundle};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1175,7 +1167,7 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1) &&
-                   (s[7] == 0 || s[7] == 1) && (s[8] == 0 || s[8] == 1);
+                   (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;

@@ -70,7 +70,6 @@ struct DeviceState {
    int *cell_written;
    double* blk;            // per-row assembled blocks A, B, C (scaled, B + I) [nRow][48]
    int *sched_warp0, *sched_nwarps, *sched_warp_ptr, *sched_jobs;   // persistent-warp job lists
-   int* sched_thread_jobs;   // open chains solved one per thread (Schedule::thread_jobs)
    double* fac;            // per-row factor storage
    double* fsc;            // per-row right-hand side / solution scratch [nRow][4]
    double* facN;           // per periodic chain: final LU of the last row (16)
@@ -170,12 +169,9 @@ void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
-// nwarps persistent warps over the warp jobs, then nthreads open chains
-// one per thread from sched_thread_jobs[first..]; either may be 0
+// nwarps persistent warps over their job lists (nwarps may be 0)
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
-void launch_adi_tfactor(const DeviceState& d, int first, int nthreads, cudaStream_t st);
 void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
-void launch_adi_tsolve(const DeviceState& d, int first, int nthreads, cudaStream_t st);
 int adi_configure(int max_dynamic_smem);
 // launcher (forces.cu): per instance k, out[3k..3k+2] = {Fx, Fy, M} over
 // its wall faces wall0[k]..wall0[k+1]-1; scr = 3 doubles per wall face

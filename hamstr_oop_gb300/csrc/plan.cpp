@@ -314,48 +314,58 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, bool thread_open)
+Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows)
 {
    Schedule S;
    S.warp_ptr.push_back(0);
-   auto assign = [&](const std::vector<int>& chains) {
-      // jobs: a periodic chain alone, open chains alone or in pairs of
-      // neighbours in length order (a pair costs its longer chain: both
-      // halves issue the same instructions).  Cost model: rows of FP64
-      // recurrence, periodic rows carrying the fill-in column and the
-      // last-row elimination.
+   // cost model, FP64 warp instructions per row: a warp or a pair of
+   // half-warps on a row (both halves issue the same instructions), a
+   // bundle of up to 32 one-per-lane chains on a row; factorisation and
+   // solve differ (the solve's per-lane form has no block LU)
+   auto assign = [&](const std::vector<int>& chains, bool factor) {
+      const double row_warp = factor ? 42.0 : 29.0, row_bundle = factor ? 274.0 : 92.0;
       std::vector<int> sorted(chains);
       std::stable_sort(sorted.begin(), sorted.end(),
                        [&](int a, int b) { return p.chain_nrows[a] > p.chain_nrows[b]; });
-      struct Job { double cost; int a, b; };
+      struct Job { double cost; std::vector<int> entries; };
       std::vector<Job> order;
+      std::vector<int> bundle;
       int pending = -1;
-      S.thread0.push_back((int)S.thread_jobs.size());
+      auto flush_bundle = [&]() {
+         if (bundle.empty()) return;
+         Job j;
+         j.cost = row_bundle * p.chain_nrows[bundle.front()];   // longest first
+         j.entries.push_back(kBundleJob | (int)bundle.size());
+         j.entries.insert(j.entries.end(), bundle.begin(), bundle.end());
+         order.push_back(j);
+         bundle.clear();
+      };
       for (int c : sorted) {
-         if (thread_open && !p.chain_periodic[c]) S.thread_jobs.push_back(c);
-         else if (p.chain_periodic[c]) order.push_back({1.3 * p.chain_nrows[c], c, -1});
-         else if (!pair_open) order.push_back({(double)p.chain_nrows[c], c, -1});
-         else if (pending < 0) pending = c;
-         else {
-            order.push_back({(double)p.chain_nrows[pending], pending, c});
+         const int n = p.chain_nrows[c];
+         if (p.chain_periodic[c]) {
+            order.push_back({1.3 * row_warp * n, {c}});
+         } else if (n <= bundle_rows) {
+            bundle.push_back(c);
+            if (bundle.size() == 32) flush_bundle();
+         } else if (!pair_open) {
+            order.push_back({row_warp * n, {c}});
+         } else if (pending < 0) {
+            pending = c;
+         } else {
+            order.push_back({row_warp * p.chain_nrows[pending], {pending | kPairJob, c}});
             pending = -1;
          }
       }
-      if (pending >= 0) order.push_back({(double)p.chain_nrows[pending], pending, -1});
+      flush_bundle();
+      if (pending >= 0) order.push_back({row_warp * p.chain_nrows[pending], {pending}});
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
-      S.nthreads.push_back((int)S.thread_jobs.size() - S.thread0.back());
       const int W = std::min((int)order.size(), max_warps);
       std::vector<double> load(W, 0.0);
       std::vector<std::vector<int>> lists(W);
       for (const Job& j : order) {
          const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
          load[w] += j.cost;
-         if (j.b >= 0) {
-            lists[w].push_back(j.a | kPairJob);
-            lists[w].push_back(j.b);
-         } else {
-            lists[w].push_back(j.a);
-         }
+         lists[w].insert(lists[w].end(), j.entries.begin(), j.entries.end());
       }
       S.warp0.push_back((int)S.warp_ptr.size() - 1);
       S.nwarps.push_back(W);
@@ -366,10 +376,10 @@ Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, bool threa
    };
    std::vector<int> all(p.nChain);
    for (int c = 0; c < p.nChain; c++) all[c] = c;
-   assign(all);
+   assign(all, true);
    for (int w = 0; w < p.nWave; w++) {
       std::vector<int> cs(p.wave_chains.begin() + p.wave_ptr[w], p.wave_chains.begin() + p.wave_ptr[w + 1]);
-      assign(cs);
+      assign(cs, false);
    }
    return S;
 }

@@ -73,20 +73,19 @@ std::string build_plan(const MeshInput& in, Plan& out);
 // per SM sub-partition: schedule 0 is the factorisation (all chains),
 // schedule 1+v the solve of wave v.  Warp w of schedule s owns
 // jobs[warp_ptr[warp0[s] + w] .. warp_ptr[warp0[s] + w + 1]) (nwarps[s]
-// may be 0).  With pair_open, open chains of similar length go in pairs,
-// one per half-warp: an entry with kPairJob set is such a chain, and the
-// next entry its partner.  With thread_open, open chains instead go one
-// per thread: thread_jobs[thread0[s] .. thread0[s] + nthreads[s]), longest
-// first, and the warps keep the periodic chains.
+// may be 0).  A job is
+//   - a chain id: the chain on the whole warp;
+//   - (a | kPairJob), b: open chains a and b, one per half-warp (pair_open);
+//   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
+//     bundle_rows rows, one per lane (bundle_rows > 0).
 constexpr int kPairJob = 1 << 30;
+constexpr int kBundleJob = 1 << 29;
 struct Schedule {
    std::vector<int> warp0, nwarps;   // per schedule
    std::vector<int> warp_ptr;        // per global warp, +1
-   std::vector<int> jobs;            // chain ids (| kPairJob: paired with the next)
-   std::vector<int> thread0, nthreads;   // per schedule
-   std::vector<int> thread_jobs;         // chain ids, one per thread
+   std::vector<int> jobs;            // job entries, as above
 };
-Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, bool thread_open);
+Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows);
 
 }  // namespace hamstr
 #endif
