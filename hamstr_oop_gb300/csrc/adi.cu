@@ -29,6 +29,8 @@
 //   [64..79] c_{N-1} at elimination step i (periodic, triSolvers.cpp:967-999)
 // Periodic chains also keep the LU of the final last-row block (facN).
 // ##################################################################
+#include <algorithm>
+
 #include "device_state.h"
 #include "plan.h"
 #include "line_solve.cuh"
@@ -70,6 +72,7 @@ __device__ __forceinline__ double assemble(const DeviceState& d, const int* __re
 __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t < d.sched_nctr) d.sched_ctr[t] = 0;   // the line kernels' job counters, for this step
    if (t >= 48 * d.nRow || halted(d)) return;
    const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
    if (frozen_cell(d, d.row_scell[row])) return;
@@ -105,16 +108,29 @@ __device__ __forceinline__ void factor_pair(const DeviceState& d, int ia, int ib
    factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
 }
 
-// persistent warps, one per SM sub-partition, each with a job list
+// next job index of a persistent warp: lane 0 takes it from the counter
+__device__ __forceinline__ int take_job(int* ctr, int lane)
+{
+   int k = 0;
+   if (lane == 0) k = atomicAdd(ctr, 1);
+   return __shfl_sync(kLaneMask, k, 0);
+}
+
+// persistent warps, one or two per SM sub-partition, taking jobs from the
+// factorisation's queue (longest first) until it is empty
 template <bool SD>
 __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
 {
    if (halted(d)) return;
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
-   const int g = d.sched_warp0[0] + w;
-   const int end = d.sched_warp_ptr[g + 1], lane = threadIdx.x & 31;
-   for (int job = d.sched_warp_ptr[g]; job < end; job++) {
+   const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
+   int* ctr = d.sched_ctr;
+   for (int k = take_job(ctr, lane); k < nj;) {
+      // the next job's index is fetched while this one runs
+      int kn = 0;
+      if (lane == 0) kn = atomicAdd(ctr, 1);
+      const int job = d.sched_job_ptr[j0 + k];
       const int ich = d.sched_jobs[job];
       if (ich & kBundleJob) {
          const int n = ich & 63;
@@ -125,14 +141,12 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
                factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c], d.fac + (size_t)kFacRec * row0);
             }
          }
-         __syncwarp();
-         job += n;
       } else if (ich & kPairJob) {
          factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
-         job++;
       } else if (!frozen_chain(d, ich)) {
          factor_chain<SD>(d, ich, lane);
       }
+      k = __shfl_sync(kLaneMask, kn, 0);
    }
 }
 
@@ -187,14 +201,17 @@ __device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib,
    }
 }
 
-__global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wave, int nwarps)
+__global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sweep, int wave, int nwarps)
 {
    if (halted(d)) return;
    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
    if (w >= nwarps) return;
-   const int g = d.sched_warp0[1 + wave] + w;
-   const int end = d.sched_warp_ptr[g + 1], lane = threadIdx.x & 31;
-   for (int job = d.sched_warp_ptr[g]; job < end; job++) {
+   const int lane = threadIdx.x & 31, nj = d.sched_njobs[1 + wave], j0 = d.sched_job0[1 + wave];
+   int* ctr = d.sched_ctr + 1 + sweep * d.nWave + wave;
+   for (int k = take_job(ctr, lane); k < nj;) {
+      int kn = 0;
+      if (lane == 0) kn = atomicAdd(ctr, 1);
+      const int job = d.sched_job_ptr[j0 + k];
       const int ich = d.sched_jobs[job];
       if (ich & kBundleJob) {
          const int n = ich & 63;
@@ -206,14 +223,12 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int wa
                                  d.row_scell + row0, d.fsc + 4 * (size_t)row0);
             }
          }
-         __syncwarp();
-         job += n;
       } else if (ich & kPairJob) {
          solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
-         job++;
       } else if (!frozen_chain(d, ich)) {
          solve_chain(d, ich, lane);
       }
+      k = __shfl_sync(kLaneMask, kn, 0);
    }
 }
 
@@ -242,7 +257,7 @@ int adi_configure(int max_dynamic_smem)
 
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
 {
-   const int n = 48 * d.nRow;
+   const int n = std::max(48 * d.nRow, d.sched_nctr);
    adi_assemble_kernel<<<(n + 255) / 256, 256, 0, st>>>(d);
 }
 
@@ -254,10 +269,11 @@ void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
    else adi_factor_kernel<false><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
 }
 
-void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st)
+void launch_adi_solve(const DeviceState& d, int sweep, int wave, int nwarps, cudaStream_t st)
 {
    const int wpb = d.adi_wpb;
-   if (nwarps > 0) adi_solve_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, wave, nwarps);
+   if (nwarps > 0)
+      adi_solve_kernel<<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, sweep, wave, nwarps);
 }
 
 }  // namespace hamstr

@@ -211,7 +211,7 @@ struct hamstr_gpu {
       L("adi_assemble", n, [&] { launch_adi_assemble(d, stream); });
       adi_factor_launches(n);
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++) adi_solve_launches(w, n);
+         for (int w = 0; w < plan.nWave; w++) adi_solve_launches(s, w, n);
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
          L("lin_face", n, [&] { launch_lin_face(d, true, stream); });
          L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
@@ -249,9 +249,9 @@ struct hamstr_gpu {
    int upload_schedule()
    {
       int st;
-      if ((st = reupload(&d.sched_warp0, sched.warp0, owned))) return st;
-      if ((st = reupload(&d.sched_nwarps, sched.nwarps, owned))) return st;
-      if ((st = reupload(&d.sched_warp_ptr, sched.warp_ptr, owned))) return st;
+      if ((st = reupload(&d.sched_job0, sched.job0, owned))) return st;
+      if ((st = reupload(&d.sched_njobs, sched.njobs, owned))) return st;
+      if ((st = reupload(&d.sched_job_ptr, sched.job_ptr, owned))) return st;
       return reupload(&d.sched_jobs, sched.jobs, owned);
    }
 
@@ -261,9 +261,9 @@ struct hamstr_gpu {
    {
       if (sched.nwarps[0] > 0) L("adi_factor", n, [&] { launch_adi_factor(d, sched.nwarps[0], stream); });
    }
-   void adi_solve_launches(int w, int& n)
+   void adi_solve_launches(int s, int w, int& n)
    {
-      if (sched.nwarps[1 + w] > 0) L("adi_solve", n, [&] { launch_adi_solve(d, w, sched.nwarps[1 + w], stream); });
+      if (sched.nwarps[1 + w] > 0) L("adi_solve", n, [&] { launch_adi_solve(d, s, w, sched.nwarps[1 + w], stream); });
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair,
@@ -569,6 +569,9 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_bundle);
    }
    TRY(g->upload_schedule());
+   d.nWave = P.nWave;
+   d.sched_nctr = 1 + g->msweep * P.nWave;
+   TRY(dalloc(&d.sched_ctr, (size_t)d.sched_nctr, o));
    TRY(dalloc(&d.blk, 48 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fac, 80 * (size_t)std::max(P.nRow, 1), o));
    TRY(dalloc(&d.fsc, 4 * (size_t)std::max(P.nRow, 1), o));
@@ -765,7 +768,7 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    const Schedule& S = g->sched;
    launch_adi_factor(d, S.nwarps[0], g->stream);
    for (int s = 0; s < g->msweep; s++) {
-      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, w, S.nwarps[1 + w], g->stream);
+      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, s, w, S.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
       launch_lin_face(d, g->wlin_valid, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);

@@ -65,11 +65,14 @@ struct DeviceState {
    double4* refl;
    int *cell_ptr, *cell_ent;
    int *chain_periodic, *chain_nrows, *chain_row0;
+   int nWave;
    int *wave_chains;
    int *row_scell, *row_fcell, *row_ops;
    int *cell_written;
    double* blk;            // per-row assembled blocks A, B, C (scaled, B + I) [nRow][48]
-   int *sched_warp0, *sched_nwarps, *sched_warp_ptr, *sched_jobs;   // persistent-warp job lists
+   int *sched_job0, *sched_njobs, *sched_job_ptr, *sched_jobs;   // persistent-warp job queues (plan.h)
+   int* sched_ctr;         // [sched_nctr = 1 + msweep*nWave] next-job counters: factorisation, then sweep s
+   int sched_nctr;         // wave w at 1 + s*nWave + w; adi_assemble zeroes them
    double* fac;            // per-row factor storage
    double* fsc;            // per-row right-hand side / solution scratch [nRow][4]
    double* facN;           // per periodic chain: final LU of the last row (16)
@@ -169,9 +172,10 @@ void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
-// nwarps persistent warps over their job lists (nwarps may be 0)
+// nwarps persistent warps over the schedule's job queue (nwarps may be 0);
+// the solve of wave `wave` in sweep `sweep` takes counter 1 + sweep*nWave + wave
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st);
-void launch_adi_solve(const DeviceState& d, int wave, int nwarps, cudaStream_t st);
+void launch_adi_solve(const DeviceState& d, int sweep, int wave, int nwarps, cudaStream_t st);
 int adi_configure(int max_dynamic_smem);
 // launcher (forces.cu): per instance k, out[3k..3k+2] = {Fx, Fy, M} over
 // its wall faces wall0[k]..wall0[k+1]-1; scr = 3 doubles per wall face

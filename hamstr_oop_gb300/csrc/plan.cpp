@@ -317,11 +317,11 @@ std::string build_plan(const MeshInput& in, Plan& p)
 Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows)
 {
    Schedule S;
-   S.warp_ptr.push_back(0);
-   // cost model, FP64 warp instructions per row: a warp or a pair of
-   // half-warps on a row (both halves issue the same instructions), a
-   // bundle of up to 32 one-per-lane chains on a row; factorisation and
-   // solve differ (the solve's per-lane form has no block LU)
+   S.job_ptr.push_back(0);
+   // jobs ordered by their FP64 warp instructions (longest first): per row,
+   // a warp or a pair of half-warps (both halves issue the same
+   // instructions) or a bundle of one-per-lane chains; the factorisation's
+   // per-lane form also factors the block, the solve's does not
    auto assign = [&](const std::vector<int>& chains, bool factor) {
       const double row_warp = factor ? 42.0 : 29.0, row_bundle = factor ? 274.0 : 92.0;
       std::vector<int> sorted(chains);
@@ -359,19 +359,12 @@ Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle
       flush_bundle();
       if (pending >= 0) order.push_back({row_warp * p.chain_nrows[pending], {pending}});
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
-      const int W = std::min((int)order.size(), max_warps);
-      std::vector<double> load(W, 0.0);
-      std::vector<std::vector<int>> lists(W);
+      S.job0.push_back((int)S.job_ptr.size() - 1);
+      S.njobs.push_back((int)order.size());
+      S.nwarps.push_back(std::min((int)order.size(), max_warps));
       for (const Job& j : order) {
-         const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-         load[w] += j.cost;
-         lists[w].insert(lists[w].end(), j.entries.begin(), j.entries.end());
-      }
-      S.warp0.push_back((int)S.warp_ptr.size() - 1);
-      S.nwarps.push_back(W);
-      for (int w = 0; w < W; w++) {
-         for (int c : lists[w]) S.jobs.push_back(c);
-         S.warp_ptr.push_back((int)S.jobs.size());
+         S.jobs.insert(S.jobs.end(), j.entries.begin(), j.entries.end());
+         S.job_ptr.push_back((int)S.jobs.size());
       }
    };
    std::vector<int> all(p.nChain);

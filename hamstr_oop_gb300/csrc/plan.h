@@ -69,21 +69,23 @@ struct Plan {
 // Builds the plan; returns "" on success or a description of the problem.
 std::string build_plan(const MeshInput& in, Plan& out);
 
-// Longest-job-first assignment of chains to persistent warps, one warp
-// per SM sub-partition: schedule 0 is the factorisation (all chains),
-// schedule 1+v the solve of wave v.  Warp w of schedule s owns
-// jobs[warp_ptr[warp0[s] + w] .. warp_ptr[warp0[s] + w + 1]) (nwarps[s]
-// may be 0).  A job is
+// Job queues of the persistent FP64 line kernels: schedule 0 is the
+// factorisation (all chains), schedule 1+v the solve of wave v.  Schedule
+// s holds njobs[s] jobs, longest first; job k of it is the entries
+// jobs[job_ptr[job0[s] + k] .. job_ptr[job0[s] + k + 1]).  Each warp takes
+// the next job from a counter in device memory, so the longest jobs start
+// first and no cost model decides which warp runs what.  A job is
 //   - a chain id: the chain on the whole warp;
 //   - (a | kPairJob), b: open chains a and b, one per half-warp (pair_open);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
 //     bundle_rows rows, one per lane (bundle_rows > 0).
+// nwarps[s] = min(njobs[s], max_warps) warps are launched.
 constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;
 struct Schedule {
-   std::vector<int> warp0, nwarps;   // per schedule
-   std::vector<int> warp_ptr;        // per global warp, +1
-   std::vector<int> jobs;            // job entries, as above
+   std::vector<int> job0, njobs, nwarps;   // per schedule
+   std::vector<int> job_ptr;               // per job (all schedules), +1
+   std::vector<int> jobs;                  // job entries, as above
 };
 Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows);
 
