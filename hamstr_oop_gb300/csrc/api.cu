@@ -565,7 +565,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       g->nsm = nsm;
       // the shortest open chains one per lane where chains are short (the
       // autotuner checks the alternatives)
-      g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 2 : 0;
+      g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 8 : 0;
       g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_bundle);
    }
    TRY(g->upload_schedule());
@@ -1092,7 +1092,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
             for (int w : {4, 8})
                for (int psoft : {0, 1})
                   for (int pair : {0, 1})
-                     for (int bu : {0, 2, 4})
+                     for (int bu : {0, 4, 8, 16})
                         cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, bu, 0.f});
          }
       }

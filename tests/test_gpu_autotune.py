@@ -10,7 +10,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     case = make_case(32, 8, order=3, CFL=10.0, msweep=2)
     g = native.GpuSolver(native.Case(case))
     rep = g.autotune(reps=2)
-    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 96
+    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 128
     assert all(c["ms"] > 0 for c in rep["candidates"])
     o = oracle_lib.OracleCase(case, "port")
     for it in range(5):
@@ -22,7 +22,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
 FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_pair=pr,
                     adi_bundle_rows=bu)
                for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for pr in (0, 1)
-               for bu in (0, 2, 64)]
+               for bu in (0, 4, 64)]
 
 
 @pytest.mark.parametrize("order,split", [(3, 0.5), (5, 0.5), (5, 0.0)])
