@@ -213,7 +213,8 @@ struct hamstr_gpu {
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++) adi_solve_launches(s, w, n);
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
-         L("lin_face", n, [&] { launch_lin_face(d, true, stream); });
+         if (d.recon == 5) L("lin_recon5", n, [&] { launch_lin_recon5(d, true, stream); });
+         L("lin_face", n, [&] { launch_lin_face(d, stream); });
          L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
          if (s == msweep - 1) L("norm_final", n, [&] { launch_norm_final(d, 2, false, stream); });
       }
@@ -243,7 +244,7 @@ struct hamstr_gpu {
    int ensure_wlin()
    {
       if (wlin_buf) return HAMSTR_GPU_OK;
-      return dalloc(&wlin_buf, 2 * 4 * 16 * (size_t)std::max(d.nSlot, 1), owned);
+      return dalloc(&wlin_buf, kWlinPerSlot * (size_t)std::max(d.nSlot, 1), owned);
    }
 
    int upload_schedule()
@@ -745,7 +746,8 @@ int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf)
    int st = g->reset_ctl(0.0);
    if (st) return st;
    launch_dtfac(g->d, g->stream);
-   launch_lin_face(g->d, g->wlin_valid, g->stream);
+   launch_lin_recon5(g->d, g->wlin_valid, g->stream);
+   launch_lin_face(g->d, g->stream);
    launch_lin_cell(g->d, false, g->stream);
    launch_norm_final(g->d, 2, false, g->stream);
    CK(cudaGetLastError());
@@ -770,7 +772,8 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    for (int s = 0; s < g->msweep; s++) {
       for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, s, w, S.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
-      launch_lin_face(d, g->wlin_valid, g->stream);
+      launch_lin_recon5(d, g->wlin_valid, g->stream);
+      launch_lin_face(d, g->stream);
       launch_lin_cell(d, s == g->msweep - 1, g->stream);
    }
    g->wlin_valid = false;   // q += dq

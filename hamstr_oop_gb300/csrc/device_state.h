@@ -32,6 +32,8 @@ struct FlowConst {
    double gamma, rinf, uinf, vinf, einf, cfl;
 };
 
+constexpr int kWlinPerSlot = 2 * 4 * 18;   // sides x components x values (recon.cuh Weno5Lin)
+
 struct DeviceState {
    int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
    int recon;              // reconstruction code: order, or 31/32 for MUSCL with a project limiter (recon.cuh)
@@ -52,8 +54,9 @@ struct DeviceState {
    double* qt;             // second state of the RK3 scheme (solnBlock.h:47)
    double *flux, *spec, *ff;
    // order 5, FP64: f-only values of the WENO linearisation, written by the
-   // implicit computeRHS face kernel and read by the sweeps' linear face
-   // kernels of the same step ([2*4*16][nSlot]); null when not kept
+   // implicit computeRHS reconstruction and read by the sweeps' linearised
+   // reconstructions of the same step ([kWlinPerSlot][nSlot]); null when
+   // not kept
    double* wlin;
    // order 5: the two reconstructed states of every slot, [2*4][nSlot]
    // (recon5 kernel, read by the face kernels); null otherwise
@@ -149,8 +152,11 @@ __device__ __forceinline__ int norm_cell(const DeviceState& d)
 void launch_recon5(const DeviceState& d, bool keep_lin, cudaStream_t st);
 void launch_rhs_face(const DeviceState& d, bool jacobian, cudaStream_t st);
 void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st);
-// kept: this step's implicit rhs_face wrote d.wlin from the current q
-void launch_lin_face(const DeviceState& d, bool kept, cudaStream_t st);
+// order 5: the linearised face states into qface ahead of lin_face; kept:
+// this step's implicit recon5 wrote d.wlin from the current q (a no-op at
+// other orders)
+void launch_lin_recon5(const DeviceState& d, bool kept, cudaStream_t st);
+void launch_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 // norms -> d.norms[off], d.norms[off+1] and hist row ctl[1] (when logging);
 // with check_tol, raises the stop flag when L2 <= tol

@@ -309,15 +309,20 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
 // two in sequence, the same operations in the same order.
 template <typename T>
 struct Weno5Lin {
-   T djm1, ejm1, dj, ej, djp1, ejp1, beta0, beta1, beta2, q30, q31, q32, w0, w1, w2, dwd;
+   T cdjm1, cejm1, cdj, cej, cdjp1, cejp1;   // (13/12 * 2) d_k and (0.25 * 2) e_k: the dbeta_k coefficients
+   T beta0, beta1, beta2, bb12;              // smoothness sums with eps; beta1 * beta2
+   T q30, q31, q32;                          // candidate stencils
+   T b2w0, b2w1, b2w2;                       // 1/6 * weights
+   T dwd, dwd2;                              // the weights' common denominator and its square
 };
-constexpr int kWeno5LinVals = 16;
+constexpr int kWeno5LinVals = 18;
+static_assert(2 * 4 * kWeno5LinVals == kWlinPerSlot, "kept WENO values per face slot");
 
 template <typename T>
 __device__ __forceinline__ void weno5_lin_put(const Weno5Lin<T>& p, T* __restrict__ out, size_t stride)
 {
-   const T v[kWeno5LinVals] = {p.djm1, p.ejm1, p.dj, p.ej, p.djp1, p.ejp1, p.beta0, p.beta1,
-                               p.beta2, p.q30, p.q31, p.q32, p.w0, p.w1, p.w2, p.dwd};
+   const T v[kWeno5LinVals] = {p.cdjm1, p.cejm1, p.cdj,  p.cej,  p.cdjp1, p.cejp1, p.beta0, p.beta1, p.beta2,
+                               p.bb12,  p.q30,   p.q31,  p.q32,  p.b2w0,  p.b2w1,  p.b2w2,  p.dwd,   p.dwd2};
 #pragma unroll
    for (int i = 0; i < kWeno5LinVals; i++) out[stride * i] = v[i];
 }
@@ -325,40 +330,47 @@ __device__ __forceinline__ void weno5_lin_put(const Weno5Lin<T>& p, T* __restric
 template <typename T>
 __device__ __forceinline__ Weno5Lin<T> weno5_lin_get(const T* __restrict__ in, size_t stride)
 {
+   T v[kWeno5LinVals];
+#pragma unroll
+   for (int i = 0; i < kWeno5LinVals; i++) v[i] = in[stride * i];
    Weno5Lin<T> p;
-   p.djm1 = in[0];
-   p.ejm1 = in[stride];
-   p.dj = in[2 * stride];
-   p.ej = in[3 * stride];
-   p.djp1 = in[4 * stride];
-   p.ejp1 = in[5 * stride];
-   p.beta0 = in[6 * stride];
-   p.beta1 = in[7 * stride];
-   p.beta2 = in[8 * stride];
-   p.q30 = in[9 * stride];
-   p.q31 = in[10 * stride];
-   p.q32 = in[11 * stride];
-   p.w0 = in[12 * stride];
-   p.w1 = in[13 * stride];
-   p.w2 = in[14 * stride];
-   p.dwd = in[15 * stride];
+   p.cdjm1 = v[0]; p.cejm1 = v[1]; p.cdj = v[2]; p.cej = v[3]; p.cdjp1 = v[4]; p.cejp1 = v[5];
+   p.beta0 = v[6]; p.beta1 = v[7]; p.beta2 = v[8]; p.bb12 = v[9];
+   p.q30 = v[10]; p.q31 = v[11]; p.q32 = v[12];
+   p.b2w0 = v[13]; p.b2w1 = v[14]; p.b2w2 = v[15];
+   p.dwd = v[16]; p.dwd2 = v[17];
    return p;
 }
 
-// the weights from the smoothness sums (eps added) and the sums' common
-// denominator, shared by weno5_lin_pre and weno5_with_lin
+// the f-only values from the differences d_k, e_k, the smoothness sums
+// (eps added) and the candidate stencils; shared by weno5_lin_pre and
+// weno5_with_lin.  Each is an intermediate value of the reference's
+// expressions, formed the same way (b1 * 2 is exact).
 template <typename T, bool SD>
-__device__ __forceinline__ void weno5_lin_weights(Weno5Lin<T>& p)
+__device__ __forceinline__ void weno5_lin_fill(Weno5Lin<T>& p, T djm1, T ejm1, T dj, T ej, T djp1, T ejp1)
 {
+   const T b1 = T(13. / 12.), b2 = T(1. / 6.);
+   const T c1 = b1 * T(2), c2 = T(0.25) * T(2);
+   p.cdjm1 = c1 * djm1;
+   p.cejm1 = c2 * ejm1;
+   p.cdj = c1 * dj;
+   p.cej = c2 * ej;
+   p.cdjp1 = c1 * djp1;
+   p.cejp1 = c2 * ejp1;
    const Dv<T, SD> r1(p.beta1), r2(p.beta2);
    const T d01 = r1.div(p.beta0);
    const T d02 = r2.div(p.beta0);
    const T a1ba0 = T(6.) * d01;
    const T a2ba0 = T(3.) * d02;
-   p.w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
-   p.w1 = a1ba0 * p.w0;
-   p.w2 = T(1.) - p.w0 - p.w1;
+   const T w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
+   const T w1 = a1ba0 * w0;
+   const T w2 = T(1.) - w0 - w1;
+   p.b2w0 = b2 * w0;
+   p.b2w1 = b2 * w1;
+   p.b2w2 = b2 * w2;
+   p.bb12 = p.beta1 * p.beta2;
    p.dwd = p.beta1 * p.beta2 + T(6) * p.beta0 * p.beta2 + T(3) * p.beta0 * p.beta1;
+   p.dwd2 = p.dwd * p.dwd;
 }
 
 template <typename T, bool SD>
@@ -367,26 +379,26 @@ __device__ __forceinline__ Weno5Lin<T> weno5_lin_pre(T a, T b, T c, T d, T e)
    const T epsw = T(1e-10);
    const T b1 = T(13. / 12.);
    Weno5Lin<T> p;
-   p.djm1 = a - T(2.) * b + c;
-   p.ejm1 = a - T(4.) * b + T(3.) * c;
-   p.dj = b - T(2.) * c + d;
-   p.ej = b - d;
-   p.djp1 = c - T(2.) * d + e;
-   p.ejp1 = T(3.) * c - T(4.) * d + e;
-   p.beta0 = b1 * p.djm1 * p.djm1 + T(0.25) * p.ejm1 * p.ejm1 + epsw;
-   p.beta1 = b1 * p.dj * p.dj + T(0.25) * p.ej * p.ej + epsw;
-   p.beta2 = b1 * p.djp1 * p.djp1 + T(0.25) * p.ejp1 * p.ejp1 + epsw;
+   const T djm1 = a - T(2.) * b + c;
+   const T ejm1 = a - T(4.) * b + T(3.) * c;
+   const T dj = b - T(2.) * c + d;
+   const T ej = b - d;
+   const T djp1 = c - T(2.) * d + e;
+   const T ejp1 = T(3.) * c - T(4.) * d + e;
+   p.beta0 = b1 * djm1 * djm1 + T(0.25) * ejm1 * ejm1 + epsw;
+   p.beta1 = b1 * dj * dj + T(0.25) * ej * ej + epsw;
+   p.beta2 = b1 * djp1 * djp1 + T(0.25) * ejp1 * ejp1 + epsw;
    p.q30 = T(2.) * a - T(7.) * b + T(11.) * c;
    p.q31 = -b + T(5.) * c + T(2.) * d;
    p.q32 = T(2.) * c + T(5.) * d - e;
-   weno5_lin_weights<T, SD>(p);
+   weno5_lin_fill<T, SD>(p, djm1, ejm1, dj, ej, djp1, ejp1);
    return p;
 }
 
 template <typename T, bool SD>
 __device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d, T c_d, T d_d, T e_d)
 {
-   const T b1 = T(13. / 12.), b2 = T(1. / 6.);
+   const T b2 = T(1. / 6.);
    const T djm1_d = a_d - T(2.) * b_d + c_d;
    const T ejm1_d = a_d - T(4.) * b_d + T(3.) * c_d;
    const T dj_d = b_d - T(2.) * c_d + d_d;
@@ -396,18 +408,18 @@ __device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d,
    const T q30_d = T(2.) * a_d - T(7.) * b_d + T(11.) * c_d;
    const T q31_d = -b_d + T(5.) * c_d + T(2.) * d_d;
    const T q32_d = T(2.) * c_d + T(5.) * d_d - e_d;
-   const T term1 = b2 * p.w0 * q30_d;
-   const T term2 = b2 * p.w1 * q31_d;
-   const T term3 = b2 * p.w2 * q32_d;
-   const T dbeta0 = b1 * T(2) * p.djm1 * djm1_d + T(0.25) * T(2) * p.ejm1 * ejm1_d;
-   const T dbeta1 = b1 * T(2) * p.dj * dj_d + T(0.25) * T(2) * p.ej * ej_d;
-   const T dbeta2 = b1 * T(2) * p.djp1 * djp1_d + T(0.25) * T(2) * p.ejp1 * ejp1_d;
+   const T term1 = p.b2w0 * q30_d;
+   const T term2 = p.b2w1 * q31_d;
+   const T term3 = p.b2w2 * q32_d;
+   const T dbeta0 = p.cdjm1 * djm1_d + p.cejm1 * ejm1_d;
+   const T dbeta1 = p.cdj * dj_d + p.cej * ej_d;
+   const T dbeta2 = p.cdjp1 * djp1_d + p.cejp1 * ejp1_d;
    const T beta0 = p.beta0, beta1 = p.beta1, beta2 = p.beta2;
    const T dw0_down = p.dwd;
    const T dw0_up_1 = (dbeta1 * beta2 + beta1 * dbeta2) * dw0_down;
-   const T dw0_up_2 = beta1 * beta2 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
-                                       + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
-   const Dv<T, SD> rd(dw0_down * dw0_down);
+   const T dw0_up_2 = p.bb12 * (dbeta1 * beta2 + beta1 * dbeta2 + T(6) * (dbeta0 * beta2 + beta0 * dbeta2)
+                                + T(3) * (dbeta0 * beta1 + beta0 * dbeta1));
+   const Dv<T, SD> rd(p.dwd2);
    const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
    const T dw1_up_1 = T(6) * (dbeta0 * beta2 + beta0 * dbeta2) * dw0_down;
    const T dw1_up_2 = Dv<T, SD>(beta1).div(T(6) * dw0_up_2) * beta0;
@@ -432,15 +444,15 @@ __device__ __forceinline__ double weno5_with_lin(double a, double b, double c, d
                                                  Weno5Lin<double>& p)
 {
    const double b1 = 13. / 12., b2 = 1. / 6.;
-   p.djm1 = a - 2. * b + c;
-   p.ejm1 = a - 4. * b + 3. * c;
-   p.dj = b - 2. * c + d;
-   p.ej = b - d;
-   p.djp1 = c - 2. * d + e;
-   p.ejp1 = 3. * c - 4. * d + e;
-   const double s0 = b1 * p.djm1 * p.djm1 + 0.25 * p.ejm1 * p.ejm1;
-   const double s1 = b1 * p.dj * p.dj + 0.25 * p.ej * p.ej;
-   const double s2 = b1 * p.djp1 * p.djp1 + 0.25 * p.ejp1 * p.ejp1;
+   const double djm1 = a - 2. * b + c;
+   const double ejm1 = a - 4. * b + 3. * c;
+   const double dj = b - 2. * c + d;
+   const double ej = b - d;
+   const double djp1 = c - 2. * d + e;
+   const double ejp1 = 3. * c - 4. * d + e;
+   const double s0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1;
+   const double s1 = b1 * dj * dj + 0.25 * ej * ej;
+   const double s2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1;
    const double dis0 = s0 + 1e-15, dis1 = s1 + 1e-15, dis2 = s2 + 1e-15;
    p.q30 = 2. * a - 7. * b + 11. * c;
    p.q31 = -b + 5. * c + 2. * d;
@@ -455,7 +467,7 @@ __device__ __forceinline__ double weno5_with_lin(double a, double b, double c, d
    p.beta0 = s0 + 1e-10;
    p.beta1 = s1 + 1e-10;
    p.beta2 = s2 + 1e-10;
-   weno5_lin_weights<double, SD>(p);
+   weno5_lin_fill<double, SD>(p, djm1, ejm1, dj, ej, djp1, ejp1);
    return b2 * (w0 * p.q30 + w1 * p.q31 + w2 * p.q32);
 }
 
@@ -566,7 +578,52 @@ __device__ __forceinline__ void recon5_one(const DeviceState& d, int s, int side
    d.qface[(size_t)sk * ns + s] = v;
 }
 
-// the face states recon5_one left for slot s, swapped as face_states does
+// component k of stencil entry idx of the increments dqv, as load_dsten
+// forms it
+__device__ __forceinline__ double dsten_comp(const DeviceState& d, const double* __restrict__ dqv, int idx, int k)
+{
+   const int4 e = d.sten[idx];
+   if (e.y == STEN_CELL) return dqv[4 * (size_t)e.x + k];
+   if (e.y == STEN_WALL) {
+      const double* t = dqv + 4 * (size_t)e.x;
+      if (k == 0 || k == 3) return t[k];
+      const double4 R = d.refl[e.z];
+      const double t1 = t[1], t2 = t[2];
+      return k == 1 ? (t1 * R.x + t2 * R.y) : (t1 * R.z + t2 * R.w);
+   }
+   return 0.0;
+}
+
+// One linearised order-5 face state (computeLinearRHS.cpp:281-315) of
+// slot s into d.qface, like recon5_one: from the f-only values the
+// implicit computeRHS kept (WL) or formed here from q, and the increments
+template <bool SD, bool WL>
+__device__ __forceinline__ void lin_recon5_one(const DeviceState& d, const double* __restrict__ dqv, int s, int side,
+                                               int k)
+{
+   const int n = d.slot[s].x;
+   const size_t ns = (size_t)d.nSlot;
+   const int sk = 4 * side + k;
+   double df[6];
+#pragma unroll
+   for (int j = 0; j < 6; j++) df[j] = dsten_comp(d, dqv, n - 2 + j, k);
+   Weno5Lin<double> p;
+   if (WL) {
+      p = weno5_lin_get(d.wlin + (size_t)(kWeno5LinVals * sk) * ns + s, ns);
+   } else {
+      double f[6];
+#pragma unroll
+      for (int j = 0; j < 6; j++) f[j] = sten_comp(d, n - 2 + j, k);
+      p = side ? weno5_lin_pre<double, SD>(f[5], f[4], f[3], f[2], f[1])
+               : weno5_lin_pre<double, SD>(f[0], f[1], f[2], f[3], f[4]);
+   }
+   const double v = side ? weno5_lin_apply<double, SD>(p, df[5], df[4], df[3], df[2], df[1])
+                         : weno5_lin_apply<double, SD>(p, df[0], df[1], df[2], df[3], df[4]);
+   d.qface[(size_t)sk * ns + s] = v;
+}
+
+// the face states recon5_one (or lin_recon5_one) left for slot s, swapped
+// as face_states does
 __device__ __forceinline__ void face_states_pre(const DeviceState& d, int s, bool swap, double (&L)[4],
                                                 double (&R)[4])
 {
@@ -576,31 +633,6 @@ __device__ __forceinline__ void face_states_pre(const DeviceState& d, int s, boo
       const double qln = d.qface[(size_t)k * ns + s], qrn1 = d.qface[(size_t)(4 + k) * ns + s];
       L[k] = swap ? qln : qrn1;
       R[k] = swap ? qrn1 : qln;
-   }
-}
-
-// face_dstates at order 5 from the kept f-only values (recon5_one with WL
-// on the same q, at d.wlin[(16*(4*side + k) + v) * nSlot + s]): only the
-// increments are gathered
-template <bool SD>
-__device__ __forceinline__ void face_dstates_w5(const DeviceState& d, const double* __restrict__ dqv, int n, bool swap,
-                                                int s, double (&L)[4], double (&R)[4])
-{
-   double df[6][4], qln[4], qrn1[4];
-#pragma unroll
-   for (int j = 0; j < 6; j++) load_dsten<double>(d, dqv, n - 2 + j, df[j]);
-   const size_t ns = (size_t)d.nSlot;
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      const Weno5Lin<double> pl = weno5_lin_get(d.wlin + (size_t)(kWeno5LinVals * k) * ns + s, ns);
-      qln[k] = weno5_lin_apply<double, SD>(pl, df[0][k], df[1][k], df[2][k], df[3][k], df[4][k]);
-      const Weno5Lin<double> pr = weno5_lin_get(d.wlin + (size_t)(kWeno5LinVals * (4 + k)) * ns + s, ns);
-      qrn1[k] = weno5_lin_apply<double, SD>(pr, df[5][k], df[4][k], df[3][k], df[2][k], df[1][k]);
-   }
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      L[k] = swap ? qln[k] : qrn1[k];
-      R[k] = swap ? qrn1[k] : qln[k];
    }
 }
 

@@ -69,15 +69,26 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
    }
 }
 
-// WL: order 5 only, the f-only WENO values kept by this step's rhs_face
-template <int ORDER, bool SD, bool WL = false>
+// eight linearised order-5 reconstructions per slot, one thread each
+template <bool SD, bool WL>
+__global__ void __launch_bounds__(kThreads) lin_recon5_kernel(DeviceState d)
+{
+   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = (int)(t >> 3);
+   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
+   const int sk = (int)(t & 7);
+   lin_recon5_one<SD, WL>(d, d.dq, s, sk >> 2, sk & 3);
+}
+
+// PRE: the linearised states come from lin_recon5_kernel (order 5)
+template <int ORDER, bool SD, bool PRE = false>
 __global__ void __launch_bounds__(kThreads) lin_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    double dL[4], dR[4];
-   if (WL) face_dstates_w5<SD>(d, d.dq, sl.x, (sl.w & 1) != 0, s, dL, dR);
+   if (PRE) face_states_pre(d, s, (sl.w & 1) != 0, dL, dR);
    else face_dstates<ORDER, double, SD>(d, d.dq, sl.x, (sl.w & 1) != 0, dL, dR);
    const double* m = d.ff + 32 * (size_t)(sl.w >> 1);
    double g[4];
@@ -352,7 +363,22 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
    else rhs_cell_kernel<false><<<d.norm_blocks, kThreads, 0, st>>>(d);
 }
 
-void launch_lin_face(const DeviceState& d, bool kept, cudaStream_t st)
+void launch_lin_recon5(const DeviceState& d, bool kept, cudaStream_t st)
+{
+   if (d.recon != 5 || !d.qface) return;
+   const size_t n = 8 * (size_t)d.nSlot;
+   const int b = (int)((n + kThreads - 1) / kThreads);
+   const bool wl = kept && d.wlin;
+   if (d.face_soft) {
+      if (wl) lin_recon5_kernel<true, true><<<b, kThreads, 0, st>>>(d);
+      else lin_recon5_kernel<true, false><<<b, kThreads, 0, st>>>(d);
+   } else {
+      if (wl) lin_recon5_kernel<false, true><<<b, kThreads, 0, st>>>(d);
+      else lin_recon5_kernel<false, false><<<b, kThreads, 0, st>>>(d);
+   }
+}
+
+void launch_lin_face(const DeviceState& d, cudaStream_t st)
 {
    const int kThreads = d.face_block;
    const int b = (d.nSlot + kThreads - 1) / kThreads;
@@ -361,13 +387,9 @@ void launch_lin_face(const DeviceState& d, bool kept, cudaStream_t st)
       case 1: lin_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
       case 3: lin_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;
       case 5:
-         if (kept && d.wlin) {
-            if (d.face_soft) lin_face_kernel<5, true, true><<<b, kThreads, 0, st>>>(d);
-            else lin_face_kernel<5, false, true><<<b, kThreads, 0, st>>>(d);
-         } else {
-            if (d.face_soft) lin_face_kernel<5, true><<<b, kThreads, 0, st>>>(d);
-            else lin_face_kernel<5, false><<<b, kThreads, 0, st>>>(d);
-         }
+         if (d.qface) lin_face_kernel<5, true, true><<<b, kThreads, 0, st>>>(d);
+         else if (d.face_soft) lin_face_kernel<5, true><<<b, kThreads, 0, st>>>(d);
+         else lin_face_kernel<5, false><<<b, kThreads, 0, st>>>(d);
          break;
       case 31: lin_face_kernel<31, true><<<b, kThreads, 0, st>>>(d); break;
       default: lin_face_kernel<32, true><<<b, kThreads, 0, st>>>(d); break;
