@@ -33,14 +33,15 @@ namespace {
 
 constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
-// eight order-5 reconstructions per slot, one thread each (recon5_one)
+// eight order-5 reconstructions per slot, one thread each (recon5_one):
+// blockIdx.y is the state (side * 4 + component), so a warp's loads and
+// stores of the per-state arrays are contiguous
 template <bool SD, bool WL>
 __global__ void __launch_bounds__(kThreads) recon5_kernel(DeviceState d)
 {
-   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-   const int s = (int)(t >> 3);
+   const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
-   const int sk = (int)(t & 7);
+   const int sk = blockIdx.y;
    recon5_one<SD, WL>(d, s, sk >> 2, sk & 3);
 }
 
@@ -70,13 +71,13 @@ __global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
 }
 
 // eight linearised order-5 reconstructions per slot, one thread each
+// (blockIdx.y: the state, as in recon5_kernel)
 template <bool SD, bool WL>
 __global__ void __launch_bounds__(kThreads) lin_recon5_kernel(DeviceState d)
 {
-   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-   const int s = (int)(t >> 3);
+   const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
-   const int sk = (int)(t & 7);
+   const int sk = blockIdx.y;
    lin_recon5_one<SD, WL>(d, d.dq, s, sk >> 2, sk & 3);
 }
 
@@ -337,8 +338,7 @@ void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
 void launch_recon5(const DeviceState& d, bool keep_lin, cudaStream_t st)
 {
    if (d.recon != 5 || !d.qface) return;
-   const size_t n = 8 * (size_t)d.nSlot;
-   const int b = (int)((n + kThreads - 1) / kThreads);
+   const dim3 b((d.nSlot + kThreads - 1) / kThreads, 8);
    const bool wl = keep_lin && d.wlin;
    if (d.face_soft) {
       if (wl) recon5_kernel<true, true><<<b, kThreads, 0, st>>>(d);
@@ -366,8 +366,7 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
 void launch_lin_recon5(const DeviceState& d, bool kept, cudaStream_t st)
 {
    if (d.recon != 5 || !d.qface) return;
-   const size_t n = 8 * (size_t)d.nSlot;
-   const int b = (int)((n + kThreads - 1) / kThreads);
+   const dim3 b((d.nSlot + kThreads - 1) / kThreads, 8);
    const bool wl = kept && d.wlin;
    if (d.face_soft) {
       if (wl) lin_recon5_kernel<true, true><<<b, kThreads, 0, st>>>(d);
