@@ -34,15 +34,14 @@ namespace {
 constexpr int kThreads = 256;
 static_assert(kThreads == kNormBlock, "cell kernels run one norm block per thread block");
 // eight order-5 reconstructions per slot, one thread each (recon5_one):
-// blockIdx.y is the state (side * 4 + component), so a warp's loads and
-// stores of the per-state arrays are contiguous
+// the four components of a slot in adjacent lanes (one 32-byte sector of
+// q per stencil cell), blockIdx.y the side
 template <bool SD, bool WL>
 __global__ void __launch_bounds__(kThreads) recon5_kernel(DeviceState d)
 {
-   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+   const int s = blockIdx.x * (kThreads / 4) + (threadIdx.x >> 2);
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
-   const int sk = blockIdx.y;
-   recon5_one<SD, WL>(d, s, sk >> 2, sk & 3);
+   recon5_one<SD, WL>(d, s, blockIdx.y, threadIdx.x & 3);
 }
 
 // PRE: the face states come from recon5_kernel (order 5)
@@ -338,7 +337,7 @@ void rhs_face_go(const DeviceState& d, bool jac, int b, int t, cudaStream_t st)
 void launch_recon5(const DeviceState& d, bool keep_lin, cudaStream_t st)
 {
    if (d.recon != 5 || !d.qface) return;
-   const dim3 b((d.nSlot + kThreads - 1) / kThreads, 8);
+   const dim3 b((4 * d.nSlot + kThreads - 1) / kThreads, 2);
    const bool wl = keep_lin && d.wlin;
    if (d.face_soft) {
       if (wl) recon5_kernel<true, true><<<b, kThreads, 0, st>>>(d);
