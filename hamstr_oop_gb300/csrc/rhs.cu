@@ -44,9 +44,12 @@ __global__ void __launch_bounds__(kThreads) recon5_kernel(DeviceState d)
    recon5_one<SD, WL>(d, s, blockIdx.y, threadIdx.x & 3);
 }
 
-// PRE: the face states come from recon5_kernel (order 5)
+// PRE: the face states come from recon5_kernel (order 5).  Two blocks per
+// SM at least: the Roe Jacobian is a long chain of dependent FP64
+// operations, and more warps hide more of it than the few spilled
+// registers cost.
 template <int ORDER, bool JAC, bool SD, bool PRE = false>
-__global__ void __launch_bounds__(kThreads) rhs_face_kernel(DeviceState d)
+__global__ void __launch_bounds__(kThreads, 2) rhs_face_kernel(DeviceState d)
 {
    const int s = blockIdx.x * blockDim.x + threadIdx.x;
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;

@@ -136,21 +136,30 @@ __host__ __device__ __forceinline__ Divisor divisor(double b)
    return D;
 }
 
+// the operands the integer path leaves to the `/` operator; kept out of
+// line so that the many inlined divisions of a kernel share one copy of the
+// hardware division sequence
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ double div_other(double a, double b) { return a / b; }
+#else
+inline double div_other(double a, double b) { return a / b; }
+#endif
+
 // a / D.b rounded to nearest even, equal to the `/` operator
 __host__ __device__ __forceinline__ double div(double a, const Divisor& D)
 {
    const uint64_t A = bits(a);
    const int ea = (int)((A >> 52) & 0x7FF);
-   if (!D.ok || ea == 0x7FF) return a / D.b;
+   if (!D.ok || ea == 0x7FF) return div_other(a, D.b);
    const uint64_t sign = (A & 0x8000000000000000ull) ^ D.sign;
    if ((A & 0x7FFFFFFFFFFFFFFFull) == 0) return from_bits(sign);   // +-0 / normal
-   if (ea == 0) return a / D.b;                                     // subnormal dividend
+   if (ea == 0) return div_other(a, D.b);                           // subnormal dividend
    const uint64_t ma = (A & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
    const uint64_t mb = D.d >> 11;
    // quotient significand in [1, 2): scale by 2^54 (ma >= mb) or 2^55
    const int s = ma < mb ? 1 : 0;
    const int e = ea - D.eb + 1023 - s;
-   if (e <= 0) return a / D.b;                                      // subnormal or zero quotient
+   if (e <= 0) return div_other(a, D.b);                            // subnormal or zero quotient
    uint64_t r;
    // floor(ma * 2^(54+s) / mb) = floor(ma * 2^(65+s) / d), numerator (ma << (1+s)) * 2^64
    const uint64_t q = div_2by1(ma << (1 + s), 0, D.d, D.v, r);    // in [2^54, 2^55)
