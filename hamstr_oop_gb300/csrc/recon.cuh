@@ -279,18 +279,18 @@ __device__ __forceinline__ double weno5(double a, double b, double c, double d, 
 {
    const double epsw = 1e-15;
    const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double djm1 = a - 2. * b + c;
-   const double ejm1 = a - 4. * b + 3. * c;
-   const double dj = b - 2. * c + d;
+   const double djm1 = a - p2<1, SD>(b) + c;
+   const double ejm1 = a - p2<2, SD>(b) + 3. * c;
+   const double dj = b - p2<1, SD>(c) + d;
    const double ej = b - d;
-   const double djp1 = c - 2. * d + e;
-   const double ejp1 = 3. * c - 4. * d + e;
-   const double dis0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1 + epsw;
-   const double dis1 = b1 * dj * dj + 0.25 * ej * ej + epsw;
-   const double dis2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1 + epsw;
-   const double q30 = 2. * a - 7. * b + 11. * c;
-   const double q31 = -b + 5. * c + 2. * d;
-   const double q32 = 2. * c + 5. * d - e;
+   const double djp1 = c - p2<1, SD>(d) + e;
+   const double ejp1 = 3. * c - p2<2, SD>(d) + e;
+   const double dis0 = b1 * djm1 * djm1 + p2<-2, SD>(ejm1) * ejm1 + epsw;
+   const double dis1 = b1 * dj * dj + p2<-2, SD>(ej) * ej + epsw;
+   const double dis2 = b1 * djp1 * djp1 + p2<-2, SD>(ejp1) * ejp1 + epsw;
+   const double q30 = p2<1, SD>(a) - 7. * b + 11. * c;
+   const double q31 = -b + 5. * c + p2<1, SD>(d);
+   const double q32 = p2<1, SD>(c) + 5. * d - e;
    const double d01 = Dv<double, SD>(dis1).div(dis0);
    const double d02 = Dv<double, SD>(dis2).div(dis0);
    const double a1ba0 = 6. * d01;
@@ -350,13 +350,13 @@ template <typename T, bool SD>
 __device__ __forceinline__ void weno5_lin_fill(Weno5Lin<T>& p, T djm1, T ejm1, T dj, T ej, T djp1, T ejp1)
 {
    const T b1 = T(13. / 12.), b2 = T(1. / 6.);
-   const T c1 = b1 * T(2), c2 = T(0.25) * T(2);
+   const T c1 = b1 * T(2);   // exact; the e_k coefficients are 0.25 * 2 = 2^-1
    p.cdjm1 = c1 * djm1;
-   p.cejm1 = c2 * ejm1;
+   p.cejm1 = p2<-1, SD>(ejm1);
    p.cdj = c1 * dj;
-   p.cej = c2 * ej;
+   p.cej = p2<-1, SD>(ej);
    p.cdjp1 = c1 * djp1;
-   p.cejp1 = c2 * ejp1;
+   p.cejp1 = p2<-1, SD>(ejp1);
    const Dv<T, SD> r1(p.beta1), r2(p.beta2);
    const T d01 = r1.div(p.beta0);
    const T d02 = r2.div(p.beta0);
@@ -379,18 +379,18 @@ __device__ __forceinline__ Weno5Lin<T> weno5_lin_pre(T a, T b, T c, T d, T e)
    const T epsw = T(1e-10);
    const T b1 = T(13. / 12.);
    Weno5Lin<T> p;
-   const T djm1 = a - T(2.) * b + c;
-   const T ejm1 = a - T(4.) * b + T(3.) * c;
-   const T dj = b - T(2.) * c + d;
+   const T djm1 = a - p2<1, SD>(b) + c;
+   const T ejm1 = a - p2<2, SD>(b) + T(3.) * c;
+   const T dj = b - p2<1, SD>(c) + d;
    const T ej = b - d;
-   const T djp1 = c - T(2.) * d + e;
-   const T ejp1 = T(3.) * c - T(4.) * d + e;
-   p.beta0 = b1 * djm1 * djm1 + T(0.25) * ejm1 * ejm1 + epsw;
-   p.beta1 = b1 * dj * dj + T(0.25) * ej * ej + epsw;
-   p.beta2 = b1 * djp1 * djp1 + T(0.25) * ejp1 * ejp1 + epsw;
-   p.q30 = T(2.) * a - T(7.) * b + T(11.) * c;
-   p.q31 = -b + T(5.) * c + T(2.) * d;
-   p.q32 = T(2.) * c + T(5.) * d - e;
+   const T djp1 = c - p2<1, SD>(d) + e;
+   const T ejp1 = T(3.) * c - p2<2, SD>(d) + e;
+   p.beta0 = b1 * djm1 * djm1 + p2<-2, SD>(ejm1) * ejm1 + epsw;
+   p.beta1 = b1 * dj * dj + p2<-2, SD>(ej) * ej + epsw;
+   p.beta2 = b1 * djp1 * djp1 + p2<-2, SD>(ejp1) * ejp1 + epsw;
+   p.q30 = p2<1, SD>(a) - T(7.) * b + T(11.) * c;
+   p.q31 = -b + T(5.) * c + p2<1, SD>(d);
+   p.q32 = p2<1, SD>(c) + T(5.) * d - e;
    weno5_lin_fill<T, SD>(p, djm1, ejm1, dj, ej, djp1, ejp1);
    return p;
 }
@@ -399,15 +399,15 @@ template <typename T, bool SD>
 __device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d, T c_d, T d_d, T e_d)
 {
    const T b2 = T(1. / 6.);
-   const T djm1_d = a_d - T(2.) * b_d + c_d;
-   const T ejm1_d = a_d - T(4.) * b_d + T(3.) * c_d;
-   const T dj_d = b_d - T(2.) * c_d + d_d;
+   const T djm1_d = a_d - p2<1, SD>(b_d) + c_d;
+   const T ejm1_d = a_d - p2<2, SD>(b_d) + T(3.) * c_d;
+   const T dj_d = b_d - p2<1, SD>(c_d) + d_d;
    const T ej_d = b_d - d_d;
-   const T djp1_d = c_d - T(2.) * d_d + e_d;
-   const T ejp1_d = T(3.) * c_d - T(4.) * d_d + e_d;
-   const T q30_d = T(2.) * a_d - T(7.) * b_d + T(11.) * c_d;
-   const T q31_d = -b_d + T(5.) * c_d + T(2.) * d_d;
-   const T q32_d = T(2.) * c_d + T(5.) * d_d - e_d;
+   const T djp1_d = c_d - p2<1, SD>(d_d) + e_d;
+   const T ejp1_d = T(3.) * c_d - p2<2, SD>(d_d) + e_d;
+   const T q30_d = p2<1, SD>(a_d) - T(7.) * b_d + T(11.) * c_d;
+   const T q31_d = -b_d + T(5.) * c_d + p2<1, SD>(d_d);
+   const T q32_d = p2<1, SD>(c_d) + T(5.) * d_d - e_d;
    const T term1 = p.b2w0 * q30_d;
    const T term2 = p.b2w1 * q31_d;
    const T term3 = p.b2w2 * q32_d;
@@ -444,19 +444,19 @@ __device__ __forceinline__ double weno5_with_lin(double a, double b, double c, d
                                                  Weno5Lin<double>& p)
 {
    const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double djm1 = a - 2. * b + c;
-   const double ejm1 = a - 4. * b + 3. * c;
-   const double dj = b - 2. * c + d;
+   const double djm1 = a - p2<1, SD>(b) + c;
+   const double ejm1 = a - p2<2, SD>(b) + 3. * c;
+   const double dj = b - p2<1, SD>(c) + d;
    const double ej = b - d;
-   const double djp1 = c - 2. * d + e;
-   const double ejp1 = 3. * c - 4. * d + e;
-   const double s0 = b1 * djm1 * djm1 + 0.25 * ejm1 * ejm1;
-   const double s1 = b1 * dj * dj + 0.25 * ej * ej;
-   const double s2 = b1 * djp1 * djp1 + 0.25 * ejp1 * ejp1;
+   const double djp1 = c - p2<1, SD>(d) + e;
+   const double ejp1 = 3. * c - p2<2, SD>(d) + e;
+   const double s0 = b1 * djm1 * djm1 + p2<-2, SD>(ejm1) * ejm1;
+   const double s1 = b1 * dj * dj + p2<-2, SD>(ej) * ej;
+   const double s2 = b1 * djp1 * djp1 + p2<-2, SD>(ejp1) * ejp1;
    const double dis0 = s0 + 1e-15, dis1 = s1 + 1e-15, dis2 = s2 + 1e-15;
-   p.q30 = 2. * a - 7. * b + 11. * c;
-   p.q31 = -b + 5. * c + 2. * d;
-   p.q32 = 2. * c + 5. * d - e;
+   p.q30 = p2<1, SD>(a) - 7. * b + 11. * c;
+   p.q31 = -b + 5. * c + p2<1, SD>(d);
+   p.q32 = p2<1, SD>(c) + 5. * d - e;
    const double d01 = Dv<double, SD>(dis1).div(dis0);
    const double d02 = Dv<double, SD>(dis2).div(dis0);
    const double a1ba0 = 6. * d01;

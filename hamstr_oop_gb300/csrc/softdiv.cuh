@@ -174,7 +174,44 @@ __host__ __device__ __forceinline__ double div(double a, const Divisor& D)
 
 __host__ __device__ __forceinline__ double div(double a, double b) { return div(a, divisor(b)); }
 
+// x * 2^K on the integer pipes: for a normal x whose product stays normal
+// the exponent field moves by K and the significand is unchanged, which is
+// exactly the rounded product; zeros stay; anything else (subnormal,
+// infinite, NaN, a product that overflows or turns subnormal) goes to the
+// multiply.  Equal to x * 2^K for every x.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ double mul_other(double x, double s) { return x * s; }
+#else
+inline double mul_other(double x, double s) { return x * s; }
+#endif
+
+template <int K>
+__host__ __device__ __forceinline__ double scale2(double x)
+{
+   constexpr double kScale = K >= 0 ? double(1ull << (K >= 0 ? K : 0)) : 1.0 / double(1ull << (K < 0 ? -K : 0));
+   const uint64_t u = bits(x);
+   const int e = (int)((u >> 52) & 0x7FF);
+   if (e >= 1 && e <= 0x7FE && e + K >= 1 && e + K <= 0x7FE) return from_bits(u + (uint64_t)((int64_t)K << 52));
+   if ((u << 1) == 0) return x;   // +-0
+   return mul_other(x, kScale);
+}
+
 }  // namespace sd
+
+// x * 2^K in the reconstructions: with SOFT (FP64 only) on the integer
+// pipes (sd::scale2, identical results), otherwise the multiply
+template <int K, bool SOFT>
+__host__ __device__ __forceinline__ double p2(double x)
+{
+   constexpr double kScale = K >= 0 ? double(1ull << (K >= 0 ? K : 0)) : 1.0 / double(1ull << (K < 0 ? -K : 0));
+   return SOFT ? sd::scale2<K>(x) : kScale * x;
+}
+template <int K, bool SOFT>
+__host__ __device__ __forceinline__ float p2(float x)
+{
+   constexpr float kScale = K >= 0 ? float(1u << (K >= 0 ? K : 0)) : 1.0f / float(1u << (K < 0 ? -K : 0));
+   return kScale * x;
+}
 
 // Division by one divisor, possibly several times: in FP64 with SOFT the
 // correctly rounded integer-pipe division above (identical results to `/`,

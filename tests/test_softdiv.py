@@ -96,3 +96,46 @@ def test_softdiv_matches_the_device_division(native_lib):
     assert np.sum((sb != hb) & ~nan) == 0
     # and the host's IEEE division agrees too
     assert np.array_equal(hb, (a / b).view(np.uint64)) or np.sum(hb != (a / b).view(np.uint64)) == 0
+
+
+SCALE_PROGRAM = r"""
+#include "softdiv.cuh"
+#include <cstdio>
+#include <random>
+using namespace hamstr::sd;
+template <int K> long check(double x, double s) {
+   const double w = x * s, g = scale2<K>(x);
+   return (bits(w) != bits(g) && !(w != w && g != g)) ? 1 : 0;
+}
+int main() {
+   std::mt19937_64 rng(2);
+   long bad = 0, n = 0;
+   for (long i = 0; i < 4000000; i++) {
+      uint64_t u = rng();
+      const int mode = (int)(i % 8);
+      if (mode == 0) u &= 0x800FFFFFFFFFFFFFull;                 // zeros and subnormals
+      if (mode == 1) u = (u & 0x800FFFFFFFFFFFFFull) | (1ull << 52) * (1 + rng() % 3);   // near the bottom
+      if (mode == 2) u = (u & 0x800FFFFFFFFFFFFFull) | (0x7FEull - rng() % 3) << 52;   // near the top
+      if (mode == 3) u = (u & 0x800FFFFFFFFFFFFFull) | 0x7FF0000000000000ull;          // inf, NaN
+      if (mode == 4) u &= 0x8000000000000000ull;                 // +-0
+      const double x = from_bits(u);
+      bad += check<1>(x, 2.0) + check<2>(x, 4.0) + check<-1>(x, 0.5) + check<-2>(x, 0.25);
+      n += 4;
+   }
+   printf("%ld %ld\n", bad, n);
+   return bad != 0;
+}
+"""
+
+
+def test_scale2_matches_the_multiply_on_the_host(tmp_path):
+    """x * 2^K on the integer pipes equals the FP64 multiply for every
+    class of x (normal, near the exponent limits, subnormal, zero, inf, NaN)."""
+    src = tmp_path / "s.cpp"
+    src.write_text(SCALE_PROGRAM)
+    exe = tmp_path / "s"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    bad, n = (int(x) for x in out.stdout.split())
+    assert out.returncode == 0 and bad == 0 and n == 16000000
