@@ -52,13 +52,13 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const Dv<double, SD> by_rol(rol);
    const double ul = by_rol.div(ql[1]);
    const double vl = by_rol.div(ql[2]);
-   const double pl = gm1 * (ql[3] - 0.5 * rol * (ul * ul + vl * vl));
+   const double pl = gm1 * (ql[3] - p2<-1, SD>(rol) * (ul * ul + vl * vl));
    const double hl = by_rol.div(ql[3] + pl);
    const double ror = qr[0];
    const Dv<double, SD> by_ror(ror);
    const double ur = by_ror.div(qr[1]);
    const double vr = by_ror.div(qr[2]);
-   const double pr = gm1 * (qr[3] - 0.5 * ror * (ur * ur + vr * vr));
+   const double pr = gm1 * (qr[3] - p2<-1, SD>(ror) * (ur * ur + vr * vr));
    const double hr = by_ror.div(qr[3] + pr);
    const double dp = pr - pl;
    const double uconr = ur * nx + vr * ny;
@@ -72,7 +72,7 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double ubar = ul * A + ur * B;
    const double vbar = vl * A + vr * B;
    const double hbar = hl * A + hr * B;
-   double cbar = gm1 * (hbar - 0.5 * (ubar * ubar + vbar * vbar));
+   double cbar = gm1 * (hbar - p2<-1, SD>(ubar * ubar + vbar * vbar));
    cbar = sqrt(cbar);
    const Dv<double, SD> by_c(cbar);
    const double uconbar = ubar * nx + vbar * ny;
@@ -83,8 +83,8 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
       const double eig3 = fabs(uconbar - cbar);
       double spec = eig1 + cbar;
       if (spec != spec) return false;
-      const double term1 = -eig1 + 0.5 * (eig2 + eig3);
-      const double term2 = 0.5 * (eig2 - eig3);
+      const double term1 = -eig1 + p2<-1, SD>(eig2 + eig3);
+      const double term2 = p2<-1, SD>(eig2 - eig3);
       const double del1 = by_c.div(by_c.div(term1 * dp)) + by_c.div(term2 * robar * (uconr - uconl));
       const double del2 = term1 * (uconr - uconl) * robar + by_c.div(term2 * dp);
       double fm0 = eig1 * (qr[0] - ql[0]);
@@ -99,10 +99,10 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
       const double fl1 = rol * uconl * ul + nx * pl, fr1 = ror * uconr * ur + nx * pr;
       const double fl2 = rol * uconl * vl + ny * pl, fr2 = ror * uconr * vr + ny * pr;
       const double fl3 = (ql[3] + pl) * uconl, fr3 = (qr[3] + pr) * uconr;
-      o.flux[0] = 0.5 * (fl0 + fr0 - fm0);
-      o.flux[1] = 0.5 * (fl1 + fr1 - fm1);
-      o.flux[2] = 0.5 * (fl2 + fr2 - fm2);
-      o.flux[3] = 0.5 * (fl3 + fr3 - fm3);
+      o.flux[0] = p2<-1, SD>(fl0 + fr0 - fm0);
+      o.flux[1] = p2<-1, SD>(fl1 + fr1 - fm1);
+      o.flux[2] = p2<-1, SD>(fl2 + fr2 - fm2);
+      o.flux[3] = p2<-1, SD>(fl3 + fr3 - fm3);
       o.flux[0] *= area;
       o.flux[1] *= area;
       o.flux[2] *= area;
@@ -121,8 +121,8 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double e1 = fabs(uconbarj);
    const double e2 = fabs(uconbarj + cbar);
    const double e3 = fabs(uconbarj - cbar);
-   const double t1 = -e1 + 0.5 * (e2 + e3);
-   const double t2 = 0.5 * (e2 - e3);
+   const double t1 = -e1 + p2<-1, SD>(e2 + e3);
+   const double t2 = p2<-1, SD>(e2 - e3);
    const double t2rb = t2 * robar;
 
    // derivative vectors, kept components {rho, rho u, rho v, E}
@@ -130,7 +130,7 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double du0l = by_rol.div(-ul);
    const double irl = by_rol.div(1.0);
    const double dv0l = by_rol.div(-vl);
-   const double dp0l = 0.5 * gm1 * (ul * ul + vl * vl);
+   const double dp0l = p2<-1, SD>(gm1) * (ul * ul + vl * vl);
    const double dp1l = -gm1 * ul;
    const double dp2l = -gm1 * vl;
    const double dc0l = by_rol.div(-uconlj);
@@ -140,7 +140,7 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
    const double du0r = by_ror.div(-ur);
    const double irr = by_ror.div(1.0);
    const double dv0r = by_ror.div(-vr);
-   const double dp0r = 0.5 * gm1 * (ur * ur + vr * vr);
+   const double dp0r = p2<-1, SD>(gm1) * (ur * ur + vr * vr);
    const double dp1r = -gm1 * ur;
    const double dp2r = -gm1 * vr;
    const double dc0r = by_ror.div(-uconrj);
@@ -225,8 +225,8 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
                mr = D1r[c] * rowc[rI] + D2r[c] * rown[rI];
             }
          }
-         lm[4 * rI + c] = 0.5 * (L1[4 * rI + c] - ml) * area;
-         rm[4 * rI + c] = 0.5 * (R1[4 * rI + c] - mr) * area;
+         lm[4 * rI + c] = p2<-1, SD>(L1[4 * rI + c] - ml) * area;
+         rm[4 * rI + c] = p2<-1, SD>(R1[4 * rI + c] - mr) * area;
       }
    }
    return true;
