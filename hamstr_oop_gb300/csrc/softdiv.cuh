@@ -196,7 +196,61 @@ __host__ __device__ __forceinline__ double scale2(double x)
    return mul_other(x, kScale);
 }
 
+// a * b rounded to nearest even on the integer pipes, equal to the FP64
+// multiply: for normal operands with a normal product the 53-bit
+// significands multiply exactly in 128 bits (each shifted to the top of a
+// 64-bit word), the top 53 bits round on the next bit and the OR of the
+// rest; a zero times a zero or a normal number is a signed zero; anything
+// else (subnormal, infinite or NaN operands, a product that overflows or
+// turns subnormal) goes to the multiply.
+__host__ __device__ __forceinline__ double mul(double a, double b)
+{
+   constexpr uint64_t kMant = 0xFFFFFFFFFFFFFull, kHidden = 0x10000000000000ull;
+   const uint64_t ua = bits(a), ub = bits(b);
+   const uint64_t sign = (ua ^ ub) & 0x8000000000000000ull;
+   const int ea = (int)((ua >> 52) & 0x7FF), eb = (int)((ub >> 52) & 0x7FF);
+   const bool na = (unsigned)(ea - 1) < 0x7FEu, nb = (unsigned)(eb - 1) < 0x7FEu;
+   if (!na || !nb) {
+      const bool za = (ua << 1) == 0, zb = (ub << 1) == 0;
+      if ((za && (zb || nb)) || (zb && na)) return from_bits(sign);
+      return mul_other(a, b);
+   }
+   int e = ea + eb - 1023;   // biased exponent of a product in [1, 2)
+   const uint64_t A = ((ua & kMant) | kHidden) << 11, B = ((ub & kMant) | kHidden) << 11;
+   uint64_t hi = mulhi(A, B), lo = A * B;
+   if (hi >> 63) {
+      e += 1;
+   } else {
+      hi = (hi << 1) | (lo >> 63);
+      lo <<= 1;
+   }
+   if (e < 1) return mul_other(a, b);   // subnormal or zero product
+   uint64_t m = hi >> 11;
+   const uint64_t g = (hi >> 10) & 1;
+   const bool st = ((hi & 0x3FF) | lo) != 0;
+   if (g && (st || (m & 1))) m = m + 1;
+   if (m >> 53) {
+      m >>= 1;
+      e += 1;
+   }
+   if (e > 0x7FE) return mul_other(a, b);   // overflow
+   return from_bits(sign | ((uint64_t)e << 52) | (m & kMant));
+}
+
 }  // namespace sd
+
+// a * b in the reconstructions and fluxes: with SOFT (FP64) on the integer
+// pipes (sd::mul, identical results), otherwise the multiply
+template <bool SOFT>
+__host__ __device__ __forceinline__ double pm(double a, double b)
+{
+   return SOFT ? sd::mul(a, b) : a * b;
+}
+template <bool SOFT>
+__host__ __device__ __forceinline__ float pm(float a, float b)
+{
+   return a * b;
+}
 
 // x * 2^K in the reconstructions: with SOFT (FP64 only) on the integer
 // pipes (sd::scale2, identical results), otherwise the multiply

@@ -139,3 +139,57 @@ def test_scale2_matches_the_multiply_on_the_host(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     bad, n = (int(x) for x in out.stdout.split())
     assert out.returncode == 0 and bad == 0 and n == 16000000
+
+
+MUL_PROGRAM = r"""
+#include "softdiv.cuh"
+#include <cstdio>
+#include <random>
+using namespace hamstr::sd;
+int main() {
+   std::mt19937_64 rng(3);
+   long bad = 0, n = 0;
+   auto rnd = [&](int emin, int emax) {
+      uint64_t m = rng() & 0xFFFFFFFFFFFFFull;
+      const int e = emin + (int)(rng() % (uint64_t)(emax - emin + 1));
+      const uint64_t s = rng() & 0x8000000000000000ull, k = rng() % 16;
+      if (k == 0) m = 0;
+      if (k == 1) m = 0xFFFFFFFFFFFFFull;
+      if (k == 2) m = rng() & 0xFFull;
+      if (k == 3) m = 0xFFFFFFFFFFFFFull - (rng() & 0xFF);
+      if (k == 4) m = (rng() & 0xFFFFFFFull) << 24;
+      return from_bits(s | ((uint64_t)e << 52) | m);
+   };
+   for (long i = 0; i < 30000000; i++) {
+      double a, b;
+      const int mode = (int)(i % 6);
+      if (mode == 0) { a = rnd(1000, 1046); b = rnd(1000, 1046); }
+      else if (mode == 1) { a = rnd(1, 2046); b = rnd(1, 2046); }
+      else if (mode == 2) { a = rnd(1, 60); b = rnd(960, 1023); }              // products near the subnormal edge
+      else if (mode == 3) { a = rnd(1500, 2046); b = rnd(1023, 1100); }        // near overflow
+      else if (mode == 4) { a = rnd(0, 0); b = rnd(900, 1100); }              // zeros and subnormals
+      else { a = rnd(1020, 1026); b = from_bits(bits(1.0) + (rng() & 0xFF)); }
+      if (i % 89 == 0) a = (i % 2) ? 0.0 : -0.0;
+      if (i % 97 == 0) b = from_bits(0x7FF0000000000000ull | (rng() & 1));   // inf or NaN
+      const double w = a * b, g = mul(a, b);
+      n++;
+      if (bits(w) != bits(g) && !(w != w && g != g)) bad++;
+   }
+   printf("%ld %ld\n", bad, n);
+   return bad != 0;
+}
+"""
+
+
+def test_soft_multiply_matches_the_multiply_on_the_host(tmp_path):
+    """The integer-pipe FP64 multiply equals IEEE multiplication (round to
+    nearest even) for normal, boundary, zero, subnormal, infinite and NaN
+    operands."""
+    src = tmp_path / "m.cpp"
+    src.write_text(MUL_PROGRAM)
+    exe = tmp_path / "m"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    bad, n = (int(x) for x in out.stdout.split())
+    assert out.returncode == 0 and bad == 0 and n == 30000000
