@@ -348,31 +348,35 @@ __device__ __forceinline__ Weno5Lin<T> weno5_lin_get(const T* __restrict__ in, s
 // (eps added) and the candidate stencils; shared by weno5_lin_pre and
 // weno5_with_lin.  Each is an intermediate value of the reference's
 // expressions, formed the same way (b1 * 2 is exact).
+// The multiplies of the linearisation stay on the FP64 pipe (the integer
+// pipes already carry its divisions; measured slower with both there)
+constexpr bool kLinSoftMul = false;
+
 template <typename T, bool SD>
 __device__ __forceinline__ void weno5_lin_fill(Weno5Lin<T>& p, T djm1, T ejm1, T dj, T ej, T djp1, T ejp1)
 {
    const T b1 = T(13. / 12.), b2 = T(1. / 6.);
    const T c1 = b1 * T(2);   // exact; the e_k coefficients are 0.25 * 2 = 2^-1
-   p.cdjm1 = pm<SD>(c1, djm1);
+   p.cdjm1 = pm<kLinSoftMul>(c1, djm1);
    p.cejm1 = p2<-1, SD>(ejm1);
-   p.cdj = pm<SD>(c1, dj);
+   p.cdj = pm<kLinSoftMul>(c1, dj);
    p.cej = p2<-1, SD>(ej);
-   p.cdjp1 = pm<SD>(c1, djp1);
+   p.cdjp1 = pm<kLinSoftMul>(c1, djp1);
    p.cejp1 = p2<-1, SD>(ejp1);
    const Dv<T, SD> r1(p.beta1), r2(p.beta2);
    const T d01 = r1.div(p.beta0);
    const T d02 = r2.div(p.beta0);
-   const T a1ba0 = pm<SD>(T(6.), d01);
-   const T a2ba0 = pm<SD>(T(3.), d02);
+   const T a1ba0 = pm<kLinSoftMul>(T(6.), d01);
+   const T a2ba0 = pm<kLinSoftMul>(T(3.), d02);
    const T w0 = Dv<T, SD>(T(1.0) + a1ba0 + a2ba0).div(T(1.0));
-   const T w1 = pm<SD>(a1ba0, w0);
+   const T w1 = pm<kLinSoftMul>(a1ba0, w0);
    const T w2 = T(1.) - w0 - w1;
-   p.b2w0 = pm<SD>(b2, w0);
-   p.b2w1 = pm<SD>(b2, w1);
-   p.b2w2 = pm<SD>(b2, w2);
-   p.bb12 = pm<SD>(p.beta1, p.beta2);
-   p.dwd = p.bb12 + pm<SD>(pm<SD>(T(6), p.beta0), p.beta2) + pm<SD>(pm<SD>(T(3), p.beta0), p.beta1);
-   p.dwd2 = pm<SD>(p.dwd, p.dwd);
+   p.b2w0 = pm<kLinSoftMul>(b2, w0);
+   p.b2w1 = pm<kLinSoftMul>(b2, w1);
+   p.b2w2 = pm<kLinSoftMul>(b2, w2);
+   p.bb12 = pm<kLinSoftMul>(p.beta1, p.beta2);
+   p.dwd = p.bb12 + pm<kLinSoftMul>(pm<kLinSoftMul>(T(6), p.beta0), p.beta2) + pm<kLinSoftMul>(pm<kLinSoftMul>(T(3), p.beta0), p.beta1);
+   p.dwd2 = pm<kLinSoftMul>(p.dwd, p.dwd);
 }
 
 template <typename T, bool SD>
@@ -381,19 +385,19 @@ __device__ __forceinline__ Weno5Lin<T> weno5_lin_pre(T a, T b, T c, T d, T e)
    const T epsw = T(1e-10);
    const T b1 = T(13. / 12.);
    Weno5Lin<T> p;
-   const T c3 = pm<SD>(T(3.), c);
+   const T c3 = pm<kLinSoftMul>(T(3.), c);
    const T djm1 = a - p2<1, SD>(b) + c;
    const T ejm1 = a - p2<2, SD>(b) + c3;
    const T dj = b - p2<1, SD>(c) + d;
    const T ej = b - d;
    const T djp1 = c - p2<1, SD>(d) + e;
    const T ejp1 = c3 - p2<2, SD>(d) + e;
-   p.beta0 = pm<SD>(pm<SD>(b1, djm1), djm1) + pm<SD>(p2<-2, SD>(ejm1), ejm1) + epsw;
-   p.beta1 = pm<SD>(pm<SD>(b1, dj), dj) + pm<SD>(p2<-2, SD>(ej), ej) + epsw;
-   p.beta2 = pm<SD>(pm<SD>(b1, djp1), djp1) + pm<SD>(p2<-2, SD>(ejp1), ejp1) + epsw;
-   p.q30 = p2<1, SD>(a) - pm<SD>(T(7.), b) + pm<SD>(T(11.), c);
-   p.q31 = -b + pm<SD>(T(5.), c) + p2<1, SD>(d);
-   p.q32 = p2<1, SD>(c) + pm<SD>(T(5.), d) - e;
+   p.beta0 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djm1), djm1) + pm<kLinSoftMul>(p2<-2, SD>(ejm1), ejm1) + epsw;
+   p.beta1 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, dj), dj) + pm<kLinSoftMul>(p2<-2, SD>(ej), ej) + epsw;
+   p.beta2 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djp1), djp1) + pm<kLinSoftMul>(p2<-2, SD>(ejp1), ejp1) + epsw;
+   p.q30 = p2<1, SD>(a) - pm<kLinSoftMul>(T(7.), b) + pm<kLinSoftMul>(T(11.), c);
+   p.q31 = -b + pm<kLinSoftMul>(T(5.), c) + p2<1, SD>(d);
+   p.q32 = p2<1, SD>(c) + pm<kLinSoftMul>(T(5.), d) - e;
    weno5_lin_fill<T, SD>(p, djm1, ejm1, dj, ej, djp1, ejp1);
    return p;
 }
@@ -402,39 +406,39 @@ template <typename T, bool SD>
 __device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d, T c_d, T d_d, T e_d)
 {
    const T b2 = T(1. / 6.);
-   const T c3 = pm<SD>(T(3.), c_d);
+   const T c3 = pm<kLinSoftMul>(T(3.), c_d);
    const T djm1_d = a_d - p2<1, SD>(b_d) + c_d;
    const T ejm1_d = a_d - p2<2, SD>(b_d) + c3;
    const T dj_d = b_d - p2<1, SD>(c_d) + d_d;
    const T ej_d = b_d - d_d;
    const T djp1_d = c_d - p2<1, SD>(d_d) + e_d;
    const T ejp1_d = c3 - p2<2, SD>(d_d) + e_d;
-   const T q30_d = p2<1, SD>(a_d) - pm<SD>(T(7.), b_d) + pm<SD>(T(11.), c_d);
-   const T q31_d = -b_d + pm<SD>(T(5.), c_d) + p2<1, SD>(d_d);
-   const T q32_d = p2<1, SD>(c_d) + pm<SD>(T(5.), d_d) - e_d;
-   const T term1 = pm<SD>(p.b2w0, q30_d);
-   const T term2 = pm<SD>(p.b2w1, q31_d);
-   const T term3 = pm<SD>(p.b2w2, q32_d);
-   const T dbeta0 = pm<SD>(p.cdjm1, djm1_d) + pm<SD>(p.cejm1, ejm1_d);
-   const T dbeta1 = pm<SD>(p.cdj, dj_d) + pm<SD>(p.cej, ej_d);
-   const T dbeta2 = pm<SD>(p.cdjp1, djp1_d) + pm<SD>(p.cejp1, ejp1_d);
+   const T q30_d = p2<1, SD>(a_d) - pm<kLinSoftMul>(T(7.), b_d) + pm<kLinSoftMul>(T(11.), c_d);
+   const T q31_d = -b_d + pm<kLinSoftMul>(T(5.), c_d) + p2<1, SD>(d_d);
+   const T q32_d = p2<1, SD>(c_d) + pm<kLinSoftMul>(T(5.), d_d) - e_d;
+   const T term1 = pm<kLinSoftMul>(p.b2w0, q30_d);
+   const T term2 = pm<kLinSoftMul>(p.b2w1, q31_d);
+   const T term3 = pm<kLinSoftMul>(p.b2w2, q32_d);
+   const T dbeta0 = pm<kLinSoftMul>(p.cdjm1, djm1_d) + pm<kLinSoftMul>(p.cejm1, ejm1_d);
+   const T dbeta1 = pm<kLinSoftMul>(p.cdj, dj_d) + pm<kLinSoftMul>(p.cej, ej_d);
+   const T dbeta2 = pm<kLinSoftMul>(p.cdjp1, djp1_d) + pm<kLinSoftMul>(p.cejp1, ejp1_d);
    const T beta0 = p.beta0, beta1 = p.beta1, beta2 = p.beta2;
    const T dw0_down = p.dwd;
-   const T s12 = pm<SD>(dbeta1, beta2) + pm<SD>(beta1, dbeta2);
-   const T s6 = pm<SD>(T(6), pm<SD>(dbeta0, beta2) + pm<SD>(beta0, dbeta2));
-   const T s3 = pm<SD>(T(3), pm<SD>(dbeta0, beta1) + pm<SD>(beta0, dbeta1));
-   const T dw0_up_1 = pm<SD>(s12, dw0_down);
-   const T dw0_up_2 = pm<SD>(p.bb12, s12 + s6 + s3);
+   const T s12 = pm<kLinSoftMul>(dbeta1, beta2) + pm<kLinSoftMul>(beta1, dbeta2);
+   const T s6 = pm<kLinSoftMul>(T(6), pm<kLinSoftMul>(dbeta0, beta2) + pm<kLinSoftMul>(beta0, dbeta2));
+   const T s3 = pm<kLinSoftMul>(T(3), pm<kLinSoftMul>(dbeta0, beta1) + pm<kLinSoftMul>(beta0, dbeta1));
+   const T dw0_up_1 = pm<kLinSoftMul>(s12, dw0_down);
+   const T dw0_up_2 = pm<kLinSoftMul>(p.bb12, s12 + s6 + s3);
    const Dv<T, SD> rd(p.dwd2);
    const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
-   const T dw1_up_1 = pm<SD>(s6, dw0_down);
-   const T dw1_up_2 = pm<SD>(Dv<T, SD>(beta1).div(pm<SD>(T(6), dw0_up_2)), beta0);
+   const T dw1_up_1 = pm<kLinSoftMul>(s6, dw0_down);
+   const T dw1_up_2 = pm<kLinSoftMul>(Dv<T, SD>(beta1).div(pm<kLinSoftMul>(T(6), dw0_up_2)), beta0);
    const T dw1 = rd.div(dw1_up_1 - dw1_up_2);
-   const T dw2_up_1 = pm<SD>(s3, dw0_down);
-   const T dw2_up_2 = pm<SD>(Dv<T, SD>(beta2).div(pm<SD>(T(3), dw0_up_2)), beta0);
+   const T dw2_up_1 = pm<kLinSoftMul>(s3, dw0_down);
+   const T dw2_up_2 = pm<kLinSoftMul>(Dv<T, SD>(beta2).div(pm<kLinSoftMul>(T(3), dw0_up_2)), beta0);
    const T dw2 = rd.div(dw2_up_1 - dw2_up_2);
-   return term1 + term2 + term3 + pm<SD>(pm<SD>(b2, dw0), p.q30) + pm<SD>(pm<SD>(b2, dw1), p.q31) +
-          pm<SD>(pm<SD>(b2, dw2), p.q32);
+   return term1 + term2 + term3 + pm<kLinSoftMul>(pm<kLinSoftMul>(b2, dw0), p.q30) + pm<kLinSoftMul>(pm<kLinSoftMul>(b2, dw1), p.q31) +
+          pm<kLinSoftMul>(pm<kLinSoftMul>(b2, dw2), p.q32);
 }
 
 template <typename T, bool SD>
@@ -451,32 +455,32 @@ __device__ __forceinline__ double weno5_with_lin(double a, double b, double c, d
                                                  Weno5Lin<double>& p)
 {
    const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double c3 = pm<SD>(3., c);
+   const double c3 = pm<kLinSoftMul>(3., c);
    const double djm1 = a - p2<1, SD>(b) + c;
    const double ejm1 = a - p2<2, SD>(b) + c3;
    const double dj = b - p2<1, SD>(c) + d;
    const double ej = b - d;
    const double djp1 = c - p2<1, SD>(d) + e;
    const double ejp1 = c3 - p2<2, SD>(d) + e;
-   const double s0 = pm<SD>(pm<SD>(b1, djm1), djm1) + pm<SD>(p2<-2, SD>(ejm1), ejm1);
-   const double s1 = pm<SD>(pm<SD>(b1, dj), dj) + pm<SD>(p2<-2, SD>(ej), ej);
-   const double s2 = pm<SD>(pm<SD>(b1, djp1), djp1) + pm<SD>(p2<-2, SD>(ejp1), ejp1);
+   const double s0 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djm1), djm1) + pm<kLinSoftMul>(p2<-2, SD>(ejm1), ejm1);
+   const double s1 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, dj), dj) + pm<kLinSoftMul>(p2<-2, SD>(ej), ej);
+   const double s2 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djp1), djp1) + pm<kLinSoftMul>(p2<-2, SD>(ejp1), ejp1);
    const double dis0 = s0 + 1e-15, dis1 = s1 + 1e-15, dis2 = s2 + 1e-15;
-   p.q30 = p2<1, SD>(a) - pm<SD>(7., b) + pm<SD>(11., c);
-   p.q31 = -b + pm<SD>(5., c) + p2<1, SD>(d);
-   p.q32 = p2<1, SD>(c) + pm<SD>(5., d) - e;
+   p.q30 = p2<1, SD>(a) - pm<kLinSoftMul>(7., b) + pm<kLinSoftMul>(11., c);
+   p.q31 = -b + pm<kLinSoftMul>(5., c) + p2<1, SD>(d);
+   p.q32 = p2<1, SD>(c) + pm<kLinSoftMul>(5., d) - e;
    const double d01 = Dv<double, SD>(dis1).div(dis0);
    const double d02 = Dv<double, SD>(dis2).div(dis0);
-   const double a1ba0 = pm<SD>(6., d01);
-   const double a2ba0 = pm<SD>(3., d02);
+   const double a1ba0 = pm<kLinSoftMul>(6., d01);
+   const double a2ba0 = pm<kLinSoftMul>(3., d02);
    const double w0 = Dv<double, SD>(1.0 + a1ba0 + a2ba0).div(1.0);
-   const double w1 = pm<SD>(a1ba0, w0);
+   const double w1 = pm<kLinSoftMul>(a1ba0, w0);
    const double w2 = 1. - w0 - w1;
    p.beta0 = s0 + 1e-10;
    p.beta1 = s1 + 1e-10;
    p.beta2 = s2 + 1e-10;
    weno5_lin_fill<double, SD>(p, djm1, ejm1, dj, ej, djp1, ejp1);
-   return pm<SD>(b2, pm<SD>(w0, p.q30) + pm<SD>(w1, p.q31) + pm<SD>(w2, p.q32));
+   return pm<kLinSoftMul>(b2, pm<kLinSoftMul>(w0, p.q30) + pm<kLinSoftMul>(w1, p.q31) + pm<kLinSoftMul>(w2, p.q32));
 }
 
 // reconstructed states at the two sides of a face slot, FP64
