@@ -476,6 +476,19 @@ def algorithmic_bytes(kernel: str, lay: dict, sizes: dict, order: int) -> float:
     nc, ns, nr = sizes["nCell"], lay["nSlot"], lay["nRow"]
     npr = lay["nPeriodicRows"]
     sten = {1: 2, 3: 4, 5: 6}[order]
+    if kernel == "recon5":
+        # order 5, implicit: slot record 16, stencil entries 16 (shared by neighbours), q once
+        # per cell; writes the slot's two states 64 and the kept WENO values 8 * 144
+        return ns * (16 + 16 + 64 + 8 * 144) + nc * 32
+    if kernel == "lin_recon5":
+        # slot record 16, stencil 16, kept WENO values 8 * 144, dq once per cell; writes 64
+        return ns * (16 + 16 + 8 * 144 + 64) + nc * 32
+    if kernel == "rhs_face" and order == 5:
+        # slot record 16, normal 16, the states recon5 left 64; writes flux 32, spec 8, ff 256
+        return ns * (16 + 16 + 64 + 32 + 8 + 256)
+    if kernel == "lin_face" and order == 5:
+        # slot record 16, the linearised states 64, ff 256; writes flux 32
+        return ns * (16 + 64 + 256 + 32)
     if kernel == "rhs_face":
         # slot record 32 + normal 16 + stencil entries 16*sten/2 (shared by neighbours)
         # + q once per cell; writes flux 32, spec 8, ff 256
@@ -645,9 +658,8 @@ def run_gpu(args, wl, rank, local_rank, world):
         fp64 = None
         if row.get("workload") == wl["name"]:
             fp64 = {"pipe_active_pct": row["fp64_pipe_pct"], "peak_warp_inst_per_s": FP64_WARP_INSTR_PER_S,
-                    "source": "ncu sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active, " +
-                              ("profiles/fp64_kernels_naca512x128_split50_weno5.md" if wl["split"] > 0
-                               else "profiles/%s_naca512x128_weno5.md" % dom),
+                    "source": "ncu sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active, "
+                              "profiles/fp64_kernels_naca512x128_split50_weno5.md",
                     "note": "the path is FP64-issue bound on GB300; HBM fraction is reported as the contract asks"}
         roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
                     "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
