@@ -324,9 +324,7 @@ Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle
    // per-lane form also factors the block, the solve's does not
    auto assign = [&](const std::vector<int>& chains, bool factor) {
       const double row_warp = factor ? 42.0 : 29.0, row_bundle = factor ? 274.0 : 92.0;
-      // a bundle row of the factorisation costs three times one of the
-      // solve: its bundles take chains half as long
-      const int max_bundled = factor ? bundle_rows / 2 : bundle_rows;
+      const int max_bundled = bundle_rows;
       std::vector<int> sorted(chains);
       std::stable_sort(sorted.begin(), sorted.end(),
                        [&](int a, int b) { return p.chain_nrows[a] > p.chain_nrows[b]; });

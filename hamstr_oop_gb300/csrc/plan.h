@@ -78,7 +78,7 @@ std::string build_plan(const MeshInput& in, Plan& out);
 //   - a chain id: the chain on the whole warp;
 //   - (a | kPairJob), b: open chains a and b, one per half-warp (pair_open);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
-//     bundle_rows rows (half that in the factorisation), one per lane.
+//     bundle_rows rows, one per lane.
 // nwarps[s] = min(njobs[s], max_warps) warps are launched.
 constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;

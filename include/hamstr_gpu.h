@@ -193,8 +193,7 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
  * or two per sub-partition, schedules rebuilt longest-job-first), with open
  * chains one per warp or two per warp (one per half), and the shortest
- * (up to 0, 4, 8 or 16 rows; half that when factoring) 32 per warp, one
- * per lane; FP32
+ * (up to 0, 4, 8 or 16 rows) 32 per warp, one per lane; FP32
  * line kernels 32..128 threads per block, with the blocks assembled by a
  * separate coalesced kernel or inside the factorisation; FP64 divisions of the face
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
@@ -215,9 +214,8 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       once per step by the implicit computeRHS and kept for the sweeps
  *       (1 KiB per face slot of device memory): 0 or 1 (default 1; not
  *       tuned by hamstr_gpu_autotune)
- *   [8] FP64 line kernels: open chains of at most this many rows (half
- *       that in the factorisation) go 32 to a warp, one per lane (0: none):
- *       0..64
+ *   [8] FP64 line kernels: open chains of at most this many rows go 32 to
+ *       a warp, one per lane (0: none): 0..64
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
  * not depend on the shape. */
 #define HAMSTR_SHAPE_N 9
