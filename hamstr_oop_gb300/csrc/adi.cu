@@ -17,9 +17,10 @@
 // a 4x4 block; in periodic chains half h=0 carries the C' recurrence and
 // half h=1 the fill-in column a' (triSolvers.cpp:877-891), which follow
 // the same instruction sequence.  Open chains need one half only, so the
-// schedule may pair them: two open chains per warp, one per half.  Short
-// open chains may also go 32 to a warp, one per lane (a bundle), which
-// spends far fewer warp instructions per row on them.
+// schedule may pair them (two per warp, one per half) or put eight in a
+// warp, four lanes each (lane 4g + r on row r of every block).  Short open
+// chains may also go 32 to a warp, one per lane (a bundle), which spends
+// far fewer warp instructions per row on them.
 //
 // Per-row factor record (80 doubles):
 //   [ 0..15] A_i scaled      (f update in the forward sweep)
@@ -141,6 +142,14 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
                factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c], d.fac + (size_t)kFacRec * row0);
             }
          }
+      } else if (ich & kQuadJob) {
+         int c = 0, N = 0;
+         if ((lane >> 2) < (ich & 63)) {
+            c = d.sched_jobs[job + 1 + (lane >> 2)];
+            N = live_rows(d, c);
+         }
+         const int row0 = d.chain_row0[c];
+         factor_line_quad<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
       } else if (ich & kPairJob) {
          factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
       } else if (!frozen_chain(d, ich)) {
@@ -223,6 +232,15 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sw
                                  d.row_scell + row0, d.fsc + 4 * (size_t)row0);
             }
          }
+      } else if (ich & kQuadJob) {
+         int c = 0, N = 0;
+         if ((lane >> 2) < (ich & 63)) {
+            c = d.sched_jobs[job + 1 + (lane >> 2)];
+            N = live_rows(d, c);
+         }
+         const int row0 = d.chain_row0[c];
+         solve_line_quad(d.fac + (size_t)kFacRec * row0, N, d.r, d.row_fcell + row0, d.row_scell + row0,
+                         d.fsc + 4 * (size_t)row0, lane);
       } else if (ich & kPairJob) {
          solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
       } else if (!frozen_chain(d, ich)) {

@@ -109,7 +109,7 @@ struct hamstr_gpu {
    double* wall_scr = nullptr;          // device: 3 per wall face + 3 sums per instance
 
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
-   int adi_pair = 1;                    // open chains two per warp in the FP64 line kernels
+   int adi_lanes = 4;                   // lanes per open chain in the FP64 line kernels: 32, 16 or 4
    int adi_bundle = 0;                  // open chains of up to this many rows one per lane (0: none)
    // order 5, FP64: the WENO linearisation's f-only values kept from the
    // implicit computeRHS for the sweeps (d.wlin points here when on)
@@ -267,7 +267,7 @@ struct hamstr_gpu {
       if (sched.nwarps[1 + w] > 0) L("adi_solve", n, [&] { launch_adi_solve(d, s, w, sched.nwarps[1 + w], stream); });
    }
 
-   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int pair,
+   int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int lanes,
                    int wkeep, int bundle)
    {
       if (wkeep && d.recon == 5) {
@@ -286,10 +286,10 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb || pair != adi_pair || bundle != adi_bundle) {
-         adi_pair = pair;
+      if (adi_wpb != d.adi_wpb || lanes != adi_lanes || bundle != adi_bundle) {
+         adi_lanes = lanes;
          adi_bundle = bundle;
-         sched = build_schedule(plan, adi_wpb * nsm, pair != 0, bundle);
+         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle);
          const int st = upload_schedule();
          if (st) return st;
       }
@@ -567,7 +567,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       // the shortest open chains one per lane where chains are short (the
       // autotuner checks the alternatives)
       g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 8 : 0;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_pair != 0, g->adi_bundle);
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle);
    }
    TRY(g->upload_schedule());
    d.nWave = P.nWave;
@@ -1082,7 +1082,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, pair, bundle; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle; float ms; };
    const int wk = g->weno_keep;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
@@ -1090,13 +1090,13 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          if (g->mixed) {
             for (int fused : {0, 1})
                for (int mb : {32, 64, 128})
-                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_pair, g->adi_bundle, 0.f});
+                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_lanes, g->adi_bundle, 0.f});
          } else {
             for (int w : {4, 8})
                for (int psoft : {0, 1})
-                  for (int pair : {0, 1})
+                  for (int ln : {16, 4})
                      for (int bu : {0, 4, 8, 16})
-                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, pair, bu, 0.f});
+                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, ln, bu, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1109,7 +1109,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.pair, wk, c.bundle))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1130,7 +1130,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    const Cand* best = &cands[0];
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
-   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, wk,
+   st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
                        best->bundle);
    if (st) return st;
    if (report && report_len > 0) {
@@ -1139,17 +1139,17 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          char buf[256];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_bundle_rows\": %d, "
+                       "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d, "
                        "\"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].pair, cands[i].bundle, cands[i].ms);
+                       cands[i].psoft, cands[i].lanes, cands[i].bundle, cands[i].ms);
          r += buf;
       }
       char buf[256];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_pair\": %d, \"adi_bundle_rows\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->pair, best->bundle);
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, best->bundle);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }
@@ -1161,7 +1161,7 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
-                                  d.piv_soft,   g->adi_pair, g->weno_keep, g->adi_bundle};
+                                  d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1172,7 +1172,7 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const int* s = shape;
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
-                   (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 0 || s[6] == 1) &&
+                   (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
                    (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");

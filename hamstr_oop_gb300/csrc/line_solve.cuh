@@ -317,6 +317,187 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
    }
 }
 
+// ---- eight open lines per warp, four lanes each --------------------------
+// Lane 4g + r works on row r of every block of line g: the row products run
+// on all 32 lanes at once, and the block LU and the 4-vector solves run as
+// in the warp form (lu_wavefront, lu_solve_lanes) on four lanes.  Same
+// operations and order as factor_line / solve_line on an open line, so the
+// records are the same.  Lines of a warp run to the longest one's count,
+// the shorter ones idle (loads and stores skipped); N = 0 for an unused
+// group.
+
+// the LU of B' (lane r holds row r in w[0..3]), lu_wavefront's steps
+template <bool SD>
+__device__ __forceinline__ void lu_rows_quad(double (&w)[4], int r, int base)
+{
+   const double piv0 = SD ? sd::div(1., __shfl_sync(kLaneMask, w[0], base)) : 1. / __shfl_sync(kLaneMask, w[0], base);
+#pragma unroll
+   for (int j = 1; j < 4; j++) {
+      const double m = w[j] * piv0;
+      if (r == 0) w[j] = m;
+   }
+#pragma unroll
+   for (int j = 1; j < 4; j++) {
+      const double U = __shfl_sync(kLaneMask, w[j], base);
+      const double t = w[j] - w[0] * U;
+      if (r >= 1) w[j] = t;
+   }
+   const double piv1 = SD ? sd::div(1., __shfl_sync(kLaneMask, w[1], base + 1))
+                          : 1. / __shfl_sync(kLaneMask, w[1], base + 1);
+#pragma unroll
+   for (int j = 2; j < 4; j++) {
+      const double m = w[j] * piv1;
+      if (r == 1) w[j] = m;
+   }
+#pragma unroll
+   for (int j = 2; j < 4; j++) {
+      const double U = __shfl_sync(kLaneMask, w[j], base + 1);
+      const double t = w[j] - w[1] * U;
+      if (r >= 2) w[j] = t;
+   }
+   const double piv2 = SD ? sd::div(1., __shfl_sync(kLaneMask, w[2], base + 2))
+                          : 1. / __shfl_sync(kLaneMask, w[2], base + 2);
+   {
+      const double m = w[3] * piv2;
+      if (r == 2) w[3] = m;
+   }
+   {
+      const double U = __shfl_sync(kLaneMask, w[3], base + 2);
+      const double t = w[3] - w[2] * U;
+      if (r == 3) w[3] = t;
+   }
+   const double piv3 = SD ? sd::div(1., __shfl_sync(kLaneMask, w[3], base + 3))
+                          : 1. / __shfl_sync(kLaneMask, w[3], base + 3);
+   const double pv = (r == 0) ? piv0 : (r == 1) ? piv1 : (r == 2) ? piv2 : piv3;
+#pragma unroll
+   for (int j = 0; j < 4; j++)
+      if (j == r) w[j] = pv;
+}
+
+__device__ __forceinline__ void ld4row(const double* __restrict__ p, double (&v)[4])
+{
+   const double2 a = *reinterpret_cast<const double2*>(p);
+   const double2 b = *reinterpret_cast<const double2*>(p + 2);
+   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+__device__ __forceinline__ void st4row(double* __restrict__ p, const double (&v)[4])
+{
+   *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+   *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+
+// factor_line on open line g of the warp: blocks of row i at blk + i*stride
+// (A, B, C consecutive, 16 each)
+template <bool SD>
+__device__ __forceinline__ void factor_line_quad(const double* __restrict__ blk, size_t stride, int N,
+                                                 double* __restrict__ fac, int lane)
+{
+   const int r = lane & 3, base = lane & ~3;
+   const int Nmax = __reduce_max_sync(kLaneMask, N);
+   double Pr[4] = {0.0, 0.0, 0.0, 0.0};   // row r of the previous row's C'
+   for (int i = 0; i < Nmax; i++) {
+      const bool live = i < N;
+      double A[4] = {0.0, 0.0, 0.0, 0.0}, w[4] = {0.0, 0.0, 0.0, 0.0}, C[4] = {0.0, 0.0, 0.0, 0.0};
+      double* rec = fac + (size_t)kFacRec * i;
+      if (live) {
+         const double* b = blk + stride * (size_t)i;
+         ld4row(b + 4 * r, A);
+         ld4row(b + 16 + 4 * r, w);
+         ld4row(b + 32 + 4 * r, C);
+         st4row(rec + 4 * r, A);
+      }
+      if (i > 0) {
+         // b(i) -= a(i) c'(i-1): entry (r, j) subtracts a(r,l) c'(l,j), l = 0..3 in order
+         double P[4][4];
+#pragma unroll
+         for (int l = 0; l < 4; l++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) P[l][j] = __shfl_sync(kLaneMask, Pr[j], base + l);
+#pragma unroll
+         for (int j = 0; j < 4; j++) {
+            double acc = w[j];
+#pragma unroll
+            for (int l = 0; l < 4; l++) acc -= A[l] * P[l][j];
+            w[j] = acc;
+         }
+      }
+      lu_rows_quad<SD>(w, r, base);
+      if (live) st4row(rec + 16 + 4 * r, w);
+      // c'(i) = B'^{-1} c(i), column by column (component r of each in this lane)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+         double xs[4];
+         Pr[j] = lu_solve_lanes(w, r, C[j], base, 1, xs);
+      }
+      if (live) st4row(rec + 32 + 4 * r, Pr);
+   }
+}
+
+// solve_line on open line g of the warp: the right-hand side from
+// r[fcell[i]] (zero where fcell < 0), the solution into r[scell[i]]; fs
+// holds the forward sweep's rows.  Row i+1's record and right-hand side
+// are loaded while row i is solved.
+__device__ __forceinline__ void solve_line_quad(const double* __restrict__ fac, int N, double* __restrict__ rv,
+                                                const int* __restrict__ fcell, const int* __restrict__ scell,
+                                                double* __restrict__ fs, int lane)
+{
+   const int r = lane & 3, base = lane & ~3;
+   const int Nmax = __reduce_max_sync(kLaneMask, N);
+   double xp[4] = {0.0, 0.0, 0.0, 0.0};
+   double a[4] = {0.0, 0.0, 0.0, 0.0}, lu[4] = {0.0, 0.0, 0.0, 0.0}, xr = 0.0;
+   if (N > 0) {
+      const int fc = fcell[0];
+      if (fc >= 0) xr = rv[4 * (size_t)fc + r];
+      ld4row(fac + 16 + 4 * r, lu);
+   }
+   for (int i = 0; i < Nmax; i++) {
+      double an[4] = {0.0, 0.0, 0.0, 0.0}, lun[4] = {0.0, 0.0, 0.0, 0.0}, xrn = 0.0;
+      if (i + 1 < N) {
+         const double* rn = fac + (size_t)kFacRec * (i + 1);
+         const int fcn = fcell[i + 1];
+         if (fcn >= 0) xrn = rv[4 * (size_t)fcn + r];
+         ld4row(rn + 4 * r, an);
+         ld4row(rn + 16 + 4 * r, lun);
+      }
+      double x = xr;
+      if (i > 0) {
+         // f(i) -= a(i) f(i-1), this component's products in order
+#pragma unroll
+         for (int j = 0; j < 4; j++) x = x - a[j] * xp[j];
+      }
+      double xs[4];
+      x = lu_solve_lanes(lu, r, x, base, 1, xs);
+      const bool live = i < N;
+      if (live) fs[4 * i + r] = x;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+         if (live) xp[m] = xs[m];
+         a[m] = an[m];
+         lu[m] = lun[m];
+      }
+      xr = xrn;
+   }
+   // back substitution f(i) -= c'(i) f(i+1), i = N-2..0 (t = 0..Nmax-2, i = N-2-t)
+   if (N > 0) rv[4 * (size_t)scell[N - 1] + r] = sel4(xp, r);
+   for (int t = 0; t <= Nmax - 2; t++) {
+      const int ii = N - 2 - t;
+      double x = 0.0, c[4] = {0.0, 0.0, 0.0, 0.0};
+      if (ii >= 0) {
+         x = fs[4 * ii + r];
+         ld4row(fac + (size_t)kFacRec * ii + 32 + 4 * r, c);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) x = x - c[j] * xp[j];
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+         const double v = __shfl_sync(kLaneMask, x, base + m);
+         if (ii >= 0) xp[m] = v;
+      }
+      if (ii >= 0) rv[4 * (size_t)scell[ii] + r] = x;
+   }
+}
+
 // ---- one open line per thread -------------------------------------------
 // The same operations as factor_line / solve_line on an open line, written
 // out for one thread: a warp then carries 32 lines and every FP64

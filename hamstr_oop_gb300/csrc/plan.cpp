@@ -314,51 +314,54 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows)
+Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows)
 {
    Schedule S;
    S.job_ptr.push_back(0);
-   // jobs ordered by their FP64 warp instructions (longest first): per row,
-   // a warp or a pair of half-warps (both halves issue the same
-   // instructions) or a bundle of one-per-lane chains; the factorisation's
-   // per-lane form also factors the block, the solve's does not
+   // jobs ordered by their estimated time, longest first: a row of a warp,
+   // half-warp or four-lane form is a chain of dependent FP64 operations
+   // (latency; the factorisation's block LU about three times the solve's),
+   // a row of a bundle is ~274 (factorisation) or ~92 (solve) FP64 warp
+   // instructions issued back to back
    auto assign = [&](const std::vector<int>& chains, bool factor) {
-      const double row_warp = factor ? 42.0 : 29.0, row_bundle = factor ? 274.0 : 92.0;
-      const int max_bundled = bundle_rows;
+      const double row_warp = factor ? 6.0 : 2.0, row_bundle = factor ? 22.0 : 7.4;
       std::vector<int> sorted(chains);
       std::stable_sort(sorted.begin(), sorted.end(),
                        [&](int a, int b) { return p.chain_nrows[a] > p.chain_nrows[b]; });
       struct Job { double cost; std::vector<int> entries; };
       std::vector<Job> order;
-      std::vector<int> bundle;
-      int pending = -1;
-      auto flush_bundle = [&]() {
-         if (bundle.empty()) return;
+      std::vector<int> bundle, group;
+      auto flush = [&](std::vector<int>& v, int flag, double row_cost) {
+         if (v.empty()) return;
          Job j;
-         j.cost = row_bundle * p.chain_nrows[bundle.front()];   // longest first
-         j.entries.push_back(kBundleJob | (int)bundle.size());
-         j.entries.insert(j.entries.end(), bundle.begin(), bundle.end());
+         j.cost = row_cost * p.chain_nrows[v.front()];   // longest first
+         if (flag == kPairJob && v.size() == 2) {
+            j.entries = {v[0] | kPairJob, v[1]};
+         } else if (flag == kPairJob || flag == 0) {
+            j.entries = {v[0]};
+         } else {
+            j.entries.push_back(flag | (int)v.size());
+            j.entries.insert(j.entries.end(), v.begin(), v.end());
+         }
          order.push_back(j);
-         bundle.clear();
+         v.clear();
       };
+      const int group_size = open_lanes == 4 ? 8 : open_lanes == 16 ? 2 : 1;
+      const int group_flag = open_lanes == 4 ? kQuadJob : open_lanes == 16 ? kPairJob : 0;
       for (int c : sorted) {
          const int n = p.chain_nrows[c];
          if (p.chain_periodic[c]) {
             order.push_back({1.3 * row_warp * n, {c}});
-         } else if (n <= max_bundled) {
+         } else if (n <= bundle_rows) {
             bundle.push_back(c);
-            if (bundle.size() == 32) flush_bundle();
-         } else if (!pair_open) {
-            order.push_back({row_warp * n, {c}});
-         } else if (pending < 0) {
-            pending = c;
+            if ((int)bundle.size() == 32) flush(bundle, kBundleJob, row_bundle);
          } else {
-            order.push_back({row_warp * p.chain_nrows[pending], {pending | kPairJob, c}});
-            pending = -1;
+            group.push_back(c);
+            if ((int)group.size() == group_size) flush(group, group_flag, row_warp);
          }
       }
-      flush_bundle();
-      if (pending >= 0) order.push_back({row_warp * p.chain_nrows[pending], {pending}});
+      flush(bundle, kBundleJob, row_bundle);
+      flush(group, group_flag, row_warp);
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
       S.job0.push_back((int)S.job_ptr.size() - 1);
       S.njobs.push_back((int)order.size());

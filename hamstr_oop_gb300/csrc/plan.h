@@ -75,19 +75,24 @@ std::string build_plan(const MeshInput& in, Plan& out);
 // jobs[job_ptr[job0[s] + k] .. job_ptr[job0[s] + k + 1]).  Each warp takes
 // the next job from a counter in device memory, so the longest jobs start
 // first and no cost model decides which warp runs what.  A job is
-//   - a chain id: the chain on the whole warp;
-//   - (a | kPairJob), b: open chains a and b, one per half-warp (pair_open);
+//   - a chain id: the chain on the whole warp (periodic chains; open ones
+//     with open_lanes = 32);
+//   - (a | kPairJob), b: open chains a and b, one per half-warp
+//     (open_lanes = 16);
+//   - (kQuadJob | n), c_1 .. c_n: n <= 8 open chains, four lanes each
+//     (open_lanes = 4);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
 //     bundle_rows rows, one per lane.
 // nwarps[s] = min(njobs[s], max_warps) warps are launched.
 constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;
+constexpr int kQuadJob = 1 << 28;
 struct Schedule {
    std::vector<int> job0, njobs, nwarps;   // per schedule
    std::vector<int> job_ptr;               // per job (all schedules), +1
    std::vector<int> jobs;                  // job entries, as above
 };
-Schedule build_schedule(const Plan& p, int max_warps, bool pair_open, int bundle_rows);
+Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows);
 
 }  // namespace hamstr
 #endif

@@ -192,8 +192,9 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * precision for each candidate launch shape -- face kernels 128 or 256
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
  * or two per sub-partition, schedules rebuilt longest-job-first), with open
- * chains one per warp or two per warp (one per half), and the shortest
- * (up to 0, 4, 8 or 16 rows) 32 per warp, one per lane; FP32
+ * chains two per warp (one per half) or eight per warp (four lanes
+ * each), and the shortest (up to 0, 4, 8 or 16 rows) 32 per warp, one per
+ * lane; FP32
  * line kernels 32..128 threads per block, with the blocks assembled by a
  * separate coalesced kernel or inside the factorisation; FP64 divisions of the face
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
@@ -209,7 +210,8 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *   [3] FP32 blocks assembled inside the factorisation: 0 or 1
  *   [4] face kernels' divisions on the integer pipes: 0 or 1
  *   [5] FP64 LU pivot reciprocals on the integer pipes: 0 or 1
- *   [6] open chains two per warp in the FP64 line kernels: 0 or 1
+ *   [6] FP64 line kernels: lanes per open chain -- 32 (a warp), 16 (two
+ *       per warp) or 4 (eight per warp): 32, 16 or 4
  *   [7] order 5, FP64: the WENO linearisation's state-only values formed
  *       once per step by the implicit computeRHS and kept for the sweeps
  *       (1 KiB per face slot of device memory): 0 or 1 (default 1; not

@@ -19,9 +19,9 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     assert np.array_equal(g.get("q"), o.get("q"))
 
 
-FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_pair=pr,
+FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_softdiv=ps, adi_open_lanes=ln,
                     adi_bundle_rows=bu)
-               for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for pr in (0, 1)
+               for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for ln in (32, 16, 4)
                for bu in (0, 4, 64)]
 
 
@@ -53,7 +53,7 @@ def test_set_shape_rejects_bad_values(make_case, native_lib):
     from hamstr_oop_gb300 import native
     g = native.GpuSolver(native.Case(make_case(16, 4, order=1, CFL=5.0)))
     before = g.shape()
-    for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_pair=2), dict(adi_bundle_rows=65)):
+    for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_open_lanes=8), dict(adi_bundle_rows=65)):
         with pytest.raises(native.HamstrError):
             g.set_shape(**bad)
     assert g.shape() == before
