@@ -348,8 +348,11 @@ __device__ __forceinline__ Weno5Lin<T> weno5_lin_get(const T* __restrict__ in, s
 // (eps added) and the candidate stencils; shared by weno5_lin_pre and
 // weno5_with_lin.  Each is an intermediate value of the reference's
 // expressions, formed the same way (b1 * 2 is exact).
-// The multiplies of the linearisation stay on the FP64 pipe (the integer
-// pipes already carry its divisions; measured slower with both there)
+// The linearisation's multiplies: its divisions already load the integer
+// pipes, so only the increment part's first multiplies (candidate
+// stencils, the weight and smoothness derivative terms) go there with SD,
+// about half of them, and the rest stay on the FP64 pipe (all of them
+// there, or none, measured slower)
 constexpr bool kLinSoftMul = false;
 
 template <typename T, bool SD>
@@ -406,35 +409,35 @@ template <typename T, bool SD>
 __device__ __forceinline__ T weno5_lin_apply(const Weno5Lin<T>& p, T a_d, T b_d, T c_d, T d_d, T e_d)
 {
    const T b2 = T(1. / 6.);
-   const T c3 = pm<kLinSoftMul>(T(3.), c_d);
+   const T c3 = pm<SD>(T(3.), c_d);
    const T djm1_d = a_d - p2<1, SD>(b_d) + c_d;
    const T ejm1_d = a_d - p2<2, SD>(b_d) + c3;
    const T dj_d = b_d - p2<1, SD>(c_d) + d_d;
    const T ej_d = b_d - d_d;
    const T djp1_d = c_d - p2<1, SD>(d_d) + e_d;
    const T ejp1_d = c3 - p2<2, SD>(d_d) + e_d;
-   const T q30_d = p2<1, SD>(a_d) - pm<kLinSoftMul>(T(7.), b_d) + pm<kLinSoftMul>(T(11.), c_d);
-   const T q31_d = -b_d + pm<kLinSoftMul>(T(5.), c_d) + p2<1, SD>(d_d);
-   const T q32_d = p2<1, SD>(c_d) + pm<kLinSoftMul>(T(5.), d_d) - e_d;
-   const T term1 = pm<kLinSoftMul>(p.b2w0, q30_d);
-   const T term2 = pm<kLinSoftMul>(p.b2w1, q31_d);
-   const T term3 = pm<kLinSoftMul>(p.b2w2, q32_d);
-   const T dbeta0 = pm<kLinSoftMul>(p.cdjm1, djm1_d) + pm<kLinSoftMul>(p.cejm1, ejm1_d);
-   const T dbeta1 = pm<kLinSoftMul>(p.cdj, dj_d) + pm<kLinSoftMul>(p.cej, ej_d);
-   const T dbeta2 = pm<kLinSoftMul>(p.cdjp1, djp1_d) + pm<kLinSoftMul>(p.cejp1, ejp1_d);
+   const T q30_d = p2<1, SD>(a_d) - pm<SD>(T(7.), b_d) + pm<SD>(T(11.), c_d);
+   const T q31_d = -b_d + pm<SD>(T(5.), c_d) + p2<1, SD>(d_d);
+   const T q32_d = p2<1, SD>(c_d) + pm<SD>(T(5.), d_d) - e_d;
+   const T term1 = pm<SD>(p.b2w0, q30_d);
+   const T term2 = pm<SD>(p.b2w1, q31_d);
+   const T term3 = pm<SD>(p.b2w2, q32_d);
+   const T dbeta0 = pm<SD>(p.cdjm1, djm1_d) + pm<SD>(p.cejm1, ejm1_d);
+   const T dbeta1 = pm<SD>(p.cdj, dj_d) + pm<SD>(p.cej, ej_d);
+   const T dbeta2 = pm<SD>(p.cdjp1, djp1_d) + pm<SD>(p.cejp1, ejp1_d);
    const T beta0 = p.beta0, beta1 = p.beta1, beta2 = p.beta2;
    const T dw0_down = p.dwd;
    const T s12 = pm<kLinSoftMul>(dbeta1, beta2) + pm<kLinSoftMul>(beta1, dbeta2);
    const T s6 = pm<kLinSoftMul>(T(6), pm<kLinSoftMul>(dbeta0, beta2) + pm<kLinSoftMul>(beta0, dbeta2));
    const T s3 = pm<kLinSoftMul>(T(3), pm<kLinSoftMul>(dbeta0, beta1) + pm<kLinSoftMul>(beta0, dbeta1));
-   const T dw0_up_1 = pm<kLinSoftMul>(s12, dw0_down);
+   const T dw0_up_1 = pm<SD>(s12, dw0_down);
    const T dw0_up_2 = pm<kLinSoftMul>(p.bb12, s12 + s6 + s3);
    const Dv<T, SD> rd(p.dwd2);
    const T dw0 = rd.div(dw0_up_1 - dw0_up_2);
-   const T dw1_up_1 = pm<kLinSoftMul>(s6, dw0_down);
+   const T dw1_up_1 = pm<SD>(s6, dw0_down);
    const T dw1_up_2 = pm<kLinSoftMul>(Dv<T, SD>(beta1).div(pm<kLinSoftMul>(T(6), dw0_up_2)), beta0);
    const T dw1 = rd.div(dw1_up_1 - dw1_up_2);
-   const T dw2_up_1 = pm<kLinSoftMul>(s3, dw0_down);
+   const T dw2_up_1 = pm<SD>(s3, dw0_down);
    const T dw2_up_2 = pm<kLinSoftMul>(Dv<T, SD>(beta2).div(pm<kLinSoftMul>(T(3), dw0_up_2)), beta0);
    const T dw2 = rd.div(dw2_up_1 - dw2_up_2);
    return term1 + term2 + term3 + pm<kLinSoftMul>(pm<kLinSoftMul>(b2, dw0), p.q30) + pm<kLinSoftMul>(pm<kLinSoftMul>(b2, dw1), p.q31) +
