@@ -458,20 +458,20 @@ __device__ __forceinline__ double weno5_with_lin(double a, double b, double c, d
                                                  Weno5Lin<double>& p)
 {
    const double b1 = 13. / 12., b2 = 1. / 6.;
-   const double c3 = pm<kLinSoftMul>(3., c);
+   const double c3 = pm<SD>(3., c);
    const double djm1 = a - p2<1, SD>(b) + c;
    const double ejm1 = a - p2<2, SD>(b) + c3;
    const double dj = b - p2<1, SD>(c) + d;
    const double ej = b - d;
    const double djp1 = c - p2<1, SD>(d) + e;
    const double ejp1 = c3 - p2<2, SD>(d) + e;
-   const double s0 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djm1), djm1) + pm<kLinSoftMul>(p2<-2, SD>(ejm1), ejm1);
-   const double s1 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, dj), dj) + pm<kLinSoftMul>(p2<-2, SD>(ej), ej);
-   const double s2 = pm<kLinSoftMul>(pm<kLinSoftMul>(b1, djp1), djp1) + pm<kLinSoftMul>(p2<-2, SD>(ejp1), ejp1);
+   const double s0 = pm<SD>(pm<SD>(b1, djm1), djm1) + pm<SD>(p2<-2, SD>(ejm1), ejm1);
+   const double s1 = pm<SD>(pm<SD>(b1, dj), dj) + pm<SD>(p2<-2, SD>(ej), ej);
+   const double s2 = pm<SD>(pm<SD>(b1, djp1), djp1) + pm<SD>(p2<-2, SD>(ejp1), ejp1);
    const double dis0 = s0 + 1e-15, dis1 = s1 + 1e-15, dis2 = s2 + 1e-15;
-   p.q30 = p2<1, SD>(a) - pm<kLinSoftMul>(7., b) + pm<kLinSoftMul>(11., c);
-   p.q31 = -b + pm<kLinSoftMul>(5., c) + p2<1, SD>(d);
-   p.q32 = p2<1, SD>(c) + pm<kLinSoftMul>(5., d) - e;
+   p.q30 = p2<1, SD>(a) - pm<SD>(7., b) + pm<SD>(11., c);
+   p.q31 = -b + pm<SD>(5., c) + p2<1, SD>(d);
+   p.q32 = p2<1, SD>(c) + pm<SD>(5., d) - e;
    const double d01 = Dv<double, SD>(dis1).div(dis0);
    const double d02 = Dv<double, SD>(dis2).div(dis0);
    const double a1ba0 = pm<kLinSoftMul>(6., d01);
