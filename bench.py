@@ -174,6 +174,18 @@ def run_warmstart(args, wl, rank, local_rank, world):
     model, trep = warmstart.train(case, data["q"], train_conds, epochs=wl["epochs"], batch=wl["batch"], lr=wl["lr"])
     test_conds = warmstart.conditions(ntest, seed=1)
     ev = warmstart.evaluate(case, model, test_conds, wl["tol"], wl["cap"])
+    # the plain FP64 drop-in on the first held-out conditions: the baseline
+    # and the reference converged state for the warm-started batched form
+    nplain = min(8, ntest)
+    plain = warmstart.plain_fp64_solves(case, test_conds[:nplain], wl["tol"], wl["cap"])
+    qw = ev.pop("_q_warm")
+    sw = ev.pop("_steps_warm")
+    rel = [float(np.max(np.abs(a - b)) / np.max(np.abs(b))) for a, b in zip(qw[:nplain], plain["q"])]
+    plain_cmp = {"conditions": nplain, "solves_per_s": plain["solves_per_s"], "seconds": plain["seconds"],
+                 "steps_mean": float(np.mean(plain["steps"])), "all_converged": plain["all_converged"],
+                 "warm_batched_steps_mean": float(np.mean(sw[:nplain])),
+                 "warm_batched_vs_plain_fp64_max_rel": max(rel), "warm_batched_vs_plain_fp64_rel": rel,
+                 "speedup_warm_batched_vs_plain_fp64": ev["solves_per_s_warm"] / plain["solves_per_s"]}
     peak = gemm_peak()
     peaks = measured_peaks()
     trep.pop("loss_curve", None)
@@ -186,7 +198,7 @@ def run_warmstart(args, wl, rank, local_rank, world):
                        "tol": wl["tol"], "cap": wl["cap"]},
             "freestream_start": {"solves_per_s": ev["solves_per_s_freestream"], "steps_mean": ev["steps_freestream_mean"],
                                  "seconds": ev["seconds_freestream"]},
-            "warm_start": ev, "training": trep,
+            "warm_start": ev, "plain_fp64_drop_in": plain_cmp, "training": trep,
             "data_generation": {"conditions": ntrain, "seconds": t_data, "all_converged": data["all_converged"],
                                 "steps_mean": float(np.mean(data["steps"]))},
             "roofline": {"kernel": "tcgen05 bf16 GEMM (mlp_gemm.cu)", "bound": "tensor",

@@ -209,8 +209,10 @@ def evaluate(case, model: WarmStartModel, conds: list, tol: float, cap: int, mix
     probe_pick = np.array([at(hb, probe) <= at(ha, probe) for ha, hb in zip(a["hist"], b["hist"])])
     s_probe = np.where(probe_pick, sb, sa) + np.minimum(np.where(probe_pick, sa, sb), probe)
     err = [np.max(np.abs(w - q)) / np.max(np.abs(q)) for w, q in zip(ws, a["q"])]
-    diff = [np.max(np.abs(p - q)) / np.max(np.abs(q)) for p, q in zip(a["q"], b["q"])]
+    diff = np.array([np.max(np.abs(p - q)) / np.max(np.abs(q)) for p, q in zip(a["q"], b["q"])])
+    worst = np.argsort(-diff)[:5]
     return {"conditions": len(conds), "tol": tol, "cap": cap,
+            "_q_warm": b["q"], "_steps_warm": sb,
             "initial_l2_freestream_median": float(np.median(r_fs)), "initial_l2_warm_median": float(np.median(r_ws)),
             "guess_max_rel_error_median": float(np.median(err)),
             "steps_freestream_mean": float(sa.mean()), "steps_warm_mean": float(sb.mean()),
@@ -222,4 +224,36 @@ def evaluate(case, model: WarmStartModel, conds: list, tol: float, cap: int, mix
             "seconds_freestream": a["seconds"], "seconds_warm": b["seconds"],
             "solves_per_s_freestream": len(conds) / a["seconds"], "solves_per_s_warm": len(conds) / b["seconds"],
             "all_converged": bool(a["all_converged"] and b["all_converged"]),
-            "converged_state_difference_max": float(np.max(diff))}
+            "converged_state_difference_max": float(np.max(diff)),
+            "converged_state_difference_median": float(np.median(diff)),
+            "converged_state_difference_below_1e-8": int(np.sum(diff <= 1e-8)),
+            "converged_state_difference_worst": [
+                {"mach": conds[k][0], "alpha": conds[k][1], "difference": float(diff[k]),
+                 "steps_freestream": int(sa[k]), "steps_warm": int(sb[k])} for k in worst]}
+
+
+def plain_fp64_solves(case, conds: list, tol: float, cap: int) -> dict:
+    """The plain FP64 drop-in (one handle per condition, freestream start,
+    FP64 operator) solving conditions one after another: the baseline the
+    batched, mixed-precision, warm-started form is measured against, and
+    the reference converged state (its steps are the oracle's bit for bit)."""
+    import torch
+    from . import native
+    steps, qs, secs, conv = [], [], 0.0, True
+    for m, a in conds:
+        c = case.clone()
+        c.set_flow(m, a)
+        g = native.GpuSolver(c)
+        g.march(2, 0.0)                                   # graph capture, warm-up
+        g.set("q", c.get("q"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist, ok = g.march(cap, tol)
+        secs += time.perf_counter() - t0
+        conv = conv and ok
+        hit = np.flatnonzero(hist[:, 0] <= tol)
+        steps.append(int(hit[0]) + 1 if hit.size else cap)
+        qs.append(g.get("q").reshape(-1, 4).copy())
+        g.close()
+    return {"steps": steps, "q": qs, "seconds": secs, "all_converged": conv,
+            "solves_per_s": len(conds) / secs if secs > 0 else None}

@@ -26,6 +26,11 @@ def test_warm_start_cuts_iterations(make_case, native_lib):
     assert ev["steps_guard_probe_mean"] < ev["steps_freestream_mean"], ev
     # both starts reach the same steady state (to the tolerance's reach)
     assert ev["converged_state_difference_max"] < 1e-3, ev
+    # and so does the plain FP64 drop-in from freestream (the oracle's own steps)
+    plain = warmstart.plain_fp64_solves(case, test[:3], 1e-10, 6000)
+    assert plain["all_converged"]
+    for qw, qp in zip(ev["_q_warm"][:3], plain["q"]):
+        assert np.max(np.abs(qw - qp)) / np.max(np.abs(qp)) < 1e-3
 
 
 def test_features_and_geometry(make_case, native_lib):
