@@ -172,28 +172,41 @@ struct hamstr_gpu {
       const size_t nc = (size_t)d.nCell;
       int st;
       if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
-      if (!d.mx_fused && (st = ensure_blk32())) return st;
-      if ((st = dalloc(&d.fsc32, 4 * (size_t)std::max(d.nRow, 1), owned))) return st;
-      if ((st = dalloc(&d.fac32, 80 * (size_t)std::max(d.nRow, 1), owned))) return st;
-      int nper = 0;
-      for (int c = 0; c < plan.nChain; c++) nper += plan.chain_periodic[c] ? 1 : 0;
-      if ((st = dalloc(&d.facN32, 16 * (size_t)std::max(nper, 1), owned))) return st;
-      std::vector<int> all(plan.nChain);
-      for (int c = 0; c < plan.nChain; c++) all[c] = c;
-      std::stable_sort(all.begin(), all.end(),
-                       [&](int a, int b) { return plan.chain_nrows[a] > plan.chain_nrows[b]; });
-      if ((st = upload(&d.fac_chains32, all, owned))) return st;
-      if ((st = dalloc(&d.r32, 4 * nc, owned))) return st;
-      if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
-      if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
-      if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
       // chains of each wave ordered longest first, so a warp's threads
-      // (one chain each) run for similar lengths
+      // (one chain each) run for similar lengths; the same order tiles the
+      // FP32 line data (DeviceState)
       std::vector<int> lc(plan.wave_chains);
       for (int w = 0; w < plan.nWave; w++)
          std::stable_sort(lc.begin() + plan.wave_ptr[w], lc.begin() + plan.wave_ptr[w + 1],
                           [&](int a, int b) { return plan.chain_nrows[a] > plan.chain_nrows[b]; });
       if ((st = upload(&d.line_chains, lc, owned))) return st;
+      const int ngrp = (plan.nChain + 31) / 32;
+      std::vector<int> grp_row0(ngrp + 1, 0);
+      for (int g = 0; g < ngrp; g++) {
+         int len = 0;
+         for (int p = 32 * g; p < std::min(32 * g + 32, plan.nChain); p++) len = std::max(len, plan.chain_nrows[lc[p]]);
+         grp_row0[g + 1] = grp_row0[g] + len;
+      }
+      d.tile_rows = grp_row0[ngrp];
+      std::vector<int> tile_row(32 * (size_t)std::max(d.tile_rows, 1), -1);
+      for (int p = 0; p < plan.nChain; p++) {
+         const int c = lc[p];
+         for (int i = 0; i < plan.chain_nrows[c]; i++)
+            tile_row[32 * (size_t)(grp_row0[p >> 5] + i) + (p & 31)] = plan.chain_row0[c] + i;
+      }
+      if ((st = upload(&d.grp_row0, grp_row0, owned))) return st;
+      if ((st = upload(&d.tile_row, tile_row, owned))) return st;
+      const size_t tiles = 32 * (size_t)std::max(d.tile_rows, 1);
+      if (!d.mx_fused && (st = ensure_blk32())) return st;
+      if ((st = dalloc(&d.fsc32, 4 * tiles, owned))) return st;
+      if ((st = dalloc(&d.fac32, 80 * tiles, owned))) return st;
+      int nper = 0;
+      for (int c = 0; c < plan.nChain; c++) nper += plan.chain_periodic[c] ? 1 : 0;
+      if ((st = dalloc(&d.facN32, 16 * (size_t)std::max(nper, 1), owned))) return st;
+      if ((st = dalloc(&d.r32, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
+      if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
       CK(cudaMemsetAsync(d.ff32, 0, 32 * (size_t)d.nSlot * sizeof(float), stream));
       CK(cudaMemsetAsync(d.dq32, 0, 4 * nc * sizeof(float), stream));
       return HAMSTR_GPU_OK;
@@ -227,7 +240,7 @@ struct hamstr_gpu {
    int ensure_blk32()
    {
       if (d.blk32) return HAMSTR_GPU_OK;
-      return dalloc(&d.blk32, 48 * (size_t)std::max(d.nRow, 1), owned);
+      return dalloc(&d.blk32, 48 * 32 * (size_t)std::max(d.tile_rows, 1), owned);
    }
 
    // drop the captured step (launch shapes or constants changed)

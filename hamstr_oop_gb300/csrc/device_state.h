@@ -100,11 +100,18 @@ struct DeviceState {
 
    // mixed-precision defect correction (FP64 residual, FP32 operator)
    float* ff32;            // [nSlot][32] FP32 face Jacobians
-   float* blk32;           // [nRow][48] FP32 assembled blocks A, B, C (B + I), unfused assembly only
-   float* fsc32;           // [nRow][4]
-   float* fac32;           // [nRow][80] FP32 factor records
+   // The FP32 line data is tiled by groups of 32 chains in line_chains
+   // order, one chain per thread: element e of row i of the chain at
+   // position p sits at ((grp_row0[p >> 5] + i) * W + e) * 32 + (p & 31) of
+   // a W-wide record array, so each load or store of a warp is one whole
+   // 128-byte line.  A group takes as many tile rows as its longest chain.
+   float* blk32;           // W = 48: assembled blocks A, B, C (B + I), unfused assembly only
+   float* fsc32;           // W = 4: right-hand side / forward sweep
+   float* fac32;           // W = 80: factor records
    float* facN32;          // [periodic chains][16]
-   int* fac_chains32;      // all chains, longest first (thread per chain)
+   int* grp_row0;          // [groups + 1] first tile row of each group of 32 positions
+   int* tile_row;          // [tile_rows * 32] ADI row at (tile row, lane), -1 for padding
+   int tile_rows;
    float *r32, *r032, *dq32;   // [nCell][4]
    float* g32;             // [nSlot][4] linear face fluxes
    int* line_chains;       // chains of each wave, longest first (thread per chain)

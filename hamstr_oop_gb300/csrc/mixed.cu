@@ -74,10 +74,14 @@ __global__ void __launch_bounds__(kThreads) mx_init_kernel(DeviceState d)
 // faster where chains are short (the autotuner picks)
 __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
 {
-   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-   if (t >= 48 * d.nRow || halted(d)) return;
-   const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
-   if (frozen_cell(d, d.row_scell[row])) return;
+   // one thread per tiled entry (DeviceState: blk32), so stores are whole lines
+   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= 48 * 32 * (size_t)d.tile_rows || halted(d)) return;
+   const int lane = (int)(t & 31);
+   const size_t q = t >> 5;
+   const int e48 = (int)(q % 48), srow = (int)(q / 48), b = e48 >> 4, e = e48 & 15;
+   const int row = d.tile_row[32 * (size_t)srow + lane];
+   if (row < 0 || frozen_cell(d, d.row_scell[row])) return;
    const int* ops = d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b;
    float acc = 0.f;
 #pragma unroll
@@ -100,6 +104,26 @@ __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
    acc *= float(d.dtfac[d.row_scell[row]]);
    if (b == 1 && (e >> 2) == (e & 3)) acc += 1.f;
    d.blk32[t] = acc;
+}
+
+// the tiled index of element e of tile row s in lane `lane` of a W-wide array
+__device__ __forceinline__ size_t tix(int s, int W, int e, int lane)
+{
+   return (((size_t)s * W + e) << 5) + lane;
+}
+
+// 16 consecutive elements of a tiled record (stride 32 floats: each load of
+// a warp is one 128-byte line)
+__device__ __forceinline__ void ld16t(const float* __restrict__ p, float (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) v[m] = p[32 * m];
+}
+
+__device__ __forceinline__ void st16t(float* __restrict__ p, const float (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) p[32 * m] = v[m];
 }
 
 // ---------------- FP32 line solves, one thread per chain ----------------
@@ -166,6 +190,24 @@ __device__ __forceinline__ LUf luf_load(const float* p)
    LUf u;
    u.p0 = v[0]; u.u01 = v[1]; u.u02 = v[2]; u.u03 = v[3]; u.l10 = v[4]; u.p1 = v[5]; u.u12 = v[6]; u.u13 = v[7];
    u.l20 = v[8]; u.l21 = v[9]; u.p2 = v[10]; u.u23 = v[11]; u.l30 = v[12]; u.l31 = v[13]; u.l32 = v[14]; u.p3 = v[15];
+   return u;
+}
+
+// the LU record of a tiled row (stride 32 floats)
+__device__ __forceinline__ void luf_store_t(float* p, const LUf& u)
+{
+   const float v[16] = {u.p0, u.u01, u.u02, u.u03, u.l10, u.p1, u.u12, u.u13,
+                        u.l20, u.l21, u.p2, u.u23, u.l30, u.l31, u.l32, u.p3};
+#pragma unroll
+   for (int m = 0; m < 16; m++) p[32 * m] = v[m];
+}
+
+__device__ __forceinline__ LUf luf_load_t(const float* p)
+{
+   LUf u;
+   u.p0 = p[0]; u.u01 = p[32]; u.u02 = p[64]; u.u03 = p[96]; u.l10 = p[128]; u.p1 = p[160]; u.u12 = p[192];
+   u.u13 = p[224]; u.l20 = p[256]; u.l21 = p[288]; u.p2 = p[320]; u.u23 = p[352]; u.l30 = p[384];
+   u.l31 = p[416]; u.l32 = p[448]; u.p3 = p[480];
    return u;
 }
 
@@ -258,37 +300,37 @@ __device__ __forceinline__ void mx_row(const DeviceState& d, int row, float (&A)
 
 // FUSED: each thread builds its chain's blocks straight from the FP32 face
 // Jacobians (no block array round trip; best for long chains); otherwise
-// it reads the blocks mx_assemble_kernel wrote
+// it reads the blocks mx_assemble_kernel wrote (tile row s, its lane)
 template <bool FUSED>
-__device__ __forceinline__ void mx_rows(const DeviceState& d, int row, float (&A)[16], float (&B)[16], float (&C)[16])
+__device__ __forceinline__ void mx_rows(const DeviceState& d, int row, int s, int lane, float (&A)[16], float (&B)[16],
+                                        float (&C)[16])
 {
    if (FUSED) {
       mx_row(d, row, A, B, C);
    } else {
-      const float* blk = d.blk32 + 48 * (size_t)row;
-      ld16f(blk, A);
-      ld16f(blk + 16, B);
-      ld16f(blk + 32, C);
+      ld16t(d.blk32 + tix(s, 48, 0, lane), A);
+      ld16t(d.blk32 + tix(s, 48, 16, lane), B);
+      ld16t(d.blk32 + tix(s, 48, 32, lane), C);
    }
 }
 
+// all chains, thread p on the chain at position p of line_chains
 template <bool FUSED>
 __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
-   const int ich = d.fac_chains32[t];
+   const int ich = d.line_chains[t];
    if (frozen_chain(d, ich)) return;
-   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
+   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = t & 31, s0 = d.grp_row0[t >> 5];
    const bool per = d.chain_periodic[ich] != 0;
-   float* fac = d.fac32 + (size_t)kRec * row0;
    float A[16], B[16], C[16], cp[16], ap[16];
-   mx_rows<FUSED>(d, row0, A, B, C);
+   mx_rows<FUSED>(d, row0, s0, lane, A, B, C);
    for (int i = 0; i < N; i++) {
       float An[16], Bn[16], Cn[16];
-      if (i + 1 < N) mx_rows<FUSED>(d, row0 + i + 1, An, Bn, Cn);
-      float* rec = fac + (size_t)kRec * i;
-      st16f(rec, A);
+      if (i + 1 < N) mx_rows<FUSED>(d, row0 + i + 1, s0 + i + 1, lane, An, Bn, Cn);
+      float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
+      st16t(rec, A);
       float fill[16];
       if (i > 0) {
          mm_sub(A, cp, B);
@@ -300,7 +342,7 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
          for (int m = 0; m < 16; m++) fill[m] = A[m];
       }
       const LUf u = luf_factor(B);
-      luf_store(rec + 16, u);
+      luf_store_t(rec + 32 * 16, u);
       if (per && i == N - 2) {
 #pragma unroll
          for (int m = 0; m < 16; m++) C[m] += fill[m];
@@ -311,8 +353,8 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
          luf_cols(u, C);
          if (per) luf_cols(u, fill);
       }
-      st16f(rec + 32, C);
-      if (per) st16f(rec + 48, fill);
+      st16t(rec + 32 * 32, C);
+      if (per) st16t(rec + 32 * 48, fill);
 #pragma unroll
       for (int m = 0; m < 16; m++) { cp[m] = C[m]; ap[m] = fill[m]; }
       if (i + 1 < N) {
@@ -326,11 +368,11 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
 #pragma unroll
    for (int m = 0; m < 16; m++) { cN[m] = cp[m]; bN[m] = ((m >> 2) == (m & 3)) ? 1.f : 0.f; }
    for (int i = 0; i < N - 1; i++) {
-      float* rec = fac + (size_t)kRec * i;
+      float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
       float ci[16], ai[16], tt[16];
-      ld16f(rec + 32, ci);
-      ld16f(rec + 48, ai);
-      st16f(rec + 64, cN);
+      ld16t(rec + 32 * 32, ci);
+      ld16t(rec + 32 * 48, ai);
+      st16t(rec + 32 * 64, cN);
 #pragma unroll
       for (int m = 0; m < 16; m++) tt[m] = 0.f;
       mm_sub(cN, ci, tt);
@@ -341,21 +383,21 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
 
-// One sweep's solve of one chain per thread.  The recurrence only carries
-// the 4-vector x in registers; everything a row needs (its factor record,
-// its right-hand side, the cell it writes) is loaded one row ahead, so the
-// loads overlap the previous row's arithmetic.  Solutions go straight to
-// r32 (each cell is written once per chain; chains of a wave share no cell).
+// One sweep's solve of one chain per thread (the chain at position first +
+// t of line_chains).  The recurrence only carries the 4-vector x in
+// registers; everything a row needs (its factor record, its right-hand
+// side, the cell it writes) is loaded one row ahead, so the loads overlap
+// the previous row's arithmetic.  Solutions go straight to r32 (each cell
+// is written once per chain; chains of a wave share no cell).
 __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
-   const int ich = d.line_chains[first + t];
+   const int p = first + t;
+   const int ich = d.line_chains[p];
    if (frozen_chain(d, ich)) return;
-   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
+   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
    const bool per = d.chain_periodic[ich] != 0;
-   const float* fac = d.fac32 + (size_t)kRec * row0;
-   float* fs = d.fsc32 + 4 * (size_t)row0;
    const int* fcell = d.row_fcell + row0;
    const int* scell = d.row_scell + row0;
    // forward: f(i) = LU^{-1}(F(i) - A(i) f(i-1)), F(i) = r[fcell]
@@ -365,7 +407,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    {
       const int fc = fcell[0];
       if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, xr);
-      u = luf_load(fac + 16);
+      u = luf_load_t(d.fac32 + tix(s0, kRec, 16, lane));
 #pragma unroll
       for (int m = 0; m < 16; m++) a[m] = 0.f;
    }
@@ -374,11 +416,11 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       float an[16], xrn[4] = {0.f, 0.f, 0.f, 0.f};
       LUf un;
       if (i + 1 < N) {
-         const float* rn = fac + (size_t)kRec * (i + 1);
+         const float* rn = d.fac32 + tix(s0 + i + 1, kRec, 0, lane);
          const int fcn = fcell[i + 1];
          if (fcn >= 0) ld4(d.r32 + 4 * (size_t)fcn, xrn);
-         ld16f(rn, an);
-         un = luf_load(rn + 16);
+         ld16t(rn, an);
+         un = luf_load_t(rn + 32 * 16);
       }
       float x[4] = {xr[0], xr[1], xr[2], xr[3]};
       if (i > 0) {
@@ -388,7 +430,9 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
             for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-a[4 * k + j], xp[j], x[k]);
       }
       luf_solve(u, x[0], x[1], x[2], x[3]);
-      st4(fs + 4 * i, x);
+      float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+      for (int k = 0; k < 4; k++) fs[32 * k] = x[k];
 #pragma unroll
       for (int k = 0; k < 4; k++) xp[k] = x[k];
       if (i + 1 < N) {
@@ -404,8 +448,10 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       float fN[4] = {xp[0], xp[1], xp[2], xp[3]};
       for (int i = 0; i < N - 1; i++) {
          float c[16], f[4];
-         ld16f(fac + (size_t)kRec * i + 64, c);
-         ld4(fs + 4 * i, f);
+         ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), c);
+         const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+         for (int k = 0; k < 4; k++) f[k] = fs[32 * k];
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
@@ -417,11 +463,13 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
 #pragma unroll
       for (int k = 0; k < 4; k++) xn[k] = fN[k];
       for (int i = N - 2; i >= 0; i--) {
-         const float* rec = fac + (size_t)kRec * i;
+         const float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
          float c[16], aa[16], x[4];
-         ld16f(rec + 32, c);
-         ld16f(rec + 48, aa);
-         ld4(fs + 4 * i, x);
+         ld16t(rec + 32 * 32, c);
+         ld16t(rec + 32 * 48, aa);
+         const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+         for (int k = 0; k < 4; k++) x[k] = fs[32 * k];
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
@@ -441,16 +489,20 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       float c[16], x[4];
       int sc = 0;
       if (N >= 2) {
-         ld16f(fac + (size_t)kRec * (N - 2) + 32, c);
-         ld4(fs + 4 * (N - 2), x);
+         ld16t(d.fac32 + tix(s0 + N - 2, kRec, 32, lane), c);
+         const float* fs = d.fsc32 + tix(s0 + N - 2, 4, 0, lane);
+#pragma unroll
+         for (int k = 0; k < 4; k++) x[k] = fs[32 * k];
          sc = scell[N - 2];
       }
       for (int i = N - 2; i >= 0; i--) {
          float cn[16], xnx[4];
          int scn = 0;
          if (i >= 1) {
-            ld16f(fac + (size_t)kRec * (i - 1) + 32, cn);
-            ld4(fs + 4 * (i - 1), xnx);
+            ld16t(d.fac32 + tix(s0 + i - 1, kRec, 32, lane), cn);
+            const float* fs = d.fsc32 + tix(s0 + i - 1, 4, 0, lane);
+#pragma unroll
+            for (int k = 0; k < 4; k++) xnx[k] = fs[32 * k];
             scn = scell[i - 1];
          }
 #pragma unroll
@@ -588,7 +640,8 @@ void launch_mx_rhs_face(const DeviceState& d, cudaStream_t st)
 
 void launch_mx_assemble(const DeviceState& d, cudaStream_t st)
 {
-   if (!d.mx_fused) mx_assemble_kernel<<<blocks_for(48 * d.nRow), kThreads, 0, st>>>(d);
+   const size_t n = 48 * 32 * (size_t)d.tile_rows;
+   if (!d.mx_fused && n > 0) mx_assemble_kernel<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, st>>>(d);
 }
 
 void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d); }
