@@ -87,26 +87,27 @@ __device__ __forceinline__ bool roe_face(double nxd, double nyd, const double (&
       const double term2 = p2<-1, SD>(eig2 - eig3);
       const double del1 = by_c.div(by_c.div(term1 * dp)) + by_c.div(term2 * robar * (uconr - uconl));
       const double del2 = term1 * (uconr - uconl) * robar + by_c.div(term2 * dp);
-      // without the Jacobian the integer pipes have room for these
-      // multiplies too (SM: sd::mul, identical results)
-      constexpr bool SM = SD && !JAC;
-      double fm0 = pm<SM>(eig1, qr[0] - ql[0]);
-      double fm1 = pm<SM>(eig1, qr[1] - ql[1]);
-      double fm2 = pm<SM>(eig1, qr[2] - ql[2]);
-      double fm3 = pm<SM>(eig1, qr[3] - ql[3]);
+      double fm0 = eig1 * (qr[0] - ql[0]);
+      double fm1 = eig1 * (qr[1] - ql[1]);
+      double fm2 = eig1 * (qr[2] - ql[2]);
+      double fm3 = eig1 * (qr[3] - ql[3]);
       fm0 = fm0 + del1;
-      fm1 = fm1 + pm<SM>(del1, ubar) + pm<SM>(del2, nx);
-      fm2 = fm2 + pm<SM>(del1, vbar) + pm<SM>(del2, ny);
-      fm3 = fm3 + pm<SM>(del1, hbar) + pm<SM>(del2, uconbar);
-      const double fl0 = pm<SM>(rol, uconl), fr0 = pm<SM>(ror, uconr);
-      const double fl1 = pm<SM>(fl0, ul) + pm<SM>(nx, pl), fr1 = pm<SM>(fr0, ur) + pm<SM>(nx, pr);
-      const double fl2 = pm<SM>(fl0, vl) + pm<SM>(ny, pl), fr2 = pm<SM>(fr0, vr) + pm<SM>(ny, pr);
-      const double fl3 = pm<SM>(ql[3] + pl, uconl), fr3 = pm<SM>(qr[3] + pr, uconr);
-      o.flux[0] = pm<SM>(p2<-1, SD>(fl0 + fr0 - fm0), area);
-      o.flux[1] = pm<SM>(p2<-1, SD>(fl1 + fr1 - fm1), area);
-      o.flux[2] = pm<SM>(p2<-1, SD>(fl2 + fr2 - fm2), area);
-      o.flux[3] = pm<SM>(p2<-1, SD>(fl3 + fr3 - fm3), area);
-      spec = pm<SM>(spec, area);
+      fm1 = fm1 + del1 * ubar + del2 * nx;
+      fm2 = fm2 + del1 * vbar + del2 * ny;
+      fm3 = fm3 + del1 * hbar + del2 * uconbar;
+      const double fl0 = rol * uconl, fr0 = ror * uconr;
+      const double fl1 = rol * uconl * ul + nx * pl, fr1 = ror * uconr * ur + nx * pr;
+      const double fl2 = rol * uconl * vl + ny * pl, fr2 = ror * uconr * vr + ny * pr;
+      const double fl3 = (ql[3] + pl) * uconl, fr3 = (qr[3] + pr) * uconr;
+      o.flux[0] = p2<-1, SD>(fl0 + fr0 - fm0);
+      o.flux[1] = p2<-1, SD>(fl1 + fr1 - fm1);
+      o.flux[2] = p2<-1, SD>(fl2 + fr2 - fm2);
+      o.flux[3] = p2<-1, SD>(fl3 + fr3 - fm3);
+      o.flux[0] *= area;
+      o.flux[1] *= area;
+      o.flux[2] *= area;
+      o.flux[3] *= area;
+      spec *= area;
       o.spec = spec;
    }
    if (!JAC) return true;
