@@ -32,27 +32,40 @@ static_assert(kThreads == kNormBlock, "cell kernels run one norm block per threa
 template <int ORDER, bool SD, bool PRE = false>
 __global__ void __launch_bounds__(kThreads) mx_rhs_face_kernel(DeviceState d)
 {
-   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-   if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
-   const int4 sl = d.slot[s];
-   const double2 nv = d.normal[s];
-   double L[4], R[4];
-   if (ORDER == 5 && PRE) face_states_pre(d, s, (sl.w & 1) != 0, L, R);
-   else face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
-   RoeOut o;
-   if (!roe_face<false, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, nullptr, nullptr)) atomicOr(d.status, DEV_ERR_NAN_SPEC);
-   st4(d.flux + 4 * (size_t)s, o.flux);
-   d.spec[s] = o.spec;
-   const float Lf[4] = {float(L[0]), float(L[1]), float(L[2]), float(L[3])};
-   const float Rf[4] = {float(R[0]), float(R[1]), float(R[2]), float(R[3])};
-   float lm[16], rm[16];
-   roe_jacobian_only<float>(float(nv.x), float(nv.y), Lf, Rf, float(d.fc.gamma), lm, rm);
-   float* out = d.ff32 + 32 * (size_t)s;
+   // the FP32 Jacobians leave through shared memory, so their stores are
+   // whole lines (8 float4 per slot, consecutive slots; row stride 9)
+   __shared__ float4 sj[kThreads * 9];
+   __shared__ unsigned char live[kThreads];
+   if (halted(d)) return;
+   const int nb = blockDim.x, s0 = blockIdx.x * nb, s = s0 + threadIdx.x;
+   const bool act = s < d.nSlot && !frozen_slot(d, s);
+   live[threadIdx.x] = act ? 1 : 0;
+   if (act) {
+      const int4 sl = d.slot[s];
+      const double2 nv = d.normal[s];
+      double L[4], R[4];
+      if (ORDER == 5 && PRE) face_states_pre(d, s, (sl.w & 1) != 0, L, R);
+      else face_states<ORDER, SD>(d, sl.x, (sl.w & 1) != 0, L, R);
+      RoeOut o;
+      if (!roe_face<false, SD>(nv.x, nv.y, L, R, d.fc.gamma, o, nullptr, nullptr))
+         atomicOr(d.status, DEV_ERR_NAN_SPEC);
+      st4(d.flux + 4 * (size_t)s, o.flux);
+      d.spec[s] = o.spec;
+      const float Lf[4] = {float(L[0]), float(L[1]), float(L[2]), float(L[3])};
+      const float Rf[4] = {float(R[0]), float(R[1]), float(R[2]), float(R[3])};
+      float lm[16], rm[16];
+      roe_jacobian_only<float>(float(nv.x), float(nv.y), Lf, Rf, float(d.fc.gamma), lm, rm);
 #pragma unroll
-   for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(out + i) = make_float4(lm[i], lm[i + 1], lm[i + 2], lm[i + 3]);
-#pragma unroll
-   for (int i = 0; i < 16; i += 4)
-      *reinterpret_cast<float4*>(out + 16 + i) = make_float4(rm[i], rm[i + 1], rm[i + 2], rm[i + 3]);
+      for (int q = 0; q < 4; q++) {
+         sj[threadIdx.x * 9 + q] = make_float4(lm[4 * q], lm[4 * q + 1], lm[4 * q + 2], lm[4 * q + 3]);
+         sj[threadIdx.x * 9 + 4 + q] = make_float4(rm[4 * q], rm[4 * q + 1], rm[4 * q + 2], rm[4 * q + 3]);
+      }
+   }
+   __syncthreads();
+   const int nloc = min(nb, d.nSlot - s0);
+   float4* __restrict__ dst = reinterpret_cast<float4*>(d.ff32 + 32 * (size_t)s0);
+   for (int c = threadIdx.x; c < 8 * nloc; c += nb)
+      if (live[c >> 3]) dst[c] = sj[(c >> 3) * 9 + (c & 7)];
 }
 
 // r (already scaled by CFL/sigma in FP64) -> FP32 r, r0; dq = 0
@@ -538,12 +551,32 @@ __global__ void __launch_bounds__(kThreads) mx_dq_update_kernel(DeviceState d)
 template <int ORDER>
 __global__ void __launch_bounds__(kThreads) mx_lin_face_kernel(DeviceState d)
 {
-   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+   // the block's face Jacobians staged through shared memory: read with
+   // whole-line loads (8 float4 per slot, consecutive slots), then each
+   // thread takes its own (row stride 9 float4: no bank conflicts)
+   __shared__ float4 sj[kThreads * 9];
+   const int nb = blockDim.x, s0 = blockIdx.x * nb, s = s0 + threadIdx.x;
+   const int nloc = min(nb, d.nSlot - s0);
+   const float4* __restrict__ src = reinterpret_cast<const float4*>(d.ff32 + 32 * (size_t)s0);
+   for (int c = threadIdx.x; c < 8 * nloc; c += nb) sj[(c >> 3) * 9 + (c & 7)] = src[c];
+   __syncthreads();
    if (s >= d.nSlot || halted(d) || frozen_slot(d, s)) return;
    const int4 sl = d.slot[s];
    float dL[4], dR[4];
    face_dstates<ORDER, float>(d, d.dq32, sl.x, (sl.w & 1) != 0, dL, dR);
-   const float* m = d.ff32 + 32 * (size_t)(sl.w >> 1);
+   // the Jacobian kept for this face is its owner slot's (a periodic
+   // chain's repeated face); almost always the slot itself
+   const int own = sl.w >> 1;
+   float m[32];
+#pragma unroll
+   for (int q = 0; q < 8; q++) {
+      const float4 v = (own == s) ? sj[threadIdx.x * 9 + q]
+                                  : reinterpret_cast<const float4*>(d.ff32 + 32 * (size_t)own)[q];
+      m[4 * q] = v.x;
+      m[4 * q + 1] = v.y;
+      m[4 * q + 2] = v.z;
+      m[4 * q + 3] = v.w;
+   }
    float g[4];
 #pragma unroll
    for (int j = 0; j < 4; j++) {
