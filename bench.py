@@ -267,6 +267,17 @@ def run_batch(args, wl, rank, local_rank, world):
     t_setup = time.perf_counter() - t_setup
     nc = g.sizes["nCell"]
     g.set_precision(wl["precision"] == "mixed")
+    if args.profile_steps:
+        # a plain run for ncu: N captured steps after two warm-up steps
+        if args.shape:
+            g.set_shape(**parse_shape(args.shape))
+        g.enqueue_steps(2 + args.profile_steps)
+        g.sync()
+        if rank == 0:
+            print(json.dumps({"profile_steps": args.profile_steps, "workload": wl["name"], "conditions": len(cases),
+                              "cells": nc, "launches_per_step": g.launches_per_step()}), flush=True)
+        g.close()
+        return None
     tune = g.autotune(reps=2)
     hs = torch.cuda.ExternalStream(g.stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -851,6 +862,8 @@ def main():
     ap.add_argument("--c5-train", type=int, default=0, help="c5: training conditions (default: the config's)")
     ap.add_argument("--c5-test", type=int, default=0, help="c5: held-out conditions (default: the config's)")
     ap.add_argument("--msweep", type=int, default=0, help="ADI sweeps per step (default: the workload's, 2)")
+    ap.add_argument("--batch-conditions", type=int, default=0,
+                    help="batched workloads: number of conditions (default: the workload's)")
     ap.add_argument("--shape", default="", help="launch shape instead of the autotuner's, e.g. "
                     "face_block=128,adi_warps_per_sm=8 (hamstr_gpu_set_shape keys)")
     args = ap.parse_args()
@@ -864,6 +877,9 @@ def main():
     if args.msweep:
         wl["name"] = wl["name"].replace("msweep%d" % wl["msweep"], "msweep%d" % args.msweep)
         wl["msweep"] = args.msweep
+    if args.batch_conditions and wl.get("batch"):
+        wl["name"] = wl["name"].replace("batch%d" % wl["n"], "batch%d" % args.batch_conditions)
+        wl["n"] = args.batch_conditions
     if args.impl == "reference":
         out = run_reference(args, wl, rank)
         if out is not None:

@@ -293,14 +293,38 @@ __device__ __forceinline__ void mx_block(const DeviceState& d, const int* __rest
    }
 }
 
-// the three blocks of one ADI row, scaled by CFL/sigma, B + I (ADI.cpp:197-217)
-__device__ __forceinline__ void mx_row(const DeviceState& d, int row, float (&A)[16], float (&B)[16], float (&C)[16])
+// what the fused assembly of one row looks up first: its term lists and
+// its scaled cell (the face Jacobians and the CFL/sigma factor follow from
+// them), loaded a row earlier than the blocks so that each row waits on
+// one memory round trip, not two
+struct RowRef {
+   int4 ops[3];
+   int scell;
+};
+
+__device__ __forceinline__ RowRef mx_rowref(const DeviceState& d, int row)
 {
-   const int* ops = d.row_ops + 3 * kOpsPerBlock * (size_t)row;
-   mx_block(d, ops, A);
-   mx_block(d, ops + kOpsPerBlock, B);
-   mx_block(d, ops + 2 * kOpsPerBlock, C);
-   const float s = float(d.dtfac[d.row_scell[row]]);
+   RowRef r;
+   const int4* p = reinterpret_cast<const int4*>(d.row_ops + 3 * kOpsPerBlock * (size_t)row);
+   r.ops[0] = p[0];
+   r.ops[1] = p[1];
+   r.ops[2] = p[2];
+   r.scell = d.row_scell[row];
+   return r;
+}
+
+// the three blocks of one ADI row from its looked-up references, scaled by
+// CFL/sigma, B + I (ADI.cpp:197-217)
+__device__ __forceinline__ void mx_row_ref(const DeviceState& d, const RowRef& r, float (&A)[16], float (&B)[16],
+                                           float (&C)[16])
+{
+   const int oa[4] = {r.ops[0].x, r.ops[0].y, r.ops[0].z, r.ops[0].w};
+   const int ob[4] = {r.ops[1].x, r.ops[1].y, r.ops[1].z, r.ops[1].w};
+   const int oc[4] = {r.ops[2].x, r.ops[2].y, r.ops[2].z, r.ops[2].w};
+   mx_block(d, oa, A);
+   mx_block(d, ob, B);
+   mx_block(d, oc, C);
+   const float s = float(d.dtfac[r.scell]);
 #pragma unroll
    for (int m = 0; m < 16; m++) {
       A[m] *= s;
@@ -312,14 +336,15 @@ __device__ __forceinline__ void mx_row(const DeviceState& d, int row, float (&A)
 }
 
 // FUSED: each thread builds its chain's blocks straight from the FP32 face
-// Jacobians (no block array round trip; best for long chains); otherwise
-// it reads the blocks mx_assemble_kernel wrote (tile row s, its lane)
+// Jacobians (no block array round trip; best for long chains) from the
+// references r of the row; otherwise it reads the blocks mx_assemble_kernel
+// wrote (tile row s, its lane)
 template <bool FUSED>
-__device__ __forceinline__ void mx_rows(const DeviceState& d, int row, int s, int lane, float (&A)[16], float (&B)[16],
-                                        float (&C)[16])
+__device__ __forceinline__ void mx_rows(const DeviceState& d, const RowRef& r, int s, int lane, float (&A)[16],
+                                        float (&B)[16], float (&C)[16])
 {
    if (FUSED) {
-      mx_row(d, row, A, B, C);
+      mx_row_ref(d, r, A, B, C);
    } else {
       ld16t(d.blk32 + tix(s, 48, 0, lane), A);
       ld16t(d.blk32 + tix(s, 48, 16, lane), B);
@@ -338,10 +363,20 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = t & 31, s0 = d.grp_row0[t >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    float A[16], B[16], C[16], cp[16], ap[16];
-   mx_rows<FUSED>(d, row0, s0, lane, A, B, C);
+   RowRef rnext{};   // fused: references of row i + 1, looked up a row ahead
+   if (FUSED) {
+      const RowRef r0 = mx_rowref(d, row0);
+      if (N > 1) rnext = mx_rowref(d, row0 + 1);
+      mx_rows<FUSED>(d, r0, s0, lane, A, B, C);
+   } else {
+      mx_rows<FUSED>(d, rnext, s0, lane, A, B, C);
+   }
    for (int i = 0; i < N; i++) {
       float An[16], Bn[16], Cn[16];
-      if (i + 1 < N) mx_rows<FUSED>(d, row0 + i + 1, s0 + i + 1, lane, An, Bn, Cn);
+      if (i + 1 < N) {
+         mx_rows<FUSED>(d, rnext, s0 + i + 1, lane, An, Bn, Cn);
+         if (FUSED && i + 2 < N) rnext = mx_rowref(d, row0 + i + 2);
+      }
       float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
       st16t(rec, A);
       float fill[16];
@@ -417,9 +452,11 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    float xp[4] = {0.f, 0.f, 0.f, 0.f};
    float a[16], xr[4] = {0.f, 0.f, 0.f, 0.f};
    LUf u;
+   int fcn = -1;   // the next row's right-hand-side cell, looked up a row ahead
    {
       const int fc = fcell[0];
       if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, xr);
+      if (N > 1) fcn = fcell[1];
       u = luf_load_t(d.fac32 + tix(s0, kRec, 16, lane));
 #pragma unroll
       for (int m = 0; m < 16; m++) a[m] = 0.f;
@@ -430,8 +467,8 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       LUf un;
       if (i + 1 < N) {
          const float* rn = d.fac32 + tix(s0 + i + 1, kRec, 0, lane);
-         const int fcn = fcell[i + 1];
          if (fcn >= 0) ld4(d.r32 + 4 * (size_t)fcn, xrn);
+         fcn = (i + 2 < N) ? fcell[i + 2] : -1;
          ld16t(rn, an);
          un = luf_load_t(rn + 32 * 16);
       }
