@@ -473,18 +473,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
 #pragma unroll
       for (int m = 0; m < 16; m++) a[m] = 0.f;
    }
-   // rows further ahead are pulled into L1 early: lane l asks for the line
-   // of element l (A and LU) of row i + kAhead, and for its own right-hand
-   // side cell (looked up a row before that)
-   constexpr int kAhead = 4;
-   int fcp = (kAhead < N) ? fcell[kAhead] : -1;
    for (int i = 0; i < N; i++) {
-      if (i + kAhead < N) {
-         const float* line = d.fac32 + tix(s0 + i + kAhead, kRec, lane, lane);
-         asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
-         if (fcp >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(d.r32 + 4 * (size_t)fcp));
-         fcp = (i + kAhead + 1 < N) ? fcell[i + kAhead + 1] : -1;
-      }
       // next row's record and right-hand side, in flight during this row
       float an[16], xrn[4] = {0.f, 0.f, 0.f, 0.f};
       LUf un;
