@@ -415,19 +415,11 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    float cN[16], bN[16];
 #pragma unroll
    for (int m = 0; m < 16; m++) { cN[m] = cp[m]; bN[m] = ((m >> 2) == (m & 3)) ? 1.f : 0.f; }
-   // row i+1's c' and a' are loaded while row i is eliminated
-   float ci[16], ai[16];
-   if (N > 1) {
-      ld16t(d.fac32 + tix(s0, kRec, 32, lane), ci);
-      ld16t(d.fac32 + tix(s0, kRec, 48, lane), ai);
-   }
    for (int i = 0; i < N - 1; i++) {
       float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
-      float cin[16], ain[16], tt[16];
-      if (i + 1 < N - 1) {
-         ld16t(rec + 32 * (kRec + 32), cin);
-         ld16t(rec + 32 * (kRec + 48), ain);
-      }
+      float ci[16], ai[16], tt[16];
+      ld16t(rec + 32 * 32, ci);
+      ld16t(rec + 32 * 48, ai);
       st16t(rec + 32 * 64, cN);
 #pragma unroll
       for (int m = 0; m < 16; m++) tt[m] = 0.f;
@@ -435,10 +427,6 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
       mm_sub(cN, ai, bN);
 #pragma unroll
       for (int m = 0; m < 16; m++) cN[m] = tt[m];
-      if (i + 1 < N - 1) {
-#pragma unroll
-         for (int m = 0; m < 16; m++) { ci[m] = cin[m]; ai[m] = ain[m]; }
-      }
    }
    luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
@@ -508,78 +496,40 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    float xn[4];
    if (per) {
       float fN[4] = {xp[0], xp[1], xp[2], xp[3]};
-      // row i+1's c_N and f are loaded while row i is eliminated
-      float c[16], f[4];
-      if (N > 1) {
-         ld16t(d.fac32 + tix(s0, kRec, 64, lane), c);
-         const float* fs = d.fsc32 + tix(s0, 4, 0, lane);
+      for (int i = 0; i < N - 1; i++) {
+         float c[16], f[4];
+         ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), c);
+         const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
          for (int k = 0; k < 4; k++) f[k] = fs[32 * k];
-      }
-      for (int i = 0; i < N - 1; i++) {
-         float cn[16], fn[4];
-         if (i + 1 < N - 1) {
-            ld16t(d.fac32 + tix(s0 + i + 1, kRec, 64, lane), cn);
-            const float* fs = d.fsc32 + tix(s0 + i + 1, 4, 0, lane);
-#pragma unroll
-            for (int k = 0; k < 4; k++) fn[k] = fs[32 * k];
-         }
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
             for (int j = 0; j < 4; j++) fN[k] = __fmaf_rn(-c[4 * k + j], f[j], fN[k]);
-         if (i + 1 < N - 1) {
-#pragma unroll
-            for (int m = 0; m < 16; m++) c[m] = cn[m];
-#pragma unroll
-            for (int k = 0; k < 4; k++) f[k] = fn[k];
-         }
       }
       const LUf uN = luf_load(d.facN32 + 16 * d.chain_facN[ich]);
       luf_solve(uN, fN[0], fN[1], fN[2], fN[3]);
       st4(d.r32 + 4 * (size_t)scell[N - 1], fN);
 #pragma unroll
       for (int k = 0; k < 4; k++) xn[k] = fN[k];
-      // back substitution, row i-1's records, f and cell loaded while row i is solved
-      float cb[16], ab[16], xb[4];
-      int sb = 0;
-      if (N >= 2) {
-         ld16t(d.fac32 + tix(s0 + N - 2, kRec, 32, lane), cb);
-         ld16t(d.fac32 + tix(s0 + N - 2, kRec, 48, lane), ab);
-         const float* fs = d.fsc32 + tix(s0 + N - 2, 4, 0, lane);
-#pragma unroll
-         for (int k = 0; k < 4; k++) xb[k] = fs[32 * k];
-         sb = scell[N - 2];
-      }
       for (int i = N - 2; i >= 0; i--) {
-         float cbn[16], abn[16], xbn[4];
-         int sbn = 0;
-         if (i >= 1) {
-            ld16t(d.fac32 + tix(s0 + i - 1, kRec, 32, lane), cbn);
-            ld16t(d.fac32 + tix(s0 + i - 1, kRec, 48, lane), abn);
-            const float* fs = d.fsc32 + tix(s0 + i - 1, 4, 0, lane);
+         const float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
+         float c[16], aa[16], x[4];
+         ld16t(rec + 32 * 32, c);
+         ld16t(rec + 32 * 48, aa);
+         const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-            for (int k = 0; k < 4; k++) xbn[k] = fs[32 * k];
-            sbn = scell[i - 1];
-         }
-         float x[4] = {xb[0], xb[1], xb[2], xb[3]};
+         for (int k = 0; k < 4; k++) x[k] = fs[32 * k];
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-               const float sv = (i == N - 2) ? cb[4 * k + j] * xn[j] : __fmaf_rn(ab[4 * k + j], fN[j], cb[4 * k + j] * xn[j]);
+               const float sv = (i == N - 2) ? c[4 * k + j] * xn[j] : __fmaf_rn(aa[4 * k + j], fN[j], c[4 * k + j] * xn[j]);
                x[k] -= sv;
             }
-         st4(d.r32 + 4 * (size_t)sb, x);
+         st4(d.r32 + 4 * (size_t)scell[i], x);
 #pragma unroll
          for (int k = 0; k < 4; k++) xn[k] = x[k];
-         if (i >= 1) {
-#pragma unroll
-            for (int m = 0; m < 16; m++) { cb[m] = cbn[m]; ab[m] = abn[m]; }
-#pragma unroll
-            for (int k = 0; k < 4; k++) xb[k] = xbn[k];
-            sb = sbn;
-         }
       }
    } else {
 #pragma unroll
