@@ -328,7 +328,7 @@ def run_batch(args, wl, rank, local_rank, world):
     for _ in range(e2e_steps):
         g.set("q", qnp)
         g.step()
-        qnp[:] = g.get("q")
+        g.get("q", out=qnp)
         g.instance_norms()
     e2e_s = time.perf_counter() - t0
     out = None
@@ -667,7 +667,7 @@ def run_gpu(args, wl, rank, local_rank, world):
     for _ in range(e2e_steps):
         gpu.set("q", qnp)
         gpu.step()
-        qnp[:] = gpu.get("q")
+        gpu.get("q", out=qnp)
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")

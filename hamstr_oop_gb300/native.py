@@ -350,9 +350,15 @@ class GpuSolver:
     def update_solution(self, qold: str, qnew: str, coef: float) -> None:
         _check(load().hamstr_gpu_update_solution(self.h, qold.encode(), qnew.encode(), coef))
 
-    def get(self, name: str) -> np.ndarray:
+    def get(self, name: str, out: np.ndarray = None) -> np.ndarray:
+        """Copy a device array to the host; `out` (contiguous float64 of the
+        right size, e.g. a pinned buffer) receives it in place of a new array."""
         key, w = self._DW[name]
-        out = np.zeros(self.sizes[key] * w)
+        n = self.sizes[key] * w
+        if out is None:
+            out = np.zeros(n)
+        elif out.dtype != np.float64 or out.size != n or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("%s needs a contiguous float64 array of %d values" % (name, n))
         _check(load().hamstr_gpu_get(self.h, name.encode(), _ptr(out)))
         return out
 
