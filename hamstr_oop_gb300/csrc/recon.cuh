@@ -568,7 +568,7 @@ __device__ __forceinline__ void face_dstates(const DeviceState& d, const T* __re
 // One order-5 face state: component k of side `side` (0: left-biased at
 // stencil n, 1: right-biased at n+1) of slot s, into d.qface[(4*side + k) *
 // nSlot + s]; with WL also the f-only values of its linearisation into
-// d.wlin (layout of face_states_w5).  The face kernels then read the
+// d.wlin[(18*(4*side + k) + v) * nSlot + s].  The face kernels then read the
 // states: computeRHS.cpp:266-304 with its 8 reconstructions per face spread
 // over 8 threads.
 template <bool SD, bool WL>
