@@ -185,14 +185,29 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
    }
 }
 
-// the same for two open chains, one per half-warp, straight from r and
-// back into it
+// the same for two open chains, one per half-warp
 __device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib, int lane)
 {
-   const int ich = (lane >> 4) ? ib : ia;
+   const int ich = (lane >> 4) ? ib : ia, l16 = lane & 15;
    const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
-   solve_line_pair(d.fac + (size_t)kFacRec * row0, N, d.r, d.row_fcell + row0, d.row_scell + row0,
-                   d.fsc + 4 * (size_t)row0, lane);
+   double* fs = d.fsc + 4 * (size_t)row0;
+   for (int r = l16; r < N; r += 16) {
+      const int fc = d.row_fcell[row0 + r];
+      double v[4] = {0.0, 0.0, 0.0, 0.0};
+      if (fc >= 0) ld4(d.r + 4 * (size_t)fc, v);
+      *reinterpret_cast<double2*>(fs + 4 * r) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
+   }
+   __syncwarp();
+   solve_line_pair(d.fac + (size_t)kFacRec * row0, N, fs, lane);
+   __syncwarp();
+   for (int r = l16; r < N; r += 16) {
+      const int sc = d.row_scell[row0 + r];
+      double v[4];
+      ld4(fs + 4 * r, v);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc + 2) = make_double2(v[2], v[3]);
+   }
 }
 
 __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sweep, int wave, int nwarps)

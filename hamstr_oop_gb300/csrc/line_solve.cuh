@@ -248,24 +248,15 @@ __device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, 
 }
 
 // Right-hand-side replay of two factored open lines, one per half-warp:
-// the operations of solve_line's open branch on lanes 0-15, per half.  The
-// right-hand side comes straight from rv[4*fcell[i]] (zero where fcell <
-// 0) and the solution goes straight to rv[4*scell[i]]; fs holds the forward
-// sweep's rows.  Row i+1's record and right-hand side are loaded while row
-// i is solved, its cell index a row before that.
-__device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, int N, double* __restrict__ rv,
-                                                const int* __restrict__ fcell, const int* __restrict__ scell,
-                                                double* __restrict__ fs, int lane)
+// the operations of solve_line's open branch on lanes 0-15, per half.
+__device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs, int lane)
 {
    const int e = lane & 15, pj = e & 3, r = lane & 3, hb = lane & 16;
    const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
    double xprev[4] = {0.0, 0.0, 0.0, 0.0};
    double fv = 0.0, av = 0.0, lu[4] = {0.0, 0.0, 0.0, 0.0};
-   int fcn = -1;
    if (N > 0) {
-      const int fc = fcell[0];
-      if (fc >= 0) fv = rv[4 * (size_t)fc + r];
-      if (N > 1) fcn = fcell[1];
+      fv = fs[r];
 #pragma unroll
       for (int c = 0; c < 4; c++) lu[c] = fac[16 + 4 * r + c];
    }
@@ -273,8 +264,7 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
       double fvn = 0.0, avn = 0.0, lun[4] = {0.0, 0.0, 0.0, 0.0};
       if (i + 1 < N) {
          const double* nr = fac + (size_t)kFacRec * (i + 1);
-         if (fcn >= 0) fvn = rv[4 * (size_t)fcn + r];
-         fcn = (i + 2 < N) ? fcell[i + 2] : -1;
+         fvn = fs[4 * (i + 1) + r];
          avn = nr[e];
 #pragma unroll
          for (int c = 0; c < 4; c++) lun[c] = nr[16 + 4 * r + c];
@@ -298,8 +288,6 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
       av = avn;
    }
    __syncwarp();
-   // the last row's solution is its forward one
-   if (e < 4 && N > 0) rv[4 * (size_t)scell[N - 1] + e] = sel4(xprev, e);
    // back substitution f(i) -= c'(i) f(i+1), i = N-2..0; the halves run
    // t = 0..Nmax-2 with i = N-2-t
    double xnext[4];
@@ -323,7 +311,7 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
       for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, prod, hb + 4 * r + jj);
 #pragma unroll
       for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, hb + m);
-      if (e < 4 && ii >= 0) rv[4 * (size_t)scell[ii] + e] = x;
+      if (e < 4 && ii >= 0) fs[4 * ii + e] = x;
       mv = mvn;
       xi = xin;
    }
