@@ -87,6 +87,19 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest x over the ranks: a replicated job takes as long as its
+    slowest rank (an all-reduce on the process group, NCCL on GPUs, gloo on
+    the host)."""
+    if world <= 1:
+        return x
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_case(wl: dict, rank: int) -> str:
     from hamstr_oop_gb300 import meshgen  # noqa: F401
     base = os.environ.get("HAMSTR_BENCH_DIR", "/tmp/hamstr_bench")
@@ -299,11 +312,7 @@ def run_batch(args, wl, rank, local_rank, world):
     g.sync()
     torch.cuda.synchronize()
     clocks = sampler.stop()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
     value = world * nc * args.steps / (ms * 1e-3)
     prof = g.profile_step(reps=2) if rank == 0 else {}
     # the same batch with the FP64 operator, for comparison
@@ -630,11 +639,8 @@ def run_gpu(args, wl, rank, local_rank, world):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), world)
     if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
     value = world * nc * args.steps / (ms * 1e-3)
 
@@ -668,11 +674,7 @@ def run_gpu(args, wl, rank, local_rank, world):
         gpu.set("q", qnp)
         gpu.step()
         gpu.get("q", out=qnp)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = {"value": world * nc * e2e_steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": 32 * nc, "d2h_bytes_per_step": 32 * nc + 32, "steps": e2e_steps}
 
