@@ -115,6 +115,7 @@ struct hamstr_gpu {
    // implicit computeRHS for the sweeps (d.wlin points here when on)
    double* wlin_buf = nullptr;
    int weno_keep = 1;
+   int mx_chunk = 1;                    // FP32 solve: rows loaded in chunks where a wave's chains all fit
    bool wlin_valid = false;             // kept values match the current q (standalone entry points)
 
    // instances (a plain handle has one)
@@ -281,7 +282,7 @@ struct hamstr_gpu {
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int lanes,
-                   int wkeep, int bundle)
+                   int wkeep, int bundle, int chunk)
    {
       if (wkeep && d.recon == 5) {
          const int st = ensure_wlin();
@@ -309,6 +310,8 @@ struct hamstr_gpu {
       d.face_block = face_block;
       d.adi_wpb = adi_wpb;
       d.mx_block = mx_block;
+      mx_chunk = chunk;
+      d.mx_chunk_chains = chunk ? mx_solve_chunk_capacity(mx_block) : 0;
       invalidate();
       return HAMSTR_GPU_OK;
    }
@@ -571,6 +574,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.face_block = 256;
       d.adi_wpb = 4;
       d.mx_block = 64;
+      d.mx_chunk_chains = mx_solve_chunk_capacity(d.mx_block);
       // FP32 assembly inside the factorisation pays off on long chains, as
       // do the hardware pivot divisions (their latency is shorter per row)
       d.mx_fused = (P.nChain > 0 && P.nRow >= 16 * P.nChain) ? 1 : 0;
@@ -1096,7 +1100,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
    struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle; float ms; };
-   const int wk = g->weno_keep;
+   const int wk = g->weno_keep, ck = g->mx_chunk;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
@@ -1122,7 +1126,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1144,7 +1148,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
-                       best->bundle);
+                       best->bundle, ck);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1174,7 +1178,7 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
-                                  d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle};
+                                  d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle, g->mx_chunk};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1186,12 +1190,12 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
-                   (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64);
+                   (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

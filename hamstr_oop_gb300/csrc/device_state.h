@@ -95,6 +95,7 @@ struct DeviceState {
    int adi_wpb;            // warps per block (= per SM) of the persistent FP64 line kernels (4 or 8)
    int mx_block;           // threads per block of the FP32 thread-per-chain line kernels
    int mx_fused;           // 1: FP32 blocks assembled inside the factorisation; 0: mx_assemble first
+   int mx_chunk_chains;    // FP32 line kernels over at most this many chains load rows in chunks (all resident)
    int face_soft;          // 1: FP64 divisions of the face kernels on the integer pipes (softdiv.cuh)
    int piv_soft;           // 1: the same for the LU pivots of the FP64 line factorisation
 
@@ -181,6 +182,8 @@ void launch_mx_init(const DeviceState& d, cudaStream_t st);
 void launch_mx_assemble(const DeviceState& d, cudaStream_t st);   // no-op when d.mx_fused
 void launch_mx_factor(const DeviceState& d, cudaStream_t st);
 void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st);
+// chains the chunked FP32 solve holds resident at once with `block` threads per block (0 on error)
+int mx_solve_chunk_capacity(int block);
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);

@@ -143,8 +143,8 @@ __device__ __forceinline__ void st16t(float* __restrict__ p, const float (&v)[16
 // The same split as the FP64 path: the block factorisation runs once per
 // step (mx_factor), each sweep replays the right-hand side (mx_solve).  One
 // thread carries a whole chain in registers (FP32 latency is 4 cycles, so
-// the recurrence is short), rows are prefetched one ahead, and products use
-// FMA since this operator is approximate by design.  Record layout per row
+// the recurrence is short), rows are loaded one ahead or several rows at a
+// time, and products use FMA since this operator is approximate by design.  Record layout per row
 // (80 floats): A, LU of B', C', fill-in a', c_{N-1} at elimination step i.
 constexpr int kRec = 80;
 
@@ -352,8 +352,14 @@ __device__ __forceinline__ void mx_rows(const DeviceState& d, const RowRef& r, i
    }
 }
 
-// all chains, thread p on the chain at position p of line_chains
-template <bool FUSED>
+// rows of the periodic last-row elimination whose loads issue together
+// where all chains are resident at once (1 otherwise: there the kernel is
+// bound by throughput, not by one chain's round trips)
+constexpr int kElimChunk = 2;
+
+// all chains, thread p on the chain at position p of line_chains; ED rows of
+// the last-row elimination per chunk
+template <bool FUSED, int ED>
 __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count)
 {
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -411,22 +417,34 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
       }
    }
    if (!per) return;
-   // last-row elimination (triSolvers.cpp:967-999)
+   // last-row elimination (triSolvers.cpp:967-999).  A row's arithmetic is
+   // short, so the loads of ED rows are issued before it; the main loop's
+   // arrays are dead here, so a chunk of 2 adds no registers.
+   constexpr int D = ED;
    float cN[16], bN[16];
 #pragma unroll
    for (int m = 0; m < 16; m++) { cN[m] = cp[m]; bN[m] = ((m >> 2) == (m & 3)) ? 1.f : 0.f; }
-   for (int i = 0; i < N - 1; i++) {
-      float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
-      float ci[16], ai[16], tt[16];
-      ld16t(rec + 32 * 32, ci);
-      ld16t(rec + 32 * 48, ai);
-      st16t(rec + 32 * 64, cN);
+   for (int i0 = 0; i0 < N - 1; i0 += D) {
+      float ci[D][16], ai[D][16];
 #pragma unroll
-      for (int m = 0; m < 16; m++) tt[m] = 0.f;
-      mm_sub(cN, ci, tt);
-      mm_sub(cN, ai, bN);
+      for (int u = 0; u < D; u++)
+         if (i0 + u < N - 1) {
+            const float* rec = d.fac32 + tix(s0 + i0 + u, kRec, 0, lane);
+            ld16t(rec + 32 * 32, ci[u]);
+            ld16t(rec + 32 * 48, ai[u]);
+         }
 #pragma unroll
-      for (int m = 0; m < 16; m++) cN[m] = tt[m];
+      for (int u = 0; u < D; u++)
+         if (i0 + u < N - 1) {
+            st16t(d.fac32 + tix(s0 + i0 + u, kRec, 64, lane), cN);
+            float tt[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) tt[m] = 0.f;
+            mm_sub(cN, ci[u], tt);
+            mm_sub(cN, ai[u], bN);
+#pragma unroll
+            for (int m = 0; m < 16; m++) cN[m] = tt[m];
+         }
    }
    luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
 }
@@ -568,6 +586,174 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
 #pragma unroll
             for (int k = 0; k < 4; k++) x[k] = xnx[k];
             sc = scn;
+         }
+      }
+   }
+}
+
+// rows whose loads mx_solve_chunk_kernel issues together
+constexpr int kSolveChunk = 4;
+
+// The same solve with the loads of kSolveChunk rows issued together before
+// their arithmetic, in each of the row loops.  A row's own arithmetic is a
+// few dozen dependent FP32 operations, far shorter than one memory round
+// trip, so a chain of N rows waits about N / kSolveChunk round trips instead
+// of N.  The operations and their order are those of mx_solve_kernel, so
+// the results are identical.  It takes more registers; the host launches it
+// for waves whose chains are all resident at once.
+__global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int first, int count)
+{
+   constexpr int D = kSolveChunk;
+   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+   if (t >= count || halted(d)) return;
+   const int p = first + t;
+   const int ich = d.line_chains[p];
+   if (frozen_chain(d, ich)) return;
+   const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
+   const bool per = d.chain_periodic[ich] != 0;
+   const int* fcell = d.row_fcell + row0;
+   const int* scell = d.row_scell + row0;
+   // forward: f(i) = LU^{-1}(F(i) - A(i) f(i-1)), F(i) = r[fcell]; the
+   // right-hand-side cells of a chunk are looked up during the chunk before
+   float xp[4] = {0.f, 0.f, 0.f, 0.f};
+   int fcb[D];
+#pragma unroll
+   for (int u = 0; u < D; u++) fcb[u] = (u < N) ? fcell[u] : -1;
+   for (int i0 = 0; i0 < N; i0 += D) {
+      float ab[D][16], xb[D][4];
+      LUf ub[D];
+#pragma unroll
+      for (int u = 0; u < D; u++) {
+         const int i = i0 + u;
+#pragma unroll
+         for (int k = 0; k < 4; k++) xb[u][k] = 0.f;
+         if (i < N) {
+            const float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
+            if (fcb[u] >= 0) ld4(d.r32 + 4 * (size_t)fcb[u], xb[u]);
+            if (i > 0) ld16t(rec, ab[u]);
+            ub[u] = luf_load_t(rec + 32 * 16);
+         }
+      }
+#pragma unroll
+      for (int u = 0; u < D; u++) fcb[u] = (i0 + D + u < N) ? fcell[i0 + D + u] : -1;
+#pragma unroll
+      for (int u = 0; u < D; u++) {
+         const int i = i0 + u;
+         if (i < N) {
+            float x[4] = {xb[u][0], xb[u][1], xb[u][2], xb[u][3]};
+            if (i > 0) {
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+#pragma unroll
+                  for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-ab[u][4 * k + j], xp[j], x[k]);
+            }
+            luf_solve(ub[u], x[0], x[1], x[2], x[3]);
+            float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+            for (int k = 0; k < 4; k++) fs[32 * k] = x[k];
+#pragma unroll
+            for (int k = 0; k < 4; k++) xp[k] = x[k];
+         }
+      }
+   }
+   float xn[4];
+   if (per) {
+      // last row: f(N-1) - sum over i < N-1 of cN(i) f(i), in row order
+      float fN[4] = {xp[0], xp[1], xp[2], xp[3]};
+      for (int i0 = 0; i0 < N - 1; i0 += D) {
+         float cb[D][16], fb[D][4];
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            const int i = i0 + u;
+            if (i < N - 1) {
+               ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), cb[u]);
+               const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+            }
+         }
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            if (i0 + u < N - 1) {
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+#pragma unroll
+                  for (int j = 0; j < 4; j++) fN[k] = __fmaf_rn(-cb[u][4 * k + j], fb[u][j], fN[k]);
+            }
+         }
+      }
+      const LUf uN = luf_load(d.facN32 + 16 * d.chain_facN[ich]);
+      luf_solve(uN, fN[0], fN[1], fN[2], fN[3]);
+      st4(d.r32 + 4 * (size_t)scell[N - 1], fN);
+#pragma unroll
+      for (int k = 0; k < 4; k++) xn[k] = fN[k];
+      // back substitution with the fill-in column, rows N-2 down to 0
+      for (int i0 = N - 2; i0 >= 0; i0 -= D) {
+         float cb[D][16], ab[D][16], fb[D][4];
+         int sb[D];
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            const int i = i0 - u;
+            if (i >= 0) {
+               const float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
+               ld16t(rec + 32 * 32, cb[u]);
+               ld16t(rec + 32 * 48, ab[u]);
+               const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+               sb[u] = scell[i];
+            }
+         }
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            const int i = i0 - u;
+            if (i >= 0) {
+               float x[4] = {fb[u][0], fb[u][1], fb[u][2], fb[u][3]};
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+#pragma unroll
+                  for (int j = 0; j < 4; j++) {
+                     const float sv = (i == N - 2) ? cb[u][4 * k + j] * xn[j]
+                                                   : __fmaf_rn(ab[u][4 * k + j], fN[j], cb[u][4 * k + j] * xn[j]);
+                     x[k] -= sv;
+                  }
+               st4(d.r32 + 4 * (size_t)sb[u], x);
+#pragma unroll
+               for (int k = 0; k < 4; k++) xn[k] = x[k];
+            }
+         }
+      }
+   } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) xn[k] = xp[k];
+      st4(d.r32 + 4 * (size_t)scell[N - 1], xn);
+      // back substitution, rows N-2 down to 0
+      for (int i0 = N - 2; i0 >= 0; i0 -= D) {
+         float cb[D][16], fb[D][4];
+         int sb[D];
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            const int i = i0 - u;
+            if (i >= 0) {
+               ld16t(d.fac32 + tix(s0 + i, kRec, 32, lane), cb[u]);
+               const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
+#pragma unroll
+               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+               sb[u] = scell[i];
+            }
+         }
+#pragma unroll
+         for (int u = 0; u < D; u++) {
+            if (i0 - u >= 0) {
+               float x[4] = {fb[u][0], fb[u][1], fb[u][2], fb[u][3]};
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+#pragma unroll
+                  for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-cb[u][4 * k + j], xn[j], x[k]);
+               st4(d.r32 + 4 * (size_t)sb[u], x);
+#pragma unroll
+               for (int k = 0; k < 4; k++) xn[k] = x[k];
+            }
          }
       }
    }
@@ -719,14 +905,33 @@ void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<bl
 void launch_mx_factor(const DeviceState& d, cudaStream_t st)
 {
    const int tb = d.mx_block;
-   if (d.mx_fused) mx_factor_kernel<true><<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
-   else mx_factor_kernel<false><<<(d.nChain + tb - 1) / tb, tb, 0, st>>>(d, d.nChain);
+   const unsigned nb = (d.nChain + tb - 1) / tb;
+   const bool chunk = d.nChain <= d.mx_chunk_chains;
+   if (d.mx_fused) {
+      if (chunk) mx_factor_kernel<true, kElimChunk><<<nb, tb, 0, st>>>(d, d.nChain);
+      else mx_factor_kernel<true, 1><<<nb, tb, 0, st>>>(d, d.nChain);
+   } else {
+      if (chunk) mx_factor_kernel<false, kElimChunk><<<nb, tb, 0, st>>>(d, d.nChain);
+      else mx_factor_kernel<false, 1><<<nb, tb, 0, st>>>(d, d.nChain);
+   }
 }
 
 void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st)
 {
    const int tb = d.mx_block;
-   if (count > 0) mx_solve_kernel<<<(count + tb - 1) / tb, tb, 0, st>>>(d, first, count);
+   if (count <= 0) return;
+   if (count <= d.mx_chunk_chains) mx_solve_chunk_kernel<<<(count + tb - 1) / tb, tb, 0, st>>>(d, first, count);
+   else mx_solve_kernel<<<(count + tb - 1) / tb, tb, 0, st>>>(d, first, count);
+}
+
+int mx_solve_chunk_capacity(int block)
+{
+   int dev = 0, sms = 0, per_sm = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_solve_chunk_kernel, block, 0) != cudaSuccess)
+      return 0;
+   return sms * per_sm * block;
 }
 
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)

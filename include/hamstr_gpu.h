@@ -218,9 +218,13 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       tuned by hamstr_gpu_autotune)
  *   [8] FP64 line kernels: open chains of at most this many rows go 32 to
  *       a warp, one per lane (0: none): 0..64
+ *   [9] FP32 line kernels: the loads of several rows issued together (4 in
+ *       the solve, 2 in the periodic elimination), where the launch's chains
+ *       are all resident at once with the larger register count this takes:
+ *       0 or 1 (default 1; not tuned)
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
  * not depend on the shape. */
-#define HAMSTR_SHAPE_N 9
+#define HAMSTR_SHAPE_N 10
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

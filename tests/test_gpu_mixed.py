@@ -54,3 +54,31 @@ def test_mixed_batched_line_solve_runs_all_orders(make_case, native_lib):
         case, g = _solver(make_case, 16, 5, True, order=order, msweep=3)
         h, _ = g.march(5, 0.0)
         assert np.all(np.isfinite(h[:, :2]))
+
+
+@pytest.mark.parametrize("split,order", [(0.0, 1), (0.5, 5)])
+def test_chunked_fp32_solve_matches_row_by_row(make_case, native_lib, split, order):
+    """The FP32 line solve that loads rows four at a time (shape key mx_chunk)
+    does the row-by-row solve's operations in its order: identical states, on
+    periodic loops and open lines, with either block assembly."""
+    from hamstr_oop_gb300 import native
+    case = make_case(40, 12, split=split, seed=1, order=order, CFL=10.0, msweep=2)
+    solvers = []
+    for _ in range(2):
+        host = native.Case(case)
+        if split:
+            host.set_option("chain_end_rule", 1)     # the split mesh's open chains end at interior faces
+        solvers.append(native.GpuSolver(host))
+    a, b = solvers
+    for g in (a, b):
+        g.set_precision(True)
+    assert a.shape()["mx_chunk"] == 1
+    b.set_shape(mx_chunk=0)
+    q0 = a.get("q")
+    for fused in (0, 1):
+        for g in (a, b):
+            g.set("q", q0)
+            g.set_shape(mx_fused=fused)
+        ha, _ = a.march(4, 0.0)
+        hb, _ = b.march(4, 0.0)
+        assert np.array_equal(ha, hb) and np.array_equal(a.get("q"), b.get("q")), fused
