@@ -42,7 +42,10 @@ namespace {
 
 
 // one block entry (row-major element e) in the reference's term order
-// (ADI.cpp:103-188): 0.0, then += / -= the listed face-matrix entries
+// (ADI.cpp:103-188): 0.0, then += / -= the listed face-matrix entries.
+// The first term needs no FP64 add: 0.0 + v is v and 0.0 - v is -v, except
+// that both are +0.0 when v is a zero, so it is formed on the integer pipes
+// with the same result (this kernel is FP64-issue bound).
 __device__ __forceinline__ double assemble(const DeviceState& d, const int* __restrict__ ops, int e)
 {
    double acc = 0.0;
@@ -62,8 +65,15 @@ __device__ __forceinline__ double assemble(const DeviceState& d, const int* __re
       } else {
          v = m[(sel == OP_SEL_L ? 0 : 16) + e];
       }
-      if (op & 1) acc -= v;
-      else acc += v;
+      if (o == 0) {
+         const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+         const unsigned long long flip = (op & 1) ? 0x8000000000000000ull : 0ull;
+         acc = __longlong_as_double((long long)(((u << 1) == 0) ? 0ull : (u ^ flip)));
+      } else if (op & 1) {
+         acc -= v;
+      } else {
+         acc += v;
+      }
    }
    return acc;
 }
@@ -78,7 +88,7 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
    const int row = t / 48, e48 = t - 48 * row, b = e48 >> 4, e = e48 & 15;
    if (frozen_cell(d, d.row_scell[row])) return;
    double v = assemble(d, d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b, e);
-   v *= d.dtfac[d.row_scell[row]];
+   v = sd::mul(v, d.dtfac[d.row_scell[row]]);   // v * CFL/sigma on the integer pipes, identical
    if (b == 1 && (e >> 2) == (e & 3)) v += 1.0;
    d.blk[t] = v;
 }
