@@ -66,9 +66,7 @@ __device__ __forceinline__ double assemble(const DeviceState& d, const int* __re
          v = m[(sel == OP_SEL_L ? 0 : 16) + e];
       }
       if (o == 0) {
-         const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-         const unsigned long long flip = (op & 1) ? 0x8000000000000000ull : 0ull;
-         acc = __longlong_as_double((long long)(((u << 1) == 0) ? 0ull : (u ^ flip)));
+         acc = sd::zero_plus(v, (op & 1) != 0);
       } else if (op & 1) {
          acc -= v;
       } else {

@@ -237,6 +237,15 @@ __host__ __device__ __forceinline__ double mul(double a, double b)
    return from_bits(sign | ((uint64_t)e << 52) | (m & kMant));
 }
 
+// 0.0 + v (sub false) or 0.0 - v (sub true) on the integer pipes, equal to
+// the FP64 add: +-v with the sign flipped for sub, except that a zero v
+// gives +0.0 either way
+__host__ __device__ __forceinline__ double zero_plus(double v, bool sub)
+{
+   const uint64_t u = bits(v);
+   return from_bits(((u << 1) == 0) ? 0ull : (sub ? u ^ 0x8000000000000000ull : u));
+}
+
 }  // namespace sd
 
 // a * b in the reconstructions and fluxes: with SOFT (FP64) on the integer

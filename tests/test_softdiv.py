@@ -193,3 +193,44 @@ def test_soft_multiply_matches_the_multiply_on_the_host(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     bad, n = (int(x) for x in out.stdout.split())
     assert out.returncode == 0 and bad == 0 and n == 30000000
+
+
+ZERO_PLUS_PROGRAM = r"""
+#include "softdiv.cuh"
+#include <cstdio>
+#include <random>
+using namespace hamstr::sd;
+int main() {
+   std::mt19937_64 rng(5);
+   long bad = 0, n = 0;
+   const double special[] = {0.0, -0.0, 1.0, -1.0, 4.9e-324, -4.9e-324, 2.2250738585072014e-308, -2.2e-308,
+                             1.7976931348623157e308, -1.7976931348623157e308, from_bits(0x7FF0000000000000ull),
+                             from_bits(0xFFF0000000000000ull)};
+   volatile double zero = 0.0;
+   for (long i = 0; i < 20000000; i++) {
+      const double v = (i < 24) ? special[i / 2] : from_bits(rng());
+      if (v != v) continue;
+      const bool sub = (i & 1) != 0;
+      const double w = sub ? zero - v : zero + v;
+      n++;
+      if (bits(w) != bits(zero_plus(v, sub))) bad++;
+   }
+   printf("%ld %ld\n", bad, n);
+   return bad != 0;
+}
+"""
+
+
+def test_zero_plus_matches_the_add_on_the_host(tmp_path):
+    """The ADI assembly's first term on the integer pipes (sd::zero_plus)
+    equals 0.0 + v and 0.0 - v bit for bit: random doubles over all
+    exponents, zeros of both signs, subnormals, the largest finite values
+    and infinities (NaN has no defined sign and is left out)."""
+    src = tmp_path / "z.cpp"
+    src.write_text(ZERO_PLUS_PROGRAM)
+    exe = tmp_path / "z"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    bad, n = (int(x) for x in out.stdout.split())
+    assert out.returncode == 0 and bad == 0 and n > 19900000
