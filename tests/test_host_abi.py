@@ -13,6 +13,21 @@ def test_library_exports_header_symbols(native_lib):
     assert not missing, missing
 
 
+def test_shape_keys_match_the_header():
+    """The Python shape keys and the header's HAMSTR_SHAPE_N (the length of
+    the array hamstr_gpu_get_shape / set_shape read and write) agree, and the
+    header documents every index."""
+    import os
+    import re
+    from hamstr_oop_gb300 import native
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "hamstr_gpu.h")
+    text = open(hdr).read()
+    n = int(re.search(r"#define HAMSTR_SHAPE_N (\d+)", text).group(1))
+    assert n == len(native.GpuSolver.SHAPE_KEYS) == len(set(native.GpuSolver.SHAPE_KEYS))
+    for i in range(n):
+        assert re.search(r"\*\s+\[%d\] " % i, text), i
+
+
 @pytest.mark.parametrize("ni,nj,order,loop_start", [(16, 4, 3, None), (24, 6, 5, 0), (40, 8, 1, 3)])
 def test_reader_and_preprocess_match_oracle(make_case, oracle_lib, native_lib, ni, nj, order, loop_start):
     from hamstr_oop_gb300 import native
