@@ -23,7 +23,6 @@ LIBDIR = os.path.join(PKG, "lib")
 BINDIR = os.path.join(PKG, "bin")
 LIB = os.path.join(LIBDIR, "libhamstr_gb300.so")
 EXE = os.path.join(BINDIR, "hamstr_gb300")
-PROBE = os.path.join(BINDIR, "hamstr_fp64_probe")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -87,9 +86,6 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(out)
     if force or _newer(objs, LIB):
         _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs + ["-lcudart"])
-    probe_src = os.path.join(CSRC, "fp64_probe.cu")
-    if force or _newer([probe_src], PROBE):
-        _run([NVCC] + ARCH + ["-O3", "-std=c++17", probe_src, "-o", PROBE])
     main_src = os.path.join(CSRC, "host", "main.cpp")
     if force or _newer([main_src, LIB], EXE):
         _run(["g++"] + CXXFLAGS + [main_src, "-o", EXE, "-L" + LIBDIR, "-lhamstr_gb300",
@@ -100,7 +96,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 def clean() -> None:
     for d in (BUILD,):
         shutil.rmtree(d, ignore_errors=True)
-    for f in (LIB, EXE, PROBE):
+    for f in (LIB, EXE):
         if os.path.exists(f):
             os.remove(f)
 

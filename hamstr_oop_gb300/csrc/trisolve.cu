@@ -151,10 +151,13 @@ extern "C" int hamstr_gpu_block_tridag4_noalloc(int nlines, int N, int periodic,
 {
    int st = block_tridag_check(nlines, N, periodic, A, B, C, F);
    if (st || nlines == 0) return st;
-   const size_t need = (size_t)nlines * ((size_t)kFacRec * N + 16);
-   if (need > kNoAllocScratchDoubles) {
-      set_last_error("block_tridag4_noalloc: nlines*(80*N+16) = " + std::to_string(need) +
-                     " doubles exceeds the fixed scratch of " + std::to_string(kNoAllocScratchDoubles));
+   // per-line need compared against the per-line share, so no product of
+   // two large ints can wrap past the limit
+   const size_t per_line = (size_t)kFacRec * N + 16;
+   if (per_line > kNoAllocScratchDoubles / (size_t)nlines) {
+      set_last_error("block_tridag4_noalloc: nlines*(80*N+16) with nlines = " + std::to_string(nlines) +
+                     ", N = " + std::to_string(N) + " exceeds the fixed scratch of " +
+                     std::to_string(kNoAllocScratchDoubles) + " doubles");
       return HAMSTR_GPU_ERR_ARG;
    }
    double* scratch = nullptr;

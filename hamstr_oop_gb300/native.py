@@ -130,29 +130,49 @@ def declared_symbols() -> list:
     return sorted(set(re.findall(r"\b(hamstr_[a-z_0-9]+)\s*\(", txt)))
 
 
+def _tridag_operands(name: str, A, B, C, F):
+    """(nlines, N) of a batched block-tridiagonal system after checking that
+    A, B, C are (nlines, N, 4, 4) and F is (nlines, N, 4), all contiguous
+    float64 CUDA tensors on one device: the kernel reads every block of
+    every line, so a smaller operand would be read past its end."""
+    import torch
+    if F.dim() != 3 or F.shape[2] != 4:
+        raise ValueError("%s: F must be (nlines, N, 4), got %s" % (name, tuple(F.shape)))
+    nl, n = int(F.shape[0]), int(F.shape[1])
+    for t in (A, B, C, F):
+        if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float64):
+            raise ValueError("%s needs contiguous float64 CUDA tensors" % name)
+        if t.device != F.device:
+            raise ValueError("%s: every operand must be on %s" % (name, F.device))
+    for label, t in (("A", A), ("B", B), ("C", C)):
+        if tuple(t.shape) != (nl, n, 4, 4):
+            raise ValueError("%s: %s must be %s, got %s" % (name, label, (nl, n, 4, 4), tuple(t.shape)))
+    return nl, n
+
+
 def block_tridag4(A, B, C, F, periodic: bool, stream: int = 0):
     """Batched block-tridiagonal solve on device memory (torch CUDA tensors).
 
-    A, B, C: (nlines, N, 4, 4) float64; F: (nlines, N, 4) float64, solved in place."""
-    nl, n = int(F.shape[0]), int(F.shape[1])
-    for t in (A, B, C, F):
-        if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float64"):
-            raise ValueError("block_tridag4 needs contiguous float64 CUDA tensors")
-    _check(load().hamstr_gpu_block_tridag4(nl, n, int(periodic), A.data_ptr(), B.data_ptr(), C.data_ptr(),
-                                           F.data_ptr(), stream or None))
+    A, B, C: (nlines, N, 4, 4) float64; F: (nlines, N, 4) float64, solved in
+    place.  Runs on the operands' device."""
+    import torch
+    nl, n = _tridag_operands("block_tridag4", A, B, C, F)
+    with torch.cuda.device(F.device):
+        _check(load().hamstr_gpu_block_tridag4(nl, n, int(periodic), A.data_ptr(), B.data_ptr(), C.data_ptr(),
+                                               F.data_ptr(), stream or None))
 
 
 def block_tridag4_noalloc(A, B, C, F, periodic: bool, stream: int = 0):
     """block_tridag4 without device allocation (fixed 8 MiB scratch in the
     library; nlines*(80*N+16) <= 1048576).  Only enqueues on `stream`: the
     caller synchronises before reading F.  For callers that cannot allocate
-    device memory per call (loops beside other streams, pool-owned memory)."""
-    nl, n = int(F.shape[0]), int(F.shape[1])
-    for t in (A, B, C, F):
-        if not (t.is_cuda and t.is_contiguous() and str(t.dtype) == "torch.float64"):
-            raise ValueError("block_tridag4_noalloc needs contiguous float64 CUDA tensors")
-    _check(load().hamstr_gpu_block_tridag4_noalloc(nl, n, int(periodic), A.data_ptr(), B.data_ptr(),
-                                                   C.data_ptr(), F.data_ptr(), stream or None))
+    device memory per call (loops beside other streams, pool-owned memory).
+    Runs on the operands' device, with that device's scratch."""
+    import torch
+    nl, n = _tridag_operands("block_tridag4_noalloc", A, B, C, F)
+    with torch.cuda.device(F.device):
+        _check(load().hamstr_gpu_block_tridag4_noalloc(nl, n, int(periodic), A.data_ptr(), B.data_ptr(),
+                                                       C.data_ptr(), F.data_ptr(), stream or None))
 
 
 def _ptr(a: np.ndarray):

@@ -305,10 +305,13 @@ int hamstr_gpu_block_tridag4(int nlines, int N, int periodic, const double* A, c
  * the call needs nlines*(80*N+16) <= 1048576 doubles and returns
  * HAMSTR_GPU_ERR_ARG beyond that.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  The call only enqueues
- * work on `stream` (synchronise it before reading F).  All calls share the
- * one array: calls whose work overlaps on the GPU (different streams, or
- * different host threads) race and must be serialised by the caller. */
+ * make that first call before any stream capture.  The address is kept
+ * for the life of the process, so do not call this entry point after a
+ * cudaDeviceReset of that device (the array may then sit elsewhere).
+ * The call only enqueues work on `stream` (synchronise it before reading
+ * F).  All calls share the one array: calls whose work overlaps on the GPU
+ * (different streams, or different host threads) race and must be
+ * serialised by the caller. */
 int hamstr_gpu_block_tridag4_noalloc(int nlines, int N, int periodic, const double* A, const double* B,
                                      const double* C, double* F, void* stream);
 

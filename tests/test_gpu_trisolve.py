@@ -42,3 +42,23 @@ def test_block_tridag_rejects_bad_sizes(native_lib):
     f = torch.zeros((1, 1, 4), dtype=torch.float64, device="cuda")
     with pytest.raises(native.HamstrError):
         native.block_tridag4(z, z, z, f, True)     # periodic line of one row
+
+
+@pytest.mark.parametrize("fn", ["block_tridag4", "block_tridag4_noalloc"])
+def test_block_tridag_rejects_mismatched_operands(native_lib, fn):
+    """Operands smaller than F's (nlines, N) would be read past their end by
+    the kernel; the binding refuses them before anything is launched."""
+    import torch
+    from hamstr_oop_gb300 import native
+    solve = getattr(native, fn)
+    full = torch.zeros((3, 8, 4, 4), dtype=torch.float64, device="cuda")
+    short = torch.zeros((3, 7, 4, 4), dtype=torch.float64, device="cuda")
+    f = torch.zeros((3, 8, 4), dtype=torch.float64, device="cuda")
+    with pytest.raises(ValueError):
+        solve(short, full, full, f, False)
+    with pytest.raises(ValueError):
+        solve(full, full, short, f, True)
+    with pytest.raises(ValueError):
+        solve(full, full, full, f.reshape(3, 32), False)
+    with pytest.raises(ValueError):
+        solve(full.float(), full, full, f, False)
