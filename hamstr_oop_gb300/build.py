@@ -32,8 +32,9 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relax
 CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
             "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["rhs.cu", "adi.cu", "api.cu", "trisolve.cu", "mixed.cu", "forces.cu", "mlp_gemm.cu", "mlp_api.cu", "mlp_net.cu", "checks.cu"]
-CXX_SOURCES = ["plan.cpp", os.path.join("host", "hamstr_host.cpp")]
+CU_SOURCES = ["rhs.cu", "adi.cu", "api.cu", "trisolve.cu", "mixed.cu", "forces.cu", "mlp_gemm.cu", "mlp_api.cu", "mlp_net.cu", "checks.cu",
+              "pointwise.cu"]
+CXX_SOURCES = ["plan.cpp", os.path.join("host", "hamstr_host.cpp"), os.path.join("host", "hamstr_dropin.cpp")]
 
 
 def _newer(src_list, dst):

@@ -93,12 +93,12 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
 
 // block-Thomas factorisation of chain ich (its assembled rows in blk)
 template <bool SD>
-__device__ __forceinline__ void factor_chain(const DeviceState& d, int ich, int lane)
+__device__ __forceinline__ bool factor_chain(const DeviceState& d, int ich, int lane)
 {
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const double* blk = d.blk + 48 * (size_t)row0;
-   factor_line<SD>(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
+   return factor_line<SD>(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
                per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane);
 }
 
@@ -110,11 +110,11 @@ __device__ __forceinline__ int live_rows(const DeviceState& d, int ich)
 
 // two open chains, one per half-warp (line_solve.cuh factor_line_pair)
 template <bool SD>
-__device__ __forceinline__ void factor_pair(const DeviceState& d, int ia, int ib, int lane)
+__device__ __forceinline__ bool factor_pair(const DeviceState& d, int ia, int ib, int lane)
 {
    const int ich = (lane >> 4) ? ib : ia;
    const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
-   factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
+   return factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
 }
 
 // next job index of a persistent warp: lane 0 takes it from the counter
@@ -126,7 +126,9 @@ __device__ __forceinline__ int take_job(int* ctr, int lane)
 }
 
 // persistent warps, one or two per SM sub-partition, taking jobs from the
-// factorisation's queue (longest first) until it is empty
+// factorisation's queue (longest first) until it is empty; a zero or
+// non-finite pivot raises DEV_ERR_PIVOT (the factors are still stored, as
+// the reference divides regardless)
 template <bool SD>
 __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
 {
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    if (w >= nwarps) return;
    const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
    int* ctr = d.sched_ctr;
+   bool bad = false;
    for (int k = take_job(ctr, lane); k < nj;) {
       // the next job's index is fetched while this one runs
       int kn = 0;
@@ -147,7 +150,8 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
             const int c = d.sched_jobs[job + 1 + lane];
             if (!frozen_chain(d, c)) {
                const int row0 = d.chain_row0[c];
-               factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c], d.fac + (size_t)kFacRec * row0);
+               bad |= factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c],
+                                             d.fac + (size_t)kFacRec * row0);
             }
          }
       } else if (ich & kQuadJob) {
@@ -157,14 +161,15 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
             N = live_rows(d, c);
          }
          const int row0 = d.chain_row0[c];
-         factor_line_quad<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
+         bad |= factor_line_quad<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
       } else if (ich & kPairJob) {
-         factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
+         bad |= factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
       } else if (!frozen_chain(d, ich)) {
-         factor_chain<SD>(d, ich, lane);
+         bad |= factor_chain<SD>(d, ich, lane);
       }
       k = __shfl_sync(kLaneMask, kn, 0);
    }
+   if (__any_sync(kLaneMask, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
 }
 
 // one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the

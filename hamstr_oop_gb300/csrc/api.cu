@@ -218,7 +218,7 @@ struct hamstr_gpu {
    {
       if (mixed) return enqueue_mixed_step(check_tol);
       int n = 0;
-      if (d.recon == 5) L("recon5", n, [&] { launch_recon5(d, true, stream); });
+      if (d.recon == 5) L("recon5", n, [&] { launch_recon5(d, d.lin_order != 1, stream); });
       L("rhs_face", n, [&] { launch_rhs_face(d, true, stream); });
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
@@ -227,7 +227,7 @@ struct hamstr_gpu {
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++) adi_solve_launches(s, w, n);
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
-         if (d.recon == 5) L("lin_recon5", n, [&] { launch_lin_recon5(d, true, stream); });
+         if (d.recon == 5 && d.lin_order != 1) L("lin_recon5", n, [&] { launch_lin_recon5(d, true, stream); });
          L("lin_face", n, [&] { launch_lin_face(d, stream); });
          L("lin_cell", n, [&] { launch_lin_cell(d, s == msweep - 1, stream); });
          if (s == msweep - 1) L("norm_final", n, [&] { launch_norm_final(d, 2, false, stream); });
@@ -349,12 +349,19 @@ struct hamstr_gpu {
       int s = 0;
       CK(cudaMemcpyAsync(&s, d.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
       CK(cudaStreamSynchronize(stream));
+      if (!s) return HAMSTR_GPU_OK;
+      CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
+      // the first failure of a step in its order: flux, factorisation, sweep
       if (s & DEV_ERR_NAN_SPEC) {
          set_error("NaN spectral radius (non-physical state)");
-         CK(cudaMemsetAsync(d.status, 0, sizeof(int), stream));
          return HAMSTR_GPU_ERR_NAN;
       }
-      return HAMSTR_GPU_OK;
+      if (s & DEV_ERR_PIVOT) {
+         set_error("zero or non-finite LU pivot in an ADI line factorisation");
+         return HAMSTR_GPU_ERR_SINGULAR;
+      }
+      set_error("non-finite dq after an ADI sweep");
+      return HAMSTR_GPU_ERR_NONFINITE;
    }
 
    int read_norms(double* out, int n)
@@ -376,6 +383,8 @@ const char* hamstr_gpu_strerror(int st)
       case HAMSTR_GPU_ERR_NAN: return "NaN spectral radius";
       case HAMSTR_GPU_ERR_IO: return "missing or malformed input file";
       case HAMSTR_GPU_ERR_NOMEM: return "out of memory";
+      case HAMSTR_GPU_ERR_SINGULAR: return "singular ADI block pivot";
+      case HAMSTR_GPU_ERR_NONFINITE: return "non-finite ADI update";
       default: return "unknown status";
    }
 }
@@ -439,6 +448,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
    d.nChain = P.nChain;
    d.order = P.order;
    d.recon = (P.order == 3 && p->limiter != HAMSTR_LIMITER_REFERENCE) ? 30 + p->limiter : P.order;
+   d.lin_order = 0;
    d.nGhost = P.nGhost;
    d.fc.gamma = p->gamma;
    d.fc.rinf = p->rinf;
@@ -1203,6 +1213,17 @@ extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)
    if (!g || !(cfl > 0.0) || !(cfl < 1e300)) return HAMSTR_GPU_ERR_ARG;
    if (g->d.fc.cfl != cfl) {
       g->d.fc.cfl = cfl;   // kernels take the state by value: recapture the step
+      g->invalidate();
+   }
+   return HAMSTR_GPU_OK;
+}
+
+extern "C" int hamstr_gpu_set_sweep_order(hamstr_gpu* g, int order)
+{
+   if (!g || (order != 0 && order != 1)) return HAMSTR_GPU_ERR_ARG;
+   if (g->d.lin_order != order) {
+      g->d.lin_order = order;   // kernels take the state by value: recapture the step
+      g->wlin_valid = false;
       g->invalidate();
    }
    return HAMSTR_GPU_OK;

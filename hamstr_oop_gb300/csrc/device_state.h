@@ -21,11 +21,15 @@
 
 #include <cuda_runtime.h>
 
+#include "lu4.cuh"
+
 namespace hamstr {
 
 // status bits raised by kernels into DeviceState::status
 enum {
    DEV_ERR_NAN_SPEC = 1,     // spectral radius is NaN (interfaceFlux.cpp:117-124)
+   DEV_ERR_PIVOT = 2,        // an ADI line's LU pivot is zero or not finite (reciprocal not finite)
+   DEV_ERR_DQ = 4,           // an ADI sweep left a non-finite dq
 };
 
 struct FlowConst {
@@ -37,6 +41,7 @@ constexpr int kWlinPerSlot = 2 * 4 * 18;   // sides x components x values (recon
 struct DeviceState {
    int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
    int recon;              // reconstruction code: order, or 31/32 for MUSCL with a project limiter (recon.cuh)
+   int lin_order;          // 0: the sweeps' linearised residual at the scheme's order; 1: at first order
    FlowConst fc;
 
    // instances: the batched form holds several meshes / flow conditions in

@@ -116,6 +116,12 @@ class SOLVER
    void computeLinearRHS(void);          // computeLinearRHS.cpp:13-371
    void ADI(void);                       // ADI.cpp:15-266
    void basicScreenOutput(void);         // io.cpp:412-446
+   // interfaceFlux.cpp:24-169: one face on the GPU (hamstr_gpu_flux_roe2d);
+   // a NaN spectral radius throws hamstr::Error (HAMSTR_GPU_ERR_NAN) where
+   // the reference exits
+   void fluxRoe2D(double* nxyz, double* ql, double* qr, double* flux, double* specRadius, double gamma);
+   // jacobianRoe.cpp:9-70: one face on the GPU (hamstr_gpu_jacobian_roe2d)
+   void jacobianRoe2D(double* nxyz, double* ql, double* qr, double** lmat, double** rmat, double gamma);
    void syncHost(void);
    hamstr_gpu* device(void) { ensureGpu(); return gpu; }
    double l2Norm() const { return sb->L2Norm; }
@@ -142,6 +148,31 @@ class HAMSTR
    void thanks(void);
    SOLVER* solver() { return solv; }
 };
+
+// ------------------------------------------------------------------
+// The reference's numerics namespaces (reconstruction.h:11-110,
+// triSolvers.h:18-46) over host arrays, each call run on the GPU through
+// the function-level C ABI (hamstr_gpu_muscl etc., hamstr_gpu_block_tridag4)
+// with the same arguments and results.  Differences a caller sees: errors
+// throw hamstr::Error; MUSCL and MUSCL_DERIV with qt != 0 at ie = imax-1
+// (computeRHS.cpp:267's call) leave entry imax-1 of ql and qr as it was
+// (the reference fills it from work-array entries left by an earlier
+// chain, and its callers never read it); blockTridag4 and
+// blockTridagPeriodic4 leave b and c unchanged (the reference uses them as
+// scratch) and need nq == 4.
+namespace RECONSTRUCTION {
+void MUSCL(double** f, double** ql, double** qr, double** f2, int is, int ie, double th, double qt, double eps,
+           int imax, int nq);
+void WENO(double** f, double** ql, double** qr, int is, int ie, double epsw, int imax, int nq);
+void MUSCL_DERIV(double** f, double** ql, double** qr, double** f2, double** dq, int is, int ie, double th, double qt,
+                 double eps, int imax, int nq);
+void WENO_DERIV(double** f, double** ql, double** qr, double** dq, int is, int ie, double eps, int imax, int nq);
+}  // namespace RECONSTRUCTION
+
+namespace TRISOLVER {
+void blockTridag4(double*** a, double*** b, double*** c, double** f, int N, int nq);
+void blockTridagPeriodic4(double*** a, double*** b, double*** c, double** f, int N, int nq);
+}  // namespace TRISOLVER
 
 // freestream + initial state (initFlow.cpp:12-93) on host arrays
 void hamstr_init_flow(SOLNBLOCK& sb, int nCell);

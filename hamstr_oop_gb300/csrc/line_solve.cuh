@@ -114,15 +114,18 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
 // Block-Thomas factorisation of one line of N rows by one warp: blocks
 // A_i = Ab + i*stride, B_i = Bb + i*stride, C_i = Cb + i*stride (row-major
 // 4x4); writes the per-row records `fac` (kFacRec doubles per row) and,
-// periodic, the LU of the final last-row block into facN.
+// periodic, the LU of the final last-row block into facN.  Returns, in the
+// lanes that hold a pivot, whether a stored reciprocal pivot is infinite or
+// NaN (a zero or non-finite pivot; the reference divides by it regardless).
 template <bool SD = true>
-__device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const double* __restrict__ Bb,
+__device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const double* __restrict__ Bb,
                                             const double* __restrict__ Cb, size_t stride, int N, bool per,
                                             double* __restrict__ fac, double* __restrict__ facN, int lane)
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
    double A = Ab[e], B = Bb[e], C = Cb[e];
    double P = 0.0;   // previous row's solved C' (h=0) or a' (h=1), element (k,j)
+   bool bad = false;
    for (int i = 0; i < N; i++) {
       // next row's blocks are loaded while this row is factored
       double An = 0.0, Bn = 0.0, Cn = 0.0;
@@ -149,6 +152,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
       // LU of B'(i), computed by both halves on their own copy
       const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, acc, e), 16 * h, e);
       if (h == 0) rec[16 + e] = w;
+      bad |= h == 0 && k == j && nonfinite(w);
       double lu[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, 16 * h + 4 * k + c);
@@ -169,7 +173,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
       B = Bn;
       C = Cn;
    }
-   if (!per) return;
+   if (!per) return bad;
    // last-row elimination (triSolvers.cpp:967-999)
    double cN = __shfl_sync(kLaneMask, P, e);
    double bN = (k == j) ? 1.0 : 0.0;
@@ -191,6 +195,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
    }
    const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, bN, 16 + e), 16 * h, e);
    if (h == 0) facN[e] = w;
+   return bad || (h == 0 && k == j && nonfinite(w));
 }
 
 // Two open lines per warp, one per half (h = lane >> 4): the same
@@ -200,7 +205,7 @@ __device__ __forceinline__ void factor_line(const double* __restrict__ Ab, const
 // loads and stores skipped).  Short open lines -- the rule on split meshes
 // -- leave half of factor_line's warp with nothing to do.
 template <bool SD = true>
-__device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
+__device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
                                                  double* __restrict__ fac, int lane)
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3, hb = 16 * h;
@@ -212,6 +217,7 @@ __device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, 
       C = Ab[32 + e];
    }
    double P = 0.0;
+   bool bad = false;   // a live row's reciprocal pivot is not finite
    for (int i = 0; i < Nmax; i++) {
       double An = 0.0, Bn = 0.0, Cn = 0.0;
       if (i + 1 < N) {
@@ -234,6 +240,7 @@ __device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, 
       }
       const double w = lu_wavefront<SD>(acc, hb, e);
       if (live) rec[16 + e] = w;
+      bad |= live && k == j && nonfinite(w);
       double lu[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, hb + 4 * k + c);
@@ -245,6 +252,7 @@ __device__ __forceinline__ void factor_line_pair(const double* __restrict__ Ab, 
       B = Bn;
       C = Cn;
    }
+   return bad;
 }
 
 // Right-hand-side replay of two factored open lines, one per half-warp:
@@ -390,12 +398,13 @@ __device__ __forceinline__ void st4row(double* __restrict__ p, const double (&v)
 // factor_line on open line g of the warp: blocks of row i at blk + i*stride
 // (A, B, C consecutive, 16 each)
 template <bool SD>
-__device__ __forceinline__ void factor_line_quad(const double* __restrict__ blk, size_t stride, int N,
+__device__ __forceinline__ bool factor_line_quad(const double* __restrict__ blk, size_t stride, int N,
                                                  double* __restrict__ fac, int lane)
 {
    const int r = lane & 3, base = lane & ~3;
    const int Nmax = __reduce_max_sync(kLaneMask, N);
    double Pr[4] = {0.0, 0.0, 0.0, 0.0};   // row r of the previous row's C'
+   bool bad = false;                      // a live row's reciprocal pivot is not finite
    for (int i = 0; i < Nmax; i++) {
       const bool live = i < N;
       double A[4] = {0.0, 0.0, 0.0, 0.0}, w[4] = {0.0, 0.0, 0.0, 0.0}, C[4] = {0.0, 0.0, 0.0, 0.0};
@@ -424,6 +433,7 @@ __device__ __forceinline__ void factor_line_quad(const double* __restrict__ blk,
       }
       lu_rows_quad<SD>(w, r, base);
       if (live) st4row(rec + 16 + 4 * r, w);
+      bad |= live && nonfinite(sel4(w, r));
       // c'(i) = B'^{-1} c(i), column by column (component r of each in this lane)
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -432,6 +442,7 @@ __device__ __forceinline__ void factor_line_quad(const double* __restrict__ blk,
       }
       if (live) st4row(rec + 32 + 4 * r, Pr);
    }
+   return bad;
 }
 
 // solve_line on open line g of the warp: the right-hand side from
@@ -574,10 +585,11 @@ __device__ __forceinline__ void st16(double* __restrict__ p, const double (&v)[1
 // factor_line on an open line by one thread: blocks of row i at
 // blk + i*stride (A, B, C consecutive, 16 each), records into fac
 template <bool SD>
-__device__ __forceinline__ void factor_line_thread(const double* __restrict__ blk, size_t stride, int N,
+__device__ __forceinline__ bool factor_line_thread(const double* __restrict__ blk, size_t stride, int N,
                                                    double* __restrict__ fac)
 {
    double P[16];   // previous row's C'
+   bool bad = false;   // a reciprocal pivot is not finite
    for (int i = 0; i < N; i++) {
       const double* b = blk + stride * (size_t)i;
       double* rec = fac + (size_t)kFacRec * i;
@@ -600,6 +612,7 @@ __device__ __forceinline__ void factor_line_thread(const double* __restrict__ bl
       }
       lu4_thread<SD>(w);
       st16(rec + 16, w);
+      bad |= nonfinite(w[0]) || nonfinite(w[5]) || nonfinite(w[10]) || nonfinite(w[15]);
       // c'(i) = B'^{-1} c(i), column by column
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -610,6 +623,7 @@ __device__ __forceinline__ void factor_line_thread(const double* __restrict__ bl
       }
       st16(rec + 32, P);
    }
+   return bad;
 }
 
 // solve_line on an open line by one thread, the right-hand side read from

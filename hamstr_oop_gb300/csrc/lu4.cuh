@@ -73,6 +73,11 @@ __device__ __forceinline__ LU4 lu_load(const double* __restrict__ p)
    return u;
 }
 
+// true for an infinite or NaN value: the exponent field all ones, tested on
+// the integer pipes (no FP64 instruction)
+__device__ __forceinline__ bool nonfinite(double x) { return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000; }
+__device__ __forceinline__ bool nonfinite(float x) { return (__float_as_int(x) & 0x7f800000) == 0x7f800000; }
+
 __device__ __forceinline__ double sel4(const double (&x)[4], int k)
 {
    double v = x[0];

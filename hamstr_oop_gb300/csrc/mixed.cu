@@ -369,6 +369,7 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = t & 31, s0 = d.grp_row0[t >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    float A[16], B[16], C[16], cp[16], ap[16];
+   bool bad = false;   // a reciprocal pivot is not finite (DEV_ERR_PIVOT)
    RowRef rnext{};   // fused: references of row i + 1, looked up a row ahead
    if (FUSED) {
       const RowRef r0 = mx_rowref(d, row0);
@@ -397,6 +398,7 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
       }
       const LUf u = luf_factor(B);
       luf_store_t(rec + 32 * 16, u);
+      bad |= nonfinite(u.p0) || nonfinite(u.p1) || nonfinite(u.p2) || nonfinite(u.p3);
       if (per && i == N - 2) {
 #pragma unroll
          for (int m = 0; m < 16; m++) C[m] += fill[m];
@@ -416,7 +418,10 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
          for (int m = 0; m < 16; m++) { A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
       }
    }
-   if (!per) return;
+   if (!per) {
+      if (bad) atomicOr(d.status, DEV_ERR_PIVOT);
+      return;
+   }
    // last-row elimination (triSolvers.cpp:967-999).  A row's arithmetic is
    // short, so the loads of ED rows are issued before it; the main loop's
    // arrays are dead here, so a chunk of 2 adds no registers.
@@ -446,7 +451,10 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
             for (int m = 0; m < 16; m++) cN[m] = tt[m];
          }
    }
-   luf_store(d.facN32 + 16 * d.chain_facN[ich], luf_factor(bN));
+   const LUf uN = luf_factor(bN);
+   luf_store(d.facN32 + 16 * d.chain_facN[ich], uN);
+   bad |= nonfinite(uN.p0) || nonfinite(uN.p1) || nonfinite(uN.p2) || nonfinite(uN.p3);
+   if (bad) atomicOr(d.status, DEV_ERR_PIVOT);
 }
 
 // One sweep's solve of one chain per thread (the chain at position first +
@@ -769,6 +777,7 @@ __global__ void __launch_bounds__(kThreads) mx_dq_update_kernel(DeviceState d)
 #pragma unroll
    for (int k = 0; k < 4; k++) dq[k] += r[k];
    st4(d.dq32 + 4 * (size_t)c, dq);
+   if (nonfinite(dq[0]) || nonfinite(dq[1]) || nonfinite(dq[2]) || nonfinite(dq[3])) atomicOr(d.status, DEV_ERR_DQ);
 }
 
 template <int ORDER>
@@ -943,6 +952,10 @@ void launch_mx_lin_face(const DeviceState& d, cudaStream_t st)
 {
    const int kThreads = d.face_block;
    const int b = (d.nSlot + kThreads - 1) / kThreads;
+   if (d.lin_order == 1) {
+      mx_lin_face_kernel<1><<<b, kThreads, 0, st>>>(d);
+      return;
+   }
    switch (d.recon) {
       case 1: mx_lin_face_kernel<1><<<b, kThreads, 0, st>>>(d); break;
       case 3: mx_lin_face_kernel<3><<<b, kThreads, 0, st>>>(d); break;

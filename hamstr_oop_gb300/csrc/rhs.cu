@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(kThreads) dq_update_kernel(DeviceState d)
 #pragma unroll
    for (int k = 0; k < 4; k++) dq[k] += r[k];
    st4(d.dq + 4 * (size_t)c, dq);
+   if (nonfinite(dq[0]) || nonfinite(dq[1]) || nonfinite(dq[2]) || nonfinite(dq[3])) atomicOr(d.status, DEV_ERR_DQ);
 }
 
 inline int blocks_for(int n) { return (n + kThreads - 1) / kThreads; }
@@ -367,7 +368,7 @@ void launch_rhs_cell(const DeviceState& d, bool adi_init, cudaStream_t st)
 
 void launch_lin_recon5(const DeviceState& d, bool kept, cudaStream_t st)
 {
-   if (d.recon != 5 || !d.qface) return;
+   if (d.recon != 5 || !d.qface || d.lin_order == 1) return;
    const dim3 b((d.nSlot + kThreads - 1) / kThreads, 8);
    const bool wl = kept && d.wlin;
    if (d.face_soft) {
@@ -384,6 +385,10 @@ void launch_lin_face(const DeviceState& d, cudaStream_t st)
    const int kThreads = d.face_block;
    const int b = (d.nSlot + kThreads - 1) / kThreads;
    // only the WENO linearisation divides in FP64 here
+   if (d.lin_order == 1) {
+      lin_face_kernel<1, true><<<b, kThreads, 0, st>>>(d);
+      return;
+   }
    switch (d.recon) {
       case 1: lin_face_kernel<1, true><<<b, kThreads, 0, st>>>(d); break;
       case 3: lin_face_kernel<3, true><<<b, kThreads, 0, st>>>(d); break;

@@ -106,6 +106,7 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_stream": (vp, [vp]),
         "hamstr_gpu_step_explicit": (i, [vp, i, vp]),
         "hamstr_gpu_set_precision": (i, [vp, i]),
+        "hamstr_gpu_set_sweep_order": (i, [vp, i]),
         "hamstr_gpu_update_solution": (i, [vp, cp, cp, d]),
         "hamstr_gpu_enqueue_steps": (i, [vp, i]),
         "hamstr_gpu_sync": (i, [vp]),
@@ -114,6 +115,12 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_launches_per_step": (i, [vp]),
         "hamstr_gpu_block_tridag4": (i, [i, i, i, vp, vp, vp, vp, vp]),
         "hamstr_gpu_block_tridag4_noalloc": (i, [i, i, i, vp, vp, vp, vp, vp]),
+        "hamstr_gpu_flux_roe2d": (i, [i, vp, vp, vp, vp, vp, d, vp]),
+        "hamstr_gpu_jacobian_roe2d": (i, [i, vp, vp, vp, vp, vp, d, vp]),
+        "hamstr_gpu_muscl": (i, [i, i, i, vp, vp, vp, vp, i, i, d, d, d, vp]),
+        "hamstr_gpu_muscl_deriv": (i, [i, i, i, vp, vp, vp, vp, vp, i, i, d, d, d, vp]),
+        "hamstr_gpu_weno": (i, [i, i, i, vp, vp, vp, i, i, d, vp]),
+        "hamstr_gpu_weno_deriv": (i, [i, i, i, vp, vp, vp, vp, i, i, d, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -173,6 +180,82 @@ def block_tridag4_noalloc(A, B, C, F, periodic: bool, stream: int = 0):
     with torch.cuda.device(F.device):
         _check(load().hamstr_gpu_block_tridag4_noalloc(nl, n, int(periodic), A.data_ptr(), B.data_ptr(),
                                                        C.data_ptr(), F.data_ptr(), stream or None))
+
+
+def _f64_cuda(name: str, shape: tuple, *ts):
+    """Check that every tensor is a contiguous float64 CUDA tensor of `shape`
+    on the first one's device (the kernels index them by that shape)."""
+    import torch
+    dev = ts[0].device
+    for t in ts:
+        if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float64):
+            raise ValueError("%s needs contiguous float64 CUDA tensors" % name)
+        if t.device != dev:
+            raise ValueError("%s: every operand must be on %s" % (name, dev))
+        if tuple(t.shape) != tuple(shape):
+            raise ValueError("%s: operand of shape %s, expected %s" % (name, tuple(t.shape), tuple(shape)))
+    return dev
+
+
+def flux_roe2d(nxy, ql, qr, gamma: float = 1.4):
+    """SOLVER::fluxRoe2D over n faces (hamstr_gpu_flux_roe2d) on torch CUDA
+    tensors nxy (n, 2), ql, qr (n, 4): returns (flux (n, 4), spec (n,))."""
+    import torch
+    n = int(nxy.shape[0])
+    dev = _f64_cuda("flux_roe2d", (n, 2), nxy)
+    _f64_cuda("flux_roe2d", (n, 4), ql, qr)
+    flux = torch.empty((n, 4), dtype=torch.float64, device=dev)
+    spec = torch.empty((n,), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _check(load().hamstr_gpu_flux_roe2d(n, nxy.data_ptr(), ql.data_ptr(), qr.data_ptr(), flux.data_ptr(),
+                                            spec.data_ptr(), float(gamma), torch.cuda.current_stream().cuda_stream))
+    return flux, spec
+
+
+def jacobian_roe2d(nxy, ql, qr, gamma: float = 1.4):
+    """SOLVER::jacobianRoe2D over n faces (hamstr_gpu_jacobian_roe2d):
+    returns (lmat (n, 4, 4), rmat (n, 4, 4)), times the face area."""
+    import torch
+    n = int(nxy.shape[0])
+    dev = _f64_cuda("jacobian_roe2d", (n, 2), nxy)
+    _f64_cuda("jacobian_roe2d", (n, 4), ql, qr)
+    lm = torch.empty((n, 4, 4), dtype=torch.float64, device=dev)
+    rm = torch.empty((n, 4, 4), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _check(load().hamstr_gpu_jacobian_roe2d(n, nxy.data_ptr(), ql.data_ptr(), qr.data_ptr(), lm.data_ptr(),
+                                                rm.data_ptr(), float(gamma), torch.cuda.current_stream().cuda_stream))
+    return lm, rm
+
+
+def reconstruct(name: str, f, ql, qr, is_: int, ie: int, *, dq=None, f2=None, th: float = 1.0 / 3.0,
+                qt: float = 0.25, eps: float = 1e-10) -> None:
+    """RECONSTRUCTION::MUSCL / MUSCL_DERIV / WENO / WENO_DERIV over lines
+    (hamstr_gpu_muscl etc.): f, ql, qr (and dq, f2) are (nlines, imax, nq)
+    torch CUDA tensors; ql, qr (and f2) are written in place on the entries
+    the reference writes, on the current stream."""
+    import torch
+    nl, imax, nq = (int(x) for x in f.shape)
+    shape = (nl, imax, nq)
+    ops = [f, ql, qr] + ([dq] if name in ("muscl_deriv", "weno_deriv") else []) + \
+        ([f2] if name in ("muscl", "muscl_deriv") else [])
+    dev = _f64_cuda(name, shape, *ops)
+    L = load()
+    with torch.cuda.device(dev):
+        st = torch.cuda.current_stream().cuda_stream
+        if name == "muscl":
+            rc = L.hamstr_gpu_muscl(nl, imax, nq, f.data_ptr(), ql.data_ptr(), qr.data_ptr(), f2.data_ptr(), is_, ie,
+                                    th, qt, eps, st)
+        elif name == "muscl_deriv":
+            rc = L.hamstr_gpu_muscl_deriv(nl, imax, nq, f.data_ptr(), dq.data_ptr(), ql.data_ptr(), qr.data_ptr(),
+                                          f2.data_ptr(), is_, ie, th, qt, eps, st)
+        elif name == "weno":
+            rc = L.hamstr_gpu_weno(nl, imax, nq, f.data_ptr(), ql.data_ptr(), qr.data_ptr(), is_, ie, eps, st)
+        elif name == "weno_deriv":
+            rc = L.hamstr_gpu_weno_deriv(nl, imax, nq, f.data_ptr(), dq.data_ptr(), ql.data_ptr(), qr.data_ptr(),
+                                         is_, ie, eps, st)
+        else:
+            raise ValueError(name)
+    _check(rc)
 
 
 def _ptr(a: np.ndarray):
@@ -325,6 +408,11 @@ class GpuSolver:
         """False: plain FP64 (bit-identical); True: FP64 residual with an FP32
         Jacobian/ADI operator (defect correction)."""
         _check(load().hamstr_gpu_set_precision(self.h, int(bool(mixed))))
+
+    def set_sweep_order(self, order: int) -> None:
+        """0: the reference's sweeps (linearised residual at the scheme's
+        order); 1: first-order linearised residual (same converged state)."""
+        _check(load().hamstr_gpu_set_sweep_order(self.h, int(order)))
 
     def forces(self) -> dict:
         """Wall pressure force of the current state: Fx, Fy, M (about x=0.25), CL, CD, CM."""

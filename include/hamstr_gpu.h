@@ -42,6 +42,13 @@ extern "C" {
 #define HAMSTR_GPU_ERR_NAN       -4   /* NaN spectral radius (interfaceFlux.cpp:117-124) */
 #define HAMSTR_GPU_ERR_IO        -5   /* missing or malformed case file (io.cpp:19-23,138-141) */
 #define HAMSTR_GPU_ERR_NOMEM     -6   /* host or device allocation failed */
+/* An ADI line factorisation met a zero or non-finite pivot: the reciprocal
+   1/b of triSolvers.cpp:796-811 (and :900-929) is infinite or NaN.  The
+   reference divides regardless and carries the inf/NaN on. */
+#define HAMSTR_GPU_ERR_SINGULAR  -7
+/* An ADI sweep produced a non-finite dq (dq += r, ADI.cpp:247-248); the
+   reference prints a NaN residual at most (march.cpp:157-158). */
+#define HAMSTR_GPU_ERR_NONFINITE -8
 
 typedef struct hamstr_case hamstr_case; /* host mesh + inputs: MESHBLOCK + SOLNBLOCK */
 typedef struct hamstr_gpu hamstr_gpu;   /* device solver: SOLVER */
@@ -157,6 +164,19 @@ int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* e
  *                converged state is the FP64 residual's zero; the iteration
  *                history differs from the reference's. */
 int hamstr_gpu_set_precision(hamstr_gpu* g, int mixed);
+
+/* Order of the ADI sweeps' linearised residual (no counterpart in the
+ * reference, which always linearises the scheme's reconstruction,
+ * computeLinearRHS.cpp:281-292):
+ *   0 (default)  the reference's: dq reconstructed at the scheme's order;
+ *   1            first order: each face takes dq of its two cells, the
+ *                linearisation that matches the line operator (whose blocks
+ *                couple neighbouring cells only).
+ * The residual, and so the converged state, is unchanged; the iteration's
+ * path differs.  The reference's higher-order sweeps can diverge as msweep
+ * grows and leave a residual plateau that rises with CFL; the first-order
+ * sweeps are a convergent defect-correction iteration. */
+int hamstr_gpu_set_sweep_order(hamstr_gpu* g, int order);
 
 /* Batched form (no counterpart in the reference): several cases -- meshes
  * of any sizes and their flow conditions -- in one handle.  They are held
@@ -314,6 +334,50 @@ int hamstr_gpu_block_tridag4(int nlines, int N, int periodic, const double* A, c
  * serialised by the caller. */
 int hamstr_gpu_block_tridag4_noalloc(int nlines, int N, int periodic, const double* A, const double* B,
                                      const double* C, double* F, void* stream);
+
+/* ---------------- function-level entry points ---------------------------
+ * The reference's per-face and per-chain numerics, batched, on DEVICE
+ * arrays; each only enqueues on `stream` (a cudaStream_t or NULL).  Every
+ * output equals one reference call's bit for bit.
+ *
+ * SOLVER::fluxRoe2D (interfaceFlux.cpp:24-169) for n faces: nxy [n][2]
+ * (the face normal (dy, -dx), solver.h:46's nxyz), ql, qr [n][4] ->
+ * flux [n][4] (times the face area) and spec [n] (spectral radius times the
+ * area).  Where the reference exits on a NaN spectral radius
+ * (interfaceFlux.cpp:117-124) spec holds the NaN; callers check it. */
+int hamstr_gpu_flux_roe2d(int n, const double* nxy, const double* ql, const double* qr, double* flux, double* spec,
+                          double gamma, void* stream);
+/* SOLVER::jacobianRoe2D (jacobianRoe.cpp:9-70; IMODE 1, frozen Roe
+ * eigenvalues) for n faces: lmat, rmat [n][4][4], row-major, times the
+ * area -- the reference's lmat2[i][j], rmat2[i][j]. */
+int hamstr_gpu_jacobian_roe2d(int n, const double* nxy, const double* ql, const double* qr, double* lmat,
+                              double* rmat, double gamma, void* stream);
+/* RECONSTRUCTION::MUSCL / MUSCL_DERIV / WENO / WENO_DERIV
+ * (reconstruction.h:19-108, reconstruction.cpp:16-386) over nlines
+ * independent lines: f, dq, ql, qr, f2 are [nlines][imax][nq] (the
+ * reference's f[i][n] per line).  ql, qr are written for the entries the
+ * reference writes and left alone elsewhere:
+ *   MUSCL, MUSCL_DERIV: i in [is, ie]; qt == 0 copies f (dq), otherwise
+ *     the kappa scheme (th, qt, eps as the reference takes them), which
+ *     also leaves f2[i] = f[i+1] - f[i] for i < imax-1 as the reference
+ *     does.  Needs 1 <= is and ie <= imax-2 when qt != 0: at ie = imax-1
+ *     (computeRHS.cpp:267's call) the reference reads f2[imax-1] or
+ *     dq[imax], work-array entries left over from an earlier chain, and
+ *     its callers never use that last value.
+ *   WENO, WENO_DERIV: i in [is, imax-3], is >= 2, from f (dq) at i-2..i+2.
+ *     WENO's smoothness epsilon is 1e-15 whatever epsw says (the reference
+ *     overwrites the argument, reconstruction.cpp:145); WENO_DERIV uses
+ *     eps as given.  The reference reads a copy of f[0..ie]; these read f,
+ *     so results agree for ie = imax-1, its callers' value.
+ * HAMSTR_GPU_ERR_ARG for indices outside these ranges. */
+int hamstr_gpu_muscl(int nlines, int imax, int nq, const double* f, double* ql, double* qr, double* f2, int is,
+                     int ie, double th, double qt, double eps, void* stream);
+int hamstr_gpu_muscl_deriv(int nlines, int imax, int nq, const double* f, const double* dq, double* ql, double* qr,
+                           double* f2, int is, int ie, double th, double qt, double eps, void* stream);
+int hamstr_gpu_weno(int nlines, int imax, int nq, const double* f, double* ql, double* qr, int is, int ie,
+                    double epsw, void* stream);
+int hamstr_gpu_weno_deriv(int nlines, int imax, int nq, const double* f, const double* dq, double* ql, double* qr,
+                          int is, int ie, double eps, void* stream);
 
 /* Enqueues n pseudo-time steps on the handle's stream and returns without
  * waiting (no tolerance stop, no host copies): for callers that keep the

@@ -56,6 +56,7 @@ struct ho_case {
    int end_rule;
    /* project option: MUSCL limiter of order 3 (HO_LIMITER_*) */
    int limiter;
+   int sweep_order;   /* project option: 1 = first-order linearised residual in the ADI sweeps */
    double L2Norm, LInfNorm;
    /* solution arrays (solver.cpp:26-38) */
    double *q, *qt, *r, *r0, *dq, *sigma;
@@ -605,10 +606,9 @@ static void weno(ho_case* c, int is, int size)
 }
 
 /* WENO_5 linearisation, reconstruction.cpp:243-347 */
-static double weno5_deriv(double a, double b, double cc, double d, double e,
-                          double a_d, double b_d, double c_d, double d_d, double e_d)
+static double weno5_deriv_eps(double a, double b, double cc, double d, double e,
+                              double a_d, double b_d, double c_d, double d_d, double e_d, double epsw)
 {
-   const double epsw = 1e-10; /* the caller passes eps=1e-10 (computeLinearRHS.cpp:286) */
    double b1 = 13. / 12., b2 = 1. / 6.;
    double djm1 = a - 2. * b + cc;
    double ejm1 = a - 4. * b + 3. * cc;
@@ -655,6 +655,13 @@ static double weno5_deriv(double a, double b, double cc, double d, double e,
    double dw2_up_2 = 3 * dw0_up_2 / beta2 * beta0;
    double dw2 = (dw2_up_1 - dw2_up_2) / (dw0_down * dw0_down);
    return term1 + term2 + term3 + b2 * dw0 * q30 + b2 * dw1 * q31 + b2 * dw2 * q32;
+}
+
+static double weno5_deriv(double a, double b, double cc, double d, double e,
+                          double a_d, double b_d, double c_d, double d_d, double e_d)
+{
+   /* the caller passes eps=1e-10 (computeLinearRHS.cpp:286) */
+   return weno5_deriv_eps(a, b, cc, d, e, a_d, b_d, c_d, d_d, e_d, 1e-10);
 }
 
 /* WENO_DERIV wrapper, reconstruction.cpp:353-386 */
@@ -870,6 +877,127 @@ static void roe_jacobian(const double* s, const double* ql2, const double* qr2,
 }
 
 /* ------------------------------------------------------------------ */
+/* The reference's per-face and per-line functions on flat arrays      */
+/* (the checker of the library's function-level entry points)          */
+/* ------------------------------------------------------------------ */
+
+/* SOLVER::fluxRoe2D (interfaceFlux.cpp:24-169): -1 where the reference
+   exits on a NaN spectral radius */
+int ho_flux_roe2d(const double* nxy, const double* ql, const double* qr, double* flux, double* spec, double gamma)
+{
+   return roe_flux(nxy, ql, qr, flux, spec, gamma);
+}
+
+/* SOLVER::jacobianRoe2D (jacobianRoe.cpp:9-70): lm, rm [4][4] row-major */
+void ho_jacobian_roe2d(const double* nxy, const double* ql, const double* qr, double* lm, double* rm, double gamma)
+{
+   roe_jacobian(nxy, ql, qr, lm, rm, gamma);
+}
+
+/* RECONSTRUCTION::MUSCL (reconstruction.cpp:16-70) on one line: f, ql, qr,
+   f2 are [imax][nq]; loops and reads as the reference's, including f2[ie]
+   at ie = imax-1, which it does not write */
+void ho_muscl_line(const double* f, double* ql, double* qr, double* f2, int is, int ie, double th, double qt,
+                   double eps, int imax, int nq)
+{
+   int i, n, im = imax - 1;
+   double thm, thp;
+   if (qt == 0.0) {
+      for (n = 0; n < nq; n++)
+         for (i = is; i <= ie; i++) {
+            ql[i * nq + n] = f[i * nq + n];
+            qr[i * nq + n] = f[i * nq + n];
+         }
+      return;
+   }
+   thm = 1.0 - th;
+   thp = 1.0 + th;
+   for (n = 0; n < nq; n++) {
+      for (i = 0; i < im; i++) f2[i * nq + n] = f[(i + 1) * nq + n] - f[i * nq + n];
+      for (i = is; i <= ie; i++) {
+         double f2i = f2[i * nq + n], f2i1 = f2[(i - 1) * nq + n];
+         double a1 = 3.0 * (f2i * f2i1 + eps);
+         double a2 = 2.0 * (f2i - f2i1) * (f2i - f2i1) + a1;
+         double f3i = a1 / a2;
+         double f3qt = qt * f3i;
+         ql[i * nq + n] = f[i * nq + n] + f3qt * (thm * f2i1 + thp * f2i);
+         qr[i * nq + n] = f[i * nq + n] - f3qt * (thp * f2i1 + thm * f2i);
+      }
+   }
+}
+
+/* RECONSTRUCTION::MUSCL_DERIV (reconstruction.cpp:168-236) on one line */
+void ho_muscl_deriv_line(const double* f, double* ql, double* qr, double* f2, const double* dq, int is, int ie,
+                         double th, double qt, double eps, int imax, int nq)
+{
+   int i, n, im = imax - 1;
+   double thm, thp;
+   if (qt == 0.0) {
+      for (n = 0; n < nq; n++)
+         for (i = is; i <= ie; i++) {
+            ql[i * nq + n] = dq[i * nq + n];
+            qr[i * nq + n] = dq[i * nq + n];
+         }
+      return;
+   }
+   thm = 1.0 - th;
+   thp = 1.0 + th;
+   for (n = 0; n < nq; n++) {
+      for (i = 0; i < im; i++) f2[i * nq + n] = f[(i + 1) * nq + n] - f[i * nq + n];
+      for (i = is; i <= ie; i++) {
+         double f2i = f2[i * nq + n], f2i1 = f2[(i - 1) * nq + n];
+         double df2i = dq[(i + 1) * nq + n] - dq[i * nq + n];
+         double df2i1 = dq[i * nq + n] - dq[(i - 1) * nq + n];
+         double a1 = 3.0 * (f2i * f2i1 + eps);
+         double da1 = 3.0 * (df2i * f2i1 + f2i * df2i1);
+         double a2 = 2.0 * (f2i - f2i1) * (f2i - f2i1) + a1;
+         double da2 = 2.0 * 2.0 * (f2i - f2i1) * (df2i - df2i1) + da1;
+         double f3i = a1 / a2;
+         double df3i = da1 / a2 - a1 * da2 / (a2 * a2);
+         double f3qt = qt * f3i, df3qt = qt * df3i;
+         ql[i * nq + n] = dq[i * nq + n] + df3qt * (thm * f2i1 + thp * f2i) + f3qt * (thm * df2i1 + thp * df2i);
+         qr[i * nq + n] = dq[i * nq + n] - df3qt * (thp * f2i1 + thm * f2i) - f3qt * (thp * df2i1 + thm * df2i);
+      }
+   }
+}
+
+/* RECONSTRUCTION::WENO (reconstruction.cpp:133-160) on one line: entries
+   is .. imax-3 from f[i-2 .. i+2]; the smoothness epsilon is 1e-15 (the
+   reference overwrites epsw) */
+void ho_weno_line(const double* f, double* ql, double* qr, int is, int ie, double epsw, int imax, int nq)
+{
+   int i, n;
+   (void)ie;
+   (void)epsw;
+   for (n = 0; n < nq; n++)
+      for (i = is; i < imax - 2; i++) {
+         ql[i * nq + n] = weno5(f[(i - 2) * nq + n], f[(i - 1) * nq + n], f[i * nq + n], f[(i + 1) * nq + n],
+                                f[(i + 2) * nq + n]);
+         qr[i * nq + n] = weno5(f[(i + 2) * nq + n], f[(i + 1) * nq + n], f[i * nq + n], f[(i - 1) * nq + n],
+                                f[(i - 2) * nq + n]);
+      }
+}
+
+/* RECONSTRUCTION::WENO_DERIV (reconstruction.cpp:353-386) on one line */
+void ho_weno_deriv_line(const double* f, double* ql, double* qr, const double* dq, int is, int ie, double eps,
+                        int imax, int nq)
+{
+   int i, n;
+   (void)ie;
+   for (n = 0; n < nq; n++)
+      for (i = is; i < imax - 2; i++) {
+         const double* a = f + n;
+         const double* d = dq + n;
+         ql[i * nq + n] = weno5_deriv_eps(a[(i - 2) * nq], a[(i - 1) * nq], a[i * nq], a[(i + 1) * nq],
+                                          a[(i + 2) * nq], d[(i - 2) * nq], d[(i - 1) * nq], d[i * nq],
+                                          d[(i + 1) * nq], d[(i + 2) * nq], eps);
+         qr[i * nq + n] = weno5_deriv_eps(a[(i + 2) * nq], a[(i + 1) * nq], a[i * nq], a[(i - 1) * nq],
+                                          a[(i - 2) * nq], d[(i + 2) * nq], d[(i + 1) * nq], d[i * nq],
+                                          d[(i - 1) * nq], d[(i - 2) * nq], eps);
+      }
+}
+
+/* ------------------------------------------------------------------ */
 /* residual (computeRHS.cpp:17-427)                                    */
 /* ------------------------------------------------------------------ */
 
@@ -936,8 +1064,9 @@ int ho_linear_rhs(ho_case* c, double* l2, double* linf)
       int size = chain_stencil(c, i);
       int is = c->nGhost - 1, ie = size - 1, n, per;
       if (chain_gather(c, i, size, c->dq) != 0) return -2;
-      if (c->order == 1 || c->order == 3) muscl_deriv(c, is, ie, c->order == 1 ? 0.0 : 0.25);
-      if (c->order == 5) weno_deriv(c, is, size);
+      if (c->sweep_order == 1 || c->order == 1) muscl_deriv(c, is, ie, 0.0);
+      else if (c->order == 3) muscl_deriv(c, is, ie, 0.25);
+      else if (c->order == 5) weno_deriv(c, is, size);
       n = is;
       per = (c->chainConn[f1] == c->chainConn[f2 - 1]);
       for (f = f1; f < f2 - per; f++) {
@@ -1470,6 +1599,11 @@ int ho_set_option(ho_case* c, const char* name, int value)
    if (strcmp(name, "chain_end_rule") == 0) {
       if (value != HO_END_RULE_REFERENCE && value != HO_END_RULE_EXTENDED) return -1;
       c->end_rule = value;
+      return 0;
+   }
+   if (strcmp(name, "sweep_order") == 0) {
+      if (value != 0 && value != 1) return -1;
+      c->sweep_order = value;
       return 0;
    }
    return -1;

@@ -60,6 +60,12 @@ void ho_set_run(ho_case* c, int order, int msweep, double cfl);
 #define HO_LIMITER_REFERENCE 0
 #define HO_LIMITER_MINMOD 1
 #define HO_LIMITER_VANALBADA 2
+/*   "sweep_order"     0 (default): the ADI sweeps' linearised residual
+ *                     reconstructs dq at the scheme's order
+ *                     (computeLinearRHS.cpp:281-292); 1: at first order
+ *                     (dq of the two cells of each face), a project option
+ *                     that leaves the residual and so the converged state
+ *                     unchanged. */
 int  ho_set_option(ho_case* c, const char* name, int value);
 
 /* Each returns 0, or -1 when a spectral radius is NaN (the reference exits
@@ -86,6 +92,21 @@ int ho_forces(const ho_case* c, double* out6);
 /* triSolvers.cpp blockTridag4 / blockTridagPeriodic4 on flat [N][4][4]
  * blocks and [N][4] right-hand sides, in place like the reference. */
 int ho_block_tridag4(double* a, double* b, double* c, double* f, int N, int periodic);
+
+/* The reference's per-face and per-line functions on flat arrays:
+ * SOLVER::fluxRoe2D / jacobianRoe2D (interfaceFlux.cpp:24-169,
+ * jacobianRoe.cpp:9-70) for one face, and RECONSTRUCTION::MUSCL /
+ * MUSCL_DERIV / WENO / WENO_DERIV (reconstruction.cpp:16-386) for one line
+ * of [imax][nq] values, with the reference's loops and index ranges. */
+int  ho_flux_roe2d(const double* nxy, const double* ql, const double* qr, double* flux, double* spec, double gamma);
+void ho_jacobian_roe2d(const double* nxy, const double* ql, const double* qr, double* lm, double* rm, double gamma);
+void ho_muscl_line(const double* f, double* ql, double* qr, double* f2, int is, int ie, double th, double qt,
+                   double eps, int imax, int nq);
+void ho_muscl_deriv_line(const double* f, double* ql, double* qr, double* f2, const double* dq, int is, int ie,
+                         double th, double qt, double eps, int imax, int nq);
+void ho_weno_line(const double* f, double* ql, double* qr, int is, int ie, double epsw, int imax, int nq);
+void ho_weno_deriv_line(const double* f, double* ql, double* qr, const double* dq, int is, int ie, double eps,
+                        int imax, int nq);
 
 /* Named arrays: q qt r r0 dq sigma ff x vol normVec refMtx (doubles) and
  * faces chainConn faceStartPerChain c2chain bFaces chainsPerColor (ints). */

@@ -274,3 +274,91 @@ def march_replicas(cases, iters: int) -> None:
     rc = lib.ho_march_replicas(arr, len(cases), iters)
     if rc != 0:
         raise RuntimeError("oracle replica march failed")
+
+
+# ---------------------------------------------------------------------------
+# The reference's per-face and per-line functions (checkers of the library's
+# function-level entry points).  Arrays are numpy float64; "reference" needs
+# an open reference case handle for the SOLVER methods.
+# ---------------------------------------------------------------------------
+
+def flux_roe2d(nxy, ql, qr, gamma: float = 1.4, kind: str = "port", case: "OracleCase" = None):
+    """SOLVER::fluxRoe2D face by face: (flux [n][4], spec [n])."""
+    lib, p = _lib(kind)
+    nxy, ql, qr = (np.ascontiguousarray(a, dtype=np.float64) for a in (nxy, ql, qr))
+    n = nxy.shape[0]
+    flux, spec = np.zeros((n, 4)), np.zeros(n)
+    if kind == "port":
+        fn = lib.ho_flux_roe2d
+        fn.restype, fn.argtypes = ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_double]
+    else:
+        fn = lib.ref_flux_roe2d
+        fn.restype, fn.argtypes = None, [ctypes.c_void_p] * 6 + [ctypes.c_double]
+    for k in range(n):
+        s = np.array(nxy[k])
+        a, b = np.array(ql[k]), np.array(qr[k])
+        fl, sp = np.zeros(4), np.zeros(1)
+        if kind == "port":
+            fn(_ptr(s), _ptr(a), _ptr(b), _ptr(fl), _ptr(sp), gamma)
+        else:
+            fn(case.h, _ptr(s), _ptr(a), _ptr(b), _ptr(fl), _ptr(sp), gamma)
+        flux[k], spec[k] = fl, sp[0]
+    return flux, spec
+
+
+def jacobian_roe2d(nxy, ql, qr, gamma: float = 1.4, kind: str = "port", case: "OracleCase" = None):
+    """SOLVER::jacobianRoe2D face by face: (lmat [n][4][4], rmat [n][4][4])."""
+    lib, p = _lib(kind)
+    nxy, ql, qr = (np.ascontiguousarray(a, dtype=np.float64) for a in (nxy, ql, qr))
+    n = nxy.shape[0]
+    lm, rm = np.zeros((n, 4, 4)), np.zeros((n, 4, 4))
+    if kind == "port":
+        fn = lib.ho_jacobian_roe2d
+        fn.restype, fn.argtypes = None, [ctypes.c_void_p] * 5 + [ctypes.c_double]
+    else:
+        fn = lib.ref_jacobian_roe2d
+        fn.restype, fn.argtypes = None, [ctypes.c_void_p] * 6 + [ctypes.c_double]
+    for k in range(n):
+        s = np.array(nxy[k])
+        a, b = np.array(ql[k]), np.array(qr[k])
+        l4, r4 = np.zeros(16), np.zeros(16)
+        if kind == "port":
+            fn(_ptr(s), _ptr(a), _ptr(b), _ptr(l4), _ptr(r4), gamma)
+        else:
+            fn(case.h, _ptr(s), _ptr(a), _ptr(b), _ptr(l4), _ptr(r4), gamma)
+        lm[k], rm[k] = l4.reshape(4, 4), r4.reshape(4, 4)
+    return lm, rm
+
+
+def recon_line(name: str, f, is_: int, ie: int, *, dq=None, th: float = 1.0 / 3.0, qt: float = 0.25,
+               eps: float = 1e-10, ql=None, qr=None, f2=None, kind: str = "port"):
+    """RECONSTRUCTION::MUSCL / MUSCL_DERIV / WENO / WENO_DERIV on one line
+    f [imax][nq] (name "muscl", "muscl_deriv", "weno", "weno_deriv").
+    ql, qr, f2 give the arrays' prior contents (entries the function does
+    not write keep them); returns (ql, qr, f2)."""
+    lib, p = _lib(kind)
+    f = np.array(f, dtype=np.float64, order="C", copy=True)
+    imax, nq = f.shape
+    ql = np.zeros_like(f) if ql is None else np.array(ql, dtype=np.float64, order="C", copy=True)
+    qr = np.zeros_like(f) if qr is None else np.array(qr, dtype=np.float64, order="C", copy=True)
+    f2 = np.zeros_like(f) if f2 is None else np.array(f2, dtype=np.float64, order="C", copy=True)
+    vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    fn = getattr(lib, p + name + "_line")
+    fn.restype = None
+    if name == "muscl":
+        fn.argtypes = [vp] * 4 + [i, i, d, d, d, i, i]
+        fn(_ptr(f), _ptr(ql), _ptr(qr), _ptr(f2), is_, ie, th, qt, eps, imax, nq)
+    elif name == "muscl_deriv":
+        dqa = np.array(dq, dtype=np.float64, order="C", copy=True)
+        fn.argtypes = [vp] * 5 + [i, i, d, d, d, i, i]
+        fn(_ptr(f), _ptr(ql), _ptr(qr), _ptr(f2), _ptr(dqa), is_, ie, th, qt, eps, imax, nq)
+    elif name == "weno":
+        fn.argtypes = [vp] * 3 + [i, i, d, i, i]
+        fn(_ptr(f), _ptr(ql), _ptr(qr), is_, ie, eps, imax, nq)
+    elif name == "weno_deriv":
+        dqa = np.array(dq, dtype=np.float64, order="C", copy=True)
+        fn.argtypes = [vp] * 4 + [i, i, d, i, i]
+        fn(_ptr(f), _ptr(ql), _ptr(qr), _ptr(dqa), is_, ie, eps, imax, nq)
+    else:
+        raise ValueError(name)
+    return ql, qr, f2

@@ -32,7 +32,10 @@
 #include <unistd.h>
 #include <limits.h>
 
+#include <vector>
+
 #include "hamstr.h"
+#include "reconstruction.h"
 #include "triSolvers.h"
 
 // ------------------------------------------------------------------
@@ -280,6 +283,56 @@ int ref_get_int(void* h, const char* name, int* out)
    }
    if (!strcmp(name, "chainsPerColor")) { memcpy(out, m->chainsPerColor, sizeof(int) * m->nColor); return 0; }
    return -1;
+}
+
+// SOLVER::fluxRoe2D / jacobianRoe2D of the handle's solver on one face
+void ref_flux_roe2d(void* h, double* nxy, double* ql, double* qr, double* flux, double* spec, double gamma)
+{
+   ((RefCase*)h)->solv->fluxRoe2D(nxy, ql, qr, flux, spec, gamma);
+}
+
+void ref_jacobian_roe2d(void* h, double* nxy, double* ql, double* qr, double* lm, double* rm, double gamma)
+{
+   ArenaScope arena;   // jacobianRoe2D / 3D leak their per-call arrays
+   double* L[4] = {lm, lm + 4, lm + 8, lm + 12};
+   double* R[4] = {rm, rm + 4, rm + 8, rm + 12};
+   ((RefCase*)h)->solv->jacobianRoe2D(nxy, ql, qr, L, R, gamma);
+}
+
+// RECONSTRUCTION::* on one line of flat [imax][nq] arrays (rows views)
+static std::vector<double*> rows(double* p, int imax, int nq)
+{
+   std::vector<double*> v((size_t)imax + 1);
+   for (int i = 0; i < imax; i++) v[i] = p + (size_t)i * nq;
+   v[imax] = nullptr;
+   return v;
+}
+
+void ref_muscl_line(double* f, double* ql, double* qr, double* f2, int is, int ie, double th, double qt, double eps,
+                    int imax, int nq)
+{
+   auto F = rows(f, imax, nq), QL = rows(ql, imax, nq), QR = rows(qr, imax, nq), F2 = rows(f2, imax, nq);
+   RECONSTRUCTION::MUSCL(F.data(), QL.data(), QR.data(), F2.data(), is, ie, th, qt, eps, imax, nq);
+}
+
+void ref_muscl_deriv_line(double* f, double* ql, double* qr, double* f2, double* dq, int is, int ie, double th,
+                          double qt, double eps, int imax, int nq)
+{
+   auto F = rows(f, imax, nq), QL = rows(ql, imax, nq), QR = rows(qr, imax, nq), F2 = rows(f2, imax, nq);
+   auto DQ = rows(dq, imax, nq);
+   RECONSTRUCTION::MUSCL_DERIV(F.data(), QL.data(), QR.data(), F2.data(), DQ.data(), is, ie, th, qt, eps, imax, nq);
+}
+
+void ref_weno_line(double* f, double* ql, double* qr, int is, int ie, double epsw, int imax, int nq)
+{
+   auto F = rows(f, imax, nq), QL = rows(ql, imax, nq), QR = rows(qr, imax, nq);
+   RECONSTRUCTION::WENO(F.data(), QL.data(), QR.data(), is, ie, epsw, imax, nq);
+}
+
+void ref_weno_deriv_line(double* f, double* ql, double* qr, double* dq, int is, int ie, double eps, int imax, int nq)
+{
+   auto F = rows(f, imax, nq), QL = rows(ql, imax, nq), QR = rows(qr, imax, nq), DQ = rows(dq, imax, nq);
+   RECONSTRUCTION::WENO_DERIV(F.data(), QL.data(), QR.data(), DQ.data(), is, ie, eps, imax, nq);
 }
 
 // TRISOLVER::blockTridag4 / blockTridagPeriodic4 on flat [N][4][4] blocks

@@ -137,3 +137,29 @@ def test_cfl_ramp_matches_oracle(make_case, oracle_lib, native_lib):
             ho, hg = orc.step(), gpu.step()
             _close(hg[0], ho[0], "L2 at CFL %g step %d" % (cfl, it))
     _eq(gpu.get("q"), orc.get("q"), "q after the ramp")
+
+
+@pytest.mark.parametrize("order,mixed_precision", [(3, False), (5, False), (5, True)])
+def test_first_order_sweeps(make_case, oracle_lib, native_lib, order, mixed_precision):
+    """hamstr_gpu_set_sweep_order(1): the sweeps' linearised residual at
+    first order.  FP64: equal to the oracle's option bit for bit.  The
+    first residual of every form is the plain one (the residual itself is
+    unchanged)."""
+    orc, gpu = _pair(make_case, oracle_lib, HALF, 1, order=order, CFL=5.0, msweep=2)
+    orc.set_option("sweep_order", 1)
+    gpu.set_sweep_order(1)
+    gpu.set_precision(mixed_precision)
+    _perturb(orc, gpu, 13, 0.02)
+    for it in range(5):
+        ho, hg = orc.step(), gpu.step()
+        if it == 0 or not mixed_precision:
+            _close(hg[0], ho[0], "rhs L2 step %d" % it)
+    if not mixed_precision:
+        for name in ("q", "dq", "r", "sigma"):
+            _eq(gpu.get(name), orc.get(name), name)
+    else:
+        q, qo = gpu.get("q"), orc.get("q")
+        assert np.max(np.abs(q - qo)) < 1e-5 * np.max(np.abs(qo))
+    gpu.set_sweep_order(0)
+    with pytest.raises(Exception):
+        gpu.set_sweep_order(2)

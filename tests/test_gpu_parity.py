@@ -182,3 +182,56 @@ def test_update_solution_bitexact(make_case, oracle_lib, native_lib):
     assert fn(orc.h, b"q", b"qt", 0.25) == 0
     gpu.update_solution("q", "qt", 0.25)
     _eq(gpu.get("qt"), orc.get("qt"), "qt")
+
+
+def _closed_chain_face(host, k=2):
+    """A face inside a closed chain (periodic loop), k faces from its start."""
+    fs, cc = host.get_int("faceStartPerChain"), host.get_int("chainConn")
+    for c in range(len(fs) - 1):
+        if cc[fs[c]] == cc[fs[c + 1] - 1] and fs[c + 1] - fs[c] > k + 2:
+            return int(cc[fs[c] + k])
+    raise AssertionError("no closed chain")
+
+
+def test_singular_pivot_reports_error(make_case, oracle_lib, native_lib):
+    """A zero block pivot made on the host: with every face Jacobian zero
+    except lmat[0][0] = -1 of one loop face and CFL/sigma = 1 exactly, that
+    face's left row assembles to B = I + (-1) e00 (ADI.cpp:103-118, 197-217),
+    whose first pivot is 0, so 1/0 is infinite (triSolvers.cpp:796)."""
+    from hamstr_oop_gb300 import native
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 16, 4, order=1, CFL=10.0)
+    gpu.compute_rhs(True)
+    ff_ok, sig_ok = gpu.get("ff"), gpu.get("sigma")
+    nf, nc = host.sizes["nFace"], host.sizes["nCell"]
+    ff = np.zeros((nf, 32))
+    ff[_closed_chain_face(host), 0] = -1.0
+    gpu.set("ff", ff.ravel())
+    gpu.set("sigma", np.full(nc, 10.0))
+    gpu.set("r", 1e-3 * np.random.default_rng(1).standard_normal(4 * nc))
+    with pytest.raises(native.HamstrError) as ei:
+        gpu.adi()
+    assert ei.value.status == -7 and "pivot" in str(ei.value)
+    # the status is cleared and the handle stays usable
+    gpu.set("q", orc.get("q"))
+    gpu.set("ff", ff_ok)
+    gpu.set("sigma", sig_ok)
+    gpu.compute_rhs(True)
+    gpu.adi()
+
+
+def test_nonfinite_dq_reports_error(make_case, oracle_lib, native_lib):
+    """A NaN right-hand side set on the host reaches dq through the line
+    solve; the sweep reports it instead of carrying it into q unnoticed."""
+    from hamstr_oop_gb300 import native
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 16, 4, order=3, CFL=10.0)
+    gpu.compute_rhs(True)
+    r = gpu.get("r")
+    r[4 * 7 + 2] = np.nan
+    gpu.set("r", r)
+    with pytest.raises(native.HamstrError) as ei:
+        gpu.adi()
+    assert ei.value.status == -8
+    gpu.set("q", orc.get("q"))
+    gpu.compute_rhs(True)
+    gpu.adi()
+    assert np.all(np.isfinite(gpu.get("q")))

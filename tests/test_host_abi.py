@@ -66,3 +66,14 @@ def test_testcase_nonzero_rejected(make_case, native_lib):
     case = make_case(16, 4, testcase=1)
     with pytest.raises(native.HamstrError):
         native.Case(case)
+
+
+def test_every_status_code_has_a_message(native_lib):
+    """Each HAMSTR_GPU_ERR_* of the header has its own hamstr_gpu_strerror text."""
+    import os
+    import re
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "hamstr_gpu.h")
+    codes = [int(v) for v in re.findall(r"#define HAMSTR_GPU_ERR_\w+\s+(-\d+)", open(hdr).read())]
+    assert len(codes) >= 8 and len(set(codes)) == len(codes)
+    msgs = [native_lib.hamstr_gpu_strerror(c).decode() for c in codes]
+    assert "unknown status" not in msgs and len(set(msgs)) == len(msgs)

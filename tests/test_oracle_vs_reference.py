@@ -47,3 +47,35 @@ def test_explicit_schemes_bitexact(make_case, oracle_lib, order):
         assert np.array_equal(ref.step_explicit(scheme), port.step_explicit(scheme))
     for name in ("q", "qt", "r", "sigma"):
         assert np.array_equal(ref.get(name), port.get(name)), name
+
+
+def test_flux_and_jacobian_per_face_bitexact(make_case, oracle_lib):
+    """ho_flux_roe2d / ho_jacobian_roe2d against SOLVER::fluxRoe2D /
+    jacobianRoe2D of the reference, face by face."""
+    from pointwise_inputs import faces
+    ref = oracle_lib.OracleCase(make_case(16, 4), "reference")
+    nxy, ql, qr = faces(300, 21)
+    f1, s1 = oracle_lib.flux_roe2d(nxy, ql, qr, kind="port")
+    f2, s2 = oracle_lib.flux_roe2d(nxy, ql, qr, kind="reference", case=ref)
+    assert np.array_equal(f1, f2) and np.array_equal(s1, s2)
+    l1, r1 = oracle_lib.jacobian_roe2d(nxy, ql, qr, kind="port")
+    l2, r2 = oracle_lib.jacobian_roe2d(nxy, ql, qr, kind="reference", case=ref)
+    assert np.array_equal(l1, l2) and np.array_equal(r1, r2)
+
+
+@pytest.mark.parametrize("name,is_,ie_off,qt", [("muscl", 1, 2, 0.25), ("muscl", 1, 1, 0.25), ("muscl", 0, 1, 0.0),
+                                                ("muscl_deriv", 2, 2, 0.25), ("muscl_deriv", 1, 1, 0.0),
+                                                ("weno", 2, 1, 0.25), ("weno_deriv", 2, 1, 0.25),
+                                                ("weno_deriv", 3, 1, 0.25)])
+def test_reconstructions_per_line_bitexact(oracle_lib, name, is_, ie_off, qt):
+    """ho_*_line against RECONSTRUCTION::* of the reference on one line,
+    outputs and the f2 work array (ie = imax - ie_off)."""
+    from pointwise_inputs import lines
+    f, dq, prior = lines(3, 23, 4, 9)
+    for k in range(f.shape[0]):
+        kw = dict(dq=dq[k], qt=qt, th=1.0 / 3.0, eps=1e-10, ql=prior[0, k], qr=prior[1, k], f2=prior[2, k])
+        ie = f.shape[1] - ie_off
+        a = oracle_lib.recon_line(name, f[k], is_, ie, kind="port", **kw)
+        b = oracle_lib.recon_line(name, f[k], is_, ie, kind="reference", **kw)
+        for x, y, what in zip(a, b, ("ql", "qr", "f2")):
+            assert np.array_equal(x, y), (name, k, what)
