@@ -89,7 +89,7 @@ WORKLOADS["c5"] = dict(warm=True, ni=256, nj=64, split=0.0, seed=0, end_rule=0, 
 # approaching from its own side, so the ladder runs on until every
 # condition's fields agree with the plain FP64 drop-in's to 1e-8.
 TARGET = dict(ni=128, nj=32, split=0.0, seed=0, end_rule=0, order=1, CFL=10.0, msweep=2, Mach=0.5, alpha=1.25,
-              train=64, test=16, tols=(1e-10, 1e-12, 1e-13, 1e-14, 1e-15), cap=12000, epochs=40, batch=16384,
+              train=64, test=16, tols=(1e-10, 1e-12, 1e-13, 1e-14, 1e-15, 1e-16), cap=12000, epochs=40, batch=16384,
               lr=2e-3, repeats=3, accuracy=1e-8, name="naca0012_ogrid_128x32_order1_cfl10_msweep2_target_form")
 L2_FLUSH_BYTES = 512 << 20
 
@@ -518,19 +518,20 @@ def measured_peaks() -> dict:
 FP64_WARP_INSTR_PER_S = 15.8e9
 
 # Per-launch figures of the FP64 kernels on the c2 workload (512 x 128 half
-# split, WENO, after the CFL ramp) from one ncu capture of
-# `bench.py --workload c2 --profile-steps 1`:
+# split, WENO, after the CFL ramp, the autotuner's shape on this mesh) from
+# one ncu capture of `bench.py --profile-steps 2 --shape ...` (two steps):
 #   dram_bytes     dram__bytes_read.sum + dram__bytes_write.sum
 #   fp64_inst      smsp__inst_executed_pipe_fp64.sum (warp instructions)
-# adi_solve is the mean of its launches (two waves, two sweeps).
+# Kernels launched more than once a step (adi_solve: two waves, two sweeps;
+# the per-sweep kernels) give the mean of their launches.
 NCU_PER_LAUNCH = {
     "naca0012_ogrid_512x128_split50_weno5_cfl20_msweep2": {
-        "recon5": {"dram_bytes": 156.2e6, "fp64_inst": None},
-        "rhs_face": {"dram_bytes": 16.8e6, "fp64_inst": None},
-        "adi_factor": {"dram_bytes": 55.3e6, "fp64_inst": None},
+        "recon5": {"dram_bytes": 154.9e6, "fp64_inst": 2898203},
+        "rhs_face": {"dram_bytes": 16.84e6, "fp64_inst": 2620380},
+        "adi_factor": {"dram_bytes": 54.0e6, "fp64_inst": None},
         "adi_solve": {"dram_bytes": 24.5e6, "fp64_inst": None},
-        "lin_recon5": {"dram_bytes": 209.2e6, "fp64_inst": None},
-        "lin_face": {"dram_bytes": 55.2e6, "fp64_inst": None},
+        "lin_recon5": {"dram_bytes": 209.3e6, "fp64_inst": 2554292},
+        "lin_face": {"dram_bytes": 55.25e6, "fp64_inst": 328832},
     },
 }
 
@@ -834,14 +835,15 @@ def ladder_march(g, tols, cap: int, n_inst: int) -> list:
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     out, done = [], 0
+    own = [0] * n_inst        # steps each instance took (a batch freezes an instance at its own stop)
     for tol in tols:
         hist, ok = g.march(cap - done, tol)
         secs = time.perf_counter() - t0
         h = hist if hist.ndim == 3 else hist[:, None, :]
-        steps = []
         for k in range(n_inst):
             hit = np.flatnonzero(h[:, k, 0] <= tol)
-            steps.append(done + (int(hit[0]) + 1 if hit.size else h.shape[0]))
+            own[k] += int(hit[0]) + 1 if hit.size else h.shape[0]
+        steps = list(own)
         done += h.shape[0]
         out.append({"tol": tol, "seconds": secs, "converged": bool(ok), "steps": steps, "q": g.get("q")})
         if not ok or done >= cap:
@@ -934,9 +936,15 @@ def target_form() -> dict:
                           "speedup_vs_plain_fp64": p_secs / med}
         ladder.append(row)
     acc = c["accuracy"]
-    meet = [r for r in ladder if r["batched_fp32_op_warm"]["max_rel_vs_plain_fp64"] <= acc
-            and r["plain_fp64"]["all_converged"] and r["batched_fp32_op_warm"]["all_converged"]]
-    pick = meet[0] if meet else None
+
+    def first_meeting(label):
+        for r in ladder:
+            if (r[label]["max_rel_vs_plain_fp64"] <= acc and r["plain_fp64"]["all_converged"]
+                    and r[label]["all_converged"]):
+                return r
+        return None
+    pick = first_meeting("batched_fp32_op_warm")
+    cold = first_meeting("batched_fp32_op_freestream")
     out = {"workload": c["name"], "cells_per_condition": nc, "conditions": len(conds),
            "conditions_distribution": "Mach U[0.3, 0.85], alpha U[-2, 4] deg, seed 1 (held out)",
            "cap": cap, "accuracy": acc, "ladder": ladder,
@@ -947,6 +955,12 @@ def target_form() -> dict:
            "solves_per_s": pick["batched_fp32_op_warm"]["solves_per_s"] if pick else None,
            "plain_fp64_solves_per_s": pick["plain_fp64"]["solves_per_s"] if pick else None,
            "speedup_vs_plain_fp64": pick["batched_fp32_op_warm"]["speedup_vs_plain_fp64"] if pick else None,
+           "without_warm_start": {
+               "tol": cold["tol"] if cold else None,
+               "max_rel_vs_fp64": cold["batched_fp32_op_freestream"]["max_rel_vs_plain_fp64"] if cold else None,
+               "solves_per_s": cold["batched_fp32_op_freestream"]["solves_per_s"] if cold else None,
+               "plain_fp64_solves_per_s": cold["plain_fp64"]["solves_per_s"] if cold else None,
+               "speedup_vs_plain_fp64": cold["batched_fp32_op_freestream"]["speedup_vs_plain_fp64"] if cold else None},
            "note": "tol: the loosest tolerance of the ladder at which every condition's warm-started batched "
                    "FP32-operator state is within `accuracy` (max |q - q_fp64| / max |q_fp64|) of the plain FP64 "
                    "drop-in's state at the same tolerance; the plain drop-in's steps are the oracle's bit for bit"}

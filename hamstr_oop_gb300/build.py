@@ -33,7 +33,7 @@ CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall", "-Wno-un
             "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["rhs.cu", "adi.cu", "api.cu", "trisolve.cu", "mixed.cu", "forces.cu", "mlp_gemm.cu", "mlp_api.cu", "mlp_net.cu", "checks.cu",
-              "pointwise.cu"]
+              "pointwise.cu", "strand5.cu"]
 CXX_SOURCES = ["plan.cpp", os.path.join("host", "hamstr_host.cpp"), os.path.join("host", "hamstr_dropin.cpp")]
 
 

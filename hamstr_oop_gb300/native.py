@@ -121,6 +121,9 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_muscl_deriv": (i, [i, i, i, vp, vp, vp, vp, vp, i, i, d, d, d, vp]),
         "hamstr_gpu_weno": (i, [i, i, i, vp, vp, vp, i, i, d, vp]),
         "hamstr_gpu_weno_deriv": (i, [i, i, i, vp, vp, vp, vp, i, i, d, vp]),
+        "hamstr_gpu_flux_roe3d": (i, [i, vp, vp, vp, vp, vp, d, vp]),
+        "hamstr_gpu_jacobian_roe3d": (i, [i, vp, vp, vp, vp, vp, d, vp]),
+        "hamstr_gpu_block_tridag5": (i, [i, i, i, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -225,6 +228,54 @@ def jacobian_roe2d(nxy, ql, qr, gamma: float = 1.4):
         _check(load().hamstr_gpu_jacobian_roe2d(n, nxy.data_ptr(), ql.data_ptr(), qr.data_ptr(), lm.data_ptr(),
                                                 rm.data_ptr(), float(gamma), torch.cuda.current_stream().cuda_stream))
     return lm, rm
+
+
+def flux_roe3d(nxyz, ql, qr, gamma: float = 1.4):
+    """SOLVER::fluxRoe3D over n faces (hamstr_gpu_flux_roe3d): nxyz (n, 3),
+    ql, qr (n, 5) -> (flux (n, 5), spec (n,)), not scaled by the area."""
+    import torch
+    n = int(nxyz.shape[0])
+    dev = _f64_cuda("flux_roe3d", (n, 3), nxyz)
+    _f64_cuda("flux_roe3d", (n, 5), ql, qr)
+    flux = torch.empty((n, 5), dtype=torch.float64, device=dev)
+    spec = torch.empty((n,), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _check(load().hamstr_gpu_flux_roe3d(n, nxyz.data_ptr(), ql.data_ptr(), qr.data_ptr(), flux.data_ptr(),
+                                            spec.data_ptr(), float(gamma), torch.cuda.current_stream().cuda_stream))
+    return flux, spec
+
+
+def jacobian_roe3d(nxyz, ql, qr, gamma: float = 1.4):
+    """SOLVER::jacobianRoe3D over n faces (hamstr_gpu_jacobian_roe3d):
+    returns (lmat (n, 5, 5), rmat (n, 5, 5))."""
+    import torch
+    n = int(nxyz.shape[0])
+    dev = _f64_cuda("jacobian_roe3d", (n, 3), nxyz)
+    _f64_cuda("jacobian_roe3d", (n, 5), ql, qr)
+    lm = torch.empty((n, 5, 5), dtype=torch.float64, device=dev)
+    rm = torch.empty((n, 5, 5), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _check(load().hamstr_gpu_jacobian_roe3d(n, nxyz.data_ptr(), ql.data_ptr(), qr.data_ptr(), lm.data_ptr(),
+                                                rm.data_ptr(), float(gamma), torch.cuda.current_stream().cuda_stream))
+    return lm, rm
+
+
+def block_tridag5(A, B, C, F, periodic: bool) -> None:
+    """TRISOLVER::blockTridag / blockTridagPeriodic (nq = 5) over lines
+    (hamstr_gpu_block_tridag5), in place on torch CUDA tensors: A, B, C
+    (nlines, N, 5, 5) become the reference's scratch, F (nlines, N, 5) the
+    solution; on the current stream."""
+    import torch
+    if F.dim() != 3 or F.shape[2] != 5:
+        raise ValueError("block_tridag5: F must be (nlines, N, 5), got %s" % (tuple(F.shape),))
+    nl, n = int(F.shape[0]), int(F.shape[1])
+    dev = _f64_cuda("block_tridag5", (nl, n, 5, 5), A, B, C)
+    _f64_cuda("block_tridag5", (nl, n, 5), F)
+    if F.device != dev:
+        raise ValueError("block_tridag5: every operand must be on %s" % dev)
+    with torch.cuda.device(dev):
+        _check(load().hamstr_gpu_block_tridag5(nl, n, int(periodic), A.data_ptr(), B.data_ptr(), C.data_ptr(),
+                                               F.data_ptr(), torch.cuda.current_stream().cuda_stream))
 
 
 def reconstruct(name: str, f, ql, qr, is_: int, ie: int, *, dq=None, f2=None, th: float = 1.0 / 3.0,

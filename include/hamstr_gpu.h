@@ -379,6 +379,26 @@ int hamstr_gpu_weno(int nlines, int imax, int nq, const double* f, double* ql, d
 int hamstr_gpu_weno_deriv(int nlines, int imax, int nq, const double* f, const double* dq, double* ql, double* qr,
                           int is, int ie, double eps, void* stream);
 
+/* The 5-variable (3D strand) numerics, batched on DEVICE arrays.  The
+ * reference's -DDim3 driver does not compile (io.cpp:306), but these
+ * functions are compiled in every reference build and are given here at
+ * function level, each output equal to one reference call's bit for bit:
+ *   SOLVER::fluxRoe3D (interfaceFlux.cpp:176-319): nxyz [n][3], ql, qr
+ *     [n][5] (rho, rho u, rho v, rho w, E) -> flux [n][5], spec [n]; unlike
+ *     the 2D flux neither is multiplied by the face area;
+ *   SOLVER::jacobianRoe3D (jacobianRoe.cpp:92-620, frozen eigenvalues,
+ *     IMODE 1) -> lmat, rmat [n][5][5] row-major;
+ *   TRISOLVER::blockTridag / blockTridagPeriodic (triSolvers.cpp:443-766,
+ *     nq = 5) over nlines lines of N block rows, in place: A, B, C
+ *     [nlines][N][5][5] are overwritten as the reference's scratch and F
+ *     [nlines][N][5] with the solution; periodic needs N >= 2. */
+int hamstr_gpu_flux_roe3d(int n, const double* nxyz, const double* ql, const double* qr, double* flux, double* spec,
+                          double gamma, void* stream);
+int hamstr_gpu_jacobian_roe3d(int n, const double* nxyz, const double* ql, const double* qr, double* lmat,
+                              double* rmat, double gamma, void* stream);
+int hamstr_gpu_block_tridag5(int nlines, int N, int periodic, double* A, double* B, double* C, double* F,
+                             void* stream);
+
 /* Enqueues n pseudo-time steps on the handle's stream and returns without
  * waiting (no tolerance stop, no host copies): for callers that keep the
  * state on the GPU and synchronise themselves (timing, pipelines). */

@@ -734,14 +734,14 @@ static int roe_flux(const double* s, const double* ql, const double* qr,
 
 /* ------------------------------------------------------------------ */
 /* Roe flux Jacobian, frozen eigenvalues (jacobianRoe.cpp:9-70,92-620) */
-/* Restated on the 5-variable embedding (w = 0) and reduced with the   */
-/* index map {0,1,2,4}, times the face area.                           */
+/* jacobianRoe3D (IMODE 1) on 5 variables; the 2D form embeds its      */
+/* state (w = 0) and reduces with the index map {0,1,2,4} x area.      */
 /* ------------------------------------------------------------------ */
 
-static void roe_jacobian(const double* s, const double* ql2, const double* qr2,
-                         double* lm2, double* rm2, double gam)
+static void roe_jacobian3d(const double* nxyz, const double* ql, const double* qr, double lmat[5][5],
+                           double rmat[5][5], double gam)
 {
-   double ql[5], qr[5], nxd, nyd, nzd, area, nx, ny, nz;
+   double nxd, nyd, nzd, area, nx, ny, nz;
    double gm1 = gam - 1.0;
    double rol, ul, vl, wl, pl, hl, ror, ur, vr, wr, pr, hr, dp, uconl, uconr;
    double dro_dql[5], dro_dqr[5], du_dql[5], du_dqr[5], dv_dql[5], dv_dqr[5];
@@ -749,15 +749,10 @@ static void roe_jacobian(const double* s, const double* ql2, const double* qr2,
    double dq5_dql[5], dq5_dqr[5];
    double ddel1_dql[5], ddel1_dqr[5], ddel2_dql[5], ddel2_dqr[5];
    double fact, A, B, robar, ubar, vbar, wbar, hbar, cbar, uconbar, eig1, eig2, eig3, term1, term2;
-   double lmat[5][5], rmat[5][5], lmat1[5][5], rmat1[5][5];
-   double area2;
-   static const int idiv[4] = {0, 1, 2, 4};
+   double lmat1[5][5], rmat1[5][5];
    int i, j;
 
-   ql[0] = ql2[0]; ql[1] = ql2[1]; ql[2] = ql2[2]; ql[3] = 0; ql[4] = ql2[3];
-   qr[0] = qr2[0]; qr[1] = qr2[1]; qr[2] = qr2[2]; qr[3] = 0; qr[4] = qr2[3];
-   area2 = sqrt(s[0] * s[0] + s[1] * s[1]);
-   nxd = s[0]; nyd = s[1]; nzd = 0;
+   nxd = nxyz[0]; nyd = nxyz[1]; nzd = nxyz[2];
    area = sqrt(nxd * nxd + nyd * nyd + nzd * nzd);
    nx = nxd / area; ny = nyd / area; nz = nzd / area;
 
@@ -869,6 +864,22 @@ static void roe_jacobian(const double* s, const double* ql2, const double* qr2,
          lmat[i][j] = 0.5 * (lmat1[i][j] - lmat[i][j]);
          rmat[i][j] = 0.5 * (rmat1[i][j] - rmat[i][j]);
       }
+}
+
+/* jacobianRoe2D (jacobianRoe.cpp:9-70): the state embedded in 5 variables
+   with w = 0 and nz = 0, the 3D Jacobian, rows and columns {0,1,2,4} kept,
+   times the face area */
+static void roe_jacobian(const double* s, const double* ql2, const double* qr2,
+                         double* lm2, double* rm2, double gam)
+{
+   double ql[5], qr[5], nxyz[3], lmat[5][5], rmat[5][5], area2;
+   static const int idiv[4] = {0, 1, 2, 4};
+   int i, j;
+   ql[0] = ql2[0]; ql[1] = ql2[1]; ql[2] = ql2[2]; ql[3] = 0; ql[4] = ql2[3];
+   qr[0] = qr2[0]; qr[1] = qr2[1]; qr[2] = qr2[2]; qr[3] = 0; qr[4] = qr2[3];
+   nxyz[0] = s[0]; nxyz[1] = s[1]; nxyz[2] = 0;
+   area2 = sqrt(s[0] * s[0] + s[1] * s[1]);
+   roe_jacobian3d(nxyz, ql, qr, lmat, rmat, gam);
    for (i = 0; i < 4; i++)
       for (j = 0; j < 4; j++) {
          lm2[4 * i + j] = lmat[idiv[i]][idiv[j]] * area2;
@@ -892,6 +903,199 @@ int ho_flux_roe2d(const double* nxy, const double* ql, const double* qr, double*
 void ho_jacobian_roe2d(const double* nxy, const double* ql, const double* qr, double* lm, double* rm, double gamma)
 {
    roe_jacobian(nxy, ql, qr, lm, rm, gamma);
+}
+
+/* SOLVER::fluxRoe3D (interfaceFlux.cpp:176-319) for one face of the 5-variable
+   (3D strand) build: unlike the 2D flux, neither the flux nor the spectral
+   radius is multiplied by the face area */
+void ho_flux_roe3d(const double* nxyz, const double* ql, const double* qr, double* flux, double* spec, double gamma)
+{
+   double gm1 = gamma - 1.0;
+   double nxd = nxyz[0], nyd = nxyz[1], nzd = nxyz[2];
+   double area = sqrt(nxd * nxd + nyd * nyd + nzd * nzd);
+   double invArea = 1. / area;
+   double nx = nxd * invArea, ny = nyd * invArea, nz = nzd * invArea;
+   double rol = ql[0], ul = ql[1] / ql[0], vl = ql[2] / ql[0], wl = ql[3] / ql[0];
+   double pl = gm1 * (ql[4] - 0.5 * rol * (ul * ul + vl * vl + wl * wl));
+   double hl = (ql[4] + pl) / rol;
+   double ror = qr[0], ur = qr[1] / qr[0], vr = qr[2] / qr[0], wr = qr[3] / qr[0];
+   double pr = gm1 * (qr[4] - 0.5 * ror * (ur * ur + vr * vr + wr * wr));
+   double hr = (qr[4] + pr) / ror;
+   double dp = pr - pl;
+   double uconr = ur * nx + vr * ny + wr * nz, uconl = ul * nx + vl * ny + wl * nz;
+   double fact = sqrt(ror / rol);
+   double A = 1.0 / (1.0 + fact), B = fact / (1.0 + fact);
+   double robar = rol * fact;
+   double ubar = ul * A + ur * B, vbar = vl * A + vr * B, wbar = wl * A + wr * B, hbar = hl * A + hr * B;
+   double cbar = gm1 * (hbar - 0.5 * (ubar * ubar + vbar * vbar + wbar * wbar));
+   double uconbar, eig1, eig2, eig3, term1, term2, del1, del2, fm[5], fl[5], fr[5];
+   int i;
+   cbar = sqrt(cbar);
+   uconbar = ubar * nx + vbar * ny + wbar * nz;
+   eig1 = fabs(uconbar);
+   eig2 = fabs(uconbar + cbar);
+   eig3 = fabs(uconbar - cbar);
+   *spec = eig1 + cbar;
+   term1 = -eig1 + 0.5 * (eig2 + eig3);
+   term2 = 0.5 * (eig2 - eig3);
+   del1 = term1 * dp / cbar / cbar + term2 * robar * (uconr - uconl) / cbar;
+   del2 = term1 * (uconr - uconl) * robar + term2 * dp / cbar;
+   for (i = 0; i < 5; i++) fm[i] = eig1 * (qr[i] - ql[i]);
+   fm[0] = fm[0] + del1;
+   fm[1] = fm[1] + del1 * ubar + del2 * nx;
+   fm[2] = fm[2] + del1 * vbar + del2 * ny;
+   fm[3] = fm[3] + del1 * wbar + del2 * nz;
+   fm[4] = fm[4] + del1 * hbar + del2 * uconbar;
+   fl[0] = rol * uconl;                fr[0] = ror * uconr;
+   fl[1] = rol * uconl * ul + nx * pl; fr[1] = ror * uconr * ur + nx * pr;
+   fl[2] = rol * uconl * vl + ny * pl; fr[2] = ror * uconr * vr + ny * pr;
+   fl[3] = rol * uconl * wl + nz * pl; fr[3] = ror * uconr * wr + nz * pr;
+   fl[4] = (ql[4] + pl) * uconl;       fr[4] = (qr[4] + pr) * uconr;
+   for (i = 0; i < 5; i++) flux[i] = 0.5 * (fl[i] + fr[i] - fm[i]);
+}
+
+/* SOLVER::jacobianRoe3D (jacobianRoe.cpp:92-620, IMODE 1): lm, rm [5][5] */
+void ho_jacobian_roe3d(const double* nxyz, const double* ql, const double* qr, double* lm, double* rm, double gamma)
+{
+   double lmat[5][5], rmat[5][5];
+   int i, j;
+   roe_jacobian3d(nxyz, ql, qr, lmat, rmat, gamma);
+   for (i = 0; i < 5; i++)
+      for (j = 0; j < 5; j++) {
+         lm[5 * i + j] = lmat[i][j];
+         rm[5 * i + j] = rmat[i][j];
+      }
+}
+
+/* The 5x5 unpivoted LU with reciprocal pivots of triSolvers.cpp:481-506
+   (blockTridag and blockTridagPeriodic use the same steps) and its solve
+   (:508-518, :523-534) */
+typedef struct { double b11, b21, b22, b31, b32, b33, b41, b42, b43, b44, b51, b52, b53, b54, b55,
+                 u12, u13, u14, u15, u23, u24, u25, u34, u35, u45; } lu5;
+
+static lu5 lu5_factor(double b[5][5])
+{
+   lu5 u;
+   u.b11 = 1. / b[0][0];
+   u.u12 = b[0][1] * u.b11; u.u13 = b[0][2] * u.b11; u.u14 = b[0][3] * u.b11; u.u15 = b[0][4] * u.b11;
+   u.b21 = b[1][0];
+   u.b22 = 1. / (b[1][1] - u.b21 * u.u12);
+   u.u23 = (b[1][2] - u.b21 * u.u13) * u.b22;
+   u.u24 = (b[1][3] - u.b21 * u.u14) * u.b22;
+   u.u25 = (b[1][4] - u.b21 * u.u15) * u.b22;
+   u.b31 = b[2][0];
+   u.b32 = b[2][1] - u.b31 * u.u12;
+   u.b33 = 1. / (b[2][2] - u.b31 * u.u13 - u.b32 * u.u23);
+   u.u34 = (b[2][3] - u.b31 * u.u14 - u.b32 * u.u24) * u.b33;
+   u.u35 = (b[2][4] - u.b31 * u.u15 - u.b32 * u.u25) * u.b33;
+   u.b41 = b[3][0];
+   u.b42 = b[3][1] - u.b41 * u.u12;
+   u.b43 = b[3][2] - u.b41 * u.u13 - u.b42 * u.u23;
+   u.b44 = 1. / (b[3][3] - u.b41 * u.u14 - u.b42 * u.u24 - u.b43 * u.u34);
+   u.u45 = (b[3][4] - u.b41 * u.u15 - u.b42 * u.u25 - u.b43 * u.u35) * u.b44;
+   u.b51 = b[4][0];
+   u.b52 = b[4][1] - u.b51 * u.u12;
+   u.b53 = b[4][2] - u.b51 * u.u13 - u.b52 * u.u23;
+   u.b54 = b[4][3] - u.b51 * u.u14 - u.b52 * u.u24 - u.b53 * u.u34;
+   u.b55 = 1. / (b[4][4] - u.b51 * u.u15 - u.b52 * u.u25 - u.b53 * u.u35 - u.b54 * u.u45);
+   return u;
+}
+
+/* x <- LU^{-1} x for the 5 values x[0], x[s], ..., x[4s] */
+static void lu5_solve(const lu5* u, double* x, int s)
+{
+   double d1 = x[0] * u->b11;
+   double d2 = (x[s] - u->b21 * d1) * u->b22;
+   double d3 = (x[2 * s] - u->b31 * d1 - u->b32 * d2) * u->b33;
+   double d4 = (x[3 * s] - u->b41 * d1 - u->b42 * d2 - u->b43 * d3) * u->b44;
+   double d5 = (x[4 * s] - u->b51 * d1 - u->b52 * d2 - u->b53 * d3 - u->b54 * d4) * u->b55;
+   x[4 * s] = d5;
+   x[3 * s] = d4 - u->u45 * d5;
+   x[2 * s] = d3 - u->u34 * x[3 * s] - u->u35 * d5;
+   x[s] = d2 - u->u23 * x[2 * s] - u->u24 * x[3 * s] - u->u25 * d5;
+   x[0] = d1 - u->u12 * x[s] - u->u13 * x[2 * s] - u->u14 * x[3 * s] - u->u15 * d5;
+}
+
+/* TRISOLVER::blockTridag (triSolvers.cpp:443-536) and blockTridagPeriodic
+   (:540-766), nq = 5, on flat [N][5][5] blocks and [N][5] right-hand sides,
+   in place: a, b, c are overwritten as the reference's scratch */
+int ho_block_tridag5(double* ap, double* bp, double* cp, double* fp, int N, int periodic)
+{
+   double (*a)[5][5] = (double (*)[5][5])ap, (*b)[5][5] = (double (*)[5][5])bp, (*c)[5][5] = (double (*)[5][5])cp;
+   double (*f)[5] = (double (*)[5])fp;
+   double t[5][5];
+   int i, j, k, l;
+   if (N < 1 || (periodic && N < 2)) return -1;
+   for (i = 0; i < N; i++) {
+      lu5 u;
+      if (i != 0) {
+         for (k = 0; k < 5; k++)
+            for (j = 0; j < 5; j++)
+               for (l = 0; l < 5; l++) b[i][k][j] -= a[i][k][l] * c[i - 1][l][j];
+         for (k = 0; k < 5; k++)
+            for (j = 0; j < 5; j++) f[i][k] -= a[i][k][j] * f[i - 1][j];
+         if (periodic) {
+            for (k = 0; k < 5; k++)
+               for (j = 0; j < 5; j++) t[k][j] = 0;
+            for (k = 0; k < 5; k++)
+               for (j = 0; j < 5; j++)
+                  for (l = 0; l < 5; l++) t[k][j] -= a[i][k][l] * a[i - 1][l][j];
+            for (k = 0; k < 5; k++)
+               for (j = 0; j < 5; j++) a[i][k][j] = t[k][j];
+         }
+      }
+      u = lu5_factor(b[i]);
+      lu5_solve(&u, f[i], 1);
+      if (!periodic) {
+         if (i != N - 1)
+            for (j = 0; j < 5; j++) lu5_solve(&u, &c[i][0][j], 5);
+      } else if (i != N - 2) {
+         for (j = 0; j < 5; j++) {
+            lu5_solve(&u, &c[i][0][j], 5);
+            lu5_solve(&u, &a[i][0][j], 5);
+         }
+      } else {
+         for (k = 0; k < 5; k++)
+            for (j = 0; j < 5; j++) c[i][j][k] += a[i][j][k];
+         for (j = 0; j < 5; j++) lu5_solve(&u, &c[i][0][j], 5);
+         for (k = 0; k < 5; k++)
+            for (j = 0; j < 5; j++) a[i][k][j] = c[i][k][j];
+      }
+   }
+   if (!periodic) {
+      for (i = N - 2; i >= 0; i--)
+         for (k = 0; k < 5; k++)
+            for (j = 0; j < 5; j++) f[i][k] -= c[i][k][j] * f[i + 1][j];
+      return 0;
+   }
+   i = N - 1;
+   for (k = 0; k < 5; k++)
+      for (j = 0; j < 5; j++) b[i][j][k] = (j == k) ? 1.0 : 0.0;
+   for (i = 0; i < N - 1; i++) {
+      for (k = 0; k < 5; k++)
+         for (j = 0; j < 5; j++) t[k][j] = 0;
+      for (k = 0; k < 5; k++)
+         for (j = 0; j < 5; j++)
+            for (l = 0; l < 5; l++) {
+               t[k][j] -= c[N - 1][k][l] * c[i][l][j];
+               b[N - 1][k][j] -= c[N - 1][k][l] * a[i][l][j];
+            }
+      for (k = 0; k < 5; k++)
+         for (j = 0; j < 5; j++) f[N - 1][k] -= c[N - 1][k][j] * f[i][j];
+      for (k = 0; k < 5; k++)
+         for (j = 0; j < 5; j++) c[N - 1][k][j] = t[k][j];
+   }
+   {
+      lu5 u = lu5_factor(b[N - 1]);
+      lu5_solve(&u, f[N - 1], 1);
+   }
+   i = N - 2;
+   for (k = 0; k < 5; k++)
+      for (j = 0; j < 5; j++) f[i][k] -= (c[i][k][j] * f[i + 1][j]);
+   for (i = N - 3; i >= 0; i--)
+      for (k = 0; k < 5; k++)
+         for (j = 0; j < 5; j++) f[i][k] -= (c[i][k][j] * f[i + 1][j] + a[i][k][j] * f[N - 1][j]);
+   return 0;
 }
 
 /* RECONSTRUCTION::MUSCL (reconstruction.cpp:16-70) on one line: f, ql, qr,

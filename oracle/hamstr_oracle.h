@@ -108,6 +108,17 @@ void ho_weno_line(const double* f, double* ql, double* qr, int is, int ie, doubl
 void ho_weno_deriv_line(const double* f, double* ql, double* qr, const double* dq, int is, int ie, double eps,
                         int imax, int nq);
 
+/* The 5-variable (3D strand) functions, reachable only from the reference's
+ * -DDim3 build (which does not compile, io.cpp:306) but compiled in every
+ * build: SOLVER::fluxRoe3D (interfaceFlux.cpp:176-319, flux and spectral
+ * radius not scaled by the area), jacobianRoe3D (jacobianRoe.cpp:92-620,
+ * IMODE 1; lm, rm [5][5]) and TRISOLVER::blockTridag / blockTridagPeriodic
+ * (triSolvers.cpp:443-766; a, b, c [N][5][5] and f [N][5] in place, a, b, c
+ * overwritten as the reference's scratch). */
+void ho_flux_roe3d(const double* nxyz, const double* ql, const double* qr, double* flux, double* spec, double gamma);
+void ho_jacobian_roe3d(const double* nxyz, const double* ql, const double* qr, double* lm, double* rm, double gamma);
+int  ho_block_tridag5(double* a, double* b, double* c, double* f, int N, int periodic);
+
 /* Named arrays: q qt r r0 dq sigma ff x vol normVec refMtx (doubles) and
  * faces chainConn faceStartPerChain c2chain bFaces chainsPerColor (ints). */
 int ho_get(const ho_case* c, const char* name, double* out);

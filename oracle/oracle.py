@@ -362,3 +362,50 @@ def recon_line(name: str, f, is_: int, ie: int, *, dq=None, th: float = 1.0 / 3.
     else:
         raise ValueError(name)
     return ql, qr, f2
+
+
+def _face_loop(fn_port, fn_ref, nq: int, nout: int, nxyz, ql, qr, gamma, kind, case):
+    """Calls a per-face function face by face: returns its two outputs."""
+    lib, p = _lib(kind)
+    nxyz, ql, qr = (np.ascontiguousarray(a, dtype=np.float64) for a in (nxyz, ql, qr))
+    n = nxyz.shape[0]
+    fn = getattr(lib, fn_port if kind == "port" else fn_ref)
+    if kind == "port":
+        fn.restype, fn.argtypes = None, [ctypes.c_void_p] * 5 + [ctypes.c_double]
+    else:
+        fn.restype, fn.argtypes = None, [ctypes.c_void_p] * 6 + [ctypes.c_double]
+    o1, o2 = np.zeros((n, nout[0])), np.zeros((n, nout[1]))
+    for k in range(n):
+        s, a, b = np.array(nxyz[k]), np.array(ql[k]), np.array(qr[k])
+        x, y = np.zeros(nout[0]), np.zeros(nout[1])
+        if kind == "port":
+            fn(_ptr(s), _ptr(a), _ptr(b), _ptr(x), _ptr(y), gamma)
+        else:
+            fn(case.h, _ptr(s), _ptr(a), _ptr(b), _ptr(x), _ptr(y), gamma)
+        o1[k], o2[k] = x, y
+    return o1, o2
+
+
+def flux_roe3d(nxyz, ql, qr, gamma: float = 1.4, kind: str = "port", case: "OracleCase" = None):
+    """SOLVER::fluxRoe3D face by face: (flux [n][5], spec [n])."""
+    flux, spec = _face_loop("ho_flux_roe3d", "ref_flux_roe3d", 5, (5, 1), nxyz, ql, qr, gamma, kind, case)
+    return flux, spec[:, 0]
+
+
+def jacobian_roe3d(nxyz, ql, qr, gamma: float = 1.4, kind: str = "port", case: "OracleCase" = None):
+    """SOLVER::jacobianRoe3D face by face: (lmat [n][5][5], rmat [n][5][5])."""
+    lm, rm = _face_loop("ho_jacobian_roe3d", "ref_jacobian_roe3d", 5, (25, 25), nxyz, ql, qr, gamma, kind, case)
+    return lm.reshape(-1, 5, 5), rm.reshape(-1, 5, 5)
+
+
+def block_tridag5(a, b, c, f, periodic: bool, kind: str = "port"):
+    """TRISOLVER::blockTridag / blockTridagPeriodic (nq = 5) on copies of one
+    line: returns (a, b, c, f) after the call (a, b, c are its scratch)."""
+    lib, p = _lib(kind)
+    fn = getattr(lib, p + "block_tridag5")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int]
+    a, b, c, f = (np.array(x, dtype=np.float64, order="C", copy=True) for x in (a, b, c, f))
+    if fn(_ptr(a), _ptr(b), _ptr(c), _ptr(f), int(f.shape[0]), int(periodic)) != 0:
+        raise ValueError("bad block_tridag5 arguments")
+    return a, b, c, f

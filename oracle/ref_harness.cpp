@@ -299,6 +299,42 @@ void ref_jacobian_roe2d(void* h, double* nxy, double* ql, double* qr, double* lm
    ((RefCase*)h)->solv->jacobianRoe2D(nxy, ql, qr, L, R, gamma);
 }
 
+// SOLVER::fluxRoe3D / jacobianRoe3D of the handle's solver on one face
+void ref_flux_roe3d(void* h, double* nxyz, double* ql, double* qr, double* flux, double* spec, double gamma)
+{
+   ((RefCase*)h)->solv->fluxRoe3D(nxyz, ql, qr, flux, spec, gamma);
+}
+
+void ref_jacobian_roe3d(void* h, double* nxyz, double* ql, double* qr, double* lm, double* rm, double gamma)
+{
+   ArenaScope arena;
+   double* L[5] = {lm, lm + 5, lm + 10, lm + 15, lm + 20};
+   double* R[5] = {rm, rm + 5, rm + 10, rm + 15, rm + 20};
+   ((RefCase*)h)->solv->jacobianRoe3D(nxyz, ql, qr, L, R, gamma);
+}
+
+// TRISOLVER::blockTridag / blockTridagPeriodic (nq = 5) on flat [N][5][5] blocks
+int ref_block_tridag5(double* a, double* b, double* c, double* f, int N, int periodic)
+{
+   if (N < 1 || (periodic && N < 2)) return -1;
+   std::vector<double**> A(N), B(N), C(N);
+   std::vector<double*> F(N), rowsA(5 * (size_t)N), rowsB(5 * (size_t)N), rowsC(5 * (size_t)N);
+   for (int i = 0; i < N; i++) {
+      for (int k = 0; k < 5; k++) {
+         rowsA[5 * i + k] = a + 25 * (size_t)i + 5 * k;
+         rowsB[5 * i + k] = b + 25 * (size_t)i + 5 * k;
+         rowsC[5 * i + k] = c + 25 * (size_t)i + 5 * k;
+      }
+      A[i] = &rowsA[5 * i];
+      B[i] = &rowsB[5 * i];
+      C[i] = &rowsC[5 * i];
+      F[i] = f + 5 * (size_t)i;
+   }
+   if (periodic) TRISOLVER::blockTridagPeriodic(A.data(), B.data(), C.data(), F.data(), N, 5);
+   else TRISOLVER::blockTridag(A.data(), B.data(), C.data(), F.data(), N, 5);
+   return 0;
+}
+
 // RECONSTRUCTION::* on one line of flat [imax][nq] arrays (rows views)
 static std::vector<double*> rows(double* p, int imax, int nq)
 {

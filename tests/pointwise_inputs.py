@@ -37,3 +37,33 @@ def lines(nlines: int, imax: int, nq: int, seed: int):
     dq = 1e-3 * rng.standard_normal((nlines, imax, nq))
     prior = rng.standard_normal((3, nlines, imax, nq))
     return f, dq, prior
+
+
+def faces3d(n: int, seed: int):
+    """n faces of the 5-variable (3D) form: normals in every direction with
+    lengths 1e-3..1 and physical states rho, rho u, rho v, rho w, E."""
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((n, 3))
+    v /= np.linalg.norm(v, axis=1)[:, None]
+    nxyz = v * (10.0 ** rng.uniform(-3.0, 0.0, n))[:, None]
+
+    def states():
+        rho = rng.uniform(0.4, 1.6, n)
+        u = rng.uniform(-0.8, 0.8, (n, 3))
+        p = rng.uniform(0.3, 1.3, n)
+        e = p / (GAMMA - 1.0) + 0.5 * rho * (u * u).sum(axis=1)
+        return np.column_stack([rho, rho[:, None] * u, e])
+    ql, qr = states(), states()
+    near = rng.random(n) < 0.25
+    qr[near] = ql[near] * (1.0 + 1e-9 * rng.standard_normal((int(near.sum()), 5)))
+    return nxyz, ql, qr
+
+
+def blocks5(nlines: int, n: int, seed: int, dominance: float = 8.0):
+    """nlines systems of n 5x5 block rows, diagonally dominant."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((nlines, n, 5, 5))
+    b = rng.standard_normal((nlines, n, 5, 5)) + dominance * np.eye(5)
+    c = rng.standard_normal((nlines, n, 5, 5))
+    f = rng.standard_normal((nlines, n, 5))
+    return a, b, c, f

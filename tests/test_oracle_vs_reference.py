@@ -79,3 +79,30 @@ def test_reconstructions_per_line_bitexact(oracle_lib, name, is_, ie_off, qt):
         b = oracle_lib.recon_line(name, f[k], is_, ie, kind="reference", **kw)
         for x, y, what in zip(a, b, ("ql", "qr", "f2")):
             assert np.array_equal(x, y), (name, k, what)
+
+
+def test_flux_and_jacobian_3d_per_face_bitexact(make_case, oracle_lib):
+    """ho_flux_roe3d / ho_jacobian_roe3d against SOLVER::fluxRoe3D /
+    jacobianRoe3D of the reference (5 variables, any normal)."""
+    from pointwise_inputs import faces3d
+    ref = oracle_lib.OracleCase(make_case(16, 4), "reference")
+    nxyz, ql, qr = faces3d(300, 41)
+    f1, s1 = oracle_lib.flux_roe3d(nxyz, ql, qr, kind="port")
+    f2, s2 = oracle_lib.flux_roe3d(nxyz, ql, qr, kind="reference", case=ref)
+    assert np.array_equal(f1, f2) and np.array_equal(s1, s2)
+    l1, r1 = oracle_lib.jacobian_roe3d(nxyz, ql, qr, kind="port")
+    l2, r2 = oracle_lib.jacobian_roe3d(nxyz, ql, qr, kind="reference", case=ref)
+    assert np.array_equal(l1, l2) and np.array_equal(r1, r2)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_block_tridag5_bitexact(oracle_lib, periodic):
+    """ho_block_tridag5 against TRISOLVER::blockTridag / blockTridagPeriodic:
+    the solution and the scratch the reference leaves in a, b and c."""
+    from pointwise_inputs import blocks5
+    a, b, c, f = blocks5(1, 19, 7 + int(periodic))
+    for n in (2, 3, 5, 19):
+        x1 = oracle_lib.block_tridag5(a[0, :n], b[0, :n], c[0, :n], f[0, :n], periodic, "port")
+        x2 = oracle_lib.block_tridag5(a[0, :n], b[0, :n], c[0, :n], f[0, :n], periodic, "reference")
+        for u, v, what in zip(x1, x2, "abcf"):
+            assert np.array_equal(u, v), (n, what)
