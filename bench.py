@@ -55,6 +55,8 @@ WORKLOADS = {
                alpha=1.25, ramp=(), name="naca0012_ogrid_128x32_muscl_minmod_cfl10_msweep2"),
     "c3": dict(ni=1024, nj=256, split=0.3, seed=0, end_rule=1, order=3, limiter=2, CFL=10.0, msweep=2, Mach=0.8,
                alpha=1.25, ramp=((50, 2.0), (50, 5.0)),
+               # the converged leg: both operators to L2 <= tol from the ramped state
+               converge=dict(tol=1e-10, cap=20000),
                name="naca0012_ogrid_1024x256_split30_muscl_vanalbada_m08_cfl10_msweep2"),
 }
 # The batched form: `n` flow conditions (Mach, alpha drawn uniformly from a
@@ -526,12 +528,14 @@ FP64_WARP_INSTR_PER_S = 15.8e9
 # the per-sweep kernels) give the mean of their launches.
 NCU_PER_LAUNCH = {
     "naca0012_ogrid_512x128_split50_weno5_cfl20_msweep2": {
-        "recon5": {"dram_bytes": 154.9e6, "fp64_inst": 2898203},
-        "rhs_face": {"dram_bytes": 16.84e6, "fp64_inst": 2620380},
-        "adi_factor": {"dram_bytes": 54.0e6, "fp64_inst": None},
-        "adi_solve": {"dram_bytes": 24.5e6, "fp64_inst": None},
-        "lin_recon5": {"dram_bytes": 209.3e6, "fp64_inst": 2554292},
-        "lin_face": {"dram_bytes": 55.25e6, "fp64_inst": 328832},
+        "recon5": {"dram_bytes": 155.0e6, "fp64_inst": 2898203},
+        "rhs_face": {"dram_bytes": 16.8e6, "fp64_inst": 2620380},
+        "adi_assemble": {"dram_bytes": 55.1e6, "fp64_inst": 873663},
+        "adi_factor": {"dram_bytes": 55.3e6, "fp64_inst": 1934731},
+        "adi_solve": {"dram_bytes": 24.5e6, "fp64_inst": 416819},
+        "lin_recon5": {"dram_bytes": 209.2e6, "fp64_inst": 2554292},
+        "lin_face": {"dram_bytes": 55.2e6, "fp64_inst": 328832},
+        "lin_cell": {"dram_bytes": 15.6e6, "fp64_inst": 343608},
     },
 }
 
@@ -805,6 +809,7 @@ def run_gpu(args, wl, rank, local_rank, world):
         roofline = roofline_of(dom, prof, lay, sizes, wl, ms / args.steps)
         cpu = cpu_baseline(wl, case_dir, nc, q_timed) if (world == 1 and not args.no_cpu) else None
         conv = target_form() if not args.no_converge else None
+        conv_wl = (converged_errors(wl, case_dir) if (wl.get("converge") and not args.no_converge) else None)
         mixed = {"value": world * nc * args.steps / (mixed_ms * 1e-3), "unit": UNIT,
                  "ms_per_step": mixed_ms / args.steps,
                  "note": "FP64 residual (bit-identical to the reference), FP32 Jacobians, ADI and linear "
@@ -818,6 +823,7 @@ def run_gpu(args, wl, rank, local_rank, world):
             "config": workload_config(wl, sizes, world),
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
             "mixed_precision": mixed, "target_form": conv, "autotune": tune64, "weno_keep_trade": keep_trade,
+            "converged": conv_wl,
             "gpu_launches": gpu.launches_per_step() * args.steps,
             "wall_s_timed_region": wall,
         }
@@ -969,6 +975,45 @@ def target_form() -> dict:
         out["at_1e-10"] = {"solves_per_s": first["batched_fp32_op_warm"]["solves_per_s"],
                            "plain_fp64_solves_per_s": first["plain_fp64"]["solves_per_s"],
                            "max_rel_vs_fp64": first["batched_fp32_op_warm"]["max_rel_vs_plain_fp64"]}
+    return out
+
+
+def converged_errors(wl: dict, case_dir: str) -> dict:
+    """The workload's own mesh and condition to L2 <= tol with the FP64
+    drop-in (the oracle's steps, bit for bit) and with the FP32 operator,
+    from the same ramped state: steps, seconds, and the FP32-operator
+    state's error against the FP64 one in density, pressure and the wall
+    force coefficients."""
+    import numpy as np
+    import torch
+    from hamstr_oop_gb300 import native
+    cv = wl["converge"]
+    out = {"tol": cv["tol"], "cap": cv["cap"], "start": "after the CFL ramp %r" % (list(wl["ramp"]),)}
+    res = {}
+    for label, mixed in (("fp64", False), ("fp32_operator", True)):
+        g = native.GpuSolver(open_case(wl, case_dir))
+        for n, cfl in wl["ramp"]:
+            g.set_cfl(cfl)
+            g.march(n, 0.0)
+        g.set_cfl(wl["CFL"])
+        g.set_precision(mixed)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist, ok = g.march(cv["cap"], cv["tol"])
+        dt = time.perf_counter() - t0
+        res[label] = (g.get("q").reshape(-1, 4), g.forces())
+        out[label] = {"converged": bool(ok), "steps": int(hist.shape[0]), "seconds": dt,
+                      "final_l2": float(hist[-1, 0]), "CL": res[label][1]["CL"], "CD": res[label][1]["CD"]}
+        g.close()
+    (q64, f64), (q32, f32) = res["fp64"], res["fp32_operator"]
+    gm1 = 0.4
+
+    def pres(q):
+        return gm1 * (q[:, 3] - 0.5 * (q[:, 1] ** 2 + q[:, 2] ** 2) / q[:, 0])
+    out["fp32_operator_vs_fp64"] = {
+        "density_max_rel": float(np.max(np.abs(q32[:, 0] - q64[:, 0]) / np.abs(q64[:, 0]))),
+        "pressure_max_rel": float(np.max(np.abs(pres(q32) - pres(q64)) / np.abs(pres(q64)))),
+        "dCL": abs(f32["CL"] - f64["CL"]), "dCD": abs(f32["CD"] - f64["CD"])}
     return out
 
 

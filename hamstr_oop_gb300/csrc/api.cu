@@ -116,6 +116,7 @@ struct hamstr_gpu {
    double* wlin_buf = nullptr;
    int weno_keep = 1;
    int mx_chunk = 1;                    // FP32 solve: rows loaded in chunks where a wave's chains all fit
+   std::vector<int> sp_wave_ptr;        // segmented FP32 solve: spike chains of each wave (host copy)
    bool wlin_valid = false;             // kept values match the current q (standalone entry points)
 
    // instances (a plain handle has one)
@@ -152,9 +153,13 @@ struct hamstr_gpu {
       L("mx_init", n, [&] { launch_mx_init(d, stream); });
       if (!d.mx_fused) L("mx_assemble", n, [&] { launch_mx_assemble(d, stream); });
       L("mx_factor", n, [&] { launch_mx_factor(d, stream); });
+      if (d.sp_on && d.nSpike > 0) L("mx_spike_factor", n, [&] { launch_mx_spike_factor(d, stream); });
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++)
+         for (int w = 0; w < plan.nWave; w++) {
             L("mx_solve", n, [&] { launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream); });
+            const int c0 = sp_wave_ptr[w], cnt = sp_wave_ptr[w + 1] - c0;
+            if (d.sp_on && cnt > 0) L("mx_spike_solve", n, [&] { launch_mx_spike_solve(d, c0, cnt, stream); });
+         }
          L("mx_dq_update", n, [&] { launch_mx_dq_update(d, stream); });
          L("mx_lin_face", n, [&] { launch_mx_lin_face(d, stream); });
          L("mx_lin_cell", n, [&] { launch_mx_lin_cell(d, s == msweep - 1, stream); });
@@ -208,6 +213,43 @@ struct hamstr_gpu {
       if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
+      // long periodic chains take the segmented solve: P segments of about
+      // kSpikeRows rows each (at most kSpikeMaxSeg), grouped by wave
+      {
+         std::vector<int> chain_spike(std::max(plan.nChain, 1), -1), sp_chain, sp_seg, sp_nseg, sp_rec0;
+         sp_wave_ptr.assign(plan.nWave + 1, 0);
+         int rows = 0;
+         for (int w = 0; w < plan.nWave; w++) {
+            for (int k = plan.wave_ptr[w]; k < plan.wave_ptr[w + 1]; k++) {
+               const int c = plan.wave_chains[k];
+               const int n = plan.chain_nrows[c];
+               if (!plan.chain_periodic[c] || n < kSpikeMinRows) continue;
+               const int P = std::min(kSpikeMaxSeg, n / kSpikeRows);
+               chain_spike[c] = (int)sp_chain.size();
+               sp_chain.push_back(c);
+               sp_nseg.push_back(P);
+               sp_rec0.push_back(rows);
+               for (int p = 0; p <= kSpikeMaxSeg; p++) sp_seg.push_back(p <= P ? (int)((long long)p * n / P) : n);
+               rows += n;
+            }
+            sp_wave_ptr[w + 1] = (int)sp_chain.size();
+         }
+         d.nSpike = (int)sp_chain.size();
+         if (sp_chain.empty()) {
+            sp_chain.push_back(0);
+            sp_nseg.push_back(0);
+            sp_rec0.push_back(0);
+            sp_seg.assign(kSpikeMaxSeg + 1, 0);
+         }
+         if ((st = upload(&d.chain_spike, chain_spike, owned))) return st;
+         if ((st = upload(&d.sp_chain, sp_chain, owned))) return st;
+         if ((st = upload(&d.sp_seg, sp_seg, owned))) return st;
+         if ((st = upload(&d.sp_nseg, sp_nseg, owned))) return st;
+         if ((st = upload(&d.sp_rec0, sp_rec0, owned))) return st;
+         if ((st = dalloc(&d.sp_fac, 80 * (size_t)std::max(rows, 1), owned))) return st;
+         if ((st = dalloc(&d.sp_y, 4 * (size_t)std::max(rows, 1), owned))) return st;
+         if ((st = dalloc(&d.sp_red, (size_t)kSpikeRedStride * std::max(d.nSpike, 1), owned))) return st;
+      }
       CK(cudaMemsetAsync(d.ff32, 0, 32 * (size_t)d.nSlot * sizeof(float), stream));
       CK(cudaMemsetAsync(d.dq32, 0, 4 * nc * sizeof(float), stream));
       return HAMSTR_GPU_OK;
@@ -282,8 +324,9 @@ struct hamstr_gpu {
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int lanes,
-                   int wkeep, int bundle, int chunk)
+                   int wkeep, int bundle, int chunk, int spike)
    {
+      d.sp_on = spike;
       if (wkeep && d.recon == 5) {
          const int st = ensure_wlin();
          if (st) return st;
@@ -585,6 +628,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.adi_wpb = 4;
       d.mx_block = 64;
       d.mx_chunk_chains = mx_solve_chunk_capacity(d.mx_block);
+      d.sp_on = 1;   // long periodic chains of the FP32 form by segments
       // FP32 assembly inside the factorisation pays off on long chains, as
       // do the hardware pivot divisions (their latency is shorter per row)
       d.mx_fused = (P.nChain > 0 && P.nRow >= 16 * P.nChain) ? 1 : 0;
@@ -1110,7 +1154,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
    struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle; float ms; };
-   const int wk = g->weno_keep, ck = g->mx_chunk;
+   const int wk = g->weno_keep, ck = g->mx_chunk, spk = d.sp_on;
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
@@ -1136,7 +1180,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, spk))) break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1158,7 +1202,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
-                       best->bundle, ck);
+                       best->bundle, ck, spk);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1188,7 +1232,8 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    if (!g || !shape) return HAMSTR_GPU_ERR_ARG;
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
-                                  d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle, g->mx_chunk};
+                                  d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle, g->mx_chunk,
+                                  d.sp_on};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1200,12 +1245,13 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
    const bool ok = (s[0] == 128 || s[0] == 256) && (s[1] == 4 || s[1] == 8) &&
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
-                   (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1);
+                   (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1) &&
+                   (s[10] == 0 || s[10] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], s[10]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

@@ -38,6 +38,15 @@ struct FlowConst {
 
 constexpr int kWlinPerSlot = 2 * 4 * 18;   // sides x components x values (recon.cuh Weno5Lin)
 
+// FP32 form, segmented solve of long periodic chains: chains of at least
+// kSpikeMinRows rows, kSpikeRows rows per segment (at most kSpikeMaxSeg
+// segments, one warp lane each), kSpikeRedStride floats of boundary-system
+// factors per chain
+constexpr int kSpikeMinRows = 64;
+constexpr int kSpikeRows = 16;
+constexpr int kSpikeMaxSeg = 32;
+constexpr int kSpikeRedStride = 256 * kSpikeMaxSeg;
+
 struct DeviceState {
    int nCell, nFace, nSlot, nSten, nRow, nChain, order, nGhost;
    int recon;              // reconstruction code: order, or 31/32 for MUSCL with a project limiter (recon.cuh)
@@ -121,6 +130,24 @@ struct DeviceState {
    float *r32, *r032, *dq32;   // [nCell][4]
    float* g32;             // [nSlot][4] linear face fluxes
    int* line_chains;       // chains of each wave, longest first (thread per chain)
+
+   // FP32 form: long periodic chains solved by segments (spike.cuh).  A
+   // chain of N >= kSpikeMinRows rows is cut into P segments, one warp lane
+   // each; each lane factors its segment and the two "spikes" (its local
+   // responses to the couplings across its ends), and a small cyclic system
+   // on the segment boundaries joins them.  Same linear system as the
+   // sequential cyclic block Thomas, about N/P rows of latency instead of N.
+   int sp_on;              // 1: long periodic chains take the segmented solve (shape key)
+   int nSpike;             // chains solved by segments
+   int* chain_spike;       // [nChain] index into the sp_* arrays, or -1
+   int* sp_chain;          // [nSpike] chain id
+   int* sp_wave_ptr;       // [nWave+1] spike chains of each wave: sp indices sp_wave_ptr[w] .. [w+1]-1
+   int* sp_seg;            // [nSpike][kSpikeMaxSeg+1] first row (in the chain) of each segment, then N
+   int* sp_nseg;           // [nSpike] P
+   int* sp_rec0;           // [nSpike] first record of the chain in sp_fac / sp_y
+   float* sp_fac;          // [spike rows][80]: A, LU(B'), C' (local), V (right spike), W (left spike)
+   float* sp_y;            // [spike rows][4]: the sweep's local solutions
+   float* sp_red;          // [nSpike][kSpikeRedStride]: factors of the boundary system
 };
 
 // true once a march has met its tolerance: every later kernel of the step
@@ -192,6 +219,10 @@ int mx_solve_chunk_capacity(int block);
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
+// segmented solve of the long periodic chains (d.nSpike > 0 and d.sp_on):
+// factorisation once per step, the solve of wave w's chains per sweep
+void launch_mx_spike_factor(const DeviceState& d, cudaStream_t st);
+void launch_mx_spike_solve(const DeviceState& d, int first, int count, cudaStream_t st);
 void launch_adi_assemble(const DeviceState& d, cudaStream_t st);
 // nwarps persistent warps over the schedule's job queue (nwarps may be 0);
 // the solve of wave `wave` in sweep `sweep` takes counter 1 + sweep*nWave + wave

@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
    const int ich = d.line_chains[t];
-   if (frozen_chain(d, ich)) return;
+   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = t & 31, s0 = d.grp_row0[t >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    float A[16], B[16], C[16], cp[16], ap[16];
@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    if (t >= count || halted(d)) return;
    const int p = first + t;
    const int ich = d.line_chains[p];
-   if (frozen_chain(d, ich)) return;
+   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    const int* fcell = d.row_fcell + row0;
@@ -616,7 +616,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
    if (t >= count || halted(d)) return;
    const int p = first + t;
    const int ich = d.line_chains[p];
-   if (frozen_chain(d, ich)) return;
+   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    const int* fcell = d.row_fcell + row0;
@@ -763,6 +763,386 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
                for (int k = 0; k < 4; k++) xn[k] = x[k];
             }
          }
+      }
+   }
+}
+
+// ---------------- long periodic chains by segments ----------------------
+// A periodic chain of N rows (A_i x_{i-1} + B_i x_i + C_i x_{i+1} = f_i,
+// indices mod N) is cut into P segments of about N/P rows, one lane of a
+// warp each.  With D_p the block-tridiagonal matrix of segment p alone
+// (rows s..e), its solution is
+//     x_i = y_i + V_i x_{e+1} + W_i x_{s-1},
+// where D_p y = f, D_p V = -C_e (in the last row) and D_p W = -A_s (in the
+// first row): V and W are the "spikes", the segment's responses to the
+// couplings across its two ends.  With b_p = x_e and t_p = x_s of segment
+// p, the rows at the segment ends give a cyclic system in the interface
+// pairs Z_p = (b_p, t_{p+1}):
+//     b_p     - V_e(p) t_{p+1} - W_e(p) b_{p-1}   = y_e(p)
+//     t_{p+1} - V_s(p+1) t_{p+2} - W_s(p+1) b_p   = y_s(p+1)
+// i.e. L_p Z_{p-1} + D_p Z_p + U_p Z_{p+1} = R_p with 8x8 blocks, which
+// lane 0 solves by a cyclic block elimination onto Z_{P-1}.  This is the
+// same linear system the sequential cyclic block Thomas solves (in FP32 it
+// differs in rounding only), with N/P + P rows of latency instead of N.
+// The segment factors and spikes, and the boundary system's factors, are
+// formed once per step; each sweep replays the right-hand side.
+
+// sp_fac record of one row: A, LU of the segment's B', C' (no C' on a
+// segment's last row), V, W
+constexpr int kSpRec = 80;
+
+// 8x8 row-major matrices of the boundary system (lane 0, local arrays)
+// LU with reciprocal pivots: M = L U, U unit upper; L below and on the
+// diagonal (the diagonal holding 1/L_kk)
+__device__ void m8_lu(float* M)
+{
+   for (int k = 0; k < 8; k++) {
+      const float piv = 1.f / M[9 * k];
+      M[9 * k] = piv;
+      for (int j = k + 1; j < 8; j++) M[8 * k + j] *= piv;
+      for (int i = k + 1; i < 8; i++) {
+         const float l = M[8 * i + k];
+         for (int j = k + 1; j < 8; j++) M[8 * i + j] = __fmaf_rn(-l, M[8 * k + j], M[8 * i + j]);
+      }
+   }
+}
+
+// x <- M^{-1} x for the 8 values x[0], x[s], .., x[7s]
+__device__ void m8_solve(const float* LU, float* x, int s)
+{
+   for (int i = 0; i < 8; i++) {
+      float v = x[s * i];
+      for (int k = 0; k < i; k++) v = __fmaf_rn(-LU[8 * i + k], x[s * k], v);
+      x[s * i] = v * LU[9 * i];
+   }
+   for (int i = 6; i >= 0; i--) {
+      float v = x[s * i];
+      for (int j = i + 1; j < 8; j++) v = __fmaf_rn(-LU[8 * i + j], x[s * j], v);
+      x[s * i] = v;
+   }
+}
+
+// C = alpha C - A B (alpha 0 or 1)
+__device__ void m8_msub(float* C, const float* A, const float* B, bool keep)
+{
+   for (int i = 0; i < 8; i++)
+      for (int j = 0; j < 8; j++) {
+         float v = keep ? C[8 * i + j] : 0.f;
+         for (int k = 0; k < 8; k++) v = __fmaf_rn(-A[8 * i + k], B[8 * k + j], v);
+         C[8 * i + j] = v;
+      }
+}
+
+// y = alpha y - M x on 8-vectors
+__device__ __forceinline__ void v8_msub(float* y, const float* M, const float* x)
+{
+   for (int i = 0; i < 8; i++) {
+      float v = y[i];
+      for (int k = 0; k < 8; k++) v = __fmaf_rn(-M[8 * i + k], x[k], v);
+      y[i] = v;
+   }
+}
+
+__device__ __forceinline__ void ldm8(const float* __restrict__ p, float* m)
+{
+   for (int e = 0; e < 64; e += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(p + e);
+      m[e] = v.x; m[e + 1] = v.y; m[e + 2] = v.z; m[e + 3] = v.w;
+   }
+}
+
+__device__ __forceinline__ void stm8(float* __restrict__ p, const float* m)
+{
+   for (int e = 0; e < 64; e += 4) *reinterpret_cast<float4*>(p + e) = make_float4(m[e], m[e + 1], m[e + 2], m[e + 3]);
+}
+
+// the blocks of row p of the boundary system from the segments' spike tips
+// (sh: [p][4][16] = V_s, W_s, V_e, W_e of segment p)
+__device__ void red_blocks(const float* sh, int p, int P, float* L, float* D, float* U)
+{
+   const int q = (p + 1 == P) ? 0 : p + 1;
+   const float* Vs1 = sh + 64 * q;
+   const float* Ws1 = sh + 64 * q + 16;
+   const float* Ve = sh + 64 * p + 32;
+   const float* We = sh + 64 * p + 48;
+   for (int e = 0; e < 64; e++) { L[e] = 0.f; D[e] = 0.f; U[e] = 0.f; }
+   for (int k = 0; k < 4; k++)
+      for (int j = 0; j < 4; j++) {
+         L[8 * k + j] = -We[4 * k + j];
+         D[8 * k + 4 + j] = -Ve[4 * k + j];
+         D[8 * (4 + k) + j] = -Ws1[4 * k + j];
+         U[8 * (4 + k) + 4 + j] = -Vs1[4 * k + j];
+      }
+   for (int k = 0; k < 8; k++) D[9 * k] = 1.f;
+}
+
+// sp_red layout of one chain: row p < P-1 at 256 p: LU(M_p), L_p, G_p, B_p;
+// then LU(K), L_{P-1}, U_{P-1} at 256 (kSpikeMaxSeg - 1)
+__device__ __forceinline__ float* red_row(float* red, int p, int m) { return red + 256 * p + 64 * m; }
+__device__ __forceinline__ const float* red_row(const float* red, int p, int m) { return red + 256 * p + 64 * m; }
+
+__global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
+{
+   __shared__ float tips[kSpikeMaxSeg * 64];
+   const int sp = blockIdx.x, lane = threadIdx.x;
+   const int ich = d.sp_chain[sp];
+   if (halted(d) || frozen_chain(d, ich)) return;
+   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], rec0 = d.sp_rec0[sp];
+   bool bad = false;
+   if (lane < P) {
+      const int s = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane], e = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane + 1] - 1;
+      float cp[16], gw[16];
+      for (int i = s; i <= e; i++) {
+         float A[16], B[16], C[16];
+         mx_row_ref(d, mx_rowref(d, row0 + i), A, B, C);
+         float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
+         st16f(rec, A);
+         if (i > s) mm_sub(A, cp, B);
+         const LUf u = luf_factor(B);
+         luf_store(rec + 16, u);
+         bad |= nonfinite(u.p0) || nonfinite(u.p1) || nonfinite(u.p2) || nonfinite(u.p3);
+         // left spike, forward: g_s = B'^{-1}(-A_s), g_i = B'^{-1}(-A_i g_{i-1})
+         float w[16];
+         if (i == s) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) w[m] = -A[m];
+         } else {
+#pragma unroll
+            for (int m = 0; m < 16; m++) w[m] = 0.f;
+            mm_sub(A, gw, w);
+         }
+         luf_cols(u, w);
+         st16f(rec + 64, w);
+#pragma unroll
+         for (int m = 0; m < 16; m++) gw[m] = w[m];
+         if (i < e) {
+            luf_cols(u, C);
+            st16f(rec + 32, C);
+#pragma unroll
+            for (int m = 0; m < 16; m++) cp[m] = C[m];
+         } else {
+            // right spike at the last row: B'^{-1}(-C_e)
+#pragma unroll
+            for (int m = 0; m < 16; m++) C[m] = -C[m];
+            luf_cols(u, C);
+            st16f(rec + 48, C);
+         }
+      }
+      // back substitution of both spikes: V_i = -C'_i V_{i+1},
+      // W_i = g_i - C'_i W_{i+1}
+      float vn[16], wn[16];
+      ld16f(d.sp_fac + (size_t)kSpRec * (rec0 + e) + 48, vn);
+      ld16f(d.sp_fac + (size_t)kSpRec * (rec0 + e) + 64, wn);
+      float* tip = tips + 64 * lane;
+      st16f(tip + 32, vn);      // V_e
+      st16f(tip + 48, wn);      // W_e
+      for (int i = e - 1; i >= s; i--) {
+         float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
+         float c[16], v[16], w[16];
+         ld16f(rec + 32, c);
+         ld16f(rec + 64, w);
+#pragma unroll
+         for (int m = 0; m < 16; m++) v[m] = 0.f;
+         mm_sub(c, vn, v);
+         mm_sub(c, wn, w);
+         st16f(rec + 48, v);
+         st16f(rec + 64, w);
+#pragma unroll
+         for (int m = 0; m < 16; m++) { vn[m] = v[m]; wn[m] = w[m]; }
+      }
+      st16f(tip, vn);           // V_s
+      st16f(tip + 16, wn);      // W_s
+   }
+   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
+   __syncwarp();
+   if (lane != 0) return;
+   // boundary system: M_0 = D_0, M_p = D_p - L_p G_{p-1}; G_p = M_p^{-1} U_p;
+   // H_0 = M_0^{-1} L_0, H_p = -M_p^{-1} L_p H_{p-1}; at p = P-2 the
+   // coupling U_{P-2} goes to Z_{P-1} itself
+   float* red = d.sp_red + (size_t)kSpikeRedStride * sp;
+   float L[64], D[64], U[64], G[64], H[64], T[64];
+   for (int p = 0; p <= P - 2; p++) {
+      red_blocks(tips, p, P, L, D, U);
+      if (p > 0) m8_msub(D, L, G, true);                   // M_p = D_p - L_p G_{p-1}
+      m8_lu(D);
+      stm8(red_row(red, p, 0), D);
+      stm8(red_row(red, p, 1), L);
+      for (int j = 0; j < 8; j++) m8_solve(D, U + j, 8);   // G_p = M_p^{-1} U_p
+      if (p == 0) {
+         for (int e = 0; e < 64; e++) H[e] = L[e];
+      } else {
+         m8_msub(T, L, H, false);                            // T = -L_p H_{p-1}
+         for (int e = 0; e < 64; e++) H[e] = T[e];
+      }
+      for (int j = 0; j < 8; j++) m8_solve(D, H + j, 8);
+      for (int e = 0; e < 64; e++) G[e] = U[e];
+      stm8(red_row(red, p, 2), G);
+      stm8(red_row(red, p, 3), H);                           // H_p, turned into B_p below
+   }
+   // Z_p = a_p + B_p Z_{P-1}: B_{P-2} = -(G_{P-2} + H_{P-2}),
+   // B_p = -G_p B_{p+1} - H_p
+   float Bn[64];
+   ldm8(red_row(red, P - 2, 3), H);
+   for (int e = 0; e < 64; e++) Bn[e] = -(G[e] + H[e]);
+   stm8(red_row(red, P - 2, 3), Bn);
+   float B0[64];
+   for (int e = 0; e < 64; e++) B0[e] = Bn[e];
+   for (int p = P - 3; p >= 0; p--) {
+      ldm8(red_row(red, p, 2), G);
+      ldm8(red_row(red, p, 3), H);
+      for (int e = 0; e < 64; e++) T[e] = -H[e];
+      m8_msub(T, G, Bn, true);
+      stm8(red_row(red, p, 3), T);
+      for (int e = 0; e < 64; e++) Bn[e] = T[e];
+      if (p == 0)
+         for (int e = 0; e < 64; e++) B0[e] = T[e];
+   }
+   // K = D_{P-1} + L_{P-1} B_{P-2} + U_{P-1} B_0
+   red_blocks(tips, P - 1, P, L, D, U);
+   ldm8(red_row(red, P - 2, 3), Bn);
+   for (int e = 0; e < 64; e++) { L[e] = -L[e]; U[e] = -U[e]; }
+   m8_msub(D, L, Bn, true);
+   m8_msub(D, U, B0, true);
+   for (int e = 0; e < 64; e++) { L[e] = -L[e]; U[e] = -U[e]; }
+   m8_lu(D);
+   float* last = red + 256 * (kSpikeMaxSeg - 1);
+   stm8(last, D);
+   stm8(last + 64, L);
+   stm8(last + 128, U);
+   bool kbad = false;
+   for (int k = 0; k < 8; k++) kbad |= nonfinite(D[9 * k]);
+   if (kbad) atomicOr(d.status, DEV_ERR_PIVOT);
+}
+
+// one sweep's solve of the spike chains sp = first .. first+count-1 of a
+// wave: right-hand sides r32[fcell], solutions into r32[scell]
+__global__ void __launch_bounds__(32) mx_spike_solve_kernel(DeviceState d, int first)
+{
+   __shared__ float ry[kSpikeMaxSeg * 8];   // per segment: y_s then y_e
+   __shared__ float zs[kSpikeMaxSeg * 8];   // Z_p = (b_p, t_{p+1})
+   const int sp = first + blockIdx.x, lane = threadIdx.x;
+   const int ich = d.sp_chain[sp];
+   if (halted(d) || frozen_chain(d, ich)) return;
+   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], rec0 = d.sp_rec0[sp];
+   int s = 0, e = -1;
+   if (lane < P) {
+      s = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane];
+      e = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane + 1] - 1;
+      // y' forward: y'_i = B'^{-1}(f_i - A_i y'_{i-1})
+      float yp[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int i = s; i <= e; i++) {
+         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
+         const int fc = d.row_fcell[row0 + i];
+         float x[4] = {0.f, 0.f, 0.f, 0.f};
+         if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, x);
+         if (i > s) {
+            float a[16];
+            ld16f(rec, a);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+#pragma unroll
+               for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-a[4 * k + j], yp[j], x[k]);
+         }
+         luf_solve(luf_load(rec + 16), x[0], x[1], x[2], x[3]);
+         st4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+#pragma unroll
+         for (int k = 0; k < 4; k++) yp[k] = x[k];
+      }
+      // back: y_i = y'_i - C'_i y_{i+1}
+#pragma unroll
+      for (int k = 0; k < 4; k++) ry[8 * lane + 4 + k] = yp[k];
+      for (int i = e - 1; i >= s; i--) {
+         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
+         float c[16], x[4];
+         ld16f(rec + 32, c);
+         ld4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-c[4 * k + j], yp[j], x[k]);
+         st4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+#pragma unroll
+         for (int k = 0; k < 4; k++) yp[k] = x[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) ry[8 * lane + k] = yp[k];
+   }
+   __syncwarp();
+   if (lane == 0) {
+      // R_p = (y_e(p), y_s(p+1)); g_p = M_p^{-1}(R_p - L_p g_{p-1});
+      // a_{P-2} = g_{P-2}, a_p = g_p - G_p a_{p+1};
+      // Z_{P-1} = K^{-1}(R_{P-1} - L_{P-1} a_{P-2} - U_{P-1} a_0);
+      // Z_p = a_p + B_p Z_{P-1}
+      const float* red = d.sp_red + (size_t)kSpikeRedStride * sp;
+      float M[64], g[8];
+      for (int p = 0; p <= P - 2; p++) {
+         for (int k = 0; k < 4; k++) {
+            g[k] = ry[8 * p + 4 + k];
+            g[4 + k] = ry[8 * (p + 1) + k];
+         }
+         if (p > 0) {
+            float prev[8];
+            for (int k = 0; k < 8; k++) prev[k] = zs[8 * (p - 1) + k];
+            ldm8(red_row(red, p, 1), M);
+            v8_msub(g, M, prev);
+         }
+         ldm8(red_row(red, p, 0), M);
+         m8_solve(M, g, 1);
+         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+      }
+      for (int p = P - 3; p >= 0; p--) {
+         float nx[8];
+         for (int k = 0; k < 8; k++) { g[k] = zs[8 * p + k]; nx[k] = zs[8 * (p + 1) + k]; }
+         ldm8(red_row(red, p, 2), M);
+         v8_msub(g, M, nx);
+         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+      }
+      const float* last = red + 256 * (kSpikeMaxSeg - 1);
+      float z[8], a0[8], ap[8];
+      for (int k = 0; k < 4; k++) {
+         z[k] = ry[8 * (P - 1) + 4 + k];
+         z[4 + k] = ry[k];
+      }
+      for (int k = 0; k < 8; k++) { ap[k] = zs[8 * (P - 2) + k]; a0[k] = zs[k]; }
+      ldm8(last + 64, M);
+      v8_msub(z, M, ap);
+      ldm8(last + 128, M);
+      v8_msub(z, M, a0);
+      ldm8(last, M);
+      m8_solve(M, z, 1);
+      for (int p = 0; p <= P - 2; p++) {
+         for (int k = 0; k < 8; k++) g[k] = zs[8 * p + k];
+         ldm8(red_row(red, p, 3), M);
+         for (int i = 0; i < 8; i++) {
+            float v = g[i];
+            for (int k = 0; k < 8; k++) v = __fmaf_rn(M[8 * i + k], z[k], v);
+            g[i] = v;
+         }
+         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+      }
+      for (int k = 0; k < 8; k++) zs[8 * (P - 1) + k] = z[k];
+   }
+   __syncwarp();
+   if (lane < P) {
+      // x_i = y_i + V_i t_{p+1} + W_i b_{p-1}
+      float tn[4], bp[4];
+      const int pm = (lane == 0) ? P - 1 : lane - 1;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+         tn[k] = zs[8 * lane + 4 + k];
+         bp[k] = zs[8 * pm + k];
+      }
+      for (int i = s; i <= e; i++) {
+         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
+         float v[16], w[16], x[4];
+         ld16f(rec + 48, v);
+         ld16f(rec + 64, w);
+         ld4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+#pragma unroll
+         for (int k = 0; k < 4; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(v[4 * k + j], tn[j], __fmaf_rn(w[4 * k + j], bp[j], x[k]));
+         st4(d.r32 + 4 * (size_t)d.row_scell[row0 + i], x);
       }
    }
 }
@@ -941,6 +1321,16 @@ int mx_solve_chunk_capacity(int block)
    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_solve_chunk_kernel, block, 0) != cudaSuccess)
       return 0;
    return sms * per_sm * block;
+}
+
+void launch_mx_spike_factor(const DeviceState& d, cudaStream_t st)
+{
+   if (d.sp_on && d.nSpike > 0) mx_spike_factor_kernel<<<d.nSpike, 32, 0, st>>>(d);
+}
+
+void launch_mx_spike_solve(const DeviceState& d, int first, int count, cudaStream_t st)
+{
+   if (d.sp_on && count > 0) mx_spike_solve_kernel<<<count, 32, 0, st>>>(d, first);
 }
 
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st)

@@ -242,9 +242,16 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       the solve, 2 in the periodic elimination), where the launch's chains
  *       are all resident at once with the larger register count this takes:
  *       0 or 1 (default 1; not tuned)
- * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); results do
- * not depend on the shape. */
-#define HAMSTR_SHAPE_N 10
+ *  [10] FP32 line kernels: periodic chains of 64 rows or more solved by
+ *       segments (16 rows each, up to 32, one warp lane per segment, joined
+ *       by a small cyclic system on the segment ends) instead of one thread
+ *       running the whole cyclic recurrence: 0 or 1 (default 1; not tuned).
+ *       The same linear system; in FP32 the rounding differs, so the FP32
+ *       form's iterates differ in the last bits and its steady state (the
+ *       FP64 residual's zero) does not.
+ * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); FP64
+ * results do not depend on the shape. */
+#define HAMSTR_SHAPE_N 11
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

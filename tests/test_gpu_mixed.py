@@ -82,3 +82,54 @@ def test_chunked_fp32_solve_matches_row_by_row(make_case, native_lib, split, ord
         ha, _ = a.march(4, 0.0)
         hb, _ = b.march(4, 0.0)
         assert np.array_equal(ha, hb) and np.array_equal(a.get("q"), b.get("q")), fused
+
+
+def _spike_pair(make_case, ni, nj, **inputs):
+    """Two FP32-operator handles on one case: periodic loops by segments
+    (shape key mx_spike, the default) and by one thread each."""
+    from hamstr_oop_gb300 import native
+    case = make_case(ni, nj, **inputs)
+    a, b = native.GpuSolver(native.Case(case)), native.GpuSolver(native.Case(case))
+    for g in (a, b):
+        g.set_precision(True)
+    assert a.shape()["mx_spike"] == 1
+    b.set_shape(mx_spike=0)
+    return case, a, b
+
+
+@pytest.mark.parametrize("ni,order", [(64, 1), (128, 3), (384, 1)])
+def test_segmented_periodic_solve_is_the_same_linear_solve(make_case, native_lib, ni, order):
+    """One step of the FP32 operator with the long periodic loops solved by
+    segments (4, 8 and 24 of them here) against the sequential cyclic solve:
+    the same linear system, so the increments agree to FP32 rounding."""
+    case, a, b = _spike_pair(make_case, ni, 8, order=order, CFL=10.0, msweep=2)
+    rng = np.random.default_rng(ni)
+    q0 = a.get("q").reshape(-1, 4)
+    q0 = (q0 * (1.0 + 0.01 * rng.standard_normal(q0.shape))).ravel()
+    for g in (a, b):
+        g.set("q", q0)
+        g.step()
+    da, db = a.get("q") - q0, b.get("q") - q0
+    assert np.all(np.isfinite(da))
+    err = np.max(np.abs(da - db)) / np.max(np.abs(db))
+    assert err < 1e-4, err
+
+
+def test_segmented_periodic_solve_converges_to_the_oracle(make_case, oracle_lib, native_lib):
+    """With 64-row loops in segments the FP32 form reaches L2 <= 1e-10 in
+    as many steps as the sequential form, at the same state, and that state
+    is the FP64 oracle's to 1e-8."""
+    case, a, b = _spike_pair(make_case, 64, 16, order=1, CFL=10.0, msweep=2)
+    ha, ca = a.march(4000, 1e-10)
+    hb, cb = b.march(4000, 1e-10)
+    assert ca and cb
+    assert abs(ha.shape[0] - hb.shape[0]) <= 2, (ha.shape[0], hb.shape[0])
+    qa, qb = a.get("q"), b.get("q")
+    assert np.max(np.abs(qa - qb)) <= 1e-8 * np.max(np.abs(qb))
+    orc = oracle_lib.OracleCase(case, "port")
+    ho = orc.march(4000)
+    k = int(np.argmax(ho[:, 0] <= 1e-10))
+    orc2 = oracle_lib.OracleCase(case, "port")
+    orc2.march(k)
+    qo = orc2.get("q")
+    assert np.max(np.abs(qa - qo)) / np.max(np.abs(qo)) <= FIELD_RTOL
