@@ -1153,21 +1153,28 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // candidates for the current precision: face-kernel block size, and the
    // line kernels' shape (FP64: warps per SM of the persistent warp-per-chain
    // kernels; FP32: threads per block of the thread-per-chain kernels)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle; float ms; };
-   const int wk = g->weno_keep, ck = g->mx_chunk, spk = d.sp_on;
+   // (FP32 form with long periodic chains: also their segmented solve or
+   // not -- it shortens each chain's latency but does several times the
+   // work, which loses where the chains alone fill the GPU)
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle, spike; float ms; };
+   const int wk = g->weno_keep, ck = g->mx_chunk;
+   std::vector<int> spikes = {d.sp_on};
+   if (g->mixed && d.nSpike > 0) spikes = {0, 1};
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
          if (g->mixed) {
             for (int fused : {0, 1})
                for (int mb : {32, 64, 128})
-                  cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_lanes, g->adi_bundle, 0.f});
+                  for (int sp : spikes)
+                     cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_lanes, g->adi_bundle, sp,
+                                      0.f});
          } else {
             for (int w : {4, 8})
                for (int psoft : {0, 1})
                   for (int ln : {16, 4})
                      for (int bu : {0, 4, 8, 16})
-                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, ln, bu, 0.f});
+                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, ln, bu, d.sp_on, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1180,7 +1187,8 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, spk))) break;
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, c.spike)))
+         break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
       CK(cudaGraphLaunch(g->step_exec, g->stream));   // warm-up
@@ -1202,25 +1210,27 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
-                       best->bundle, ck, spk);
+                       best->bundle, ck, best->spike);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
       for (size_t i = 0; i < cands.size(); i++) {
-         char buf[256];
+         char buf[320];
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
                        "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d, "
-                       "\"ms\": %.4f}",
+                       "\"mx_spike\": %d, \"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].lanes, cands[i].bundle, cands[i].ms);
+                       cands[i].psoft, cands[i].lanes, cands[i].bundle, cands[i].spike, cands[i].ms);
          r += buf;
       }
-      char buf[256];
+      char buf[320];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
-                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d}}",
-                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, best->bundle);
+                    "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d, "
+                    "\"mx_spike\": %d}}",
+                    best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, best->bundle,
+                    best->spike);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }

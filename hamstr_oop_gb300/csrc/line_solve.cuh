@@ -301,17 +301,23 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
    double xnext[4];
 #pragma unroll
    for (int m = 0; m < 4; m++) xnext[m] = xprev[m];
-   double mv = 0.0, xi = 0.0;
+   // a row here is a few dependent operations, shorter than a load: rows
+   // ii-1 and ii-2 are in flight while row ii is solved
+   double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
    if (N >= 2) {
       mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
       xi = fs[4 * (N - 2) + r];
    }
+   if (N >= 3) {
+      mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
+      xi1 = fs[4 * (N - 3) + r];
+   }
    for (int t = 0; t <= Nmax - 2; t++) {
       const int ii = N - 2 - t;
-      double mvn = 0.0, xin = 0.0;
-      if (ii > 0) {
-         mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + e];
-         xin = fs[4 * (ii - 1) + r];
+      double mv2 = 0.0, xi2 = 0.0;
+      if (ii > 1) {
+         mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
+         xi2 = fs[4 * (ii - 2) + r];
       }
       const double prod = mv * sel4(xnext, pj);
       double x = xi;
@@ -320,8 +326,10 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
 #pragma unroll
       for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, hb + m);
       if (e < 4 && ii >= 0) fs[4 * ii + e] = x;
-      mv = mvn;
-      xi = xin;
+      mv = mv1;
+      xi = xi1;
+      mv1 = mv2;
+      xi1 = xi2;
    }
 }
 
@@ -490,14 +498,25 @@ __device__ __forceinline__ void solve_line_quad(const double* __restrict__ fac, 
       xr = xrn;
    }
    // back substitution f(i) -= c'(i) f(i+1), i = N-2..0 (t = 0..Nmax-2, i = N-2-t)
+   // (row ii-1's C' row and forward value are loaded while row ii is solved)
    if (N > 0) rv[4 * (size_t)scell[N - 1] + r] = sel4(xp, r);
+   double xf = 0.0, c[4] = {0.0, 0.0, 0.0, 0.0};
+   int sc = 0;
+   if (N >= 2) {
+      xf = fs[4 * (N - 2) + r];
+      ld4row(fac + (size_t)kFacRec * (N - 2) + 32 + 4 * r, c);
+      sc = scell[N - 2];
+   }
    for (int t = 0; t <= Nmax - 2; t++) {
       const int ii = N - 2 - t;
-      double x = 0.0, c[4] = {0.0, 0.0, 0.0, 0.0};
-      if (ii >= 0) {
-         x = fs[4 * ii + r];
-         ld4row(fac + (size_t)kFacRec * ii + 32 + 4 * r, c);
+      double xfn = 0.0, cn[4] = {0.0, 0.0, 0.0, 0.0};
+      int scn = 0;
+      if (ii > 0) {
+         xfn = fs[4 * (ii - 1) + r];
+         ld4row(fac + (size_t)kFacRec * (ii - 1) + 32 + 4 * r, cn);
+         scn = scell[ii - 1];
       }
+      double x = xf;
 #pragma unroll
       for (int j = 0; j < 4; j++) x = x - c[j] * xp[j];
 #pragma unroll
@@ -505,7 +524,11 @@ __device__ __forceinline__ void solve_line_quad(const double* __restrict__ fac, 
          const double v = __shfl_sync(kLaneMask, x, base + m);
          if (ii >= 0) xp[m] = v;
       }
-      if (ii >= 0) rv[4 * (size_t)scell[ii] + r] = x;
+      if (ii >= 0) rv[4 * (size_t)sc + r] = x;
+      xf = xfn;
+#pragma unroll
+      for (int m = 0; m < 4; m++) c[m] = cn[m];
+      sc = scn;
    }
 }
 
@@ -682,21 +705,40 @@ __device__ __forceinline__ void solve_line_thread(const double* __restrict__ fac
       *reinterpret_cast<double2*>(o) = make_double2(xp[0], xp[1]);
       *reinterpret_cast<double2*>(o + 2) = make_double2(xp[2], xp[3]);
    }
+   // row i-1's C' and forward value are loaded while row i is solved
+   double c[16], xf[4];
+   int sc = 0;
+   if (N >= 2) {
+      ld16(fac + (size_t)kFacRec * (N - 2) + 32, c);
+      ld4row(fs + 4 * (N - 2), xf);
+      sc = scell[N - 2];
+   }
    for (int i = N - 2; i >= 0; i--) {
-      double c[16], x[4];
-      ld16(fac + (size_t)kFacRec * i + 32, c);
-      const double2 u = *reinterpret_cast<const double2*>(fs + 4 * i);
-      const double2 v = *reinterpret_cast<const double2*>(fs + 4 * i + 2);
-      x[0] = u.x; x[1] = u.y; x[2] = v.x; x[3] = v.y;
+      double cn[16], xfn[4];
+      int scn = 0;
+      if (i > 0) {
+         ld16(fac + (size_t)kFacRec * (i - 1) + 32, cn);
+         ld4row(fs + 4 * (i - 1), xfn);
+         scn = scell[i - 1];
+      } else {
+#pragma unroll
+         for (int m = 0; m < 16; m++) cn[m] = 0.0;
+#pragma unroll
+         for (int m = 0; m < 4; m++) xfn[m] = 0.0;
+      }
+      double x[4] = {xf[0], xf[1], xf[2], xf[3]};
 #pragma unroll
       for (int k = 0; k < 4; k++)
 #pragma unroll
          for (int j = 0; j < 4; j++) x[k] = x[k] - c[4 * k + j] * xp[j];
-      double* o = r + 4 * (size_t)scell[i];
+      double* o = r + 4 * (size_t)sc;
       *reinterpret_cast<double2*>(o) = make_double2(x[0], x[1]);
       *reinterpret_cast<double2*>(o + 2) = make_double2(x[2], x[3]);
 #pragma unroll
-      for (int k = 0; k < 4; k++) xp[k] = x[k];
+      for (int k = 0; k < 4; k++) { xp[k] = x[k]; xf[k] = xfn[k]; }
+#pragma unroll
+      for (int m = 0; m < 16; m++) c[m] = cn[m];
+      sc = scn;
    }
 }
 
@@ -792,16 +834,21 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       double xnext[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) xnext[m] = xn[m];
-      double mv = 0.0, xi = 0.0;
+      // rows ii-1 and ii-2 are in flight while row ii is solved
+      double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
       if (N >= 2) {
          mv = fac[(size_t)kFacRec * (N - 2) + 32 + 16 * hi + e];
          xi = fs[4 * (N - 2) + r];
       }
+      if (N >= 3) {
+         mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + 16 * hi + e];
+         xi1 = fs[4 * (N - 3) + r];
+      }
       for (int ii = N - 2; ii >= 0; ii--) {
-         double mvn = 0.0, xin = 0.0;
-         if (ii > 0) {
-            mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + 16 * hi + e];
-            xin = fs[4 * (ii - 1) + r];
+         double mv2 = 0.0, xi2 = 0.0;
+         if (ii > 1) {
+            mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + 16 * hi + e];
+            xi2 = fs[4 * (ii - 2) + r];
          }
          const double prod = mv * (hi ? sel4(fNall, pj) : sel4(xnext, pj));
          const double other = __shfl_sync(kLaneMask, prod, e + 16);
@@ -812,24 +859,31 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
 #pragma unroll
          for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, m);
          if (lane < 4) fs[4 * ii + lane] = x;
-         mv = mvn;
-         xi = xin;
+         mv = mv1;
+         xi = xi1;
+         mv1 = mv2;
+         xi1 = xi2;
       }
    } else {
       // back substitution (triSolvers.cpp:839-846): f(i) -= c'(i) f(i+1)
       double xnext[4];
 #pragma unroll
       for (int m = 0; m < 4; m++) xnext[m] = xprev[m];
-      double mv = 0.0, xi = 0.0;
+      // rows ii-1 and ii-2 are in flight while row ii is solved
+      double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
       if (N >= 2) {
          mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
          xi = fs[4 * (N - 2) + r];
       }
+      if (N >= 3) {
+         mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
+         xi1 = fs[4 * (N - 3) + r];
+      }
       for (int ii = N - 2; ii >= 0; ii--) {
-         double mvn = 0.0, xin = 0.0;
-         if (ii > 0) {
-            mvn = fac[(size_t)kFacRec * (ii - 1) + 32 + e];
-            xin = fs[4 * (ii - 1) + r];
+         double mv2 = 0.0, xi2 = 0.0;
+         if (ii > 1) {
+            mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
+            xi2 = fs[4 * (ii - 2) + r];
          }
          const double prod = mv * sel4(xnext, pj);
          double x = xi;
@@ -838,8 +892,10 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
 #pragma unroll
          for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, m);
          if (lane < 4) fs[4 * ii + lane] = x;
-         mv = mvn;
-         xi = xin;
+         mv = mv1;
+         xi = xi1;
+         mv1 = mv2;
+         xi1 = xi2;
       }
    }
 }

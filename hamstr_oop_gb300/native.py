@@ -474,8 +474,8 @@ class GpuSolver:
     def autotune(self, reps: int = 3) -> dict:
         """Pick the fastest launch shapes for the current precision (hamstr_gpu_autotune)."""
         import json
-        buf = ctypes.create_string_buffer(32768)
-        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 32768))
+        buf = ctypes.create_string_buffer(65536)
+        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 65536))
         return json.loads(buf.value.decode())
 
     SHAPE_KEYS = ("face_block", "adi_warps_per_sm", "mx_block", "mx_fused", "face_softdiv", "pivot_softdiv",

@@ -216,11 +216,14 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * each), and the shortest (up to 0, 4, 8 or 16 rows) 32 per warp, one per
  * lane; FP32
  * line kernels 32..128 threads per block, with the blocks assembled by a
- * separate coalesced kernel or inside the factorisation; FP64 divisions of the face
+ * separate coalesced kernel or inside the factorisation, and, where there
+ * are periodic chains of 64 rows or more, those solved by segments or not
+ * (shape key 10); FP64 divisions of the face
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
  * (bit-identical) -- and keeps the fastest.  The state is restored
- * afterwards; results do not depend on the shape.  report (may be NULL)
- * receives a JSON summary of the timings (about 200 bytes per candidate). */
+ * afterwards; FP64 results do not depend on the shape.  report (may be
+ * NULL) receives a JSON summary of the timings (about 210 bytes per
+ * candidate, at most 128 candidates). */
 int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
 
 /* The launch shape itself (no reference counterpart), HAMSTR_SHAPE_N ints:
@@ -245,7 +248,8 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *  [10] FP32 line kernels: periodic chains of 64 rows or more solved by
  *       segments (16 rows each, up to 32, one warp lane per segment, joined
  *       by a small cyclic system on the segment ends) instead of one thread
- *       running the whole cyclic recurrence: 0 or 1 (default 1; not tuned).
+ *       running the whole cyclic recurrence: 0 or 1 (default 1; tuned in
+ *       the FP32 form where such chains exist).
  *       The same linear system; in FP32 the rounding differs, so the FP32
  *       form's iterates differ in the last bits and its steady state (the
  *       FP64 residual's zero) does not.

@@ -764,7 +764,8 @@ static void roe_jacobian3d(const double* nxyz, const double* ql, const double* q
    ur = qr[1] / qr[0]; vr = qr[2] / qr[0]; wr = qr[3] / qr[0];
    pr = gm1 * (qr[4] - 0.5 * ror * (ur * ur + vr * vr + wr * wr));
    hr = (qr[4] + pr) / ror;
-   dp = pr - pl;
+   dp = pr - pl;   /* formed as the reference forms it; the Jacobian does not use it */
+   (void)dp;
    uconr = ur * nx + vr * ny + wr * nz;
    uconl = ul * nx + vl * ny + wl * nz;
 
