@@ -214,7 +214,8 @@ struct hamstr_gpu {
       if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
       // long periodic chains take the segmented solve: P segments of about
-      // kSpikeRows rows each (at most kSpikeMaxSeg), grouped by wave
+      // kSpikeRows rows each (at most kSpikeMaxSeg), grouped by wave; their
+      // rows are tiled across the segments (sp_rec0 in tile rows)
       {
          std::vector<int> chain_spike(std::max(plan.nChain, 1), -1), sp_chain, sp_seg, sp_nseg, sp_rec0;
          sp_wave_ptr.assign(plan.nWave + 1, 0);
@@ -229,8 +230,12 @@ struct hamstr_gpu {
                sp_chain.push_back(c);
                sp_nseg.push_back(P);
                sp_rec0.push_back(rows);
-               for (int p = 0; p <= kSpikeMaxSeg; p++) sp_seg.push_back(p <= P ? (int)((long long)p * n / P) : n);
-               rows += n;
+               int longest = 0;
+               for (int p = 0; p <= kSpikeMaxSeg; p++) {
+                  sp_seg.push_back(p <= P ? (int)((long long)p * n / P) : n);
+                  if (p >= 1 && p <= P) longest = std::max(longest, sp_seg.back() - sp_seg[sp_seg.size() - 2]);
+               }
+               rows += longest;   // tile rows: local row k of every segment in one
             }
             sp_wave_ptr[w + 1] = (int)sp_chain.size();
          }
@@ -246,8 +251,8 @@ struct hamstr_gpu {
          if ((st = upload(&d.sp_seg, sp_seg, owned))) return st;
          if ((st = upload(&d.sp_nseg, sp_nseg, owned))) return st;
          if ((st = upload(&d.sp_rec0, sp_rec0, owned))) return st;
-         if ((st = dalloc(&d.sp_fac, 80 * (size_t)std::max(rows, 1), owned))) return st;
-         if ((st = dalloc(&d.sp_y, 4 * (size_t)std::max(rows, 1), owned))) return st;
+         if ((st = dalloc(&d.sp_fac, 80 * 32 * (size_t)std::max(rows, 1), owned))) return st;
+         if ((st = dalloc(&d.sp_y, 4 * 32 * (size_t)std::max(rows, 1), owned))) return st;
          if ((st = dalloc(&d.sp_red, (size_t)kSpikeRedStride * std::max(d.nSpike, 1), owned))) return st;
       }
       CK(cudaMemsetAsync(d.ff32, 0, 32 * (size_t)d.nSlot * sizeof(float), stream));

@@ -144,9 +144,11 @@ struct DeviceState {
    int* sp_wave_ptr;       // [nWave+1] spike chains of each wave: sp indices sp_wave_ptr[w] .. [w+1]-1
    int* sp_seg;            // [nSpike][kSpikeMaxSeg+1] first row (in the chain) of each segment, then N
    int* sp_nseg;           // [nSpike] P
-   int* sp_rec0;           // [nSpike] first record of the chain in sp_fac / sp_y
-   float* sp_fac;          // [spike rows][80]: A, LU(B'), C' (local), V (right spike), W (left spike)
-   float* sp_y;            // [spike rows][4]: the sweep's local solutions
+   int* sp_rec0;           // [nSpike] first tile row of the chain in sp_fac / sp_y (it takes as many
+                           // tile rows as its longest segment has rows)
+   float* sp_fac;          // [tile rows][80][32 segments]: A, LU(B'), C' (local), V (right spike),
+                           // W (left spike) of local row k of each segment
+   float* sp_y;            // [tile rows][4][32 segments]: the sweep's local solutions
    float* sp_red;          // [nSpike][kSpikeRedStride]: factors of the boundary system
 };
 

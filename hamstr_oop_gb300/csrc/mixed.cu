@@ -780,20 +780,79 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
 // pairs Z_p = (b_p, t_{p+1}):
 //     b_p     - V_e(p) t_{p+1} - W_e(p) b_{p-1}   = y_e(p)
 //     t_{p+1} - V_s(p+1) t_{p+2} - W_s(p+1) b_p   = y_s(p+1)
-// i.e. L_p Z_{p-1} + D_p Z_p + U_p Z_{p+1} = R_p with 8x8 blocks, which
-// lane 0 solves by a cyclic block elimination onto Z_{P-1}.  This is the
-// same linear system the sequential cyclic block Thomas solves (in FP32 it
+// i.e. L_p Z_{p-1} + D_p Z_p + U_p Z_{p+1} = R_p with 8x8 blocks
+//     D_p = [I, -V_e(p); -W_s(p+1), I],  L_p = [-W_e(p), 0; 0, 0],
+//     U_p = [0, 0; 0, -V_s(p+1)],
+// which lane 0 eliminates onto Z_{P-1} (a cyclic block Thomas of P rows).
+// Their sparsity keeps every step in 4x4 blocks: the pivot blocks are
+// M_p = [I, X_p; -W_s(p+1), I] and are solved through the 4x4 Schur
+// complement S_p = I + W_s(p+1) X_p; the couplings G_p = M_p^{-1} U_p and
+// H_p (to Z_{P-1}) have four non-zero columns each.  This is the same
+// linear system the sequential cyclic block Thomas solves (in FP32 it
 // differs in rounding only), with N/P + P rows of latency instead of N.
 // The segment factors and spikes, and the boundary system's factors, are
 // formed once per step; each sweep replays the right-hand side.
+//
+// Layout: the rows of a chain's segments are tiled like the other FP32 line
+// data (element e of local row k of segment p at tix(R0 + k, W, e, p), R0
+// the chain's first tile row), so every load and store of the warp is one
+// 128-byte line.
 
 // sp_fac record of one row: A, LU of the segment's B', C' (no C' on a
 // segment's last row), V, W
 constexpr int kSpRec = 80;
 
-// 8x8 row-major matrices of the boundary system (lane 0, local arrays)
-// LU with reciprocal pivots: M = L U, U unit upper; L below and on the
-// diagonal (the diagonal holding 1/L_kk)
+// sp_red layout of one chain: for p = 0 .. P-2, at kRedRow * p: X_p, LU(S_p),
+// G_p (top 4 rows, bottom 4 rows; its non-zero columns 4-7), H_p (top,
+// bottom; columns 0-3), W_e(p), W_s(p+1); then at kRedLast: LU(K) (8x8),
+// W_e(P-1), V_s(0)
+constexpr int kRedRow = 128;
+constexpr int kRedLast = kRedRow * (kSpikeMaxSeg - 1);
+static_assert(kRedLast + 64 + 32 <= kSpikeRedStride, "boundary-system factors fit their stride");
+enum { RX = 0, RS = 16, RGT = 32, RGB = 48, RHT = 64, RHB = 80, RWE = 96, RWS = 112 };
+
+// y -= M x (4x4, 4-vector)
+__device__ __forceinline__ void mv_sub(const float (&M)[16], const float (&x)[4], float (&y)[4])
+{
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) y[k] = __fmaf_rn(-M[4 * k + j], x[j], y[k]);
+}
+
+__device__ __forceinline__ void mv_add(const float (&M)[16], const float (&x)[4], float (&y)[4])
+{
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) y[k] = __fmaf_rn(M[4 * k + j], x[j], y[k]);
+}
+
+// out = M X (4x4)
+__device__ __forceinline__ void mm_mul(const float (&M)[16], const float (&X)[16], float (&out)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) out[m] = 0.f;
+   mm_sub(M, X, out);
+#pragma unroll
+   for (int m = 0; m < 16; m++) out[m] = -out[m];
+}
+
+__device__ __forceinline__ void ld16s(const float* p, float (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) v[m] = p[m];
+}
+
+__device__ __forceinline__ void st16s(float* p, const float (&v)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) p[m] = v[m];
+}
+
+// 8x8 row-major LU with reciprocal pivots (K, once per chain and step):
+// M = L U, U unit upper; L below and on the diagonal (the diagonal holding
+// 1/L_kk)
 __device__ void m8_lu(float* M)
 {
    for (int k = 0; k < 8; k++) {
@@ -807,210 +866,236 @@ __device__ void m8_lu(float* M)
    }
 }
 
-// x <- M^{-1} x for the 8 values x[0], x[s], .., x[7s]
-__device__ void m8_solve(const float* LU, float* x, int s)
+// x <- M^{-1} x with the LU of m8_lu
+__device__ void m8_solve(const float* LU, float (&x)[8])
 {
    for (int i = 0; i < 8; i++) {
-      float v = x[s * i];
-      for (int k = 0; k < i; k++) v = __fmaf_rn(-LU[8 * i + k], x[s * k], v);
-      x[s * i] = v * LU[9 * i];
+      float v = x[i];
+      for (int k = 0; k < i; k++) v = __fmaf_rn(-LU[8 * i + k], x[k], v);
+      x[i] = v * LU[9 * i];
    }
    for (int i = 6; i >= 0; i--) {
-      float v = x[s * i];
-      for (int j = i + 1; j < 8; j++) v = __fmaf_rn(-LU[8 * i + j], x[s * j], v);
-      x[s * i] = v;
+      float v = x[i];
+      for (int j = i + 1; j < 8; j++) v = __fmaf_rn(-LU[8 * i + j], x[j], v);
+      x[i] = v;
    }
 }
 
-// C = alpha C - A B (alpha 0 or 1)
-__device__ void m8_msub(float* C, const float* A, const float* B, bool keep)
+// M [u; v] = [f; h] with M = [I, X; -Ws, I] and the LU of S = I + Ws X:
+// v = S^{-1}(h + Ws f), u = f - X v, for the four columns of F and Hh
+// (Hh = nullptr for h = 0)
+__device__ __forceinline__ void schur_cols(const float (&X)[16], const LUf& s, const float (&Ws)[16],
+                                           const float (&F)[16], const float* Hh, float (&U)[16], float (&Vv)[16])
 {
-   for (int i = 0; i < 8; i++)
-      for (int j = 0; j < 8; j++) {
-         float v = keep ? C[8 * i + j] : 0.f;
-         for (int k = 0; k < 8; k++) v = __fmaf_rn(-A[8 * i + k], B[8 * k + j], v);
-         C[8 * i + j] = v;
-      }
+#pragma unroll
+   for (int m = 0; m < 16; m++) Vv[m] = Hh ? Hh[m] : 0.f;
+   float WF[16];
+   mm_mul(Ws, F, WF);
+#pragma unroll
+   for (int m = 0; m < 16; m++) Vv[m] += WF[m];
+   luf_cols(s, Vv);
+#pragma unroll
+   for (int m = 0; m < 16; m++) U[m] = F[m];
+   mm_sub(X, Vv, U);
 }
-
-// y = alpha y - M x on 8-vectors
-__device__ __forceinline__ void v8_msub(float* y, const float* M, const float* x)
-{
-   for (int i = 0; i < 8; i++) {
-      float v = y[i];
-      for (int k = 0; k < 8; k++) v = __fmaf_rn(-M[8 * i + k], x[k], v);
-      y[i] = v;
-   }
-}
-
-__device__ __forceinline__ void ldm8(const float* __restrict__ p, float* m)
-{
-   for (int e = 0; e < 64; e += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(p + e);
-      m[e] = v.x; m[e + 1] = v.y; m[e + 2] = v.z; m[e + 3] = v.w;
-   }
-}
-
-__device__ __forceinline__ void stm8(float* __restrict__ p, const float* m)
-{
-   for (int e = 0; e < 64; e += 4) *reinterpret_cast<float4*>(p + e) = make_float4(m[e], m[e + 1], m[e + 2], m[e + 3]);
-}
-
-// the blocks of row p of the boundary system from the segments' spike tips
-// (sh: [p][4][16] = V_s, W_s, V_e, W_e of segment p)
-__device__ void red_blocks(const float* sh, int p, int P, float* L, float* D, float* U)
-{
-   const int q = (p + 1 == P) ? 0 : p + 1;
-   const float* Vs1 = sh + 64 * q;
-   const float* Ws1 = sh + 64 * q + 16;
-   const float* Ve = sh + 64 * p + 32;
-   const float* We = sh + 64 * p + 48;
-   for (int e = 0; e < 64; e++) { L[e] = 0.f; D[e] = 0.f; U[e] = 0.f; }
-   for (int k = 0; k < 4; k++)
-      for (int j = 0; j < 4; j++) {
-         L[8 * k + j] = -We[4 * k + j];
-         D[8 * k + 4 + j] = -Ve[4 * k + j];
-         D[8 * (4 + k) + j] = -Ws1[4 * k + j];
-         U[8 * (4 + k) + 4 + j] = -Vs1[4 * k + j];
-      }
-   for (int k = 0; k < 8; k++) D[9 * k] = 1.f;
-}
-
-// sp_red layout of one chain: row p < P-1 at 256 p: LU(M_p), L_p, G_p, B_p;
-// then LU(K), L_{P-1}, U_{P-1} at 256 (kSpikeMaxSeg - 1)
-__device__ __forceinline__ float* red_row(float* red, int p, int m) { return red + 256 * p + 64 * m; }
-__device__ __forceinline__ const float* red_row(const float* red, int p, int m) { return red + 256 * p + 64 * m; }
 
 __global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
 {
-   __shared__ float tips[kSpikeMaxSeg * 64];
+   __shared__ __align__(16) float tips[kSpikeMaxSeg * 64];   // per segment: V_s, W_s, V_e, W_e
    const int sp = blockIdx.x, lane = threadIdx.x;
    const int ich = d.sp_chain[sp];
    if (halted(d) || frozen_chain(d, ich)) return;
-   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], rec0 = d.sp_rec0[sp];
+   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], R0 = d.sp_rec0[sp];
+   const int* seg = d.sp_seg + (kSpikeMaxSeg + 1) * sp;
    bool bad = false;
    if (lane < P) {
-      const int s = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane], e = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane + 1] - 1;
-      float cp[16], gw[16];
-      for (int i = s; i <= e; i++) {
-         float A[16], B[16], C[16];
-         mx_row_ref(d, mx_rowref(d, row0 + i), A, B, C);
-         float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
-         st16f(rec, A);
-         if (i > s) mm_sub(A, cp, B);
-         const LUf u = luf_factor(B);
-         luf_store(rec + 16, u);
-         bad |= nonfinite(u.p0) || nonfinite(u.p1) || nonfinite(u.p2) || nonfinite(u.p3);
-         // left spike, forward: g_s = B'^{-1}(-A_s), g_i = B'^{-1}(-A_i g_{i-1})
+      const int s = seg[lane], n = seg[lane + 1] - s;   // n >= 2
+      // forward: B'_k = B_k - A_k C'_{k-1}; C'_k = B'^{-1} C_k; the left
+      // spike's forward values g_0 = B'^{-1}(-A_0), g_k = B'^{-1}(-A_k g_{k-1});
+      // at the last row the right spike B'^{-1}(-C_e).  The next row's blocks
+      // are assembled from references looked up a row earlier.
+      float A[16], B[16], C[16], cp[16], gw[16];
+      RowRef rnext = mx_rowref(d, row0 + s + 1);
+      mx_row_ref(d, mx_rowref(d, row0 + s), A, B, C);
+      for (int k = 0; k < n; k++) {
+         float An[16], Bn[16], Cn[16];
+         if (k + 1 < n) {
+            mx_row_ref(d, rnext, An, Bn, Cn);
+            if (k + 2 < n) rnext = mx_rowref(d, row0 + s + k + 2);
+         }
+         float* rec = d.sp_fac + tix(R0 + k, kSpRec, 0, lane);
+         st16t(rec, A);
          float w[16];
-         if (i == s) {
+         if (k == 0) {
 #pragma unroll
             for (int m = 0; m < 16; m++) w[m] = -A[m];
          } else {
+            mm_sub(A, cp, B);
 #pragma unroll
             for (int m = 0; m < 16; m++) w[m] = 0.f;
             mm_sub(A, gw, w);
          }
+         const LUf u = luf_factor(B);
+         luf_store_t(rec + 32 * 16, u);
+         bad |= nonfinite(u.p0) || nonfinite(u.p1) || nonfinite(u.p2) || nonfinite(u.p3);
          luf_cols(u, w);
-         st16f(rec + 64, w);
+         st16t(rec + 32 * 64, w);
 #pragma unroll
          for (int m = 0; m < 16; m++) gw[m] = w[m];
-         if (i < e) {
+         if (k + 1 < n) {
             luf_cols(u, C);
-            st16f(rec + 32, C);
+            st16t(rec + 32 * 32, C);
 #pragma unroll
-            for (int m = 0; m < 16; m++) cp[m] = C[m];
+            for (int m = 0; m < 16; m++) { cp[m] = C[m]; A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
          } else {
-            // right spike at the last row: B'^{-1}(-C_e)
 #pragma unroll
             for (int m = 0; m < 16; m++) C[m] = -C[m];
             luf_cols(u, C);
-            st16f(rec + 48, C);
+            st16t(rec + 32 * 48, C);
          }
       }
-      // back substitution of both spikes: V_i = -C'_i V_{i+1},
-      // W_i = g_i - C'_i W_{i+1}
-      float vn[16], wn[16];
-      ld16f(d.sp_fac + (size_t)kSpRec * (rec0 + e) + 48, vn);
-      ld16f(d.sp_fac + (size_t)kSpRec * (rec0 + e) + 64, wn);
+      // back substitution of both spikes: V_k = -C'_k V_{k+1},
+      // W_k = g_k - C'_k W_{k+1}; row k-1's C' and g are loaded while row k
+      // is formed
+      float vn[16], wn[16], c[16], g[16];
+      ld16t(d.sp_fac + tix(R0 + n - 1, kSpRec, 48, lane), vn);
+      ld16t(d.sp_fac + tix(R0 + n - 1, kSpRec, 64, lane), wn);
       float* tip = tips + 64 * lane;
-      st16f(tip + 32, vn);      // V_e
-      st16f(tip + 48, wn);      // W_e
-      for (int i = e - 1; i >= s; i--) {
-         float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
-         float c[16], v[16], w[16];
-         ld16f(rec + 32, c);
-         ld16f(rec + 64, w);
+      st16s(tip + 32, vn);   // V_e
+      st16s(tip + 48, wn);   // W_e
+      ld16t(d.sp_fac + tix(R0 + n - 2, kSpRec, 32, lane), c);
+      ld16t(d.sp_fac + tix(R0 + n - 2, kSpRec, 64, lane), g);
+      for (int k = n - 2; k >= 0; k--) {
+         float cn[16], gn[16];
+         if (k > 0) {
+            ld16t(d.sp_fac + tix(R0 + k - 1, kSpRec, 32, lane), cn);
+            ld16t(d.sp_fac + tix(R0 + k - 1, kSpRec, 64, lane), gn);
+         }
+         float v[16];
 #pragma unroll
          for (int m = 0; m < 16; m++) v[m] = 0.f;
          mm_sub(c, vn, v);
-         mm_sub(c, wn, w);
-         st16f(rec + 48, v);
-         st16f(rec + 64, w);
+         mm_sub(c, wn, g);
+         float* rec = d.sp_fac + tix(R0 + k, kSpRec, 0, lane);
+         st16t(rec + 32 * 48, v);
+         st16t(rec + 32 * 64, g);
 #pragma unroll
-         for (int m = 0; m < 16; m++) { vn[m] = v[m]; wn[m] = w[m]; }
+         for (int m = 0; m < 16; m++) { vn[m] = v[m]; wn[m] = g[m]; }
+         if (k > 0) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) { c[m] = cn[m]; g[m] = gn[m]; }
+         }
       }
-      st16f(tip, vn);           // V_s
-      st16f(tip + 16, wn);      // W_s
+      st16s(tip, vn);        // V_s
+      st16s(tip + 16, wn);   // W_s
    }
    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
    __syncwarp();
    if (lane != 0) return;
-   // boundary system: M_0 = D_0, M_p = D_p - L_p G_{p-1}; G_p = M_p^{-1} U_p;
-   // H_0 = M_0^{-1} L_0, H_p = -M_p^{-1} L_p H_{p-1}; at p = P-2 the
-   // coupling U_{P-2} goes to Z_{P-1} itself
+   // boundary system, p = 0 .. P-2 (q = p + 1):
+   //   X_p = -V_e(p) + W_e(p) Gtop_{p-1}  (X_0 = -V_e(0)),  S_p = I + W_s(q) X_p,
+   //   G_p = M_p^{-1} [0; -V_s(q)],
+   //   H_0 = M_0^{-1} [-W_e(0); 0],  H_p = M_p^{-1} [W_e(p) Htop_{p-1}; 0]
    float* red = d.sp_red + (size_t)kSpikeRedStride * sp;
-   float L[64], D[64], U[64], G[64], H[64], T[64];
-   for (int p = 0; p <= P - 2; p++) {
-      red_blocks(tips, p, P, L, D, U);
-      if (p > 0) m8_msub(D, L, G, true);                   // M_p = D_p - L_p G_{p-1}
-      m8_lu(D);
-      stm8(red_row(red, p, 0), D);
-      stm8(red_row(red, p, 1), L);
-      for (int j = 0; j < 8; j++) m8_solve(D, U + j, 8);   // G_p = M_p^{-1} U_p
-      if (p == 0) {
-         for (int e = 0; e < 64; e++) H[e] = L[e];
-      } else {
-         m8_msub(T, L, H, false);                            // T = -L_p H_{p-1}
-         for (int e = 0; e < 64; e++) H[e] = T[e];
-      }
-      for (int j = 0; j < 8; j++) m8_solve(D, H + j, 8);
-      for (int e = 0; e < 64; e++) G[e] = U[e];
-      stm8(red_row(red, p, 2), G);
-      stm8(red_row(red, p, 3), H);                           // H_p, turned into B_p below
-   }
-   // Z_p = a_p + B_p Z_{P-1}: B_{P-2} = -(G_{P-2} + H_{P-2}),
-   // B_p = -G_p B_{p+1} - H_p
-   float Bn[64];
-   ldm8(red_row(red, P - 2, 3), H);
-   for (int e = 0; e < 64; e++) Bn[e] = -(G[e] + H[e]);
-   stm8(red_row(red, P - 2, 3), Bn);
-   float B0[64];
-   for (int e = 0; e < 64; e++) B0[e] = Bn[e];
-   for (int p = P - 3; p >= 0; p--) {
-      ldm8(red_row(red, p, 2), G);
-      ldm8(red_row(red, p, 3), H);
-      for (int e = 0; e < 64; e++) T[e] = -H[e];
-      m8_msub(T, G, Bn, true);
-      stm8(red_row(red, p, 3), T);
-      for (int e = 0; e < 64; e++) Bn[e] = T[e];
-      if (p == 0)
-         for (int e = 0; e < 64; e++) B0[e] = T[e];
-   }
-   // K = D_{P-1} + L_{P-1} B_{P-2} + U_{P-1} B_0
-   red_blocks(tips, P - 1, P, L, D, U);
-   ldm8(red_row(red, P - 2, 3), Bn);
-   for (int e = 0; e < 64; e++) { L[e] = -L[e]; U[e] = -U[e]; }
-   m8_msub(D, L, Bn, true);
-   m8_msub(D, U, B0, true);
-   for (int e = 0; e < 64; e++) { L[e] = -L[e]; U[e] = -U[e]; }
-   m8_lu(D);
-   float* last = red + 256 * (kSpikeMaxSeg - 1);
-   stm8(last, D);
-   stm8(last + 64, L);
-   stm8(last + 128, U);
+   float Gt[16], Ht[16], Gb[16], Hb[16];
    bool kbad = false;
-   for (int k = 0; k < 8; k++) kbad |= nonfinite(D[9 * k]);
+   for (int p = 0; p <= P - 2; p++) {
+      const int q = p + 1;
+      float X[16], We[16], Ws[16], T[16];
+      ld16s(tips + 64 * p + 32, X);
+      ld16s(tips + 64 * p + 48, We);
+      ld16s(tips + 64 * q + 16, Ws);
+#pragma unroll
+      for (int m = 0; m < 16; m++) X[m] = -X[m];
+      if (p > 0) {
+         mm_mul(We, Gt, T);
+#pragma unroll
+         for (int m = 0; m < 16; m++) X[m] += T[m];
+      }
+      float S[16];
+      mm_mul(Ws, X, S);
+#pragma unroll
+      for (int k = 0; k < 4; k++) S[5 * k] += 1.f;
+      const LUf su = luf_factor(S);
+      kbad |= nonfinite(su.p0) || nonfinite(su.p1) || nonfinite(su.p2) || nonfinite(su.p3);
+      float F[16], Hh[16];
+      // G_p: f = 0, h = -V_s(q): v = S^{-1}(-V_s(q)), u = -X v
+      ld16s(tips + 64 * q, Hh);
+#pragma unroll
+      for (int m = 0; m < 16; m++) { Hh[m] = -Hh[m]; F[m] = 0.f; }
+      schur_cols(X, su, Ws, F, Hh, Gt, Gb);
+      // H_p
+      if (p == 0) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) F[m] = -We[m];
+      } else {
+         mm_mul(We, Ht, F);
+      }
+      schur_cols(X, su, Ws, F, nullptr, Ht, Hb);
+      float* rr = red + kRedRow * p;
+      st16s(rr + RX, X);
+      luf_store(rr + RS, su);
+      st16s(rr + RGT, Gt);
+      st16s(rr + RGB, Gb);
+      st16s(rr + RHT, Ht);
+      st16s(rr + RHB, Hb);
+      st16s(rr + RWE, We);
+      st16s(rr + RWS, Ws);
+   }
+   // Z_p = a_p + B_p Z_{P-1}; only the rows of B_{P-2} (top) and B_0
+   // (bottom) enter K: B_{P-2} = -[H_{P-2} | G_{P-2}],
+   // B_p = -G_p Bbot_{p+1} - [H_p | 0], carried on its bottom rows
+   float Bl[16], Br[16];   // bottom rows of B_p: columns 0-3, 4-7
+#pragma unroll
+   for (int m = 0; m < 16; m++) { Bl[m] = -Hb[m]; Br[m] = -Gb[m]; }
+   float BtopL[16], BtopR[16];   // top rows of B_{P-2}
+#pragma unroll
+   for (int m = 0; m < 16; m++) { BtopL[m] = -Ht[m]; BtopR[m] = -Gt[m]; }
+   for (int p = P - 3; p >= 0; p--) {
+      float g[16], h[16], nl[16], nr[16];
+      ld16s(red + kRedRow * p + RGB, g);
+      ld16s(red + kRedRow * p + RHB, h);
+      mm_mul(g, Bl, nl);
+      mm_mul(g, Br, nr);
+#pragma unroll
+      for (int m = 0; m < 16; m++) { Bl[m] = -nl[m] - h[m]; Br[m] = -nr[m]; }
+   }
+   // K = D_{P-1} + L_{P-1} B_{P-2} + U_{P-1} B_0:
+   //   top rows    [I, -V_e(P-1)] - W_e(P-1) Btop_{P-2}
+   //   bottom rows [-W_s(0), I]   - V_s(0) Bbot_0
+   float K[64], We[16], Vs0[16], M4[16], t[16];
+   ld16s(tips + 64 * (P - 1) + 48, We);
+   ld16s(tips, Vs0);
+   ld16s(tips + 64 * (P - 1) + 32, t);   // V_e(P-1)
+   mm_mul(We, BtopL, M4);
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+         K[8 * k + j] = ((k == j) ? 1.f : 0.f) - M4[4 * k + j];
+      }
+   mm_mul(We, BtopR, M4);
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) K[8 * k + 4 + j] = -t[4 * k + j] - M4[4 * k + j];
+   ld16s(tips + 16, t);   // W_s(0)
+   mm_mul(Vs0, Bl, M4);
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) K[8 * (4 + k) + j] = -t[4 * k + j] - M4[4 * k + j];
+   mm_mul(Vs0, Br, M4);
+#pragma unroll
+   for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) K[8 * (4 + k) + 4 + j] = ((k == j) ? 1.f : 0.f) - M4[4 * k + j];
+   m8_lu(K);
+   for (int k = 0; k < 8; k++) kbad |= nonfinite(K[9 * k]);
+   float* last = red + kRedLast;
+   for (int m = 0; m < 64; m++) last[m] = K[m];
+   st16s(last + 64, We);
+   st16s(last + 80, Vs0);
    if (kbad) atomicOr(d.status, DEV_ERR_PIVOT);
 }
 
@@ -1018,131 +1103,213 @@ __global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
 // wave: right-hand sides r32[fcell], solutions into r32[scell]
 __global__ void __launch_bounds__(32) mx_spike_solve_kernel(DeviceState d, int first)
 {
-   __shared__ float ry[kSpikeMaxSeg * 8];   // per segment: y_s then y_e
-   __shared__ float zs[kSpikeMaxSeg * 8];   // Z_p = (b_p, t_{p+1})
+   // (red_s is read with float4 loads: 16-byte aligned)
+   __shared__ __align__(16) float red_s[kRedLast + 96];   // the chain's boundary-system factors
+   __shared__ __align__(16) float ry[kSpikeMaxSeg * 8];   // per segment: y_s then y_e
+   __shared__ __align__(16) float zs[kSpikeMaxSeg * 8];   // Z_p = (b_p, t_{p+1})
    const int sp = first + blockIdx.x, lane = threadIdx.x;
    const int ich = d.sp_chain[sp];
    if (halted(d) || frozen_chain(d, ich)) return;
-   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], rec0 = d.sp_rec0[sp];
-   int s = 0, e = -1;
+   const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], R0 = d.sp_rec0[sp];
+   const int* seg = d.sp_seg + (kSpikeMaxSeg + 1) * sp;
+   {
+      // the boundary-system factors into shared memory (lane 0 reads them
+      // one step after another below)
+      const float* red = d.sp_red + (size_t)kSpikeRedStride * sp;
+      const int nrow = kRedRow * (P - 1);
+      for (int m = lane; m < nrow; m += 32) red_s[m] = red[m];
+      for (int m = lane; m < 96; m += 32) red_s[kRedLast + m] = red[kRedLast + m];
+   }
+   int s = 0, n = 0;
    if (lane < P) {
-      s = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane];
-      e = d.sp_seg[(kSpikeMaxSeg + 1) * sp + lane + 1] - 1;
-      // y' forward: y'_i = B'^{-1}(f_i - A_i y'_{i-1})
-      float yp[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int i = s; i <= e; i++) {
-         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
-         const int fc = d.row_fcell[row0 + i];
-         float x[4] = {0.f, 0.f, 0.f, 0.f};
+      s = seg[lane];
+      n = seg[lane + 1] - s;
+      const int* fcell = d.row_fcell + row0 + s;
+      // forward: y'_k = B'^{-1}(f_k - A_k y'_{k-1}); row k+1's record and
+      // right-hand side are loaded while row k is solved
+      float a[16], yp[4] = {0.f, 0.f, 0.f, 0.f}, x[4] = {0.f, 0.f, 0.f, 0.f};
+      LUf u = luf_load_t(d.sp_fac + tix(R0, kSpRec, 16, lane));
+      {
+         const int fc = fcell[0];
          if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, x);
-         if (i > s) {
-            float a[16];
-            ld16f(rec, a);
+      }
 #pragma unroll
-            for (int k = 0; k < 4; k++)
-#pragma unroll
-               for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-a[4 * k + j], yp[j], x[k]);
+      for (int m = 0; m < 16; m++) a[m] = 0.f;
+      for (int k = 0; k < n; k++) {
+         float an[16], xn[4] = {0.f, 0.f, 0.f, 0.f};
+         LUf un;
+         if (k + 1 < n) {
+            const float* rn = d.sp_fac + tix(R0 + k + 1, kSpRec, 0, lane);
+            ld16t(rn, an);
+            un = luf_load_t(rn + 32 * 16);
+            const int fc = fcell[k + 1];
+            if (fc >= 0) ld4(d.r32 + 4 * (size_t)fc, xn);
          }
-         luf_solve(luf_load(rec + 16), x[0], x[1], x[2], x[3]);
-         st4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+         if (k > 0) mv_sub(a, yp, x);
+         luf_solve(u, x[0], x[1], x[2], x[3]);
 #pragma unroll
-         for (int k = 0; k < 4; k++) yp[k] = x[k];
+         for (int c = 0; c < 4; c++) {
+            d.sp_y[tix(R0 + k, 4, c, lane)] = x[c];
+            yp[c] = x[c];
+         }
+         if (k + 1 < n) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) a[m] = an[m];
+            u = un;
+#pragma unroll
+            for (int c = 0; c < 4; c++) x[c] = xn[c];
+         }
       }
-      // back: y_i = y'_i - C'_i y_{i+1}
+      // back: y_k = y'_k - C'_k y_{k+1}
 #pragma unroll
-      for (int k = 0; k < 4; k++) ry[8 * lane + 4 + k] = yp[k];
-      for (int i = e - 1; i >= s; i--) {
-         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
-         float c[16], x[4];
-         ld16f(rec + 32, c);
-         ld4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+      for (int c = 0; c < 4; c++) ry[8 * lane + 4 + c] = yp[c];
+      float cm[16], yk[4];
+      ld16t(d.sp_fac + tix(R0 + n - 2, kSpRec, 32, lane), cm);
 #pragma unroll
-         for (int k = 0; k < 4; k++)
+      for (int c = 0; c < 4; c++) yk[c] = d.sp_y[tix(R0 + n - 2, 4, c, lane)];
+      for (int k = n - 2; k >= 0; k--) {
+         float cn[16], ykn[4];
+         if (k > 0) {
+            ld16t(d.sp_fac + tix(R0 + k - 1, kSpRec, 32, lane), cn);
 #pragma unroll
-            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(-c[4 * k + j], yp[j], x[k]);
-         st4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+            for (int c = 0; c < 4; c++) ykn[c] = d.sp_y[tix(R0 + k - 1, 4, c, lane)];
+         }
+         mv_sub(cm, yp, yk);
 #pragma unroll
-         for (int k = 0; k < 4; k++) yp[k] = x[k];
+         for (int c = 0; c < 4; c++) {
+            d.sp_y[tix(R0 + k, 4, c, lane)] = yk[c];
+            yp[c] = yk[c];
+         }
+         if (k > 0) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) cm[m] = cn[m];
+#pragma unroll
+            for (int c = 0; c < 4; c++) yk[c] = ykn[c];
+         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; k++) ry[8 * lane + k] = yp[k];
+      for (int c = 0; c < 4; c++) ry[8 * lane + c] = yp[c];
    }
    __syncwarp();
    if (lane == 0) {
-      // R_p = (y_e(p), y_s(p+1)); g_p = M_p^{-1}(R_p - L_p g_{p-1});
-      // a_{P-2} = g_{P-2}, a_p = g_p - G_p a_{p+1};
-      // Z_{P-1} = K^{-1}(R_{P-1} - L_{P-1} a_{P-2} - U_{P-1} a_0);
-      // Z_p = a_p + B_p Z_{P-1}
-      const float* red = d.sp_red + (size_t)kSpikeRedStride * sp;
-      float M[64], g[8];
+      // R_p = (y_e(p), y_s(p+1));
+      //   g_p: f = y_e(p) + W_e(p) gtop_{p-1}, h = y_s(p+1):
+      //        v = S_p^{-1}(h + W_s(p+1) f), u = f - X_p v;
+      //   a_{P-2} = g_{P-2}, a_p = g_p - G_p abot_{p+1};
+      //   Z_{P-1} = K^{-1}(R_{P-1} + [W_e(P-1) atop_{P-2}; V_s(0) abot_0]);
+      //   Z_{P-2} = g_{P-2} - G_{P-2} zbot - H_{P-2} ztop,
+      //   Z_p = g_p - G_p Zbot_{p+1} - H_p ztop
+      float gt[4] = {0.f, 0.f, 0.f, 0.f};
       for (int p = 0; p <= P - 2; p++) {
-         for (int k = 0; k < 4; k++) {
-            g[k] = ry[8 * p + 4 + k];
-            g[4 + k] = ry[8 * (p + 1) + k];
-         }
+         const float* rr = red_s + kRedRow * p;
+         float f[4], v[4], M[16];
+#pragma unroll
+         for (int c = 0; c < 4; c++) { f[c] = ry[8 * p + 4 + c]; v[c] = ry[8 * (p + 1) + c]; }
          if (p > 0) {
-            float prev[8];
-            for (int k = 0; k < 8; k++) prev[k] = zs[8 * (p - 1) + k];
-            ldm8(red_row(red, p, 1), M);
-            v8_msub(g, M, prev);
+            ld16s(rr + RWE, M);
+            mv_add(M, gt, f);
          }
-         ldm8(red_row(red, p, 0), M);
-         m8_solve(M, g, 1);
-         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+         ld16s(rr + RWS, M);
+         mv_add(M, f, v);
+         const LUf su = luf_load(rr + RS);
+         luf_solve(su, v[0], v[1], v[2], v[3]);
+         ld16s(rr + RX, M);
+         mv_sub(M, v, f);
+#pragma unroll
+         for (int c = 0; c < 4; c++) { zs[8 * p + c] = f[c]; zs[8 * p + 4 + c] = v[c]; gt[c] = f[c]; }
       }
+      // a_p: only atop_{P-2} and abot_0 enter Z_{P-1}, so the recurrence
+      // carries the bottom rows
+      float at[4], ab[4], an[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) { at[c] = zs[8 * (P - 2) + c]; ab[c] = zs[8 * (P - 2) + 4 + c]; }
+      const float yeL[4] = {ry[8 * (P - 1) + 4], ry[8 * (P - 1) + 5], ry[8 * (P - 1) + 6], ry[8 * (P - 1) + 7]};
+      const float ys0[4] = {ry[0], ry[1], ry[2], ry[3]};
+      const float atL[4] = {at[0], at[1], at[2], at[3]};
       for (int p = P - 3; p >= 0; p--) {
-         float nx[8];
-         for (int k = 0; k < 8; k++) { g[k] = zs[8 * p + k]; nx[k] = zs[8 * (p + 1) + k]; }
-         ldm8(red_row(red, p, 2), M);
-         v8_msub(g, M, nx);
-         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+         const float* rr = red_s + kRedRow * p;
+         float M[16], ub[4];
+#pragma unroll
+         for (int c = 0; c < 4; c++) { ub[c] = zs[8 * p + 4 + c]; an[c] = ab[c]; }
+         ld16s(rr + RGB, M);
+         mv_sub(M, an, ub);
+#pragma unroll
+         for (int c = 0; c < 4; c++) ab[c] = ub[c];
       }
-      const float* last = red + 256 * (kSpikeMaxSeg - 1);
-      float z[8], a0[8], ap[8];
-      for (int k = 0; k < 4; k++) {
-         z[k] = ry[8 * (P - 1) + 4 + k];
-         z[4 + k] = ry[k];
+      // ab = abot_0
+      float z[8], M[16];
+      const float* last = red_s + kRedLast;
+#pragma unroll
+      for (int c = 0; c < 4; c++) { z[c] = yeL[c]; z[4 + c] = ys0[c]; }
+      {
+         float zt[4] = {z[0], z[1], z[2], z[3]}, zb[4] = {z[4], z[5], z[6], z[7]};
+         ld16s(last + 64, M);
+         mv_add(M, atL, zt);
+         ld16s(last + 80, M);
+         mv_add(M, ab, zb);
+#pragma unroll
+         for (int c = 0; c < 4; c++) { z[c] = zt[c]; z[4 + c] = zb[c]; }
       }
-      for (int k = 0; k < 8; k++) { ap[k] = zs[8 * (P - 2) + k]; a0[k] = zs[k]; }
-      ldm8(last + 64, M);
-      v8_msub(z, M, ap);
-      ldm8(last + 128, M);
-      v8_msub(z, M, a0);
-      ldm8(last, M);
-      m8_solve(M, z, 1);
-      for (int p = 0; p <= P - 2; p++) {
-         for (int k = 0; k < 8; k++) g[k] = zs[8 * p + k];
-         ldm8(red_row(red, p, 3), M);
-         for (int i = 0; i < 8; i++) {
-            float v = g[i];
-            for (int k = 0; k < 8; k++) v = __fmaf_rn(M[8 * i + k], z[k], v);
-            g[i] = v;
-         }
-         for (int k = 0; k < 8; k++) zs[8 * p + k] = g[k];
+      m8_solve(last, z);
+      const float ztop[4] = {z[0], z[1], z[2], z[3]};
+      float zb[4] = {z[4], z[5], z[6], z[7]};   // bottom of Z_{p+1} (Z_{P-1} = z first)
+#pragma unroll
+      for (int c = 0; c < 8; c++) zs[8 * (P - 1) + c] = z[c];
+      for (int p = P - 2; p >= 0; p--) {
+         const float* rr = red_s + kRedRow * p;
+         float ut[4], ub[4];
+#pragma unroll
+         for (int c = 0; c < 4; c++) { ut[c] = zs[8 * p + c]; ub[c] = zs[8 * p + 4 + c]; }
+         ld16s(rr + RGT, M);
+         mv_sub(M, zb, ut);
+         ld16s(rr + RGB, M);
+         mv_sub(M, zb, ub);
+         ld16s(rr + RHT, M);
+         mv_sub(M, ztop, ut);
+         ld16s(rr + RHB, M);
+         mv_sub(M, ztop, ub);
+#pragma unroll
+         for (int c = 0; c < 4; c++) { zs[8 * p + c] = ut[c]; zs[8 * p + 4 + c] = ub[c]; zb[c] = ub[c]; }
       }
-      for (int k = 0; k < 8; k++) zs[8 * (P - 1) + k] = z[k];
    }
    __syncwarp();
    if (lane < P) {
-      // x_i = y_i + V_i t_{p+1} + W_i b_{p-1}
+      // x_k = y_k + V_k t_{p+1} + W_k b_{p-1}; row k+1's data loaded while
+      // row k is formed
       float tn[4], bp[4];
       const int pm = (lane == 0) ? P - 1 : lane - 1;
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-         tn[k] = zs[8 * lane + 4 + k];
-         bp[k] = zs[8 * pm + k];
+      for (int c = 0; c < 4; c++) {
+         tn[c] = zs[8 * lane + 4 + c];
+         bp[c] = zs[8 * pm + c];
       }
-      for (int i = s; i <= e; i++) {
-         const float* rec = d.sp_fac + (size_t)kSpRec * (rec0 + i);
-         float v[16], w[16], x[4];
-         ld16f(rec + 48, v);
-         ld16f(rec + 64, w);
-         ld4(d.sp_y + 4 * (size_t)(rec0 + i), x);
+      const int* scell = d.row_scell + row0 + s;
+      float v[16], w[16], x[4];
+      ld16t(d.sp_fac + tix(R0, kSpRec, 48, lane), v);
+      ld16t(d.sp_fac + tix(R0, kSpRec, 64, lane), w);
 #pragma unroll
-         for (int k = 0; k < 4; k++)
+      for (int c = 0; c < 4; c++) x[c] = d.sp_y[tix(R0, 4, c, lane)];
+      int sc = scell[0];
+      for (int k = 0; k < n; k++) {
+         float vn[16], wn[16], xn[4];
+         int scn = 0;
+         if (k + 1 < n) {
+            ld16t(d.sp_fac + tix(R0 + k + 1, kSpRec, 48, lane), vn);
+            ld16t(d.sp_fac + tix(R0 + k + 1, kSpRec, 64, lane), wn);
 #pragma unroll
-            for (int j = 0; j < 4; j++) x[k] = __fmaf_rn(v[4 * k + j], tn[j], __fmaf_rn(w[4 * k + j], bp[j], x[k]));
-         st4(d.r32 + 4 * (size_t)d.row_scell[row0 + i], x);
+            for (int c = 0; c < 4; c++) xn[c] = d.sp_y[tix(R0 + k + 1, 4, c, lane)];
+            scn = scell[k + 1];
+         }
+         mv_add(w, bp, x);
+         mv_add(v, tn, x);
+         st4(d.r32 + 4 * (size_t)sc, x);
+         if (k + 1 < n) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) { v[m] = vn[m]; w[m] = wn[m]; }
+#pragma unroll
+            for (int c = 0; c < 4; c++) x[c] = xn[c];
+            sc = scn;
+         }
       }
    }
 }
