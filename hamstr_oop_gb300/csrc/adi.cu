@@ -125,53 +125,6 @@ __device__ __forceinline__ int take_job(int* ctr, int lane)
    return __shfl_sync(kLaneMask, k, 0);
 }
 
-// persistent warps, one or two per SM sub-partition, taking jobs from the
-// factorisation's queue (longest first) until it is empty; a zero or
-// non-finite pivot raises DEV_ERR_PIVOT (the factors are still stored, as
-// the reference divides regardless)
-template <bool SD>
-__global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
-{
-   if (halted(d)) return;
-   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-   if (w >= nwarps) return;
-   const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
-   int* ctr = d.sched_ctr;
-   bool bad = false;
-   for (int k = take_job(ctr, lane); k < nj;) {
-      // the next job's index is fetched while this one runs
-      int kn = 0;
-      if (lane == 0) kn = atomicAdd(ctr, 1);
-      const int job = d.sched_job_ptr[j0 + k];
-      const int ich = d.sched_jobs[job];
-      if (ich & kBundleJob) {
-         const int n = ich & 63;
-         if (lane < n) {
-            const int c = d.sched_jobs[job + 1 + lane];
-            if (!frozen_chain(d, c)) {
-               const int row0 = d.chain_row0[c];
-               bad |= factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c],
-                                             d.fac + (size_t)kFacRec * row0);
-            }
-         }
-      } else if (ich & kQuadJob) {
-         int c = 0, N = 0;
-         if ((lane >> 2) < (ich & 63)) {
-            c = d.sched_jobs[job + 1 + (lane >> 2)];
-            N = live_rows(d, c);
-         }
-         const int row0 = d.chain_row0[c];
-         bad |= factor_line_quad<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
-      } else if (ich & kPairJob) {
-         bad |= factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
-      } else if (!frozen_chain(d, ich)) {
-         bad |= factor_chain<SD>(d, ich, lane);
-      }
-      k = __shfl_sync(kLaneMask, kn, 0);
-   }
-   if (__any_sync(kLaneMask, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
-}
-
 // one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the
 // replay, and the write-back r[scell] = F (ADI.cpp:232-244)
 __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int lane)
@@ -223,6 +176,101 @@ __device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib,
    }
 }
 
+// the factorisation of one job (entries at `job`, first entry `ich`
+// without kFusedJob); returns whether a pivot was zero or not finite
+template <bool SD>
+__device__ __forceinline__ bool factor_job(const DeviceState& d, int job, int ich, int lane)
+{
+   bool bad = false;
+   if (ich & kBundleJob) {
+      const int n = ich & 63;
+      if (lane < n) {
+         const int c = d.sched_jobs[job + 1 + lane];
+         if (!frozen_chain(d, c)) {
+            const int row0 = d.chain_row0[c];
+            bad |= factor_line_thread<SD>(d.blk + 48 * (size_t)row0, 48, d.chain_nrows[c],
+                                          d.fac + (size_t)kFacRec * row0);
+         }
+      }
+   } else if (ich & kQuadJob) {
+      int c = 0, N = 0;
+      if ((lane >> 2) < (ich & 63)) {
+         c = d.sched_jobs[job + 1 + (lane >> 2)];
+         N = live_rows(d, c);
+      }
+      const int row0 = d.chain_row0[c];
+      bad |= factor_line_quad<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
+   } else if (ich & kPairJob) {
+      bad |= factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
+   } else if (!frozen_chain(d, ich)) {
+      bad |= factor_chain<SD>(d, ich, lane);
+   }
+   return bad;
+}
+
+// one sweep's solve of one job (as factor_job)
+__device__ __forceinline__ void solve_job(const DeviceState& d, int job, int ich, int lane)
+{
+   if (ich & kBundleJob) {
+      const int n = ich & 63;
+      if (lane < n) {
+         const int c = d.sched_jobs[job + 1 + lane];
+         if (!frozen_chain(d, c)) {
+            const int row0 = d.chain_row0[c];
+            solve_line_thread(d.fac + (size_t)kFacRec * row0, d.chain_nrows[c], d.r, d.row_fcell + row0,
+                              d.row_scell + row0, d.fsc + 4 * (size_t)row0);
+         }
+      }
+   } else if (ich & kQuadJob) {
+      int c = 0, N = 0;
+      if ((lane >> 2) < (ich & 63)) {
+         c = d.sched_jobs[job + 1 + (lane >> 2)];
+         N = live_rows(d, c);
+      }
+      const int row0 = d.chain_row0[c];
+      solve_line_quad(d.fac + (size_t)kFacRec * row0, N, d.r, d.row_fcell + row0, d.row_scell + row0,
+                      d.fsc + 4 * (size_t)row0, lane);
+   } else if (ich & kPairJob) {
+      solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
+   } else if (!frozen_chain(d, ich)) {
+      solve_chain(d, ich, lane);
+   }
+}
+
+// persistent warps, one or two per SM sub-partition, taking jobs from the
+// factorisation's queue (longest first) until it is empty; a zero or
+// non-finite pivot raises DEV_ERR_PIVOT (the factors are still stored, as
+// the reference divides regardless).  A job marked kFusedJob (the first
+// wave's chains, when the schedule fuses) is solved for the first sweep by
+// the same warp right after its factorisation: its right-hand sides are
+// the computeRHS residuals, ready before this kernel, and the chains of
+// one wave share no cell, so no other job waits for it.
+template <bool SD>
+__global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
+{
+   if (halted(d)) return;
+   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+   if (w >= nwarps) return;
+   const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
+   int* ctr = d.sched_ctr;
+   bool bad = false;
+   for (int k = take_job(ctr, lane); k < nj;) {
+      // the next job's index is fetched while this one runs
+      int kn = 0;
+      if (lane == 0) kn = atomicAdd(ctr, 1);
+      const int job = d.sched_job_ptr[j0 + k];
+      const int head = d.sched_jobs[job], ich = head & ~kFusedJob;
+      bad |= factor_job<SD>(d, job, ich, lane);
+      if (head & kFusedJob) {
+         __syncwarp();   // the records of every lane are written
+         solve_job(d, job, ich, lane);
+      }
+      k = __shfl_sync(kLaneMask, kn, 0);
+   }
+   if (__any_sync(kLaneMask, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
+}
+
+
 __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sweep, int wave, int nwarps)
 {
    if (halted(d)) return;
@@ -234,31 +282,7 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sw
       int kn = 0;
       if (lane == 0) kn = atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
-      const int ich = d.sched_jobs[job];
-      if (ich & kBundleJob) {
-         const int n = ich & 63;
-         if (lane < n) {
-            const int c = d.sched_jobs[job + 1 + lane];
-            if (!frozen_chain(d, c)) {
-               const int row0 = d.chain_row0[c];
-               solve_line_thread(d.fac + (size_t)kFacRec * row0, d.chain_nrows[c], d.r, d.row_fcell + row0,
-                                 d.row_scell + row0, d.fsc + 4 * (size_t)row0);
-            }
-         }
-      } else if (ich & kQuadJob) {
-         int c = 0, N = 0;
-         if ((lane >> 2) < (ich & 63)) {
-            c = d.sched_jobs[job + 1 + (lane >> 2)];
-            N = live_rows(d, c);
-         }
-         const int row0 = d.chain_row0[c];
-         solve_line_quad(d.fac + (size_t)kFacRec * row0, N, d.r, d.row_fcell + row0, d.row_scell + row0,
-                         d.fsc + 4 * (size_t)row0, lane);
-      } else if (ich & kPairJob) {
-         solve_pair(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
-      } else if (!frozen_chain(d, ich)) {
-         solve_chain(d, ich, lane);
-      }
+      solve_job(d, job, d.sched_jobs[job], lane);
       k = __shfl_sync(kLaneMask, kn, 0);
    }
 }

@@ -93,6 +93,8 @@ struct hamstr_gpu {
    Schedule sched;
    int msweep = 1;
    cudaStream_t stream = nullptr;
+   cudaStream_t stream2 = nullptr;      // side stream: parallel branches of the FP32 step
+   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
    std::vector<void*> owned;
    cudaGraphExec_t step_exec = nullptr;
    cudaGraph_t step_graph = nullptr;
@@ -111,6 +113,7 @@ struct hamstr_gpu {
    int nsm = 1;                         // SMs of the device (persistent-warp schedules)
    int adi_lanes = 4;                   // lanes per open chain in the FP64 line kernels: 32, 16 or 4
    int adi_bundle = 0;                  // open chains of up to this many rows one per lane (0: none)
+   int adi_fuse = 1;                    // first wave's first-sweep solve inside the factorisation kernel
    // order 5, FP64: the WENO linearisation's f-only values kept from the
    // implicit computeRHS for the sweeps (d.wlin points here when on)
    double* wlin_buf = nullptr;
@@ -151,14 +154,32 @@ struct hamstr_gpu {
       L("rhs_cell", n, [&] { launch_rhs_cell(d, true, stream); });
       L("norm_final", n, [&] { launch_norm_final(d, 0, check_tol, stream); });
       L("mx_init", n, [&] { launch_mx_init(d, stream); });
+      // the segmented chains' kernels touch no chain of the others and no
+      // cell of another chain of their wave, so they run beside them on the
+      // side stream (a parallel branch of the captured graph); per-kernel
+      // timing keeps them in line
+      const bool side = d.sp_on && d.nSpike > 0 && !prof;
+      cudaStream_t sst = side ? stream2 : stream;
+      if (side) {
+         CK(cudaEventRecord(ev_fork, stream));
+         CK(cudaStreamWaitEvent(stream2, ev_fork, 0));
+      }
+      if (d.sp_on && d.nSpike > 0) L("mx_spike_factor", n, [&] { launch_mx_spike_factor(d, sst); });
       if (!d.mx_fused) L("mx_assemble", n, [&] { launch_mx_assemble(d, stream); });
       L("mx_factor", n, [&] { launch_mx_factor(d, stream); });
-      if (d.sp_on && d.nSpike > 0) L("mx_spike_factor", n, [&] { launch_mx_spike_factor(d, stream); });
       for (int s = 0; s < msweep; s++) {
          for (int w = 0; w < plan.nWave; w++) {
-            L("mx_solve", n, [&] { launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream); });
             const int c0 = sp_wave_ptr[w], cnt = sp_wave_ptr[w + 1] - c0;
-            if (d.sp_on && cnt > 0) L("mx_spike_solve", n, [&] { launch_mx_spike_solve(d, c0, cnt, stream); });
+            if (side && (s > 0 || w > 0) && cnt > 0) {
+               CK(cudaEventRecord(ev_fork, stream));
+               CK(cudaStreamWaitEvent(stream2, ev_fork, 0));
+            }
+            if (d.sp_on && cnt > 0) L("mx_spike_solve", n, [&] { launch_mx_spike_solve(d, c0, cnt, sst); });
+            L("mx_solve", n, [&] { launch_mx_solve(d, plan.wave_ptr[w], plan.wave_ptr[w + 1] - plan.wave_ptr[w], stream); });
+            if (side && (cnt > 0 || (s == 0 && w == 0))) {
+               CK(cudaEventRecord(ev_join, stream2));
+               CK(cudaStreamWaitEvent(stream, ev_join, 0));
+            }
          }
          L("mx_dq_update", n, [&] { launch_mx_dq_update(d, stream); });
          L("mx_lin_face", n, [&] { launch_mx_lin_face(d, stream); });
@@ -272,7 +293,8 @@ struct hamstr_gpu {
       L("adi_assemble", n, [&] { launch_adi_assemble(d, stream); });
       adi_factor_launches(n);
       for (int s = 0; s < msweep; s++) {
-         for (int w = 0; w < plan.nWave; w++) adi_solve_launches(s, w, n);
+         for (int w = 0; w < plan.nWave; w++)
+            if (!(adi_fuse && s == 0 && w == 0)) adi_solve_launches(s, w, n);   // fused: done by adi_factor
          L("dq_update", n, [&] { launch_dq_update(d, stream); });
          if (d.recon == 5 && d.lin_order != 1) L("lin_recon5", n, [&] { launch_lin_recon5(d, true, stream); });
          L("lin_face", n, [&] { launch_lin_face(d, stream); });
@@ -329,7 +351,7 @@ struct hamstr_gpu {
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int lanes,
-                   int wkeep, int bundle, int chunk, int spike)
+                   int wkeep, int bundle, int chunk, int spike, int fuse)
    {
       d.sp_on = spike;
       if (wkeep && d.recon == 5) {
@@ -348,10 +370,11 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb || lanes != adi_lanes || bundle != adi_bundle) {
+      if (adi_wpb != d.adi_wpb || lanes != adi_lanes || bundle != adi_bundle || fuse != adi_fuse) {
          adi_lanes = lanes;
          adi_bundle = bundle;
-         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle);
+         adi_fuse = fuse;
+         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle, fuse != 0);
          const int st = upload_schedule();
          if (st) return st;
       }
@@ -643,7 +666,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       // the shortest open chains one per lane where chains are short (the
       // autotuner checks the alternatives)
       g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 8 : 0;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle);
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle, g->adi_fuse != 0);
    }
    TRY(g->upload_schedule());
    d.nWave = P.nWave;
@@ -683,6 +706,9 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
    TRY(dalloc(&g->wall_scr, 3 * wall_cell.size() + 3 * (size_t)ni, o));
 #undef TRY
    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream2, cudaStreamNonBlocking);
+   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming);
+   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->ev_join, cudaEventDisableTiming);
    if (e != cudaSuccess) {
       set_error(cudaGetErrorString(e));
       hamstr_gpu_destroy(g);
@@ -729,7 +755,11 @@ int hamstr_gpu_destroy(hamstr_gpu* g)
    if (g->stream) cudaStreamSynchronize(g->stream);
    if (g->step_exec) cudaGraphExecDestroy(g->step_exec);
    if (g->step_graph) cudaGraphDestroy(g->step_graph);
+   if (g->stream2) cudaStreamSynchronize(g->stream2);
    for (void* p : g->owned) cudaFree(p);
+   if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+   if (g->ev_join) cudaEventDestroy(g->ev_join);
+   if (g->stream2) cudaStreamDestroy(g->stream2);
    if (g->stream) cudaStreamDestroy(g->stream);
    delete g;
    return HAMSTR_GPU_OK;
@@ -846,7 +876,8 @@ int hamstr_gpu_adi(hamstr_gpu* g, double* l2, double* linf)
    const Schedule& S = g->sched;
    launch_adi_factor(d, S.nwarps[0], g->stream);
    for (int s = 0; s < g->msweep; s++) {
-      for (int w = 0; w < g->plan.nWave; w++) launch_adi_solve(d, s, w, S.nwarps[1 + w], g->stream);
+      for (int w = 0; w < g->plan.nWave; w++)
+         if (!(g->adi_fuse && s == 0 && w == 0)) launch_adi_solve(d, s, w, S.nwarps[1 + w], g->stream);
       launch_dq_update(d, g->stream);
       launch_lin_recon5(d, g->wlin_valid, g->stream);
       launch_lin_face(d, g->stream);
@@ -1192,7 +1223,8 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    CK(cudaEventCreate(&e1));
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
-      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, c.spike)))
+      if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, c.spike,
+                               g->adi_fuse)))
          break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
@@ -1215,7 +1247,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
-                       best->bundle, ck, best->spike);
+                       best->bundle, ck, best->spike, g->adi_fuse);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1248,7 +1280,7 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
                                   d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle, g->mx_chunk,
-                                  d.sp_on};
+                                  d.sp_on,      g->adi_fuse};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1261,12 +1293,12 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
                    (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1) &&
-                   (s[10] == 0 || s[10] == 1);
+                   (s[10] == 0 || s[10] == 1) && (s[11] == 0 || s[11] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], s[10]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], s[10], s[11]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

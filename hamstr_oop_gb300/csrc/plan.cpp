@@ -314,7 +314,7 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows)
+Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows, bool fuse_first_wave)
 {
    Schedule S;
    S.job_ptr.push_back(0);
@@ -323,12 +323,12 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
    // (latency; the factorisation's block LU about three times the solve's),
    // a row of a bundle is ~274 (factorisation) or ~92 (solve) FP64 warp
    // instructions issued back to back
-   auto assign = [&](const std::vector<int>& chains, bool factor) {
-      const double row_warp = factor ? 6.0 : 2.0, row_bundle = factor ? 22.0 : 7.4;
+   struct Job { double cost; std::vector<int> entries; };
+   // the jobs of one chain set, with their cost per row of the longest chain
+   auto pack = [&](const std::vector<int>& chains, double row_warp, double row_bundle) {
       std::vector<int> sorted(chains);
       std::stable_sort(sorted.begin(), sorted.end(),
                        [&](int a, int b) { return p.chain_nrows[a] > p.chain_nrows[b]; });
-      struct Job { double cost; std::vector<int> entries; };
       std::vector<Job> order;
       std::vector<int> bundle, group;
       auto flush = [&](std::vector<int>& v, int flag, double row_cost) {
@@ -362,6 +362,9 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
       }
       flush(bundle, kBundleJob, row_bundle);
       flush(group, group_flag, row_warp);
+      return order;
+   };
+   auto emit = [&](std::vector<Job>& order) {
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
       S.job0.push_back((int)S.job_ptr.size() - 1);
       S.njobs.push_back((int)order.size());
@@ -371,12 +374,28 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
          S.job_ptr.push_back((int)S.jobs.size());
       }
    };
-   std::vector<int> all(p.nChain);
-   for (int c = 0; c < p.nChain; c++) all[c] = c;
-   assign(all, true);
+   auto wave = [&](int w) {
+      return std::vector<int>(p.wave_chains.begin() + p.wave_ptr[w], p.wave_chains.begin() + p.wave_ptr[w + 1]);
+   };
+   constexpr double kFacWarp = 6.0, kFacBundle = 22.0, kSolWarp = 2.0, kSolBundle = 7.4;
+   // schedule 0, the factorisation: all chains; fused, the first wave's jobs
+   // are packed as its solve packs them and carry that solve as well
+   std::vector<Job> fac;
+   if (fuse_first_wave && p.nWave > 0) {
+      fac = pack(wave(0), kFacWarp + kSolWarp, kFacBundle + kSolBundle);
+      for (Job& j : fac) j.entries[0] |= kFusedJob;
+      std::vector<int> rest(p.wave_chains.begin() + p.wave_ptr[1], p.wave_chains.end());
+      std::vector<Job> more = pack(rest, kFacWarp, kFacBundle);
+      fac.insert(fac.end(), more.begin(), more.end());
+   } else {
+      std::vector<int> all(p.nChain);
+      for (int c = 0; c < p.nChain; c++) all[c] = c;
+      fac = pack(all, kFacWarp, kFacBundle);
+   }
+   emit(fac);
    for (int w = 0; w < p.nWave; w++) {
-      std::vector<int> cs(p.wave_chains.begin() + p.wave_ptr[w], p.wave_chains.begin() + p.wave_ptr[w + 1]);
-      assign(cs, false);
+      std::vector<Job> sol = pack(wave(w), kSolWarp, kSolBundle);
+      emit(sol);
    }
    return S;
 }

@@ -83,16 +83,21 @@ std::string build_plan(const MeshInput& in, Plan& out);
 //     (open_lanes = 4);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
 //     bundle_rows rows, one per lane.
-// nwarps[s] = min(njobs[s], max_warps) warps are launched.
+// nwarps[s] = min(njobs[s], max_warps) warps are launched.  With
+// fuse_first_wave the factorisation's jobs for the first wave's chains are
+// packed as that wave's solve packs them and carry kFusedJob on their first
+// entry: the warp that factors them runs their first sweep's solve at once.
 constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;
 constexpr int kQuadJob = 1 << 28;
+constexpr int kFusedJob = 1 << 27;
 struct Schedule {
    std::vector<int> job0, njobs, nwarps;   // per schedule
    std::vector<int> job_ptr;               // per job (all schedules), +1
    std::vector<int> jobs;                  // job entries, as above
 };
-Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows);
+Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows,
+                        bool fuse_first_wave = false);
 
 }  // namespace hamstr
 #endif

@@ -479,7 +479,7 @@ class GpuSolver:
         return json.loads(buf.value.decode())
 
     SHAPE_KEYS = ("face_block", "adi_warps_per_sm", "mx_block", "mx_fused", "face_softdiv", "pivot_softdiv",
-                  "adi_open_lanes", "weno_keep", "adi_bundle_rows", "mx_chunk", "mx_spike")
+                  "adi_open_lanes", "weno_keep", "adi_bundle_rows", "mx_chunk", "mx_spike", "adi_fuse")
 
     def shape(self) -> dict:
         """The launch shape in use (hamstr_gpu_get_shape), keyed as the autotuner's report."""

@@ -253,9 +253,14 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       The same linear system; in FP32 the rounding differs, so the FP32
  *       form's iterates differ in the last bits and its steady state (the
  *       FP64 residual's zero) does not.
+ *  [11] FP64 line kernels: the first wave's chains solved for the first
+ *       sweep by the warp that has just factored them, inside the
+ *       factorisation kernel (the other chains' factorisation goes on
+ *       beside them), instead of by a separate launch: 0 or 1 (default 1;
+ *       not tuned)
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); FP64
  * results do not depend on the shape. */
-#define HAMSTR_SHAPE_N 11
+#define HAMSTR_SHAPE_N 12
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

@@ -23,6 +23,9 @@ FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_so
                     adi_bundle_rows=bu)
                for fb in (128, 256) for w in (4, 8) for fs in (0, 1) for ps in (0, 1) for ln in (32, 16, 4)
                for bu in (0, 4, 64)]
+# with the first wave's first-sweep solve in its own launch (the default
+# runs it inside the factorisation kernel)
+FP64_SHAPES += [dict(sh, adi_fuse=0) for sh in FP64_SHAPES[::4]]
 
 
 @pytest.mark.parametrize("order,split", [(3, 0.5), (5, 0.5), (5, 0.0)])
@@ -54,7 +57,7 @@ def test_set_shape_rejects_bad_values(make_case, native_lib):
     g = native.GpuSolver(native.Case(make_case(16, 4, order=1, CFL=5.0)))
     before = g.shape()
     for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_open_lanes=8), dict(adi_bundle_rows=65),
-                dict(mx_spike=2)):
+                dict(mx_spike=2), dict(adi_fuse=2)):
         with pytest.raises(native.HamstrError):
             g.set_shape(**bad)
     assert g.shape() == before

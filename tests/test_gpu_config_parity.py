@@ -44,7 +44,8 @@ BATCH_MESHES = ((128, 32), (256, 64), (384, 96), (512, 128))
 # kernels' code paths, each set on top of the default shape
 SHAPES = ([dict(adi_bundle_rows=b) for b in (0, 4, 8, 16, 64)] +
           [dict(adi_open_lanes=n) for n in (32, 16, 4)] +
-          [dict(adi_warps_per_sm=8), dict(face_block=256), dict(face_softdiv=0), dict(pivot_softdiv=1)])
+          [dict(adi_warps_per_sm=8), dict(face_block=256), dict(face_softdiv=0), dict(pivot_softdiv=1),
+           dict(adi_fuse=0)])
 
 
 @pytest.fixture(scope="module")

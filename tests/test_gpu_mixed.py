@@ -133,3 +133,19 @@ def test_segmented_periodic_solve_converges_to_the_oracle(make_case, oracle_lib,
     orc2.march(k)
     qo = orc2.get("q")
     assert np.max(np.abs(qa - qo)) / np.max(np.abs(qo)) <= FIELD_RTOL
+
+
+def test_segmented_branch_runs_beside_the_others(make_case, native_lib):
+    """In the captured FP32 step the segmented chains' kernels run on a
+    parallel branch beside the other chains' kernels; the per-kernel
+    profile launches everything in one line.  Both orders give the same
+    state bit for bit (the two touch disjoint chains and cells)."""
+    from hamstr_oop_gb300 import native
+    case = make_case(128, 8, order=3, CFL=10.0, msweep=2)
+    a, b = native.GpuSolver(native.Case(case)), native.GpuSolver(native.Case(case))
+    for g in (a, b):
+        g.set_precision(True)
+        assert g.shape()["mx_spike"] == 1
+    a.march(4, 0.0)
+    b.profile_step(4)
+    assert np.array_equal(a.get("q"), b.get("q"))

@@ -4,7 +4,9 @@ A small C++ program links the library, reads a case through the C ABI, builds th
 plan and the queues for every launch-shape choice, and checks what the kernels rely
 on: every chain of a launch's waves is in exactly one job; periodic chains run on a
 whole warp; pairs hold two open chains, quads up to 8, bundles up to 32 open chains of
-at most bundle_rows rows (longest first); no more warps than jobs."""
+at most bundle_rows rows (longest first); no more warps than jobs; with the first wave's
+first-sweep solve fused into the factorisation, exactly the factorisation queue's first-wave
+jobs carry the fused flag."""
 import os
 import subprocess
 
@@ -50,14 +52,18 @@ int main(int argc, char** argv) {
    for (int ch = 0; ch < p.nChain; ch++) nper += p.chain_periodic[ch];
    for (int maxw : {1, 7, 608})
       for (int lanes : {32, 16, 4})
-         for (int br : {0, 2, 8, 64}) {
-            const Schedule S = build_schedule(p, maxw, lanes, br);
+         for (int br : {0, 2, 8, 64})
+          for (int fuse : {0, 1}) {
+            const Schedule S = build_schedule(p, maxw, lanes, br, fuse != 0);
             if ((int)S.njobs.size() != 1 + p.nWave) return fail("schedules", (int)S.njobs.size(), p.nWave);
             for (int s = 0; s <= p.nWave; s++) {
                std::vector<int> seen(p.nChain, 0);
                for (int k = 0; k < S.njobs[s]; k++) {
                   const int b = S.job_ptr[S.job0[s] + k], e2 = S.job_ptr[S.job0[s] + k + 1];
-                  const int h = S.jobs[b];
+                  const int h = S.jobs[b] & ~kFusedJob;
+                  // fused jobs: factorisation queue only, fusing on, chains of the first wave only
+                  const bool fused = (S.jobs[b] & kFusedJob) != 0;
+                  if (fused && (s != 0 || !fuse)) return fail("fused flag", s, fuse);
                   std::vector<int> ids;
                   if (h & kBundleJob) {
                      const int n = h & 63;
@@ -84,6 +90,8 @@ int main(int argc, char** argv) {
                   }
                   for (int id : ids) {
                      if (id < 0 || id >= p.nChain) return fail("chain id", id, p.nChain);
+                     if (fused && p.chain_wave[id] != 0) return fail("fused wave", id, p.chain_wave[id]);
+                     if (s == 0 && fuse && p.chain_wave[id] == 0 && !fused) return fail("first wave unfused", id, 0);
                      if (s > 0 && p.chain_wave[id] != s - 1) return fail("wave", id, s - 1);
                      seen[id]++;
                   }
@@ -122,6 +130,6 @@ def test_line_job_queues(harness, make_case, ni, nj, split, extended):
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0 and out.stdout.startswith("OK"), out.stdout + out.stderr
     checked, nchain, nper, nwave = (int(x) for x in out.stdout.split()[1:])
-    assert checked == 3 * 3 * 4 * (1 + nwave) and nchain > 0
+    assert checked == 3 * 3 * 4 * 2 * (1 + nwave) and nchain > 0
     if split == 0.0:
         assert nper > 0                  # the plain O-grid has periodic loops beside open lines
