@@ -309,8 +309,14 @@ def run_batch(args, wl, rank, local_rank, world):
         # a plain run for ncu: N captured steps after two warm-up steps
         if args.shape:
             g.set_shape(**parse_shape(args.shape))
-        g.enqueue_steps(2 + args.profile_steps)
+        g.enqueue_steps(2)
         g.sync()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        g.enqueue_steps(args.profile_steps)
+        g.sync()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         if rank == 0:
             print(json.dumps({"profile_steps": args.profile_steps, "workload": wl["name"], "conditions": len(cases),
                               "cells": nc, "launches_per_step": g.launches_per_step()}), flush=True)
@@ -700,8 +706,16 @@ def run_gpu(args, wl, rank, local_rank, world):
         gpu.set_precision(args.profile_precision == "mixed")
         if args.shape:
             gpu.set_shape(**parse_shape(args.shape))
+        gpu.enqueue_steps(1)   # the graph is captured and warm before the profiled range
+        gpu.sync()
+        # only the profiled steps lie between profiler start and stop (for
+        # `ncu --profile-from-start off`; without a profiler these do nothing)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
         gpu.enqueue_steps(args.profile_steps)
         gpu.sync()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
         if rank == 0:
             print(json.dumps({"profile_steps": args.profile_steps, "precision": args.profile_precision,
                               "workload": wl["name"], "ramp_steps": sum(n for n, _ in wl["ramp"]),
