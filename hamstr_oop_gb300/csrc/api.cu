@@ -234,7 +234,7 @@ struct hamstr_gpu {
       if ((st = dalloc(&d.r032, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.dq32, 4 * nc, owned))) return st;
       if ((st = dalloc(&d.g32, 4 * (size_t)d.nSlot, owned))) return st;
-      // long periodic chains take the segmented solve: P segments of about
+      // long chains take the segmented solve: P segments of about
       // kSpikeRows rows each (at most kSpikeMaxSeg), grouped by wave; their
       // rows are tiled across the segments (sp_rec0 in tile rows)
       {
@@ -245,7 +245,7 @@ struct hamstr_gpu {
             for (int k = plan.wave_ptr[w]; k < plan.wave_ptr[w + 1]; k++) {
                const int c = plan.wave_chains[k];
                const int n = plan.chain_nrows[c];
-               if (!plan.chain_periodic[c] || n < kSpikeMinRows) continue;
+               if (n < (plan.chain_periodic[c] ? kSpikeMinRows : kSpikeMinOpenRows)) continue;
                const int P = std::min(kSpikeMaxSeg, n / kSpikeRows);
                chain_spike[c] = (int)sp_chain.size();
                sp_chain.push_back(c);
@@ -656,7 +656,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.adi_wpb = 4;
       d.mx_block = 64;
       d.mx_chunk_chains = mx_solve_chunk_capacity(d.mx_block);
-      d.sp_on = 1;   // long periodic chains of the FP32 form by segments
+      d.sp_on = 1;   // long periodic chains of the FP32 form by segments (2: long open ones too)
       // FP32 assembly inside the factorisation pays off on long chains, as
       // do the hardware pivot divisions (their latency is shorter per row)
       d.mx_fused = (P.nChain > 0 && P.nRow >= 16 * P.nChain) ? 1 : 0;
@@ -1195,7 +1195,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle, spike; float ms; };
    const int wk = g->weno_keep, ck = g->mx_chunk;
    std::vector<int> spikes = {d.sp_on};
-   if (g->mixed && d.nSpike > 0) spikes = {0, 1};
+   if (g->mixed && d.nSpike > 0) spikes = {0, 1, 2};
    std::vector<Cand> cands;
    for (int fb : {128, 256})
       for (int fsoft : {0, 1}) {
@@ -1293,7 +1293,7 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
                    (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1) &&
-                   (s[10] == 0 || s[10] == 1) && (s[11] == 0 || s[11] == 1);
+                   (s[10] >= 0 && s[10] <= 2) && (s[11] == 0 || s[11] == 1);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;

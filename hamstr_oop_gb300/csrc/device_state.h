@@ -38,11 +38,15 @@ struct FlowConst {
 
 constexpr int kWlinPerSlot = 2 * 4 * 18;   // sides x components x values (recon.cuh Weno5Lin)
 
-// FP32 form, segmented solve of long periodic chains: chains of at least
-// kSpikeMinRows rows, kSpikeRows rows per segment (at most kSpikeMaxSeg
-// segments, one warp lane each), kSpikeRedStride floats of boundary-system
-// factors per chain
+// FP32 form, segmented solve of long chains: periodic chains of at least
+// kSpikeMinRows rows and open chains of at least kSpikeMinOpenRows,
+// kSpikeRows rows per segment (at most kSpikeMaxSeg segments, one warp lane
+// each), kSpikeRedStride floats of boundary-system factors per chain.  An
+// open chain is the cyclic system with its two wrap-around couplings
+// (A of its first row, C of its last, which the open solve never reads)
+// set to zero.
 constexpr int kSpikeMinRows = 64;
+constexpr int kSpikeMinOpenRows = 32;
 constexpr int kSpikeRows = 16;
 constexpr int kSpikeMaxSeg = 32;
 constexpr int kSpikeRedStride = 256 * kSpikeMaxSeg;
@@ -131,13 +135,14 @@ struct DeviceState {
    float* g32;             // [nSlot][4] linear face fluxes
    int* line_chains;       // chains of each wave, longest first (thread per chain)
 
-   // FP32 form: long periodic chains solved by segments (spike.cuh).  A
-   // chain of N >= kSpikeMinRows rows is cut into P segments, one warp lane
-   // each; each lane factors its segment and the two "spikes" (its local
-   // responses to the couplings across its ends), and a small cyclic system
-   // on the segment boundaries joins them.  Same linear system as the
-   // sequential cyclic block Thomas, about N/P rows of latency instead of N.
-   int sp_on;              // 1: long periodic chains take the segmented solve (shape key)
+   // FP32 form: long chains solved by segments (mixed.cu).  A chain of N
+   // rows (periodic, N >= kSpikeMinRows; open, N >= kSpikeMinOpenRows) is
+   // cut into P segments, one warp lane each; each lane factors its segment
+   // and the two "spikes" (its local responses to the couplings across its
+   // ends), and a small cyclic system on the segment boundaries joins them.
+   // Same linear system as the sequential block Thomas, about N/P rows of
+   // latency instead of N.
+   int sp_on;              // 1: long chains take the segmented solve (shape key)
    int nSpike;             // chains solved by segments
    int* chain_spike;       // [nChain] index into the sp_* arrays, or -1
    int* sp_chain;          // [nSpike] chain id

@@ -119,6 +119,13 @@ __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
    d.blk32[t] = acc;
 }
 
+// whether chain ich takes the segmented solve: sp_on 1 takes the long
+// periodic chains, 2 the long open ones as well
+__device__ __forceinline__ bool spike_active(const DeviceState& d, int ich)
+{
+   return d.sp_on && d.chain_spike[ich] >= 0 && (d.sp_on == 2 || d.chain_periodic[ich]);
+}
+
 // the tiled index of element e of tile row s in lane `lane` of a W-wide array
 __device__ __forceinline__ size_t tix(int s, int W, int e, int lane)
 {
@@ -365,7 +372,7 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    const int t = blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= count || halted(d)) return;
    const int ich = d.line_chains[t];
-   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
+   if (frozen_chain(d, ich) || spike_active(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = t & 31, s0 = d.grp_row0[t >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    float A[16], B[16], C[16], cp[16], ap[16];
@@ -469,7 +476,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
    if (t >= count || halted(d)) return;
    const int p = first + t;
    const int ich = d.line_chains[p];
-   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
+   if (frozen_chain(d, ich) || spike_active(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    const int* fcell = d.row_fcell + row0;
@@ -616,7 +623,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
    if (t >= count || halted(d)) return;
    const int p = first + t;
    const int ich = d.line_chains[p];
-   if (frozen_chain(d, ich) || (d.sp_on && d.chain_spike[ich] >= 0)) return;
+   if (frozen_chain(d, ich) || spike_active(d, ich)) return;
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich], lane = p & 31, s0 = d.grp_row0[p >> 5];
    const bool per = d.chain_periodic[ich] != 0;
    const int* fcell = d.row_fcell + row0;
@@ -767,10 +774,13 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
    }
 }
 
-// ---------------- long periodic chains by segments ----------------------
+// ---------------- long chains by segments -------------------------------
 // A periodic chain of N rows (A_i x_{i-1} + B_i x_i + C_i x_{i+1} = f_i,
 // indices mod N) is cut into P segments of about N/P rows, one lane of a
-// warp each.  With D_p the block-tridiagonal matrix of segment p alone
+// warp each.  An open chain is the same system with A_0 and C_{N-1} (which
+// its solve never reads) set to zero: its first segment's W and its last
+// segment's V spikes vanish, and the cyclic boundary system below has zero
+// coupling across the wrap.  With D_p the block-tridiagonal matrix of segment p alone
 // (rows s..e), its solution is
 //     x_i = y_i + V_i x_{e+1} + W_i x_{s-1},
 // where D_p y = f, D_p V = -C_e (in the last row) and D_p W = -A_s (in the
@@ -904,8 +914,9 @@ __global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
    __shared__ __align__(16) float tips[kSpikeMaxSeg * 64];   // per segment: V_s, W_s, V_e, W_e
    const int sp = blockIdx.x, lane = threadIdx.x;
    const int ich = d.sp_chain[sp];
-   if (halted(d) || frozen_chain(d, ich)) return;
+   if (halted(d) || frozen_chain(d, ich) || !spike_active(d, ich)) return;
    const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], R0 = d.sp_rec0[sp];
+   const bool per = d.chain_periodic[ich] != 0;
    const int* seg = d.sp_seg + (kSpikeMaxSeg + 1) * sp;
    bool bad = false;
    if (lane < P) {
@@ -917,6 +928,11 @@ __global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
       float A[16], B[16], C[16], cp[16], gw[16];
       RowRef rnext = mx_rowref(d, row0 + s + 1);
       mx_row_ref(d, mx_rowref(d, row0 + s), A, B, C);
+      // an open chain: no coupling from its first row back to its last
+      if (!per && lane == 0) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) A[m] = 0.f;
+      }
       for (int k = 0; k < n; k++) {
          float An[16], Bn[16], Cn[16];
          if (k + 1 < n) {
@@ -948,8 +964,10 @@ __global__ void __launch_bounds__(32) mx_spike_factor_kernel(DeviceState d)
 #pragma unroll
             for (int m = 0; m < 16; m++) { cp[m] = C[m]; A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
          } else {
+            // (an open chain's last row has no coupling forward to its first)
+            const bool wrap = per || lane + 1 < P;
 #pragma unroll
-            for (int m = 0; m < 16; m++) C[m] = -C[m];
+            for (int m = 0; m < 16; m++) C[m] = wrap ? -C[m] : 0.f;
             luf_cols(u, C);
             st16t(rec + 32 * 48, C);
          }
@@ -1109,7 +1127,7 @@ __global__ void __launch_bounds__(32) mx_spike_solve_kernel(DeviceState d, int f
    __shared__ __align__(16) float zs[kSpikeMaxSeg * 8];   // Z_p = (b_p, t_{p+1})
    const int sp = first + blockIdx.x, lane = threadIdx.x;
    const int ich = d.sp_chain[sp];
-   if (halted(d) || frozen_chain(d, ich)) return;
+   if (halted(d) || frozen_chain(d, ich) || !spike_active(d, ich)) return;
    const int P = d.sp_nseg[sp], row0 = d.chain_row0[ich], R0 = d.sp_rec0[sp];
    const int* seg = d.sp_seg + (kSpikeMaxSeg + 1) * sp;
    {

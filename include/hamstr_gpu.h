@@ -217,8 +217,8 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * lane; FP32
  * line kernels 32..128 threads per block, with the blocks assembled by a
  * separate coalesced kernel or inside the factorisation, and, where there
- * are periodic chains of 64 rows or more, those solved by segments or not
- * (shape key 10); FP64 divisions of the face
+ * are long chains, those solved by segments or not (shape key 10); FP64
+ * divisions of the face
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
  * (bit-identical) -- and keeps the fastest.  The state is restored
  * afterwards; FP64 results do not depend on the shape.  report (may be
@@ -245,11 +245,12 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       the solve, 2 in the periodic elimination), where the launch's chains
  *       are all resident at once with the larger register count this takes:
  *       0 or 1 (default 1; not tuned)
- *  [10] FP32 line kernels: periodic chains of 64 rows or more solved by
- *       segments (16 rows each, up to 32, one warp lane per segment, joined
- *       by a small cyclic system on the segment ends) instead of one thread
- *       running the whole cyclic recurrence: 0 or 1 (default 1; tuned in
- *       the FP32 form where such chains exist).
+ *  [10] FP32 line kernels: long chains solved by segments (16 rows each,
+ *       up to 32, one warp lane per segment, joined by a small cyclic
+ *       system on the segment ends) instead of one thread running the whole
+ *       recurrence: 0 none, 1 periodic chains of 64 rows or more, 2 those
+ *       and open chains of 32 rows or more (default 1; tuned in the FP32
+ *       form where such chains exist).
  *       The same linear system; in FP32 the rounding differs, so the FP32
  *       form's iterates differ in the last bits and its steady state (the
  *       FP64 residual's zero) does not.

@@ -57,7 +57,7 @@ def test_set_shape_rejects_bad_values(make_case, native_lib):
     g = native.GpuSolver(native.Case(make_case(16, 4, order=1, CFL=5.0)))
     before = g.shape()
     for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_open_lanes=8), dict(adi_bundle_rows=65),
-                dict(mx_spike=2), dict(adi_fuse=2)):
+                dict(mx_spike=3), dict(adi_fuse=2)):
         with pytest.raises(native.HamstrError):
             g.set_shape(**bad)
     assert g.shape() == before

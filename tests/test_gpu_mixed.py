@@ -84,25 +84,33 @@ def test_chunked_fp32_solve_matches_row_by_row(make_case, native_lib, split, ord
         assert np.array_equal(ha, hb) and np.array_equal(a.get("q"), b.get("q")), fused
 
 
-def _spike_pair(make_case, ni, nj, **inputs):
-    """Two FP32-operator handles on one case: periodic loops by segments
-    (shape key mx_spike, the default) and by one thread each."""
+def _spike_pair(make_case, ni, nj, rule=0, **inputs):
+    """Two FP32-operator handles on one case: long chains by segments
+    (shape key mx_spike 2: periodic and open ones) and by one thread each."""
     from hamstr_oop_gb300 import native
     case = make_case(ni, nj, **inputs)
-    a, b = native.GpuSolver(native.Case(case)), native.GpuSolver(native.Case(case))
+    hosts = [native.Case(case), native.Case(case)]
+    for h in hosts:
+        h.set_option("chain_end_rule", rule)
+    a, b = native.GpuSolver(hosts[0]), native.GpuSolver(hosts[1])
     for g in (a, b):
         g.set_precision(True)
     assert a.shape()["mx_spike"] == 1
+    a.set_shape(mx_spike=2)
     b.set_shape(mx_spike=0)
     return case, a, b
 
 
-@pytest.mark.parametrize("ni,order", [(64, 1), (128, 3), (384, 1)])
-def test_segmented_periodic_solve_is_the_same_linear_solve(make_case, native_lib, ni, order):
-    """One step of the FP32 operator with the long periodic loops solved by
-    segments (4, 8 and 24 of them here) against the sequential cyclic solve:
-    the same linear system, so the increments agree to FP32 rounding."""
-    case, a, b = _spike_pair(make_case, ni, 8, order=order, CFL=10.0, msweep=2)
+@pytest.mark.parametrize("ni,nj,split,order", [(64, 8, 0.0, 1), (128, 8, 0.0, 3), (384, 8, 0.0, 1),
+                                              (64, 40, 0.0, 1), (96, 64, 0.5, 5)])
+def test_segmented_periodic_solve_is_the_same_linear_solve(make_case, native_lib, ni, nj, split, order):
+    """One step of the FP32 operator with the long chains solved by
+    segments against the sequential solve: periodic loops of 64, 128 and
+    384 rows (4, 8 and 24 segments), open lines of 40 rows (2 segments), and
+    the open chains of 32 rows or more on a half-split mesh.  The same
+    linear system, so the increments agree to FP32 rounding."""
+    case, a, b = _spike_pair(make_case, ni, nj, rule=1 if split else 0, split=split, seed=2, order=order,
+                             CFL=10.0, msweep=2)
     rng = np.random.default_rng(ni)
     q0 = a.get("q").reshape(-1, 4)
     q0 = (q0 * (1.0 + 0.01 * rng.standard_normal(q0.shape))).ravel()

@@ -163,3 +163,30 @@ def test_first_order_sweeps(make_case, oracle_lib, native_lib, order, mixed_prec
     gpu.set_sweep_order(0)
     with pytest.raises(Exception):
         gpu.set_sweep_order(2)
+
+
+def test_mixed_precision_order5_split_mesh_plateau(make_case, oracle_lib, native_lib):
+    """FP32 operator, WENO, half-split mesh, against the FP64 oracle.
+
+    On split meshes the WENO residual has no smooth zero: both forms stop at
+    the same L2 plateau (~4e-8 here) and circle there, so the check is that
+    the FP32-operator march reaches the oracle's plateau and that its state
+    lies within 1e-6 of the oracle's (first-order sweeps, whose plateau is
+    the residual's own; measured gaps 3e-9 .. 4e-8)."""
+    from hamstr_oop_gb300 import native
+    case = make_case(64, 16, split=0.5, seed=0, order=5, CFL=5.0, msweep=2, Mach=0.5, alpha=1.25)
+    orc = oracle_lib.OracleCase(case, "port")
+    orc.set_option("chain_end_rule", 1)
+    orc.set_option("sweep_order", 1)
+    host = native.Case(case)
+    host.set_option("chain_end_rule", 1)
+    gpu = native.GpuSolver(host)
+    gpu.set_sweep_order(1)
+    gpu.set_precision(True)
+    n = 3000
+    hg, _ = gpu.march(n, 0.0)
+    ho = orc.march(n)
+    lo, lg = ho[-1000:, 0].min(), hg[-1000:, 0].min()
+    assert lo < 1e-7 and abs(lg / lo - 1.0) < 0.2, (lo, lg)
+    qo, qg = orc.get("q"), gpu.get("q")
+    assert np.max(np.abs(qg - qo)) / np.max(np.abs(qo)) < 1e-6
