@@ -910,6 +910,25 @@ int hamstr_gpu_step(hamstr_gpu* g, double* norms4)
    return HAMSTR_GPU_OK;
 }
 
+int hamstr_gpu_step_host(hamstr_gpu* g, const double* q_in, double* q_out, double* norms4)
+{
+   if (!g) return HAMSTR_GPU_ERR_ARG;
+   g->wlin_valid = false;   // q changes: the kept WENO values no longer apply
+   int st = g->capture();
+   if (st) return st;
+   const size_t bytes = 4 * (size_t)g->d.nCell * sizeof(double);
+   if (q_in) CK(cudaMemcpyAsync(g->d.q, q_in, bytes, cudaMemcpyHostToDevice, g->stream));
+   st = g->reset_ctl(0.0);
+   if (st) return st;
+   CK(cudaGraphLaunch(g->step_exec, g->stream));
+   if (q_out) CK(cudaMemcpyAsync(q_out, g->d.q, bytes, cudaMemcpyDeviceToHost, g->stream));
+   double n[4];
+   st = g->read_norms(n, 4);   // norms and the status word, then the one synchronisation
+   if (st) return st;
+   if (norms4) std::memcpy(norms4, n, sizeof(n));
+   return HAMSTR_GPU_OK;
+}
+
 int hamstr_gpu_march(hamstr_gpu* g, int nsteps, double tol, double* hist, int* evals, int* converged)
 {
    if (!g || nsteps < 0) return HAMSTR_GPU_ERR_ARG;

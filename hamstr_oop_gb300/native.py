@@ -102,6 +102,7 @@ def load(build_if_missing: bool = False):
         "hamstr_gpu_adi": (i, [vp, ctypes.POINTER(d), ctypes.POINTER(d)]),
         "hamstr_gpu_linear_rhs": (i, [vp, ctypes.POINTER(d), ctypes.POINTER(d)]),
         "hamstr_gpu_step": (i, [vp, vp]),
+        "hamstr_gpu_step_host": (i, [vp, vp, vp, vp]),
         "hamstr_gpu_march": (i, [vp, i, d, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
         "hamstr_gpu_stream": (vp, [vp]),
         "hamstr_gpu_step_explicit": (i, [vp, i, vp]),
@@ -546,6 +547,21 @@ class GpuSolver:
     def step(self) -> np.ndarray:
         out = np.zeros(4)
         _check(load().hamstr_gpu_step(self.h, _ptr(out)))
+        return out
+
+    def step_host(self, q_in: np.ndarray = None, q_out: np.ndarray = None) -> np.ndarray:
+        """One step on a host-resident solution (hamstr_gpu_step_host): q_in
+        (or None: keep the device state) in, q_out (or None) out, one
+        synchronisation.  Both are contiguous float64 arrays of 4*nCell
+        values; page-locked ones (e.g. a pinned torch tensor's numpy view)
+        copy at full speed."""
+        n = 4 * self.sizes["nCell"]
+        for a in (q_in, q_out):
+            if a is not None and (a.dtype != np.float64 or a.size != n or not a.flags["C_CONTIGUOUS"]):
+                raise ValueError("q needs a contiguous float64 array of %d values" % n)
+        out = np.zeros(4)
+        _check(load().hamstr_gpu_step_host(self.h, None if q_in is None else _ptr(q_in),
+                                           None if q_out is None else _ptr(q_out), _ptr(out)))
         return out
 
     def march(self, nsteps: int, tol: float = 0.0):

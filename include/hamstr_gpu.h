@@ -145,6 +145,13 @@ int hamstr_gpu_linear_rhs(hamstr_gpu* g, double* l2, double* linf);
 /* SOLVER::stepSolution, ADI branch (march.cpp:381-386):
  * norms4 = {computeRHS L2, Linf, final linear L2, Linf}. */
 int hamstr_gpu_step(hamstr_gpu* g, double* norms4);
+/* The same step on a host-resident solution, as the reference's
+ * stepSolution works on its host q (march.cpp:66): q_in [nCell][4] (NULL:
+ * keep the device state) is copied in, the step runs, and q_out (NULL: no
+ * copy) and norms4 (may be NULL) come back, with one synchronisation of the
+ * handle's stream for all of it.  Host buffers should be page-locked for
+ * the copies to overlap nothing else and run at full speed. */
+int hamstr_gpu_step_host(hamstr_gpu* g, const double* q_in, double* q_out, double* norms4);
 /* SOLVER::marchInTime (march.cpp:15-59) with a convergence stop: runs up
  * to nsteps steps; stops before the ADI of the first step whose computeRHS
  * L2 norm is <= tol (tol <= 0: never) -- on a batched handle, the first

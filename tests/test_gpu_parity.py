@@ -126,6 +126,28 @@ def test_step_history_bitexact(make_case, oracle_lib, native_lib, order):
         _eq(gpu.get(name), orc.get(name), name)
 
 
+def test_step_on_host_buffers_bitexact(make_case, oracle_lib, native_lib):
+    """hamstr_gpu_step_host: the oracle's state goes in from a page-locked
+    host buffer each step, the step's q comes back into it; equal to the
+    oracle step by step (q, norms), and q_in = NULL keeps the device state."""
+    import torch
+    orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 32, 8, order=3, CFL=10.0, msweep=2)
+    n = 4 * gpu.sizes["nCell"]
+    buf = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    for it in range(4):
+        buf[:] = orc.get("q")
+        hg = gpu.step_host(buf, buf)
+        ho = orc.step()
+        _eq(buf, orc.get("q"), "q step %d" % it)
+        _norm_close(hg[0], ho[0], "rhs L2 step %d" % it)
+        assert hg[1] == ho[1] and hg[3] == ho[3]
+    hg = gpu.step_host(None, None)
+    orc.step()
+    _eq(gpu.get("q"), orc.get("q"), "q after a step on the device state")
+    with pytest.raises(ValueError):
+        gpu.step_host(np.zeros(n - 4), None)
+
+
 def test_march_matches_steps_and_stops(make_case, oracle_lib, native_lib):
     orc, host, gpu = _pair(make_case, oracle_lib, native_lib, 32, 8, order=1, CFL=10.0, msweep=2)
     hist_o = orc.march(30)
