@@ -117,12 +117,30 @@ __device__ __forceinline__ bool factor_pair(const DeviceState& d, int ia, int ib
    return factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
 }
 
+// Where a schedule has outlier jobs (ncrit > 0), the first warp of block b
+// (one block per SM) starts with job b, so each outlier starts on an SM of
+// its own, and the other warps of the ncrit blocks holding them take no
+// job; the counter then numbers the jobs after the assigned ones (off =
+// the number of blocks).  Otherwise every warp takes every job from the
+// counter (off = 0): with many equal long jobs, spreading them one per SM
+// beside shorter ones measured slower than packing them.
+
 // next job index of a persistent warp: lane 0 takes it from the counter
-__device__ __forceinline__ int take_job(int* ctr, int lane)
+__device__ __forceinline__ int take_job(int* ctr, int off, int lane)
 {
    int k = 0;
-   if (lane == 0) k = atomicAdd(ctr, 1);
+   if (lane == 0) k = off + atomicAdd(ctr, 1);
    return __shfl_sync(kLaneMask, k, 0);
+}
+
+// a warp's first job, or -1 for a warp that stays idle beside an outlier
+__device__ __forceinline__ int first_job(int* ctr, int ncrit, int off, int lane)
+{
+   const int b = blockIdx.x, wib = threadIdx.x >> 5;
+   if (ncrit == 0) return take_job(ctr, off, lane);
+   if (wib == 0) return b;
+   if (b < ncrit) return -1;
+   return take_job(ctr, off, lane);
 }
 
 // one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the
@@ -254,10 +272,13 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
    int* ctr = d.sched_ctr;
    bool bad = false;
-   for (int k = take_job(ctr, lane); k < nj;) {
+   const int ncrit = d.sched_ncrit[0], off = ncrit ? (int)gridDim.x : 0;
+   const int k0 = first_job(ctr, ncrit, off, lane);
+   if (k0 < 0) return;
+   for (int k = k0; k < nj;) {
       // the next job's index is fetched while this one runs
       int kn = 0;
-      if (lane == 0) kn = atomicAdd(ctr, 1);
+      if (lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       const int head = d.sched_jobs[job], ich = head & ~kFusedJob;
       bad |= factor_job<SD>(d, job, ich, lane);
@@ -278,9 +299,12 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sw
    if (w >= nwarps) return;
    const int lane = threadIdx.x & 31, nj = d.sched_njobs[1 + wave], j0 = d.sched_job0[1 + wave];
    int* ctr = d.sched_ctr + 1 + sweep * d.nWave + wave;
-   for (int k = take_job(ctr, lane); k < nj;) {
+   const int ncrit = d.sched_ncrit[1 + wave], off = ncrit ? (int)gridDim.x : 0;
+   const int k0 = first_job(ctr, ncrit, off, lane);
+   if (k0 < 0) return;
+   for (int k = k0; k < nj;) {
       int kn = 0;
-      if (lane == 0) kn = atomicAdd(ctr, 1);
+      if (lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       solve_job(d, job, d.sched_jobs[job], lane);
       k = __shfl_sync(kLaneMask, kn, 0);

@@ -336,6 +336,7 @@ struct hamstr_gpu {
       if ((st = reupload(&d.sched_job0, sched.job0, owned))) return st;
       if ((st = reupload(&d.sched_njobs, sched.njobs, owned))) return st;
       if ((st = reupload(&d.sched_job_ptr, sched.job_ptr, owned))) return st;
+      if ((st = reupload(&d.sched_ncrit, sched.ncrit, owned))) return st;
       return reupload(&d.sched_jobs, sched.jobs, owned);
    }
 

@@ -92,6 +92,7 @@ struct DeviceState {
    int *cell_written;
    double* blk;            // per-row assembled blocks A, B, C (scaled, B + I) [nRow][48]
    int *sched_job0, *sched_njobs, *sched_job_ptr, *sched_jobs;   // persistent-warp job queues (plan.h)
+   int* sched_ncrit;       // per schedule: leading jobs that run alone on their SM (plan.h)
    int* sched_ctr;         // [sched_nctr = 1 + msweep*nWave] next-job counters: factorisation, then sweep s
    int sched_nctr;         // wave w at 1 + s*nWave + w; adi_assemble zeroes them
    double* fac;            // per-row factor storage

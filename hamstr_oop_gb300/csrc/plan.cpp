@@ -369,6 +369,9 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
       S.job0.push_back((int)S.job_ptr.size() - 1);
       S.njobs.push_back((int)order.size());
       S.nwarps.push_back(std::min((int)order.size(), max_warps));
+      int nc = 0;
+      while (nc < (int)order.size() && order[nc].cost >= kCritFrac * order[0].cost) nc++;
+      S.ncrit.push_back(nc <= kMaxCrit ? nc : 0);
       for (const Job& j : order) {
          S.jobs.insert(S.jobs.end(), j.entries.begin(), j.entries.end());
          S.job_ptr.push_back((int)S.jobs.size());

@@ -91,8 +91,16 @@ constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;
 constexpr int kQuadJob = 1 << 28;
 constexpr int kFusedJob = 1 << 27;
+// The ncrit[s] leading jobs of a schedule that are outliers (cost at
+// least kCritFrac of the longest, and at most kMaxCrit of them; else 0)
+// run alone on their SM: the first warp of block b starts with job b and
+// the other warps of those blocks take no job, so no other FP64 work
+// shares the SM while the chain that sets the launch's length runs.
+constexpr double kCritFrac = 0.8;
+constexpr int kMaxCrit = 8;
 struct Schedule {
    std::vector<int> job0, njobs, nwarps;   // per schedule
+   std::vector<int> ncrit;                 // per schedule: leading jobs that run alone on their SM
    std::vector<int> job_ptr;               // per job (all schedules), +1
    std::vector<int> jobs;                  // job entries, as above
 };

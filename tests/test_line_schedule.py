@@ -102,6 +102,9 @@ int main(int argc, char** argv) {
                }
                const int nw = S.nwarps[s];
                if (nw != (S.njobs[s] < maxw ? S.njobs[s] : maxw)) return fail("warps", nw, S.njobs[s]);
+               if ((int)S.ncrit.size() != 1 + p.nWave || S.ncrit[s] < 0 || S.ncrit[s] > kMaxCrit ||
+                   S.ncrit[s] > S.njobs[s])
+                  return fail("outlier jobs", S.ncrit[s], S.njobs[s]);
                checked++;
             }
          }
