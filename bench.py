@@ -537,8 +537,8 @@ NCU_PER_LAUNCH = {
         "recon5": {"dram_bytes": 155.0e6, "fp64_inst": 2898203},
         "rhs_face": {"dram_bytes": 16.8e6, "fp64_inst": 2620380},
         "adi_assemble": {"dram_bytes": 55.1e6, "fp64_inst": 873663},
-        "adi_factor": {"dram_bytes": 55.3e6, "fp64_inst": 1934731},
-        "adi_solve": {"dram_bytes": 24.5e6, "fp64_inst": 416819},
+        "adi_factor": {"dram_bytes": 62.7e6, "fp64_inst": 2700985},   # with the first wave's first solve
+        "adi_solve": {"dram_bytes": 20.1e6, "fp64_inst": 300775},
         "lin_recon5": {"dram_bytes": 209.2e6, "fp64_inst": 2554292},
         "lin_face": {"dram_bytes": 55.2e6, "fp64_inst": 328832},
         "lin_cell": {"dram_bytes": 15.6e6, "fp64_inst": 343608},
