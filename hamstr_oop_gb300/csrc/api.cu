@@ -198,6 +198,10 @@ struct hamstr_gpu {
       if (d.ff32) return HAMSTR_GPU_OK;
       const size_t nc = (size_t)d.nCell;
       int st;
+      if (mx_configure()) {
+         set_error("FP32 factorisation: shared-memory attribute refused");
+         return HAMSTR_GPU_ERR_CUDA;
+      }
       if ((st = dalloc(&d.ff32, 32 * (size_t)d.nSlot, owned))) return st;
       // chains of each wave ordered longest first, so a warp's threads
       // (one chain each) run for similar lengths; the same order tiles the

@@ -225,6 +225,9 @@ void launch_mx_solve(const DeviceState& d, int first, int count, cudaStream_t st
 // chains the chunked FP32 solve holds resident at once with `block` threads per block (0 on error)
 int mx_solve_chunk_capacity(int block);
 void launch_mx_dq_update(const DeviceState& d, cudaStream_t st);
+// allows the fused FP32 factorisation its staging shared memory (once per
+// device, before the first launch); nonzero on failure
+int mx_configure();
 void launch_mx_lin_face(const DeviceState& d, cudaStream_t st);
 void launch_mx_lin_cell(const DeviceState& d, bool update_q, cudaStream_t st);
 // segmented solve of the long periodic chains (d.nSpike > 0 and d.sp_on):

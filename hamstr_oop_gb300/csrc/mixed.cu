@@ -359,6 +359,102 @@ __device__ __forceinline__ void mx_rows(const DeviceState& d, const RowRef& r, i
    }
 }
 
+// ---- fused assembly with the next row's terms staged in shared memory ----
+// Each of a row's up to 3 x kOpsPerBlock face-Jacobian terms is a 64-byte
+// block of ff32.  Summing them as they arrive makes the row wait on one
+// round trip per term; instead the terms of row i+1 are copied into shared
+// memory with asynchronous copies (cp.async, 16 bytes each) while row i is
+// factored, and summed, in the same order as mx_block, after it.  Layout:
+// float4 q of term t of thread `tid` at ((t * 4 + q) * blockDim + tid), so
+// a warp's copies and reads of one float4 are one 512-byte span.
+constexpr int kStageTerms = 3 * kOpsPerBlock;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ float4* stage_at(float4* stage, int term, int q)
+{
+   return stage + (size_t)(term * 4 + q) * blockDim.x + threadIdx.x;
+}
+
+// issue the copies of row r's terms (terms with op < 0 copy nothing)
+__device__ __forceinline__ void mx_stage_row(const DeviceState& d, const RowRef& r, float4* stage)
+{
+   const int ops[kStageTerms] = {r.ops[0].x, r.ops[0].y, r.ops[0].z, r.ops[0].w, r.ops[1].x, r.ops[1].y,
+                                 r.ops[1].z, r.ops[1].w, r.ops[2].x, r.ops[2].y, r.ops[2].z, r.ops[2].w};
+#pragma unroll
+   for (int t = 0; t < kStageTerms; t++) {
+      const int op = ops[t];
+      if (op < 0) continue;
+      const float* src = d.ff32 + 32 * (size_t)(op >> 3) + (((op >> 1) & 3) == OP_SEL_L ? 0 : 16);
+#pragma unroll
+      for (int q = 0; q < 4; q++) cp_async16(stage_at(stage, t, q), src + 4 * q);
+   }
+   cp_async_commit();
+}
+
+// mx_block from the staged terms of block b (0, 1, 2 = A, B, C)
+__device__ __forceinline__ void mx_block_staged(const DeviceState& d, const int (&ops)[kOpsPerBlock], int b,
+                                                const float4* stage, float (&M)[16])
+{
+#pragma unroll
+   for (int m = 0; m < 16; m++) M[m] = 0.f;
+#pragma unroll
+   for (int o = 0; o < kOpsPerBlock; o++) {
+      const int op = ops[o];
+      if (op < 0) break;
+      float v[16];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+         const float4 x = *stage_at(const_cast<float4*>(stage), b * kOpsPerBlock + o, q);
+         v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+      }
+      if (((op >> 1) & 3) == OP_SEL_RREFL) {
+         const double4 rf = d.refl[d.slot_face[op >> 3]];
+#pragma unroll
+         for (int k = 0; k < 4; k++) {
+            const float r01 = v[4 * k + 1], r02 = v[4 * k + 2];
+            v[4 * k + 1] = float(rf.x) * r01 + float(rf.y) * r02;
+            v[4 * k + 2] = float(rf.z) * r01 + float(rf.w) * r02;
+         }
+      }
+      if (op & 1) {
+#pragma unroll
+         for (int m = 0; m < 16; m++) M[m] -= v[m];
+      } else {
+#pragma unroll
+         for (int m = 0; m < 16; m++) M[m] += v[m];
+      }
+   }
+}
+
+// mx_row_ref from staged terms and the row's CFL/sigma factor s
+__device__ __forceinline__ void mx_row_staged(const DeviceState& d, const RowRef& r, const float4* stage, float s,
+                                              float (&A)[16], float (&B)[16], float (&C)[16])
+{
+   const int oa[4] = {r.ops[0].x, r.ops[0].y, r.ops[0].z, r.ops[0].w};
+   const int ob[4] = {r.ops[1].x, r.ops[1].y, r.ops[1].z, r.ops[1].w};
+   const int oc[4] = {r.ops[2].x, r.ops[2].y, r.ops[2].z, r.ops[2].w};
+   mx_block_staged(d, oa, 0, stage, A);
+   mx_block_staged(d, ob, 1, stage, B);
+   mx_block_staged(d, oc, 2, stage, C);
+#pragma unroll
+   for (int m = 0; m < 16; m++) {
+      A[m] *= s;
+      B[m] *= s;
+      C[m] *= s;
+   }
+#pragma unroll
+   for (int k = 0; k < 4; k++) B[5 * k] += 1.f;
+}
+
 // rows of the periodic last-row elimination whose loads issue together
 // where all chains are resident at once (1 otherwise: there the kernel is
 // bound by throughput, not by one chain's round trips)
@@ -378,6 +474,9 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    float A[16], B[16], C[16], cp[16], ap[16];
    bool bad = false;   // a reciprocal pivot is not finite (DEV_ERR_PIVOT)
    RowRef rnext{};   // fused: references of row i + 1, looked up a row ahead
+   RowRef rstaged{};  // fused: references of the row whose terms are staged
+   float snext = 0.f;  // fused: its CFL/sigma factor
+   extern __shared__ float4 stage[];   // fused: kStageTerms x 4 float4 per thread
    if (FUSED) {
       const RowRef r0 = mx_rowref(d, row0);
       if (N > 1) rnext = mx_rowref(d, row0 + 1);
@@ -388,8 +487,15 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
    for (int i = 0; i < N; i++) {
       float An[16], Bn[16], Cn[16];
       if (i + 1 < N) {
-         mx_rows<FUSED>(d, rnext, s0 + i + 1, lane, An, Bn, Cn);
-         if (FUSED && i + 2 < N) rnext = mx_rowref(d, row0 + i + 2);
+         if (FUSED) {
+            // row i+1's terms are copied while row i is factored
+            mx_stage_row(d, rnext, stage);
+            rstaged = rnext;
+            snext = float(d.dtfac[rnext.scell]);
+            if (i + 2 < N) rnext = mx_rowref(d, row0 + i + 2);
+         } else {
+            mx_rows<FUSED>(d, rnext, s0 + i + 1, lane, An, Bn, Cn);
+         }
       }
       float* rec = d.fac32 + tix(s0 + i, kRec, 0, lane);
       st16t(rec, A);
@@ -421,8 +527,13 @@ __global__ void __launch_bounds__(256) mx_factor_kernel(DeviceState d, int count
 #pragma unroll
       for (int m = 0; m < 16; m++) { cp[m] = C[m]; ap[m] = fill[m]; }
       if (i + 1 < N) {
+         if (FUSED) {
+            cp_async_wait_all();
+            mx_row_staged(d, rstaged, stage, snext, A, B, C);
+         } else {
 #pragma unroll
-         for (int m = 0; m < 16; m++) { A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
+            for (int m = 0; m < 16; m++) { A[m] = An[m]; B[m] = Bn[m]; C[m] = Cn[m]; }
+         }
       }
    }
    if (!per) {
@@ -1476,14 +1587,29 @@ void launch_mx_assemble(const DeviceState& d, cudaStream_t st)
 
 void launch_mx_init(const DeviceState& d, cudaStream_t st) { mx_init_kernel<<<blocks_for(d.nCell), kThreads, 0, st>>>(d); }
 
+// dynamic shared memory of the fused factorisation: the staged terms
+size_t mx_factor_stage_bytes(int block) { return (size_t)kStageTerms * 4 * sizeof(float4) * block; }
+
+int mx_configure()
+{
+   const int want = (int)mx_factor_stage_bytes(128);
+   if (cudaFuncSetAttribute(mx_factor_kernel<true, kElimChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+           cudaSuccess ||
+       cudaFuncSetAttribute(mx_factor_kernel<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, want) !=
+           cudaSuccess)
+      return 1;
+   return 0;
+}
+
 void launch_mx_factor(const DeviceState& d, cudaStream_t st)
 {
    const int tb = d.mx_block;
    const unsigned nb = (d.nChain + tb - 1) / tb;
    const bool chunk = d.nChain <= d.mx_chunk_chains;
    if (d.mx_fused) {
-      if (chunk) mx_factor_kernel<true, kElimChunk><<<nb, tb, 0, st>>>(d, d.nChain);
-      else mx_factor_kernel<true, 1><<<nb, tb, 0, st>>>(d, d.nChain);
+      const size_t sm = mx_factor_stage_bytes(tb);
+      if (chunk) mx_factor_kernel<true, kElimChunk><<<nb, tb, sm, st>>>(d, d.nChain);
+      else mx_factor_kernel<true, 1><<<nb, tb, sm, st>>>(d, d.nChain);
    } else {
       if (chunk) mx_factor_kernel<false, kElimChunk><<<nb, tb, 0, st>>>(d, d.nChain);
       else mx_factor_kernel<false, 1><<<nb, tb, 0, st>>>(d, d.nChain);
