@@ -122,9 +122,11 @@ struct DeviceState {
    float* ff32;            // [nSlot][32] FP32 face Jacobians
    // The FP32 line data is tiled by groups of 32 chains in line_chains
    // order, one chain per thread: element e of row i of the chain at
-   // position p sits at ((grp_row0[p >> 5] + i) * W + e) * 32 + (p & 31) of
-   // a W-wide record array, so each load or store of a warp is one whole
-   // 128-byte line.  A group takes as many tile rows as its longest chain.
+   // position p sits at ((grp_row0[p >> 5] + i) * W + (e & ~3)) * 32 +
+   // 4 * (p & 31) + (e & 3) of a W-wide record array (mixed.cu tix): each
+   // thread moves four elements as one float4, and a warp's access of one
+   // group of four is 512 contiguous bytes.  A group takes as many tile
+   // rows as its longest chain.
    float* blk32;           // W = 48: assembled blocks A, B, C (B + I), unfused assembly only
    float* fsc32;           // W = 4: right-hand side / forward sweep
    float* fac32;           // W = 80: factor records

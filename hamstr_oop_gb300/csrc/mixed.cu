@@ -87,12 +87,13 @@ __global__ void __launch_bounds__(kThreads) mx_init_kernel(DeviceState d)
 // faster where chains are short (the autotuner picks)
 __global__ void __launch_bounds__(kThreads) mx_assemble_kernel(DeviceState d)
 {
-   // one thread per tiled entry (DeviceState: blk32), so stores are whole lines
+   // one thread per tiled entry (DeviceState: blk32), in memory order, so
+   // stores are whole lines: t = tix(srow, 48, e48, lane)
    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
    if (t >= 48 * 32 * (size_t)d.tile_rows || halted(d)) return;
-   const int lane = (int)(t & 31);
-   const size_t q = t >> 5;
-   const int e48 = (int)(q % 48), srow = (int)(q / 48), b = e48 >> 4, e = e48 & 15;
+   const int lane = (int)((t >> 2) & 31);
+   const size_t g = t >> 7;
+   const int e48 = (int)(g % 12) * 4 + (int)(t & 3), srow = (int)(g / 12), b = e48 >> 4, e = e48 & 15;
    const int row = d.tile_row[32 * (size_t)srow + lane];
    if (row < 0 || frozen_cell(d, d.row_scell[row])) return;
    const int* ops = d.row_ops + 3 * kOpsPerBlock * row + kOpsPerBlock * b;
@@ -126,24 +127,31 @@ __device__ __forceinline__ bool spike_active(const DeviceState& d, int ich)
    return d.sp_on && d.chain_spike[ich] >= 0 && (d.sp_on == 2 || d.chain_periodic[ich]);
 }
 
-// the tiled index of element e of tile row s in lane `lane` of a W-wide array
+// the tiled index of element e of tile row s in lane `lane` of a W-wide
+// array (W a multiple of 4): each lane's elements 4k .. 4k+3 are one float4,
+// and the 32 lanes' float4 of one group lie together, so a warp's access of
+// one group is 512 contiguous bytes and takes one instruction per lane
 __device__ __forceinline__ size_t tix(int s, int W, int e, int lane)
 {
-   return (((size_t)s * W + e) << 5) + lane;
+   return (((size_t)s * W + (e & ~3)) << 5) + 4 * lane + (e & 3);
 }
 
-// 16 consecutive elements of a tiled record (stride 32 floats: each load of
+// 16 consecutive elements of a tiled record (4 float4, 128 floats apart: each load of
 // a warp is one 128-byte line)
 __device__ __forceinline__ void ld16t(const float* __restrict__ p, float (&v)[16])
 {
 #pragma unroll
-   for (int m = 0; m < 16; m++) v[m] = p[32 * m];
+   for (int q = 0; q < 4; q++) {
+      const float4 x = *reinterpret_cast<const float4*>(p + 128 * q);
+      v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+   }
 }
 
 __device__ __forceinline__ void st16t(float* __restrict__ p, const float (&v)[16])
 {
 #pragma unroll
-   for (int m = 0; m < 16; m++) p[32 * m] = v[m];
+   for (int q = 0; q < 4; q++)
+      *reinterpret_cast<float4*>(p + 128 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
 }
 
 // ---------------- FP32 line solves, one thread per chain ----------------
@@ -213,21 +221,21 @@ __device__ __forceinline__ LUf luf_load(const float* p)
    return u;
 }
 
-// the LU record of a tiled row (stride 32 floats)
+// the LU record of a tiled row
 __device__ __forceinline__ void luf_store_t(float* p, const LUf& u)
 {
    const float v[16] = {u.p0, u.u01, u.u02, u.u03, u.l10, u.p1, u.u12, u.u13,
                         u.l20, u.l21, u.p2, u.u23, u.l30, u.l31, u.l32, u.p3};
-#pragma unroll
-   for (int m = 0; m < 16; m++) p[32 * m] = v[m];
+   st16t(p, v);
 }
 
 __device__ __forceinline__ LUf luf_load_t(const float* p)
 {
+   float v[16];
+   ld16t(p, v);
    LUf u;
-   u.p0 = p[0]; u.u01 = p[32]; u.u02 = p[64]; u.u03 = p[96]; u.l10 = p[128]; u.p1 = p[160]; u.u12 = p[192];
-   u.u13 = p[224]; u.l20 = p[256]; u.l21 = p[288]; u.p2 = p[320]; u.u23 = p[352]; u.l30 = p[384];
-   u.l31 = p[416]; u.l32 = p[448]; u.p3 = p[480];
+   u.p0 = v[0]; u.u01 = v[1]; u.u02 = v[2]; u.u03 = v[3]; u.l10 = v[4]; u.p1 = v[5]; u.u12 = v[6]; u.u13 = v[7];
+   u.l20 = v[8]; u.l21 = v[9]; u.p2 = v[10]; u.u23 = v[11]; u.l30 = v[12]; u.l31 = v[13]; u.l32 = v[14]; u.p3 = v[15];
    return u;
 }
 
@@ -626,7 +634,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       luf_solve(u, x[0], x[1], x[2], x[3]);
       float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-      for (int k = 0; k < 4; k++) fs[32 * k] = x[k];
+      *reinterpret_cast<float4*>(fs) = make_float4(x[0], x[1], x[2], x[3]);
 #pragma unroll
       for (int k = 0; k < 4; k++) xp[k] = x[k];
       if (i + 1 < N) {
@@ -645,7 +653,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), c);
          const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-         for (int k = 0; k < 4; k++) f[k] = fs[32 * k];
+         { const float4 y = *reinterpret_cast<const float4*>(fs); f[0] = y.x; f[1] = y.y; f[2] = y.z; f[3] = y.w; }
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
@@ -663,7 +671,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          ld16t(rec + 32 * 48, aa);
          const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-         for (int k = 0; k < 4; k++) x[k] = fs[32 * k];
+         { const float4 y = *reinterpret_cast<const float4*>(fs); x[0] = y.x; x[1] = y.y; x[2] = y.z; x[3] = y.w; }
 #pragma unroll
          for (int k = 0; k < 4; k++)
 #pragma unroll
@@ -686,7 +694,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          ld16t(d.fac32 + tix(s0 + N - 2, kRec, 32, lane), c);
          const float* fs = d.fsc32 + tix(s0 + N - 2, 4, 0, lane);
 #pragma unroll
-         for (int k = 0; k < 4; k++) x[k] = fs[32 * k];
+         { const float4 y = *reinterpret_cast<const float4*>(fs); x[0] = y.x; x[1] = y.y; x[2] = y.z; x[3] = y.w; }
          sc = scell[N - 2];
       }
       for (int i = N - 2; i >= 0; i--) {
@@ -696,7 +704,7 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
             ld16t(d.fac32 + tix(s0 + i - 1, kRec, 32, lane), cn);
             const float* fs = d.fsc32 + tix(s0 + i - 1, 4, 0, lane);
 #pragma unroll
-            for (int k = 0; k < 4; k++) xnx[k] = fs[32 * k];
+            { const float4 y = *reinterpret_cast<const float4*>(fs); xnx[0] = y.x; xnx[1] = y.y; xnx[2] = y.z; xnx[3] = y.w; }
             scn = scell[i - 1];
          }
 #pragma unroll
@@ -776,7 +784,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
             luf_solve(ub[u], x[0], x[1], x[2], x[3]);
             float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-            for (int k = 0; k < 4; k++) fs[32 * k] = x[k];
+            *reinterpret_cast<float4*>(fs) = make_float4(x[0], x[1], x[2], x[3]);
 #pragma unroll
             for (int k = 0; k < 4; k++) xp[k] = x[k];
          }
@@ -795,7 +803,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
                ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), cb[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+               { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
             }
          }
 #pragma unroll
@@ -826,7 +834,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
                ld16t(rec + 32 * 48, ab[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+               { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
                sb[u] = scell[i];
             }
          }
@@ -864,7 +872,7 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
                ld16t(d.fac32 + tix(s0 + i, kRec, 32, lane), cb[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
 #pragma unroll
-               for (int k = 0; k < 4; k++) fb[u][k] = fs[32 * k];
+               { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
                sb[u] = scell[i];
             }
          }
