@@ -633,7 +633,6 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       }
       luf_solve(u, x[0], x[1], x[2], x[3]);
       float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
       *reinterpret_cast<float4*>(fs) = make_float4(x[0], x[1], x[2], x[3]);
 #pragma unroll
       for (int k = 0; k < 4; k++) xp[k] = x[k];
@@ -652,7 +651,6 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          float c[16], f[4];
          ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), c);
          const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
          { const float4 y = *reinterpret_cast<const float4*>(fs); f[0] = y.x; f[1] = y.y; f[2] = y.z; f[3] = y.w; }
 #pragma unroll
          for (int k = 0; k < 4; k++)
@@ -670,7 +668,6 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          ld16t(rec + 32 * 32, c);
          ld16t(rec + 32 * 48, aa);
          const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
          { const float4 y = *reinterpret_cast<const float4*>(fs); x[0] = y.x; x[1] = y.y; x[2] = y.z; x[3] = y.w; }
 #pragma unroll
          for (int k = 0; k < 4; k++)
@@ -693,7 +690,6 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
       if (N >= 2) {
          ld16t(d.fac32 + tix(s0 + N - 2, kRec, 32, lane), c);
          const float* fs = d.fsc32 + tix(s0 + N - 2, 4, 0, lane);
-#pragma unroll
          { const float4 y = *reinterpret_cast<const float4*>(fs); x[0] = y.x; x[1] = y.y; x[2] = y.z; x[3] = y.w; }
          sc = scell[N - 2];
       }
@@ -703,7 +699,6 @@ __global__ void __launch_bounds__(256) mx_solve_kernel(DeviceState d, int first,
          if (i >= 1) {
             ld16t(d.fac32 + tix(s0 + i - 1, kRec, 32, lane), cn);
             const float* fs = d.fsc32 + tix(s0 + i - 1, 4, 0, lane);
-#pragma unroll
             { const float4 y = *reinterpret_cast<const float4*>(fs); xnx[0] = y.x; xnx[1] = y.y; xnx[2] = y.z; xnx[3] = y.w; }
             scn = scell[i - 1];
          }
@@ -783,7 +778,6 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
             }
             luf_solve(ub[u], x[0], x[1], x[2], x[3]);
             float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
             *reinterpret_cast<float4*>(fs) = make_float4(x[0], x[1], x[2], x[3]);
 #pragma unroll
             for (int k = 0; k < 4; k++) xp[k] = x[k];
@@ -802,7 +796,6 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
             if (i < N - 1) {
                ld16t(d.fac32 + tix(s0 + i, kRec, 64, lane), cb[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
                { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
             }
          }
@@ -833,7 +826,6 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
                ld16t(rec + 32 * 32, cb[u]);
                ld16t(rec + 32 * 48, ab[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
                { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
                sb[u] = scell[i];
             }
@@ -871,7 +863,6 @@ __global__ void __launch_bounds__(256) mx_solve_chunk_kernel(DeviceState d, int 
             if (i >= 0) {
                ld16t(d.fac32 + tix(s0 + i, kRec, 32, lane), cb[u]);
                const float* fs = d.fsc32 + tix(s0 + i, 4, 0, lane);
-#pragma unroll
                { const float4 y = *reinterpret_cast<const float4*>(fs); fb[u][0] = y.x; fb[u][1] = y.y; fb[u][2] = y.z; fb[u][3] = y.w; }
                sb[u] = scell[i];
             }
