@@ -342,7 +342,7 @@ void launch_adi_assemble(const DeviceState& d, cudaStream_t st)
 
 void launch_adi_factor(const DeviceState& d, int nwarps, cudaStream_t st)
 {
-   const int wpb = d.adi_wpb;
+   const int wpb = d.adi_fwpb;
    if (nwarps <= 0) return;
    if (d.piv_soft) adi_factor_kernel<true><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);
    else adi_factor_kernel<false><<<(nwarps + wpb - 1) / wpb, 32 * wpb, d.exclusive_smem, st>>>(d, nwarps);

@@ -356,7 +356,7 @@ struct hamstr_gpu {
    }
 
    int apply_shape(int face_block, int adi_wpb, int mx_block, int mx_fused, int face_soft, int piv_soft, int lanes,
-                   int wkeep, int bundle, int chunk, int spike, int fuse)
+                   int wkeep, int bundle, int chunk, int spike, int fuse, int adi_fwpb)
    {
       d.sp_on = spike;
       if (wkeep && d.recon == 5) {
@@ -375,16 +375,18 @@ struct hamstr_gpu {
          if (st) return st;
       }
       d.mx_fused = mx_fused;
-      if (adi_wpb != d.adi_wpb || lanes != adi_lanes || bundle != adi_bundle || fuse != adi_fuse) {
+      if (adi_wpb != d.adi_wpb || adi_fwpb != d.adi_fwpb || lanes != adi_lanes || bundle != adi_bundle ||
+          fuse != adi_fuse) {
          adi_lanes = lanes;
          adi_bundle = bundle;
          adi_fuse = fuse;
-         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle, fuse != 0);
+         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle, fuse != 0, adi_fwpb * nsm);
          const int st = upload_schedule();
          if (st) return st;
       }
       d.face_block = face_block;
       d.adi_wpb = adi_wpb;
+      d.adi_fwpb = adi_fwpb;
       d.mx_block = mx_block;
       mx_chunk = chunk;
       d.mx_chunk_chains = chunk ? mx_solve_chunk_capacity(mx_block) : 0;
@@ -659,6 +661,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       d.exclusive_smem = adi_configure(optin);
       d.face_block = 256;
       d.adi_wpb = 4;
+      d.adi_fwpb = 4;
       d.mx_block = 64;
       d.mx_chunk_chains = mx_solve_chunk_capacity(d.mx_block);
       d.sp_on = 1;   // long periodic chains of the FP32 form by segments (2: long open ones too)
@@ -671,7 +674,7 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       // the shortest open chains one per lane where chains are short (the
       // autotuner checks the alternatives)
       g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 8 : 0;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle, g->adi_fuse != 0);
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle, g->adi_fuse != 0, d.adi_fwpb * nsm);
    }
    TRY(g->upload_schedule());
    d.nWave = P.nWave;
@@ -1216,7 +1219,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    // (FP32 form with long periodic chains: also their segmented solve or
    // not -- it shortens each chain's latency but does several times the
    // work, which loses where the chains alone fill the GPU)
-   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle, spike; float ms; };
+   struct Cand { int fb, wpb, mb, fused, fsoft, psoft, lanes, bundle, spike, fwpb; float ms; };
    const int wk = g->weno_keep, ck = g->mx_chunk;
    std::vector<int> spikes = {d.sp_on};
    if (g->mixed && d.nSpike > 0) spikes = {0, 1, 2};
@@ -1228,13 +1231,14 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
                for (int mb : {32, 64, 128})
                   for (int sp : spikes)
                      cands.push_back({fb, d.adi_wpb, mb, fused, fsoft, d.piv_soft, g->adi_lanes, g->adi_bundle, sp,
-                                      0.f});
+                                      d.adi_fwpb, 0.f});
          } else {
             for (int w : {4, 8})
-               for (int psoft : {0, 1})
-                  for (int ln : {16, 4})
-                     for (int bu : {0, 4, 8, 16})
-                        cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, ln, bu, d.sp_on, 0.f});
+               for (int fw : {4, 8})
+                  for (int psoft : {0, 1})
+                     for (int ln : {16, 4})
+                        for (int bu : {0, 4, 8, 16})
+                           cands.push_back({fb, w, d.mx_block, d.mx_fused, fsoft, psoft, ln, bu, d.sp_on, fw, 0.f});
          }
       }
    // the tuning steps advance the state: keep q and put it back afterwards
@@ -1248,7 +1252,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    int st = HAMSTR_GPU_OK;
    for (Cand& c : cands) {
       if ((st = g->apply_shape(c.fb, c.wpb, c.mb, c.fused, c.fsoft, c.psoft, c.lanes, wk, c.bundle, ck, c.spike,
-                               g->adi_fuse)))
+                               g->adi_fuse, c.fwpb)))
          break;
       if ((st = g->capture())) break;
       if ((st = g->reset_ctl(0.0))) break;
@@ -1271,7 +1275,7 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
    for (const Cand& c : cands)
       if (c.ms < best->ms) best = &c;
    st = g->apply_shape(best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, wk,
-                       best->bundle, ck, best->spike, g->adi_fuse);
+                       best->bundle, ck, best->spike, g->adi_fuse, best->fwpb);
    if (st) return st;
    if (report && report_len > 0) {
       std::string r = "{\"precision\": \"" + std::string(g->mixed ? "mixed" : "fp64") + "\", \"candidates\": [";
@@ -1280,18 +1284,18 @@ extern "C" int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int re
          std::snprintf(buf, sizeof(buf),
                        "%s{\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
                        "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d, "
-                       "\"mx_spike\": %d, \"ms\": %.4f}",
+                       "\"mx_spike\": %d, \"adi_factor_warps_per_sm\": %d, \"ms\": %.4f}",
                        i ? ", " : "", cands[i].fb, cands[i].wpb, cands[i].mb, cands[i].fused, cands[i].fsoft,
-                       cands[i].psoft, cands[i].lanes, cands[i].bundle, cands[i].spike, cands[i].ms);
+                       cands[i].psoft, cands[i].lanes, cands[i].bundle, cands[i].spike, cands[i].fwpb, cands[i].ms);
          r += buf;
       }
       char buf[320];
       std::snprintf(buf, sizeof(buf),
                     "], \"best\": {\"face_block\": %d, \"adi_warps_per_sm\": %d, \"mx_block\": %d, \"mx_fused\": %d, "
                     "\"face_softdiv\": %d, \"pivot_softdiv\": %d, \"adi_open_lanes\": %d, \"adi_bundle_rows\": %d, "
-                    "\"mx_spike\": %d}}",
+                    "\"mx_spike\": %d, \"adi_factor_warps_per_sm\": %d}}",
                     best->fb, best->wpb, best->mb, best->fused, best->fsoft, best->psoft, best->lanes, best->bundle,
-                    best->spike);
+                    best->spike, best->fwpb);
       r += buf;
       std::snprintf(report, (size_t)report_len, "%s", r.c_str());
    }
@@ -1304,7 +1308,7 @@ extern "C" int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape)
    const DeviceState& d = g->d;
    const int v[HAMSTR_SHAPE_N] = {d.face_block, d.adi_wpb,    d.mx_block,    d.mx_fused,     d.face_soft,
                                   d.piv_soft,   g->adi_lanes, g->weno_keep, g->adi_bundle, g->mx_chunk,
-                                  d.sp_on,      g->adi_fuse};
+                                  d.sp_on,      g->adi_fuse, d.adi_fwpb};
    std::memcpy(shape, v, sizeof(v));
    return HAMSTR_GPU_OK;
 }
@@ -1317,12 +1321,12 @@ extern "C" int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape)
                    (s[2] == 32 || s[2] == 64 || s[2] == 128) && (s[3] == 0 || s[3] == 1) &&
                    (s[4] == 0 || s[4] == 1) && (s[5] == 0 || s[5] == 1) && (s[6] == 32 || s[6] == 16 || s[6] == 4) &&
                    (s[7] == 0 || s[7] == 1) && (s[8] >= 0 && s[8] <= 64) && (s[9] == 0 || s[9] == 1) &&
-                   (s[10] >= 0 && s[10] <= 2) && (s[11] == 0 || s[11] == 1);
+                   (s[10] >= 0 && s[10] <= 2) && (s[11] == 0 || s[11] == 1) && (s[12] == 4 || s[12] == 8);
    if (!ok) {
       set_error("set_shape: a value outside its allowed set");
       return HAMSTR_GPU_ERR_ARG;
    }
-   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], s[10], s[11]);
+   return g->apply_shape(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8], s[9], s[10], s[11], s[12]);
 }
 
 extern "C" int hamstr_gpu_set_cfl(hamstr_gpu* g, double cfl)

@@ -111,7 +111,8 @@ struct DeviceState {
 
    // launch shapes chosen by hamstr_gpu_autotune (host-side only)
    int face_block;         // threads per block of the face kernels (<= 256)
-   int adi_wpb;            // warps per block (= per SM) of the persistent FP64 line kernels (4 or 8)
+   int adi_wpb;            // warps per block (= per SM) of the persistent FP64 solve kernel (4 or 8)
+   int adi_fwpb;           // the same for the FP64 factorisation kernel
    int mx_block;           // threads per block of the FP32 thread-per-chain line kernels
    int mx_fused;           // 1: FP32 blocks assembled inside the factorisation; 0: mx_assemble first
    int mx_chunk_chains;    // FP32 line kernels over at most this many chains load rows in chunks (all resident)

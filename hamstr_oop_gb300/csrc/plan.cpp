@@ -314,7 +314,8 @@ std::string build_plan(const MeshInput& in, Plan& p)
    return "";
 }
 
-Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows, bool fuse_first_wave)
+Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows, bool fuse_first_wave,
+                        int max_warps_factor)
 {
    Schedule S;
    S.job_ptr.push_back(0);
@@ -364,11 +365,11 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
       flush(group, group_flag, row_warp);
       return order;
    };
-   auto emit = [&](std::vector<Job>& order) {
+   auto emit = [&](std::vector<Job>& order, int maxw) {
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
       S.job0.push_back((int)S.job_ptr.size() - 1);
       S.njobs.push_back((int)order.size());
-      S.nwarps.push_back(std::min((int)order.size(), max_warps));
+      S.nwarps.push_back(std::min((int)order.size(), maxw));
       int nc = 0;
       while (nc < (int)order.size() && order[nc].cost >= kCritFrac * order[0].cost) nc++;
       S.ncrit.push_back(nc <= kMaxCrit ? nc : 0);
@@ -395,10 +396,10 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
       for (int c = 0; c < p.nChain; c++) all[c] = c;
       fac = pack(all, kFacWarp, kFacBundle);
    }
-   emit(fac);
+   emit(fac, max_warps_factor > 0 ? max_warps_factor : max_warps);
    for (int w = 0; w < p.nWave; w++) {
       std::vector<Job> sol = pack(wave(w), kSolWarp, kSolBundle);
-      emit(sol);
+      emit(sol, max_warps);
    }
    return S;
 }

@@ -83,7 +83,8 @@ std::string build_plan(const MeshInput& in, Plan& out);
 //     (open_lanes = 4);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
 //     bundle_rows rows, one per lane.
-// nwarps[s] = min(njobs[s], max_warps) warps are launched.  With
+// nwarps[s] = min(njobs[s], max_warps) warps are launched (max_warps_factor
+// for the factorisation).  With
 // fuse_first_wave the factorisation's jobs for the first wave's chains are
 // packed as that wave's solve packs them and carry kFusedJob on their first
 // entry: the warp that factors them runs their first sweep's solve at once.
@@ -104,8 +105,9 @@ struct Schedule {
    std::vector<int> job_ptr;               // per job (all schedules), +1
    std::vector<int> jobs;                  // job entries, as above
 };
+// max_warps_factor (0: max_warps) bounds the factorisation's warps, max_warps the solves'.
 Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows,
-                        bool fuse_first_wave = false);
+                        bool fuse_first_wave = false, int max_warps_factor = 0);
 
 }  // namespace hamstr
 #endif

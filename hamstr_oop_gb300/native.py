@@ -475,12 +475,13 @@ class GpuSolver:
     def autotune(self, reps: int = 3) -> dict:
         """Pick the fastest launch shapes for the current precision (hamstr_gpu_autotune)."""
         import json
-        buf = ctypes.create_string_buffer(65536)
-        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 65536))
+        buf = ctypes.create_string_buffer(131072)
+        _check(load().hamstr_gpu_autotune(self.h, int(reps), buf, 131072))
         return json.loads(buf.value.decode())
 
     SHAPE_KEYS = ("face_block", "adi_warps_per_sm", "mx_block", "mx_fused", "face_softdiv", "pivot_softdiv",
-                  "adi_open_lanes", "weno_keep", "adi_bundle_rows", "mx_chunk", "mx_spike", "adi_fuse")
+                  "adi_open_lanes", "weno_keep", "adi_bundle_rows", "mx_chunk", "mx_spike", "adi_fuse",
+                  "adi_factor_warps_per_sm")
 
     def shape(self) -> dict:
         """The launch shape in use (hamstr_gpu_get_shape), keyed as the autotuner's report."""

@@ -218,7 +218,8 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
 /* Autotuner (no reference counterpart): times `reps` steps of the current
  * precision for each candidate launch shape -- face kernels 128 or 256
  * threads per block; FP64 line kernels 4 or 8 persistent warps per SM (one
- * or two per sub-partition, schedules rebuilt longest-job-first), with open
+ * or two per sub-partition; the factorisation and the solves each their
+ * own; schedules rebuilt longest-job-first), with open
  * chains two per warp (one per half) or eight per warp (four lanes
  * each), and the shortest (up to 0, 4, 8 or 16 rows) 32 per warp, one per
  * lane; FP32
@@ -229,8 +230,8 @@ int hamstr_gpu_forces(hamstr_gpu* g, double* out6);
  * kernels and of the LU pivots on the FP64 pipe or on the integer pipes
  * (bit-identical) -- and keeps the fastest.  The state is restored
  * afterwards; FP64 results do not depend on the shape.  report (may be
- * NULL) receives a JSON summary of the timings (about 210 bytes per
- * candidate, at most 128 candidates). */
+ * NULL) receives a JSON summary of the timings (about 240 bytes per
+ * candidate, at most 256 candidates). */
 int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
 
 /* The launch shape itself (no reference counterpart), HAMSTR_SHAPE_N ints:
@@ -266,9 +267,11 @@ int hamstr_gpu_autotune(hamstr_gpu* g, int reps, char* report, int report_len);
  *       factorisation kernel (the other chains' factorisation goes on
  *       beside them), instead of by a separate launch: 0 or 1 (default 1;
  *       not tuned)
+ *  [12] FP64 factorisation kernel: persistent warps per SM, 4 or 8 (as [1]
+ *       for the solves; default 4; tuned with it)
  * set_shape checks every value (HAMSTR_GPU_ERR_ARG otherwise); FP64
  * results do not depend on the shape. */
-#define HAMSTR_SHAPE_N 12
+#define HAMSTR_SHAPE_N 13
 int hamstr_gpu_get_shape(hamstr_gpu* g, int* shape);
 int hamstr_gpu_set_shape(hamstr_gpu* g, const int* shape);
 

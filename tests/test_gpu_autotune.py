@@ -10,7 +10,7 @@ def test_autotune_fp64_keeps_bit_exactness(make_case, oracle_lib, native_lib):
     case = make_case(32, 8, order=3, CFL=10.0, msweep=2)
     g = native.GpuSolver(native.Case(case))
     rep = g.autotune(reps=2)
-    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 128
+    assert rep["precision"] == "fp64" and len(rep["candidates"]) == 256
     assert all(c["ms"] > 0 for c in rep["candidates"])
     o = oracle_lib.OracleCase(case, "port")
     for it in range(5):
@@ -26,6 +26,8 @@ FP64_SHAPES = [dict(face_block=fb, adi_warps_per_sm=w, face_softdiv=fs, pivot_so
 # with the first wave's first-sweep solve in its own launch (the default
 # runs it inside the factorisation kernel)
 FP64_SHAPES += [dict(sh, adi_fuse=0) for sh in FP64_SHAPES[::4]]
+# the factorisation kernel with a warp count of its own
+FP64_SHAPES += [dict(sh, adi_factor_warps_per_sm=8 if sh["adi_warps_per_sm"] == 4 else 4) for sh in FP64_SHAPES[1::4]]
 
 
 @pytest.mark.parametrize("order,split", [(3, 0.5), (5, 0.5), (5, 0.0)])
@@ -57,7 +59,7 @@ def test_set_shape_rejects_bad_values(make_case, native_lib):
     g = native.GpuSolver(native.Case(make_case(16, 4, order=1, CFL=5.0)))
     before = g.shape()
     for bad in (dict(face_block=192), dict(adi_warps_per_sm=6), dict(mx_block=96), dict(adi_open_lanes=8), dict(adi_bundle_rows=65),
-                dict(mx_spike=3), dict(adi_fuse=2)):
+                dict(mx_spike=3), dict(adi_fuse=2), dict(adi_factor_warps_per_sm=6)):
         with pytest.raises(native.HamstrError):
             g.set_shape(**bad)
     assert g.shape() == before

@@ -45,7 +45,7 @@ BATCH_MESHES = ((128, 32), (256, 64), (384, 96), (512, 128))
 SHAPES = ([dict(adi_bundle_rows=b) for b in (0, 4, 8, 16, 64)] +
           [dict(adi_open_lanes=n) for n in (32, 16, 4)] +
           [dict(adi_warps_per_sm=8), dict(face_block=256), dict(face_softdiv=0), dict(pivot_softdiv=1),
-           dict(adi_fuse=0)])
+           dict(adi_fuse=0), dict(adi_factor_warps_per_sm=8)])
 
 
 @pytest.fixture(scope="module")
