@@ -194,6 +194,41 @@ __device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib,
    }
 }
 
+// a fused first-wave pair job: both chains' right-hand sides gathered,
+// then factorisation and the first sweep's forward substitution in one
+// pass over the rows (factor_line_pair<SD, true>), the back substitution
+// and the write-back; the same values as factor_pair then solve_pair
+template <bool SD>
+__device__ __forceinline__ bool factor_solve_pair(const DeviceState& d, int ia, int ib, int lane)
+{
+   const int ich = (lane >> 4) ? ib : ia, l16 = lane & 15;
+   const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
+   double* fs = d.fsc + 4 * (size_t)row0;
+   const double* fac = d.fac + (size_t)kFacRec * row0;
+   for (int r = l16; r < N; r += 16) {
+      const int fc = d.row_fcell[row0 + r];
+      double v[4] = {0.0, 0.0, 0.0, 0.0};
+      if (fc >= 0) ld4(d.r + 4 * (size_t)fc, v);
+      *reinterpret_cast<double2*>(fs + 4 * r) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
+   }
+   __syncwarp();
+   double xlast[4];
+   const bool bad = factor_line_pair<SD, true>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0,
+                                               lane, fs, xlast);
+   __syncwarp();
+   back_line_pair(fac, N, fs, lane, xlast);
+   __syncwarp();
+   for (int r = l16; r < N; r += 16) {
+      const int sc = d.row_scell[row0 + r];
+      double v[4];
+      ld4(fs + 4 * r, v);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(d.r + 4 * (size_t)sc + 2) = make_double2(v[2], v[3]);
+   }
+   return bad;
+}
+
 // the factorisation of one job (entries at `job`, first entry `ich`
 // without kFusedJob); returns whether a pivot was zero or not finite
 template <bool SD>
@@ -281,10 +316,14 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
       if (lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       const int head = d.sched_jobs[job], ich = head & ~kFusedJob;
-      bad |= factor_job<SD>(d, job, ich, lane);
-      if (head & kFusedJob) {
-         __syncwarp();   // the records of every lane are written
-         solve_job(d, job, ich, lane);
+      if ((head & kFusedJob) && (ich & kPairJob)) {
+         bad |= factor_solve_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
+      } else {
+         bad |= factor_job<SD>(d, job, ich, lane);
+         if (head & kFusedJob) {
+            __syncwarp();   // the records of every lane are written
+            solve_job(d, job, ich, lane);
+         }
       }
       k = __shfl_sync(kLaneMask, kn, 0);
    }

@@ -111,6 +111,94 @@ __device__ __forceinline__ double lu_wavefront(double w, int base, int e)
    return w;
 }
 
+// lu_wavefront together with the forward substitution of right-hand sides
+// through the block being factored (triSolvers.cpp:813-816 for f and
+// :825-828 for the columns of c): xc is element (k,j) of c(i) (column j is
+// solved by the lanes of column j) and, with F, xf is component k of f(i)
+// (the same in the four lanes of row k).  Each substitution step rides on
+// the elimination step that produces its pivot and multipliers, so the
+// right-hand sides are substituted by the time the last pivot is known
+// instead of after the factorisation.  Returns the LU element as
+// lu_wavefront does; dc (column j) and df (f) receive the substituted
+// values c1..c4 / d1..d4 of the reference in every lane, U the multipliers
+// u12 u13 u14 u23 u24 u34 in every lane.
+template <bool SD, bool F>
+__device__ __forceinline__ double lu_wavefront_rhs(double w, double xc, double xf, int base, int e, double (&dc)[4],
+                                                   double (&df)[4], double (&U)[6])
+{
+   const int k = e >> 2, j = e & 3;
+   const double piv0 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base)) : 1. / __shfl_sync(kLaneMask, w, base);
+   {
+      const double m = w * piv0;
+      if (k == 0 && j >= 1) w = m;
+   }
+   {
+      const double tc = xc * piv0, tf = F ? xf * piv0 : 0.0;
+      const double L = __shfl_sync(kLaneMask, w, base + 4 * k), Uj = __shfl_sync(kLaneMask, w, base + j);
+      dc[0] = __shfl_sync(kLaneMask, tc, base + j);
+      if (F) df[0] = __shfl_sync(kLaneMask, tf, base);
+      const double t = w - L * Uj;
+      xc = xc - L * dc[0];
+      if (F) xf = xf - L * df[0];
+      U[0] = __shfl_sync(kLaneMask, w, base + 1);
+      U[1] = __shfl_sync(kLaneMask, w, base + 2);
+      U[2] = __shfl_sync(kLaneMask, w, base + 3);
+      if (k >= 1 && j >= 1) w = t;
+   }
+   const double piv1 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 5)) : 1. / __shfl_sync(kLaneMask, w, base + 5);
+   {
+      const double m = w * piv1;
+      if (k == 1 && j >= 2) w = m;
+   }
+   {
+      const double tc = xc * piv1, tf = F ? xf * piv1 : 0.0;
+      const double L = __shfl_sync(kLaneMask, w, base + 4 * k + 1), Uj = __shfl_sync(kLaneMask, w, base + 4 + j);
+      dc[1] = __shfl_sync(kLaneMask, tc, base + 4 + j);
+      if (F) df[1] = __shfl_sync(kLaneMask, tf, base + 4);
+      const double t = w - L * Uj;
+      xc = xc - L * dc[1];
+      if (F) xf = xf - L * df[1];
+      U[3] = __shfl_sync(kLaneMask, w, base + 6);
+      U[4] = __shfl_sync(kLaneMask, w, base + 7);
+      if (k >= 2 && j >= 2) w = t;
+   }
+   const double piv2 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 10)) : 1. / __shfl_sync(kLaneMask, w, base + 10);
+   {
+      const double m = w * piv2;
+      if (k == 2 && j == 3) w = m;
+   }
+   {
+      const double tc = xc * piv2, tf = F ? xf * piv2 : 0.0;
+      const double L = __shfl_sync(kLaneMask, w, base + 14), Uj = __shfl_sync(kLaneMask, w, base + 11);
+      dc[2] = __shfl_sync(kLaneMask, tc, base + 8 + j);
+      if (F) df[2] = __shfl_sync(kLaneMask, tf, base + 8);
+      const double t = w - L * Uj;
+      xc = xc - L * dc[2];
+      if (F) xf = xf - L * df[2];
+      U[5] = Uj;
+      if (k == 3 && j == 3) w = t;
+   }
+   const double piv3 = SD ? sd::div(1., __shfl_sync(kLaneMask, w, base + 15)) : 1. / __shfl_sync(kLaneMask, w, base + 15);
+   {
+      const double tc = xc * piv3, tf = F ? xf * piv3 : 0.0;
+      dc[3] = __shfl_sync(kLaneMask, tc, base + 12 + j);
+      if (F) df[3] = __shfl_sync(kLaneMask, tf, base + 12);
+   }
+   if (k == j) w = (k == 0) ? piv0 : (k == 1) ? piv1 : (k == 2) ? piv2 : piv3;
+   return w;
+}
+
+// back substitution inside one block (triSolvers.cpp:818-821): d holds the
+// forward-substituted d1..d4 (or c1..c4), U the multipliers u12 u13 u14 u23
+// u24 u34; every component, in the reference's order, in every lane
+__device__ __forceinline__ void lu_back4(const double (&d)[4], const double (&U)[6], double (&x)[4])
+{
+   x[3] = d[3];
+   x[2] = d[2] - U[5] * x[3];
+   x[1] = (d[1] - U[3] * x[2]) - U[4] * x[3];
+   x[0] = ((d[0] - U[0] * x[1]) - U[1] * x[2]) - U[2] * x[3];
+}
+
 // Block-Thomas factorisation of one line of N rows by one warp: blocks
 // A_i = Ab + i*stride, B_i = Bb + i*stride, C_i = Cb + i*stride (row-major
 // 4x4); writes the per-row records `fac` (kFacRec doubles per row) and,
@@ -124,7 +212,10 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
    double A = Ab[e], B = Bb[e], C = Cb[e];
-   double P = 0.0;   // previous row's solved C' (h=0) or a' (h=1), element (k,j)
+   // column j of the previous row's solved C' (h=0) or a' (h=1), whole in
+   // every lane of the column (the block back substitution runs in each)
+   double P[4] = {0.0, 0.0, 0.0, 0.0};
+   double Yp = 0.0;   // element (k,j) of it
    bool bad = false;
    for (int i = 0; i < N; i++) {
       // next row's blocks are loaded while this row is factored
@@ -143,39 +234,40 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
 #pragma unroll
          for (int l = 0; l < 4; l++) {
             const double a = __shfl_sync(kLaneMask, A, 16 * h + 4 * k + l);
-            const double x = __shfl_sync(kLaneMask, P, 16 * h + 4 * l + j);
-            acc -= a * x;
+            acc -= a * P[l];
          }
       } else if (h) {
          acc = A;
       }
-      // LU of B'(i), computed by both halves on their own copy
-      const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, acc, e), 16 * h, e);
-      if (h == 0) rec[16 + e] = w;
-      bad |= h == 0 && k == j && nonfinite(w);
-      double lu[4];
-#pragma unroll
-      for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, 16 * h + 4 * k + c);
       // c'(i) = B'^{-1} c(i), a'(i) = B'^{-1} a(i), one column per lane
-      // group (component k of column j in lane 16h + 4k + j); at i == N-2
-      // of a periodic chain c(i) += a(i) first and a'(i) = c'(i)
+      // group (component k of column j in lane 16h + 4k + j), substituted
+      // along the LU of B'(i), which both halves compute on their own copy;
+      // at i == N-2 of a periodic chain c(i) += a(i) first and a'(i) = c'(i)
       const bool last2 = per && (i == N - 2);
       double Y = h ? acc : C;
       const double fillv = __shfl_sync(kLaneMask, acc, 16 + e);
       if (last2 && h == 0) Y = C + fillv;
-      double ys[4];
-      double Yp = lu_solve_lanes(lu, k, Y, 16 * h + j, 4, ys);
-      const double fromc = __shfl_sync(kLaneMask, Yp, e);
-      if (last2 && h == 1) Yp = fromc;
+      double dc[4], df[4], U[6];
+      const double w = lu_wavefront_rhs<SD, false>(__shfl_sync(kLaneMask, acc, e), Y, 0.0, 16 * h, e, dc, df, U);
+      if (h == 0) rec[16 + e] = w;
+      bad |= h == 0 && k == j && nonfinite(w);
+      lu_back4(dc, U, P);
+      if (last2) {
+#pragma unroll
+         for (int m = 0; m < 4; m++) {
+            const double fromc = __shfl_sync(kLaneMask, P[m], e);
+            if (h == 1) P[m] = fromc;
+         }
+      }
+      Yp = sel4(P, k);
       rec[32 + 16 * h + e] = Yp;
-      P = Yp;
       A = An;
       B = Bn;
       C = Cn;
    }
    if (!per) return bad;
    // last-row elimination (triSolvers.cpp:967-999)
-   double cN = __shfl_sync(kLaneMask, P, e);
+   double cN = __shfl_sync(kLaneMask, Yp, e);
    double bN = (k == j) ? 1.0 : 0.0;
    double Y = (N > 1) ? fac[32 + 16 * h + e] : 0.0;
    for (int i = 0; i < N - 1; i++) {
@@ -204,55 +296,127 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
 // length run to the longer one's count with the shorter half idle (its
 // loads and stores skipped).  Short open lines -- the rule on split meshes
 // -- leave half of factor_line's warp with nothing to do.
-template <bool SD = true>
+//
+// Lane (k,j) keeps column j of the previous row's C' whole (the block back
+// substitution runs in every lane of the column), so the next row's
+// b(i) -= a(i) c'(i-1) needs no shuffle of it, and the columns of c(i) are
+// substituted along the factorisation's wavefront (lu_wavefront_rhs).
+// With F the line's first solve runs in the same loop: fs holds f (the
+// right-hand sides, rows of 4) and receives the forward sweep's rows
+// (triSolvers.cpp:786-822, the reference's own loop), and xlast the last
+// row's solution, for the back substitution (back_line_pair).
+template <bool SD, bool F>
 __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
-                                                 double* __restrict__ fac, int lane)
+                                                 double* __restrict__ fac, int lane, double* __restrict__ fs,
+                                                 double (&xlast)[4])
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3, hb = 16 * h;
    const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
-   double A = 0.0, B = 0.0, C = 0.0;
+   double A = 0.0, B = 0.0, C = 0.0, fv = 0.0;
    if (N > 0) {
       A = Ab[e];
       B = Ab[16 + e];
       C = Ab[32 + e];
+      if (F) fv = fs[k];
    }
-   double P = 0.0;
+   double P[4] = {0.0, 0.0, 0.0, 0.0};   // column j of the previous row's C'
+   double X[4] = {0.0, 0.0, 0.0, 0.0};   // F: the previous row's solution
    bool bad = false;   // a live row's reciprocal pivot is not finite
    for (int i = 0; i < Nmax; i++) {
-      double An = 0.0, Bn = 0.0, Cn = 0.0;
+      double An = 0.0, Bn = 0.0, Cn = 0.0, fvn = 0.0;
       if (i + 1 < N) {
          const size_t o = stride * (size_t)(i + 1);
          An = Ab[o + e];
          Bn = Ab[o + 16 + e];
          Cn = Ab[o + 32 + e];
+         if (F) fvn = fs[4 * (i + 1) + k];
       }
       const bool live = i < N;
       double* rec = fac + (size_t)kFacRec * i;
       if (live) rec[e] = A;
-      double acc = B;
+      // b(i) -= a(i) c'(i-1) and f(i) -= a(i) f(i-1), products subtracted in order
+      double acc = B, xf = fv;
       if (i > 0) {
 #pragma unroll
          for (int l = 0; l < 4; l++) {
             const double a = __shfl_sync(kLaneMask, A, hb + 4 * k + l);
-            const double x = __shfl_sync(kLaneMask, P, hb + 4 * l + j);
-            acc -= a * x;
+            acc -= a * P[l];
+            if (F) xf = xf - a * X[l];
          }
       }
-      const double w = lu_wavefront<SD>(acc, hb, e);
+      double dc[4], df[4], U[6];
+      const double w = lu_wavefront_rhs<SD, F>(acc, C, xf, hb, e, dc, df, U);
       if (live) rec[16 + e] = w;
       bad |= live && k == j && nonfinite(w);
-      double lu[4];
+      lu_back4(dc, U, P);
+      if (live) rec[32 + e] = sel4(P, k);
+      if (F) {
+         double x[4];
+         lu_back4(df, U, x);
+         if (e < 4 && live) fs[4 * i + e] = sel4(x, e);
 #pragma unroll
-      for (int c = 0; c < 4; c++) lu[c] = __shfl_sync(kLaneMask, w, hb + 4 * k + c);
-      double ys[4];
-      const double Yp = lu_solve_lanes(lu, k, C, hb + j, 4, ys);
-      if (live) rec[32 + e] = Yp;
-      P = Yp;
+         for (int m = 0; m < 4; m++)
+            if (live) X[m] = x[m];   // the shorter line keeps its last row's solution
+      }
       A = An;
       B = Bn;
       C = Cn;
+      fv = fvn;
    }
+#pragma unroll
+   for (int m = 0; m < 4; m++) xlast[m] = X[m];
    return bad;
+}
+
+template <bool SD = true>
+__device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
+                                                 double* __restrict__ fac, int lane)
+{
+   double unused[4];
+   return factor_line_pair<SD, false>(Ab, stride, N, fac, lane, nullptr, unused);
+}
+
+// back substitution f(i) -= c'(i) f(i+1), i = N-2..0, of two open lines,
+// one per half-warp (triSolvers.cpp:839-846): fs holds the forward sweep's
+// rows and receives the solution, xlast is row N-1's solution (every lane)
+__device__ __forceinline__ void back_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs,
+                                               int lane, const double (&xlast)[4])
+{
+   const int e = lane & 15, pj = e & 3, r = lane & 3, hb = lane & 16;
+   const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
+   double xnext[4];
+#pragma unroll
+   for (int m = 0; m < 4; m++) xnext[m] = xlast[m];
+   // a row here is a few dependent operations, shorter than a load: rows
+   // ii-1 and ii-2 are in flight while row ii is solved
+   double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
+   if (N >= 2) {
+      mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
+      xi = fs[4 * (N - 2) + r];
+   }
+   if (N >= 3) {
+      mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
+      xi1 = fs[4 * (N - 3) + r];
+   }
+   for (int t = 0; t <= Nmax - 2; t++) {
+      const int ii = N - 2 - t;
+      double mv2 = 0.0, xi2 = 0.0;
+      if (ii > 1) {
+         mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
+         xi2 = fs[4 * (ii - 2) + r];
+      }
+      const double prod = mv * sel4(xnext, pj);
+      double x = xi;
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, prod, hb + 4 * r + jj);
+#pragma unroll
+      for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, hb + m);
+      if (e < 4 && ii >= 0) fs[4 * ii + e] = x;
+      mv = mv1;
+      xi = xi1;
+      mv1 = mv2;
+      xi1 = xi2;
+   }
 }
 
 // Right-hand-side replay of two factored open lines, one per half-warp:
@@ -296,41 +460,7 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
       av = avn;
    }
    __syncwarp();
-   // back substitution f(i) -= c'(i) f(i+1), i = N-2..0; the halves run
-   // t = 0..Nmax-2 with i = N-2-t
-   double xnext[4];
-#pragma unroll
-   for (int m = 0; m < 4; m++) xnext[m] = xprev[m];
-   // a row here is a few dependent operations, shorter than a load: rows
-   // ii-1 and ii-2 are in flight while row ii is solved
-   double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
-   if (N >= 2) {
-      mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
-      xi = fs[4 * (N - 2) + r];
-   }
-   if (N >= 3) {
-      mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
-      xi1 = fs[4 * (N - 3) + r];
-   }
-   for (int t = 0; t <= Nmax - 2; t++) {
-      const int ii = N - 2 - t;
-      double mv2 = 0.0, xi2 = 0.0;
-      if (ii > 1) {
-         mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
-         xi2 = fs[4 * (ii - 2) + r];
-      }
-      const double prod = mv * sel4(xnext, pj);
-      double x = xi;
-#pragma unroll
-      for (int jj = 0; jj < 4; jj++) x = x - __shfl_sync(kLaneMask, prod, hb + 4 * r + jj);
-#pragma unroll
-      for (int m = 0; m < 4; m++) xnext[m] = __shfl_sync(kLaneMask, x, hb + m);
-      if (e < 4 && ii >= 0) fs[4 * ii + e] = x;
-      mv = mv1;
-      xi = xi1;
-      mv1 = mv2;
-      xi1 = xi2;
-   }
+   back_line_pair(fac, N, fs, lane, xprev);
 }
 
 // ---- eight open lines per warp, four lanes each --------------------------
