@@ -117,13 +117,13 @@ __device__ __forceinline__ bool factor_pair(const DeviceState& d, int ia, int ib
    return factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
 }
 
-// Where a schedule has outlier jobs (ncrit > 0), the first warp of block b
-// (one block per SM) starts with job b, so each outlier starts on an SM of
-// its own, and the other warps of the ncrit blocks holding them take no
-// job; the counter then numbers the jobs after the assigned ones (off =
-// the number of blocks).  Otherwise every warp takes every job from the
-// counter (off = 0): with many equal long jobs, spreading them one per SM
-// beside shorter ones measured slower than packing them.
+// Where a schedule has long jobs to place (ncrit != 0), the first warp of
+// block b (one block per SM) starts with job b, so each long job starts on
+// an SM of its own; beside a few outliers (ncrit > 0) the other warps of
+// the blocks holding them take no job, beside many (ncrit < 0, the loops of
+// a quad O-grid) they take jobs as usual.  The counter then numbers the jobs
+// after the assigned ones (off = the number of blocks).  Otherwise every
+// warp takes every job from the counter (off = 0).
 
 // next job index of a persistent warp: lane 0 takes it from the counter
 __device__ __forceinline__ int take_job(int* ctr, int off, int lane)

@@ -380,7 +380,7 @@ struct hamstr_gpu {
          adi_lanes = lanes;
          adi_bundle = bundle;
          adi_fuse = fuse;
-         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle, fuse != 0, adi_fwpb * nsm);
+         sched = build_schedule(plan, adi_wpb * nsm, lanes, bundle, fuse != 0, adi_fwpb * nsm, nsm);
          const int st = upload_schedule();
          if (st) return st;
       }
@@ -674,7 +674,8 @@ int hamstr::create_gpu(const hamstr_gpu_params* p, int nCell, int nFace, const i
       // the shortest open chains one per lane where chains are short (the
       // autotuner checks the alternatives)
       g->adi_bundle = (P.nChain > 0 && P.nRow < 16 * P.nChain) ? 8 : 0;
-      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle, g->adi_fuse != 0, d.adi_fwpb * nsm);
+      g->sched = build_schedule(P, d.adi_wpb * nsm, g->adi_lanes, g->adi_bundle, g->adi_fuse != 0, d.adi_fwpb * nsm,
+                                nsm);
    }
    TRY(g->upload_schedule());
    d.nWave = P.nWave;

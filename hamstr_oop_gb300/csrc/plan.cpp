@@ -315,7 +315,7 @@ std::string build_plan(const MeshInput& in, Plan& p)
 }
 
 Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows, bool fuse_first_wave,
-                        int max_warps_factor)
+                        int max_warps_factor, int nsm)
 {
    Schedule S;
    S.job_ptr.push_back(0);
@@ -369,10 +369,20 @@ Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle
       std::stable_sort(order.begin(), order.end(), [](const Job& x, const Job& y) { return x.cost > y.cost; });
       S.job0.push_back((int)S.job_ptr.size() - 1);
       S.njobs.push_back((int)order.size());
-      S.nwarps.push_back(std::min((int)order.size(), maxw));
+      int nw = std::min((int)order.size(), maxw);
       int nc = 0;
       while (nc < (int)order.size() && order[nc].cost >= kCritFrac * order[0].cost) nc++;
-      S.ncrit.push_back(nc <= kMaxCrit ? nc : 0);
+      if (nc <= kMaxCrit) {
+         S.ncrit.push_back(nc);
+      } else if (nsm > 0) {
+         // many long jobs: one per SM, and a block on every SM that holds one
+         const int spread = std::min(nc, nsm), wpb = std::max(1, maxw / nsm);
+         S.ncrit.push_back(-spread);
+         nw = std::max(nw, std::min(spread * wpb, maxw));
+      } else {
+         S.ncrit.push_back(0);
+      }
+      S.nwarps.push_back(nw);
       for (const Job& j : order) {
          S.jobs.insert(S.jobs.end(), j.entries.begin(), j.entries.end());
          S.job_ptr.push_back((int)S.jobs.size());

@@ -84,7 +84,7 @@ std::string build_plan(const MeshInput& in, Plan& out);
 //   - (kBundleJob | n), c_1 .. c_n: n <= 32 open chains of at most
 //     bundle_rows rows, one per lane.
 // nwarps[s] = min(njobs[s], max_warps) warps are launched (max_warps_factor
-// for the factorisation).  With
+// for the factorisation), more where long jobs are spread (below).  With
 // fuse_first_wave the factorisation's jobs for the first wave's chains are
 // packed as that wave's solve packs them and carry kFusedJob on their first
 // entry: the warp that factors them runs their first sweep's solve at once.
@@ -92,11 +92,15 @@ constexpr int kPairJob = 1 << 30;
 constexpr int kBundleJob = 1 << 29;
 constexpr int kQuadJob = 1 << 28;
 constexpr int kFusedJob = 1 << 27;
-// The ncrit[s] leading jobs of a schedule that are outliers (cost at
-// least kCritFrac of the longest, and at most kMaxCrit of them; else 0)
-// run alone on their SM: the first warp of block b starts with job b and
-// the other warps of those blocks take no job, so no other FP64 work
-// shares the SM while the chain that sets the launch's length runs.
+// The leading jobs of a schedule whose cost is at least kCritFrac of the
+// longest set the launch's length.  ncrit[s] > 0: at most kMaxCrit such
+// outliers, each runs alone on its SM (the first warp of block b starts with
+// job b and the other warps of those blocks take no job), so no other FP64
+// work shares the SM while the chain that sets the launch's length runs.
+// ncrit[s] = -n: more of them (the periodic loops of a quad O-grid), the
+// first n = min(count, nsm) spread one per SM the same way, with a block on
+// each of those SMs, but the other warps keep taking jobs.  0: no spreading
+// (nsm = 0 or no long job).
 constexpr double kCritFrac = 0.8;
 constexpr int kMaxCrit = 8;
 struct Schedule {
@@ -105,9 +109,10 @@ struct Schedule {
    std::vector<int> job_ptr;               // per job (all schedules), +1
    std::vector<int> jobs;                  // job entries, as above
 };
-// max_warps_factor (0: max_warps) bounds the factorisation's warps, max_warps the solves'.
+// max_warps_factor (0: max_warps) bounds the factorisation's warps, max_warps the solves';
+// both are a multiple of nsm, the number of SMs (one block per SM).
 Schedule build_schedule(const Plan& p, int max_warps, int open_lanes, int bundle_rows,
-                        bool fuse_first_wave = false, int max_warps_factor = 0);
+                        bool fuse_first_wave = false, int max_warps_factor = 0, int nsm = 0);
 
 }  // namespace hamstr
 #endif

@@ -48,13 +48,16 @@ int main(int argc, char** argv) {
    Plan p;
    const std::string e = build_plan(in, p);
    if (!e.empty()) { std::printf("FAIL plan %s\n", e.c_str()); return 1; }
-   int checked = 0, nper = 0;
+   int checked = 0, nper = 0, nspread = 0;
    for (int ch = 0; ch < p.nChain; ch++) nper += p.chain_periodic[ch];
    for (int maxw : {1, 7, 608})
+    for (int spread : {0, 1})
       for (int lanes : {32, 16, 4})
          for (int br : {0, 2, 8, 64})
           for (int fuse : {0, 1}) {
-            const Schedule S = build_schedule(p, maxw, lanes, br, fuse != 0);
+            // nsm SMs with maxw / nsm warps each (0: long jobs not spread)
+            const int nsm = spread ? (maxw == 608 ? 152 : maxw) : 0;
+            const Schedule S = build_schedule(p, maxw, lanes, br, fuse != 0, 0, nsm);
             if ((int)S.njobs.size() != 1 + p.nWave) return fail("schedules", (int)S.njobs.size(), p.nWave);
             for (int s = 0; s <= p.nWave; s++) {
                std::vector<int> seen(p.nChain, 0);
@@ -100,15 +103,26 @@ int main(int argc, char** argv) {
                   const int want = (s == 0 || p.chain_wave[ch] == s - 1) ? 1 : 0;
                   if (seen[ch] != want) return fail("coverage", ch, seen[ch]);
                }
-               const int nw = S.nwarps[s];
-               if (nw != (S.njobs[s] < maxw ? S.njobs[s] : maxw)) return fail("warps", nw, S.njobs[s]);
-               if ((int)S.ncrit.size() != 1 + p.nWave || S.ncrit[s] < 0 || S.ncrit[s] > kMaxCrit ||
-                   S.ncrit[s] > S.njobs[s])
-                  return fail("outlier jobs", S.ncrit[s], S.njobs[s]);
+               const int nw = S.nwarps[s], base = S.njobs[s] < maxw ? S.njobs[s] : maxw;
+               if ((int)S.ncrit.size() != 1 + p.nWave) return fail("outlier lists", (int)S.ncrit.size(), p.nWave);
+               const int nc = S.ncrit[s];
+               if (nc >= 0) {
+                  // outliers alone on their SM, or nothing placed
+                  if (nc > kMaxCrit || nc > S.njobs[s]) return fail("outlier jobs", nc, S.njobs[s]);
+                  if (nw != base) return fail("warps", nw, S.njobs[s]);
+               } else {
+                  // long jobs spread one per SM, a block on each of those SMs
+                  const int wpb = maxw / nsm;
+                  if (nsm == 0 || -nc > S.njobs[s] || -nc > nsm || (-nc <= kMaxCrit && -nc != nsm))
+                     return fail("spread jobs", nc, S.njobs[s]);
+                  if (nw != std::max(base, std::min(-nc * wpb, maxw))) return fail("spread warps", nw, -nc);
+                  if (nw > maxw || (nw + wpb - 1) / wpb < -nc) return fail("spread blocks", nw, -nc);
+                  nspread++;
+               }
                checked++;
             }
          }
-   std::printf("OK %d %d %d %d\n", checked, p.nChain, nper, p.nWave);
+   std::printf("OK %d %d %d %d %d\n", checked, p.nChain, nper, p.nWave, nspread);
    hamstr_case_close(c);
    return 0;
 }
@@ -126,13 +140,16 @@ def harness(tmp_path_factory, native_lib):
     return str(exe)
 
 
-@pytest.mark.parametrize("ni,nj,split,extended", [(32, 8, 0.0, False), (24, 8, 0.5, True), (40, 10, 0.3, True)])
+@pytest.mark.parametrize("ni,nj,split,extended", [(32, 8, 0.0, False), (32, 12, 0.0, False), (24, 8, 0.5, True),
+                                                   (40, 10, 0.3, True)])
 def test_line_job_queues(harness, make_case, ni, nj, split, extended):
     case = make_case(ni, nj, split=split, seed=4, order=3)
     args = [harness, case] + (["extended"] if extended else [])
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0 and out.stdout.startswith("OK"), out.stdout + out.stderr
-    checked, nchain, nper, nwave = (int(x) for x in out.stdout.split()[1:])
-    assert checked == 3 * 3 * 4 * 2 * (1 + nwave) and nchain > 0
+    checked, nchain, nper, nwave, nspread = (int(x) for x in out.stdout.split()[1:])
+    assert checked == 3 * 2 * 3 * 4 * 2 * (1 + nwave) and nchain > 0
     if split == 0.0:
         assert nper > 0                  # the plain O-grid has periodic loops beside open lines
+    if nj > 8 and split == 0.0:
+        assert nspread > 0               # more equal loops than outliers: spread one per SM
