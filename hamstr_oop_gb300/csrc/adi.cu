@@ -92,14 +92,15 @@ __global__ void __launch_bounds__(256) adi_assemble_kernel(DeviceState d)
 }
 
 // block-Thomas factorisation of chain ich (its assembled rows in blk)
+// (prog: rows published for a following solve, line_solve.cuh publish_rows)
 template <bool SD>
-__device__ __forceinline__ bool factor_chain(const DeviceState& d, int ich, int lane)
+__device__ __forceinline__ bool factor_chain(const DeviceState& d, int ich, int lane, int* prog = nullptr)
 {
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
    const double* blk = d.blk + 48 * (size_t)row0;
    return factor_line<SD>(blk, blk + 16, blk + 32, 48, N, per, d.fac + (size_t)kFacRec * row0,
-               per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane);
+               per ? d.facN + 16 * d.chain_facN[ich] : nullptr, lane, prog);
 }
 
 // rows of chain ich for this half-warp's work: 0 once its instance is frozen
@@ -110,11 +111,11 @@ __device__ __forceinline__ int live_rows(const DeviceState& d, int ich)
 
 // two open chains, one per half-warp (line_solve.cuh factor_line_pair)
 template <bool SD>
-__device__ __forceinline__ bool factor_pair(const DeviceState& d, int ia, int ib, int lane)
+__device__ __forceinline__ bool factor_pair(const DeviceState& d, int ia, int ib, int lane, int* prog = nullptr)
 {
    const int ich = (lane >> 4) ? ib : ia;
    const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
-   return factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane);
+   return factor_line_pair<SD>(d.blk + 48 * (size_t)row0, 48, N, d.fac + (size_t)kFacRec * row0, lane, prog);
 }
 
 // Where a schedule has long jobs to place (ncrit != 0), the first warp of
@@ -144,8 +145,11 @@ __device__ __forceinline__ int first_job(int* ctr, int ncrit, int off, int lane)
 }
 
 // one sweep's solve of chain ich: F = r[fcell] (ADI.cpp:116,187), the
-// replay, and the write-back r[scell] = F (ADI.cpp:232-244)
-__device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int lane)
+// replay, and the write-back r[scell] = F (ADI.cpp:232-244); FOLLOW: behind
+// its factorisation by another warp of the block (line_solve.cuh)
+template <bool FOLLOW = false>
+__device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int lane, const int* prog = nullptr,
+                                            bool* ok = nullptr)
 {
    const int N = d.chain_nrows[ich], row0 = d.chain_row0[ich];
    const bool per = d.chain_periodic[ich] != 0;
@@ -158,7 +162,8 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
       *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
    }
    __syncwarp();
-   solve_line(d.fac + (size_t)kFacRec * row0, per ? d.facN + 16 * d.chain_facN[ich] : nullptr, N, per, fs, lane);
+   solve_line<FOLLOW>(d.fac + (size_t)kFacRec * row0, per ? d.facN + 16 * d.chain_facN[ich] : nullptr, N, per, fs,
+                      lane, prog, ok);
    __syncwarp();
    for (int r = lane; r < N; r += 32) {
       const int sc = d.row_scell[row0 + r];
@@ -170,7 +175,9 @@ __device__ __forceinline__ void solve_chain(const DeviceState& d, int ich, int l
 }
 
 // the same for two open chains, one per half-warp
-__device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib, int lane)
+template <bool FOLLOW = false>
+__device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib, int lane, const int* prog = nullptr,
+                                           bool* ok = nullptr)
 {
    const int ich = (lane >> 4) ? ib : ia, l16 = lane & 15;
    const int N = live_rows(d, ich), row0 = d.chain_row0[ich];
@@ -183,7 +190,7 @@ __device__ __forceinline__ void solve_pair(const DeviceState& d, int ia, int ib,
       *reinterpret_cast<double2*>(fs + 4 * r + 2) = make_double2(v[2], v[3]);
    }
    __syncwarp();
-   solve_line_pair(d.fac + (size_t)kFacRec * row0, N, fs, lane);
+   solve_line_pair<FOLLOW>(d.fac + (size_t)kFacRec * row0, N, fs, lane, prog, ok);
    __syncwarp();
    for (int r = l16; r < N; r += 16) {
       const int sc = d.row_scell[row0 + r];
@@ -298,17 +305,49 @@ __device__ __forceinline__ void solve_job(const DeviceState& d, int job, int ich
 // the same warp right after its factorisation: its right-hand sides are
 // the computeRHS residuals, ready before this kernel, and the chains of
 // one wave share no cell, so no other job waits for it.
+//
+// A long first job of block b (ncrit != 0, b < |ncrit|) that carries its
+// first sweep's solve (kFusedJob, one chain or a pair) is solved by the
+// block's second warp behind the factorisation of the first (the rows are
+// published in shared memory as their records are stored), instead of by
+// the factoring warp after it: a row's factorisation takes about three
+// times its solve, so the solve adds only its last rows and the back
+// substitution to the job's time.  Beside an outlier (ncrit > 0) that
+// second warp was idle; beside many long jobs it takes queued jobs after.
 template <bool SD>
 __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int nwarps)
 {
+   __shared__ int prog;   // rows of the block's followed job that are factored
+   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, b = blockIdx.x;
+   const int nj = d.sched_njobs[0], j0 = d.sched_job0[0];
+   const int ncrit = d.sched_ncrit[0], nlong = ncrit < 0 ? -ncrit : ncrit;
+   int fjob = -1, fich = 0;   // the followed job: warp 0's first, solved by warp 1
+   if (b < nlong && b < nj && b * (int)(blockDim.x >> 5) + 1 < nwarps) {
+      const int job = d.sched_job_ptr[j0 + b], head = d.sched_jobs[job];
+      if ((head & kFusedJob) && !(head & (kBundleJob | kQuadJob))) {
+         fjob = job;
+         fich = head & ~kFusedJob;
+      }
+   }
+   if (threadIdx.x == 0) prog = 0;
+   __syncthreads();
    if (halted(d)) return;
-   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+   const int w = b * (blockDim.x >> 5) + wib;
    if (w >= nwarps) return;
-   const int lane = threadIdx.x & 31, nj = d.sched_njobs[0], j0 = d.sched_job0[0];
    int* ctr = d.sched_ctr;
    bool bad = false;
-   const int ncrit = d.sched_ncrit[0], off = ncrit ? (int)gridDim.x : 0;
-   const int k0 = first_job(ctr, ncrit, off, lane);
+   const int off = ncrit ? (int)gridDim.x : 0;
+   int k0;
+   if (fjob >= 0 && wib == 1) {
+      bool ok = true;
+      if (fich & kPairJob) solve_pair<true>(d, fich & ~kPairJob, d.sched_jobs[fjob + 1], lane, &prog, &ok);
+      else if (!frozen_chain(d, fich)) solve_chain<true>(d, fich, lane, &prog, &ok);
+      if (!ok && lane == 0) atomicOr(d.status, DEV_ERR_WAIT);
+      if (ncrit > 0) return;
+      k0 = take_job(ctr, off, lane);
+   } else {
+      k0 = first_job(ctr, ncrit, off, lane);
+   }
    if (k0 < 0) return;
    for (int k = k0; k < nj;) {
       // the next job's index is fetched while this one runs
@@ -316,7 +355,11 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
       if (lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       const int head = d.sched_jobs[job], ich = head & ~kFusedJob;
-      if ((head & kFusedJob) && (ich & kPairJob)) {
+      if (job == fjob) {
+         // factorisation only, its solve follows in warp 1
+         if (ich & kPairJob) bad |= factor_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane, &prog);
+         else if (!frozen_chain(d, ich)) bad |= factor_chain<SD>(d, ich, lane, &prog);
+      } else if ((head & kFusedJob) && (ich & kPairJob)) {
          bad |= factor_solve_pair<SD>(d, ich & ~kPairJob, d.sched_jobs[job + 1], lane);
       } else {
          bad |= factor_job<SD>(d, job, ich, lane);

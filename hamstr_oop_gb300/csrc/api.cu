@@ -438,6 +438,10 @@ struct hamstr_gpu {
          set_error("zero or non-finite LU pivot in an ADI line factorisation");
          return HAMSTR_GPU_ERR_SINGULAR;
       }
+      if (s & DEV_ERR_WAIT) {
+         set_error("an ADI line solve gave up waiting for its factorisation");
+         return HAMSTR_GPU_ERR_CUDA;
+      }
       set_error("non-finite dq after an ADI sweep");
       return HAMSTR_GPU_ERR_NONFINITE;
    }

@@ -30,6 +30,7 @@ enum {
    DEV_ERR_NAN_SPEC = 1,     // spectral radius is NaN (interfaceFlux.cpp:117-124)
    DEV_ERR_PIVOT = 2,        // an ADI line's LU pivot is zero or not finite (reciprocal not finite)
    DEV_ERR_DQ = 4,           // an ADI sweep left a non-finite dq
+   DEV_ERR_WAIT = 8,         // a line solve gave up waiting for its factorisation (adi.cu; never expected)
 };
 
 struct FlowConst {

@@ -33,6 +33,43 @@ namespace hamstr {
 constexpr int kFacRec = 80;
 constexpr unsigned kLaneMask = 0xffffffffu;
 
+// A factorisation followed by a solving warp of the same block (adi.cu):
+// the factoring warp publishes in shared memory how many rows' records it
+// has stored (publish_rows: its stores, a block-scope fence, then the
+// count); the follower waits until the rows it needs are there
+// (wait_rows: the count, then a block-scope fence) before it loads them
+// (ldf).
+// The factoring warp never waits, so every wait ends; the bound (well
+// above the longest legitimate wait, a periodic line's last-row
+// elimination) only guards against a broken schedule: a wait that gives up
+// returns false, the follower waits no more and the caller raises an error
+// word.
+constexpr long kFollowSpin = 1L << 24;
+
+__device__ __forceinline__ void publish_rows(int* prog, int n, int lane)
+{
+   __threadfence_block();
+   __syncwarp();
+   if (lane == 0) *(volatile int*)prog = n;
+}
+
+__device__ __forceinline__ bool wait_rows(const int* prog, int need)
+{
+   long it = 0;
+   while (*(const volatile int*)prog < need)
+      if (++it > kFollowSpin) return false;
+   __threadfence_block();
+   return true;
+}
+
+// a record load of a follower: an ordinary coherent load (never the
+// read-only path, whose cache need not see stores made during the kernel)
+template <bool FOLLOW>
+__device__ __forceinline__ double ldf(const double* p)
+{
+   return FOLLOW ? __ldca(p) : *p;
+}
+
 // x <- LU^{-1} x for a 4-vector held one component per lane: component l
 // lives in lane base + stride*l, r is this lane's component and lu its LU
 // row (L[r][0..r-1], reciprocal pivot, U[r][r+1..3]).  Same operations and
@@ -205,10 +242,13 @@ __device__ __forceinline__ void lu_back4(const double (&d)[4], const double (&U)
 // periodic, the LU of the final last-row block into facN.  Returns, in the
 // lanes that hold a pivot, whether a stored reciprocal pivot is infinite or
 // NaN (a zero or non-finite pivot; the reference divides by it regardless).
+// With prog, the rows are published as they are stored (publish_rows),
+// and N + 1 once a periodic line's last-row records are.
 template <bool SD = true>
 __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const double* __restrict__ Bb,
                                             const double* __restrict__ Cb, size_t stride, int N, bool per,
-                                            double* __restrict__ fac, double* __restrict__ facN, int lane)
+                                            double* __restrict__ fac, double* __restrict__ facN, int lane,
+                                            int* prog = nullptr)
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3;
    double A = Ab[e], B = Bb[e], C = Cb[e];
@@ -261,6 +301,7 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
       }
       Yp = sel4(P, k);
       rec[32 + 16 * h + e] = Yp;
+      if (prog) publish_rows(prog, i + 1, lane);
       A = An;
       B = Bn;
       C = Cn;
@@ -287,6 +328,7 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
    }
    const double w = lu_wavefront<SD>(__shfl_sync(kLaneMask, bN, 16 + e), 16 * h, e);
    if (h == 0) facN[e] = w;
+   if (prog) publish_rows(prog, N + 1, lane);
    return bad || (h == 0 && k == j && nonfinite(w));
 }
 
@@ -308,7 +350,7 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
 template <bool SD, bool F>
 __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
                                                  double* __restrict__ fac, int lane, double* __restrict__ fs,
-                                                 double (&xlast)[4])
+                                                 double (&xlast)[4], int* prog = nullptr)
 {
    const int h = lane >> 4, e = lane & 15, k = e >> 2, j = e & 3, hb = 16 * h;
    const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
@@ -358,6 +400,7 @@ __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, 
          for (int m = 0; m < 4; m++)
             if (live) X[m] = x[m];   // the shorter line keeps its last row's solution
       }
+      if (prog) publish_rows(prog, i + 1, lane);
       A = An;
       B = Bn;
       C = Cn;
@@ -370,15 +413,16 @@ __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, 
 
 template <bool SD = true>
 __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
-                                                 double* __restrict__ fac, int lane)
+                                                 double* __restrict__ fac, int lane, int* prog = nullptr)
 {
    double unused[4];
-   return factor_line_pair<SD, false>(Ab, stride, N, fac, lane, nullptr, unused);
+   return factor_line_pair<SD, false>(Ab, stride, N, fac, lane, nullptr, unused, prog);
 }
 
 // back substitution f(i) -= c'(i) f(i+1), i = N-2..0, of two open lines,
 // one per half-warp (triSolvers.cpp:839-846): fs holds the forward sweep's
 // rows and receives the solution, xlast is row N-1's solution (every lane)
+template <bool FOLLOW = false>
 __device__ __forceinline__ void back_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs,
                                                int lane, const double (&xlast)[4])
 {
@@ -391,18 +435,18 @@ __device__ __forceinline__ void back_line_pair(const double* __restrict__ fac, i
    // ii-1 and ii-2 are in flight while row ii is solved
    double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
    if (N >= 2) {
-      mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
+      mv = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 2) + 32 + e]);
       xi = fs[4 * (N - 2) + r];
    }
    if (N >= 3) {
-      mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
+      mv1 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 3) + 32 + e]);
       xi1 = fs[4 * (N - 3) + r];
    }
    for (int t = 0; t <= Nmax - 2; t++) {
       const int ii = N - 2 - t;
       double mv2 = 0.0, xi2 = 0.0;
       if (ii > 1) {
-         mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
+         mv2 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (ii - 2) + 32 + e]);
          xi2 = fs[4 * (ii - 2) + r];
       }
       const double prod = mv * sel4(xnext, pj);
@@ -421,25 +465,31 @@ __device__ __forceinline__ void back_line_pair(const double* __restrict__ fac, i
 
 // Right-hand-side replay of two factored open lines, one per half-warp:
 // the operations of solve_line's open branch on lanes 0-15, per half.
-__device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs, int lane)
+// FOLLOW: behind the factorisation of the same lines by another warp of
+// the block (prog, publish_rows); ok turns false if a wait gave up.
+template <bool FOLLOW = false>
+__device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs, int lane,
+                                                const int* prog = nullptr, bool* ok = nullptr)
 {
    const int e = lane & 15, pj = e & 3, r = lane & 3, hb = lane & 16;
    const int Nmax = max(N, __shfl_xor_sync(kLaneMask, N, 16));
    double xprev[4] = {0.0, 0.0, 0.0, 0.0};
    double fv = 0.0, av = 0.0, lu[4] = {0.0, 0.0, 0.0, 0.0};
+   if (FOLLOW && *ok && Nmax > 0 && !wait_rows(prog, 1)) *ok = false;
    if (N > 0) {
       fv = fs[r];
 #pragma unroll
-      for (int c = 0; c < 4; c++) lu[c] = fac[16 + 4 * r + c];
+      for (int c = 0; c < 4; c++) lu[c] = ldf<FOLLOW>(&fac[16 + 4 * r + c]);
    }
    for (int i = 0; i < Nmax; i++) {
       double fvn = 0.0, avn = 0.0, lun[4] = {0.0, 0.0, 0.0, 0.0};
+      if (FOLLOW && *ok && i + 1 < Nmax && !wait_rows(prog, i + 2)) *ok = false;
       if (i + 1 < N) {
          const double* nr = fac + (size_t)kFacRec * (i + 1);
          fvn = fs[4 * (i + 1) + r];
-         avn = nr[e];
+         avn = ldf<FOLLOW>(&nr[e]);
 #pragma unroll
-         for (int c = 0; c < 4; c++) lun[c] = nr[16 + 4 * r + c];
+         for (int c = 0; c < 4; c++) lun[c] = ldf<FOLLOW>(&nr[16 + 4 * r + c]);
       }
       double x = fv;
       if (i > 0) {
@@ -460,7 +510,8 @@ __device__ __forceinline__ void solve_line_pair(const double* __restrict__ fac, 
       av = avn;
    }
    __syncwarp();
-   back_line_pair(fac, N, fs, lane, xprev);
+   if (FOLLOW && *ok && !wait_rows(prog, Nmax)) *ok = false;
+   back_line_pair<FOLLOW>(fac, N, fs, lane, xprev);
 }
 
 // ---- eight open lines per warp, four lanes each --------------------------
@@ -887,24 +938,30 @@ __device__ __forceinline__ void ld4(const double* __restrict__ p, double (&v)[4]
 // lanes e = 4*pr + pj (e = lane & 15) and handed to their owner lanes with
 // shuffles, so each row costs about 35 FP64 instructions instead of 60.
 // The subtraction order of every component is the reference's.
+// FOLLOW: behind the factorisation of the same line by another warp of the
+// block (prog, publish_rows); ok turns false if a wait gave up.
+template <bool FOLLOW = false>
 __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const double* __restrict__ facN, int N,
-                                           bool per, double* __restrict__ fs, int lane)
+                                           bool per, double* __restrict__ fs, int lane, const int* prog = nullptr,
+                                           bool* ok = nullptr)
 {
    const int e = lane & 15, pr = e >> 2, pj = e & 3, hi = lane >> 4;
    const int r = lane & 3;
    // ---- forward sweep (triSolvers.cpp:778-822 / 859-933); row i+1 prefetched
    double xprev[4] = {0.0, 0.0, 0.0, 0.0};
+   if (FOLLOW && *ok && !wait_rows(prog, 1)) *ok = false;
    double fv = fs[r], av = 0.0, lu[4];
 #pragma unroll
-   for (int c = 0; c < 4; c++) lu[c] = fac[16 + 4 * r + c];
+   for (int c = 0; c < 4; c++) lu[c] = ldf<FOLLOW>(&fac[16 + 4 * r + c]);
    for (int i = 0; i < N; i++) {
       double fvn = 0.0, avn = 0.0, lun[4] = {0.0, 0.0, 0.0, 0.0};
       if (i + 1 < N) {
+         if (FOLLOW && *ok && !wait_rows(prog, i + 2)) *ok = false;
          const double* nr = fac + (size_t)kFacRec * (i + 1);
          fvn = fs[4 * (i + 1) + r];
-         avn = nr[e];
+         avn = ldf<FOLLOW>(&nr[e]);
 #pragma unroll
-         for (int c = 0; c < 4; c++) lun[c] = nr[16 + 4 * r + c];
+         for (int c = 0; c < 4; c++) lun[c] = ldf<FOLLOW>(&nr[16 + 4 * r + c]);
       }
       double x = fv;
       if (i > 0) {
@@ -922,6 +979,7 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       av = avn;
    }
    __syncwarp();
+   if (FOLLOW && *ok && !wait_rows(prog, per ? N + 1 : N)) *ok = false;
    if (per) {
       // f(N-1) -= c_{N-1}^{(i)} f(i), i = 0..N-2 (triSolvers.cpp:991-999);
       // the products of rows i and i+1 in one instruction (lanes 0-15, 16-31)
@@ -929,14 +987,14 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       int i = 0;
       double c = 0.0, f = 0.0;
       if (hi < N - 1) {
-         c = fac[(size_t)kFacRec * hi + 64 + e];
+         c = ldf<FOLLOW>(&fac[(size_t)kFacRec * hi + 64 + e]);
          f = fs[4 * hi + pj];
       }
       for (; i < N - 1; i += 2) {
          const int rn = i + 2 + hi;
          double cn = 0.0, fn = 0.0;
          if (rn < N - 1) {
-            cn = fac[(size_t)kFacRec * rn + 64 + e];
+            cn = ldf<FOLLOW>(&fac[(size_t)kFacRec * rn + 64 + e]);
             fn = fs[4 * rn + pj];
          }
          const double p = c * f;
@@ -951,7 +1009,7 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       }
       double luN[4], xn[4];
 #pragma unroll
-      for (int cc = 0; cc < 4; cc++) luN[cc] = facN[4 * r + cc];
+      for (int cc = 0; cc < 4; cc++) luN[cc] = ldf<FOLLOW>(&facN[4 * r + cc]);
       fN = lu_solve_lanes(luN, r, fN, 0, 1, xn);
       __syncwarp();
       if (lane < 4) fs[4 * (N - 1) + lane] = fN;
@@ -967,17 +1025,17 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       // rows ii-1 and ii-2 are in flight while row ii is solved
       double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
       if (N >= 2) {
-         mv = fac[(size_t)kFacRec * (N - 2) + 32 + 16 * hi + e];
+         mv = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 2) + 32 + 16 * hi + e]);
          xi = fs[4 * (N - 2) + r];
       }
       if (N >= 3) {
-         mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + 16 * hi + e];
+         mv1 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 3) + 32 + 16 * hi + e]);
          xi1 = fs[4 * (N - 3) + r];
       }
       for (int ii = N - 2; ii >= 0; ii--) {
          double mv2 = 0.0, xi2 = 0.0;
          if (ii > 1) {
-            mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + 16 * hi + e];
+            mv2 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (ii - 2) + 32 + 16 * hi + e]);
             xi2 = fs[4 * (ii - 2) + r];
          }
          const double prod = mv * (hi ? sel4(fNall, pj) : sel4(xnext, pj));
@@ -1002,17 +1060,17 @@ __device__ __forceinline__ void solve_line(const double* __restrict__ fac, const
       // rows ii-1 and ii-2 are in flight while row ii is solved
       double mv = 0.0, xi = 0.0, mv1 = 0.0, xi1 = 0.0;
       if (N >= 2) {
-         mv = fac[(size_t)kFacRec * (N - 2) + 32 + e];
+         mv = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 2) + 32 + e]);
          xi = fs[4 * (N - 2) + r];
       }
       if (N >= 3) {
-         mv1 = fac[(size_t)kFacRec * (N - 3) + 32 + e];
+         mv1 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (N - 3) + 32 + e]);
          xi1 = fs[4 * (N - 3) + r];
       }
       for (int ii = N - 2; ii >= 0; ii--) {
          double mv2 = 0.0, xi2 = 0.0;
          if (ii > 1) {
-            mv2 = fac[(size_t)kFacRec * (ii - 2) + 32 + e];
+            mv2 = ldf<FOLLOW>(&fac[(size_t)kFacRec * (ii - 2) + 32 + e]);
             xi2 = fs[4 * (ii - 2) + r];
          }
          const double prod = mv * sel4(xnext, pj);
