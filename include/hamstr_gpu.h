@@ -38,7 +38,8 @@ extern "C" {
 #define HAMSTR_GPU_OK             0
 #define HAMSTR_GPU_ERR_ARG       -1   /* bad argument or unknown array name */
 #define HAMSTR_GPU_ERR_TOPOLOGY  -2   /* chains/faces the reference cannot process */
-#define HAMSTR_GPU_ERR_CUDA      -3   /* CUDA runtime failure */
+#define HAMSTR_GPU_ERR_CUDA      -3   /* CUDA runtime failure; also a line solve that gave up waiting
+                                         for its factorisation (never expected) */
 #define HAMSTR_GPU_ERR_NAN       -4   /* NaN spectral radius (interfaceFlux.cpp:117-124) */
 #define HAMSTR_GPU_ERR_IO        -5   /* missing or malformed case file (io.cpp:19-23,138-141) */
 #define HAMSTR_GPU_ERR_NOMEM     -6   /* host or device allocation failed */
@@ -313,6 +314,13 @@ int hamstr_mlp_train_step(hamstr_mlp* h, const float* features, const float* tar
  * (hamstr_oop_gb300/csrc/softdiv.cuh), hard[i] = the hardware a[i]/b[i],
  * on device arrays of n doubles.  Tests compare them bit for bit. */
 int hamstr_check_softdiv(const double* a, const double* b, double* soft, double* hard, int n, void* stream);
+
+/* Self-test hook for the shared-memory row count that a line solve waits on
+ * behind its factorisation (hamstr_oop_gb300/csrc/line_solve.cuh): in one
+ * block, one warp publishes 3 rows and stops; another waits for 1, 3 and 4
+ * rows.  out[0..2] (device ints) receive 1 for a wait that was met and 0 for
+ * one that gave up at its bound; expected {1, 1, 0}, and the kernel ends. */
+int hamstr_check_row_wait(int* out, void* stream);
 
 /* Changes the pseudo-time CFL number of later steps (no counterpart in the
  * reference, which reads CFL once, io.cpp:37).  Lets a caller ramp CFL up

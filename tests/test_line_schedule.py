@@ -153,3 +153,23 @@ def test_line_job_queues(harness, make_case, ni, nj, split, extended):
         assert nper > 0                  # the plain O-grid has periodic loops beside open lines
     if nj > 8 and split == 0.0:
         assert nspread > 0               # more equal loops than outliers: spread one per SM
+
+
+@pytest.mark.gpu
+def test_row_wait_gives_up_at_its_bound(native_lib):
+    """The shared-memory row count a line solve waits on behind its
+    factorisation (line_solve.cuh publish_rows / wait_rows): waits for
+    published rows are met, a wait for a row that is never published gives
+    up at its bound instead of spinning on, and the kernel ends."""
+    import ctypes
+    import time
+    import torch
+    out = torch.full((3,), -1, dtype=torch.int32, device="cuda")
+    fn = native_lib.hamstr_check_row_wait
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    t0 = time.perf_counter()
+    assert fn(out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 30
+    assert out.cpu().tolist() == [1, 1, 0]
