@@ -346,7 +346,9 @@ __device__ __forceinline__ bool factor_line(const double* __restrict__ Ab, const
 // With F the line's first solve runs in the same loop: fs holds f (the
 // right-hand sides, rows of 4) and receives the forward sweep's rows
 // (triSolvers.cpp:786-822, the reference's own loop), and xlast the last
-// row's solution, for the back substitution (back_line_pair).
+// row's solution, for the back substitution (back_line_pair).  With prog
+// each row is published once its records are stored (publish_rows), for a
+// solve that follows in another warp.
 template <bool SD, bool F>
 __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, size_t stride, int N,
                                                  double* __restrict__ fac, int lane, double* __restrict__ fs,
@@ -421,7 +423,8 @@ __device__ __forceinline__ bool factor_line_pair(const double* __restrict__ Ab, 
 
 // back substitution f(i) -= c'(i) f(i+1), i = N-2..0, of two open lines,
 // one per half-warp (triSolvers.cpp:839-846): fs holds the forward sweep's
-// rows and receives the solution, xlast is row N-1's solution (every lane)
+// rows and receives the solution, xlast is row N-1's solution (every lane);
+// FOLLOW: the records were stored by another warp of the block (ldf)
 template <bool FOLLOW = false>
 __device__ __forceinline__ void back_line_pair(const double* __restrict__ fac, int N, double* __restrict__ fs,
                                                int lane, const double (&xlast)[4])
