@@ -140,8 +140,8 @@ def harness(tmp_path_factory, native_lib):
     return str(exe)
 
 
-@pytest.mark.parametrize("ni,nj,split,extended", [(32, 8, 0.0, False), (32, 12, 0.0, False), (24, 8, 0.5, True),
-                                                   (40, 10, 0.3, True)])
+@pytest.mark.parametrize("ni,nj,split,extended", [(32, 8, 0.0, False), (32, 12, 0.0, False), (128, 32, 0.0, False),
+                                                   (24, 8, 0.5, True), (40, 10, 0.3, True)])
 def test_line_job_queues(harness, make_case, ni, nj, split, extended):
     case = make_case(ni, nj, split=split, seed=4, order=3)
     args = [harness, case] + (["extended"] if extended else [])
