@@ -134,6 +134,15 @@ __device__ __forceinline__ int take_job(int* ctr, int off, int lane)
    return __shfl_sync(kLaneMask, k, 0);
 }
 
+// Whether a warp takes its next job only after job k: after a long first
+// job (warp 0 of block b < nlong, job b).  A job index taken at its start
+// would reserve a queued job that then waits behind the long one, and the
+// launch would end with it.
+__device__ __forceinline__ bool late_next(int k, int k0, int nlong)
+{
+   return k == k0 && (threadIdx.x >> 5) == 0 && (int)blockIdx.x < nlong;
+}
+
 // a warp's first job, or -1 for a warp that stays idle beside an outlier
 __device__ __forceinline__ int first_job(int* ctr, int ncrit, int off, int lane)
 {
@@ -350,9 +359,11 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
    }
    if (k0 < 0) return;
    for (int k = k0; k < nj;) {
-      // the next job's index is fetched while this one runs
+      // the next job's index is fetched while this one runs, except after
+      // a long first job (late_next)
+      const bool late = late_next(k, k0, nlong);
       int kn = 0;
-      if (lane == 0) kn = off + atomicAdd(ctr, 1);
+      if (!late && lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       const int head = d.sched_jobs[job], ich = head & ~kFusedJob;
       if (job == fjob) {
@@ -368,6 +379,7 @@ __global__ void __launch_bounds__(256, 1) adi_factor_kernel(DeviceState d, int n
             solve_job(d, job, ich, lane);
          }
       }
+      if (late && lane == 0) kn = off + atomicAdd(ctr, 1);
       k = __shfl_sync(kLaneMask, kn, 0);
    }
    if (__any_sync(kLaneMask, bad) && lane == 0) atomicOr(d.status, DEV_ERR_PIVOT);
@@ -382,13 +394,16 @@ __global__ void __launch_bounds__(256, 1) adi_solve_kernel(DeviceState d, int sw
    const int lane = threadIdx.x & 31, nj = d.sched_njobs[1 + wave], j0 = d.sched_job0[1 + wave];
    int* ctr = d.sched_ctr + 1 + sweep * d.nWave + wave;
    const int ncrit = d.sched_ncrit[1 + wave], off = ncrit ? (int)gridDim.x : 0;
+   const int nlong = ncrit < 0 ? -ncrit : ncrit;
    const int k0 = first_job(ctr, ncrit, off, lane);
    if (k0 < 0) return;
    for (int k = k0; k < nj;) {
+      const bool late = late_next(k, k0, nlong);
       int kn = 0;
-      if (lane == 0) kn = off + atomicAdd(ctr, 1);
+      if (!late && lane == 0) kn = off + atomicAdd(ctr, 1);
       const int job = d.sched_job_ptr[j0 + k];
       solve_job(d, job, d.sched_jobs[job], lane);
+      if (late && lane == 0) kn = off + atomicAdd(ctr, 1);
       k = __shfl_sync(kLaneMask, kn, 0);
    }
 }
